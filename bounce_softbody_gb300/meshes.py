@@ -1,0 +1,228 @@
+"""Seeded body generators for the workloads this library is measured on.
+
+Every generator returns a :class:`BodyDesc` of plain numpy arrays in the layout the C ABI
+(``include/b3g.h``, ``b3g_body_desc``) takes: vertex arrays, element index arrays and
+per-element material arrays. The same arrays feed the CUDA path and the CPU oracle, so both
+see identical inputs.
+
+The tetrahedral grids split every cell into 6 tetrahedra along its main diagonal (the Kuhn or
+Freudenthal split); the reference's testbed ``GridTetMesh`` uses 5 per cell
+(examples/testbed/framework/uniform_body.h:424-517), and the workloads here ask for 6.
+Cloth grids split each cell into 2 triangles and add structural (distance-1) and bending
+(distance-2) springs, with rest lengths measured on the initial positions like
+``b3SpringForceDef::Initialize`` (src/bounce_softbody/dynamics/forces/spring_force.cpp:25-35).
+"""
+from __future__ import annotations
+
+import dataclasses
+import itertools
+from typing import Optional
+
+import numpy as np
+
+STATIC, KINEMATIC, DYNAMIC = 0, 1, 2  # b3ParticleType (include/bounce_softbody/dynamics/particle.h:31-36)
+
+
+@dataclasses.dataclass
+class BodyDesc:
+    x: np.ndarray                      # (n, 3) float64 positions (also the rest state)
+    v: np.ndarray                      # (n, 3) float64 velocities
+    type: np.ndarray                   # (n,) int32 particle types
+    damping: np.ndarray                # (n,) float64 mass damping
+    tets: np.ndarray                   # (T, 4) uint32
+    tet_E: np.ndarray                  # (T,) Young modulus
+    tet_nu: np.ndarray                 # (T,) Poisson ratio
+    tet_kdamp: np.ndarray              # (T,) stiffness damping
+    tet_density: np.ndarray            # (T,) density of the mass fixture
+    tris: np.ndarray                   # (Tr, 3) uint32
+    tri_Ex: np.ndarray
+    tri_Ey: np.ndarray
+    tri_Es: np.ndarray
+    tri_nuxy: np.ndarray
+    tri_nuyx: np.ndarray
+    tri_kdamp: np.ndarray
+    tri_density: np.ndarray
+    springs: np.ndarray                # (S, 2) uint32
+    spring_L0: np.ndarray
+    spring_ks: np.ndarray
+    spring_kd: np.ndarray
+    sphere_radius: Optional[np.ndarray] = None    # (n,) per-vertex contact radius
+    sphere_friction: Optional[np.ndarray] = None  # (n,)
+    world_spheres: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 5)))
+    gravity: np.ndarray = dataclasses.field(default_factory=lambda: np.array([0.0, -9.8, 0.0]))
+    name: str = "body"
+
+    @property
+    def n(self) -> int:
+        return int(self.x.shape[0])
+
+    @property
+    def tet_rest(self) -> np.ndarray:
+        return self.x[self.tets.astype(np.int64)]
+
+    @property
+    def tri_rest(self) -> np.ndarray:
+        return self.x[self.tris.astype(np.int64)]
+
+
+def _empty_elems(k):
+    return np.zeros((0, k), np.uint32)
+
+
+def _z():
+    return np.zeros(0, np.float64)
+
+
+def kuhn_cells(a: int, b: int, c: int) -> np.ndarray:
+    """Tetrahedra of an a x b x c vertex grid, 6 per cell, vertex id = i + a*(j + b*k).
+
+    Each cell is split along the diagonal from corner (0,0,0) to (1,1,1): one tetrahedron per
+    ordering of the three axes. Orientation is made positive (det > 0) on the regular grid.
+    """
+    i, j, k = np.meshgrid(np.arange(a - 1), np.arange(b - 1), np.arange(c - 1), indexing="ij")
+    i, j, k = i.ravel(), j.ravel(), k.ravel()
+
+    def vid(di, dj, dk):
+        return (i + di) + a * ((j + dj) + b * (k + dk))
+
+    axes = np.eye(3, dtype=np.int64)
+    tets = []
+    for perm in itertools.permutations(range(3)):
+        p0 = np.zeros(3, np.int64)
+        p1 = p0 + axes[perm[0]]
+        p2 = p1 + axes[perm[1]]
+        p3 = p2 + axes[perm[2]]
+        corners = [p0, p1, p2, p3]
+        e = np.stack([corners[1] - p0, corners[2] - p0, corners[3] - p0])
+        if np.linalg.det(e.astype(np.float64)) < 0:
+            corners[1], corners[2] = corners[2], corners[1]
+        tets.append(np.stack([vid(*q) for q in corners], axis=1))
+    # cell-major order: the 6 tetrahedra of a cell are adjacent
+    t = np.stack(tets, axis=1).reshape(-1, 4)
+    return t.astype(np.uint32)
+
+
+def tet_grid(a: int, b: int, c: int, spacing: float = 0.1, jitter: float = 0.01, seed: int = 0,
+             E: float = 1e5, nu: float = 0.3, density: float = 1000.0, damping: float = 0.01,
+             pin: str = "y0", kdamp: float = 0.0, origin=(0.0, 0.0, 0.0),
+             rng: Optional[np.random.Generator] = None, name: str = "") -> BodyDesc:
+    """Kuhn-split tetrahedral block of a x b x c vertices.
+
+    Rest positions are the grid points jittered by seeded uniform noise of +-jitter*spacing
+    per coordinate. ``pin`` selects the static vertices: "y0" (grid layer j = 0), one of
+    "x0", "x1", "y1", "z0", "z1" (a face of the block) or "none".
+    """
+    rng = rng if rng is not None else np.random.default_rng(seed)
+    i, j, k = np.meshgrid(np.arange(a), np.arange(b), np.arange(c), indexing="ij")
+    # vertex id = i + a*(j + b*k): iterate k slowest
+    i = np.transpose(i, (2, 1, 0)).ravel()
+    j = np.transpose(j, (2, 1, 0)).ravel()
+    k = np.transpose(k, (2, 1, 0)).ravel()
+    x = np.stack([i, j, k], axis=1).astype(np.float64) * spacing + np.asarray(origin, np.float64)
+    x += rng.uniform(-jitter * spacing, jitter * spacing, size=x.shape)
+    n = x.shape[0]
+    types = np.full(n, DYNAMIC, np.int32)
+    faces = {"x0": i == 0, "x1": i == a - 1, "y0": j == 0, "y1": j == b - 1, "z0": k == 0, "z1": k == c - 1}
+    if pin != "none":
+        types[faces[pin]] = STATIC
+    tets = kuhn_cells(a, b, c)
+    T = tets.shape[0]
+    return BodyDesc(
+        x=x, v=np.zeros_like(x), type=types, damping=np.full(n, damping),
+        tets=tets, tet_E=np.full(T, E), tet_nu=np.full(T, nu), tet_kdamp=np.full(T, kdamp),
+        tet_density=np.full(T, density),
+        tris=_empty_elems(3), tri_Ex=_z(), tri_Ey=_z(), tri_Es=_z(), tri_nuxy=_z(), tri_nuyx=_z(),
+        tri_kdamp=_z(), tri_density=_z(),
+        springs=_empty_elems(2), spring_L0=_z(), spring_ks=_z(), spring_kd=_z(),
+        name=name or f"tet{a}x{b}x{c}",
+    )
+
+
+def cloth_grid(m: int = 128, side: float = 2.0, height: float = 1.0, E_t: float = 50.0,
+               nu: float = 0.3, areal_density: float = 0.2, ks: float = 1e3, kd: float = 5.0,
+               contact_radius: float = 0.01, friction: float = 0.3, sphere_radius: float = 0.5,
+               sphere_center=(0.0, 0.0, 0.0), pinned_corners: int = 2, damping: float = 0.0,
+               name: str = "") -> BodyDesc:
+    """m x m cloth in the y = height plane centred over a static sphere.
+
+    Triangle elements carry membrane stiffness E*t = ``E_t`` in both directions, shear modulus
+    E*t / (2(1+nu)) and Poisson ratio nu (b3TriangleElementForce has no thickness parameter).
+    Springs: structural (grid neighbours) and bending (distance 2) with stiffness ``ks`` and
+    damping ``kd``. Every vertex carries a contact sphere of ``contact_radius``.
+    """
+    h = side / (m - 1)
+    jj, ii = np.meshgrid(np.arange(m), np.arange(m), indexing="ij")
+    ii, jj = ii.ravel(), jj.ravel()  # vertex id = i + m*j
+    x = np.stack([-0.5 * side + ii * h, np.full(ii.shape, height), -0.5 * side + jj * h], axis=1)
+    n = m * m
+    types = np.full(n, DYNAMIC, np.int32)
+    if pinned_corners >= 1:
+        types[0] = STATIC
+    if pinned_corners >= 2:
+        types[m - 1] = STATIC
+    ci, cj = np.meshgrid(np.arange(m - 1), np.arange(m - 1), indexing="ij")
+    ci, cj = ci.ravel(), cj.ravel()
+    v00 = ci + m * cj
+    v10 = v00 + 1
+    v01 = v00 + m
+    v11 = v01 + 1
+    tris = np.concatenate([np.stack([v00, v01, v10], 1), np.stack([v10, v01, v11], 1)]).astype(np.uint32)
+    Tr = tris.shape[0]
+    springs = []
+    for di, dj in ((1, 0), (0, 1)):
+        for d in (1, 2):
+            mi = (ii + d * di < m) & (jj + d * dj < m)
+            a0 = (ii + m * jj)[mi]
+            springs.append(np.stack([a0, a0 + d * di + m * d * dj], 1))
+    springs = np.concatenate(springs).astype(np.uint32)
+    L0 = np.linalg.norm(x[springs[:, 0]] - x[springs[:, 1]], axis=1)
+    S = springs.shape[0]
+    Es = E_t / (2.0 * (1.0 + nu))
+    return BodyDesc(
+        x=x, v=np.zeros_like(x), type=types, damping=np.full(n, damping),
+        tets=_empty_elems(4), tet_E=_z(), tet_nu=_z(), tet_kdamp=_z(), tet_density=_z(),
+        tris=tris, tri_Ex=np.full(Tr, E_t), tri_Ey=np.full(Tr, E_t), tri_Es=np.full(Tr, Es),
+        tri_nuxy=np.full(Tr, nu), tri_nuyx=np.full(Tr, nu), tri_kdamp=np.zeros(Tr),
+        tri_density=np.full(Tr, areal_density),
+        springs=springs, spring_L0=L0, spring_ks=np.full(S, ks), spring_kd=np.full(S, kd),
+        sphere_radius=np.full(n, contact_radius), sphere_friction=np.full(n, friction),
+        world_spheres=np.array([[*sphere_center, sphere_radius, friction]], np.float64),
+        name=name or f"cloth{m}",
+    )
+
+
+def batch_bodies(count: int = 512, lo: int = 4, hi: int = 40, seed: int = 3, spacing: float = 0.1,
+                 density: float = 1000.0, damping: float = 0.01) -> list[BodyDesc]:
+    """Independent tetrahedral blocks of uneven size.
+
+    Sizes a, b, c ~ U{lo..hi}; Young modulus log-uniform in [1e4, 1e6]; Poisson ratio
+    U[0.2, 0.45]; rest positions jittered by +-1% of the spacing; one random face pinned.
+    """
+    rng = np.random.default_rng(seed)
+    faces = ["x0", "x1", "y0", "y1", "z0", "z1"]
+    out = []
+    for bidx in range(count):
+        a, b, c = (int(s) for s in rng.integers(lo, hi + 1, size=3))
+        E = float(10.0 ** rng.uniform(4.0, 6.0))
+        nu = float(rng.uniform(0.2, 0.45))
+        face = faces[int(rng.integers(0, 6))]
+        out.append(tet_grid(a, b, c, spacing=spacing, jitter=0.01, E=E, nu=nu, density=density,
+                            damping=damping, pin=face, rng=rng, name=f"batch{bidx}_{a}x{b}x{c}"))
+    return out
+
+
+def config_tet10(seed: int = 0) -> BodyDesc:
+    """10x10x10 vertex block, 4374 tets, E=1e5, nu=0.3, rho=1000, damping 0.01, y=0 pinned."""
+    return tet_grid(10, 10, 10, spacing=0.1, jitter=0.01, seed=seed, E=1e5, nu=0.3,
+                    density=1000.0, damping=0.01, pin="y0", name="tet10")
+
+
+def config_tet64(seed: int = 0) -> BodyDesc:
+    """64^3 vertex block (262,144 vertices, 1,500,282 tets), E=1e6, nu=0.45."""
+    return tet_grid(64, 64, 64, spacing=0.1, jitter=0.01, seed=seed, E=1e6, nu=0.45,
+                    density=1000.0, damping=0.01, pin="y0", name="tet64")
+
+
+def config_cloth128() -> BodyDesc:
+    """128^2 cloth (16,384 vertices, 32,258 triangles, 64,768 springs) over a r=0.5 sphere."""
+    return cloth_grid(128, name="cloth128")

@@ -1,0 +1,1150 @@
+/*
+ * ORACLE — test infrastructure only. Never linked into, loaded by or called from the product.
+ *
+ * A plain-C restatement of the reference's implicit body step, compiled for float
+ * (-DB3O_DOUBLE absent: the reference's own `scalar`) and for double (the FP64 oracle).
+ * Parity is pinned: tests compare this restatement with the reference library compiled from
+ * its own sources (oracle/ref_harness.cpp) on the committed golden inputs.
+ *
+ * What it restates, with the reference file:line it follows:
+ *   - b3Body::Step / Solve order                 src/bounce_softbody/dynamics/body.cpp:552-604
+ *   - b3Body::ResetMass (lumped mass)            src/bounce_softbody/dynamics/body.cpp:394-466
+ *   - pack / unpack, M, S, fe += m g             src/bounce_softbody/dynamics/force_solver.cpp:88-180
+ *   - force model order particles/forces/contacts src/bounce_softbody/dynamics/force_solver.cpp:70-86
+ *   - mass damping                               src/bounce_softbody/dynamics/particle.cpp:182-199
+ *   - tetrahedron element (K0, rotation, forces) src/bounce_softbody/dynamics/forces/tetrahedron_element_force.cpp:37-464
+ *   - triangle element                           src/bounce_softbody/dynamics/forces/triangle_element_force.cpp:30-468
+ *   - spring                                     src/bounce_softbody/dynamics/forces/spring_force.cpp:61-143
+ *   - sphere contact force and friction          src/bounce_softbody/dynamics/contacts/sphere_shape_contact.cpp:53-189
+ *   - sphere shape collide                       src/bounce_softbody/collision/shapes/sphere_shape.cpp:50-77
+ *   - contact creation / destruction             src/bounce_softbody/dynamics/contact_manager.cpp:65-146
+ *   - backward Euler with pre-filter             src/bounce_softbody/sparse/sparse_force_solver.cpp:104-232
+ *   - Jacobi PCG, residual refresh every 50      src/bounce_softbody/sparse/sparse_solver.cpp:28-109
+ *   - math (quaternion, basis, perp, adjugate)   include/bounce_softbody/common/math/{quat.h:63-146,mat33.h:276-327,vec3.h:255-270}
+ *
+ * The reference keeps sparse matrices as linked lists; here they are CSR rows of 3x3 blocks
+ * with a fixed pattern. Element order follows the reference's head-inserted force and fixture
+ * lists (newest first). Sums over a row run in column order, so float results differ from the
+ * reference only by summation order.
+ */
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#ifdef B3O_DOUBLE
+typedef double real;
+#define B3O_EPS DBL_EPSILON
+#else
+typedef float real;
+#define B3O_EPS FLT_EPSILON
+#endif
+
+/* settings.h:83-95 */
+#define B3O_CONTACT_STIFFNESS ((real)1000.0)
+#define B3O_MAX_CONTACT_LINEAR_CORRECTION ((real)0.2)
+#define B3O_BAUMGARTE ((real)0.2)
+
+typedef struct { real x, y, z; } v3;
+typedef struct { v3 c[3]; } m33;   /* column-major, like b3Mat33 */
+typedef struct { real x, y; } v2;
+typedef struct { v2 c[2]; } m22;
+typedef struct { v3 v; real s; } quat;
+
+/* ------------------------------------------------------------------ small math */
+static v3 V(real x, real y, real z) { v3 r = {x, y, z}; return r; }
+static v3 add(v3 a, v3 b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
+static v3 sub(v3 a, v3 b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
+static v3 scl(real s, v3 a) { return V(s * a.x, s * a.y, s * a.z); }
+static v3 neg(v3 a) { return V(-a.x, -a.y, -a.z); }
+static real dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static v3 cross(v3 a, v3 b) { return V(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static real len(v3 a) { return (real)sqrt((double)dot(a, a)); }
+static real rsqrt_(real x) { return (real)sqrt((double)x); }
+static v3 normalize(v3 a)
+{
+	real l = rsqrt_(a.x * a.x + a.y * a.y + a.z * a.z);
+	if (l > B3O_EPS) { real s = (real)1 / l; a.x *= s; a.y *= s; a.z *= s; }
+	return a;
+}
+static m33 M3(v3 a, v3 b, v3 c) { m33 m; m.c[0] = a; m.c[1] = b; m.c[2] = c; return m; }
+static m33 mzero(void) { return M3(V(0, 0, 0), V(0, 0, 0), V(0, 0, 0)); }
+static m33 mdiag(real s) { return M3(V(s, 0, 0), V(0, s, 0), V(0, 0, s)); }
+static v3 mv(m33 A, v3 v) { return add(add(scl(v.x, A.c[0]), scl(v.y, A.c[1])), scl(v.z, A.c[2])); }
+static m33 mm(m33 A, m33 B) { return M3(mv(A, B.c[0]), mv(A, B.c[1]), mv(A, B.c[2])); }
+static m33 madd(m33 A, m33 B) { return M3(add(A.c[0], B.c[0]), add(A.c[1], B.c[1]), add(A.c[2], B.c[2])); }
+static m33 msub(m33 A, m33 B) { return M3(sub(A.c[0], B.c[0]), sub(A.c[1], B.c[1]), sub(A.c[2], B.c[2])); }
+static m33 mscl(real s, m33 A) { return M3(scl(s, A.c[0]), scl(s, A.c[1]), scl(s, A.c[2])); }
+static m33 mtr(m33 A)
+{
+	return M3(V(A.c[0].x, A.c[1].x, A.c[2].x), V(A.c[0].y, A.c[1].y, A.c[2].y), V(A.c[0].z, A.c[1].z, A.c[2].z));
+}
+static m33 outer(v3 a, v3 b) { return M3(scl(b.x, a), scl(b.y, a), scl(b.z, a)); }
+static real mget(const m33* A, int r, int c) { const real* p = &A->c[c].x; return p[r]; }
+static void mset(m33* A, int r, int c, real s) { real* p = &A->c[c].x; p[r] = s; }
+/* mat33.h:276 b3Adjugate = transpose(cofactor matrix) */
+static m33 adjugate(m33 A) { return mtr(M3(cross(A.c[1], A.c[2]), cross(A.c[2], A.c[0]), cross(A.c[0], A.c[1]))); }
+static real det3(v3 a, v3 b, v3 c) { return dot(a, cross(b, c)); }
+
+static v2 V2(real x, real y) { v2 r = {x, y}; return r; }
+static v2 add2(v2 a, v2 b) { return V2(a.x + b.x, a.y + b.y); }
+static v2 sub2(v2 a, v2 b) { return V2(a.x - b.x, a.y - b.y); }
+static v2 scl2(real s, v2 a) { return V2(s * a.x, s * a.y); }
+static v2 mv2(m22 A, v2 v) { return add2(scl2(v.x, A.c[0]), scl2(v.y, A.c[1])); }
+static m22 M2(v2 a, v2 b) { m22 m; m.c[0] = a; m.c[1] = b; return m; }
+static m22 mm2(m22 A, m22 B) { return M2(mv2(A, B.c[0]), mv2(A, B.c[1])); }
+static m22 mtr2(m22 A) { return M2(V2(A.c[0].x, A.c[1].x), V2(A.c[0].y, A.c[1].y)); }
+static v2 normalize2(v2 a)
+{
+	real l = rsqrt_(a.x * a.x + a.y * a.y);
+	if (l > B3O_EPS) { a.x /= l; a.y /= l; }
+	return a;
+}
+static real sign_(real x) { return (real)((real)0 < x) - (real)(x < (real)0); }
+
+/* quat.h:133 GetRotationMatrix */
+static m33 qmat(quat q)
+{
+	real x = q.v.x, y = q.v.y, z = q.v.z, w = q.s;
+	real x2 = x + x, y2 = y + y, z2 = z + z;
+	real xx = x * x2, xy = x * y2, xz = x * z2;
+	real yy = y * y2, yz = y * z2, zz = z * z2;
+	real wx = w * x2, wy = w * y2, wz = w * z2;
+	return M3(V((real)1 - (yy + zz), xy + wz, xz - wy),
+	          V(xy - wz, (real)1 - (xx + zz), yz + wx),
+	          V(xz + wy, yz - wx, (real)1 - (xx + yy)));
+}
+/* quat.h:204 b3Mul */
+static quat qmul(quat a, quat b)
+{
+	quat r;
+	r.v = add(add(cross(a.v, b.v), scl(a.s, b.v)), scl(b.s, a.v));
+	r.s = a.s * b.s - dot(a.v, b.v);
+	return r;
+}
+/* quat.h:63 Normalize */
+static quat qnormalize(quat q)
+{
+	real l = rsqrt_(dot(q.v, q.v) + q.s * q.s);
+	if (l > B3O_EPS) { q.v = V(q.v.x / l, q.v.y / l, q.v.z / l); q.s /= l; }
+	return q;
+}
+/* quat.h:83 SetAxisAngle: sin/cos of the half angle (evaluated in double, like ::sin) */
+static quat qaxisangle(v3 axis, real angle)
+{
+	real th = (real)0.5 * angle;
+	quat q;
+	q.v = scl((real)sin((double)th), axis);
+	q.s = (real)cos((double)th);
+	return q;
+}
+/* mat33.h:310 b3ComputeBasis */
+static void compute_basis(v3 a, v3* b, v3* c)
+{
+	const real sqrt_inv3 = rsqrt_((real)1 / (real)3);
+	if (fabs((double)a.x) >= sqrt_inv3) *b = V(a.y, -a.x, 0);
+	else *b = V(0, a.z, -a.y);
+	*b = normalize(*b);
+	*c = cross(a, *b);
+}
+/* vec3.h:255 b3Perp */
+static v3 perp(v3 v)
+{
+	const real sqrt_inv3 = rsqrt_((real)1 / (real)3);
+	v3 u;
+	if (fabs((double)v.x) >= sqrt_inv3) u = V(v.y, -v.x, 0);
+	else u = V(0, v.z, -v.y);
+	return normalize(u);
+}
+
+/* dense column-major products, math.h b3Mul / b3Transpose */
+static void dmul(real* out, const real* A, int m, int n, const real* B, int n2, int p)
+{
+	(void)n2;
+	for (int i = 0; i < m; ++i)
+		for (int j = 0; j < p; ++j)
+		{
+			real s = 0;
+			for (int k = 0; k < n; ++k) s += A[i + m * k] * B[k + n * j];
+			out[i + m * j] = s;
+		}
+}
+static void dtr(real* out, const real* A, int m, int n)
+{
+	for (int i = 0; i < m; ++i)
+		for (int j = 0; j < n; ++j) out[j + n * i] = A[i + m * j];
+}
+
+/* ------------------------------------------------------------------ body */
+typedef struct
+{
+	uint32_t n;
+	const double *x, *v;
+	const int32_t* type;
+	const double* damping;
+	uint32_t tet_count;
+	const uint32_t* tets;
+	const double *tet_rest, *tet_E, *tet_nu, *tet_kdamp, *tet_density;
+	uint32_t tri_count;
+	const uint32_t* tris;
+	const double *tri_rest, *tri_Ex, *tri_Ey, *tri_Es, *tri_nuxy, *tri_nuyx, *tri_kdamp, *tri_density;
+	uint32_t spring_count;
+	const uint32_t* springs;
+	const double *spring_L0, *spring_ks, *spring_kd;
+	const double *sphere_radius, *sphere_friction;
+	uint32_t world_sphere_count;
+	const double* world_spheres;
+	double gravity[3];
+} b3o_desc;
+
+typedef struct
+{
+	uint32_t steps;
+	double dt;
+	uint32_t newton_iters;
+	uint32_t max_sub;
+	double sub_tol;
+	int32_t use_body_step; /* unused here: the restatement always takes sub_tol */
+	double* x_out;
+	double* v_out;
+	uint32_t* sub_iters_out;
+	double* seconds_out;
+} b3o_run;
+
+enum { STATIC = 0, KINEMATIC = 1, DYNAMIC = 2 };
+
+typedef struct
+{
+	uint32_t n;
+	v3 *x, *v, *fext, *trans;
+	int32_t* type;
+	real *mass, *invmass, *damping;
+	v3 gravity;
+
+	uint32_t nt;
+	uint32_t* tet;
+	v3* tet_rest; /* 4 per tet */
+	m33* invE;
+	m33* K;       /* 16 per tet, K[i + 4j] */
+	quat* q;
+	real* tkd;
+
+	uint32_t ntr;
+	uint32_t* tri;
+	v2* tri_x;    /* 3 per tri */
+	m22* invS;
+	m22* K2;      /* 9 per tri, K[i + 3j] */
+	real* trkd;
+
+	uint32_t ns;
+	uint32_t* spr;
+	real *L0, *ks, *kd;
+
+	real *srad, *sfric;
+	uint32_t nw;
+	v3* wc;
+	real *wr, *wf;
+	/* contacts: one slot per (vertex, world fixture), index i*nw + k */
+	uint8_t* c_exists;
+	uint8_t* c_apply;
+	real* c_normalForce;
+	v3* c_normal;
+
+	/* block pattern */
+	uint32_t* rowptr;
+	uint32_t* col;
+	uint32_t nnzb;
+	uint32_t* tet_slot; /* 16 per tet */
+	uint32_t* tri_slot; /* 9 per tri */
+	uint32_t* spr_slot; /* 4 per spring: 11, 12, 21, 22 */
+	uint32_t* diag;
+
+	m33 *dfdx, *dfdv, *A;
+	v3 *x0, *v0, *fe, *y, *xx, *vv, *fi, *b, *pb, *py, *w, *tmp, *r, *d, *qv, *s, *Minv;
+	real* Mval;  /* mass-matrix scalar per row */
+	uint8_t* S;  /* 1 = free, 0 = constrained */
+	uint32_t contacts_found;
+} body_t;
+
+static void* xcalloc(size_t n, size_t s) { return calloc(n ? n : 1, s ? s : 1); }
+static v3 D3(const double* p) { return V((real)p[0], (real)p[1], (real)p[2]); }
+
+static int cmp_u64(const void* a, const void* b)
+{
+	uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+	return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+static uint32_t find_slot(const body_t* B, uint32_t i, uint32_t j)
+{
+	uint32_t lo = B->rowptr[i], hi = B->rowptr[i + 1];
+	while (lo < hi)
+	{
+		uint32_t mid = (lo + hi) >> 1;
+		if (B->col[mid] < j) lo = mid + 1;
+		else hi = mid;
+	}
+	return lo;
+}
+
+/* tetrahedron_element_force.cpp:219-265 ResetElementData */
+static void tet_reset(body_t* B, uint32_t e, real E, real nu)
+{
+	v3 x1 = B->tet_rest[4 * e + 0], x2 = B->tet_rest[4 * e + 1];
+	v3 x3 = B->tet_rest[4 * e + 2], x4 = B->tet_rest[4 * e + 3];
+	v3 e1 = sub(x2, x1), e2 = sub(x3, x1), e3 = sub(x4, x1);
+	m33 Em = M3(e1, e2, e3);
+	real det = det3(e1, e2, e3);
+	real Vol = (real)fabs((double)det) / (real)6;
+	det = (real)1 / det;
+	m33 invE = mscl(det, adjugate(Em));
+	B->invE[e] = invE;
+
+	real lambda = (nu * E) / (((real)1 + nu) * ((real)1 - (real)2 * nu));
+	real mu = E / ((real)2 * ((real)1 + nu));
+	real D[36] = {
+		lambda + 2 * mu, lambda, lambda, 0, 0, 0,
+		lambda, lambda + 2 * mu, lambda, 0, 0, 0,
+		lambda, lambda, lambda + 2 * mu, 0, 0, 0,
+		0, 0, 0, mu, 0, 0,
+		0, 0, 0, 0, mu, 0,
+		0, 0, 0, 0, 0, mu};
+	real n2x = invE.c[0].x, n3x = invE.c[0].y, n4x = invE.c[0].z, n1x = -n2x - n3x - n4x;
+	real n2y = invE.c[1].x, n3y = invE.c[1].y, n4y = invE.c[1].z, n1y = -n2y - n3y - n4y;
+	real n2z = invE.c[2].x, n3z = invE.c[2].y, n4z = invE.c[2].z, n1z = -n2z - n3z - n4z;
+	real Bm[72] = {
+		n1x, 0, 0, n1y, 0, n1z,  0, n1y, 0, n1x, n1z, 0,  0, 0, n1z, 0, n1y, n1x,
+		n2x, 0, 0, n2y, 0, n2z,  0, n2y, 0, n2x, n2z, 0,  0, 0, n2z, 0, n2y, n2x,
+		n3x, 0, 0, n3y, 0, n3z,  0, n3y, 0, n3x, n3z, 0,  0, 0, n3z, 0, n3y, n3x,
+		n4x, 0, 0, n4y, 0, n4z,  0, n4y, 0, n4x, n4z, 0,  0, 0, n4z, 0, n4y, n4x};
+	real BT[72], BTD[72], K[144];
+	dtr(BT, Bm, 6, 12);
+	dmul(BTD, BT, 12, 6, D, 6, 6);
+	dmul(K, BTD, 12, 6, Bm, 6, 12);
+	for (int i = 0; i < 144; ++i) K[i] *= Vol;
+	m33* Kb = B->K + 16 * e;
+	for (int i = 0; i < 12; ++i)
+		for (int j = 0; j < 12; ++j)
+			mset(&Kb[(i / 3) + 4 * (j / 3)], i % 3, j % 3, K[i + 12 * j]);
+}
+
+/* triangle_element_force.cpp:208-279 ResetElementData */
+static void tri_reset(body_t* B, uint32_t e, v3 p1, v3 p2, v3 p3, real Ex, real Ey, real Es, real nxy, real nyx)
+{
+	v3 n = normalize(cross(sub(p2, p1), sub(p3, p1)));
+	v3 px, py;
+	compute_basis(n, &px, &py);
+	v2 x1 = V2(px.x * p1.x + px.y * p1.y + px.z * p1.z, py.x * p1.x + py.y * p1.y + py.z * p1.z);
+	v2 x2 = V2(px.x * p2.x + px.y * p2.y + px.z * p2.z, py.x * p2.x + py.y * p2.y + py.z * p2.z);
+	v2 x3 = V2(px.x * p3.x + px.y * p3.y + px.z * p3.z, py.x * p3.x + py.y * p3.y + py.z * p3.z);
+	B->tri_x[3 * e + 0] = x1;
+	B->tri_x[3 * e + 1] = x2;
+	B->tri_x[3 * e + 2] = x3;
+	v2 e1 = sub2(x2, x1), e2 = sub2(x3, x1);
+	real det = e1.x * e2.y - e1.y * e2.x;
+	real A = (real)0.5 * (real)fabs((double)det);
+	det = (real)1 / det;
+	/* mat22.h:194 adjugate, scaled */
+	m22 invS = M2(V2(det * e2.y, det * -e1.y), V2(det * -e2.x, det * e1.x));
+	B->invS[e] = invS;
+	real s = (real)1 - nxy * nyx;
+	real C[9] = {Ex / s, Ey * nxy / s, 0, Ex * nyx / s, Ey / s, 0, 0, 0, Es};
+	real n2x = invS.c[0].x, n3x = invS.c[0].y, n1x = -n2x - n3x;
+	real n2y = invS.c[1].x, n3y = invS.c[1].y, n1y = -n2y - n3y;
+	real Bm[18] = {n1x, 0, n1y, 0, n1y, n1x, n2x, 0, n2y, 0, n2y, n2x, n3x, 0, n3y, 0, n3y, n3x};
+	real BT[18], BTC[18], K[36];
+	dtr(BT, Bm, 3, 6);
+	dmul(BTC, BT, 6, 3, C, 3, 3);
+	dmul(K, BTC, 6, 3, Bm, 3, 6);
+	for (int i = 0; i < 36; ++i) K[i] *= A;
+	m22* Kb = B->K2 + 9 * e;
+	for (int i = 0; i < 6; ++i)
+		for (int j = 0; j < 6; ++j)
+		{
+			real* p = &Kb[(i / 2) + 3 * (j / 2)].c[j % 2].x;
+			p[i % 2] = K[i + 6 * j];
+		}
+}
+
+static void body_free(body_t* B);
+
+static body_t* body_create(const b3o_desc* d)
+{
+	body_t* B = (body_t*)xcalloc(1, sizeof(body_t));
+	uint32_t n = d->n;
+	B->n = n;
+	B->x = xcalloc(n, sizeof(v3));
+	B->v = xcalloc(n, sizeof(v3));
+	B->fext = xcalloc(n, sizeof(v3));
+	B->trans = xcalloc(n, sizeof(v3));
+	B->type = xcalloc(n, sizeof(int32_t));
+	B->mass = xcalloc(n, sizeof(real));
+	B->invmass = xcalloc(n, sizeof(real));
+	B->damping = xcalloc(n, sizeof(real));
+	B->gravity = D3(d->gravity);
+	for (uint32_t i = 0; i < n; ++i)
+	{
+		B->x[i] = D3(d->x + 3 * i);
+		B->v[i] = D3(d->v + 3 * i);
+		B->type[i] = d->type[i];
+		B->damping[i] = d->damping ? (real)d->damping[i] : 0;
+		/* particle.cpp:40-49 constructor: dynamic particles start with unit mass */
+		B->mass[i] = B->type[i] == DYNAMIC ? 1 : 0;
+		B->invmass[i] = B->mass[i];
+	}
+
+	B->nt = d->tet_count;
+	B->tet = xcalloc(4 * (size_t)B->nt, sizeof(uint32_t));
+	B->tet_rest = xcalloc(4 * (size_t)B->nt, sizeof(v3));
+	B->invE = xcalloc(B->nt, sizeof(m33));
+	B->K = xcalloc(16 * (size_t)B->nt, sizeof(m33));
+	B->q = xcalloc(B->nt, sizeof(quat));
+	B->tkd = xcalloc(B->nt, sizeof(real));
+	real* tvol = xcalloc(B->nt, sizeof(real));
+	for (uint32_t e = 0; e < B->nt; ++e)
+	{
+		for (int k = 0; k < 4; ++k)
+		{
+			B->tet[4 * e + k] = d->tets[4 * e + k];
+			B->tet_rest[4 * e + k] = d->tet_rest ? D3(d->tet_rest + 12 * e + 3 * k) : D3(d->x + 3 * d->tets[4 * e + k]);
+		}
+		B->q[e].v = V(0, 0, 0);
+		B->q[e].s = 1;
+		B->tkd[e] = d->tet_kdamp ? (real)d->tet_kdamp[e] : 0;
+		tet_reset(B, e, (real)d->tet_E[e], (real)d->tet_nu[e]);
+		/* tetrahedron_fixture.cpp:34-45 volume = sign(det) det / 6 */
+		v3 a = B->tet_rest[4 * e], bb = B->tet_rest[4 * e + 1], c = B->tet_rest[4 * e + 2], dd = B->tet_rest[4 * e + 3];
+		real det = det3(sub(bb, a), sub(c, a), sub(dd, a));
+		tvol[e] = ((real)1 / (real)6) * sign_(det) * det;
+	}
+
+	B->ntr = d->tri_count;
+	B->tri = xcalloc(3 * (size_t)B->ntr, sizeof(uint32_t));
+	B->tri_x = xcalloc(3 * (size_t)B->ntr, sizeof(v2));
+	B->invS = xcalloc(B->ntr, sizeof(m22));
+	B->K2 = xcalloc(9 * (size_t)B->ntr, sizeof(m22));
+	B->trkd = xcalloc(B->ntr, sizeof(real));
+	real* tarea = xcalloc(B->ntr, sizeof(real));
+	for (uint32_t e = 0; e < B->ntr; ++e)
+	{
+		v3 p[3];
+		for (int k = 0; k < 3; ++k)
+		{
+			B->tri[3 * e + k] = d->tris[3 * e + k];
+			p[k] = d->tri_rest ? D3(d->tri_rest + 9 * e + 3 * k) : D3(d->x + 3 * d->tris[3 * e + k]);
+		}
+		B->trkd[e] = d->tri_kdamp ? (real)d->tri_kdamp[e] : 0;
+		tri_reset(B, e, p[0], p[1], p[2], (real)d->tri_Ex[e], (real)d->tri_Ey[e], (real)d->tri_Es[e],
+		          (real)d->tri_nuxy[e], (real)d->tri_nuyx[e]);
+		/* triangle_fixture.cpp:33-36 area = |cross| / 2 */
+		tarea[e] = (real)0.5 * len(cross(sub(p[1], p[0]), sub(p[2], p[0])));
+	}
+
+	B->ns = d->spring_count;
+	B->spr = xcalloc(2 * (size_t)B->ns, sizeof(uint32_t));
+	B->L0 = xcalloc(B->ns, sizeof(real));
+	B->ks = xcalloc(B->ns, sizeof(real));
+	B->kd = xcalloc(B->ns, sizeof(real));
+	for (uint32_t e = 0; e < B->ns; ++e)
+	{
+		B->spr[2 * e] = d->springs[2 * e];
+		B->spr[2 * e + 1] = d->springs[2 * e + 1];
+		B->L0[e] = (real)d->spring_L0[e];
+		B->ks[e] = (real)d->spring_ks[e];
+		B->kd[e] = (real)d->spring_kd[e];
+	}
+
+	/* body.cpp:394-466 ResetMass, fixture lists walked newest first */
+	for (uint32_t e = 0; e < B->ntr; ++e)
+		for (int k = 0; k < 3; ++k) B->mass[B->tri[3 * e + k]] = 0;
+	for (uint32_t e = 0; e < B->nt; ++e)
+		for (int k = 0; k < 4; ++k) B->mass[B->tet[4 * e + k]] = 0;
+	const real inv3 = (real)1 / (real)3, inv4 = (real)1 / (real)4;
+	for (uint32_t e = B->ntr; e-- > 0;)
+	{
+		real m = (real)d->tri_density[e] * tarea[e];
+		for (int k = 0; k < 3; ++k) B->mass[B->tri[3 * e + k]] += inv3 * m;
+	}
+	for (uint32_t e = B->nt; e-- > 0;)
+	{
+		real m = (real)d->tet_density[e] * tvol[e];
+		for (int k = 0; k < 4; ++k) B->mass[B->tet[4 * e + k]] += inv4 * m;
+	}
+	for (uint32_t i = 0; i < n; ++i)
+	{
+		if (B->type[i] != DYNAMIC) { B->mass[i] = 0; B->invmass[i] = 0; continue; }
+		if (B->mass[i] > 0) B->invmass[i] = (real)1 / B->mass[i];
+		else { B->mass[i] = 1; B->invmass[i] = 1; }
+	}
+	free(tvol);
+	free(tarea);
+
+	if (d->sphere_radius)
+	{
+		B->srad = xcalloc(n, sizeof(real));
+		B->sfric = xcalloc(n, sizeof(real));
+		for (uint32_t i = 0; i < n; ++i)
+		{
+			B->srad[i] = (real)d->sphere_radius[i];
+			B->sfric[i] = (real)d->sphere_friction[i];
+		}
+	}
+	B->nw = d->world_sphere_count;
+	B->wc = xcalloc(B->nw, sizeof(v3));
+	B->wr = xcalloc(B->nw, sizeof(real));
+	B->wf = xcalloc(B->nw, sizeof(real));
+	for (uint32_t k = 0; k < B->nw; ++k)
+	{
+		B->wc[k] = D3(d->world_spheres + 5 * k);
+		B->wr[k] = (real)d->world_spheres[5 * k + 3];
+		B->wf[k] = (real)d->world_spheres[5 * k + 4];
+	}
+	size_t nc = (size_t)n * (B->nw ? B->nw : 1);
+	B->c_exists = xcalloc(nc, 1);
+	B->c_apply = xcalloc(nc, 1);
+	B->c_normalForce = xcalloc(nc, sizeof(real));
+	B->c_normal = xcalloc(nc, sizeof(v3));
+
+	/* block pattern: diagonal + every element pair */
+	size_t npairs = (size_t)n + 16 * (size_t)B->nt + 9 * (size_t)B->ntr + 4 * (size_t)B->ns;
+	uint64_t* keys = xcalloc(npairs, sizeof(uint64_t));
+	size_t kk = 0;
+	for (uint32_t i = 0; i < n; ++i) keys[kk++] = ((uint64_t)i << 32) | i;
+	for (uint32_t e = 0; e < B->nt; ++e)
+		for (int a = 0; a < 4; ++a)
+			for (int b = 0; b < 4; ++b) keys[kk++] = ((uint64_t)B->tet[4 * e + a] << 32) | B->tet[4 * e + b];
+	for (uint32_t e = 0; e < B->ntr; ++e)
+		for (int a = 0; a < 3; ++a)
+			for (int b = 0; b < 3; ++b) keys[kk++] = ((uint64_t)B->tri[3 * e + a] << 32) | B->tri[3 * e + b];
+	for (uint32_t e = 0; e < B->ns; ++e)
+		for (int a = 0; a < 2; ++a)
+			for (int b = 0; b < 2; ++b) keys[kk++] = ((uint64_t)B->spr[2 * e + a] << 32) | B->spr[2 * e + b];
+	qsort(keys, kk, sizeof(uint64_t), cmp_u64);
+	size_t u = 0;
+	for (size_t k = 0; k < kk; ++k)
+		if (k == 0 || keys[k] != keys[u - 1]) keys[u++] = keys[k];
+	B->nnzb = (uint32_t)u;
+	B->rowptr = xcalloc(n + 1, sizeof(uint32_t));
+	B->col = xcalloc(u, sizeof(uint32_t));
+	for (size_t k = 0; k < u; ++k)
+	{
+		B->rowptr[(keys[k] >> 32) + 1]++;
+		B->col[k] = (uint32_t)(keys[k] & 0xffffffffu);
+	}
+	for (uint32_t i = 0; i < n; ++i) B->rowptr[i + 1] += B->rowptr[i];
+	free(keys);
+	B->diag = xcalloc(n, sizeof(uint32_t));
+	for (uint32_t i = 0; i < n; ++i) B->diag[i] = find_slot(B, i, i);
+	B->tet_slot = xcalloc(16 * (size_t)B->nt, sizeof(uint32_t));
+	for (uint32_t e = 0; e < B->nt; ++e)
+		for (int a = 0; a < 4; ++a)
+			for (int b = 0; b < 4; ++b)
+				B->tet_slot[16 * e + a + 4 * b] = find_slot(B, B->tet[4 * e + a], B->tet[4 * e + b]);
+	B->tri_slot = xcalloc(9 * (size_t)B->ntr, sizeof(uint32_t));
+	for (uint32_t e = 0; e < B->ntr; ++e)
+		for (int a = 0; a < 3; ++a)
+			for (int b = 0; b < 3; ++b)
+				B->tri_slot[9 * e + a + 3 * b] = find_slot(B, B->tri[3 * e + a], B->tri[3 * e + b]);
+	B->spr_slot = xcalloc(4 * (size_t)B->ns, sizeof(uint32_t));
+	for (uint32_t e = 0; e < B->ns; ++e)
+	{
+		uint32_t i1 = B->spr[2 * e], i2 = B->spr[2 * e + 1];
+		B->spr_slot[4 * e + 0] = find_slot(B, i1, i1);
+		B->spr_slot[4 * e + 1] = find_slot(B, i1, i2);
+		B->spr_slot[4 * e + 2] = find_slot(B, i2, i1);
+		B->spr_slot[4 * e + 3] = find_slot(B, i2, i2);
+	}
+
+	B->dfdx = xcalloc(B->nnzb, sizeof(m33));
+	B->dfdv = xcalloc(B->nnzb, sizeof(m33));
+	B->A = xcalloc(B->nnzb, sizeof(m33));
+	v3** vecs[] = {&B->x0, &B->v0, &B->fe, &B->y, &B->xx, &B->vv, &B->fi, &B->b, &B->pb, &B->py,
+	               &B->w, &B->tmp, &B->r, &B->d, &B->qv, &B->s, &B->Minv};
+	for (size_t k = 0; k < sizeof(vecs) / sizeof(vecs[0]); ++k) *vecs[k] = xcalloc(n, sizeof(v3));
+	B->Mval = xcalloc(n, sizeof(real));
+	B->S = xcalloc(n, 1);
+	return B;
+}
+
+static void body_free(body_t* B)
+{
+	if (!B) return;
+	void* ptrs[] = {B->x, B->v, B->fext, B->trans, B->type, B->mass, B->invmass, B->damping, B->tet,
+	                B->tet_rest, B->invE, B->K, B->q, B->tkd, B->tri, B->tri_x, B->invS, B->K2, B->trkd,
+	                B->spr, B->L0, B->ks, B->kd, B->srad, B->sfric, B->wc, B->wr, B->wf, B->c_exists,
+	                B->c_apply, B->c_normalForce, B->c_normal, B->rowptr, B->col, B->tet_slot, B->tri_slot,
+	                B->spr_slot, B->diag, B->dfdx, B->dfdv, B->A, B->x0, B->v0, B->fe, B->y, B->xx, B->vv,
+	                B->fi, B->b, B->pb, B->py, B->w, B->tmp, B->r, B->d, B->qv, B->s, B->Minv, B->Mval, B->S};
+	for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); ++k) free(ptrs[k]);
+	free(B);
+}
+
+/* ------------------------------------------------------------------ force model */
+/* tetrahedron_element_force.cpp:273-311 b3ExtractRotation */
+static quat extract_rotation(m33 A, quat q0)
+{
+	quat q = q0;
+	for (uint32_t it = 0; it < 32; ++it)
+	{
+		m33 R = qmat(q);
+		real den = (real)fabs((double)(dot(R.c[0], A.c[0]) + dot(R.c[1], A.c[1]) + dot(R.c[2], A.c[2])));
+		if (den == 0) break;
+		v3 torque = add(add(cross(R.c[0], A.c[0]), cross(R.c[1], A.c[1])), cross(R.c[2], A.c[2]));
+		const real kTol = (real)1.0e-9;
+		real inv_den = (real)1 / den + kTol;
+		v3 omega = scl(inv_den, torque);
+		real w = len(omega);
+		if (w < kTol) break;
+		quat qw = qaxisangle(V(omega.x / w, omega.y / w, omega.z / w), w);
+		q = qnormalize(qmul(qw, q));
+	}
+	return q;
+}
+
+/* tetrahedron_element_force.cpp:313-464 */
+static void tet_apply(body_t* B, uint32_t e)
+{
+	const uint32_t* is = B->tet + 4 * e;
+	v3 p[4], vel[4];
+	for (int k = 0; k < 4; ++k) { p[k] = B->xx[is[k]]; vel[k] = B->vv[is[k]]; }
+	m33 Em = M3(sub(p[1], p[0]), sub(p[2], p[0]), sub(p[3], p[0]));
+	m33 F = mm(Em, B->invE[e]);
+	quat q = extract_rotation(F, B->q[e]);
+	B->q[e] = q;
+	m33 R = qmat(q), RT = mtr(R);
+	const m33* K0 = B->K + 16 * e;
+	m33 K[16];
+	for (int i = 0; i < 4; ++i)
+		for (int j = 0; j < 4; ++j) K[i + 4 * j] = mm(mm(R, K0[i + 4 * j]), RT);
+	for (int i = 0; i < 4; ++i)
+		for (int j = 0; j < 4; ++j)
+		{
+			uint32_t s = B->tet_slot[16 * e + i + 4 * j];
+			B->dfdx[s] = msub(B->dfdx[s], K[i + 4 * j]);
+		}
+	v3 us[4], fs[4];
+	for (int k = 0; k < 4; ++k) us[k] = sub(mv(RT, p[k]), B->tet_rest[4 * e + k]);
+	for (int i = 0; i < 4; ++i)
+	{
+		fs[i] = V(0, 0, 0);
+		for (int j = 0; j < 4; ++j) fs[i] = add(fs[i], mv(K0[i + 4 * j], us[j]));
+	}
+	for (int i = 0; i < 4; ++i) B->fi[is[i]] = sub(B->fi[is[i]], mv(R, fs[i]));
+	real kd = B->tkd[e];
+	if (kd > 0)
+	{
+		v3 fds[4];
+		for (int i = 0; i < 4; ++i)
+		{
+			fds[i] = V(0, 0, 0);
+			for (int j = 0; j < 4; ++j) fds[i] = add(fds[i], mv(mscl(kd, K[i + 4 * j]), vel[j]));
+		}
+		for (int i = 0; i < 4; ++i) B->fi[is[i]] = sub(B->fi[is[i]], fds[i]);
+		for (int i = 0; i < 4; ++i)
+			for (int j = 0; j < 4; ++j)
+			{
+				uint32_t s = B->tet_slot[16 * e + i + 4 * j];
+				B->dfdv[s] = msub(B->dfdv[s], mscl(kd, K[i + 4 * j]));
+			}
+	}
+}
+
+/* triangle_element_force.cpp:131-150 polar decomposition (Shoemake-Duff) */
+static m22 polar2(m22 M)
+{
+	real m11 = M.c[0].x, m12 = M.c[1].x, m21 = M.c[0].y, m22v = M.c[1].y;
+	real det = m11 * m22v - m12 * m21;
+	m22 A = M2(V2(M.c[1].y, -M.c[1].x), V2(-M.c[0].y, M.c[0].x));
+	real sg = sign_(det);
+	m22 Q = M2(add2(M.c[0], scl2(sg, A.c[0])), add2(M.c[1], scl2(sg, A.c[1])));
+	Q.c[0] = normalize2(Q.c[0]);
+	Q.c[1] = normalize2(Q.c[1]);
+	return Q;
+}
+
+/* triangle_element_force.cpp:285-468 */
+static void tri_apply(body_t* B, uint32_t e)
+{
+	const uint32_t* is = B->tri + 3 * e;
+	v3 p1 = B->xx[is[0]], p2 = B->xx[is[1]], p3 = B->xx[is[2]];
+	v3 vel[3] = {B->vv[is[0]], B->vv[is[1]], B->vv[is[2]]};
+	v3 n = normalize(cross(sub(p2, p1), sub(p3, p1)));
+	v3 px, py;
+	compute_basis(n, &px, &py);
+	real P[6] = {px.x, py.x, px.y, py.y, px.z, py.z};   /* 2x3 */
+	real PT[6] = {px.x, px.y, px.z, py.x, py.y, py.z};  /* 3x2 */
+	v2 x1, x2, x3;
+	dmul(&x1.x, P, 2, 3, &p1.x, 3, 1);
+	dmul(&x2.x, P, 2, 3, &p2.x, 3, 1);
+	dmul(&x3.x, P, 2, 3, &p3.x, 3, 1);
+	m22 T = M2(sub2(x2, x1), sub2(x3, x1));
+	m22 F = mm2(T, B->invS[e]);
+	m22 R = polar2(F), RT = mtr2(R);
+	v2 us[3];
+	us[0] = sub2(mv2(RT, x1), B->tri_x[3 * e + 0]);
+	us[1] = sub2(mv2(RT, x2), B->tri_x[3 * e + 1]);
+	us[2] = sub2(mv2(RT, x3), B->tri_x[3 * e + 2]);
+	const m22* K0 = B->K2 + 9 * e;
+	v2 fs[3];
+	for (int i = 0; i < 3; ++i)
+	{
+		fs[i] = V2(0, 0);
+		for (int j = 0; j < 3; ++j) fs[i] = add2(fs[i], mv2(K0[i + 3 * j], us[j]));
+	}
+	for (int i = 0; i < 3; ++i) fs[i] = mv2(R, fs[i]);
+	for (int i = 0; i < 3; ++i)
+	{
+		v3 f;
+		dmul(&f.x, PT, 3, 2, &fs[i].x, 2, 1);
+		B->fi[is[i]] = sub(B->fi[is[i]], f);
+	}
+	m33 K[9];
+	for (int i = 0; i < 3; ++i)
+		for (int j = 0; j < 3; ++j)
+		{
+			m22 k = mm2(mm2(R, K0[i + 3 * j]), RT);
+			real PTk[6];
+			dmul(PTk, PT, 3, 2, &k.c[0].x, 2, 2);
+			m33 Ke;
+			dmul(&Ke.c[0].x, PTk, 3, 2, P, 2, 3);
+			K[i + 3 * j] = Ke;
+		}
+	for (int i = 0; i < 3; ++i)
+		for (int j = 0; j < 3; ++j)
+		{
+			uint32_t s = B->tri_slot[9 * e + i + 3 * j];
+			B->dfdx[s] = msub(B->dfdx[s], K[i + 3 * j]);
+		}
+	real kd = B->trkd[e];
+	if (kd > 0)
+	{
+		v3 fds[3];
+		for (int i = 0; i < 3; ++i)
+		{
+			fds[i] = V(0, 0, 0);
+			for (int j = 0; j < 3; ++j) fds[i] = add(fds[i], mv(mscl(kd, K[i + 3 * j]), vel[j]));
+		}
+		for (int i = 0; i < 3; ++i) B->fi[is[i]] = sub(B->fi[is[i]], fds[i]);
+		for (int i = 0; i < 3; ++i)
+			for (int j = 0; j < 3; ++j)
+			{
+				uint32_t s = B->tri_slot[9 * e + i + 3 * j];
+				B->dfdv[s] = msub(B->dfdv[s], mscl(kd, K[i + 3 * j]));
+			}
+	}
+}
+
+/* spring_force.cpp:61-143 (the stiffness Jacobian uses the unnormalised dx, as there) */
+static void spring_apply(body_t* B, uint32_t e)
+{
+	uint32_t i1 = B->spr[2 * e], i2 = B->spr[2 * e + 1];
+	v3 x1 = B->xx[i1], v1 = B->vv[i1], x2 = B->xx[i2], v2v = B->vv[i2];
+	m33 I = mdiag(1);
+	v3 dx = sub(x1, x2);
+	real L = len(dx);
+	if (!(L > 0)) return;
+	v3 n = V(dx.x / L, dx.y / L, dx.z / L);
+	real ks = B->ks[e], kd = B->kd[e], L0 = B->L0[e];
+	const uint32_t* sl = B->spr_slot + 4 * e;
+	if (ks > 0 && L > L0)
+	{
+		real Cc = L - L0;
+		v3 f1 = scl(-ks * Cc, n);
+		B->fi[i1] = add(B->fi[i1], f1);
+		B->fi[i2] = add(B->fi[i2], neg(f1));
+		m33 K11 = mscl(-ks, madd(outer(dx, dx), mscl((real)1 - L0 / L, msub(I, outer(dx, dx)))));
+		m33 K12 = mscl(-1, K11);
+		B->dfdx[sl[0]] = madd(B->dfdx[sl[0]], K11);
+		B->dfdx[sl[1]] = madd(B->dfdx[sl[1]], K12);
+		B->dfdx[sl[2]] = madd(B->dfdx[sl[2]], K12);
+		B->dfdx[sl[3]] = madd(B->dfdx[sl[3]], K11);
+	}
+	if (kd > 0)
+	{
+		real dCdt = dot(n, sub(v1, v2v));
+		v3 f1 = scl(-kd * dCdt, n);
+		B->fi[i1] = add(B->fi[i1], f1);
+		B->fi[i2] = add(B->fi[i2], neg(f1));
+		m33 K11 = mscl(-kd, outer(n, n));
+		m33 K12 = mscl(-1, K11);
+		B->dfdv[sl[0]] = madd(B->dfdv[sl[0]], K11);
+		B->dfdv[sl[1]] = madd(B->dfdv[sl[1]], K12);
+		B->dfdv[sl[2]] = madd(B->dfdv[sl[2]], K12);
+		B->dfdv[sl[3]] = madd(B->dfdv[sl[3]], K11);
+	}
+}
+
+/* sphere_shape.cpp:50-77 */
+static int sphere_collide(v3 center, real rshape, v3 vertex, real rsphere, v3* point, v3* normal)
+{
+	real radius = rshape + rsphere;
+	real rr = radius * radius;
+	v3 dd = sub(vertex, center);
+	real d2 = dot(dd, dd);
+	if (d2 <= rr)
+	{
+		*point = center;
+		if (d2 > B3O_EPS * B3O_EPS)
+		{
+			real dist = rsqrt_(d2);
+			*normal = V(dd.x / dist, dd.y / dist, dd.z / dist);
+		}
+		else *normal = V(0, 1, 0);
+		return 1;
+	}
+	return 0;
+}
+
+/* sphere_shape_contact.cpp:53-143 (contact damping stiffness is 0 in settings.h) */
+static void contact_apply(body_t* B, uint32_t i, uint32_t k)
+{
+	size_t c = (size_t)i * B->nw + k;
+	v3 x1 = B->xx[i];
+	real r1 = B->srad[i], r2 = B->wr[k];
+	v3 x2, n2;
+	if (!sphere_collide(B->wc[k], r2, x1, r1, &x2, &n2)) return;
+	if (!B->c_apply[c]) { B->c_normal[c] = n2; B->c_apply[c] = 1; }
+	v3 n1 = neg(n2);
+	v3 c1 = add(x1, scl(r1, n1));
+	v3 c2 = add(x2, scl(r2, n2));
+	real C = len(sub(c2, c1));
+	C = B3O_BAUMGARTE * C < B3O_MAX_CONTACT_LINEAR_CORRECTION ? B3O_BAUMGARTE * C : B3O_MAX_CONTACT_LINEAR_CORRECTION;
+	v3 f1 = scl(-B3O_CONTACT_STIFFNESS * C, n1);
+	m33 I = mdiag(1);
+	m33 K11 = mscl(-B3O_CONTACT_STIFFNESS, madd(outer(n1, n1), mscl(C, msub(I, outer(n1, n1)))));
+	B->fi[i] = add(B->fi[i], f1);
+	uint32_t s = B->diag[i];
+	B->dfdx[s] = madd(B->dfdx[s], K11);
+	B->c_normalForce[c] += len(f1);
+}
+
+static void apply_forces(body_t* B)
+{
+	uint32_t n = B->n;
+	for (uint32_t i = 0; i < n; ++i) B->fi[i] = V(0, 0, 0);
+	memset(B->dfdx, 0, sizeof(m33) * B->nnzb);
+	memset(B->dfdv, 0, sizeof(m33) * B->nnzb);
+	/* particle.cpp:182-199 mass damping */
+	for (uint32_t i = 0; i < n; ++i)
+	{
+		real c = B->damping[i];
+		if (c > 0)
+		{
+			v3 fd = scl(-c * B->mass[i], B->vv[i]);
+			B->fi[i] = add(B->fi[i], fd);
+			uint32_t s = B->diag[i];
+			B->dfdv[s] = madd(B->dfdv[s], mdiag(-c * B->mass[i]));
+		}
+	}
+	/* forces, newest first: springs, then triangles, then tetrahedra (creation order) */
+	for (uint32_t e = B->ns; e-- > 0;) spring_apply(B, e);
+	for (uint32_t e = B->ntr; e-- > 0;) tri_apply(B, e);
+	for (uint32_t e = B->nt; e-- > 0;) tet_apply(B, e);
+	if (B->srad)
+		for (uint32_t i = 0; i < n; ++i)
+			for (uint32_t k = 0; k < B->nw; ++k)
+				if (B->c_exists[(size_t)i * B->nw + k]) contact_apply(B, i, k);
+}
+
+/* ------------------------------------------------------------------ sparse helpers */
+static void spmv(const body_t* B, const m33* M, const v3* x, v3* out)
+{
+	for (uint32_t i = 0; i < B->n; ++i)
+	{
+		v3 acc = V(0, 0, 0);
+		for (uint32_t k = B->rowptr[i]; k < B->rowptr[i + 1]; ++k) acc = add(acc, mv(M[k], x[B->col[k]]));
+		out[i] = acc;
+	}
+}
+static real vdot(const v3* a, const v3* b, uint32_t n)
+{
+	real r = 0;
+	for (uint32_t i = 0; i < n; ++i) r += dot(a[i], b[i]);
+	return r;
+}
+
+/* sparse_solver.cpp:28-109 */
+static uint32_t pcg(body_t* B, const m33* A, const v3* b, v3* x, uint32_t maxIt, real eps)
+{
+	uint32_t n = B->n;
+	v3 *r = B->r, *d = B->d, *q = B->qv, *s = B->s, *Minv = B->Minv;
+	for (uint32_t i = 0; i < n; ++i)
+	{
+		m33 a = A[B->diag[i]];
+		Minv[i] = V((real)1 / a.c[0].x, (real)1 / a.c[1].y, (real)1 / a.c[2].z);
+	}
+	spmv(B, A, x, q);
+	for (uint32_t i = 0; i < n; ++i) r[i] = sub(b[i], q[i]);
+	for (uint32_t i = 0; i < n; ++i) d[i] = V(Minv[i].x * r[i].x, Minv[i].y * r[i].y, Minv[i].z * r[i].z);
+	real delta_new = vdot(r, d, n);
+	real delta_0 = delta_new;
+	uint32_t it = 0;
+	for (;;)
+	{
+		if (it == maxIt) break;
+		if (delta_new <= eps * eps * delta_0) break;
+		spmv(B, A, d, q);
+		real alpha = delta_new / vdot(d, q, n);
+		for (uint32_t i = 0; i < n; ++i) x[i] = add(x[i], scl(alpha, d[i]));
+		if (it % 50 == 0)
+		{
+			spmv(B, A, x, q);
+			for (uint32_t i = 0; i < n; ++i) r[i] = sub(b[i], q[i]);
+		}
+		else
+			for (uint32_t i = 0; i < n; ++i) r[i] = sub(r[i], scl(alpha, q[i]));
+		for (uint32_t i = 0; i < n; ++i) s[i] = V(Minv[i].x * r[i].x, Minv[i].y * r[i].y, Minv[i].z * r[i].z);
+		real delta_old = delta_new;
+		delta_new = vdot(r, s, n);
+		real beta = delta_new / delta_old;
+		for (uint32_t i = 0; i < n; ++i) d[i] = add(s[i], scl(beta, d[i]));
+		++it;
+	}
+	return it;
+}
+
+/* sparse_force_solver.cpp:104-232 (z = 0) */
+static uint32_t solve_be(body_t* B, real h, uint32_t maxIt, uint32_t maxSub, real subEps)
+{
+	uint32_t n = B->n;
+	real eps = B3O_EPS;
+	for (uint32_t i = 0; i < n; ++i)
+	{
+		B->py[i] = V(0, 0, 0);
+		B->xx[i] = B->x0[i];
+		B->vv[i] = B->v0[i];
+	}
+	real error0 = 0, error = 0;
+	uint32_t maxSubIt = 0;
+	for (uint32_t iteration = 0; iteration < maxIt;)
+	{
+		apply_forces(B);
+		/* A = M - h dfdv - h^2 dfdx */
+		for (uint32_t i = 0; i < n; ++i)
+			for (uint32_t k = B->rowptr[i]; k < B->rowptr[i + 1]; ++k)
+			{
+				m33 a = mscl(-h, B->dfdv[k]);
+				if (k == B->diag[i]) a = madd(mdiag(B->Mval[i]), a);
+				B->A[k] = msub(a, mscl(h * h, B->dfdx[k]));
+			}
+		/* b = M (v0 - v) + h (fe + fi) + (h dfdx)(x0 - x + h v + y) */
+		for (uint32_t i = 0; i < n; ++i)
+			B->w[i] = add(add(sub(B->x0[i], B->xx[i]), scl(h, B->vv[i])), B->y[i]);
+		for (uint32_t i = 0; i < n; ++i)
+		{
+			v3 acc = V(0, 0, 0);
+			for (uint32_t k = B->rowptr[i]; k < B->rowptr[i + 1]; ++k)
+				acc = add(acc, mv(mscl(h, B->dfdx[k]), B->w[B->col[k]]));
+			v3 Mdv = scl(B->Mval[i], sub(B->v0[i], B->vv[i]));
+			B->b[i] = add(add(Mdv, scl(h, add(B->fe[i], B->fi[i]))), acc);
+		}
+		/* pA = S A S^T + I - S ; pb = S b */
+		for (uint32_t i = 0; i < n; ++i)
+		{
+			for (uint32_t k = B->rowptr[i]; k < B->rowptr[i + 1]; ++k)
+			{
+				uint32_t j = B->col[k];
+				if (!(B->S[i] && B->S[j])) B->A[k] = mzero();
+			}
+			if (!B->S[i]) B->A[B->diag[i]] = mdiag(1);
+			B->pb[i] = B->S[i] ? B->b[i] : V(0, 0, 0);
+		}
+		uint32_t sub_it = pcg(B, B->A, B->pb, B->py, maxSub, subEps);
+		if (sub_it > maxSubIt) maxSubIt = sub_it;
+		for (uint32_t i = 0; i < n; ++i)
+		{
+			B->vv[i] = add(B->vv[i], B->py[i]);
+			B->xx[i] = add(add(B->x0[i], scl(h, B->vv[i])), B->y[i]);
+		}
+		error = vdot(B->py, B->py, n);
+		if (iteration == 0)
+		{
+			error0 = error;
+			if (error <= eps * eps) break;
+		}
+		else if (error <= eps * eps * error0) break;
+		++iteration;
+	}
+	return maxSubIt;
+}
+
+static int aabb_overlap_sphere(v3 p, real r, v3 c, real R)
+{
+	/* aabb.h:371 b3TestOverlap of AABB(p, r) and AABB(c, R) */
+	if (p.x + r < c.x - R || p.x - r > c.x + R) return 0;
+	if (p.y + r < c.y - R || p.y - r > c.y + R) return 0;
+	if (p.z + r < c.z - R || p.z - r > c.z + R) return 0;
+	return 1;
+}
+
+/* body.cpp:552-604 */
+static uint32_t body_step(body_t* B, real dt, uint32_t newtonIt, uint32_t maxSub, real subEps)
+{
+	uint32_t n = B->n;
+	/* contact_manager.cpp:108-146 UpdateContacts */
+	if (B->srad)
+		for (uint32_t i = 0; i < n; ++i)
+			for (uint32_t k = 0; k < B->nw; ++k)
+			{
+				size_t c = (size_t)i * B->nw + k;
+				if (!B->c_exists[c]) continue;
+				if (B->type[i] != DYNAMIC || !aabb_overlap_sphere(B->x[i], B->srad[i], B->wc[k], B->wr[k]))
+				{
+					B->c_exists[c] = 0;
+					continue;
+				}
+				B->c_normalForce[c] = 0;
+				B->c_apply[c] = 0;
+			}
+	uint32_t it = 0;
+	if (dt > 0)
+	{
+		for (uint32_t i = 0; i < n; ++i)
+		{
+			B->x0[i] = B->x[i];
+			B->v0[i] = B->v[i];
+			B->fe[i] = B->fext[i];
+			B->y[i] = B->trans[i];
+			if (B->type[i] == DYNAMIC)
+			{
+				B->Mval[i] = B->mass[i];
+				B->fe[i] = add(B->fe[i], scl(B->mass[i], B->gravity));
+				B->S[i] = 1;
+			}
+			else
+			{
+				B->Mval[i] = 1;
+				B->S[i] = 0;
+			}
+		}
+		it = solve_be(B, dt, newtonIt, maxSub, subEps);
+		for (uint32_t i = 0; i < n; ++i)
+		{
+			B->x[i] = B->xx[i];
+			B->v[i] = B->vv[i];
+		}
+		/* sphere_shape_contact.cpp:145-189 ApplyFriction */
+		if (B->srad)
+			for (uint32_t i = 0; i < n; ++i)
+				for (uint32_t k = 0; k < B->nw; ++k)
+				{
+					size_t c = (size_t)i * B->nw + k;
+					if (!B->c_exists[c] || !B->c_apply[c]) continue;
+					v3 normal = B->c_normal[c];
+					real nf = B->c_normalForce[c];
+					v3 t1 = perp(normal);
+					v3 t2 = cross(t1, normal);
+					v3 v1 = B->v[i];
+					real im1 = B->invmass[i];
+					real fr = rsqrt_(B->sfric[i] * B->wf[k]);
+					real tm = im1 > 0 ? (real)1 / im1 : 0;
+					v2 Cdot = V2(dot(v1, t1), dot(v1, t2));
+					v2 imp = scl2(tm, V2(-Cdot.x, -Cdot.y));
+					real maxImp = fr * (dt * nf);
+					if (imp.x * imp.x + imp.y * imp.y > maxImp * maxImp)
+					{
+						imp = normalize2(imp);
+						imp = scl2(maxImp, imp);
+					}
+					v3 P = add(scl(imp.x, t1), scl(imp.y, t2));
+					B->v[i] = add(v1, scl(im1, P));
+				}
+	}
+	for (uint32_t i = 0; i < n; ++i)
+	{
+		B->fext[i] = V(0, 0, 0);
+		B->trans[i] = V(0, 0, 0);
+	}
+	/* contact_manager.cpp:65-82 FindNewContacts (only dynamic particles collide) */
+	if (B->srad)
+		for (uint32_t i = 0; i < n; ++i)
+			for (uint32_t k = 0; k < B->nw; ++k)
+			{
+				size_t c = (size_t)i * B->nw + k;
+				if (B->c_exists[c]) continue;
+				if (B->type[i] != DYNAMIC) continue;
+				if (aabb_overlap_sphere(B->x[i], B->srad[i], B->wc[k], B->wr[k]))
+				{
+					B->c_exists[c] = 1;
+					B->c_normalForce[c] = 0;
+					B->c_apply[c] = 0;
+				}
+			}
+	return it;
+}
+
+static double now_sec(void)
+{
+	struct timespec ts;
+	clock_gettime(CLOCK_MONOTONIC, &ts);
+	return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+int b3o_simulate(const b3o_desc* d, b3o_run* run)
+{
+	body_t* B = body_create(d);
+	if (!B) return 1;
+	double t0 = now_sec();
+	for (uint32_t s = 0; s < run->steps; ++s)
+	{
+		uint32_t it = body_step(B, (real)run->dt, run->newton_iters, run->max_sub, (real)run->sub_tol);
+		if (run->sub_iters_out) run->sub_iters_out[s] = it;
+	}
+	double t1 = now_sec();
+	if (run->seconds_out) *run->seconds_out = t1 - t0;
+	for (uint32_t i = 0; i < B->n; ++i)
+	{
+		run->x_out[3 * i + 0] = B->x[i].x; run->x_out[3 * i + 1] = B->x[i].y; run->x_out[3 * i + 2] = B->x[i].z;
+		run->v_out[3 * i + 0] = B->v[i].x; run->v_out[3 * i + 1] = B->v[i].y; run->v_out[3 * i + 2] = B->v[i].z;
+	}
+	body_free(B);
+	return 0;
+}
+
+/* ------------------------------------------------------------------ many bodies on many threads */
+typedef struct
+{
+	const b3o_desc* descs;
+	b3o_run* runs;
+	uint32_t count;
+	uint32_t next;
+	pthread_mutex_t lock;
+} batch_job;
+
+static void* batch_worker(void* arg)
+{
+	batch_job* J = (batch_job*)arg;
+	for (;;)
+	{
+		pthread_mutex_lock(&J->lock);
+		uint32_t k = J->next++;
+		pthread_mutex_unlock(&J->lock);
+		if (k >= J->count) break;
+		b3o_simulate(J->descs + k, J->runs + k);
+	}
+	return NULL;
+}
+
+/* Independent bodies share nothing, so they run on `threads` host threads. Returns the wall
+ * time of the whole batch in *seconds. */
+int b3o_simulate_batch(const b3o_desc* descs, b3o_run* runs, uint32_t count, uint32_t threads, double* seconds)
+{
+	batch_job J;
+	J.descs = descs;
+	J.runs = runs;
+	J.count = count;
+	J.next = 0;
+	pthread_mutex_init(&J.lock, NULL);
+	if (threads < 1) threads = 1;
+	if (threads > 256) threads = 256;
+	pthread_t th[256];
+	double t0 = now_sec();
+	for (uint32_t t = 0; t < threads; ++t) pthread_create(&th[t], NULL, batch_worker, &J);
+	for (uint32_t t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+	if (seconds) *seconds = now_sec() - t0;
+	pthread_mutex_destroy(&J.lock);
+	return 0;
+}

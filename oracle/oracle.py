@@ -1,0 +1,182 @@
+"""ctypes front-end of the oracle (test infrastructure only).
+
+Two CPU implementations of the implicit body step sit behind the same call:
+
+* ``port``: the restatement in ``oracle/b3_oracle.c`` (built by ``make -C oracle port``), float
+  or double. It exists on every machine, the GPU host included.
+* ``ref``: the reference library compiled from its own sources with ``oracle/ref_harness.cpp``
+  (``make -C oracle ref``), float or double. It exists only where the reference sources were
+  present at build time; it is never shipped.
+
+Only tests, the smoke check and the CPU-baseline leg of bench.py use this module, and only as
+the checker; the product path never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REFOUT = os.path.join(HERE, "_ref")
+
+_dp = C.POINTER(C.c_double)
+_up = C.POINTER(C.c_uint32)
+_ip = C.POINTER(C.c_int32)
+
+
+class _Desc(C.Structure):
+    """Mirror of RefDesc (oracle/ref_harness.cpp) and b3o_desc (oracle/b3_oracle.c)."""
+    _fields_ = [
+        ("n", C.c_uint32), ("x", _dp), ("v", _dp), ("type", _ip), ("damping", _dp),
+        ("tet_count", C.c_uint32), ("tets", _up), ("tet_rest", _dp), ("tet_E", _dp), ("tet_nu", _dp),
+        ("tet_kdamp", _dp), ("tet_density", _dp),
+        ("tri_count", C.c_uint32), ("tris", _up), ("tri_rest", _dp), ("tri_Ex", _dp), ("tri_Ey", _dp),
+        ("tri_Es", _dp), ("tri_nuxy", _dp), ("tri_nuyx", _dp), ("tri_kdamp", _dp), ("tri_density", _dp),
+        ("spring_count", C.c_uint32), ("springs", _up), ("spring_L0", _dp), ("spring_ks", _dp),
+        ("spring_kd", _dp),
+        ("sphere_radius", _dp), ("sphere_friction", _dp),
+        ("world_sphere_count", C.c_uint32), ("world_spheres", _dp),
+        ("gravity", C.c_double * 3),
+    ]
+
+
+class _Run(C.Structure):
+    _fields_ = [
+        ("steps", C.c_uint32), ("dt", C.c_double), ("newton_iters", C.c_uint32), ("max_sub", C.c_uint32),
+        ("sub_tol", C.c_double), ("use_body_step", C.c_int32),
+        ("x_out", _dp), ("v_out", _dp), ("sub_iters_out", _up), ("seconds_out", _dp),
+    ]
+
+
+_libs: dict = {}
+_lock = threading.Lock()
+
+
+def build_port() -> None:
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+
+
+def build_ref() -> bool:
+    """Build the reference harness if the reference sources are present; return availability."""
+    if not os.path.isdir("/root/reference/src"):
+        return ref_available()
+    subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref"], check=True)
+    return ref_available()
+
+
+def ref_available() -> bool:
+    return os.path.exists(os.path.join(REFOUT, "libb3ref32.so")) and os.path.exists(
+        os.path.join(REFOUT, "libb3ref64.so"))
+
+
+def _lib(kind: str, bits: int):
+    key = (kind, bits)
+    with _lock:
+        if key in _libs:
+            return _libs[key]
+        if kind == "port":
+            path = os.path.join(BUILD, f"libb3oracle{bits}.so")
+            if not os.path.exists(path):
+                build_port()
+            lib = C.CDLL(path)
+            lib.b3o_simulate.argtypes = [C.POINTER(_Desc), C.POINTER(_Run)]
+            lib.b3o_simulate.restype = C.c_int
+        elif kind == "ref":
+            path = os.path.join(REFOUT, f"libb3ref{bits}.so")
+            if not os.path.exists(path):
+                raise FileNotFoundError(f"reference harness not built: {path}")
+            lib = C.CDLL(path)
+            lib.ref_simulate.argtypes = [C.POINTER(_Desc), C.POINTER(_Run)]
+            lib.ref_simulate.restype = C.c_int
+        else:
+            raise ValueError(kind)
+        _libs[key] = lib
+        return lib
+
+
+def _arr(a, dtype):
+    if a is None:
+        return None
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _ptr(a, ctype):
+    if a is None or a.size == 0:
+        return C.cast(None, ctype)
+    return a.ctypes.data_as(ctype)
+
+
+def _make_desc(body):
+    keep = []
+
+    def d(a):
+        a = _arr(a, np.float64)
+        keep.append(a)
+        return _ptr(a, _dp)
+
+    def u(a):
+        a = _arr(a, np.uint32)
+        keep.append(a)
+        return _ptr(a, _up)
+
+    tt = _arr(body.type, np.int32)
+    keep.append(tt)
+    desc = _Desc()
+    desc.n = body.n
+    desc.x = d(body.x)
+    desc.v = d(body.v)
+    desc.type = tt.ctypes.data_as(_ip)
+    desc.damping = d(body.damping)
+    desc.tet_count = body.tets.shape[0]
+    desc.tets = u(body.tets)
+    desc.tet_rest = C.cast(None, _dp)
+    desc.tet_E, desc.tet_nu, desc.tet_kdamp, desc.tet_density = (
+        d(body.tet_E), d(body.tet_nu), d(body.tet_kdamp), d(body.tet_density))
+    desc.tri_count = body.tris.shape[0]
+    desc.tris = u(body.tris)
+    desc.tri_rest = C.cast(None, _dp)
+    desc.tri_Ex, desc.tri_Ey, desc.tri_Es = d(body.tri_Ex), d(body.tri_Ey), d(body.tri_Es)
+    desc.tri_nuxy, desc.tri_nuyx = d(body.tri_nuxy), d(body.tri_nuyx)
+    desc.tri_kdamp, desc.tri_density = d(body.tri_kdamp), d(body.tri_density)
+    desc.spring_count = body.springs.shape[0]
+    desc.springs = u(body.springs)
+    desc.spring_L0, desc.spring_ks, desc.spring_kd = d(body.spring_L0), d(body.spring_ks), d(body.spring_kd)
+    desc.sphere_radius = d(body.sphere_radius) if body.sphere_radius is not None else C.cast(None, _dp)
+    desc.sphere_friction = d(body.sphere_friction) if body.sphere_friction is not None else C.cast(None, _dp)
+    desc.world_sphere_count = body.world_spheres.shape[0]
+    desc.world_spheres = d(body.world_spheres)
+    for k in range(3):
+        desc.gravity[k] = float(body.gravity[k])
+    return desc, keep
+
+
+def simulate(body, steps: int, dt: float = 1.0 / 60.0, newton_iters: int = 1, max_sub: int = 200,
+             sub_tol: float = 1e-5, kind: str = "port", bits: int = 32, use_body_step: bool = False,
+             threads: int = 1):
+    """Run ``steps`` implicit steps on a CPU implementation. Returns (x, v, iters, seconds)."""
+    lib = _lib(kind, bits)
+    desc, keep = _make_desc(body)
+    n = body.n
+    x = np.zeros((n, 3))
+    v = np.zeros((n, 3))
+    it = np.zeros(max(steps, 1), np.uint32)
+    sec = np.zeros(1)
+    run = _Run()
+    run.steps, run.dt, run.newton_iters, run.max_sub = steps, dt, newton_iters, max_sub
+    run.sub_tol = sub_tol
+    run.use_body_step = 1 if use_body_step else 0
+    run.x_out, run.v_out = x.ctypes.data_as(_dp), v.ctypes.data_as(_dp)
+    run.sub_iters_out = it.ctypes.data_as(_up)
+    run.seconds_out = sec.ctypes.data_as(_dp)
+    fn = lib.b3o_simulate if kind == "port" else lib.ref_simulate
+    rc = fn(C.byref(desc), C.byref(run))
+    if rc != 0:
+        raise RuntimeError(f"oracle {kind}{bits} failed with {rc}")
+    del keep
+    return x, v, it[:steps].copy(), float(sec[0])
