@@ -1,0 +1,315 @@
+"""ctypes binding of the C ABI in include/b3g.h (libb3g.so, built in-tree by build.py).
+
+This is the Python face of the drop-in boundary: the same calls a C/C++ host makes. There is no
+CPU fallback: if libb3g.so is missing, or no GPU is usable, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libb3g.so")
+
+STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
+PRECISION_FP32, PRECISION_FP64, PRECISION_BF16 = 0, 1, 2
+PRECOND_JACOBI, PRECOND_BLOCK_JACOBI = 0, 1
+SOLVE_STATUS = {0: "converged", 1: "max_iterations", 2: "nonfinite", 3: "breakdown"}
+
+_fp = C.POINTER(C.c_float)
+_up = C.POINTER(C.c_uint32)
+_ip = C.POINTER(C.c_int32)
+
+
+class BodyDescC(C.Structure):
+    _fields_ = [
+        ("vertex_count", C.c_uint32), ("positions", _fp), ("velocities", _fp), ("types", _ip),
+        ("damping", _fp), ("masses", _fp),
+        ("tet_count", C.c_uint32), ("tets", _up), ("tet_rest", _fp), ("tet_young", _fp),
+        ("tet_poisson", _fp), ("tet_stiffness_damping", _fp), ("tet_density", _fp),
+        ("tri_count", C.c_uint32), ("tris", _up), ("tri_rest", _fp), ("tri_young_x", _fp),
+        ("tri_young_y", _fp), ("tri_shear", _fp), ("tri_poisson_xy", _fp), ("tri_poisson_yx", _fp),
+        ("tri_stiffness_damping", _fp), ("tri_density", _fp),
+        ("spring_count", C.c_uint32), ("springs", _up), ("spring_rest_length", _fp),
+        ("spring_stiffness", _fp), ("spring_damping", _fp),
+        ("sphere_radius", _fp), ("sphere_friction", _fp),
+        ("world_sphere_count", C.c_uint32), ("world_spheres", _fp),
+        ("gravity", C.c_float * 3),
+    ]
+
+
+class SolverConfig(C.Structure):
+    _fields_ = [
+        ("force_iterations", C.c_uint32), ("max_pcg_iterations", C.c_uint32),
+        ("pcg_tolerance", C.c_double), ("newton_tolerance", C.c_double),
+        ("refresh_period", C.c_uint32), ("precision", C.c_int32), ("preconditioner", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class StepStats(C.Structure):
+    _fields_ = [
+        ("newton_iterations", C.c_uint32), ("pcg_iterations", C.c_uint32),
+        ("min_pcg_iterations", C.c_uint32), ("solve_status", C.c_int32),
+        ("residual_ratio", C.c_double), ("newton_error", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {"newton_iterations": self.newton_iterations, "pcg_iterations": self.pcg_iterations,
+                "min_pcg_iterations": self.min_pcg_iterations,
+                "solve_status": SOLVE_STATUS.get(self.solve_status, str(self.solve_status)),
+                "residual_ratio": self.residual_ratio, "newton_error": self.newton_error}
+
+
+# every entry point of include/b3g.h with its ctypes signature
+SIGNATURES = {
+    "b3g_solver_config_default": (None, [C.POINTER(SolverConfig)]),
+    "b3g_last_error": (C.c_char_p, []),
+    "b3g_version": (C.c_char_p, []),
+    "b3g_context_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "b3g_context_destroy": (C.c_int, [C.c_void_p]),
+    "b3g_context_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "b3g_context_synchronize": (C.c_int, [C.c_void_p]),
+    "b3g_body_create": (C.c_int, [C.c_void_p, C.POINTER(BodyDescC), C.POINTER(C.c_void_p)]),
+    "b3g_body_destroy": (C.c_int, [C.c_void_p]),
+    "b3g_body_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "b3g_body_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "b3g_body_step": (C.c_int, [C.c_void_p, C.c_float, C.POINTER(SolverConfig), C.POINTER(StepStats)]),
+    "b3g_step_batch": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.c_float,
+                                 C.POINTER(SolverConfig), C.c_uint32, C.POINTER(StepStats)]),
+    "b3g_body_get_state": (C.c_int, [C.c_void_p, _fp, _fp]),
+    "b3g_body_set_state": (C.c_int, [C.c_void_p, _fp, _fp]),
+    "b3g_body_apply_forces": (C.c_int, [C.c_void_p, _fp]),
+    "b3g_body_apply_translations": (C.c_int, [C.c_void_p, _fp]),
+    "b3g_body_set_types": (C.c_int, [C.c_void_p, _ip]),
+    "b3g_body_get_rotations": (C.c_int, [C.c_void_p, _fp]),
+    "b3g_body_set_rotations": (C.c_int, [C.c_void_p, _fp]),
+    "b3g_body_get_masses": (C.c_int, [C.c_void_p, _fp]),
+    "b3g_body_get_stats": (C.c_int, [C.c_void_p, C.POINTER(StepStats)]),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libb3g.so; raise if it is absent (there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libb3g.so not built ({path}); run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class B3gError(RuntimeError):
+    pass
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        msg = load_library().b3g_last_error().decode(errors="replace")
+        raise B3gError(f"{what} failed ({rc}): {msg}")
+
+
+def solver_config(force_iterations: int = 1, max_pcg_iterations: int = 200, pcg_tolerance: float = 1e-5,
+                  refresh_period: int = 50, precision: int = PRECISION_FP32,
+                  preconditioner: int = PRECOND_JACOBI, newton_tolerance: Optional[float] = None) -> SolverConfig:
+    lib = load_library()
+    c = SolverConfig()
+    lib.b3g_solver_config_default(C.byref(c))
+    c.force_iterations = force_iterations
+    c.max_pcg_iterations = max_pcg_iterations
+    c.pcg_tolerance = pcg_tolerance
+    c.refresh_period = refresh_period
+    c.precision = precision
+    c.preconditioner = preconditioner
+    if newton_tolerance is not None:
+        c.newton_tolerance = newton_tolerance
+    return c
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.b3g_context_create(device, C.byref(h)), "b3g_context_create")
+        self.handle = h
+        self.device = device
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(load_library().b3g_context_stream(self.handle, C.byref(s)), "b3g_context_stream")
+        return s.value or 0
+
+    def synchronize(self):
+        _check(load_library().b3g_context_synchronize(self.handle), "b3g_context_synchronize")
+
+    def close(self):
+        if self.handle:
+            load_library().b3g_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _f32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _ptr(a, t):
+    if a is None or a.size == 0:
+        return C.cast(None, t)
+    return a.ctypes.data_as(t)
+
+
+class Body:
+    """One body on the GPU, created from a meshes.BodyDesc (or anything with its fields)."""
+
+    def __init__(self, ctx: Context, desc, masses=None):
+        lib = load_library()
+        self.ctx = ctx
+        keep = []
+
+        def f(a):
+            a = _f32(a)
+            keep.append(a)
+            return _ptr(a, _fp)
+
+        def u(a):
+            a = np.ascontiguousarray(a, dtype=np.uint32)
+            keep.append(a)
+            return _ptr(a, _up)
+
+        d = BodyDescC()
+        d.vertex_count = desc.n
+        d.positions = f(desc.x)
+        d.velocities = f(desc.v)
+        types = np.ascontiguousarray(desc.type, dtype=np.int32)
+        keep.append(types)
+        d.types = types.ctypes.data_as(_ip)
+        d.damping = f(desc.damping)
+        d.masses = f(masses) if masses is not None else C.cast(None, _fp)
+        d.tet_count = desc.tets.shape[0]
+        d.tets = u(desc.tets)
+        d.tet_rest = C.cast(None, _fp)
+        d.tet_young, d.tet_poisson = f(desc.tet_E), f(desc.tet_nu)
+        d.tet_stiffness_damping, d.tet_density = f(desc.tet_kdamp), f(desc.tet_density)
+        d.tri_count = desc.tris.shape[0]
+        d.tris = u(desc.tris)
+        d.tri_rest = C.cast(None, _fp)
+        d.tri_young_x, d.tri_young_y, d.tri_shear = f(desc.tri_Ex), f(desc.tri_Ey), f(desc.tri_Es)
+        d.tri_poisson_xy, d.tri_poisson_yx = f(desc.tri_nuxy), f(desc.tri_nuyx)
+        d.tri_stiffness_damping, d.tri_density = f(desc.tri_kdamp), f(desc.tri_density)
+        d.spring_count = desc.springs.shape[0]
+        d.springs = u(desc.springs)
+        d.spring_rest_length, d.spring_stiffness, d.spring_damping = (
+            f(desc.spring_L0), f(desc.spring_ks), f(desc.spring_kd))
+        d.sphere_radius = f(desc.sphere_radius) if desc.sphere_radius is not None else C.cast(None, _fp)
+        d.sphere_friction = f(desc.sphere_friction) if desc.sphere_friction is not None else C.cast(None, _fp)
+        d.world_sphere_count = desc.world_spheres.shape[0]
+        d.world_spheres = f(desc.world_spheres)
+        for k in range(3):
+            d.gravity[k] = float(desc.gravity[k])
+        h = C.c_void_p()
+        _check(lib.b3g_body_create(ctx.handle, C.byref(d), C.byref(h)), "b3g_body_create")
+        del keep
+        self.handle = h
+        self.n = desc.n
+        self.tet_count = desc.tets.shape[0]
+
+    def info(self) -> dict:
+        a = (C.c_uint64 * 6)()
+        _check(load_library().b3g_body_info(self.handle, a), "b3g_body_info")
+        return dict(zip(["vertices", "tets", "tris", "springs", "nnzb", "slots"], list(a)))
+
+    def device_bytes(self) -> int:
+        b = C.c_uint64()
+        _check(load_library().b3g_body_device_bytes(self.handle, C.byref(b)), "b3g_body_device_bytes")
+        return int(b.value)
+
+    def step(self, dt: float, config: Optional[SolverConfig] = None, stats: bool = True) -> Optional[dict]:
+        cfg = config if config is not None else solver_config()
+        st = StepStats()
+        _check(load_library().b3g_body_step(self.handle, dt, C.byref(cfg), C.byref(st) if stats else None),
+               "b3g_body_step")
+        return st.as_dict() if stats else None
+
+    def state(self):
+        x = np.zeros((self.n, 3), np.float32)
+        v = np.zeros((self.n, 3), np.float32)
+        _check(load_library().b3g_body_get_state(self.handle, x.ctypes.data_as(_fp), v.ctypes.data_as(_fp)),
+               "b3g_body_get_state")
+        return x, v
+
+    def set_state(self, x=None, v=None):
+        xa, va = _f32(x), _f32(v)
+        _check(load_library().b3g_body_set_state(self.handle, _ptr(xa, _fp), _ptr(va, _fp)), "b3g_body_set_state")
+
+    def apply_forces(self, f):
+        fa = _f32(f)
+        _check(load_library().b3g_body_apply_forces(self.handle, fa.ctypes.data_as(_fp)), "b3g_body_apply_forces")
+        self.ctx.synchronize()
+
+    def apply_translations(self, t):
+        ta = _f32(t)
+        _check(load_library().b3g_body_apply_translations(self.handle, ta.ctypes.data_as(_fp)),
+               "b3g_body_apply_translations")
+        self.ctx.synchronize()
+
+    def set_types(self, types):
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        _check(load_library().b3g_body_set_types(self.handle, t.ctypes.data_as(_ip)), "b3g_body_set_types")
+
+    def rotations(self) -> np.ndarray:
+        q = np.zeros((self.tet_count, 4), np.float32)
+        _check(load_library().b3g_body_get_rotations(self.handle, q.ctypes.data_as(_fp)), "b3g_body_get_rotations")
+        return q
+
+    def set_rotations(self, q):
+        qa = _f32(q)
+        _check(load_library().b3g_body_set_rotations(self.handle, qa.ctypes.data_as(_fp)), "b3g_body_set_rotations")
+
+    def masses(self) -> np.ndarray:
+        m = np.zeros(self.n, np.float32)
+        _check(load_library().b3g_body_get_masses(self.handle, m.ctypes.data_as(_fp)), "b3g_body_get_masses")
+        return m
+
+    def stats(self) -> dict:
+        st = StepStats()
+        _check(load_library().b3g_body_get_stats(self.handle, C.byref(st)), "b3g_body_get_stats")
+        return st.as_dict()
+
+    def close(self):
+        if self.handle:
+            load_library().b3g_body_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def step_batch(ctx: Context, bodies: Sequence[Body], dt: float, steps: int = 1,
+               config: Optional[SolverConfig] = None, stats: bool = True):
+    lib = load_library()
+    cfg = config if config is not None else solver_config()
+    arr = (C.c_void_p * len(bodies))(*[b.handle for b in bodies])
+    st = (StepStats * len(bodies))()
+    _check(lib.b3g_step_batch(ctx.handle, arr, len(bodies), dt, C.byref(cfg), steps, st if stats else None),
+           "b3g_step_batch")
+    return [s.as_dict() for s in st] if stats else None

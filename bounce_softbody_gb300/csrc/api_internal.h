@@ -1,0 +1,73 @@
+// Host-side objects behind the opaque handles of include/b3g.h.
+#pragma once
+
+#include "internal.h"
+#include "ops.h"
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+struct BatchCache;
+
+struct b3g_context
+{
+	int device = 0;
+	int sm_count = 0;
+	cudaStream_t stream = nullptr;
+	b3g::Scalars* h_scalars = nullptr;   // pinned, 1024 entries
+	BatchCache* batch = nullptr;
+};
+
+namespace b3g {
+
+// Solver vectors and low-precision matrix storage for one precision mode.
+struct PrecBuffers
+{
+	char* mem = nullptr;
+	size_t bytes = 0;
+	void* vec[7] = {};   // pb r d d2 q s py
+	void* minv = nullptr;
+	void* alo = nullptr;
+};
+
+} // namespace b3g
+
+struct b3g_body
+{
+	b3g_context* ctx = nullptr;
+	uint32_t n = 0, nt = 0, ntr = 0, ns = 0, nw = 0;
+	uint64_t nnzb = 0;
+	b3g::DevBody d{};
+	char* arena = nullptr;
+	size_t arena_bytes = 0;
+	float* staging = nullptr;            // 3 floats per vertex of upload space
+	b3g::PrecBuffers prec[3];
+	// host copies needed by ResetMass / SetType
+	std::vector<int32_t> h_type;
+	std::vector<uint32_t> h_tets, h_tris;
+	std::vector<float> h_tet_mass, h_tri_mass, h_given_mass;
+	std::vector<float> h_mass, h_invmass;
+	b3g_step_stats last{};
+};
+
+namespace b3g {
+
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* where);
+void reset_mass(b3g_body* b);
+int upload_masses(b3g_body* b);
+int ensure_precision(b3g_body* b, int prec);
+DevBody dev_for(const b3g_body* b, int prec, int precond);
+int prec_of(const b3g_solver_config* c);
+int check_config(const b3g_solver_config* c);
+void stats_from(const Scalars& sc, b3g_step_stats* st);
+int read_scalars(b3g_body* b, Scalars* out);
+
+cudaError_t op_accumulate(float* dst, const float* src, size_t count, cudaStream_t st);
+cudaError_t op_set_types(const DevBody& B, const int8_t* new_types, cudaStream_t st);
+
+} // namespace b3g
+
+void destroy_batch_cache(b3g_context* c);
+void forget_body_in_batch_cache(b3g_context* c, b3g_body* b);

@@ -1,0 +1,723 @@
+// Device building blocks of the implicit step, shared by the per-op kernels (kernels.cu) and
+// the persistent batch kernel (persistent.cu). Matrices in registers are row-major float[9].
+#pragma once
+
+#include "internal.h"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace b3g {
+
+// settings.h:83-95 of the reference
+constexpr float kContactStiffness = 1000.0f;
+constexpr float kMaxContactCorrection = 0.2f;
+constexpr float kBaumgarte = 0.2f;
+constexpr float kFltEps = 1.1920928955078125e-7f;
+
+// ------------------------------------------------------------------ storage conversions
+template <class T> __device__ __forceinline__ float to_f(T v);
+template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ float to_f<double>(double v) { return (float)v; }
+template <> __device__ __forceinline__ float to_f<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+template <class T> __device__ __forceinline__ T from_f(float v);
+template <> __device__ __forceinline__ float from_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ double from_f<double>(float v) { return (double)v; }
+template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+// arithmetic type of a SpMV over storage T: blocks are widened before the multiply
+template <class T> struct Acc { typedef float type; };
+template <> struct Acc<double> { typedef double type; };
+
+template <class T> __device__ __forceinline__ typename Acc<T>::type widen(T v) { return (typename Acc<T>::type)to_f(v); }
+template <> __device__ __forceinline__ double widen<double>(double v) { return v; }
+
+// ------------------------------------------------------------------ small vector math
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b)
+{
+	return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float len3(float3 a) { return sqrtf(dot3(a, a)); }
+// vec3.h:93 Normalize: multiply by the reciprocal when longer than FLT_EPSILON
+__device__ __forceinline__ float3 normalize3(float3 a)
+{
+	float l = sqrtf(a.x * a.x + a.y * a.y + a.z * a.z);
+	if (l > kFltEps)
+	{
+		float s = 1.0f / l;
+		a = f3(a.x * s, a.y * s, a.z * s);
+	}
+	return a;
+}
+__device__ __forceinline__ float3 ld3(const float* p, int i) { return f3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+__device__ __forceinline__ void st3(float* p, int i, float3 v)
+{
+	p[3 * i] = v.x;
+	p[3 * i + 1] = v.y;
+	p[3 * i + 2] = v.z;
+}
+// rows r of a row-major 3x3 times v
+__device__ __forceinline__ float3 mv9(const float* M, float3 v)
+{
+	return f3(M[0] * v.x + M[1] * v.y + M[2] * v.z, M[3] * v.x + M[4] * v.y + M[5] * v.z,
+	          M[6] * v.x + M[7] * v.y + M[8] * v.z);
+}
+__device__ __forceinline__ float3 mtv9(const float* M, float3 v)
+{
+	return f3(M[0] * v.x + M[3] * v.y + M[6] * v.z, M[1] * v.x + M[4] * v.y + M[7] * v.z,
+	          M[2] * v.x + M[5] * v.y + M[8] * v.z);
+}
+
+// quat.h:133 GetRotationMatrix, row-major
+__device__ __forceinline__ void quat_to_mat(float4 q, float R[9])
+{
+	float x = q.x, y = q.y, z = q.z, w = q.w;
+	float x2 = x + x, y2 = y + y, z2 = z + z;
+	float xx = x * x2, xy = x * y2, xz = x * z2;
+	float yy = y * y2, yz = y * z2, zz = z * z2;
+	float wx = w * x2, wy = w * y2, wz = w * z2;
+	R[0] = 1.0f - (yy + zz); R[1] = xy - wz;          R[2] = xz + wy;
+	R[3] = xy + wz;          R[4] = 1.0f - (xx + zz); R[5] = yz - wx;
+	R[6] = xz - wy;          R[7] = yz + wx;          R[8] = 1.0f - (xx + yy);
+}
+
+// Rotation of the deformation gradient F (row-major) by the iterative method of
+// Mueller et al., "A Robust Method to Extract the Rotational Part of Deformations", warm
+// started from q0, with the stopping rules of tetrahedron_element_force.cpp:273-311
+// (den == 0, |omega| < 1e-9, inverse denominator + 1e-9, at most 32 iterations).
+__device__ __forceinline__ float4 extract_rotation(const float F[9], float4 q)
+{
+	const float kTol = 1.0e-9f;
+#pragma unroll 1
+	for (int it = 0; it < 32; ++it)
+	{
+		float R[9];
+		quat_to_mat(q, R);
+		// columns: R(:, c) . F(:, c) and R(:, c) x F(:, c)
+		float3 r0 = f3(R[0], R[3], R[6]), r1 = f3(R[1], R[4], R[7]), r2 = f3(R[2], R[5], R[8]);
+		float3 a0 = f3(F[0], F[3], F[6]), a1 = f3(F[1], F[4], F[7]), a2 = f3(F[2], F[5], F[8]);
+		float den = fabsf(dot3(r0, a0) + dot3(r1, a1) + dot3(r2, a2));
+		if (den == 0.0f) break;
+		float3 torque = cross3(r0, a0) + cross3(r1, a1) + cross3(r2, a2);
+		float inv_den = 1.0f / den + kTol;
+		float3 omega = inv_den * torque;
+		float w = len3(omega);
+		if (w < kTol) break;
+		float3 axis = f3(omega.x / w, omega.y / w, omega.z / w);
+		float sn, cs;
+		sincosf(0.5f * w, &sn, &cs);
+		float4 qw = make_float4(sn * axis.x, sn * axis.y, sn * axis.z, cs);
+		// quat.h:204 b3Mul(qw, q)
+		float3 av = f3(qw.x, qw.y, qw.z), bv = f3(q.x, q.y, q.z);
+		float3 rv = cross3(av, bv) + qw.w * bv + q.w * av;
+		float rs = qw.w * q.w - dot3(av, bv);
+		float l = sqrtf(dot3(rv, rv) + rs * rs);
+		if (l > kFltEps)
+		{
+			rv = f3(rv.x / l, rv.y / l, rv.z / l);
+			rs = rs / l;
+		}
+		q = make_float4(rv.x, rv.y, rv.z, rs);
+	}
+	return q;
+}
+
+// X = [e1 e2 e3] * invE with invE column-major (ie[3 j + r] = invE(r, j)); result row-major.
+__device__ __forceinline__ void edge_times_invE(float3 e1, float3 e2, float3 e3, const float ie[9], float X[9])
+{
+#pragma unroll
+	for (int j = 0; j < 3; ++j)
+	{
+		float c0 = ie[3 * j], c1 = ie[3 * j + 1], c2 = ie[3 * j + 2];
+		X[0 + j] = c0 * e1.x + c1 * e2.x + c2 * e3.x;
+		X[3 + j] = c0 * e1.y + c1 * e2.y + c2 * e3.y;
+		X[6 + j] = c0 * e1.z + c1 * e2.z + c2 * e3.z;
+	}
+}
+
+// ------------------------------------------------------------------ element kernels (one element)
+struct StepParams
+{
+	float h;
+	int first_newton;   // iterate == state (x, v)
+};
+
+// Corotational tetrahedron (tetrahedron_element_force.cpp:313-464), in stress form.
+// With U = R^T (F + W + kd Vg) - I, where F, W and Vg are the gradients of the positions, of
+// w = x0 - x + h v + y and of the velocities, the reference's
+//   h (f + f_damping + dfdx w)_a = -h R K0_a* (R^T (p + w + kd v) - rest)
+// equals -h V R sigma(sym U) g_a with sigma(e) = lambda tr(e) I + 2 mu e, because
+// K0 = V B^T D B is that isotropic operator. The A contribution (h^2 + h kd) R K0_ab R^T is
+// kept in factored form: rows of R times the shape gradients, scaled (tet_rec).
+__device__ __forceinline__ void tet_element(const DevBody& B, int e, const StepParams& P)
+{
+	const float h = P.h;
+	uint4 id = B.tet[e];
+	const float* X = P.first_newton ? B.x : B.xi;
+	const float* Vv = P.first_newton ? B.v : B.vi;
+	float ie[9];
+#pragma unroll
+	for (int k = 0; k < 9; ++k) ie[k] = B.tet_invE[9 * (size_t)e + k];
+	float4 mat = B.tet_mat[e];  // volume, lambda, mu, kd
+	float3 p1 = ld3(X, id.x), p2 = ld3(X, id.y), p3 = ld3(X, id.z), p4 = ld3(X, id.w);
+	float F[9];
+	edge_times_invE(p2 - p1, p3 - p1, p4 - p1, ie, F);
+	float4 q = extract_rotation(F, B.tet_q[e]);
+	B.tet_q[e] = q;
+	float R[9];
+	quat_to_mat(q, R);
+
+	// w = x0 - x + h v + y
+	float3 v1 = ld3(Vv, id.x), v2 = ld3(Vv, id.y), v3 = ld3(Vv, id.z), v4 = ld3(Vv, id.w);
+	float3 y1 = ld3(B.trans, id.x), y2 = ld3(B.trans, id.y), y3 = ld3(B.trans, id.z), y4 = ld3(B.trans, id.w);
+	float3 w1 = h * v1 + y1, w2 = h * v2 + y2, w3 = h * v3 + y3, w4 = h * v4 + y4;
+	if (!P.first_newton)
+	{
+		w1 = w1 + (ld3(B.x, id.x) - p1);
+		w2 = w2 + (ld3(B.x, id.y) - p2);
+		w3 = w3 + (ld3(B.x, id.z) - p3);
+		w4 = w4 + (ld3(B.x, id.w) - p4);
+	}
+	float G[9];
+	edge_times_invE(w2 - w1, w3 - w1, w4 - w1, ie, G);
+	const float kd = mat.w;
+	if (kd > 0.0f)
+	{
+		float Vg[9];
+		edge_times_invE(v2 - v1, v3 - v1, v4 - v1, ie, Vg);
+#pragma unroll
+		for (int k = 0; k < 9; ++k) G[k] += kd * Vg[k];
+	}
+#pragma unroll
+	for (int k = 0; k < 9; ++k) G[k] += F[k];
+	// U = R^T G - I
+	float U[9];
+#pragma unroll
+	for (int r = 0; r < 3; ++r)
+#pragma unroll
+		for (int c = 0; c < 3; ++c)
+			U[3 * r + c] = R[r] * G[c] + R[3 + r] * G[3 + c] + R[6 + r] * G[6 + c] - (r == c ? 1.0f : 0.0f);
+	const float vol = mat.x, lam = mat.y, mu = mat.z;
+	float tr = U[0] + U[4] + U[8];
+	float S[9];
+#pragma unroll
+	for (int r = 0; r < 3; ++r)
+#pragma unroll
+		for (int c = 0; c < 3; ++c) S[3 * r + c] = mu * (U[3 * r + c] + U[3 * c + r]) + (r == c ? lam * tr : 0.0f);
+
+	float3 g2 = f3(ie[0], ie[3], ie[6]), g3 = f3(ie[1], ie[4], ie[7]), g4 = f3(ie[2], ie[5], ie[8]);
+	float3 g1 = -(g2 + g3 + g4);
+	float3 g[4] = {g1, g2, g3, g4};
+	const float c = (h * h + h * kd) * vol;
+	const float su = sqrtf(c * mu);
+	const float ratio = mu > 0.0f ? lam / mu : 0.0f;
+	float* bc = B.tet_bc + 12 * (size_t)e;
+	float4* rec = B.tet_rec + 4 * (size_t)e;
+#pragma unroll
+	for (int a = 0; a < 4; ++a)
+	{
+		float3 t = mv9(S, g[a]);
+		float3 f = mv9(R, t);
+		float s = -h * vol;
+		bc[3 * a + 0] = s * f.x;
+		bc[3 * a + 1] = s * f.y;
+		bc[3 * a + 2] = s * f.z;
+		float3 rg = mv9(R, g[a]);
+		rec[a] = make_float4(su * rg.x, su * rg.y, su * rg.z, ratio);
+	}
+}
+
+// mat33.h:310 b3ComputeBasis
+__device__ __forceinline__ void compute_basis(float3 a, float3& b, float3& c)
+{
+	const float sqrt_inv3 = sqrtf(1.0f / 3.0f);
+	if (fabsf(a.x) >= sqrt_inv3) b = f3(a.y, -a.x, 0.0f);
+	else b = f3(0.0f, a.z, -a.y);
+	b = normalize3(b);
+	c = cross3(a, b);
+}
+
+// Corotational orthotropic membrane triangle (triangle_element_force.cpp:285-468). Writes the
+// 9 blocks (h^2 + h kd) K_ab of A and the 3 right-hand-side vectors
+// h (f_a - kd (K v)_a - (K w)_a).
+__device__ __forceinline__ void tri_element(const DevBody& B, int e, const StepParams& P)
+{
+	const float h = P.h;
+	uint4 id = B.tri[e];
+	const float* X = P.first_newton ? B.x : B.xi;
+	const float* Vv = P.first_newton ? B.v : B.vi;
+	float3 p[3] = {ld3(X, id.x), ld3(X, id.y), ld3(X, id.z)};
+	int ids[3] = {(int)id.x, (int)id.y, (int)id.z};
+	float3 n = normalize3(cross3(p[1] - p[0], p[2] - p[0]));
+	float3 px, py;
+	compute_basis(n, px, py);
+	float2 x2[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+		x2[k] = make_float2(px.x * p[k].x + px.y * p[k].y + px.z * p[k].z, py.x * p[k].x + py.y * p[k].y + py.z * p[k].z);
+	const float* iS = B.tri_invS + 4 * (size_t)e;  // column-major 2x2
+	float2 t0 = make_float2(x2[1].x - x2[0].x, x2[1].y - x2[0].y);
+	float2 t1 = make_float2(x2[2].x - x2[0].x, x2[2].y - x2[0].y);
+	// F = T invS, column-major
+	float F00 = t0.x * iS[0] + t1.x * iS[1], F10 = t0.y * iS[0] + t1.y * iS[1];
+	float F01 = t0.x * iS[2] + t1.x * iS[3], F11 = t0.y * iS[2] + t1.y * iS[3];
+	// triangle_element_force.cpp:131-150 polar decomposition
+	float det = F00 * F11 - F01 * F10;
+	float sg = (float)(0.0f < det) - (float)(det < 0.0f);
+	float q00 = F00 + sg * F11, q10 = F10 - sg * F01;
+	float q01 = F01 - sg * F10, q11 = F11 + sg * F00;
+	float l0 = sqrtf(q00 * q00 + q10 * q10), l1 = sqrtf(q01 * q01 + q11 * q11);
+	if (l0 > kFltEps) { q00 /= l0; q10 /= l0; }
+	if (l1 > kFltEps) { q01 /= l1; q11 /= l1; }
+	// R = [q00 q01; q10 q11]; us_k = R^T x_k - rest_k
+	const float* rest = B.tri_x + 6 * (size_t)e;
+	float2 us[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+		us[k] = make_float2(q00 * x2[k].x + q10 * x2[k].y - rest[2 * k], q01 * x2[k].x + q11 * x2[k].y - rest[2 * k + 1]);
+	const float* K0 = B.tri_K + 36 * (size_t)e;
+	const float kd = B.tri_kd ? B.tri_kd[e] : 0.0f;
+	const float cA = h * h + h * kd;
+	float3 fa[3];
+#pragma unroll
+	for (int a = 0; a < 3; ++a)
+	{
+		float fx = 0.0f, fy = 0.0f;
+#pragma unroll
+		for (int b = 0; b < 3; ++b)
+		{
+			const float* k = K0 + 4 * (a + 3 * b);
+			fx += k[0] * us[b].x + k[2] * us[b].y;
+			fy += k[1] * us[b].x + k[3] * us[b].y;
+		}
+		float rx = q00 * fx + q01 * fy, ry = q10 * fx + q11 * fy;
+		fa[a] = -(rx * px + ry * py);
+	}
+	// 3-D blocks K_ab = P^T (R K0_ab R^T) P, P = [px^T; py^T]
+	float3 vv[3] = {ld3(Vv, ids[0]), ld3(Vv, ids[1]), ld3(Vv, ids[2])};
+	float3 ww[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+	{
+		ww[k] = h * vv[k] + ld3(B.trans, ids[k]);
+		if (!P.first_newton) ww[k] = ww[k] + (ld3(B.x, ids[k]) - p[k]);
+	}
+	float3 acc[3] = {fa[0], fa[1], fa[2]};
+	float* blk = B.blocks + 81 * (size_t)e;
+#pragma unroll
+	for (int a = 0; a < 3; ++a)
+#pragma unroll
+		for (int b = 0; b < 3; ++b)
+		{
+			const float* k = K0 + 4 * (a + 3 * b);
+			// RK = R k R^T (2x2, column-major k)
+			float m00 = q00 * k[0] + q01 * k[1], m10 = q10 * k[0] + q11 * k[1];
+			float m01 = q00 * k[2] + q01 * k[3], m11 = q10 * k[2] + q11 * k[3];
+			float r00 = m00 * q00 + m01 * q01, r01 = m00 * q10 + m01 * q11;
+			float r10 = m10 * q00 + m11 * q01, r11 = m10 * q10 + m11 * q11;
+			// K = P^T RK P: K[r][c] = sum_{i,j} P[i][r] RK[i][j] P[j][c]
+			float3 c0 = r00 * px + r10 * py;  // P^T * RK column 0
+			float3 c1 = r01 * px + r11 * py;  // column 1
+			float Kb[9];
+			Kb[0] = c0.x * px.x + c1.x * py.x; Kb[1] = c0.x * px.y + c1.x * py.y; Kb[2] = c0.x * px.z + c1.x * py.z;
+			Kb[3] = c0.y * px.x + c1.y * py.x; Kb[4] = c0.y * px.y + c1.y * py.y; Kb[5] = c0.y * px.z + c1.y * py.z;
+			Kb[6] = c0.z * px.x + c1.z * py.x; Kb[7] = c0.z * px.y + c1.z * py.y; Kb[8] = c0.z * px.z + c1.z * py.z;
+			float3 kw = mv9(Kb, ww[b]);
+			acc[a] = acc[a] - kw;
+			if (kd > 0.0f) acc[a] = acc[a] - kd * mv9(Kb, vv[b]);
+			float* o = blk + 9 * (3 * a + b);
+#pragma unroll
+			for (int t = 0; t < 9; ++t) o[t] = cA * Kb[t];
+		}
+	float* bv = B.bvec + 9 * (size_t)e;
+#pragma unroll
+	for (int a = 0; a < 3; ++a)
+	{
+		bv[3 * a + 0] = h * acc[a].x;
+		bv[3 * a + 1] = h * acc[a].y;
+		bv[3 * a + 2] = h * acc[a].z;
+	}
+}
+
+// Tension-only spring (spring_force.cpp:61-143). The stiffness Jacobian keeps the reference's
+// unnormalised outer product dx dx^T. Writes one block h^2 Ks + h Kd (+ on the diagonal,
+// - off it) and one vector h (f1 - Ks (w1 - w2)) (+ for vertex 1, - for vertex 2).
+__device__ __forceinline__ void spring_element(const DevBody& B, int s, const StepParams& P)
+{
+	const float h = P.h;
+	uint2 id = B.spr[s];
+	const float* X = P.first_newton ? B.x : B.xi;
+	const float* Vv = P.first_newton ? B.v : B.vi;
+	float3 x1 = ld3(X, id.x), x2 = ld3(X, id.y);
+	float3 v1 = ld3(Vv, id.x), v2 = ld3(Vv, id.y);
+	float3 dx = x1 - x2;
+	float L = len3(dx);
+	float blk[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+	float3 f = f3(0, 0, 0);
+	float3 kw = f3(0, 0, 0);
+	if (L > 0.0f)
+	{
+		float3 n = f3(dx.x / L, dx.y / L, dx.z / L);
+		float ks = B.spr_ks[s], kd = B.spr_kd[s], L0 = B.spr_L0[s];
+		float3 w1 = h * v1 + ld3(B.trans, id.x), w2 = h * v2 + ld3(B.trans, id.y);
+		if (!P.first_newton)
+		{
+			w1 = w1 + (ld3(B.x, id.x) - x1);
+			w2 = w2 + (ld3(B.x, id.y) - x2);
+		}
+		float3 dw = w1 - w2;
+		if (ks > 0.0f && L > L0)
+		{
+			float C = L - L0;
+			f = -(ks * C) * n;
+			float t = 1.0f - L0 / L;
+			float d[3] = {dx.x, dx.y, dx.z};
+			float Ks[9];
+#pragma unroll
+			for (int r = 0; r < 3; ++r)
+#pragma unroll
+				for (int c = 0; c < 3; ++c)
+				{
+					float o = d[r] * d[c];
+					Ks[3 * r + c] = ks * (o + t * ((r == c ? 1.0f : 0.0f) - o));
+				}
+			kw = mv9(Ks, dw);
+#pragma unroll
+			for (int k = 0; k < 9; ++k) blk[k] += h * h * Ks[k];
+		}
+		if (kd > 0.0f)
+		{
+			float dCdt = dot3(n, v1 - v2);
+			f = f + (-(kd * dCdt)) * n;
+			float nn[3] = {n.x, n.y, n.z};
+#pragma unroll
+			for (int r = 0; r < 3; ++r)
+#pragma unroll
+				for (int c = 0; c < 3; ++c) blk[3 * r + c] += h * kd * nn[r] * nn[c];
+		}
+	}
+	float* o = B.blocks + 9 * ((size_t)9 * B.ntr + s);
+#pragma unroll
+	for (int k = 0; k < 9; ++k) o[k] = blk[k];
+	float3 bvv = h * (f - kw);
+	st3(B.bvec, 3 * B.ntr + s, bvv);
+}
+
+// ------------------------------------------------------------------ row assembly
+// sphere_shape.cpp:50-77 against one static sphere
+__device__ __forceinline__ bool sphere_collide(float4 sh, float3 x, float r1, float3& normal)
+{
+	float radius = sh.w + r1;
+	float rr = radius * radius;
+	float3 d = x - f3(sh.x, sh.y, sh.z);
+	float dd = dot3(d, d);
+	if (dd <= rr)
+	{
+		if (dd > kFltEps * kFltEps)
+		{
+			float dist = sqrtf(dd);
+			normal = f3(d.x / dist, d.y / dist, d.z / dist);
+		}
+		else normal = f3(0.0f, 1.0f, 0.0f);
+		return true;
+	}
+	return false;
+}
+
+// aabb.h:371 b3TestOverlap of AABB(vertex, r) and the sphere's AABB
+__device__ __forceinline__ bool aabb_overlap(float3 p, float r, float4 sh)
+{
+	if (p.x + r < sh.x - sh.w || p.x - r > sh.x + sh.w) return false;
+	if (p.y + r < sh.y - sh.w || p.y - r > sh.y + sh.w) return false;
+	if (p.z + r < sh.z - sh.w || p.z - r > sh.z + sh.w) return false;
+	return true;
+}
+
+template <class TV>
+__device__ __forceinline__ TV* vp(void* p) { return (TV*)p; }
+
+// Assembles row i of the pre-filtered system: pA = S A S^T + I - S and pb = S b with
+//   A = M - h dfdv - h^2 dfdx,  b = M (v0 - v) + h (fe + fi) + h dfdx (x0 - x + h v + y)
+// (sparse_force_solver.cpp:165-174), S = I for dynamic vertices and 0 otherwise
+// (force_solver.cpp:110-129). Also forms the Jacobi preconditioner and, when init_pcg is set
+// (initial guess zero), r = pb, s = M^-1 r, d = s; returns this row's r.s.
+template <class TA, class TV>
+__device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int lane, const StepParams& P,
+                                               bool init_pcg)
+{
+	const int i = slice * kSlice + lane;
+	if (i >= B.n) return 0.0;
+	const float h = P.h;
+	const int w = B.rowlen[i];
+	const int base = B.slice_ptr[slice];
+	const bool Si = B.type[i] == B3G_DYNAMIC;
+	const float* X = P.first_newton ? B.x : B.xi;
+	const float* Vv = P.first_newton ? B.v : B.vi;
+	const float m = B.mass[i];
+	const float Mi = Si ? m : 1.0f;
+	const float damp = B.damping[i];
+	float3 xi = ld3(X, i), vi = ld3(Vv, i), x0 = ld3(B.x, i), v0 = ld3(B.v, i), yi = ld3(B.trans, i);
+	float3 wi = (x0 - xi) + h * vi + yi;
+
+	// vertex terms of b: M (v0 - v) + h (fe + m g + damping force)
+	float3 fe = ld3(B.fext, i);
+	if (Si) fe = fe + m * f3(B.gravity[0], B.gravity[1], B.gravity[2]);
+	float3 fi = f3(0, 0, 0);
+	float diagExtra = Mi;
+	if (damp > 0.0f)
+	{
+		fi = fi + (-damp * m) * vi;
+		diagExtra += h * damp * m;
+	}
+	float Kc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+	if (B.contacts)
+	{
+		const float r1 = B.srad[i];
+		for (int k = 0; k < B.nw; ++k)
+		{
+			const int c = i * B.nw + k;
+			const float4 sh = B.world[k];
+			if (P.first_newton)
+			{
+				// contact_manager.cpp:108-146 UpdateContacts at the start of the step
+				if (B.c_exists[c])
+				{
+					if (!Si || !aabb_overlap(x0, r1, sh)) B.c_exists[c] = 0;
+					else
+					{
+						B.c_nf[c] = 0.0f;
+						B.c_apply[c] = 0;
+					}
+				}
+			}
+			if (!B.c_exists[c]) continue;
+			float3 n2;
+			if (!sphere_collide(sh, xi, r1, n2)) continue;
+			if (!B.c_apply[c])
+			{
+				st3(B.c_normal, c, n2);
+				B.c_apply[c] = 1;
+			}
+			// sphere_shape_contact.cpp:98-126
+			float3 n1 = -n2;
+			float3 c1 = xi + r1 * n1;
+			float3 c2 = f3(sh.x, sh.y, sh.z) + sh.w * n2;
+			float C = len3(c2 - c1);
+			C = fminf(kBaumgarte * C, kMaxContactCorrection);
+			float3 f1 = (-kContactStiffness * C) * n1;
+			fi = fi + f1;
+			float nn[3] = {n1.x, n1.y, n1.z};
+#pragma unroll
+			for (int r = 0; r < 3; ++r)
+#pragma unroll
+				for (int cc = 0; cc < 3; ++cc)
+				{
+					float o = nn[r] * nn[cc];
+					// positive form of -K11 = 1000 (n n^T + C (I - n n^T))
+					Kc[3 * r + cc] += kContactStiffness * (o + C * ((r == cc ? 1.0f : 0.0f) - o));
+				}
+			B.c_nf[c] += len3(f1);
+		}
+	}
+	float3 bi = Mi * (v0 - vi) + h * (fe + fi);
+	// contact dfdx w term: h dfdx w = -h Kc w
+	bi = bi - h * mv9(Kc, wi);
+	for (uint32_t t = B.vt_ptr[i]; t < B.vt_ptr[i + 1]; ++t) bi = bi + ld3(B.tet_bc, B.vt_list[t]);
+	for (uint32_t t = B.vb_ptr[i]; t < B.vb_ptr[i + 1]; ++t)
+	{
+		uint32_t e = B.vb_list[t];
+		float3 c = ld3(B.bvec, e >> 1);
+		bi = (e & 1) ? bi - c : bi + c;
+	}
+
+	float diag[9];
+	for (int k = 0; k < w; ++k)
+	{
+		const int slot = base + k * kSlice + lane;
+		const int j = B.col[slot];
+		float a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+		for (uint32_t t = B.tet_cptr[slot]; t < B.tet_cptr[slot + 1]; ++t)
+		{
+			uint32_t code = B.tet_clist[t];
+			uint32_t e = code >> 4, la = (code >> 2) & 3u, lb = code & 3u;
+			float4 ua = B.tet_rec[4 * (size_t)e + la];
+			float4 ub = B.tet_rec[4 * (size_t)e + lb];
+			float ratio = ua.w;
+			float uab = ua.x * ub.x + ua.y * ub.y + ua.z * ub.z;
+			float A3[3] = {ua.x, ua.y, ua.z}, B3[3] = {ub.x, ub.y, ub.z};
+#pragma unroll
+			for (int r = 0; r < 3; ++r)
+#pragma unroll
+				for (int c = 0; c < 3; ++c) a[3 * r + c] += ratio * A3[r] * B3[c] + B3[r] * A3[c] + (r == c ? uab : 0.0f);
+		}
+		for (uint32_t t = B.blk_cptr[slot]; t < B.blk_cptr[slot + 1]; ++t)
+		{
+			uint32_t code = B.blk_clist[t];
+			const float* blk = B.blocks + 9 * (size_t)(code >> 1);
+			if (code & 1)
+			{
+#pragma unroll
+				for (int q = 0; q < 9; ++q) a[q] -= blk[q];
+			}
+			else
+			{
+#pragma unroll
+				for (int q = 0; q < 9; ++q) a[q] += blk[q];
+			}
+		}
+		const bool Sj = B.type[j] == B3G_DYNAMIC;
+		if (k == 0)
+		{
+#pragma unroll
+			for (int q = 0; q < 9; ++q) a[q] += h * h * Kc[q];
+			a[0] += diagExtra;
+			a[4] += diagExtra;
+			a[8] += diagExtra;
+			if (!Si)
+			{
+#pragma unroll
+				for (int q = 0; q < 9; ++q) a[q] = (q == 0 || q == 4 || q == 8) ? 1.0f : 0.0f;
+			}
+#pragma unroll
+			for (int q = 0; q < 9; ++q) diag[q] = a[q];
+		}
+		else if (!(Si && Sj))
+		{
+#pragma unroll
+			for (int q = 0; q < 9; ++q) a[q] = 0.0f;
+		}
+#pragma unroll
+		for (int q = 0; q < 9; ++q) B.A32[(size_t)q * B.nslots + slot] = a[q];
+		if (B.Alo)
+		{
+#pragma unroll
+			for (int q = 0; q < 9; ++q) ((TA*)B.Alo)[(size_t)q * B.nslots + slot] = from_f<TA>(a[q]);
+		}
+	}
+	if (!Si) bi = f3(0, 0, 0);
+	TV* pb = vp<TV>(B.pb);
+	const int np = B.npad;
+	pb[i] = (TV)bi.x;
+	pb[np + i] = (TV)bi.y;
+	pb[2 * np + i] = (TV)bi.z;
+
+	// preconditioner
+	TV* Mv = vp<TV>(B.Minv);
+	TV m3[9];
+	if (B.precond == B3G_PRECOND_BLOCK_JACOBI)
+	{
+		double d0 = diag[0], d1 = diag[1], d2 = diag[2], d3 = diag[3], d4 = diag[4], d5 = diag[5], d6 = diag[6],
+		       d7 = diag[7], d8 = diag[8];
+		double c00 = d4 * d8 - d5 * d7, c01 = d2 * d7 - d1 * d8, c02 = d1 * d5 - d2 * d4;
+		double c10 = d5 * d6 - d3 * d8, c11 = d0 * d8 - d2 * d6, c12 = d2 * d3 - d0 * d5;
+		double c20 = d3 * d7 - d4 * d6, c21 = d1 * d6 - d0 * d7, c22 = d0 * d4 - d1 * d3;
+		double det = d0 * c00 + d1 * c10 + d2 * c20;
+		double id = 1.0 / det;
+		double inv[9] = {c00 * id, c01 * id, c02 * id, c10 * id, c11 * id, c12 * id, c20 * id, c21 * id, c22 * id};
+#pragma unroll
+		for (int q = 0; q < 9; ++q)
+		{
+			m3[q] = (TV)inv[q];
+			Mv[(size_t)q * np + i] = m3[q];
+		}
+	}
+	else
+	{
+		// sparse_solver.cpp:38-55
+		m3[0] = (TV)(1.0f / diag[0]);
+		m3[4] = (TV)(1.0f / diag[4]);
+		m3[8] = (TV)(1.0f / diag[8]);
+		Mv[i] = m3[0];
+		Mv[np + i] = m3[4];
+		Mv[2 * np + i] = m3[8];
+	}
+	if (!init_pcg) return 0.0;
+	TV r0 = pb[i], r1 = pb[np + i], r2 = pb[2 * np + i];
+	TV s0, s1, s2;
+	if (B.precond == B3G_PRECOND_BLOCK_JACOBI)
+	{
+		s0 = m3[0] * r0 + m3[1] * r1 + m3[2] * r2;
+		s1 = m3[3] * r0 + m3[4] * r1 + m3[5] * r2;
+		s2 = m3[6] * r0 + m3[7] * r1 + m3[8] * r2;
+	}
+	else
+	{
+		s0 = m3[0] * r0;
+		s1 = m3[4] * r1;
+		s2 = m3[8] * r2;
+	}
+	TV* rr = vp<TV>(B.r);
+	TV* dd = vp<TV>(B.d);
+	TV* ss = vp<TV>(B.s);
+	TV* yy = vp<TV>(B.py);
+	rr[i] = r0; rr[np + i] = r1; rr[2 * np + i] = r2;
+	ss[i] = s0; ss[np + i] = s1; ss[2 * np + i] = s2;
+	dd[i] = s0; dd[np + i] = s1; dd[2 * np + i] = s2;
+	yy[i] = 0; yy[np + i] = 0; yy[2 * np + i] = 0;
+	return (double)r0 * (double)s0 + (double)r1 * (double)s1 + (double)r2 * (double)s2;
+}
+
+// q_i = (A x)_i for row i over a SELL-32 slice; TA = block storage, TV = vector type.
+template <class TA, class TV>
+__device__ __forceinline__ void spmv_row(const TA* __restrict__ A, const int* __restrict__ col,
+                                         const uint8_t* __restrict__ rowlen, int nslots, int base, int w,
+                                         int lane, int i, const TV* __restrict__ x, int np, TV out[3])
+{
+	typedef typename Acc<TA>::type AT;
+	AT o0 = 0, o1 = 0, o2 = 0;
+	const int len = rowlen[i];
+#pragma unroll 4
+	for (int k = 0; k < w; ++k)
+	{
+		if (k >= len) break;
+		const int slot = base + k * kSlice + lane;
+		const int j = __ldg(col + slot);
+		AT x0 = (AT)x[j], x1 = (AT)x[np + j], x2 = (AT)x[2 * np + j];
+		AT a0 = widen(A[slot]), a1 = widen(A[(size_t)nslots + slot]), a2 = widen(A[2 * (size_t)nslots + slot]);
+		AT a3 = widen(A[3 * (size_t)nslots + slot]), a4 = widen(A[4 * (size_t)nslots + slot]), a5 = widen(A[5 * (size_t)nslots + slot]);
+		AT a6 = widen(A[6 * (size_t)nslots + slot]), a7 = widen(A[7 * (size_t)nslots + slot]), a8 = widen(A[8 * (size_t)nslots + slot]);
+		o0 += a0 * x0 + a1 * x1 + a2 * x2;
+		o1 += a3 * x0 + a4 * x1 + a5 * x2;
+		o2 += a6 * x0 + a7 * x1 + a8 * x2;
+	}
+	out[0] = (TV)o0;
+	out[1] = (TV)o1;
+	out[2] = (TV)o2;
+}
+
+// M^-1 r for one row (scalar or block Jacobi)
+template <class TV>
+__device__ __forceinline__ void precond_row(const DevBody& B, int i, const TV r[3], TV s[3])
+{
+	const TV* M = (const TV*)B.Minv;
+	const int np = B.npad;
+	if (B.precond == B3G_PRECOND_BLOCK_JACOBI)
+	{
+#pragma unroll
+		for (int a = 0; a < 3; ++a)
+			s[a] = M[(size_t)(3 * a) * np + i] * r[0] + M[(size_t)(3 * a + 1) * np + i] * r[1] + M[(size_t)(3 * a + 2) * np + i] * r[2];
+	}
+	else
+	{
+		s[0] = M[i] * r[0];
+		s[1] = M[np + i] * r[1];
+		s[2] = M[2 * np + i] * r[2];
+	}
+}
+
+// ------------------------------------------------------------------ reductions
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+} // namespace b3g

@@ -1,0 +1,179 @@
+// Internal layout of a body on the device, shared by the host builder (pattern.cpp), the
+// kernels (kernels.cu, persistent.cu) and the C ABI (api.cu).
+//
+// Matrix storage: sliced block-ELL with 32 rows per slice ("SELL-32", one warp per slice, one
+// lane per block row). Slice s owns slots [slice_ptr[s], slice_ptr[s+1]) = width_s * 32 slots;
+// the k-th block of row i = 32 s + lane sits in slot slice_ptr[s] + 32 k + lane. The 3x3 block
+// values live in 9 planes (plane p holds entry p = 3 * row + col of every slot), so a warp reads
+// 32 consecutive values per plane per k: fully coalesced, no reduction across lanes, no padding
+// bytes read (rowlen predicates the tail). The diagonal block is always slot k = 0 of its row.
+//
+// Solver vectors are planar too: component c of vertex i at c * npad + i (npad = 32 * nslices).
+// Vertex state (x, v, external force, translation) stays 3 floats per vertex, like b3Vec3 arrays.
+#pragma once
+
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/b3g.h"
+
+#include <vector_types.h>
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#define B3G_HD __host__ __device__ __forceinline__
+#else
+#define B3G_HD inline
+#endif
+
+namespace b3g {
+
+constexpr int kSlice = 32;
+constexpr int kMaxWorld = 4;
+constexpr int kMaxTeamCtas = 16;
+
+// Device-resident solver scalars of one body; everything the PCG decides is taken here.
+struct Scalars
+{
+	double delta;      // r.s of the current residual
+	double delta0;     // r0.s0
+	double dq;         // d.q
+	double alpha, beta;
+	double tol2;       // pcg_tolerance^2
+	double newton_err, newton_err0;
+	double newton_tol2;
+	int iter;          // PCG iteration of the current solve
+	int max_iter;
+	int done;          // current PCG solve finished
+	int status;        // b3g_solve_status
+	int newton_iter;
+	int newton_done;
+	int min_it, max_it;
+	int refresh;       // refresh period
+	unsigned counter;  // arrival counter of the deterministic grid reduction (plain path)
+	int pending_check; // bf16 mode: recursive residual met the tolerance, confirm with a refresh
+	int pad;
+};
+
+// Everything a kernel needs about one body. Passed by value to the per-op kernels and read
+// from a device array by the persistent batch kernel.
+struct DevBody
+{
+	int n, nslices, npad, nslots;
+	int nt, ntr, ns, nw;
+	int maxw;                   // widest slice
+	int contacts;               // per-vertex contact spheres present
+
+	// matrix structure
+	const int* slice_ptr;       // nslices + 1
+	const int* col;             // nslots
+	const uint8_t* rowlen;      // npad (0 for padding rows)
+	float* A32;                 // 9 * nslots
+	void* Alo;                  // 9 * nslots of the precision's storage type (double / bf16), or null
+	void* Minv;                 // 3 * npad (scalar Jacobi) or 9 * npad (block Jacobi), vector type
+
+	// contribution lists, in slot order and element order (deterministic)
+	const uint32_t* tet_cptr;   // nslots + 1
+	const uint32_t* tet_clist;  // e << 4 | a << 2 | b
+	const uint32_t* blk_cptr;   // nslots + 1
+	const uint32_t* blk_clist;  // block index << 1 | negate
+	const uint32_t* vt_ptr;     // n + 1
+	const uint32_t* vt_list;    // 4 e + a
+	const uint32_t* vb_ptr;     // n + 1
+	const uint32_t* vb_list;    // vector index << 1 | negate
+
+	// vertex state
+	float* x;
+	float* v;
+	float* fext;
+	float* trans;
+	float* xi;                  // Newton iterate (force_iterations > 1)
+	float* vi;
+	const float* mass;
+	const float* invmass;
+	const float* damping;
+	const int8_t* type;
+
+	// tetrahedra
+	const uint4* tet;
+	const float* tet_invE;      // 9 per tet, column-major like b3Mat33
+	const float4* tet_mat;      // volume, lambda, mu, stiffness damping
+	float4* tet_q;              // rotation quaternion (x, y, z, w)
+	float4* tet_rec;            // 4 float4 per tet: (sqrt(c mu) R g_a, lambda / mu), c = (h^2 + h kd) V
+	float* tet_bc;              // 12 per tet: h * (f + dfdx w) per local vertex
+
+	// triangles
+	const uint4* tri;           // 3 ids + pad
+	const float* tri_x;         // 6 per tri: rest 2-D coordinates
+	const float* tri_invS;      // 4 per tri (column-major 2x2)
+	const float* tri_K;         // 36 per tri: 9 blocks of 2x2, block (a, b) at 4 (a + 3 b)
+	const float* tri_kd;
+
+	// springs
+	const uint2* spr;
+	const float* spr_L0;
+	const float* spr_ks;
+	const float* spr_kd;
+
+	// explicit (non-tetrahedral) contributions
+	float* blocks;              // 9 per block: tri (a, b) at 9 e + 3 a + b, spring at 9 Tr + s
+	float* bvec;                // 3 per vector: tri (a) at 3 e + a, spring at 3 Tr + s
+
+	// contacts
+	const float* srad;
+	const float* sfric;
+	float4 world[kMaxWorld];    // centre, radius
+	float wfric[kMaxWorld];
+	uint8_t* c_exists;          // n * nw
+	uint8_t* c_apply;
+	float* c_nf;                // accumulated normal force
+	float* c_normal;            // 3 per contact
+
+	// solver vectors (vector type), planar
+	void* pb;
+	void* r;
+	void* d;
+	void* d2;                   // second direction buffer (persistent kernel ping-pong)
+	void* q;
+	void* s;
+	void* py;
+
+	float gravity[3];
+
+	Scalars* sc;
+	double* partials;           // reduction scratch of the per-op kernels (kMaxPartials)
+	double* team_partials;      // reduction scratch of the grid team (persistent kernel)
+	int precond;                // b3g_preconditioner
+	int pad_;
+};
+
+constexpr int kMaxPartials = 4096;
+
+// Host-side result of the pattern builder (pattern.cpp).
+struct Pattern
+{
+	int n = 0, nslices = 0, npad = 0, nslots = 0, maxw = 0;
+	uint64_t nnzb = 0;
+	int* slice_ptr = nullptr;
+	int* col = nullptr;
+	uint8_t* rowlen = nullptr;
+	uint32_t* tet_cptr = nullptr;
+	uint32_t* tet_clist = nullptr;
+	uint64_t tet_ccount = 0;
+	uint32_t* blk_cptr = nullptr;
+	uint32_t* blk_clist = nullptr;
+	uint64_t blk_ccount = 0;
+	uint32_t* vt_ptr = nullptr;
+	uint32_t* vt_list = nullptr;
+	uint32_t* vb_ptr = nullptr;
+	uint32_t* vb_list = nullptr;
+};
+
+// Builds the SELL-32 pattern and every contribution list. Returns false with a message on a
+// malformed mesh (vertex index out of range, degenerate element).
+bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, const uint32_t* tris,
+                   uint32_t ns, const uint32_t* springs, Pattern* out, char* err, size_t errlen);
+void free_pattern(Pattern* p);
+
+} // namespace b3g

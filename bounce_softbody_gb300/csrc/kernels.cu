@@ -1,0 +1,643 @@
+// Per-op kernels of the single-body ("plain") path: one kernel per phase, grid-wide
+// deterministic reductions (per-CTA partials summed in a fixed order by the last CTA to
+// arrive), solver decisions taken on the device in Scalars.
+#include "device.cuh"
+#include "ops.h"
+
+namespace b3g {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+
+int grid_for(int items, int per_block)
+{
+	int g = (items + per_block - 1) / per_block;
+	if (g < 1) g = 1;
+	if (g > kMaxPartials) g = kMaxPartials;
+	return g;
+}
+
+// Sum `v` over the whole grid. Returns true in thread 0 of the last CTA to arrive, with the
+// total in *total; the partials are summed in CTA order, so the result does not depend on
+// arrival order.
+__device__ bool grid_reduce(double v, double* partials, unsigned* counter, double* total)
+{
+	__shared__ double sh[32];
+	__shared__ int last;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	v = warp_sum(v);
+	if (lane == 0) sh[warp] = v;
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		double s = 0.0;
+		for (int k = 0; k < nw; ++k) s += sh[k];
+		partials[blockIdx.x] = s;
+		__threadfence();
+		unsigned prev = atomicAdd(counter, 1u);
+		last = (prev == gridDim.x - 1) ? 1 : 0;
+	}
+	__syncthreads();
+	if (!last) return false;
+	__threadfence();
+	double s = 0.0;
+	for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) s += ((volatile double*)partials)[k];
+	s = warp_sum(s);
+	__syncthreads();
+	if (lane == 0) sh[warp] = s;
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		double t = 0.0;
+		for (int k = 0; k < nw; ++k) t += sh[k];
+		*total = t;
+		*counter = 0u;
+	}
+	return threadIdx.x == 0;
+}
+
+__device__ __forceinline__ bool finite_d(double x) { return isfinite(x); }
+
+// PCG exit test at the top of the reference loop (sparse_solver.cpp:65-73), taken after the
+// iteration counter moved.
+__device__ void decide_after_reduction(Scalars* sc, double delta_new, bool bf16_mode, bool was_refresh)
+{
+	double delta_old = sc->delta;
+	sc->delta = delta_new;
+	sc->beta = delta_new / delta_old;
+	sc->iter += 1;
+	if (!finite_d(delta_new))
+	{
+		sc->status = B3G_SOLVE_NONFINITE;
+		sc->done = 1;
+		return;
+	}
+	bool conv = delta_new <= sc->tol2 * sc->delta0;
+	if (bf16_mode && conv && !was_refresh)
+	{
+		// the recursive residual of the bf16 iteration drifts from the true one: confirm with a
+		// true-residual refresh on the next iteration before stopping
+		sc->pending_check = 1;
+		conv = false;
+	}
+	if (conv)
+	{
+		sc->status = B3G_SOLVE_CONVERGED;
+		sc->done = 1;
+	}
+	else if (sc->iter >= sc->max_iter)
+	{
+		sc->status = B3G_SOLVE_MAX_ITERATIONS;
+		sc->done = 1;
+	}
+	if (was_refresh) sc->pending_check = 0;
+}
+
+__device__ __forceinline__ bool refresh_now(const Scalars* sc)
+{
+	return (sc->refresh > 0 && (sc->iter % sc->refresh) == 0) || sc->pending_check;
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void k_begin(Scalars* sc, int max_it, double tol2, int refresh, double newton_tol2)
+{
+	sc->iter = 0;
+	sc->max_iter = max_it;
+	sc->done = 0;
+	sc->status = B3G_SOLVE_CONVERGED;
+	sc->tol2 = tol2;
+	sc->refresh = refresh;
+	sc->newton_iter = 0;
+	sc->newton_done = 0;
+	sc->newton_tol2 = newton_tol2;
+	sc->newton_err = 0.0;
+	sc->newton_err0 = 0.0;
+	sc->min_it = 0x7fffffff;
+	sc->max_it = 0;
+	sc->counter = 0u;
+	sc->pending_check = 0;
+	sc->delta = sc->delta0 = 0.0;
+	sc->alpha = sc->beta = sc->dq = 0.0;
+}
+
+__global__ void k_newton_begin(Scalars* sc)
+{
+	sc->iter = 0;
+	sc->done = 0;
+	sc->pending_check = 0;
+	sc->status = B3G_SOLVE_CONVERGED;
+}
+
+__global__ void __launch_bounds__(kThreads) k_tets(DevBody B, StepParams P)
+{
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B.nt; e += gridDim.x * blockDim.x) tet_element(B, e, P);
+}
+
+__global__ void __launch_bounds__(kThreads) k_tris(DevBody B, StepParams P)
+{
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B.ntr; e += gridDim.x * blockDim.x) tri_element(B, e, P);
+}
+
+__global__ void __launch_bounds__(kThreads) k_springs(DevBody B, StepParams P)
+{
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B.ns; e += gridDim.x * blockDim.x) spring_element(B, e, P);
+}
+
+__device__ void pcg_start(Scalars* sc, double delta0)
+{
+	sc->delta = delta0;
+	sc->delta0 = delta0;
+	sc->iter = 0;
+	sc->pending_check = 0;
+	if (!finite_d(delta0))
+	{
+		sc->status = B3G_SOLVE_NONFINITE;
+		sc->done = 1;
+	}
+	else if (delta0 <= sc->tol2 * delta0)
+	{
+		sc->status = B3G_SOLVE_CONVERGED;
+		sc->done = 1;
+	}
+	else if (sc->max_iter <= 0)
+	{
+		sc->status = B3G_SOLVE_MAX_ITERATIONS;
+		sc->done = 1;
+	}
+	else
+		sc->done = 0;
+}
+
+template <class TA, class TV>
+__global__ void __launch_bounds__(kThreads) k_assemble(DevBody B, StepParams P, int init)
+{
+	const int lane = threadIdx.x & 31;
+	double part = 0.0;
+	for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < B.nslices; s += (gridDim.x * blockDim.x) >> 5)
+		part += assemble_row<TA, TV>(B, s, lane, P, init != 0);
+	if (!init) return;
+	double total;
+	if (grid_reduce(part, B.partials, &B.sc->counter, &total)) pcg_start(B.sc, total);
+}
+
+// r = pb - A py, s = M^-1 r, d = s (warm start from the previous Newton iteration's solution)
+template <class TA, class TV>
+__global__ void __launch_bounds__(kThreads) k_pcg_init(DevBody B, const TA* A)
+{
+	const int lane = threadIdx.x & 31;
+	const int np = B.npad;
+	double part = 0.0;
+	const TV* py = (const TV*)B.py;
+	TV* pb = (TV*)B.pb;
+	TV* r = (TV*)B.r;
+	TV* s = (TV*)B.s;
+	TV* d = (TV*)B.d;
+	for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < B.nslices; sl += (gridDim.x * blockDim.x) >> 5)
+	{
+		int i = sl * kSlice + lane;
+		if (i >= B.n) continue;
+		int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
+		TV q[3];
+		spmv_row<TA, TV>(A, B.col, B.rowlen, B.nslots, base, w, lane, i, py, np, q);
+		TV rr[3] = {pb[i] - q[0], pb[np + i] - q[1], pb[2 * np + i] - q[2]};
+		TV ss[3];
+		precond_row<TV>(B, i, rr, ss);
+#pragma unroll
+		for (int c = 0; c < 3; ++c)
+		{
+			r[c * np + i] = rr[c];
+			s[c * np + i] = ss[c];
+			d[c * np + i] = ss[c];
+			part += (double)rr[c] * (double)ss[c];
+		}
+	}
+	double total;
+	if (grid_reduce(part, B.partials, &B.sc->counter, &total)) pcg_start(B.sc, total);
+}
+
+// q = A d and alpha = delta / d.q
+template <class TA, class TV>
+__global__ void __launch_bounds__(kThreads) k_spmv_dot(DevBody B, const TA* A)
+{
+	if (B.sc->done) return;
+	const int lane = threadIdx.x & 31;
+	const int np = B.npad;
+	const TV* d = (const TV*)B.d;
+	TV* q = (TV*)B.q;
+	double part = 0.0;
+	for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < B.nslices; sl += (gridDim.x * blockDim.x) >> 5)
+	{
+		int i = sl * kSlice + lane;
+		if (i >= B.n) continue;
+		int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
+		TV o[3];
+		spmv_row<TA, TV>(A, B.col, B.rowlen, B.nslots, base, w, lane, i, d, np, o);
+#pragma unroll
+		for (int c = 0; c < 3; ++c)
+		{
+			q[c * np + i] = o[c];
+			part += (double)d[c * np + i] * (double)o[c];
+		}
+	}
+	double total;
+	if (grid_reduce(part, B.partials, &B.sc->counter, &total))
+	{
+		Scalars* sc = B.sc;
+		sc->dq = total;
+		if (!finite_d(total))
+		{
+			sc->status = B3G_SOLVE_NONFINITE;
+			sc->done = 1;
+		}
+		else if (!(total > 0.0))
+		{
+			sc->status = B3G_SOLVE_BREAKDOWN;
+			sc->done = 1;
+		}
+		else
+			sc->alpha = sc->delta / total;
+	}
+}
+
+// x += alpha d; unless this is a refresh iteration: r -= alpha q, s = M^-1 r, delta = r.s
+template <class TV>
+__global__ void __launch_bounds__(kThreads) k_update(DevBody B, int bf16_mode)
+{
+	Scalars* sc = B.sc;
+	if (sc->done) return;
+	const bool refresh = refresh_now(sc);
+	const int np = B.npad;
+	const TV alpha = (TV)sc->alpha;
+	TV* x = (TV*)B.py;
+	const TV* d = (const TV*)B.d;
+	const TV* q = (const TV*)B.q;
+	TV* r = (TV*)B.r;
+	TV* s = (TV*)B.s;
+	double part = 0.0;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
+	{
+#pragma unroll
+		for (int c = 0; c < 3; ++c) x[c * np + i] += alpha * d[c * np + i];
+		if (refresh) continue;
+		TV rr[3], ss[3];
+#pragma unroll
+		for (int c = 0; c < 3; ++c)
+		{
+			rr[c] = r[c * np + i] - alpha * q[c * np + i];
+			r[c * np + i] = rr[c];
+		}
+		precond_row<TV>(B, i, rr, ss);
+#pragma unroll
+		for (int c = 0; c < 3; ++c)
+		{
+			s[c * np + i] = ss[c];
+			part += (double)rr[c] * (double)ss[c];
+		}
+	}
+	if (refresh) return;
+	double total;
+	if (grid_reduce(part, B.partials, &sc->counter, &total)) decide_after_reduction(sc, total, bf16_mode != 0, false);
+}
+
+// refresh iteration: r = b - A x (sparse_solver.cpp:83-90), s = M^-1 r, delta = r.s
+template <class TA, class TV>
+__global__ void __launch_bounds__(kThreads) k_resid(DevBody B, const TA* A, int bf16_mode)
+{
+	Scalars* sc = B.sc;
+	if (sc->done) return;
+	if (!refresh_now(sc)) return;
+	const int lane = threadIdx.x & 31;
+	const int np = B.npad;
+	const TV* py = (const TV*)B.py;
+	const TV* pb = (const TV*)B.pb;
+	TV* r = (TV*)B.r;
+	TV* s = (TV*)B.s;
+	double part = 0.0;
+	for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < B.nslices; sl += (gridDim.x * blockDim.x) >> 5)
+	{
+		int i = sl * kSlice + lane;
+		if (i >= B.n) continue;
+		int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
+		TV q[3];
+		spmv_row<TA, TV>(A, B.col, B.rowlen, B.nslots, base, w, lane, i, py, np, q);
+		TV rr[3] = {pb[i] - q[0], pb[np + i] - q[1], pb[2 * np + i] - q[2]};
+		TV ss[3];
+		precond_row<TV>(B, i, rr, ss);
+#pragma unroll
+		for (int c = 0; c < 3; ++c)
+		{
+			r[c * np + i] = rr[c];
+			s[c * np + i] = ss[c];
+			part += (double)rr[c] * (double)ss[c];
+		}
+	}
+	double total;
+	if (grid_reduce(part, B.partials, &sc->counter, &total)) decide_after_reduction(sc, total, bf16_mode != 0, true);
+}
+
+// d = s + beta d
+template <class TV>
+__global__ void __launch_bounds__(kThreads) k_direction(DevBody B)
+{
+	Scalars* sc = B.sc;
+	if (sc->done) return;
+	const int np = B.npad;
+	const TV beta = (TV)sc->beta;
+	TV* d = (TV*)B.d;
+	const TV* s = (const TV*)B.s;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
+	{
+#pragma unroll
+		for (int c = 0; c < 3; ++c) d[c * np + i] = s[c * np + i] + beta * d[c * np + i];
+	}
+}
+
+// sphere_shape_contact.cpp:145-189 ApplyFriction for vertex i (velocity only)
+__device__ void apply_friction(const DevBody& B, int i, float h, float3& v)
+{
+	for (int k = 0; k < B.nw; ++k)
+	{
+		const int c = i * B.nw + k;
+		if (!B.c_exists[c] || !B.c_apply[c]) continue;
+		float3 normal = ld3(B.c_normal, c);
+		float nf = B.c_nf[c];
+		// vec3.h:255 b3Perp
+		const float sqrt_inv3 = sqrtf(1.0f / 3.0f);
+		float3 t1 = fabsf(normal.x) >= sqrt_inv3 ? f3(normal.y, -normal.x, 0.0f) : f3(0.0f, normal.z, -normal.y);
+		t1 = normalize3(t1);
+		float3 t2 = cross3(t1, normal);
+		float im1 = B.invmass[i];
+		float fr = sqrtf(B.sfric[i] * B.wfric[k]);
+		float tm = im1 > 0.0f ? 1.0f / im1 : 0.0f;
+		float cx = dot3(v, t1), cy = dot3(v, t2);
+		float ix = tm * -cx, iy = tm * -cy;
+		float maxImp = fr * (h * nf);
+		if (ix * ix + iy * iy > maxImp * maxImp)
+		{
+			float l = sqrtf(ix * ix + iy * iy);
+			if (l > kFltEps)
+			{
+				ix /= l;
+				iy /= l;
+			}
+			ix *= maxImp;
+			iy *= maxImp;
+		}
+		float3 Pimp = ix * t1 + iy * t2;
+		v = v + im1 * Pimp;
+	}
+}
+
+// contact_manager.cpp:65-82 FindNewContacts for vertex i at its new position
+__device__ void find_new_contacts(const DevBody& B, int i, float3 x)
+{
+	if (B.type[i] != B3G_DYNAMIC) return;
+	for (int k = 0; k < B.nw; ++k)
+	{
+		const int c = i * B.nw + k;
+		if (B.c_exists[c]) continue;
+		if (aabb_overlap(x, B.srad[i], B.world[k]))
+		{
+			B.c_exists[c] = 1;
+			B.c_nf[c] = 0.0f;
+			B.c_apply[c] = 0;
+		}
+	}
+}
+
+// v = v + dv, x = x0 + h v + y, Newton error |dv|^2 (sparse_force_solver.cpp:194-223).
+// mode 1 also finishes the step: friction, clearing of external forces and translations,
+// new contacts (body.cpp:572-603).
+template <class TV>
+__global__ void __launch_bounds__(kThreads) k_final(DevBody B, StepParams P, int mode)
+{
+	const int np = B.npad;
+	const TV* py = (const TV*)B.py;
+	const float h = P.h;
+	const float* Vit = P.first_newton ? B.v : B.vi;
+	float* vout = mode == 1 ? B.v : B.vi;
+	float* xout = mode == 1 ? B.x : B.xi;
+	double part = 0.0;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
+	{
+		float3 dv = f3((float)py[i], (float)py[np + i], (float)py[2 * np + i]);
+		float3 v = ld3(Vit, i) + dv;
+		float3 x = ld3(B.x, i) + h * v + ld3(B.trans, i);
+		part += (double)dv.x * dv.x + (double)dv.y * dv.y + (double)dv.z * dv.z;
+		if (mode == 1)
+		{
+			if (B.contacts) apply_friction(B, i, h, v);
+			st3(B.fext, i, f3(0, 0, 0));
+			st3(B.trans, i, f3(0, 0, 0));
+			if (B.contacts) find_new_contacts(B, i, x);
+		}
+		st3(xout, i, x);
+		st3(vout, i, v);
+	}
+	double total;
+	if (grid_reduce(part, B.partials, &B.sc->counter, &total))
+	{
+		Scalars* sc = B.sc;
+		sc->newton_err = total;
+		if (sc->newton_iter == 0) sc->newton_err0 = total;
+		int it = sc->iter;
+		sc->min_it = it < sc->min_it ? it : sc->min_it;
+		sc->max_it = it > sc->max_it ? it : sc->max_it;
+		// sparse_force_solver.cpp:205-223
+		if (sc->newton_iter == 0) sc->newton_done = total <= sc->newton_tol2 ? 1 : 0;
+		else sc->newton_done = total <= sc->newton_tol2 * sc->newton_err0 ? 1 : 0;
+		sc->newton_iter += 1;
+	}
+}
+
+__global__ void __launch_bounds__(kThreads) k_post(DevBody B, float h)
+{
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
+	{
+		float3 v = ld3(B.vi, i);
+		float3 x = ld3(B.xi, i);
+		if (B.contacts) apply_friction(B, i, h, v);
+		st3(B.fext, i, f3(0, 0, 0));
+		st3(B.trans, i, f3(0, 0, 0));
+		if (B.contacts) find_new_contacts(B, i, x);
+		st3(B.x, i, x);
+		st3(B.v, i, v);
+	}
+}
+
+__global__ void __launch_bounds__(kThreads) k_nostep(DevBody B)
+{
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
+	{
+		float3 x = ld3(B.x, i);
+		if (B.contacts)
+			for (int k = 0; k < B.nw; ++k)
+			{
+				const int c = i * B.nw + k;
+				if (B.c_exists[c] && (B.type[i] != B3G_DYNAMIC || !aabb_overlap(x, B.srad[i], B.world[k]))) B.c_exists[c] = 0;
+				else if (B.c_exists[c])
+				{
+					B.c_nf[c] = 0.0f;
+					B.c_apply[c] = 0;
+				}
+			}
+		st3(B.fext, i, f3(0, 0, 0));
+		st3(B.trans, i, f3(0, 0, 0));
+		if (B.contacts) find_new_contacts(B, i, x);
+	}
+}
+
+__global__ void k_accumulate(float* dst, const float* src, size_t n)
+{
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] += src[i];
+}
+
+// b3Particle::SetType (particle.cpp:58-87) for every vertex whose type changes: external force
+// and translation cleared, velocity zeroed for static vertices, contacts destroyed.
+__global__ void k_set_types(DevBody B, const int8_t* nt)
+{
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
+	{
+		int8_t t = nt[i];
+		if (t == B.type[i]) continue;
+		st3(B.fext, i, f3(0, 0, 0));
+		st3(B.trans, i, f3(0, 0, 0));
+		if (t == B3G_STATIC) st3(B.v, i, f3(0, 0, 0));
+		for (int k = 0; k < B.nw; ++k) B.c_exists[i * B.nw + k] = 0;
+		((int8_t*)B.type)[i] = t;
+	}
+}
+
+__global__ void k_fill(float* p, size_t n, float v)
+{
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+StepParams dev_params(const StepParamsHost& P)
+{
+	StepParams p;
+	p.h = P.h;
+	p.first_newton = P.first_newton;
+	return p;
+}
+
+int slice_grid(const DevBody& B) { return grid_for(B.nslices, kWarps); }
+int vertex_grid(const DevBody& B) { return grid_for(B.n, kThreads); }
+
+} // namespace
+
+cudaError_t op_begin(const DevBody& B, cudaStream_t st, int max_it, double tol2, int refresh, double newton_tol2)
+{
+	k_begin<<<1, 1, 0, st>>>(B.sc, max_it, tol2, refresh, newton_tol2);
+	return cudaGetLastError();
+}
+
+cudaError_t op_newton_begin(const DevBody& B, cudaStream_t st)
+{
+	k_newton_begin<<<1, 1, 0, st>>>(B.sc);
+	return cudaGetLastError();
+}
+
+cudaError_t op_elements(const DevBody& B, const StepParamsHost& Ph, cudaStream_t st)
+{
+	StepParams P = dev_params(Ph);
+	if (B.nt > 0) k_tets<<<grid_for(B.nt, kThreads), kThreads, 0, st>>>(B, P);
+	if (B.ntr > 0) k_tris<<<grid_for(B.ntr, kThreads), kThreads, 0, st>>>(B, P);
+	if (B.ns > 0) k_springs<<<grid_for(B.ns, kThreads), kThreads, 0, st>>>(B, P);
+	return cudaGetLastError();
+}
+
+cudaError_t op_assemble(const DevBody& B, const StepParamsHost& Ph, int prec, bool init, cudaStream_t st)
+{
+	StepParams P = dev_params(Ph);
+	int g = slice_grid(B);
+	if (prec == kP64) k_assemble<double, double><<<g, kThreads, 0, st>>>(B, P, init ? 1 : 0);
+	else if (prec == kPBF) k_assemble<__nv_bfloat16, float><<<g, kThreads, 0, st>>>(B, P, init ? 1 : 0);
+	else k_assemble<float, float><<<g, kThreads, 0, st>>>(B, P, init ? 1 : 0);
+	return cudaGetLastError();
+}
+
+cudaError_t op_pcg_init(const DevBody& B, int prec, cudaStream_t st)
+{
+	int g = slice_grid(B);
+	if (prec == kP64) k_pcg_init<double, double><<<g, kThreads, 0, st>>>(B, (const double*)B.Alo);
+	else k_pcg_init<float, float><<<g, kThreads, 0, st>>>(B, B.A32);
+	return cudaGetLastError();
+}
+
+cudaError_t op_pcg_iteration(const DevBody& B, int prec, cudaStream_t st)
+{
+	int gs = slice_grid(B), gv = vertex_grid(B);
+	if (prec == kP64)
+	{
+		const double* A = (const double*)B.Alo;
+		k_spmv_dot<double, double><<<gs, kThreads, 0, st>>>(B, A);
+		k_update<double><<<gv, kThreads, 0, st>>>(B, 0);
+		k_resid<double, double><<<gs, kThreads, 0, st>>>(B, A, 0);
+		k_direction<double><<<gv, kThreads, 0, st>>>(B);
+	}
+	else if (prec == kPBF)
+	{
+		k_spmv_dot<__nv_bfloat16, float><<<gs, kThreads, 0, st>>>(B, (const __nv_bfloat16*)B.Alo);
+		k_update<float><<<gv, kThreads, 0, st>>>(B, 1);
+		k_resid<float, float><<<gs, kThreads, 0, st>>>(B, B.A32, 1);
+		k_direction<float><<<gv, kThreads, 0, st>>>(B);
+	}
+	else
+	{
+		k_spmv_dot<float, float><<<gs, kThreads, 0, st>>>(B, B.A32);
+		k_update<float><<<gv, kThreads, 0, st>>>(B, 0);
+		k_resid<float, float><<<gs, kThreads, 0, st>>>(B, B.A32, 0);
+		k_direction<float><<<gv, kThreads, 0, st>>>(B);
+	}
+	return cudaGetLastError();
+}
+
+cudaError_t op_final(const DevBody& B, const StepParamsHost& Ph, int prec, int mode, cudaStream_t st)
+{
+	StepParams P = dev_params(Ph);
+	int g = vertex_grid(B);
+	if (prec == kP64) k_final<double><<<g, kThreads, 0, st>>>(B, P, mode);
+	else k_final<float><<<g, kThreads, 0, st>>>(B, P, mode);
+	return cudaGetLastError();
+}
+
+cudaError_t op_post(const DevBody& B, float h, cudaStream_t st)
+{
+	k_post<<<vertex_grid(B), kThreads, 0, st>>>(B, h);
+	return cudaGetLastError();
+}
+
+cudaError_t op_nostep(const DevBody& B, cudaStream_t st)
+{
+	k_nostep<<<vertex_grid(B), kThreads, 0, st>>>(B);
+	return cudaGetLastError();
+}
+
+cudaError_t op_accumulate(float* dst, const float* src, size_t count, cudaStream_t st)
+{
+	if (count == 0) return cudaSuccess;
+	int g = (int)((count + kThreads - 1) / kThreads);
+	if (g > 4096) g = 4096;
+	k_accumulate<<<g, kThreads, 0, st>>>(dst, src, count);
+	return cudaGetLastError();
+}
+
+cudaError_t op_set_types(const DevBody& B, const int8_t* new_types, cudaStream_t st)
+{
+	k_set_types<<<vertex_grid(B), kThreads, 0, st>>>(B, new_types);
+	return cudaGetLastError();
+}
+
+cudaError_t op_fill_f32(float* p, size_t count, float value, cudaStream_t st)
+{
+	if (count == 0) return cudaSuccess;
+	int g = (int)((count + kThreads - 1) / kThreads);
+	if (g > 4096) g = 4096;
+	k_fill<<<g, kThreads, 0, st>>>(p, count, value);
+	return cudaGetLastError();
+}
+
+} // namespace b3g

@@ -1,0 +1,56 @@
+// Host-callable launchers of the per-op kernels (kernels.cu) and of the persistent batch
+// kernel (persistent.cu).
+#pragma once
+
+#include "internal.h"
+
+#include <cuda_runtime.h>
+
+namespace b3g {
+
+// Storage / arithmetic of the PCG: matrix storage type and vector type.
+enum Prec
+{
+	kP32 = 0,   // float blocks, float vectors, double dot products
+	kP64 = 1,   // double blocks and vectors
+	kPBF = 2    // bf16 blocks in the iteration, float blocks for the residual refresh, float vectors
+};
+
+struct StepParamsHost
+{
+	float h;
+	int first_newton;
+};
+
+cudaError_t op_begin(const DevBody& B, cudaStream_t st, int max_it, double tol2, int refresh, double newton_tol2);
+cudaError_t op_newton_begin(const DevBody& B, cudaStream_t st);
+cudaError_t op_elements(const DevBody& B, const StepParamsHost& P, cudaStream_t st);
+cudaError_t op_assemble(const DevBody& B, const StepParamsHost& P, int prec, bool init, cudaStream_t st);
+cudaError_t op_pcg_init(const DevBody& B, int prec, cudaStream_t st);
+cudaError_t op_pcg_iteration(const DevBody& B, int prec, cudaStream_t st);
+// mode 0: write the Newton iterate (xi, vi); mode 1: write the state and finish the step
+cudaError_t op_final(const DevBody& B, const StepParamsHost& P, int prec, int mode, cudaStream_t st);
+// finish a multi-Newton step: iterate -> state, friction, clear, new contacts
+cudaError_t op_post(const DevBody& B, float h, cudaStream_t st);
+// dt <= 0: no solve, only contact bookkeeping and clearing (body.cpp:552-604)
+cudaError_t op_nostep(const DevBody& B, cudaStream_t st);
+// clear a float array on the device
+cudaError_t op_fill_f32(float* p, size_t count, float value, cudaStream_t st);
+
+// Persistent batch kernel: all bodies in `bodies` (device array) step `steps` times.
+struct BatchLaunch
+{
+	const DevBody* bodies;   // device array
+	const int* order;        // device array: body index per work item, grouped by size bucket
+	int count;
+	int steps;
+	float h;
+	int prec;
+	int newton;
+	int cluster;             // CTAs per team (1, 2, 4, 8, 16)
+	int ctas;                // total CTAs of the launch (multiple of cluster)
+};
+
+
+
+} // namespace b3g

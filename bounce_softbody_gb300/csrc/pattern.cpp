@@ -1,0 +1,266 @@
+// Host-side construction of a body's block pattern and of the precomputed scatter maps.
+//
+// The reference accumulates every element block into linked-list rows with a linear search
+// per insertion (include/bounce_softbody/sparse/sparse_mat33.h:268-288). Here the pattern is
+// built once per topology: each row lists its diagonal first, then its other columns in
+// increasing order; every (element, local row a, local column b) contribution is assigned its
+// slot ahead of time and the contributions of a slot are listed in element order. Assembly then
+// gathers per slot in that fixed order, which makes it deterministic (bitwise reproducible)
+// without float atomics.
+#include "internal.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+namespace b3g {
+
+namespace {
+
+struct Inc
+{
+	uint32_t kind;  // 0 tet, 1 tri, 2 spring
+	uint32_t e;
+	uint32_t a;     // local index of the row vertex in the element
+};
+
+template <class T>
+T* dup(const std::vector<T>& v)
+{
+	T* p = (T*)std::malloc(std::max<size_t>(1, v.size()) * sizeof(T));
+	if (!v.empty()) std::memcpy(p, v.data(), v.size() * sizeof(T));
+	return p;
+}
+
+} // namespace
+
+void free_pattern(Pattern* p)
+{
+	std::free(p->slice_ptr);
+	std::free(p->col);
+	std::free(p->rowlen);
+	std::free(p->tet_cptr);
+	std::free(p->tet_clist);
+	std::free(p->blk_cptr);
+	std::free(p->blk_clist);
+	std::free(p->vt_ptr);
+	std::free(p->vt_list);
+	std::free(p->vb_ptr);
+	std::free(p->vb_list);
+	*p = Pattern();
+}
+
+bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, const uint32_t* tris,
+                   uint32_t ns, const uint32_t* springs, Pattern* out, char* err, size_t errlen)
+{
+	*out = Pattern();
+	if (n == 0)
+	{
+		std::snprintf(err, errlen, "body has no vertices");
+		return false;
+	}
+	if ((uint64_t)nt >= (1ull << 28))
+	{
+		std::snprintf(err, errlen, "too many tetrahedra (%u, limit 2^28)", nt);
+		return false;
+	}
+
+	// incidence lists, vertex-major, elements in increasing order per kind
+	std::vector<uint32_t> inc_cnt(n + 1, 0);
+	auto check = [&](uint32_t id, const char* what, uint32_t e) -> bool {
+		if (id >= n)
+		{
+			std::snprintf(err, errlen, "%s %u references vertex %u >= vertex_count %u", what, e, id, n);
+			return false;
+		}
+		return true;
+	};
+	for (uint32_t e = 0; e < nt; ++e)
+		for (int a = 0; a < 4; ++a)
+		{
+			if (!check(tets[4 * e + a], "tetrahedron", e)) return false;
+			for (int b = 0; b < a; ++b)
+				if (tets[4 * e + a] == tets[4 * e + b])
+				{
+					std::snprintf(err, errlen, "tetrahedron %u repeats vertex %u", e, tets[4 * e + a]);
+					return false;
+				}
+			inc_cnt[tets[4 * e + a] + 1]++;
+		}
+	for (uint32_t e = 0; e < ntr; ++e)
+		for (int a = 0; a < 3; ++a)
+		{
+			if (!check(tris[3 * e + a], "triangle", e)) return false;
+			for (int b = 0; b < a; ++b)
+				if (tris[3 * e + a] == tris[3 * e + b])
+				{
+					std::snprintf(err, errlen, "triangle %u repeats vertex %u", e, tris[3 * e + a]);
+					return false;
+				}
+			inc_cnt[tris[3 * e + a] + 1]++;
+		}
+	for (uint32_t e = 0; e < ns; ++e)
+		for (int a = 0; a < 2; ++a)
+		{
+			if (!check(springs[2 * e + a], "spring", e)) return false;
+			inc_cnt[springs[2 * e + a] + 1]++;
+		}
+	for (uint32_t i = 0; i < n; ++i) inc_cnt[i + 1] += inc_cnt[i];
+	std::vector<Inc> inc(inc_cnt[n]);
+	{
+		std::vector<uint32_t> fill(inc_cnt.begin(), inc_cnt.end() - 1);
+		for (uint32_t e = 0; e < nt; ++e)
+			for (uint32_t a = 0; a < 4; ++a) inc[fill[tets[4 * e + a]]++] = Inc{0, e, a};
+		for (uint32_t e = 0; e < ntr; ++e)
+			for (uint32_t a = 0; a < 3; ++a) inc[fill[tris[3 * e + a]]++] = Inc{1, e, a};
+		for (uint32_t e = 0; e < ns; ++e)
+			for (uint32_t a = 0; a < 2; ++a) inc[fill[springs[2 * e + a]]++] = Inc{2, e, a};
+	}
+
+	auto elem_vertex = [&](const Inc& c, uint32_t b) -> uint32_t {
+		if (c.kind == 0) return tets[4 * c.e + b];
+		if (c.kind == 1) return tris[3 * c.e + b];
+		return springs[2 * c.e + b];
+	};
+	auto elem_size = [](uint32_t kind) -> uint32_t { return kind == 0 ? 4u : (kind == 1 ? 3u : 2u); };
+
+	// rows: diagonal first, then the other columns ascending
+	std::vector<uint32_t> rowptr(n + 1, 0);
+	std::vector<uint32_t> cols;
+	cols.reserve((size_t)n * 16);
+	std::vector<uint32_t> tmp;
+	for (uint32_t i = 0; i < n; ++i)
+	{
+		tmp.clear();
+		for (uint32_t k = inc_cnt[i]; k < inc_cnt[i + 1]; ++k)
+			for (uint32_t b = 0; b < elem_size(inc[k].kind); ++b)
+			{
+				uint32_t j = elem_vertex(inc[k], b);
+				if (j != i) tmp.push_back(j);
+			}
+		std::sort(tmp.begin(), tmp.end());
+		tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+		if (tmp.size() + 1 > 255)
+		{
+			std::snprintf(err, errlen, "vertex %u has %zu neighbours (limit 254)", i, tmp.size());
+			return false;
+		}
+		cols.push_back(i);
+		cols.insert(cols.end(), tmp.begin(), tmp.end());
+		rowptr[i + 1] = (uint32_t)cols.size();
+	}
+	auto find_k = [&](uint32_t i, uint32_t j) -> uint32_t {
+		if (j == i) return 0;
+		uint32_t lo = rowptr[i] + 1, hi = rowptr[i + 1];
+		while (lo < hi)
+		{
+			uint32_t mid = (lo + hi) >> 1;
+			if (cols[mid] < j) lo = mid + 1;
+			else hi = mid;
+		}
+		return lo - rowptr[i];
+	};
+
+	// SELL-32 slots
+	Pattern P;
+	P.n = (int)n;
+	P.nslices = (int)((n + kSlice - 1) / kSlice);
+	P.npad = P.nslices * kSlice;
+	P.nnzb = cols.size();
+	std::vector<int> slice_ptr(P.nslices + 1, 0);
+	std::vector<uint8_t> rowlen(P.npad, 0);
+	for (uint32_t i = 0; i < n; ++i) rowlen[i] = (uint8_t)(rowptr[i + 1] - rowptr[i]);
+	for (int s = 0; s < P.nslices; ++s)
+	{
+		int w = 0;
+		for (int l = 0; l < kSlice; ++l) w = std::max(w, (int)rowlen[s * kSlice + l]);
+		P.maxw = std::max(P.maxw, w);
+		slice_ptr[s + 1] = slice_ptr[s] + w * kSlice;
+	}
+	P.nslots = slice_ptr[P.nslices];
+	auto slot_of = [&](uint32_t i, uint32_t k) -> uint32_t {
+		return (uint32_t)slice_ptr[i / kSlice] + k * kSlice + (i % kSlice);
+	};
+	std::vector<int> col(P.nslots, 0);
+	for (int s = 0; s < P.nslices; ++s)
+		for (int l = 0; l < kSlice; ++l)
+		{
+			uint32_t i = (uint32_t)(s * kSlice + l);
+			int w = (slice_ptr[s + 1] - slice_ptr[s]) / kSlice;
+			for (int k = 0; k < w; ++k)
+				col[slice_ptr[s] + k * kSlice + l] = (i < n && (uint32_t)k < rowlen[i]) ? (int)cols[rowptr[i] + k] : (int)std::min<uint32_t>(i, n - 1);
+		}
+
+	// contribution counts per slot
+	std::vector<uint32_t> tcnt(P.nslots + 1, 0), bcnt(P.nslots + 1, 0);
+	for (uint32_t i = 0; i < n; ++i)
+		for (uint32_t k = inc_cnt[i]; k < inc_cnt[i + 1]; ++k)
+		{
+			const Inc& c = inc[k];
+			for (uint32_t b = 0; b < elem_size(c.kind); ++b)
+			{
+				uint32_t slot = slot_of(i, find_k(i, elem_vertex(c, b)));
+				if (c.kind == 0) tcnt[slot + 1]++;
+				else bcnt[slot + 1]++;
+			}
+		}
+	for (int s = 0; s < P.nslots; ++s)
+	{
+		tcnt[s + 1] += tcnt[s];
+		bcnt[s + 1] += bcnt[s];
+	}
+	std::vector<uint32_t> tlist(tcnt[P.nslots]), blist(bcnt[P.nslots]);
+	{
+		std::vector<uint32_t> tf(tcnt.begin(), tcnt.end() - 1), bf(bcnt.begin(), bcnt.end() - 1);
+		// rows in order, incidences in element order: each slot's list comes out sorted by element
+		for (uint32_t i = 0; i < n; ++i)
+			for (uint32_t k = inc_cnt[i]; k < inc_cnt[i + 1]; ++k)
+			{
+				const Inc& c = inc[k];
+				for (uint32_t b = 0; b < elem_size(c.kind); ++b)
+				{
+					uint32_t slot = slot_of(i, find_k(i, elem_vertex(c, b)));
+					if (c.kind == 0) tlist[tf[slot]++] = (c.e << 4) | (c.a << 2) | b;
+					else if (c.kind == 1) blist[bf[slot]++] = ((9u * c.e + 3u * c.a + b) << 1);
+					else blist[bf[slot]++] = ((9u * ntr + c.e) << 1) | (c.a != b ? 1u : 0u);
+				}
+			}
+	}
+
+	// vertex lists of right-hand-side contributions
+	std::vector<uint32_t> vtp(n + 1, 0), vbp(n + 1, 0), vtl, vbl;
+	vtl.reserve(4 * (size_t)nt);
+	vbl.reserve(3 * (size_t)ntr + 2 * (size_t)ns);
+	for (uint32_t i = 0; i < n; ++i)
+	{
+		for (uint32_t k = inc_cnt[i]; k < inc_cnt[i + 1]; ++k)
+		{
+			const Inc& c = inc[k];
+			if (c.kind == 0) vtl.push_back(4u * c.e + c.a);
+			else if (c.kind == 1) vbl.push_back((3u * c.e + c.a) << 1);
+			else vbl.push_back(((3u * ntr + c.e) << 1) | (c.a == 1 ? 1u : 0u));
+		}
+		vtp[i + 1] = (uint32_t)vtl.size();
+		vbp[i + 1] = (uint32_t)vbl.size();
+	}
+
+	P.slice_ptr = dup(slice_ptr);
+	P.col = dup(col);
+	P.rowlen = dup(rowlen);
+	P.tet_cptr = dup(tcnt);
+	P.tet_clist = dup(tlist);
+	P.tet_ccount = tlist.size();
+	P.blk_cptr = dup(bcnt);
+	P.blk_clist = dup(blist);
+	P.blk_ccount = blist.size();
+	P.vt_ptr = dup(vtp);
+	P.vt_list = dup(vtl);
+	P.vb_ptr = dup(vbp);
+	P.vb_list = dup(vbl);
+	*out = P;
+	return true;
+}
+
+} // namespace b3g

@@ -1,0 +1,202 @@
+/*
+ * b3g — GB300-native implicit soft-body step behind a plain C ABI.
+ *
+ * This is the drop-in boundary for the implicit (backward-Euler) step of Bounce Softbody.
+ * Every entry point takes plain pointers and sizes; host pointers unless the name says
+ * "device". All functions return a b3g_status; b3g_last_error() gives the message of the last
+ * failure on the calling thread. Nothing here falls back to the CPU: without a usable GPU the
+ * context cannot be created and every call fails with B3G_ERROR_CUDA.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   b3g_body_create            b3Body::CreateParticle / CreateForce / CreateTetrahedron /
+ *                              CreateTriangle / CreateSphere / CreateFixture and ResetMass
+ *                              (include/bounce_softbody/dynamics/body.h:68-110,
+ *                               src/bounce_softbody/dynamics/body.cpp:62-466)
+ *   b3g_body_step              b3Body::Step(dt, forceIterations, forceSubIterations)
+ *                              (include/bounce_softbody/dynamics/body.h:153,
+ *                               src/bounce_softbody/dynamics/body.cpp:552-604), which runs
+ *                              b3SparseSolveBE (include/bounce_softbody/sparse/sparse_force_solver.h:97)
+ *                              and b3SparseSolveCG (include/bounce_softbody/sparse/sparse_solver.h:47)
+ *   b3g_step_batch             no single counterpart: many independent b3Body::Step calls
+ *   b3g_body_get_state /       b3Particle::GetPosition / GetVelocity / SetPosition / SetVelocity
+ *   b3g_body_set_state         (include/bounce_softbody/dynamics/particle.h:75-90)
+ *   b3g_body_apply_forces      b3Particle::ApplyForce (particle.h:96)
+ *   b3g_body_apply_translations b3Particle::ApplyTranslation (particle.h:104)
+ *   b3g_body_set_types         b3Particle::SetType (particle.h:72, src/bounce_softbody/dynamics/particle.cpp:58-87)
+ *   b3g_body_get_rotations     b3TetrahedronElementForce::m_q, the warm-started element rotation
+ *                              (include/bounce_softbody/dynamics/forces/tetrahedron_element_force.h:154)
+ *   b3g_body_get_stats         b3_forceSolverIterations / Min / MaxSubIterations
+ *                              (src/bounce_softbody/dynamics/force_solver.cpp:29-34)
+ */
+#ifndef B3G_H
+#define B3G_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define B3G_API __attribute__((visibility("default")))
+#else
+#define B3G_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct b3g_context b3g_context;
+typedef struct b3g_body b3g_body;
+
+typedef enum b3g_status
+{
+	B3G_OK = 0,
+	B3G_ERROR_INVALID_ARGUMENT = 1,
+	B3G_ERROR_CUDA = 2,
+	B3G_ERROR_OUT_OF_MEMORY = 3,
+	B3G_ERROR_UNSUPPORTED = 4
+} b3g_status;
+
+/* How the last PCG solve of a step ended (the reference has no such report:
+ * b3SparseSolveCG always returns true, src/bounce_softbody/sparse/sparse_solver.cpp:108). */
+typedef enum b3g_solve_status
+{
+	B3G_SOLVE_CONVERGED = 0,      /* delta <= tol^2 * delta0 */
+	B3G_SOLVE_MAX_ITERATIONS = 1, /* stopped at the iteration cap (the reference's usual exit) */
+	B3G_SOLVE_NONFINITE = 2,      /* a reduction produced NaN or Inf; state left unchanged */
+	B3G_SOLVE_BREAKDOWN = 3       /* d.Ad <= 0: the filtered system is not positive definite */
+} b3g_solve_status;
+
+/* b3ParticleType (include/bounce_softbody/dynamics/particle.h:31-36). */
+enum { B3G_STATIC = 0, B3G_KINEMATIC = 1, B3G_DYNAMIC = 2 };
+
+typedef enum b3g_precision
+{
+	B3G_PRECISION_FP32 = 0,        /* FP32 blocks and vectors, FP64 dot products for alpha/beta */
+	B3G_PRECISION_FP64 = 1,        /* everything in FP64 */
+	B3G_PRECISION_BF16_BLOCKS = 2  /* BF16 matrix blocks, FP32 accumulation, FP32 outer refinement */
+} b3g_precision;
+
+typedef enum b3g_preconditioner
+{
+	B3G_PRECOND_JACOBI = 0,        /* the reference's scalar Jacobi (sparse_solver.cpp:38-55) */
+	B3G_PRECOND_BLOCK_JACOBI = 1   /* inverse of each 3x3 diagonal block */
+} b3g_preconditioner;
+
+/* One body. Arrays are host memory, read once by b3g_body_create. Per-element material arrays
+ * hold one value per element. Vertex ids index the arrays of this body. */
+typedef struct b3g_body_desc
+{
+	uint32_t vertex_count;
+	const float* positions;        /* 3 per vertex, also the rest state when *_rest is NULL */
+	const float* velocities;       /* 3 per vertex, NULL = zero */
+	const int32_t* types;          /* B3G_STATIC / B3G_KINEMATIC / B3G_DYNAMIC */
+	const float* damping;          /* mass damping per vertex, NULL = zero (b3ParticleDef::damping) */
+	const float* masses;           /* NULL = lumped from fixture densities as b3Body::ResetMass does */
+
+	uint32_t tet_count;
+	const uint32_t* tets;          /* 4 vertex ids per tetrahedron */
+	const float* tet_rest;         /* 12 per tetrahedron, NULL = positions */
+	const float* tet_young;        /* b3TetrahedronElementForceDef::youngModulus */
+	const float* tet_poisson;      /* ::poissonRatio */
+	const float* tet_stiffness_damping; /* ::stiffnessDamping, NULL = zero */
+	const float* tet_density;      /* b3TetrahedronFixtureDef::density, NULL = zero */
+
+	uint32_t tri_count;
+	const uint32_t* tris;          /* 3 vertex ids per triangle */
+	const float* tri_rest;         /* 9 per triangle, NULL = positions */
+	const float* tri_young_x;      /* b3TriangleElementForceDef::youngModulusX */
+	const float* tri_young_y;      /* ::youngModulusY */
+	const float* tri_shear;        /* ::shearModulus */
+	const float* tri_poisson_xy;   /* ::poissonRationXY */
+	const float* tri_poisson_yx;   /* ::poissonRationYX */
+	const float* tri_stiffness_damping; /* NULL = zero */
+	const float* tri_density;      /* b3TriangleFixtureDef::density, NULL = zero */
+
+	uint32_t spring_count;
+	const uint32_t* springs;       /* 2 vertex ids per spring */
+	const float* spring_rest_length; /* b3SpringForceDef::length */
+	const float* spring_stiffness;   /* ::stiffness */
+	const float* spring_damping;     /* ::dampingStiffness */
+
+	const float* sphere_radius;    /* per-vertex b3SphereFixture radius, NULL = no contacts */
+	const float* sphere_friction;  /* per-vertex friction */
+	uint32_t world_sphere_count;   /* static b3SphereShape world fixtures (at most 4) */
+	const float* world_spheres;    /* 5 per shape: center x, y, z, radius, friction */
+
+	float gravity[3];              /* b3Body::SetGravity */
+} b3g_body_desc;
+
+/* Solver settings of one step. b3g_solver_config_default() gives the reference's: one Newton
+ * iteration, FLT_EPSILON tolerances, true-residual refresh every 50 PCG iterations, scalar
+ * Jacobi, FP32. */
+typedef struct b3g_solver_config
+{
+	uint32_t force_iterations;     /* Newton iterations (Step's forceIterations) */
+	uint32_t max_pcg_iterations;   /* Step's forceSubIterations */
+	double pcg_tolerance;          /* stop when r.M^-1.r <= tol^2 * r0.M^-1.r0 (b3SolveBEInput::subTolerance) */
+	double newton_tolerance;       /* b3SolveBEInput::tolerance */
+	uint32_t refresh_period;       /* recompute r = b - A x when iteration % period == 0 */
+	int32_t precision;             /* b3g_precision */
+	int32_t preconditioner;        /* b3g_preconditioner */
+	int32_t reserved;
+} b3g_solver_config;
+
+typedef struct b3g_step_stats
+{
+	uint32_t newton_iterations;    /* b3_forceSolverIterations */
+	uint32_t pcg_iterations;       /* max over Newton iterations (b3_forceSolverMaxSubIterations) */
+	uint32_t min_pcg_iterations;   /* b3_forceSolverMinSubIterations */
+	int32_t solve_status;          /* b3g_solve_status of the last PCG solve */
+	double residual_ratio;         /* sqrt(delta / delta0) at exit of the last PCG solve */
+	double newton_error;           /* |dv|^2 of the last Newton iteration */
+} b3g_step_stats;
+
+B3G_API void b3g_solver_config_default(b3g_solver_config* config);
+B3G_API const char* b3g_last_error(void);
+B3G_API const char* b3g_version(void);
+
+/* A context owns one CUDA stream on one device; bodies belong to one context. */
+B3G_API int b3g_context_create(int device, b3g_context** out);
+B3G_API int b3g_context_destroy(b3g_context* ctx);
+/* The CUDA stream (cudaStream_t) every call of this context is ordered on. */
+B3G_API int b3g_context_stream(b3g_context* ctx, void** stream);
+B3G_API int b3g_context_synchronize(b3g_context* ctx);
+
+B3G_API int b3g_body_create(b3g_context* ctx, const b3g_body_desc* desc, b3g_body** out);
+B3G_API int b3g_body_destroy(b3g_body* body);
+/* Sizes: vertex count, tetrahedra, triangles, springs, nonzero 3x3 blocks of A, padded slots. */
+B3G_API int b3g_body_info(const b3g_body* body, uint64_t info[6]);
+/* Device bytes held by the body (state, matrix, element data, solver vectors). */
+B3G_API int b3g_body_device_bytes(const b3g_body* body, uint64_t* bytes);
+
+/* One b3Body::Step on the GPU. Asynchronous on the context stream unless stats is non-NULL,
+ * in which case the call waits and fills stats. dt <= 0 skips the solve like the reference. */
+B3G_API int b3g_body_step(b3g_body* body, float dt, const b3g_solver_config* config, b3g_step_stats* stats);
+
+/* `steps` steps of `count` independent bodies of one context in one persistent launch per
+ * size bucket (captured once in a CUDA graph and replayed). stats, if non-NULL, receives the
+ * last step's statistics of each body (count entries) and makes the call wait. */
+B3G_API int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float dt,
+                   const b3g_solver_config* config, uint32_t steps, b3g_step_stats* stats);
+
+/* Host <-> device state transfer (3 floats per vertex each; either pointer may be NULL). */
+B3G_API int b3g_body_get_state(b3g_body* body, float* positions, float* velocities);
+B3G_API int b3g_body_set_state(b3g_body* body, const float* positions, const float* velocities);
+/* Accumulate external forces / translations for the next step; both are cleared by the step
+ * like b3Body::Step clears b3Particle::m_force and m_translation (body.cpp:577-581). */
+B3G_API int b3g_body_apply_forces(b3g_body* body, const float* forces);
+B3G_API int b3g_body_apply_translations(b3g_body* body, const float* translations);
+/* b3Particle::SetType for every vertex whose type changes (masses are re-lumped). */
+B3G_API int b3g_body_set_types(b3g_body* body, const int32_t* types);
+/* Element rotations as quaternions (x, y, z, w), 4 floats per tetrahedron. */
+B3G_API int b3g_body_get_rotations(b3g_body* body, float* quaternions);
+B3G_API int b3g_body_set_rotations(b3g_body* body, const float* quaternions);
+/* Lumped vertex masses as b3Body::ResetMass computed them (1 float per vertex). */
+B3G_API int b3g_body_get_masses(b3g_body* body, float* masses);
+/* Statistics of the body's last step (waits for it). */
+B3G_API int b3g_body_get_stats(b3g_body* body, b3g_step_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* B3G_H */
