@@ -1,0 +1,379 @@
+#!/usr/bin/env python3
+"""Benchmark of the implicit soft-body step on GB300: vertex-steps/s of the batched solver.
+
+Workload (default "batch"): 512 independent Kuhn-split tetrahedral blocks of a x b x c vertices,
+a, b, c ~ U{4..40} (seeded), Young modulus log-uniform in [1e4, 1e6], Poisson ratio U[0.2, 0.45],
++-1% jitter, one random face pinned, h = 1/60, PCG relative tolerance 1e-5 with at most 200
+iterations, FP32 blocks and vectors with FP64 dot products. One "step" is one implicit step of
+every body of the batch (one persistent, graph-replayed launch).
+
+Printed on one JSON line: whole-job vertex-steps/s (device-timed, inputs resident), the same
+metric end to end through the C ABI with host buffers (e2e), p50/p99 step latency, the plain
+one-body-at-a-time GPU path on a sample of the same bodies, the roofline of the batch kernel,
+SM clocks sampled during the timed region and the CPU baseline (the oracle's C restatement of
+the reference algorithm on this host's cores, on a bounded sample).
+
+--impl reference times that CPU implementation alone on the same workload and prints its own
+line. Under torchrun every rank steps its own batch (weak scaling); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "vertex-steps/s batched vs plain at resid 1e-5; p50/p99 step latency"
+DT = 1.0 / 60.0
+PCG_TOL = 1e-5
+PCG_MAX = 200
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="batch", choices=["batch", "tet64", "cloth128", "tet10"])
+    p.add_argument("--bodies", type=int, default=512)
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "bf16"])
+    p.add_argument("--no-extras", action="store_true", help="skip e2e, plain path and CPU baseline")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ distributed plumbing
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        if args.impl == "ours" and torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg, device=None):
+    if pg is None:
+        return
+    import torch
+
+    if pg.get_backend() == "nccl":
+        pg.barrier(device_ids=[device])
+    else:
+        pg.barrier()
+
+
+def max_over_ranks(pg, value: float, device=None) -> float:
+    if pg is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=f"cuda:{device}" if pg.get_backend() == "nccl" else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, value: float, device=None) -> float:
+    if pg is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=f"cuda:{device}" if pg.get_backend() == "nccl" else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ workload
+def workload(args, rank):
+    from bounce_softbody_gb300 import meshes
+
+    if args.workload == "batch":
+        descs = meshes.batch_bodies(args.bodies, seed=3 + 1000 * rank)
+        cfg = {"workload": f"batch of {args.bodies} Kuhn tet blocks a,b,c~U{{4..40}}", "bodies": args.bodies,
+               "E": "log-uniform 1e4..1e6", "poisson": "U[0.2,0.45]", "h": "1/60", "pcg_tol": PCG_TOL,
+               "pcg_max_iter": PCG_MAX}
+    elif args.workload == "tet64":
+        descs = [meshes.tet_grid(64, 64, 64, seed=rank, E=1e6, nu=0.45, name="tet64")]
+        cfg = {"workload": "64^3 Kuhn tet block E=1e6 nu=0.45", "bodies": 1, "h": "1/30", "pcg_tol": PCG_TOL,
+               "pcg_max_iter": 2000}
+    elif args.workload == "cloth128":
+        descs = [meshes.config_cloth128()]
+        cfg = {"workload": "128^2 cloth + sphere contact", "bodies": 1, "h": "1/60", "pcg_tol": PCG_TOL,
+               "pcg_max_iter": PCG_MAX}
+    else:
+        descs = [meshes.config_tet10(seed=rank)]
+        cfg = {"workload": "10^3 Kuhn tet block", "bodies": 1, "h": "1/60", "pcg_tol": PCG_TOL,
+               "pcg_max_iter": PCG_MAX}
+    return descs, cfg
+
+
+def step_dt(args):
+    return 1.0 / 30.0 if args.workload == "tet64" else DT
+
+
+def pcg_max(args):
+    return 2000 if args.workload == "tet64" else PCG_MAX
+
+
+# ------------------------------------------------------------------ algorithmic bytes
+def spmv_bytes(info, vs=4, bs=36):
+    """One SpMV over the body's blocks: values, column ids, row lengths, x read, y written."""
+    n, nnzb = info["vertices"], info["nnzb"]
+    return (bs + 4) * nnzb + n + 3 * vs * n + 3 * vs * n
+
+
+def iteration_bytes(info, vs=4, bs=36):
+    """One PCG iteration: SpMV + (x, r, d, q, Minv read; x, r, s written) + (s, d read; d written)."""
+    n = info["vertices"]
+    return spmv_bytes(info, vs, bs) + 8 * 3 * vs * n + 3 * 3 * vs * n
+
+
+def assembly_bytes(info):
+    """Element phase and row assembly of one step (first touch of every array, FP32)."""
+    n, nt, nnzb = info["vertices"], info["tets"], info["nnzb"]
+    tets = nt * (16 + 36 + 16 + 16 + 16 + 64 + 48)     # ids, invE, material, q r/w, records, rhs parts
+    gathers = n * (12 * 4)                             # x, v, translation, fext
+    rows = 40 * nnzb + 16 * nt * 4 + nt * 4 * 4 + n * (4 + 4 + 1 + 12) + n * 12 * 7
+    return tets + gathers + rows
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    def __init__(self, device: int):
+        self.path = tempfile.mktemp(prefix="clocks_", suffix=".csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ CPU implementation (oracle port)
+def cpu_sample(descs):
+    """A bounded, size-stratified sample: every 8th body in size order (about 1/8 of the vertices)."""
+    order = sorted(range(len(descs)), key=lambda k: -descs[k].n)
+    return [descs[k] for k in order[::8]] if len(descs) > 8 else list(descs)
+
+
+def run_cpu(descs, steps, dt, max_sub, threads):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    _, _, iters, sec = oracle.simulate_batch(descs, steps, dt=dt, max_sub=max_sub, sub_tol=PCG_TOL, bits=32,
+                                             threads=threads)
+    return sum(d.n for d in descs) * steps / sec, sec, iters
+
+
+def reference_arm(args, world, rank, pg):
+    descs, cfg = workload(args, rank)
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    sample = cpu_sample(descs)
+    dt, mx = step_dt(args), pcg_max(args)
+    for _ in range(args.warmup):
+        run_cpu(sample, 1, dt, mx, threads)
+    times = []
+    for _ in range(args.steps):
+        _, sec, _ = run_cpu(sample, 1, dt, mx, threads)
+        times.append(sec)
+    total = sum(times)
+    vs = sum(d.n for d in sample) * args.steps / total
+    desc = (f"oracle C restatement (FP32, Jacobi PCG, tol 1e-5) of {len(sample)} of {len(descs)} bodies "
+            f"({sum(d.n for d in sample)} vertices), 1 step per timed step, {threads} threads")
+    line = {"metric": METRIC, "value": vs, "unit": "vertex-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes)",
+            "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": vs, "unit": "vertex-steps/s", "cores": threads, "kind": "port", "sample": desc},
+            "e2e": {"value": vs, "unit": "vertex-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "p50_step_ms": 1e3 * statistics.median(times), "p99_step_ms": 1e3 * float(np.percentile(times, 99))}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ our arm
+def ours(args, world, rank, local, pg):
+    import torch
+
+    from bounce_softbody_gb300 import b3g
+
+    descs, cfg = workload(args, rank)
+    dt, mx = step_dt(args), pcg_max(args)
+    prec = {"fp32": b3g.PRECISION_FP32, "fp64": b3g.PRECISION_FP64, "bf16": b3g.PRECISION_BF16}[args.precision]
+    scfg = b3g.solver_config(max_pcg_iterations=mx, pcg_tolerance=PCG_TOL, precision=prec)
+    ctx = b3g.Context(local)
+    t0 = time.time()
+    bodies = [b3g.Body(ctx, d) for d in descs]
+    setup_s = time.time() - t0
+    infos = [b.info() for b in bodies]
+    nverts = sum(i["vertices"] for i in infos)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+
+    def step_once():
+        b3g.step_batch(ctx, bodies, dt, 1, scfg, stats=False)
+
+    for _ in range(max(args.warmup, 3)):
+        step_once()
+    ctx.synchronize()
+    before = [b.stats()["total_pcg_iterations"] for b in bodies]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    barrier(pg, local)
+    torch.cuda.synchronize(local)
+    clocks = Clocks(local)
+    ev[0].record(stream)
+    for k in range(args.steps):
+        step_once()
+        ev[k + 1].record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize(local)
+    clk = clocks.stop()
+    barrier(pg, local)
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[args.steps])
+    after = [b.stats()["total_pcg_iterations"] for b in bodies]
+    iters = [a - b for a, b in zip(after, before)]
+    t_max = max_over_ranks(pg, total_ms / 1e3, local)
+    value = sum_over_ranks(pg, nverts * args.steps, local) / t_max
+
+    # roofline of the batch kernel (the only kernel of a step besides a 8-byte memset)
+    bs, vsz = {"fp32": (36, 4), "fp64": (72, 8), "bf16": (18, 4)}[args.precision]
+    alg = sum(args.steps * assembly_bytes(i) + it * iteration_bytes(i, vsz, bs) for i, it in zip(infos, iters))
+    achieved = alg / (total_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "k_batch (persistent, one launch per step)",
+            "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_step": alg / args.steps,
+            "pcg_iterations_per_step_mean": float(np.mean(iters)) / args.steps if iters else 0.0}
+    sched = b3g.batch_schedule(ctx) if args.workload == "batch" else None
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # e2e through the C ABI with pinned host buffers: H2D external forces, step, D2H x and v
+        f_h = torch.zeros(3 * nverts, dtype=torch.float32).pin_memory()
+        x_h = torch.empty(3 * nverts, dtype=torch.float32).pin_memory()
+        v_h = torch.empty(3 * nverts, dtype=torch.float32).pin_memory()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(local)
+        e0.record(stream)
+        for _ in range(args.steps):
+            b3g.batch_apply_forces(ctx, bodies, f_h.data_ptr())
+            step_once()
+            b3g.batch_get_state(ctx, bodies, x_h.data_ptr(), v_h.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize(local)
+        e2e_ms = e0.elapsed_time(e1)
+        extras["e2e"] = {"value": nverts * args.steps / (e2e_ms / 1e3), "unit": "vertex-steps/s",
+                         "h2d_bytes_per_step": 12 * nverts, "d2h_bytes_per_step": 24 * nverts}
+        # plain one-body-at-a-time GPU path (per-op kernels) on a size-stratified sample
+        sample = sorted(range(len(bodies)), key=lambda k: -infos[k]["vertices"])[::16] if len(bodies) > 16 else list(
+            range(len(bodies)))
+        for k in sample[:2]:
+            bodies[k].step(dt, scfg, stats=False)
+        ctx.synchronize()
+        p0 = time.perf_counter()
+        for k in sample:
+            bodies[k].step(dt, scfg, stats=False)
+        ctx.synchronize()
+        plain_s = time.perf_counter() - p0
+        plain_vs = sum(infos[k]["vertices"] for k in sample) / plain_s
+        extras["plain"] = {"value": plain_vs, "unit": "vertex-steps/s", "bodies": len(sample),
+                           "batched_over_plain": value / plain_vs}
+        # CPU baseline: the oracle restatement on this host's cores, bounded sample
+        threads = os.cpu_count() or 1
+        cs = cpu_sample(descs)
+        cvs, csec, _ = run_cpu(cs, 1, dt, mx, threads)
+        extras["cpu_baseline"] = {"value": cvs, "unit": "vertex-steps/s", "cores": threads, "kind": "port",
+                                  "sample": f"{len(cs)} of {len(descs)} bodies ({sum(d.n for d in cs)} vertices), "
+                                            f"1 step, oracle C restatement FP32, {csec:.2f} s"}
+
+    launches = args.steps  # one persistent kernel per step (graph: memset node + kernel node)
+    line = {"metric": METRIC, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "fp64": "f64", "bf16": "bf16+f32"}[args.precision],
+            "data": "synthetic (seeded meshes)",
+            "config": dict(cfg, vertices=nverts, l2="inputs larger than L2 (no flush needed)",
+                           precision=args.precision, setup_s=round(setup_s, 2)),
+            "p50_step_ms": statistics.median(step_ms), "p99_step_ms": float(np.percentile(step_ms, 99)),
+            "roofline": roof, "clocks": clk, "gpu_launches": launches}
+    if sched:
+        line["schedule"] = {k: sched[k] for k in ("cluster", "threshold", "cluster_bodies", "ctas", "autotuned")}
+    line.update(extras)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for b in bodies:
+        b.close()
+    ctx.close()
+    return 0
+
+
+def main():
+    args = parse()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        rc = reference_arm(args, world, rank, pg)
+    else:
+        rc = ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -55,13 +55,15 @@ class StepStats(C.Structure):
         ("newton_iterations", C.c_uint32), ("pcg_iterations", C.c_uint32),
         ("min_pcg_iterations", C.c_uint32), ("solve_status", C.c_int32),
         ("residual_ratio", C.c_double), ("newton_error", C.c_double),
+        ("total_pcg_iterations", C.c_uint64), ("total_steps", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:
         return {"newton_iterations": self.newton_iterations, "pcg_iterations": self.pcg_iterations,
                 "min_pcg_iterations": self.min_pcg_iterations,
                 "solve_status": SOLVE_STATUS.get(self.solve_status, str(self.solve_status)),
-                "residual_ratio": self.residual_ratio, "newton_error": self.newton_error}
+                "residual_ratio": self.residual_ratio, "newton_error": self.newton_error,
+                "total_pcg_iterations": int(self.total_pcg_iterations), "total_steps": int(self.total_steps)}
 
 
 # every entry point of include/b3g.h with its ctypes signature
@@ -80,6 +82,9 @@ SIGNATURES = {
     "b3g_body_step": (C.c_int, [C.c_void_p, C.c_float, C.POINTER(SolverConfig), C.POINTER(StepStats)]),
     "b3g_step_batch": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.c_float,
                                  C.POINTER(SolverConfig), C.c_uint32, C.POINTER(StepStats)]),
+    "b3g_batch_schedule": (C.c_int, [C.c_void_p, _ip, C.c_uint32]),
+    "b3g_batch_apply_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp]),
+    "b3g_batch_get_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp, _fp]),
     "b3g_body_get_state": (C.c_int, [C.c_void_p, _fp, _fp]),
     "b3g_body_set_state": (C.c_int, [C.c_void_p, _fp, _fp]),
     "b3g_body_apply_forces": (C.c_int, [C.c_void_p, _fp]),
@@ -313,3 +318,27 @@ def step_batch(ctx: Context, bodies: Sequence[Body], dt: float, steps: int = 1,
     _check(lib.b3g_step_batch(ctx.handle, arr, len(bodies), dt, C.byref(cfg), steps, st if stats else None),
            "b3g_step_batch")
     return [s.as_dict() for s in st] if stats else None
+
+
+def batch_schedule(ctx: Context) -> dict:
+    buf = np.zeros(256, np.int32)
+    _check(load_library().b3g_batch_schedule(ctx.handle, buf.ctypes.data_as(_ip), buf.size), "b3g_batch_schedule")
+    n = int(buf[5])
+    cands = [(int(buf[6 + 2 * k]) // 1000000, int(buf[6 + 2 * k]) % 1000000, buf[7 + 2 * k] / 1000.0)
+             for k in range(min(n, (buf.size - 6) // 2))]
+    return {"cluster": int(buf[0]), "threshold": int(buf[1]), "cluster_bodies": int(buf[2]),
+            "ctas": int(buf[3]), "autotuned": bool(buf[4]), "candidates_ms": cands}
+
+
+def batch_apply_forces(ctx: Context, bodies: Sequence[Body], forces_ptr: int):
+    """forces_ptr: host address of the concatenated forces (3 floats per vertex, list order)."""
+    arr = (C.c_void_p * len(bodies))(*[b.handle for b in bodies])
+    _check(load_library().b3g_batch_apply_forces(ctx.handle, arr, len(bodies), C.cast(forces_ptr, _fp)),
+           "b3g_batch_apply_forces")
+
+
+def batch_get_state(ctx: Context, bodies: Sequence[Body], x_ptr: int, v_ptr: int):
+    """Copy every body's positions / velocities into concatenated host arrays (addresses)."""
+    arr = (C.c_void_p * len(bodies))(*[b.handle for b in bodies])
+    _check(load_library().b3g_batch_get_state(ctx.handle, arr, len(bodies), C.cast(x_ptr, _fp), C.cast(v_ptr, _fp)),
+           "b3g_batch_get_state")

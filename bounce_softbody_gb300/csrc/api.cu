@@ -300,6 +300,8 @@ void stats_from(const Scalars& sc, b3g_step_stats* st)
 	st->solve_status = sc.status;
 	st->residual_ratio = sc.delta0 > 0.0 ? std::sqrt(std::max(0.0, sc.delta / sc.delta0)) : 0.0;
 	st->newton_error = sc.newton_err;
+	st->total_pcg_iterations = sc.total_iters;
+	st->total_steps = sc.total_steps;
 }
 
 int read_scalars(b3g_body* b, Scalars* out)

@@ -1,35 +1,406 @@
-// Batched stepping of many independent bodies (b3g_step_batch).
+// Batched stepping of many independent bodies (b3g_step_batch): one persistent launch
+// (persistent.cu) per call, captured once into a CUDA graph and replayed.
+//
+// Schedule: bodies are sorted by vertex count, largest first. Bodies with at least `threshold`
+// vertices are stepped by clusters of `cluster` CTAs, the rest by single CTAs. The schedule
+// (cluster size, threshold) is chosen per batch by an autotuner on the first call: it snapshots
+// the mutable state of every body, times one step of each candidate schedule with CUDA events,
+// restores the snapshot and keeps the fastest. Set B3G_AUTOTUNE=0 to use the size heuristic, or
+// B3G_BATCH_SCHEDULE="cluster,threshold" to force a schedule.
 #include "api_internal.h"
 
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
 #include <vector>
 
 using namespace b3g;
 
+struct Snapshot
+{
+	void* dst;
+	const void* src;
+	size_t bytes;
+};
+
 struct BatchCache
 {
+	std::vector<b3g_body*> bodies;
+	int prec = 0, precond = 0;
+	DevBody* d_bodies = nullptr;
+	int* d_order = nullptr;      // all bodies sorted by size, descending
+	unsigned* d_queue = nullptr;
+	std::vector<int> order;
+	int cluster = 1;
+	int threshold = 1 << 30;
+	int nbig = 0;
+	int ctas = 0;
+	bool tuned = false;
+	// graph of (memset queue, batch launch) for one step with the current parameters
+	cudaGraphExec_t graph = nullptr;
+	float g_h = 0.0f;
+	int g_steps = 0, g_newton = 0, g_max_iter = 0, g_refresh = 0;
+	double g_tol2 = 0.0, g_ntol2 = 0.0;
+	std::vector<std::pair<int, double>> tune_log;  // (cluster * 1e6 + threshold, ms)
 };
+
+namespace {
+
+void free_cache(BatchCache* c)
+{
+	if (!c) return;
+	if (c->graph) cudaGraphExecDestroy(c->graph);
+	cudaFree(c->d_bodies);
+	cudaFree(c->d_order);
+	cudaFree(c->d_queue);
+	delete c;
+}
+
+int schedule_ctas(int prec, int cluster, int sms)
+{
+	int m = batch_max_clusters(prec, cluster);
+	if (m <= 0) m = std::max(1, sms / cluster);
+	return m * cluster;
+}
+
+BatchArgs make_args(BatchCache* c, float h, int steps, const b3g_solver_config& cfg)
+{
+	BatchArgs A;
+	A.bodies = c->d_bodies;
+	A.big = c->d_order;
+	A.nbig = c->nbig;
+	A.small = c->d_order + c->nbig;
+	A.nsmall = (int)c->order.size() - c->nbig;
+	A.queue = c->d_queue;
+	A.steps = steps;
+	A.h = h;
+	A.newton = (int)std::max<uint32_t>(1u, cfg.force_iterations);
+	A.max_iter = (int)cfg.max_pcg_iterations;
+	A.tol2 = cfg.pcg_tolerance * cfg.pcg_tolerance;
+	A.refresh = (int)cfg.refresh_period;
+	A.newton_tol2 = cfg.newton_tolerance * cfg.newton_tolerance;
+	A.prec = c->prec;
+	A.cluster = c->cluster;
+	A.ctas = c->ctas;
+	return A;
+}
+
+void set_schedule(BatchCache* c, int cluster, int threshold, int sms)
+{
+	c->cluster = cluster;
+	c->threshold = threshold;
+	int nbig = 0;
+	if (cluster > 1)
+		for (int k : c->order)
+			if ((int)c->bodies[k]->n >= threshold) ++nbig;
+	c->nbig = nbig;
+	c->ctas = schedule_ctas(c->prec, cluster, sms);
+	if (c->graph)
+	{
+		cudaGraphExecDestroy(c->graph);
+		c->graph = nullptr;
+	}
+}
+
+// the mutable per-body state a step changes
+std::vector<Snapshot> snapshot_list(BatchCache* c, char* store, size_t* total)
+{
+	std::vector<Snapshot> L;
+	size_t off = 0;
+	auto add = [&](const void* p, size_t bytes) {
+		if (!bytes) return;
+		L.push_back(Snapshot{store ? store + off : nullptr, p, bytes});
+		off += (bytes + 255) & ~(size_t)255;
+	};
+	for (b3g_body* b : c->bodies)
+	{
+		const DevBody& d = b->d;
+		size_t v3 = 3 * (size_t)b->n * sizeof(float);
+		add(d.x, v3);
+		add(d.v, v3);
+		add(d.fext, v3);
+		add(d.trans, v3);
+		add(d.tet_q, (size_t)b->nt * sizeof(float4));
+		add(d.c_exists, (size_t)b->n * b->nw);
+		add(d.c_apply, (size_t)b->n * b->nw);
+		add(d.c_nf, (size_t)b->n * b->nw * sizeof(float));
+		add(d.c_normal, 3 * (size_t)b->n * b->nw * sizeof(float));
+		add(d.sc, sizeof(Scalars));
+	}
+	*total = off;
+	return L;
+}
+
+cudaError_t run_once(BatchCache* c, const BatchArgs& A, cudaStream_t st) { return op_batch(A, st); }
+
+int autotune(b3g_context* ctx, BatchCache* c, float h, const b3g_solver_config& cfg)
+{
+	cudaStream_t st = ctx->stream;
+	size_t total = 0;
+	snapshot_list(c, nullptr, &total);
+	char* store = nullptr;
+	cudaError_t e = cudaMalloc(&store, std::max<size_t>(total, 256));
+	if (e != cudaSuccess)
+	{
+		cudaGetLastError();
+		return B3G_OK;  // not enough memory to tune: keep the heuristic
+	}
+	std::vector<Snapshot> L = snapshot_list(c, store, &total);
+	for (const Snapshot& s : L) cudaMemcpyAsync(s.dst, s.src, s.bytes, cudaMemcpyDeviceToDevice, st);
+
+	int maxn = 0;
+	for (b3g_body* b : c->bodies) maxn = std::max(maxn, (int)b->n);
+	std::vector<std::pair<int, int>> cands;
+	cands.push_back({1, 1 << 30});
+	const int thresholds[] = {4096, 8192, 16384, 32768};
+	const int clusters[] = {2, 4, 8};
+	for (int cl : clusters)
+		for (int t : thresholds)
+			if (t <= maxn) cands.push_back({cl, t});
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	float best = 1e30f;
+	std::pair<int, int> best_c = {c->cluster, c->threshold};
+	for (auto& cd : cands)
+	{
+		set_schedule(c, cd.first, cd.second, ctx->sm_count);
+		BatchArgs A = make_args(c, h, 1, cfg);
+		e = run_once(c, A, st);  // warm-up
+		for (const Snapshot& s : L) cudaMemcpyAsync((void*)s.src, s.dst, s.bytes, cudaMemcpyDeviceToDevice, st);
+		cudaEventRecord(e0, st);
+		if (e == cudaSuccess) e = run_once(c, A, st);
+		cudaEventRecord(e1, st);
+		for (const Snapshot& s : L) cudaMemcpyAsync((void*)s.src, s.dst, s.bytes, cudaMemcpyDeviceToDevice, st);
+		if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+		if (e != cudaSuccess) break;
+		float ms = 0.0f;
+		cudaEventElapsedTime(&ms, e0, e1);
+		c->tune_log.push_back({cd.first * 1000000 + std::min(cd.second, 999999), (double)ms});
+		if (ms < best)
+		{
+			best = ms;
+			best_c = cd;
+		}
+	}
+	cudaStreamSynchronize(st);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(store);
+	if (e != cudaSuccess) return cuda_fail(e, "batch autotune");
+	set_schedule(c, best_c.first, best_c.second, ctx->sm_count);
+	c->tuned = true;
+	return B3G_OK;
+}
+
+int build_cache(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, int prec, int precond, BatchCache** out)
+{
+	BatchCache* c = new BatchCache();
+	c->bodies.assign(bodies, bodies + count);
+	c->prec = prec;
+	c->precond = precond;
+	std::vector<DevBody> h(count);
+	for (uint32_t k = 0; k < count; ++k) h[k] = dev_for(bodies[k], prec, precond);
+	c->order.resize(count);
+	std::iota(c->order.begin(), c->order.end(), 0);
+	std::stable_sort(c->order.begin(), c->order.end(), [&](int a, int b) { return bodies[a]->n > bodies[b]->n; });
+	cudaError_t e = cudaMalloc(&c->d_bodies, std::max<size_t>(1, count) * sizeof(DevBody));
+	if (e == cudaSuccess) e = cudaMalloc(&c->d_order, std::max<size_t>(1, count) * sizeof(int));
+	if (e == cudaSuccess) e = cudaMalloc(&c->d_queue, 4 * sizeof(unsigned));
+	if (e == cudaSuccess && count)
+		e = cudaMemcpyAsync(c->d_bodies, h.data(), count * sizeof(DevBody), cudaMemcpyHostToDevice, ctx->stream);
+	if (e == cudaSuccess && count)
+		e = cudaMemcpyAsync(c->d_order, c->order.data(), count * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+	if (e != cudaSuccess)
+	{
+		free_cache(c);
+		return cuda_fail(e, "batch setup");
+	}
+	// size heuristic: clusters of 4 for bodies of 16k vertices or more
+	int maxn = 0;
+	for (uint32_t k = 0; k < count; ++k) maxn = std::max(maxn, (int)bodies[k]->n);
+	if (maxn >= 16384) set_schedule(c, 4, 16384, ctx->sm_count);
+	else set_schedule(c, 1, 1 << 30, ctx->sm_count);
+	*out = c;
+	return B3G_OK;
+}
+
+} // namespace
 
 void destroy_batch_cache(b3g_context* c)
 {
-	delete c->batch;
+	free_cache(c->batch);
 	c->batch = nullptr;
 }
 
 void forget_body_in_batch_cache(b3g_context* c, b3g_body* b)
 {
-	(void)b;
-	destroy_batch_cache(c);
+	if (!c->batch) return;
+	for (b3g_body* x : c->batch->bodies)
+		if (x == b)
+		{
+			destroy_batch_cache(c);
+			return;
+		}
 }
 
 extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float dt,
-                              const b3g_solver_config* cfg, uint32_t steps, b3g_step_stats* stats)
+                              const b3g_solver_config* cfg_in, uint32_t steps, b3g_step_stats* stats)
 {
 	if (!ctx || (!bodies && count)) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
-	for (uint32_t s = 0; s < steps; ++s)
-		for (uint32_t k = 0; k < count; ++k)
+	if (count == 0 || steps == 0) return B3G_OK;
+	b3g_solver_config cfg;
+	if (cfg_in) cfg = *cfg_in;
+	else b3g_solver_config_default(&cfg);
+	int rc = check_config(&cfg);
+	if (rc != B3G_OK) return rc;
+	for (uint32_t k = 0; k < count; ++k)
+	{
+		if (!bodies[k]) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u is null", k);
+		if (bodies[k]->ctx != ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u belongs to another context", k);
+		for (uint32_t j = 0; j < k; ++j)
+			if (bodies[j] == bodies[k]) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u is listed twice", k);
+	}
+	cudaSetDevice(ctx->device);
+	cudaStream_t st = ctx->stream;
+	if (!(dt > 0.0f))
+	{
+		for (uint32_t s = 0; s < steps; ++s)
+			for (uint32_t k = 0; k < count; ++k)
+			{
+				rc = b3g_body_step(bodies[k], dt, &cfg, nullptr);
+				if (rc != B3G_OK) return rc;
+			}
+		if (stats) std::memset(stats, 0, count * sizeof(*stats));
+		return b3g_context_synchronize(ctx);
+	}
+	const int prec = prec_of(&cfg);
+	for (uint32_t k = 0; k < count; ++k)
+	{
+		rc = ensure_precision(bodies[k], prec);
+		if (rc != B3G_OK) return rc;
+	}
+	BatchCache* c = ctx->batch;
+	bool same = c && c->prec == prec && c->precond == cfg.preconditioner && c->bodies.size() == count &&
+	            std::equal(c->bodies.begin(), c->bodies.end(), bodies);
+	if (!same)
+	{
+		destroy_batch_cache(ctx);
+		rc = build_cache(ctx, bodies, count, prec, cfg.preconditioner, &c);
+		if (rc != B3G_OK) return rc;
+		ctx->batch = c;
+		const char* env = std::getenv("B3G_AUTOTUNE");
+		const char* forced = std::getenv("B3G_BATCH_SCHEDULE");  // "cluster,threshold"
+		int fc = 0, ft = 0;
+		if (forced && std::sscanf(forced, "%d,%d", &fc, &ft) == 2 && (fc == 1 || fc == 2 || fc == 4 || fc == 8))
+			set_schedule(c, fc, ft > 0 ? ft : (1 << 30), ctx->sm_count);
+		else if (!(env && env[0] == '0'))
 		{
-			int rc = b3g_body_step(bodies[k], dt, cfg, (stats && s + 1 == steps) ? stats + k : nullptr);
+			rc = autotune(ctx, c, dt, cfg);
 			if (rc != B3G_OK) return rc;
 		}
+	}
+	BatchArgs A = make_args(c, dt, 1, cfg);
+	const bool graph_ok = c->graph && c->g_h == dt && c->g_newton == A.newton && c->g_max_iter == A.max_iter &&
+	                      c->g_tol2 == A.tol2 && c->g_refresh == A.refresh && c->g_ntol2 == A.newton_tol2;
+	cudaError_t e = cudaSuccess;
+	if (!graph_ok)
+	{
+		if (c->graph)
+		{
+			cudaGraphExecDestroy(c->graph);
+			c->graph = nullptr;
+		}
+		cudaGraph_t g = nullptr;
+		e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+		if (e == cudaSuccess)
+		{
+			cudaError_t le = op_batch(A, st);
+			e = cudaStreamEndCapture(st, &g);
+			if (le != cudaSuccess) e = le;
+		}
+		if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph, g, 0);
+		if (g) cudaGraphDestroy(g);
+		if (e != cudaSuccess) return cuda_fail(e, "batch graph");
+		c->g_h = dt;
+		c->g_newton = A.newton;
+		c->g_max_iter = A.max_iter;
+		c->g_tol2 = A.tol2;
+		c->g_refresh = A.refresh;
+		c->g_ntol2 = A.newton_tol2;
+	}
+	for (uint32_t s = 0; s < steps && e == cudaSuccess; ++s) e = cudaGraphLaunch(c->graph, st);
+	if (e != cudaSuccess) return cuda_fail(e, "batch launch");
+	if (stats)
+	{
+		// read back each body's solver scalars through the pinned buffer, 1024 at a time
+		for (uint32_t k0 = 0; k0 < count && e == cudaSuccess; k0 += 1024)
+		{
+			uint32_t m = std::min<uint32_t>(1024, count - k0);
+			for (uint32_t k = 0; k < m && e == cudaSuccess; ++k)
+				e = cudaMemcpyAsync(ctx->h_scalars + k, bodies[k0 + k]->d.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st);
+			if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+			for (uint32_t k = 0; k < m && e == cudaSuccess; ++k) stats_from(ctx->h_scalars[k], stats + k0 + k);
+		}
+		if (e != cudaSuccess) return cuda_fail(e, "batch stats");
+	}
 	return B3G_OK;
+}
+
+extern "C" int b3g_batch_schedule(b3g_context* ctx, int32_t* out, uint32_t capacity)
+{
+	if (!ctx || !out) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	if (!ctx->batch) return fail(B3G_ERROR_INVALID_ARGUMENT, "no batch has been stepped on this context");
+	BatchCache* c = ctx->batch;
+	std::vector<int32_t> v = {c->cluster, c->threshold == (1 << 30) ? -1 : c->threshold, c->nbig, c->ctas,
+	                          c->tuned ? 1 : 0, (int32_t)c->tune_log.size()};
+	for (auto& t : c->tune_log)
+	{
+		v.push_back(t.first);
+		v.push_back((int32_t)(t.second * 1000.0));  // microseconds
+	}
+	for (uint32_t k = 0; k < capacity && k < v.size(); ++k) out[k] = v[k];
+	return B3G_OK;
+}
+
+extern "C" int b3g_batch_apply_forces(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, const float* forces)
+{
+	if (!ctx || (!bodies && count) || (!forces && count)) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	cudaStream_t st = ctx->stream;
+	size_t off = 0;
+	cudaError_t e = cudaSuccess;
+	for (uint32_t k = 0; k < count && e == cudaSuccess; ++k)
+	{
+		b3g_body* b = bodies[k];
+		if (!b || b->ctx != ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u is null or of another context", k);
+		size_t c = 3 * (size_t)b->n;
+		e = cudaMemcpyAsync(b->staging, forces + off, c * sizeof(float), cudaMemcpyHostToDevice, st);
+		if (e == cudaSuccess) e = op_accumulate(b->d.fext, b->staging, c, st);
+		off += c;
+	}
+	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch_apply_forces");
+}
+
+extern "C" int b3g_batch_get_state(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float* positions,
+                                   float* velocities)
+{
+	if (!ctx || (!bodies && count)) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	cudaStream_t st = ctx->stream;
+	size_t off = 0;
+	cudaError_t e = cudaSuccess;
+	for (uint32_t k = 0; k < count && e == cudaSuccess; ++k)
+	{
+		b3g_body* b = bodies[k];
+		if (!b || b->ctx != ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u is null or of another context", k);
+		size_t c = 3 * (size_t)b->n;
+		if (positions) e = cudaMemcpyAsync(positions + off, b->d.x, c * sizeof(float), cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess && velocities)
+			e = cudaMemcpyAsync(velocities + off, b->d.v, c * sizeof(float), cudaMemcpyDeviceToHost, st);
+		off += c;
+	}
+	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch_get_state");
 }

@@ -15,6 +15,19 @@ constexpr float kMaxContactCorrection = 0.2f;
 constexpr float kBaumgarte = 0.2f;
 constexpr float kFltEps = 1.1920928955078125e-7f;
 
+// ------------------------------------------------------------------ load policies
+// LdPlain: ordinary loads, for kernels that only read what earlier launches wrote.
+// LdCG: L2-coherent loads (ld.global.cg) for the persistent kernel, which reads data that other
+// threads of its team wrote earlier in the same launch; it never uses the read-only path.
+struct LdPlain
+{
+	template <class T> static __device__ __forceinline__ T ld(const T* p) { return *p; }
+};
+struct LdCG
+{
+	template <class T> static __device__ __forceinline__ T ld(const T* p) { return __ldcg(p); }
+};
+
 // ------------------------------------------------------------------ storage conversions
 template <class T> __device__ __forceinline__ float to_f(T v);
 template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
@@ -57,6 +70,11 @@ __device__ __forceinline__ float3 normalize3(float3 a)
 	return a;
 }
 __device__ __forceinline__ float3 ld3(const float* p, int i) { return f3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+template <class L>
+__device__ __forceinline__ float3 ldl3(const float* p, int i)
+{
+	return f3(L::ld(p + 3 * i), L::ld(p + 3 * i + 1), L::ld(p + 3 * i + 2));
+}
 __device__ __forceinline__ void st3(float* p, int i, float3 v)
 {
 	p[3 * i] = v.x;
@@ -156,6 +174,7 @@ struct StepParams
 // equals -h V R sigma(sym U) g_a with sigma(e) = lambda tr(e) I + 2 mu e, because
 // K0 = V B^T D B is that isotropic operator. The A contribution (h^2 + h kd) R K0_ab R^T is
 // kept in factored form: rows of R times the shape gradients, scaled (tet_rec).
+template <class L = LdPlain>
 __device__ __forceinline__ void tet_element(const DevBody& B, int e, const StepParams& P)
 {
 	const float h = P.h;
@@ -166,24 +185,24 @@ __device__ __forceinline__ void tet_element(const DevBody& B, int e, const StepP
 #pragma unroll
 	for (int k = 0; k < 9; ++k) ie[k] = B.tet_invE[9 * (size_t)e + k];
 	float4 mat = B.tet_mat[e];  // volume, lambda, mu, kd
-	float3 p1 = ld3(X, id.x), p2 = ld3(X, id.y), p3 = ld3(X, id.z), p4 = ld3(X, id.w);
+	float3 p1 = ldl3<L>(X, id.x), p2 = ldl3<L>(X, id.y), p3 = ldl3<L>(X, id.z), p4 = ldl3<L>(X, id.w);
 	float F[9];
 	edge_times_invE(p2 - p1, p3 - p1, p4 - p1, ie, F);
-	float4 q = extract_rotation(F, B.tet_q[e]);
+	float4 q = extract_rotation(F, L::ld(B.tet_q + e));
 	B.tet_q[e] = q;
 	float R[9];
 	quat_to_mat(q, R);
 
 	// w = x0 - x + h v + y
-	float3 v1 = ld3(Vv, id.x), v2 = ld3(Vv, id.y), v3 = ld3(Vv, id.z), v4 = ld3(Vv, id.w);
-	float3 y1 = ld3(B.trans, id.x), y2 = ld3(B.trans, id.y), y3 = ld3(B.trans, id.z), y4 = ld3(B.trans, id.w);
+	float3 v1 = ldl3<L>(Vv, id.x), v2 = ldl3<L>(Vv, id.y), v3 = ldl3<L>(Vv, id.z), v4 = ldl3<L>(Vv, id.w);
+	float3 y1 = ldl3<L>(B.trans, id.x), y2 = ldl3<L>(B.trans, id.y), y3 = ldl3<L>(B.trans, id.z), y4 = ldl3<L>(B.trans, id.w);
 	float3 w1 = h * v1 + y1, w2 = h * v2 + y2, w3 = h * v3 + y3, w4 = h * v4 + y4;
 	if (!P.first_newton)
 	{
-		w1 = w1 + (ld3(B.x, id.x) - p1);
-		w2 = w2 + (ld3(B.x, id.y) - p2);
-		w3 = w3 + (ld3(B.x, id.z) - p3);
-		w4 = w4 + (ld3(B.x, id.w) - p4);
+		w1 = w1 + (ldl3<L>(B.x, id.x) - p1);
+		w2 = w2 + (ldl3<L>(B.x, id.y) - p2);
+		w3 = w3 + (ldl3<L>(B.x, id.z) - p3);
+		w4 = w4 + (ldl3<L>(B.x, id.w) - p4);
 	}
 	float G[9];
 	edge_times_invE(w2 - w1, w3 - w1, w4 - w1, ie, G);
@@ -247,13 +266,14 @@ __device__ __forceinline__ void compute_basis(float3 a, float3& b, float3& c)
 // Corotational orthotropic membrane triangle (triangle_element_force.cpp:285-468). Writes the
 // 9 blocks (h^2 + h kd) K_ab of A and the 3 right-hand-side vectors
 // h (f_a - kd (K v)_a - (K w)_a).
+template <class L = LdPlain>
 __device__ __forceinline__ void tri_element(const DevBody& B, int e, const StepParams& P)
 {
 	const float h = P.h;
 	uint4 id = B.tri[e];
 	const float* X = P.first_newton ? B.x : B.xi;
 	const float* Vv = P.first_newton ? B.v : B.vi;
-	float3 p[3] = {ld3(X, id.x), ld3(X, id.y), ld3(X, id.z)};
+	float3 p[3] = {ldl3<L>(X, id.x), ldl3<L>(X, id.y), ldl3<L>(X, id.z)};
 	int ids[3] = {(int)id.x, (int)id.y, (int)id.z};
 	float3 n = normalize3(cross3(p[1] - p[0], p[2] - p[0]));
 	float3 px, py;
@@ -301,13 +321,13 @@ __device__ __forceinline__ void tri_element(const DevBody& B, int e, const StepP
 		fa[a] = -(rx * px + ry * py);
 	}
 	// 3-D blocks K_ab = P^T (R K0_ab R^T) P, P = [px^T; py^T]
-	float3 vv[3] = {ld3(Vv, ids[0]), ld3(Vv, ids[1]), ld3(Vv, ids[2])};
+	float3 vv[3] = {ldl3<L>(Vv, ids[0]), ldl3<L>(Vv, ids[1]), ldl3<L>(Vv, ids[2])};
 	float3 ww[3];
 #pragma unroll
 	for (int k = 0; k < 3; ++k)
 	{
-		ww[k] = h * vv[k] + ld3(B.trans, ids[k]);
-		if (!P.first_newton) ww[k] = ww[k] + (ld3(B.x, ids[k]) - p[k]);
+		ww[k] = h * vv[k] + ldl3<L>(B.trans, ids[k]);
+		if (!P.first_newton) ww[k] = ww[k] + (ldl3<L>(B.x, ids[k]) - p[k]);
 	}
 	float3 acc[3] = {fa[0], fa[1], fa[2]};
 	float* blk = B.blocks + 81 * (size_t)e;
@@ -349,14 +369,15 @@ __device__ __forceinline__ void tri_element(const DevBody& B, int e, const StepP
 // Tension-only spring (spring_force.cpp:61-143). The stiffness Jacobian keeps the reference's
 // unnormalised outer product dx dx^T. Writes one block h^2 Ks + h Kd (+ on the diagonal,
 // - off it) and one vector h (f1 - Ks (w1 - w2)) (+ for vertex 1, - for vertex 2).
+template <class LP = LdPlain>
 __device__ __forceinline__ void spring_element(const DevBody& B, int s, const StepParams& P)
 {
 	const float h = P.h;
 	uint2 id = B.spr[s];
 	const float* X = P.first_newton ? B.x : B.xi;
 	const float* Vv = P.first_newton ? B.v : B.vi;
-	float3 x1 = ld3(X, id.x), x2 = ld3(X, id.y);
-	float3 v1 = ld3(Vv, id.x), v2 = ld3(Vv, id.y);
+	float3 x1 = ldl3<LP>(X, id.x), x2 = ldl3<LP>(X, id.y);
+	float3 v1 = ldl3<LP>(Vv, id.x), v2 = ldl3<LP>(Vv, id.y);
 	float3 dx = x1 - x2;
 	float L = len3(dx);
 	float blk[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -366,11 +387,11 @@ __device__ __forceinline__ void spring_element(const DevBody& B, int s, const St
 	{
 		float3 n = f3(dx.x / L, dx.y / L, dx.z / L);
 		float ks = B.spr_ks[s], kd = B.spr_kd[s], L0 = B.spr_L0[s];
-		float3 w1 = h * v1 + ld3(B.trans, id.x), w2 = h * v2 + ld3(B.trans, id.y);
+		float3 w1 = h * v1 + ldl3<LP>(B.trans, id.x), w2 = h * v2 + ldl3<LP>(B.trans, id.y);
 		if (!P.first_newton)
 		{
-			w1 = w1 + (ld3(B.x, id.x) - x1);
-			w2 = w2 + (ld3(B.x, id.y) - x2);
+			w1 = w1 + (ldl3<LP>(B.x, id.x) - x1);
+			w2 = w2 + (ldl3<LP>(B.x, id.y) - x2);
 		}
 		float3 dw = w1 - w2;
 		if (ks > 0.0f && L > L0)
@@ -448,7 +469,7 @@ __device__ __forceinline__ TV* vp(void* p) { return (TV*)p; }
 // (sparse_force_solver.cpp:165-174), S = I for dynamic vertices and 0 otherwise
 // (force_solver.cpp:110-129). Also forms the Jacobi preconditioner and, when init_pcg is set
 // (initial guess zero), r = pb, s = M^-1 r, d = s; returns this row's r.s.
-template <class TA, class TV>
+template <class TA, class TV, class L = LdPlain>
 __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int lane, const StepParams& P,
                                                bool init_pcg)
 {
@@ -463,11 +484,11 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	const float m = B.mass[i];
 	const float Mi = Si ? m : 1.0f;
 	const float damp = B.damping[i];
-	float3 xi = ld3(X, i), vi = ld3(Vv, i), x0 = ld3(B.x, i), v0 = ld3(B.v, i), yi = ld3(B.trans, i);
+	float3 xi = ldl3<L>(X, i), vi = ldl3<L>(Vv, i), x0 = ldl3<L>(B.x, i), v0 = ldl3<L>(B.v, i), yi = ldl3<L>(B.trans, i);
 	float3 wi = (x0 - xi) + h * vi + yi;
 
 	// vertex terms of b: M (v0 - v) + h (fe + m g + damping force)
-	float3 fe = ld3(B.fext, i);
+	float3 fe = ldl3<L>(B.fext, i);
 	if (Si) fe = fe + m * f3(B.gravity[0], B.gravity[1], B.gravity[2]);
 	float3 fi = f3(0, 0, 0);
 	float diagExtra = Mi;
@@ -529,11 +550,11 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	float3 bi = Mi * (v0 - vi) + h * (fe + fi);
 	// contact dfdx w term: h dfdx w = -h Kc w
 	bi = bi - h * mv9(Kc, wi);
-	for (uint32_t t = B.vt_ptr[i]; t < B.vt_ptr[i + 1]; ++t) bi = bi + ld3(B.tet_bc, B.vt_list[t]);
+	for (uint32_t t = B.vt_ptr[i]; t < B.vt_ptr[i + 1]; ++t) bi = bi + ldl3<L>(B.tet_bc, B.vt_list[t]);
 	for (uint32_t t = B.vb_ptr[i]; t < B.vb_ptr[i + 1]; ++t)
 	{
 		uint32_t e = B.vb_list[t];
-		float3 c = ld3(B.bvec, e >> 1);
+		float3 c = ldl3<L>(B.bvec, e >> 1);
 		bi = (e & 1) ? bi - c : bi + c;
 	}
 
@@ -547,8 +568,8 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		{
 			uint32_t code = B.tet_clist[t];
 			uint32_t e = code >> 4, la = (code >> 2) & 3u, lb = code & 3u;
-			float4 ua = B.tet_rec[4 * (size_t)e + la];
-			float4 ub = B.tet_rec[4 * (size_t)e + lb];
+			float4 ua = L::ld(B.tet_rec + 4 * (size_t)e + la);
+			float4 ub = L::ld(B.tet_rec + 4 * (size_t)e + lb);
 			float ratio = ua.w;
 			float uab = ua.x * ub.x + ua.y * ub.y + ua.z * ub.z;
 			float A3[3] = {ua.x, ua.y, ua.z}, B3[3] = {ub.x, ub.y, ub.z};
@@ -561,16 +582,9 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		{
 			uint32_t code = B.blk_clist[t];
 			const float* blk = B.blocks + 9 * (size_t)(code >> 1);
-			if (code & 1)
-			{
+			const float sgn = (code & 1) ? -1.0f : 1.0f;
 #pragma unroll
-				for (int q = 0; q < 9; ++q) a[q] -= blk[q];
-			}
-			else
-			{
-#pragma unroll
-				for (int q = 0; q < 9; ++q) a[q] += blk[q];
-			}
+			for (int q = 0; q < 9; ++q) a[q] += sgn * L::ld(blk + q);
 		}
 		const bool Sj = B.type[j] == B3G_DYNAMIC;
 		if (k == 0)
@@ -665,10 +679,10 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 }
 
 // q_i = (A x)_i for row i over a SELL-32 slice; TA = block storage, TV = vector type.
-template <class TA, class TV>
-__device__ __forceinline__ void spmv_row(const TA* __restrict__ A, const int* __restrict__ col,
+template <class TA, class TV, class L = LdPlain>
+__device__ __forceinline__ void spmv_row(const TA* A, const int* __restrict__ col,
                                          const uint8_t* __restrict__ rowlen, int nslots, int base, int w,
-                                         int lane, int i, const TV* __restrict__ x, int np, TV out[3])
+                                         int lane, int i, const TV* x, int np, TV out[3])
 {
 	typedef typename Acc<TA>::type AT;
 	AT o0 = 0, o1 = 0, o2 = 0;
@@ -679,10 +693,10 @@ __device__ __forceinline__ void spmv_row(const TA* __restrict__ A, const int* __
 		if (k >= len) break;
 		const int slot = base + k * kSlice + lane;
 		const int j = __ldg(col + slot);
-		AT x0 = (AT)x[j], x1 = (AT)x[np + j], x2 = (AT)x[2 * np + j];
-		AT a0 = widen(A[slot]), a1 = widen(A[(size_t)nslots + slot]), a2 = widen(A[2 * (size_t)nslots + slot]);
-		AT a3 = widen(A[3 * (size_t)nslots + slot]), a4 = widen(A[4 * (size_t)nslots + slot]), a5 = widen(A[5 * (size_t)nslots + slot]);
-		AT a6 = widen(A[6 * (size_t)nslots + slot]), a7 = widen(A[7 * (size_t)nslots + slot]), a8 = widen(A[8 * (size_t)nslots + slot]);
+		AT x0 = (AT)L::ld(x + j), x1 = (AT)L::ld(x + np + j), x2 = (AT)L::ld(x + 2 * np + j);
+		AT a0 = widen(L::ld(A + slot)), a1 = widen(L::ld(A + (size_t)nslots + slot)), a2 = widen(L::ld(A + 2 * (size_t)nslots + slot));
+		AT a3 = widen(L::ld(A + 3 * (size_t)nslots + slot)), a4 = widen(L::ld(A + 4 * (size_t)nslots + slot)), a5 = widen(L::ld(A + 5 * (size_t)nslots + slot));
+		AT a6 = widen(L::ld(A + 6 * (size_t)nslots + slot)), a7 = widen(L::ld(A + 7 * (size_t)nslots + slot)), a8 = widen(L::ld(A + 8 * (size_t)nslots + slot));
 		o0 += a0 * x0 + a1 * x1 + a2 * x2;
 		o1 += a3 * x0 + a4 * x1 + a5 * x2;
 		o2 += a6 * x0 + a7 * x1 + a8 * x2;
@@ -693,7 +707,7 @@ __device__ __forceinline__ void spmv_row(const TA* __restrict__ A, const int* __
 }
 
 // M^-1 r for one row (scalar or block Jacobi)
-template <class TV>
+template <class TV, class L = LdPlain>
 __device__ __forceinline__ void precond_row(const DevBody& B, int i, const TV r[3], TV s[3])
 {
 	const TV* M = (const TV*)B.Minv;
@@ -702,14 +716,105 @@ __device__ __forceinline__ void precond_row(const DevBody& B, int i, const TV r[
 	{
 #pragma unroll
 		for (int a = 0; a < 3; ++a)
-			s[a] = M[(size_t)(3 * a) * np + i] * r[0] + M[(size_t)(3 * a + 1) * np + i] * r[1] + M[(size_t)(3 * a + 2) * np + i] * r[2];
+			s[a] = L::ld(M + (size_t)(3 * a) * np + i) * r[0] + L::ld(M + (size_t)(3 * a + 1) * np + i) * r[1] +
+			       L::ld(M + (size_t)(3 * a + 2) * np + i) * r[2];
 	}
 	else
 	{
-		s[0] = M[i] * r[0];
-		s[1] = M[np + i] * r[1];
-		s[2] = M[2 * np + i] * r[2];
+		s[0] = L::ld(M + i) * r[0];
+		s[1] = L::ld(M + np + i) * r[1];
+		s[2] = L::ld(M + 2 * np + i) * r[2];
 	}
+}
+
+// sphere_shape_contact.cpp:145-189 ApplyFriction for vertex i (velocity only)
+__device__ __forceinline__ void apply_friction(const DevBody& B, int i, float h, float3& v)
+{
+	for (int k = 0; k < B.nw; ++k)
+	{
+		const int c = i * B.nw + k;
+		if (!B.c_exists[c] || !B.c_apply[c]) continue;
+		float3 normal = ld3(B.c_normal, c);
+		float nf = B.c_nf[c];
+		// vec3.h:255 b3Perp
+		const float sqrt_inv3 = sqrtf(1.0f / 3.0f);
+		float3 t1 = fabsf(normal.x) >= sqrt_inv3 ? f3(normal.y, -normal.x, 0.0f) : f3(0.0f, normal.z, -normal.y);
+		t1 = normalize3(t1);
+		float3 t2 = cross3(t1, normal);
+		float im1 = B.invmass[i];
+		float fr = sqrtf(B.sfric[i] * B.wfric[k]);
+		float tm = im1 > 0.0f ? 1.0f / im1 : 0.0f;
+		float cx = dot3(v, t1), cy = dot3(v, t2);
+		float ix = tm * -cx, iy = tm * -cy;
+		float maxImp = fr * (h * nf);
+		if (ix * ix + iy * iy > maxImp * maxImp)
+		{
+			float l = sqrtf(ix * ix + iy * iy);
+			if (l > kFltEps)
+			{
+				ix /= l;
+				iy /= l;
+			}
+			ix *= maxImp;
+			iy *= maxImp;
+		}
+		float3 Pimp = ix * t1 + iy * t2;
+		v = v + im1 * Pimp;
+	}
+}
+
+// contact_manager.cpp:65-82 FindNewContacts for vertex i at its new position
+__device__ __forceinline__ void find_new_contacts(const DevBody& B, int i, float3 x)
+{
+	if (B.type[i] != B3G_DYNAMIC) return;
+	for (int k = 0; k < B.nw; ++k)
+	{
+		const int c = i * B.nw + k;
+		if (B.c_exists[c]) continue;
+		if (aabb_overlap(x, B.srad[i], B.world[k]))
+		{
+			B.c_exists[c] = 1;
+			B.c_nf[c] = 0.0f;
+			B.c_apply[c] = 0;
+		}
+	}
+}
+
+// v = v + dv, x = x0 + h v + y (sparse_force_solver.cpp:194-200); returns |dv|^2 of the vertex.
+// finish != 0 also ends the step: friction, clearing of external forces and translations, new
+// contacts (body.cpp:572-603), and writes the state instead of the Newton iterate.
+template <class TV, class L = LdPlain>
+__device__ __forceinline__ double final_vertex(const DevBody& B, int i, float h, bool first_newton, bool finish)
+{
+	const int np = B.npad;
+	const TV* py = (const TV*)B.py;
+	float3 dv = f3((float)L::ld(py + i), (float)L::ld(py + np + i), (float)L::ld(py + 2 * np + i));
+	float3 v = ldl3<L>(first_newton ? B.v : B.vi, i) + dv;
+	float3 x = ldl3<L>(B.x, i) + h * v + ldl3<L>(B.trans, i);
+	if (finish)
+	{
+		if (B.contacts) apply_friction(B, i, h, v);
+		st3(B.fext, i, f3(0, 0, 0));
+		st3(B.trans, i, f3(0, 0, 0));
+		if (B.contacts) find_new_contacts(B, i, x);
+	}
+	st3(finish ? B.x : B.xi, i, x);
+	st3(finish ? B.v : B.vi, i, v);
+	return (double)dv.x * dv.x + (double)dv.y * dv.y + (double)dv.z * dv.z;
+}
+
+// finish a multi-Newton step for vertex i: iterate -> state, friction, clearing, new contacts
+template <class L = LdPlain>
+__device__ __forceinline__ void post_vertex(const DevBody& B, int i, float h)
+{
+	float3 v = ldl3<L>(B.vi, i);
+	float3 x = ldl3<L>(B.xi, i);
+	if (B.contacts) apply_friction(B, i, h, v);
+	st3(B.fext, i, f3(0, 0, 0));
+	st3(B.trans, i, f3(0, 0, 0));
+	if (B.contacts) find_new_contacts(B, i, x);
+	st3(B.x, i, x);
+	st3(B.v, i, v);
 }
 
 // ------------------------------------------------------------------ reductions

@@ -54,6 +54,8 @@ struct Scalars
 	unsigned counter;  // arrival counter of the deterministic grid reduction (plain path)
 	int pending_check; // bf16 mode: recursive residual met the tolerance, confirm with a refresh
 	int pad;
+	unsigned long long total_iters;  // PCG iterations of every step since creation
+	unsigned long long total_steps;
 };
 
 // Everything a kernel needs about one body. Passed by value to the per-op kernels and read

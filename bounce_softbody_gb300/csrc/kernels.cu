@@ -354,88 +354,15 @@ __global__ void __launch_bounds__(kThreads) k_direction(DevBody B)
 	}
 }
 
-// sphere_shape_contact.cpp:145-189 ApplyFriction for vertex i (velocity only)
-__device__ void apply_friction(const DevBody& B, int i, float h, float3& v)
-{
-	for (int k = 0; k < B.nw; ++k)
-	{
-		const int c = i * B.nw + k;
-		if (!B.c_exists[c] || !B.c_apply[c]) continue;
-		float3 normal = ld3(B.c_normal, c);
-		float nf = B.c_nf[c];
-		// vec3.h:255 b3Perp
-		const float sqrt_inv3 = sqrtf(1.0f / 3.0f);
-		float3 t1 = fabsf(normal.x) >= sqrt_inv3 ? f3(normal.y, -normal.x, 0.0f) : f3(0.0f, normal.z, -normal.y);
-		t1 = normalize3(t1);
-		float3 t2 = cross3(t1, normal);
-		float im1 = B.invmass[i];
-		float fr = sqrtf(B.sfric[i] * B.wfric[k]);
-		float tm = im1 > 0.0f ? 1.0f / im1 : 0.0f;
-		float cx = dot3(v, t1), cy = dot3(v, t2);
-		float ix = tm * -cx, iy = tm * -cy;
-		float maxImp = fr * (h * nf);
-		if (ix * ix + iy * iy > maxImp * maxImp)
-		{
-			float l = sqrtf(ix * ix + iy * iy);
-			if (l > kFltEps)
-			{
-				ix /= l;
-				iy /= l;
-			}
-			ix *= maxImp;
-			iy *= maxImp;
-		}
-		float3 Pimp = ix * t1 + iy * t2;
-		v = v + im1 * Pimp;
-	}
-}
-
-// contact_manager.cpp:65-82 FindNewContacts for vertex i at its new position
-__device__ void find_new_contacts(const DevBody& B, int i, float3 x)
-{
-	if (B.type[i] != B3G_DYNAMIC) return;
-	for (int k = 0; k < B.nw; ++k)
-	{
-		const int c = i * B.nw + k;
-		if (B.c_exists[c]) continue;
-		if (aabb_overlap(x, B.srad[i], B.world[k]))
-		{
-			B.c_exists[c] = 1;
-			B.c_nf[c] = 0.0f;
-			B.c_apply[c] = 0;
-		}
-	}
-}
-
 // v = v + dv, x = x0 + h v + y, Newton error |dv|^2 (sparse_force_solver.cpp:194-223).
 // mode 1 also finishes the step: friction, clearing of external forces and translations,
 // new contacts (body.cpp:572-603).
 template <class TV>
 __global__ void __launch_bounds__(kThreads) k_final(DevBody B, StepParams P, int mode)
 {
-	const int np = B.npad;
-	const TV* py = (const TV*)B.py;
-	const float h = P.h;
-	const float* Vit = P.first_newton ? B.v : B.vi;
-	float* vout = mode == 1 ? B.v : B.vi;
-	float* xout = mode == 1 ? B.x : B.xi;
 	double part = 0.0;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
-	{
-		float3 dv = f3((float)py[i], (float)py[np + i], (float)py[2 * np + i]);
-		float3 v = ld3(Vit, i) + dv;
-		float3 x = ld3(B.x, i) + h * v + ld3(B.trans, i);
-		part += (double)dv.x * dv.x + (double)dv.y * dv.y + (double)dv.z * dv.z;
-		if (mode == 1)
-		{
-			if (B.contacts) apply_friction(B, i, h, v);
-			st3(B.fext, i, f3(0, 0, 0));
-			st3(B.trans, i, f3(0, 0, 0));
-			if (B.contacts) find_new_contacts(B, i, x);
-		}
-		st3(xout, i, x);
-		st3(vout, i, v);
-	}
+		part += final_vertex<TV>(B, i, P.h, P.first_newton != 0, mode == 1);
 	double total;
 	if (grid_reduce(part, B.partials, &B.sc->counter, &total))
 	{
@@ -449,22 +376,15 @@ __global__ void __launch_bounds__(kThreads) k_final(DevBody B, StepParams P, int
 		if (sc->newton_iter == 0) sc->newton_done = total <= sc->newton_tol2 ? 1 : 0;
 		else sc->newton_done = total <= sc->newton_tol2 * sc->newton_err0 ? 1 : 0;
 		sc->newton_iter += 1;
+		sc->total_iters += (unsigned long long)it;
+		if (mode == 1) sc->total_steps += 1ull;
 	}
 }
 
 __global__ void __launch_bounds__(kThreads) k_post(DevBody B, float h)
 {
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
-	{
-		float3 v = ld3(B.vi, i);
-		float3 x = ld3(B.xi, i);
-		if (B.contacts) apply_friction(B, i, h, v);
-		st3(B.fext, i, f3(0, 0, 0));
-		st3(B.trans, i, f3(0, 0, 0));
-		if (B.contacts) find_new_contacts(B, i, x);
-		st3(B.x, i, x);
-		st3(B.v, i, v);
-	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) B.sc->total_steps += 1ull;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x) post_vertex(B, i, h);
 }
 
 __global__ void __launch_bounds__(kThreads) k_nostep(DevBody B)

@@ -37,20 +37,29 @@ cudaError_t op_nostep(const DevBody& B, cudaStream_t st);
 // clear a float array on the device
 cudaError_t op_fill_f32(float* p, size_t count, float value, cudaStream_t st);
 
-// Persistent batch kernel: all bodies in `bodies` (device array) step `steps` times.
-struct BatchLaunch
+// Persistent batch kernel: every body listed in `big` (teams of `cluster` CTAs) and in `small`
+// (one CTA each) steps `steps` times in one launch.
+struct BatchArgs
 {
-	const DevBody* bodies;   // device array
-	const int* order;        // device array: body index per work item, grouped by size bucket
-	int count;
+	const DevBody* bodies;   // device array of all bodies of the batch
+	const int* big;          // device array: indices of bodies stepped by whole clusters
+	int nbig;
+	const int* small;        // device array: indices of bodies stepped by single CTAs
+	int nsmall;
+	unsigned* queue;         // device: two work counters, cleared by op_batch
 	int steps;
 	float h;
-	int prec;
 	int newton;
-	int cluster;             // CTAs per team (1, 2, 4, 8, 16)
-	int ctas;                // total CTAs of the launch (multiple of cluster)
+	int max_iter;
+	double tol2;
+	int refresh;
+	double newton_tol2;
+	int prec;
+	int cluster;             // CTAs per cluster: 1, 2, 4 or 8
+	int ctas;                // CTAs of the launch (multiple of cluster)
 };
-
-
+cudaError_t op_batch(const BatchArgs& A, cudaStream_t st);
+// Co-resident clusters of the batch kernel for this precision and cluster size (0 on error).
+int batch_max_clusters(int prec, int cluster);
 
 } // namespace b3g

@@ -148,6 +148,8 @@ typedef struct b3g_step_stats
 	int32_t solve_status;          /* b3g_solve_status of the last PCG solve */
 	double residual_ratio;         /* sqrt(delta / delta0) at exit of the last PCG solve */
 	double newton_error;           /* |dv|^2 of the last Newton iteration */
+	uint64_t total_pcg_iterations; /* PCG iterations of every step since the body was created */
+	uint64_t total_steps;          /* steps with dt > 0 since the body was created */
 } b3g_step_stats;
 
 B3G_API void b3g_solver_config_default(b3g_solver_config* config);
@@ -177,6 +179,18 @@ B3G_API int b3g_body_step(b3g_body* body, float dt, const b3g_solver_config* con
  * last step's statistics of each body (count entries) and makes the call wait. */
 B3G_API int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float dt,
                    const b3g_solver_config* config, uint32_t steps, b3g_step_stats* stats);
+
+/* Schedule of the context's current batch: cluster size, size threshold of cluster-stepped bodies
+ * (-1 = none), bodies stepped by clusters, CTAs per launch, autotuned (0/1), number of timed
+ * candidates, then (candidate code = cluster * 1e6 + threshold, microseconds) per candidate. */
+B3G_API int b3g_batch_schedule(b3g_context* ctx, int32_t* out, uint32_t capacity);
+
+/* Host-buffer transfers for a list of bodies of one context; the host arrays are the bodies'
+ * arrays concatenated in list order (3 floats per vertex). Pinned host memory makes them
+ * asynchronous copies; get waits for the copies. */
+B3G_API int b3g_batch_apply_forces(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, const float* forces);
+B3G_API int b3g_batch_get_state(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float* positions,
+                                float* velocities);
 
 /* Host <-> device state transfer (3 floats per vertex each; either pointer may be NULL). */
 B3G_API int b3g_body_get_state(b3g_body* body, float* positions, float* velocities);

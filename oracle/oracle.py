@@ -87,6 +87,9 @@ def _lib(kind: str, bits: int):
             lib = C.CDLL(path)
             lib.b3o_simulate.argtypes = [C.POINTER(_Desc), C.POINTER(_Run)]
             lib.b3o_simulate.restype = C.c_int
+            lib.b3o_simulate_batch.argtypes = [C.POINTER(_Desc), C.POINTER(_Run), C.c_uint32, C.c_uint32,
+                                               C.POINTER(C.c_double)]
+            lib.b3o_simulate_batch.restype = C.c_int
         elif kind == "ref":
             path = os.path.join(REFOUT, f"libb3ref{bits}.so")
             if not os.path.exists(path):
@@ -180,3 +183,37 @@ def simulate(body, steps: int, dt: float = 1.0 / 60.0, newton_iters: int = 1, ma
         raise RuntimeError(f"oracle {kind}{bits} failed with {rc}")
     del keep
     return x, v, it[:steps].copy(), float(sec[0])
+
+
+def simulate_batch(bodies, steps: int, dt: float = 1.0 / 60.0, newton_iters: int = 1, max_sub: int = 200,
+                   sub_tol: float = 1e-5, bits: int = 32, threads: int = 0):
+    """Step independent bodies on `threads` host threads with the restatement.
+
+    Returns (xs, vs, iters, step_seconds); step_seconds covers the stepping phase only (the bodies
+    are built before the clock starts)."""
+    lib = _lib("port", bits)
+    threads = threads or (os.cpu_count() or 1)
+    count = len(bodies)
+    descs = (_Desc * count)()
+    runs = (_Run * count)()
+    keep = []
+    outs = []
+    for k, body in enumerate(bodies):
+        d, kk = _make_desc(body)
+        keep.append(kk)
+        descs[k] = d
+        x = np.zeros((body.n, 3))
+        v = np.zeros((body.n, 3))
+        it = np.zeros(max(steps, 1), np.uint32)
+        outs.append((x, v, it))
+        r = runs[k]
+        r.steps, r.dt, r.newton_iters, r.max_sub, r.sub_tol, r.use_body_step = steps, dt, newton_iters, max_sub, sub_tol, 0
+        r.x_out, r.v_out = x.ctypes.data_as(_dp), v.ctypes.data_as(_dp)
+        r.sub_iters_out = it.ctypes.data_as(_up)
+        r.seconds_out = C.cast(None, _dp)
+    sec = C.c_double(0.0)
+    rc = lib.b3o_simulate_batch(descs, runs, count, threads, C.byref(sec))
+    if rc != 0:
+        raise RuntimeError(f"oracle batch failed with {rc}")
+    del keep
+    return [o[0] for o in outs], [o[1] for o in outs], [o[2][:steps] for o in outs], float(sec.value)

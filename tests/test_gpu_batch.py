@@ -1,0 +1,92 @@
+"""The persistent batch kernel (b3g_step_batch) against the per-body path and the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from bounce_softbody_gb300 import b3g, meshes
+
+pytestmark = pytest.mark.gpu
+
+DT = 1.0 / 60.0
+
+
+def small_batch(count=20, lo=4, hi=11, seed=11):
+    return meshes.batch_bodies(count=count, lo=lo, hi=hi, seed=seed)
+
+
+def disp_rel(x, xr, x0):
+    return float(np.linalg.norm(np.asarray(x, np.float64) - xr) / max(np.linalg.norm(xr - x0), 1e-30))
+
+
+def test_batch_matches_single_body_path(ctx):
+    """Each body of a batch ends where the per-op single-body path takes it (5 steps)."""
+    descs = small_batch()
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    batch = [b3g.Body(ctx, d) for d in descs]
+    alone = [b3g.Body(ctx, d) for d in descs]
+    for _ in range(5):
+        st = b3g.step_batch(ctx, batch, DT, 1, cfg)
+        for b in alone:
+            b.step(DT, cfg, stats=False)
+    for k, d in enumerate(descs):
+        xb, vb = batch[k].state()
+        xa, va = alone[k].state()
+        assert disp_rel(xb, xa.astype(np.float64), d.x) < 1e-5, d.name
+        assert np.linalg.norm(vb - va) <= 1e-4 * max(np.linalg.norm(va), 1e-12), d.name
+        assert st[k]["solve_status"] in ("converged", "max_iterations")
+
+
+def test_batch_matches_oracle(ctx):
+    descs = small_batch(count=6, seed=5)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    bodies = [b3g.Body(ctx, d) for d in descs]
+    st = b3g.step_batch(ctx, bodies, DT, 10, cfg)
+    for k, d in enumerate(descs):
+        x, v = bodies[k].state()
+        xr, vr, it, _ = oracle.simulate(d, 10, kind="port", bits=64)
+        assert disp_rel(x, xr, d.x) < 1e-4, d.name
+        assert np.linalg.norm(v - vr) < 1e-3 * np.linalg.norm(vr), d.name
+        assert abs(st[k]["pcg_iterations"] - int(it[-1])) <= 3
+        assert st[k]["total_steps"] == 10
+
+
+@pytest.mark.parametrize("schedule", ["2,8192", "4,8192", "8,8192"])
+def test_batch_cluster_teams_match_single_body_path(ctx, schedule, monkeypatch):
+    """Bodies above the cluster threshold are stepped by clusters of CTAs (DSMEM reductions)."""
+    monkeypatch.setenv("B3G_BATCH_SCHEDULE", schedule)
+    descs = [meshes.tet_grid(28, 26, 24, seed=3, E=3e5, nu=0.35, pin="x0", name="big0"),
+             meshes.tet_grid(26, 25, 27, seed=4, E=8e4, nu=0.25, pin="z1", name="big1")]
+    descs += small_batch(count=6, seed=8)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    batch = [b3g.Body(ctx, d) for d in descs]
+    alone = [b3g.Body(ctx, d) for d in descs]
+    for _ in range(3):
+        b3g.step_batch(ctx, batch, DT, 1, cfg)
+        for b in alone:
+            b.step(DT, cfg, stats=False)
+    sched = b3g.batch_schedule(ctx)
+    assert sched["cluster"] == int(schedule.split(",")[0]) and sched["cluster_bodies"] == 2
+    for k, d in enumerate(descs):
+        xb, vb = batch[k].state()
+        xa, va = alone[k].state()
+        assert disp_rel(xb, xa.astype(np.float64), d.x) < 1e-5, d.name
+        assert np.linalg.norm(vb - va) <= 1e-4 * max(np.linalg.norm(va), 1e-12), d.name
+
+
+@pytest.mark.parametrize("cluster_env", ["0"])
+def test_batch_is_deterministic(ctx, cluster_env, monkeypatch):
+    """Two batches from the same state give bitwise equal states (no float atomics)."""
+    monkeypatch.setenv("B3G_AUTOTUNE", cluster_env)
+    descs = small_batch(count=8, seed=21)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    out = []
+    for _ in range(2):
+        bodies = [b3g.Body(ctx, d) for d in descs]
+        b3g.step_batch(ctx, bodies, DT, 4, cfg)
+        out.append([b.state() for b in bodies])
+        for b in bodies:
+            b.close()
+    for (x1, v1), (x2, v2) in zip(out[0], out[1]):
+        assert np.array_equal(x1, x2) and np.array_equal(v1, v2)
