@@ -266,8 +266,14 @@ def ours(args, world, rank, local, pg):
     nverts = sum(i["vertices"] for i in infos)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
 
+    single = args.workload != "batch"
+
     def step_once():
-        b3g.step_batch(ctx, bodies, dt, 1, scfg, stats=False)
+        if single:
+            # one body: the per-op kernels of the single-body path (grid-wide SpMV / reductions)
+            bodies[0].step(dt, scfg, stats=False)
+        else:
+            b3g.step_batch(ctx, bodies, dt, 1, scfg, stats=False)
 
     for _ in range(max(args.warmup, 3)):
         step_once()
@@ -301,10 +307,10 @@ def ours(args, world, rank, local, pg):
             "traffic": None, "kernel": "k_batch (persistent, one launch per step)",
             "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_step": alg / args.steps,
             "pcg_iterations_per_step_mean": float(np.mean(iters)) / args.steps if iters else 0.0}
-    sched = b3g.batch_schedule(ctx) if args.workload == "batch" else None
+    sched = b3g.batch_schedule(ctx) if not single else None
 
     extras = {}
-    if not args.no_extras and rank == 0:
+    if not args.no_extras and rank == 0 and not single:
         # e2e through the C ABI with pinned host buffers: H2D external forces, step, D2H x and v
         f_h = torch.zeros(3 * nverts, dtype=torch.float32).pin_memory()
         x_h = torch.empty(3 * nverts, dtype=torch.float32).pin_memory()
@@ -343,7 +349,15 @@ def ours(args, world, rank, local, pg):
                                   "sample": f"{len(cs)} of {len(descs)} bodies ({sum(d.n for d in cs)} vertices), "
                                             f"1 step, oracle C restatement FP32, {csec:.2f} s"}
 
-    launches = args.steps  # one persistent kernel per step (graph: memset node + kernel node)
+    # batch: one persistent kernel per step (graph: memset node + kernel node); single body:
+    # begin + elements + assembly + 4 per PCG iteration (launched in chunks of 8) + final
+    if single:
+        chunks = [-(-int(it) // 8) * 8 for it in iters]
+        launches = int(args.steps * 4 + 4 * sum(chunks) + (args.steps if infos[0]["tris"] else 0)
+                       + (args.steps if infos[0]["springs"] else 0))
+        roof["kernel"] = "k_spmv_dot (per-op path)"
+    else:
+        launches = args.steps
     line = {"metric": METRIC, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "fp64": "f64", "bf16": "bf16+f32"}[args.precision],

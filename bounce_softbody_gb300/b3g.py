@@ -83,6 +83,7 @@ SIGNATURES = {
     "b3g_step_batch": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.c_float,
                                  C.POINTER(SolverConfig), C.c_uint32, C.POINTER(StepStats)]),
     "b3g_batch_schedule": (C.c_int, [C.c_void_p, _ip, C.c_uint32]),
+    "b3g_batch_phase_cycles": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int]),
     "b3g_batch_apply_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp]),
     "b3g_batch_get_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp, _fp]),
     "b3g_body_get_state": (C.c_int, [C.c_void_p, _fp, _fp]),
@@ -342,3 +343,12 @@ def batch_get_state(ctx: Context, bodies: Sequence[Body], x_ptr: int, v_ptr: int
     arr = (C.c_void_p * len(bodies))(*[b.handle for b in bodies])
     _check(load_library().b3g_batch_get_state(ctx.handle, arr, len(bodies), C.cast(x_ptr, _fp), C.cast(v_ptr, _fp)),
            "b3g_batch_get_state")
+
+
+PHASES = ["elements", "assembly", "spmv", "update", "direction", "final", "-", "-"]
+
+
+def batch_phase_cycles(ctx: Context, reset: bool = True) -> dict:
+    a = (C.c_uint64 * 8)()
+    _check(load_library().b3g_batch_phase_cycles(ctx.handle, a, 1 if reset else 0), "b3g_batch_phase_cycles")
+    return {PHASES[k]: int(a[k]) for k in range(6)}

@@ -34,7 +34,8 @@ def _flags(src: str) -> list[str]:
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "-I", os.path.join(HERE, "..", "include")]
     if src.endswith(".cu"):
-        return common + ARCH + ["-lineinfo", "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
+        extra = os.environ.get("B3G_NVCC_FLAGS", "").split()
+        return common + ARCH + ["-lineinfo", "-Xptxas", "-O3", "--expt-relaxed-constexpr"] + extra
     return common
 
 

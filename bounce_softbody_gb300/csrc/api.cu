@@ -491,14 +491,18 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 		D.col = C.take<int>(P.nslots);
 		D.rowlen = C.take<uint8_t>(np);
 		D.A32 = C.take<float>(9 * (size_t)P.nslots);
-		D.tet_cptr = C.take<uint32_t>(P.nslots + 1);
-		D.tet_clist = C.take<uint32_t>(P.tet_ccount);
-		D.blk_cptr = C.take<uint32_t>(P.nslots + 1);
-		D.blk_clist = C.take<uint32_t>(P.blk_ccount);
-		D.vt_ptr = C.take<uint32_t>(n + 1);
-		D.vt_list = C.take<uint32_t>(4 * (size_t)b->nt);
-		D.vb_ptr = C.take<uint32_t>(n + 1);
-		D.vb_list = C.take<uint32_t>(3 * (size_t)b->ntr + 2 * (size_t)b->ns);
+		D.tet_cstart = C.take<uint32_t>(P.tet.items);
+		D.tet_ccnt = C.take<uint16_t>(P.tet.items);
+		D.tet_clist = C.take<uint32_t>(P.tet.len);
+		D.blk_cstart = C.take<uint32_t>(P.blk.items);
+		D.blk_ccnt = C.take<uint16_t>(P.blk.items);
+		D.blk_clist = C.take<uint32_t>(P.blk.len);
+		D.vt_start = C.take<uint32_t>(P.vt.items);
+		D.vt_cnt = C.take<uint16_t>(P.vt.items);
+		D.vt_list = C.take<uint32_t>(P.vt.len);
+		D.vb_start = C.take<uint32_t>(P.vb.items);
+		D.vb_cnt = C.take<uint16_t>(P.vb.items);
+		D.vb_list = C.take<uint32_t>(P.vb.len);
 		D.x = C.take<float>(3 * (size_t)n);
 		D.v = C.take<float>(3 * (size_t)n);
 		D.fext = C.take<float>(3 * (size_t)n);
@@ -596,14 +600,15 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	up(D.slice_ptr, P.slice_ptr, (P.nslices + 1) * sizeof(int));
 	up(D.col, P.col, P.nslots * sizeof(int));
 	up(D.rowlen, P.rowlen, np);
-	up(D.tet_cptr, P.tet_cptr, (P.nslots + 1) * sizeof(uint32_t));
-	up(D.tet_clist, P.tet_clist, P.tet_ccount * sizeof(uint32_t));
-	up(D.blk_cptr, P.blk_cptr, (P.nslots + 1) * sizeof(uint32_t));
-	up(D.blk_clist, P.blk_clist, P.blk_ccount * sizeof(uint32_t));
-	up(D.vt_ptr, P.vt_ptr, (n + 1) * sizeof(uint32_t));
-	up(D.vt_list, P.vt_list, 4 * (size_t)b->nt * sizeof(uint32_t));
-	up(D.vb_ptr, P.vb_ptr, (n + 1) * sizeof(uint32_t));
-	up(D.vb_list, P.vb_list, (3 * (size_t)b->ntr + 2 * (size_t)b->ns) * sizeof(uint32_t));
+	auto up_lists = [&](const uint32_t* ds, const uint16_t* dc, const uint32_t* dl, const Pattern::Lists& L) {
+		up(ds, L.start, L.items * sizeof(uint32_t));
+		up(dc, L.cnt, L.items * sizeof(uint16_t));
+		up(dl, L.list, L.len * sizeof(uint32_t));
+	};
+	up_lists(D.tet_cstart, D.tet_ccnt, D.tet_clist, P.tet);
+	up_lists(D.blk_cstart, D.blk_ccnt, D.blk_clist, P.blk);
+	up_lists(D.vt_start, D.vt_cnt, D.vt_list, P.vt);
+	up_lists(D.vb_start, D.vb_cnt, D.vb_list, P.vb);
 	up(D.x, d->positions, 3 * (size_t)n * sizeof(float));
 	up(D.v, d->velocities ? (const void*)d->velocities : (const void*)zeros3.data(), 3 * (size_t)n * sizeof(float));
 	up(D.mass, b->h_mass.data(), n * sizeof(float));

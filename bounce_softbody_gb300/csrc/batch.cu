@@ -44,6 +44,7 @@ struct BatchCache
 	int g_steps = 0, g_newton = 0, g_max_iter = 0, g_refresh = 0;
 	double g_tol2 = 0.0, g_ntol2 = 0.0;
 	std::vector<std::pair<int, double>> tune_log;  // (cluster * 1e6 + threshold, ms)
+	unsigned long long* d_prof = nullptr;          // phase cycle counters when B3G_PHASE_PROFILE=1
 };
 
 namespace {
@@ -55,6 +56,7 @@ void free_cache(BatchCache* c)
 	cudaFree(c->d_bodies);
 	cudaFree(c->d_order);
 	cudaFree(c->d_queue);
+	cudaFree(c->d_prof);
 	delete c;
 }
 
@@ -84,6 +86,7 @@ BatchArgs make_args(BatchCache* c, float h, int steps, const b3g_solver_config& 
 	A.prec = c->prec;
 	A.cluster = c->cluster;
 	A.ctas = c->ctas;
+	A.prof = c->d_prof;
 	return A;
 }
 
@@ -218,6 +221,13 @@ int build_cache(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, int p
 	{
 		free_cache(c);
 		return cuda_fail(e, "batch setup");
+	}
+	const char* pe = std::getenv("B3G_PHASE_PROFILE");
+	if (pe && pe[0] == '1')
+	{
+		const size_t bytes = 8 * 4096 * sizeof(unsigned long long);
+		if (cudaMalloc(&c->d_prof, bytes) == cudaSuccess) cudaMemset(c->d_prof, 0, bytes);
+		else cudaGetLastError();
 	}
 	// size heuristic: clusters of 4 for bodies of 16k vertices or more
 	int maxn = 0;
@@ -403,4 +413,20 @@ extern "C" int b3g_batch_get_state(b3g_context* ctx, b3g_body* const* bodies, ui
 	}
 	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
 	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch_get_state");
+}
+
+extern "C" int b3g_batch_phase_cycles(b3g_context* ctx, uint64_t out[8], int reset)
+{
+	if (!ctx || !out) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	for (int k = 0; k < 8; ++k) out[k] = 0;
+	BatchCache* c = ctx->batch;
+	if (!c || !c->d_prof) return B3G_OK;
+	std::vector<unsigned long long> h(8 * 4096);
+	cudaError_t e = cudaMemcpyAsync(h.data(), c->d_prof, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+	                                ctx->stream);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+	if (e == cudaSuccess && reset) e = cudaMemsetAsync(c->d_prof, 0, h.size() * sizeof(unsigned long long), ctx->stream);
+	if (e != cudaSuccess) return cuda_fail(e, "phase cycles");
+	for (size_t k = 0; k < h.size(); ++k) out[k % 8] += h[k];
+	return B3G_OK;
 }

@@ -464,6 +464,19 @@ __device__ __forceinline__ bool aabb_overlap(float3 p, float r, float4 sh)
 template <class TV>
 __device__ __forceinline__ TV* vp(void* p) { return (TV*)p; }
 
+// a += (h^2 + h kd) R K0_ab R^T of one tetrahedron from its factored record:
+// ratio u_a u_b^T + u_b u_a^T + (u_a . u_b) I with u = sqrt(c mu) R g and ratio = lambda / mu
+__device__ __forceinline__ void add_tet_block(float a[9], float4 ua, float4 ub)
+{
+	const float ratio = ua.w;
+	const float uab = ua.x * ub.x + ua.y * ub.y + ua.z * ub.z;
+	const float A3[3] = {ua.x, ua.y, ua.z}, B3[3] = {ub.x, ub.y, ub.z};
+#pragma unroll
+	for (int r = 0; r < 3; ++r)
+#pragma unroll
+		for (int c = 0; c < 3; ++c) a[3 * r + c] += ratio * A3[r] * B3[c] + B3[r] * A3[c] + (r == c ? uab : 0.0f);
+}
+
 // Assembles row i of the pre-filtered system: pA = S A S^T + I - S and pb = S b with
 //   A = M - h dfdv - h^2 dfdx,  b = M (v0 - v) + h (fe + fi) + h dfdx (x0 - x + h v + y)
 // (sparse_force_solver.cpp:165-174), S = I for dynamic vertices and 0 otherwise
@@ -550,12 +563,33 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	float3 bi = Mi * (v0 - vi) + h * (fe + fi);
 	// contact dfdx w term: h dfdx w = -h Kc w
 	bi = bi - h * mv9(Kc, wi);
-	for (uint32_t t = B.vt_ptr[i]; t < B.vt_ptr[i + 1]; ++t) bi = bi + ldl3<L>(B.tet_bc, B.vt_list[t]);
-	for (uint32_t t = B.vb_ptr[i]; t < B.vb_ptr[i + 1]; ++t)
 	{
-		uint32_t e = B.vb_list[t];
-		float3 c = ldl3<L>(B.bvec, e >> 1);
-		bi = (e & 1) ? bi - c : bi + c;
+		// tetrahedra's right-hand-side parts of this vertex, four in flight at a time
+		const uint32_t st = __ldg(B.vt_start + i);
+		const int cnt = __ldg(B.vt_cnt + i);
+		int t = 0;
+		for (; t + 4 <= cnt; t += 4)
+		{
+			uint32_t e[4];
+			float3 c[4];
+#pragma unroll
+			for (int u = 0; u < 4; ++u) e[u] = __ldg(B.vt_list + st + kSlice * (t + u));
+#pragma unroll
+			for (int u = 0; u < 4; ++u) c[u] = ldl3<L>(B.tet_bc, e[u]);
+#pragma unroll
+			for (int u = 0; u < 4; ++u) bi = bi + c[u];
+		}
+		for (; t < cnt; ++t) bi = bi + ldl3<L>(B.tet_bc, __ldg(B.vt_list + st + kSlice * t));
+	}
+	{
+		const uint32_t st = __ldg(B.vb_start + i);
+		const int cnt = __ldg(B.vb_cnt + i);
+		for (int t = 0; t < cnt; ++t)
+		{
+			uint32_t e = __ldg(B.vb_list + st + kSlice * t);
+			float3 c = ldl3<L>(B.bvec, e >> 1);
+			bi = (e & 1) ? bi - c : bi + c;
+		}
 	}
 
 	float diag[9];
@@ -564,23 +598,39 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		const int slot = base + k * kSlice + lane;
 		const int j = B.col[slot];
 		float a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-		for (uint32_t t = B.tet_cptr[slot]; t < B.tet_cptr[slot + 1]; ++t)
 		{
-			uint32_t code = B.tet_clist[t];
-			uint32_t e = code >> 4, la = (code >> 2) & 3u, lb = code & 3u;
-			float4 ua = L::ld(B.tet_rec + 4 * (size_t)e + la);
-			float4 ub = L::ld(B.tet_rec + 4 * (size_t)e + lb);
-			float ratio = ua.w;
-			float uab = ua.x * ub.x + ua.y * ub.y + ua.z * ub.z;
-			float A3[3] = {ua.x, ua.y, ua.z}, B3[3] = {ub.x, ub.y, ub.z};
+			// tetrahedron contributions of this slot, four in flight at a time
+			const uint32_t st = __ldg(B.tet_cstart + slot);
+			const int cnt = __ldg(B.tet_ccnt + slot);
+			int t = 0;
+			for (; t + 4 <= cnt; t += 4)
+			{
+				uint32_t code[4];
+				float4 ua[4], ub[4];
 #pragma unroll
-			for (int r = 0; r < 3; ++r)
+				for (int u = 0; u < 4; ++u) code[u] = __ldg(B.tet_clist + st + kSlice * (t + u));
 #pragma unroll
-				for (int c = 0; c < 3; ++c) a[3 * r + c] += ratio * A3[r] * B3[c] + B3[r] * A3[c] + (r == c ? uab : 0.0f);
+				for (int u = 0; u < 4; ++u)
+				{
+					const size_t r0 = 4 * (size_t)(code[u] >> 4);
+					ua[u] = L::ld(B.tet_rec + r0 + ((code[u] >> 2) & 3u));
+					ub[u] = L::ld(B.tet_rec + r0 + (code[u] & 3u));
+				}
+#pragma unroll
+				for (int u = 0; u < 4; ++u) add_tet_block(a, ua[u], ub[u]);
+			}
+			for (; t < cnt; ++t)
+			{
+				const uint32_t code = __ldg(B.tet_clist + st + kSlice * t);
+				const size_t r0 = 4 * (size_t)(code >> 4);
+				add_tet_block(a, L::ld(B.tet_rec + r0 + ((code >> 2) & 3u)), L::ld(B.tet_rec + r0 + (code & 3u)));
+			}
 		}
-		for (uint32_t t = B.blk_cptr[slot]; t < B.blk_cptr[slot + 1]; ++t)
+		const uint32_t bst = __ldg(B.blk_cstart + slot);
+		const int bcnt = __ldg(B.blk_ccnt + slot);
+		for (int t = 0; t < bcnt; ++t)
 		{
-			uint32_t code = B.blk_clist[t];
+			uint32_t code = __ldg(B.blk_clist + bst + kSlice * t);
 			const float* blk = B.blocks + 9 * (size_t)(code >> 1);
 			const float sgn = (code & 1) ? -1.0f : 1.0f;
 #pragma unroll
@@ -679,27 +729,58 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 }
 
 // q_i = (A x)_i for row i over a SELL-32 slice; TA = block storage, TV = vector type.
+// Every lane runs the slice width w (warp-uniform trip count): slots past the end of a row hold
+// zero blocks whose column is a valid vertex, so no per-row bound is needed. The loads of four
+// consecutive blocks (9 planes, column ids, then the gathered x) are issued before their FMAs so
+// each warp keeps about 5 KB of loads in flight.
 template <class TA, class TV, class L = LdPlain>
-__device__ __forceinline__ void spmv_row(const TA* A, const int* __restrict__ col,
-                                         const uint8_t* __restrict__ rowlen, int nslots, int base, int w,
-                                         int lane, int i, const TV* x, int np, TV out[3])
+__device__ __forceinline__ void spmv_row(const TA* A, const int* __restrict__ col, int nslots, int base, int w,
+                                         int lane, const TV* x, int np, TV out[3])
 {
 	typedef typename Acc<TA>::type AT;
 	AT o0 = 0, o1 = 0, o2 = 0;
-	const int len = rowlen[i];
-#pragma unroll 4
-	for (int k = 0; k < w; ++k)
+	const size_t ns = (size_t)nslots;
+	int k = 0;
+	for (; k + 4 <= w; k += 4)
 	{
-		if (k >= len) break;
+		int slot[4], j[4];
+		AT a[4][9], xv[4][3];
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+		{
+			slot[u] = base + (k + u) * kSlice + lane;
+			j[u] = __ldg(col + slot[u]);
+		}
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+#pragma unroll
+			for (int p = 0; p < 9; ++p) a[u][p] = widen(L::ld(A + p * ns + slot[u]));
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+		{
+			xv[u][0] = (AT)L::ld(x + j[u]);
+			xv[u][1] = (AT)L::ld(x + np + j[u]);
+			xv[u][2] = (AT)L::ld(x + 2 * np + j[u]);
+		}
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+		{
+			o0 += a[u][0] * xv[u][0] + a[u][1] * xv[u][1] + a[u][2] * xv[u][2];
+			o1 += a[u][3] * xv[u][0] + a[u][4] * xv[u][1] + a[u][5] * xv[u][2];
+			o2 += a[u][6] * xv[u][0] + a[u][7] * xv[u][1] + a[u][8] * xv[u][2];
+		}
+	}
+	for (; k < w; ++k)
+	{
 		const int slot = base + k * kSlice + lane;
 		const int j = __ldg(col + slot);
+		AT a[9];
+#pragma unroll
+		for (int p = 0; p < 9; ++p) a[p] = widen(L::ld(A + p * ns + slot));
 		AT x0 = (AT)L::ld(x + j), x1 = (AT)L::ld(x + np + j), x2 = (AT)L::ld(x + 2 * np + j);
-		AT a0 = widen(L::ld(A + slot)), a1 = widen(L::ld(A + (size_t)nslots + slot)), a2 = widen(L::ld(A + 2 * (size_t)nslots + slot));
-		AT a3 = widen(L::ld(A + 3 * (size_t)nslots + slot)), a4 = widen(L::ld(A + 4 * (size_t)nslots + slot)), a5 = widen(L::ld(A + 5 * (size_t)nslots + slot));
-		AT a6 = widen(L::ld(A + 6 * (size_t)nslots + slot)), a7 = widen(L::ld(A + 7 * (size_t)nslots + slot)), a8 = widen(L::ld(A + 8 * (size_t)nslots + slot));
-		o0 += a0 * x0 + a1 * x1 + a2 * x2;
-		o1 += a3 * x0 + a4 * x1 + a5 * x2;
-		o2 += a6 * x0 + a7 * x1 + a8 * x2;
+		o0 += a[0] * x0 + a[1] * x1 + a[2] * x2;
+		o1 += a[3] * x0 + a[4] * x1 + a[5] * x2;
+		o2 += a[6] * x0 + a[7] * x1 + a[8] * x2;
 	}
 	out[0] = (TV)o0;
 	out[1] = (TV)o1;

@@ -75,14 +75,20 @@ struct DevBody
 	void* Alo;                  // 9 * nslots of the precision's storage type (double / bf16), or null
 	void* Minv;                 // 3 * npad (scalar Jacobi) or 9 * npad (block Jacobi), vector type
 
-	// contribution lists, in slot order and element order (deterministic)
-	const uint32_t* tet_cptr;   // nslots + 1
+	// contribution lists in element order (deterministic), interleaved across the 32 lanes of a
+	// slice: entry t of item j (a slot, or a row) sits at start[j] + 32 t, so a warp reading entry
+	// t of its 32 items touches 128 consecutive bytes
+	const uint32_t* tet_cstart; // per slot
+	const uint16_t* tet_ccnt;   // per slot
 	const uint32_t* tet_clist;  // e << 4 | a << 2 | b
-	const uint32_t* blk_cptr;   // nslots + 1
+	const uint32_t* blk_cstart; // per slot
+	const uint16_t* blk_ccnt;
 	const uint32_t* blk_clist;  // block index << 1 | negate
-	const uint32_t* vt_ptr;     // n + 1
+	const uint32_t* vt_start;   // per row (npad)
+	const uint16_t* vt_cnt;
 	const uint32_t* vt_list;    // 4 e + a
-	const uint32_t* vb_ptr;     // n + 1
+	const uint32_t* vb_start;   // per row (npad)
+	const uint16_t* vb_cnt;
 	const uint32_t* vb_list;    // vector index << 1 | negate
 
 	// vertex state
@@ -160,16 +166,16 @@ struct Pattern
 	int* slice_ptr = nullptr;
 	int* col = nullptr;
 	uint8_t* rowlen = nullptr;
-	uint32_t* tet_cptr = nullptr;
-	uint32_t* tet_clist = nullptr;
-	uint64_t tet_ccount = 0;
-	uint32_t* blk_cptr = nullptr;
-	uint32_t* blk_clist = nullptr;
-	uint64_t blk_ccount = 0;
-	uint32_t* vt_ptr = nullptr;
-	uint32_t* vt_list = nullptr;
-	uint32_t* vb_ptr = nullptr;
-	uint32_t* vb_list = nullptr;
+	// interleaved lists (see DevBody): start / count per item, entries at start + 32 t
+	struct Lists
+	{
+		uint32_t* start = nullptr;
+		uint16_t* cnt = nullptr;
+		uint32_t* list = nullptr;
+		uint64_t len = 0;    // entries including the padding of each group of 32 items
+		uint64_t items = 0;
+	};
+	Lists tet, blk, vt, vb;
 };
 
 // Builds the SELL-32 pattern and every contribution list. Returns false with a message on a

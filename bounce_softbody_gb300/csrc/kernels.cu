@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(DevBody B, const TA* A)
 		if (i >= B.n) continue;
 		int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 		TV q[3];
-		spmv_row<TA, TV>(A, B.col, B.rowlen, B.nslots, base, w, lane, i, py, np, q);
+		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, py, np, q);
 		TV rr[3] = {pb[i] - q[0], pb[np + i] - q[1], pb[2 * np + i] - q[2]};
 		TV ss[3];
 		precond_row<TV>(B, i, rr, ss);
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(DevBody B, const TA* A)
 		if (i >= B.n) continue;
 		int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 		TV o[3];
-		spmv_row<TA, TV>(A, B.col, B.rowlen, B.nslots, base, w, lane, i, d, np, o);
+		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, d, np, o);
 #pragma unroll
 		for (int c = 0; c < 3; ++c)
 		{
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(kThreads) k_resid(DevBody B, const TA* A, int 
 		if (i >= B.n) continue;
 		int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 		TV q[3];
-		spmv_row<TA, TV>(A, B.col, B.rowlen, B.nslots, base, w, lane, i, py, np, q);
+		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, py, np, q);
 		TV rr[3] = {pb[i] - q[0], pb[np + i] - q[1], pb[2 * np + i] - q[2]};
 		TV ss[3];
 		precond_row<TV>(B, i, rr, ss);

@@ -36,19 +36,70 @@ T* dup(const std::vector<T>& v)
 
 } // namespace
 
+// Re-lays a CSR list (ptr over `items` items) so that the items of each group of 32 consecutive
+// items interleave their entries: entry t of item j goes to start[j] + 32 t. Padding entries
+// (for items shorter than the longest of their group) are zero and never read.
+static bool interleave(const std::vector<uint32_t>& ptr, const std::vector<uint32_t>& list, size_t items,
+                       Pattern::Lists* out, char* err, size_t errlen)
+{
+	std::vector<uint32_t> start(items, 0);
+	std::vector<uint16_t> cnt(items, 0);
+	uint64_t cursor = 0;
+	for (size_t g = 0; g < items; g += kSlice)
+	{
+		uint32_t m = 0;
+		for (size_t j = g; j < g + kSlice && j < items; ++j) m = std::max(m, ptr[j + 1] - ptr[j]);
+		if (m > 65535)
+		{
+			std::snprintf(err, errlen, "an item has %u contributions (limit 65535)", m);
+			return false;
+		}
+		for (size_t j = g; j < g + kSlice && j < items; ++j)
+		{
+			start[j] = (uint32_t)(cursor + (j - g));
+			cnt[j] = (uint16_t)(ptr[j + 1] - ptr[j]);
+		}
+		cursor += (uint64_t)kSlice * m;
+		if (cursor >= (1ull << 32))
+		{
+			std::snprintf(err, errlen, "contribution lists exceed 2^32 entries");
+			return false;
+		}
+	}
+	std::vector<uint32_t> il(std::max<uint64_t>(cursor, 1), 0u);
+	for (size_t j = 0; j < items; ++j)
+		for (uint32_t t = 0; t < cnt[j]; ++t) il[start[j] + (size_t)kSlice * t] = list[ptr[j] + t];
+	out->start = (uint32_t*)std::malloc(std::max<size_t>(items, 1) * sizeof(uint32_t));
+	out->cnt = (uint16_t*)std::malloc(std::max<size_t>(items, 1) * sizeof(uint16_t));
+	out->list = (uint32_t*)std::malloc(il.size() * sizeof(uint32_t));
+	if (items)
+	{
+		std::memcpy(out->start, start.data(), items * sizeof(uint32_t));
+		std::memcpy(out->cnt, cnt.data(), items * sizeof(uint16_t));
+	}
+	std::memcpy(out->list, il.data(), il.size() * sizeof(uint32_t));
+	out->len = il.size();
+	out->items = items;
+	return true;
+}
+
+static void free_lists(Pattern::Lists* l)
+{
+	std::free(l->start);
+	std::free(l->cnt);
+	std::free(l->list);
+	*l = Pattern::Lists();
+}
+
 void free_pattern(Pattern* p)
 {
 	std::free(p->slice_ptr);
 	std::free(p->col);
 	std::free(p->rowlen);
-	std::free(p->tet_cptr);
-	std::free(p->tet_clist);
-	std::free(p->blk_cptr);
-	std::free(p->blk_clist);
-	std::free(p->vt_ptr);
-	std::free(p->vt_list);
-	std::free(p->vb_ptr);
-	std::free(p->vb_list);
+	free_lists(&p->tet);
+	free_lists(&p->blk);
+	free_lists(&p->vt);
+	free_lists(&p->vb);
 	*p = Pattern();
 }
 
@@ -230,7 +281,7 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 	}
 
 	// vertex lists of right-hand-side contributions
-	std::vector<uint32_t> vtp(n + 1, 0), vbp(n + 1, 0), vtl, vbl;
+	std::vector<uint32_t> vtp(P.npad + 1, 0), vbp(P.npad + 1, 0), vtl, vbl;
 	vtl.reserve(4 * (size_t)nt);
 	vbl.reserve(3 * (size_t)ntr + 2 * (size_t)ns);
 	for (uint32_t i = 0; i < n; ++i)
@@ -245,20 +296,21 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 		vtp[i + 1] = (uint32_t)vtl.size();
 		vbp[i + 1] = (uint32_t)vbl.size();
 	}
+	for (int i = (int)n; i < P.npad; ++i)
+	{
+		vtp[i + 1] = vtp[i];
+		vbp[i + 1] = vbp[i];
+	}
 
+	if (!interleave(tcnt, tlist, P.nslots, &P.tet, err, errlen) || !interleave(bcnt, blist, P.nslots, &P.blk, err, errlen) ||
+	    !interleave(vtp, vtl, P.npad, &P.vt, err, errlen) || !interleave(vbp, vbl, P.npad, &P.vb, err, errlen))
+	{
+		free_pattern(&P);
+		return false;
+	}
 	P.slice_ptr = dup(slice_ptr);
 	P.col = dup(col);
 	P.rowlen = dup(rowlen);
-	P.tet_cptr = dup(tcnt);
-	P.tet_clist = dup(tlist);
-	P.tet_ccount = tlist.size();
-	P.blk_cptr = dup(bcnt);
-	P.blk_clist = dup(blist);
-	P.blk_ccount = blist.size();
-	P.vt_ptr = dup(vtp);
-	P.vt_list = dup(vtl);
-	P.vb_ptr = dup(vbp);
-	P.vb_list = dup(vbl);
 	*out = P;
 	return true;
 }

@@ -16,12 +16,17 @@
 #include "ops.h"
 
 #include <cooperative_groups.h>
+#include <type_traits>
 
 namespace cg = cooperative_groups;
 
 namespace b3g {
 
 namespace {
+
+#ifndef B3G_BATCH_MIN_BLOCKS
+#define B3G_BATCH_MIN_BLOCKS 2   // resident CTAs per SM the register budget is sized for
+#endif
 
 constexpr int kPThreads = 256;
 constexpr int kPWarps = kPThreads / 32;
@@ -90,13 +95,114 @@ struct BatchParams
 	double tol2;
 	int refresh;
 	double newton_tol2;
+	unsigned long long* prof;  // optional: kPhases cycle counters per CTA
 };
+
+// Phases timed by the optional instrumentation (cycles of thread 0 of each CTA, barriers and
+// reductions included in the phase that ends with them).
+enum { kPhElem = 0, kPhAsm = 1, kPhSpmv = 2, kPhUpdate = 3, kPhDir = 4, kPhFinal = 5, kPhIdle = 6, kPhases = 8 };
+
+struct PhaseClock
+{
+	unsigned long long* slot;
+	long long t;
+	__device__ void start(unsigned long long* p)
+	{
+		slot = p ? p + (size_t)blockIdx.x * kPhases : nullptr;
+		if (slot) t = clock64();
+	}
+	__device__ void tick(int phase)
+	{
+		if (!slot) return;
+		long long now = clock64();
+		if (threadIdx.x == 0) slot[phase] += (unsigned long long)(now - t);
+		t = now;
+	}
+};
+
+// PCG update of two rows (slices sl and sl + stride of one warp) with every load issued before
+// the first store: x += alpha d and, unless this is a refresh iteration, r -= alpha q,
+// s = M^-1 r. Returns the rows' r.s.
+template <class TV, class LD>
+__device__ __forceinline__ double update_two(const DevBody& B, TV* __restrict__ py, const TV* __restrict__ d,
+                                             TV* __restrict__ r, const TV* __restrict__ q, TV* __restrict__ s,
+                                             int i0, int i1, bool ok1, TV alpha, bool refresh)
+{
+	const int np = B.npad;
+	const int ii[2] = {i0, i1};
+	const bool ok[2] = {true, ok1};
+	TV x[2][3], dd[2][3], rr[2][3], qq[2][3];
+#pragma unroll
+	for (int u = 0; u < 2; ++u)
+#pragma unroll
+		for (int c = 0; c < 3; ++c)
+			if (ok[u])
+			{
+				x[u][c] = LD::ld(py + c * np + ii[u]);
+				dd[u][c] = LD::ld(d + c * np + ii[u]);
+				if (!refresh)
+				{
+					rr[u][c] = LD::ld(r + c * np + ii[u]);
+					qq[u][c] = LD::ld(q + c * np + ii[u]);
+				}
+			}
+	double part = 0.0;
+#pragma unroll
+	for (int u = 0; u < 2; ++u)
+	{
+		if (!ok[u]) continue;
+#pragma unroll
+		for (int c = 0; c < 3; ++c) py[c * np + ii[u]] = x[u][c] + alpha * dd[u][c];
+		if (refresh) continue;
+		TV nr[3], ss[3];
+#pragma unroll
+		for (int c = 0; c < 3; ++c) nr[c] = rr[u][c] - alpha * qq[u][c];
+		precond_row<TV, LD>(B, ii[u], nr, ss);
+#pragma unroll
+		for (int c = 0; c < 3; ++c)
+		{
+			r[c * np + ii[u]] = nr[c];
+			s[c * np + ii[u]] = ss[c];
+			part += (double)nr[c] * (double)ss[c];
+		}
+	}
+	return part;
+}
+
+// d = s + beta d for two rows, loads first
+template <class TV, class LD>
+__device__ __forceinline__ void direction_two(const DevBody& B, TV* __restrict__ d, const TV* __restrict__ s, int i0,
+                                              int i1, bool ok1, TV beta)
+{
+	const int np = B.npad;
+	TV s0[3], d0[3], s1[3], d1[3];
+#pragma unroll
+	for (int c = 0; c < 3; ++c)
+	{
+		s0[c] = LD::ld(s + c * np + i0);
+		d0[c] = LD::ld(d + c * np + i0);
+		if (ok1)
+		{
+			s1[c] = LD::ld(s + c * np + i1);
+			d1[c] = LD::ld(d + c * np + i1);
+		}
+	}
+#pragma unroll
+	for (int c = 0; c < 3; ++c)
+	{
+		d[c * np + i0] = s0[c] + beta * d0[c];
+		if (ok1) d[c * np + i1] = s1[c] + beta * d1[c];
+	}
+}
 
 // The implicit step of one body by one team; mirrors the per-op path of kernels.cu phase for
 // phase (same device functions, same reduction decisions).
 template <int CL, class TA, class TV>
 __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, bool bf16)
 {
+	// A single-CTA team reads what its own threads wrote behind __syncthreads: ordinary (L1)
+	// loads are coherent there. Cluster teams read other SMs' writes: L2-coherent loads.
+	typedef typename std::conditional<CL == 1, LdPlain, LdCG>::type LD;
 	const int lane = threadIdx.x & 31;
 	const int np = B.npad;
 	const TA* Asp = (sizeof(TA) == sizeof(float) && !bf16) ? (const TA*)B.A32 : (const TA*)B.Alo;
@@ -111,19 +217,22 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 	double delta = 0.0, delta0 = 0.0, err = 0.0, err0 = 0.0;
 	int iter = 0;
 	unsigned long long iters_all = 0ull;
+	PhaseClock pc;
+	pc.start(P.prof);
 	for (int k = 0; k < P.newton; ++k)
 	{
 		StepParams sp;
 		sp.h = h;
 		sp.first_newton = k == 0 ? 1 : 0;
 		const bool finish = P.newton == 1;
-		for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LdCG>(B, e, sp);
-		for (int e = T.tid(); e < B.ntr; e += T.nthreads()) tri_element<LdCG>(B, e, sp);
-		for (int e = T.tid(); e < B.ns; e += T.nthreads()) spring_element<LdCG>(B, e, sp);
+		for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LD>(B, e, sp);
+		for (int e = T.tid(); e < B.ntr; e += T.nthreads()) tri_element<LD>(B, e, sp);
+		for (int e = T.tid(); e < B.ns; e += T.nthreads()) spring_element<LD>(B, e, sp);
 		T.sync();
+		pc.tick(kPhElem);
 		double part = 0.0;
 		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
-			part += assemble_row<TA, TV, LdCG>(B, sl, lane, sp, k == 0);
+			part += assemble_row<TA, TV, LD>(B, sl, lane, sp, k == 0);
 		if (k > 0)
 		{
 			// warm start from the previous solution: r = pb - A py
@@ -136,12 +245,12 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 				const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 				TV o[3], rr[3], ss[3];
 				if (sizeof(TA) == sizeof(double))
-					spmv_row<TA, TV, LdCG>(Asp, B.col, B.rowlen, B.nslots, base, w, lane, i, py, np, o);
+					spmv_row<TA, TV, LD>(Asp, B.col, B.nslots, base, w, lane, py, np, o);
 				else
-					spmv_row<float, TV, LdCG>(B.A32, B.col, B.rowlen, B.nslots, base, w, lane, i, py, np, o);
+					spmv_row<float, TV, LD>(B.A32, B.col, B.nslots, base, w, lane, py, np, o);
 #pragma unroll
-				for (int c = 0; c < 3; ++c) rr[c] = __ldcg(pb + c * np + i) - o[c];
-				precond_row<TV, LdCG>(B, i, rr, ss);
+				for (int c = 0; c < 3; ++c) rr[c] = LD::ld(pb + c * np + i) - o[c];
+				precond_row<TV, LD>(B, i, rr, ss);
 #pragma unroll
 				for (int c = 0; c < 3; ++c)
 				{
@@ -153,6 +262,7 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 			}
 		}
 		delta0 = T.reduce(part);
+		pc.tick(kPhAsm);
 		delta = delta0;
 		iter = 0;
 		bool pending = false;
@@ -184,15 +294,16 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 				if (i >= B.n) continue;
 				const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 				TV o[3];
-				spmv_row<TA, TV, LdCG>(Asp, B.col, B.rowlen, B.nslots, base, w, lane, i, d, np, o);
+				spmv_row<TA, TV, LD>(Asp, B.col, B.nslots, base, w, lane, d, np, o);
 #pragma unroll
 				for (int c = 0; c < 3; ++c)
 				{
 					q[c * np + i] = o[c];
-					part += (double)__ldcg(d + c * np + i) * (double)o[c];
+					part += (double)LD::ld(d + c * np + i) * (double)o[c];
 				}
 			}
 			const double dq = T.reduce(part);
+			pc.tick(kPhSpmv);
 			if (!isfinite(dq))
 			{
 				status = B3G_SOLVE_NONFINITE;
@@ -206,27 +317,13 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 			const TV alpha = (TV)(delta / dq);
 			const bool refresh = (P.refresh > 0 && (iter % P.refresh) == 0) || pending;
 			part = 0.0;
-			for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
+			for (int sl = T.warp(); sl < B.nslices; sl += 2 * T.nwarps())
 			{
-				const int i = sl * kSlice + lane;
-				if (i >= B.n) continue;
-#pragma unroll
-				for (int c = 0; c < 3; ++c) py[c * np + i] = __ldcg(py + c * np + i) + alpha * __ldcg(d + c * np + i);
-				if (refresh) continue;
-				TV rr[3], ss[3];
-#pragma unroll
-				for (int c = 0; c < 3; ++c)
-				{
-					rr[c] = __ldcg(r + c * np + i) - alpha * __ldcg(q + c * np + i);
-					r[c * np + i] = rr[c];
-				}
-				precond_row<TV, LdCG>(B, i, rr, ss);
-#pragma unroll
-				for (int c = 0; c < 3; ++c)
-				{
-					s[c * np + i] = ss[c];
-					part += (double)rr[c] * (double)ss[c];
-				}
+				const int i0 = sl * kSlice + lane;
+				const int sl1 = sl + T.nwarps();
+				const int i1 = sl1 * kSlice + lane;
+				if (i0 >= B.n) continue;
+				part += update_two<TV, LD>(B, py, d, r, q, s, i0, i1, sl1 < B.nslices && i1 < B.n, alpha, refresh);
 			}
 			if (refresh)
 			{
@@ -239,12 +336,12 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 					const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 					TV o[3], rr[3], ss[3];
 					if (sizeof(TA) == sizeof(double))
-						spmv_row<TA, TV, LdCG>(Asp, B.col, B.rowlen, B.nslots, base, w, lane, i, py, np, o);
+						spmv_row<TA, TV, LD>(Asp, B.col, B.nslots, base, w, lane, py, np, o);
 					else
-						spmv_row<float, TV, LdCG>(B.A32, B.col, B.rowlen, B.nslots, base, w, lane, i, py, np, o);
+						spmv_row<float, TV, LD>(B.A32, B.col, B.nslots, base, w, lane, py, np, o);
 #pragma unroll
-					for (int c = 0; c < 3; ++c) rr[c] = __ldcg(pb + c * np + i) - o[c];
-					precond_row<TV, LdCG>(B, i, rr, ss);
+					for (int c = 0; c < 3; ++c) rr[c] = LD::ld(pb + c * np + i) - o[c];
+					precond_row<TV, LD>(B, i, rr, ss);
 #pragma unroll
 					for (int c = 0; c < 3; ++c)
 					{
@@ -255,6 +352,7 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 				}
 			}
 			const double dn = T.reduce(part);
+			pc.tick(kPhUpdate);
 			const double beta = dn / delta;
 			delta = dn;
 			iter += 1;
@@ -281,14 +379,16 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 				break;
 			}
 			const TV bt = (TV)beta;
-			for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
+			for (int sl = T.warp(); sl < B.nslices; sl += 2 * T.nwarps())
 			{
-				const int i = sl * kSlice + lane;
-				if (i >= B.n) continue;
-#pragma unroll
-				for (int c = 0; c < 3; ++c) d[c * np + i] = __ldcg(s + c * np + i) + bt * __ldcg(d + c * np + i);
+				const int i0 = sl * kSlice + lane;
+				const int sl1 = sl + T.nwarps();
+				const int i1 = sl1 * kSlice + lane;
+				if (i0 >= B.n) continue;
+				direction_two<TV, LD>(B, d, s, i0, i1, sl1 < B.nslices && i1 < B.n, bt);
 			}
 			T.sync();
+			pc.tick(kPhDir);
 		}
 		min_it = iter < min_it ? iter : min_it;
 		max_it = iter > max_it ? iter : max_it;
@@ -299,9 +399,10 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
 		{
 			const int i = sl * kSlice + lane;
-			if (i < B.n) part += final_vertex<TV, LdCG>(B, i, h, k == 0, finish);
+			if (i < B.n) part += final_vertex<TV, LD>(B, i, h, k == 0, finish);
 		}
 		err = T.reduce(part);
+		pc.tick(kPhFinal);
 		if (k == 0) err0 = err;
 		newton_done_at = k + 1;
 		if (finish) break;
@@ -312,7 +413,7 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 			for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
 			{
 				const int i = sl * kSlice + lane;
-				if (i < B.n) post_vertex<LdCG>(B, i, h);
+				if (i < B.n) post_vertex<LD>(B, i, h);
 			}
 			break;
 		}
@@ -344,7 +445,7 @@ __device__ void load_body(DevBody* dst, const DevBody* src)
 }
 
 template <int CL, class TA, class TV>
-__global__ void __launch_bounds__(kPThreads, 2) k_batch(BatchParams P, int bf16)
+__global__ void __launch_bounds__(kPThreads, B3G_BATCH_MIN_BLOCKS) k_batch(BatchParams P, int bf16)
 {
 	__shared__ TeamShared sh;
 	__shared__ __align__(16) DevBody sb;
@@ -473,6 +574,7 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 	P.tol2 = A.tol2;
 	P.refresh = A.refresh;
 	P.newton_tol2 = A.newton_tol2;
+	P.prof = A.prof;
 	cudaError_t e = cudaMemsetAsync(A.queue, 0, 2 * sizeof(unsigned), st);
 	if (e != cudaSuccess) return e;
 	if (A.prec == kP64) return launch_prec<double, double>(P, A.cluster, A.ctas, 0, st);

@@ -185,6 +185,11 @@ B3G_API int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_t c
  * candidates, then (candidate code = cluster * 1e6 + threshold, microseconds) per candidate. */
 B3G_API int b3g_batch_schedule(b3g_context* ctx, int32_t* out, uint32_t capacity);
 
+/* Cycles spent per phase of the batch kernel, summed over CTAs (elements, assembly, SpMV, update,
+ * direction, final update, -, -). Only counted when the environment variable B3G_PHASE_PROFILE=1
+ * is set when the batch is first stepped; zeros otherwise. reset != 0 clears the counters. */
+B3G_API int b3g_batch_phase_cycles(b3g_context* ctx, uint64_t out[8], int reset);
+
 /* Host-buffer transfers for a list of bodies of one context; the host arrays are the bodies'
  * arrays concatenated in list order (3 floats per vertex). Pinned host memory makes them
  * asynchronous copies; get waits for the copies. */

@@ -1,0 +1,190 @@
+"""Cloth (triangles, springs, sphere contact, friction), precision variants, preconditioners,
+Newton iterations and the particle API of the CUDA path, against the oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from bounce_softbody_gb300 import b3g, meshes
+
+pytestmark = pytest.mark.gpu
+
+DT = 1.0 / 60.0
+
+
+def rel_disp(x, xr, x0):
+    return float(np.linalg.norm(np.asarray(x, np.float64) - xr) / max(np.linalg.norm(xr - x0), 1e-30))
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def gpu_run(ctx, desc, steps, cfg):
+    g = b3g.Body(ctx, desc)
+    its = [g.step(DT, cfg)["pcg_iterations"] for _ in range(steps)]
+    x, v = g.state()
+    m = g.masses()
+    g.close()
+    return x, v, its, m
+
+
+@pytest.mark.parametrize("m,steps", [(12, 60), (24, 40)])
+def test_cloth_contact_friction_matches_oracle(ctx, m, steps):
+    """Cloth over a sphere: triangle elements, structural and bending springs, penalty contact
+    and Coulomb friction impulses (the reference's contact semantics)."""
+    desc = meshes.cloth_grid(m, side=1.2, height=0.56, sphere_radius=0.5, contact_radius=0.05)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    x, v, its, m_gpu = gpu_run(ctx, desc, steps, cfg)
+    x64, v64, it64, _ = oracle.simulate(desc, steps, kind="port", bits=64)
+    x32, v32, _, _ = oracle.simulate(desc, steps, kind="port", bits=32)
+    # the cloth touched the sphere: some vertex ended inside the contact shell
+    r = np.linalg.norm(x64 - desc.world_spheres[0, :3], axis=1)
+    assert r.min() < 0.5 + 0.05 + 1e-3
+    floor_x = rel_disp(x32, x64, desc.x)
+    assert rel_disp(x, x64, desc.x) < max(1e-4, 20 * floor_x)
+    floor_v = rel(v32, v64)
+    assert rel(v, v64) < max(1e-3, 20 * floor_v)
+
+
+def test_lumped_masses_match_oracle_rule(ctx):
+    desc = meshes.cloth_grid(8, side=1.0)
+    g = b3g.Body(ctx, desc)
+    m = g.masses()
+    g.close()
+    area = 0.5 * (1.0 / 7) ** 2
+    expected = np.zeros(desc.n)
+    for t in desc.tris:
+        expected[t] += desc.tri_density[0] * area / 3
+    expected[desc.type != 2] = 0.0
+    np.testing.assert_allclose(m, expected, rtol=1e-5)
+
+
+@pytest.mark.parametrize("precision", [b3g.PRECISION_FP64, b3g.PRECISION_BF16])
+def test_precision_variants_reach_tolerance(ctx, precision):
+    """FP64 PCG and BF16-stored blocks (FP32 refinement) both end within 1e-4 of the FP64 oracle."""
+    desc = meshes.tet_grid(8, 8, 8, seed=5, E=1e6, nu=0.45, pin="y0")
+    cfg = b3g.solver_config(max_pcg_iterations=1000, pcg_tolerance=1e-5, precision=precision, refresh_period=25)
+    x, v, its, _ = gpu_run(ctx, desc, 10, cfg)
+    x64, v64, _, _ = oracle.simulate(desc, 10, kind="port", bits=64, max_sub=1000)
+    assert rel_disp(x, x64, desc.x) < 1e-4
+    assert rel(v, v64) < 1e-3
+
+
+def test_block_jacobi_converges_to_same_state(ctx):
+    desc = meshes.tet_grid(7, 9, 6, seed=2, E=2e5, nu=0.4, pin="x0")
+    cfg_j = b3g.solver_config(max_pcg_iterations=500, pcg_tolerance=1e-7)
+    cfg_b = b3g.solver_config(max_pcg_iterations=500, pcg_tolerance=1e-7, preconditioner=b3g.PRECOND_BLOCK_JACOBI)
+    xj, vj, itj, _ = gpu_run(ctx, desc, 5, cfg_j)
+    xb, vb, itb, _ = gpu_run(ctx, desc, 5, cfg_b)
+    assert rel_disp(xb, xj.astype(np.float64), desc.x) < 1e-5
+    assert itb[-1] <= itj[-1] + 2
+
+
+def test_newton_iterations_match_oracle(ctx):
+    desc = meshes.tet_grid(6, 6, 6, seed=9, E=5e4, nu=0.3, pin="y0", kdamp=0.01)
+    cfg = b3g.solver_config(force_iterations=3, max_pcg_iterations=200, pcg_tolerance=1e-6)
+    x, v, its, _ = gpu_run(ctx, desc, 8, cfg)
+    x64, v64, _, _ = oracle.simulate(desc, 8, kind="port", bits=64, newton_iters=3, sub_tol=1e-6)
+    assert rel_disp(x, x64, desc.x) < 1e-4
+    assert rel(v, v64) < 1e-3
+
+
+def test_stiffness_damping_matches_oracle(ctx):
+    desc = meshes.tet_grid(6, 7, 5, seed=4, E=1e5, nu=0.3, pin="z0", kdamp=0.02)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    x, v, _, _ = gpu_run(ctx, desc, 10, cfg)
+    x64, v64, _, _ = oracle.simulate(desc, 10, kind="port", bits=64)
+    assert rel_disp(x, x64, desc.x) < 1e-4
+
+
+def test_particle_api_forces_translations_types(ctx):
+    """ApplyForce / ApplyTranslation act for one step and are then cleared; SetType(static)
+    zeroes the velocity and pins the vertex."""
+    desc = meshes.tet_grid(5, 5, 5, seed=1, pin="y0")
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    g = b3g.Body(ctx, desc)
+    g.step(DT, cfg)
+    x1, v1 = g.state()
+    f = np.zeros((desc.n, 3), np.float32)
+    top = np.where(desc.x[:, 1] > desc.x[:, 1].max() - 1e-3)[0]
+    f[top, 0] = 50.0
+    g.apply_forces(f)
+    t = np.zeros((desc.n, 3), np.float32)
+    t[desc.type == 0, 2] = 0.01  # move the pinned layer (translation applies to every vertex)
+    g.apply_translations(t)
+    g.step(DT, cfg)
+    x2, v2 = g.state()
+    assert x2[top, 0].mean() > x1[top, 0].mean()
+    pinned = desc.type == 0
+    np.testing.assert_allclose(x2[pinned, 2] - x1[pinned, 2], 0.01, atol=1e-6)
+    # forces and translations were cleared: a third step moves pinned vertices no more
+    g.step(DT, cfg)
+    x3, _ = g.state()
+    np.testing.assert_allclose(x3[pinned], x2[pinned], atol=1e-7)
+    types = desc.type.copy()
+    types[top] = 0
+    g.set_types(types)
+    _, v4 = g.state()
+    assert np.abs(v4[top]).max() == 0.0
+    g.step(DT, cfg)
+    x5, v5 = g.state()
+    np.testing.assert_allclose(x5[top], x3[top], atol=1e-7)
+    assert g.masses()[top].max() == 0.0
+    g.close()
+
+
+def test_rotations_roundtrip_and_determinism(ctx):
+    """The per-tet rotation state is device resident, readable and restorable; restoring state
+    and rotations reproduces the next step bitwise (checkpoint / resume)."""
+    desc = meshes.tet_grid(6, 6, 6, seed=3, pin="y0")
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    g = b3g.Body(ctx, desc)
+    for _ in range(4):
+        g.step(DT, cfg)
+    x, v = g.state()
+    q = g.rotations()
+    assert np.allclose(np.linalg.norm(q, axis=1), 1.0, atol=1e-5)
+    g.step(DT, cfg)
+    xa, va = g.state()
+    g.set_state(x, v)
+    g.set_rotations(q)
+    g.step(DT, cfg)
+    xb, vb = g.state()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    g.close()
+
+
+def test_nonfinite_input_reports_status(ctx):
+    """A NaN external force makes the solve report NONFINITE instead of failing silently."""
+    desc = meshes.tet_grid(4, 4, 4, seed=1, pin="y0")
+    g = b3g.Body(ctx, desc)
+    f = np.zeros((desc.n, 3), np.float32)
+    f[-1, 0] = np.nan
+    g.apply_forces(f)
+    st = g.step(DT, b3g.solver_config(max_pcg_iterations=50, pcg_tolerance=1e-5))
+    assert st["solve_status"] == "nonfinite"
+    g.close()
+
+
+def test_invalid_meshes_are_rejected(ctx):
+    desc = meshes.tet_grid(3, 3, 3, pin="y0")
+    bad = meshes.tet_grid(3, 3, 3, pin="y0")
+    bad.tets = bad.tets.copy()
+    bad.tets[0, 0] = desc.n + 5
+    with pytest.raises(b3g.B3gError, match="references vertex"):
+        b3g.Body(ctx, bad)
+    deg = meshes.tet_grid(3, 3, 3, pin="y0")
+    deg.tets = deg.tets.copy()
+    deg.tets[1, 1] = deg.tets[1, 0]
+    with pytest.raises(b3g.B3gError, match="repeats vertex"):
+        b3g.Body(ctx, deg)
+
+
+def test_zero_dt_skips_the_solve(ctx):
+    desc = meshes.tet_grid(4, 4, 4, pin="y0")
+    g = b3g.Body(ctx, desc)
+    x0, v0 = g.state()
+    g.step(0.0)
+    x1, v1 = g.state()
+    assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
+    g.close()
