@@ -127,7 +127,9 @@ bool tri_setup(const float r[9], float Ex, float Ey, float Es, float nxy, float 
 	float det = e1x * e2y - e1y * e2x;
 	if (det == 0.0f) return false;
 	float A = 0.5f * std::fabs(det);
-	det = 1.0f / det;
+	// The reference multiplies the adjugate by det instead of dividing by it
+	// (triangle_element_force.cpp:260-265), so its rest-shape matrix is det^2 S^-1 and the
+	// element stiffness scales accordingly. Kept as the reference computes it, for parity.
 	invS[0] = det * e2y;
 	invS[1] = det * -e1y;
 	invS[2] = det * -e2x;

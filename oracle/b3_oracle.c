@@ -346,8 +346,9 @@ static void tri_reset(body_t* B, uint32_t e, v3 p1, v3 p2, v3 p3, real Ex, real 
 	v2 e1 = sub2(x2, x1), e2 = sub2(x3, x1);
 	real det = e1.x * e2.y - e1.y * e2.x;
 	real A = (real)0.5 * (real)fabs((double)det);
-	det = (real)1 / det;
-	/* mat22.h:194 adjugate, scaled */
+	/* triangle_element_force.cpp:260-265: the reference scales the adjugate by det itself (it
+	 * does not divide by it, unlike the tetrahedron's invE), so its "invS" is det^2 S^-1. This is
+	 * restated as written: the element's stiffness follows that matrix. mat22.h:194 adjugate. */
 	m22 invS = M2(V2(det * e2.y, det * -e1.y), V2(det * -e2.x, det * e1.x));
 	B->invS[e] = invS;
 	real s = (real)1 - nxy * nyx;

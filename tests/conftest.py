@@ -29,3 +29,25 @@ def ctx():
     c = b3g.Context(0)
     yield c
     c.close()
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GOLDEN_CASES = ["tet10", "tet10_bodystep", "tet4", "tet6_newton", "single_tet", "cloth12", "cloth12_contact"]
+
+
+def load_golden(name):
+    """A golden fixture made by the reference itself: (BodyDesc, arrays, run settings)."""
+    import numpy as np
+
+    from bounce_softbody_gb300 import meshes
+
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    kw = {k[3:]: z[k] for k in z.files if k.startswith("in_")}
+    gravity = kw.pop("gravity")
+    world = kw.pop("world_spheres")
+    sr = kw.pop("sphere_radius", None)
+    sf = kw.pop("sphere_friction", None)
+    desc = meshes.BodyDesc(**kw, sphere_radius=sr, sphere_friction=sf, world_spheres=world, gravity=gravity, name=name)
+    st = z["settings"]
+    settings = dict(max_sub=int(st[0]), sub_tol=float(st[1]), newton_iters=int(st[2]))
+    return desc, z, settings

@@ -1,0 +1,83 @@
+"""Generates the golden fixtures of tests/golden/ by running the reference library itself.
+
+The reference is compiled from its own sources by oracle/Makefile (target `ref`, float and
+double builds) and driven through oracle/ref_harness.cpp. Each fixture stores the inputs (so the
+tests need neither the reference nor the mesh generators to reproduce them) and the reference's
+positions, velocities and PCG iteration counts after a number of steps.
+
+Run here, where the reference sources exist:  python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle")]
+
+import oracle  # noqa: E402
+from bounce_softbody_gb300 import meshes  # noqa: E402
+
+
+def single_tet():
+    d = meshes.tet_grid(2, 2, 2, pin="none", E=2e4, nu=0.3, damping=0.0, name="single_tet")
+    keep = d.tets[:1]
+    used = np.unique(keep)
+    remap = {int(v): k for k, v in enumerate(used)}
+    d.x = d.x[used]
+    d.v = np.zeros_like(d.x)
+    d.type = np.array([0, 0, 0, 2], np.int32)[: len(used)]
+    d.damping = np.zeros(len(used))
+    d.tets = np.array([[remap[int(v)] for v in keep[0]]], np.uint32)
+    for f in ("tet_E", "tet_nu", "tet_kdamp", "tet_density"):
+        setattr(d, f, getattr(d, f)[:1])
+    return d
+
+
+CASES = [
+    # name, body factory, steps snapshots, run settings
+    ("tet10", meshes.config_tet10, [1, 10, 120], dict(max_sub=200, sub_tol=1e-5)),
+    ("tet10_bodystep", meshes.config_tet10, [10], dict(max_sub=40, use_body_step=True)),
+    ("tet4", lambda: meshes.tet_grid(4, 4, 4, seed=2, E=1e5, nu=0.3, pin="y0"), [20], dict(max_sub=200, sub_tol=1e-5)),
+    ("tet6_newton", lambda: meshes.tet_grid(6, 6, 6, seed=9, E=5e4, nu=0.3, pin="y0", kdamp=0.01), [8],
+     dict(max_sub=200, sub_tol=1e-6, newton_iters=3)),
+    ("single_tet", single_tet, [10], dict(max_sub=50, sub_tol=1e-6)),
+    # cloth over a sphere is chaotic (tension-only springs start exactly at rest length, so float
+    # rounding decides which engage): the reference's own FP32 and FP64 builds separate within
+    # tens of steps, so the fixture keeps a short horizon
+    ("cloth12", lambda: meshes.cloth_grid(12, side=1.2, height=0.56, sphere_radius=0.5, contact_radius=0.05), [5, 10],
+     dict(max_sub=200, sub_tol=1e-5)),
+    ("cloth12_contact", lambda: meshes.cloth_grid(12, side=1.2, height=0.52, sphere_radius=0.5, contact_radius=0.05),
+     [3, 6], dict(max_sub=200, sub_tol=1e-5)),
+]
+
+FIELDS = ["x", "v", "type", "damping", "tets", "tet_E", "tet_nu", "tet_kdamp", "tet_density", "tris", "tri_Ex",
+          "tri_Ey", "tri_Es", "tri_nuxy", "tri_nuyx", "tri_kdamp", "tri_density", "springs", "spring_L0",
+          "spring_ks", "spring_kd", "world_spheres", "gravity"]
+
+
+def main():
+    if not oracle.build_ref():
+        raise SystemExit("the reference harness could not be built (reference sources absent)")
+    for name, make, snaps, kw in CASES:
+        body = make()
+        out = {f"in_{f}": np.asarray(getattr(body, f)) for f in FIELDS}
+        if body.sphere_radius is not None:
+            out["in_sphere_radius"] = body.sphere_radius
+            out["in_sphere_friction"] = body.sphere_friction
+        out["steps"] = np.array(snaps)
+        out["settings"] = np.array([kw.get("max_sub", 200), kw.get("sub_tol", 1.1920928955078125e-07),
+                                    kw.get("newton_iters", 1), 1 if kw.get("use_body_step") else 0], np.float64)
+        for bits in (32, 64):
+            for s in snaps:
+                x, v, it, _ = oracle.simulate(body, s, kind="ref", bits=bits, **kw)
+                out[f"ref{bits}_x_{s}"] = x
+                out[f"ref{bits}_v_{s}"] = v
+                out[f"ref{bits}_it_{s}"] = it
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+        print("wrote", name, {k: v.shape for k, v in out.items() if k.startswith("ref64_x")})
+
+
+if __name__ == "__main__":
+    main()
