@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libb3g.so")
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 PRECISION_FP32, PRECISION_FP64, PRECISION_BF16 = 0, 1, 2
 PRECOND_JACOBI, PRECOND_BLOCK_JACOBI = 0, 1
-SOLVE_STATUS = {0: "converged", 1: "max_iterations", 2: "nonfinite", 3: "breakdown"}
+SOLVE_STATUS = {0: "converged", 1: "max_iterations", 2: "nonfinite", 3: "breakdown", 4: "device_timeout"}
 
 _fp = C.POINTER(C.c_float)
 _up = C.POINTER(C.c_uint32)

@@ -230,8 +230,8 @@ int ensure_precision(b3g_body* b, int prec)
 	const size_t vs = prec == kP64 ? sizeof(double) : sizeof(float);
 	const size_t np = (size_t)b->d.npad;
 	size_t bytes = 0;
-	bytes += align_up(7 * 3 * np * vs);           // pb r d d2 q s py
-	bytes += align_up(9 * np * vs);               // Minv
+	bytes += align_up(7 * 4 * np * vs);           // pb r d d2 q s py, 4-wide per vertex
+	bytes += align_up(12 * np * vs);              // Minv: 4 (scalar Jacobi) or 12 (block Jacobi) per vertex
 	size_t alo = 0;
 	if (prec == kP64) alo = 9 * (size_t)b->d.nslots * sizeof(double);
 	if (prec == kPBF) alo = 9 * (size_t)b->d.nslots * sizeof(__nv_bfloat16);
@@ -251,11 +251,11 @@ int ensure_precision(b3g_body* b, int prec)
 	for (int k = 0; k < 7; ++k)
 	{
 		pb.vec[k] = p;
-		p += 3 * np * vs;
+		p += 4 * np * vs;
 	}
-	p = mem + align_up(7 * 3 * np * vs);
+	p = mem + align_up(7 * 4 * np * vs);
 	pb.minv = p;
-	p += align_up(9 * np * vs);
+	p += align_up(12 * np * vs);
 	pb.alo = alo ? p : nullptr;
 	return B3G_OK;
 }
@@ -299,7 +299,7 @@ void stats_from(const Scalars& sc, b3g_step_stats* st)
 	st->newton_iterations = (uint32_t)sc.newton_iter;
 	st->pcg_iterations = (uint32_t)sc.max_it;
 	st->min_pcg_iterations = sc.min_it == 0x7fffffff ? 0u : (uint32_t)sc.min_it;
-	st->solve_status = sc.status;
+	st->solve_status = sc.fault ? B3G_SOLVE_DEVICE_TIMEOUT : sc.status;
 	st->residual_ratio = sc.delta0 > 0.0 ? std::sqrt(std::max(0.0, sc.delta / sc.delta0)) : 0.0;
 	st->newton_error = sc.newton_err;
 	st->total_pcg_iterations = sc.total_iters;

@@ -28,6 +28,52 @@ struct LdCG
 	template <class T> static __device__ __forceinline__ T ld(const T* p) { return __ldcg(p); }
 };
 
+// ------------------------------------------------------------------ 4-wide solver vectors
+// Component c of vertex i at 4 i + c (the fourth component is padding, kept zero).
+template <class TV, class L>
+__device__ __forceinline__ void vld(const TV* v, int i, TV o[3]);
+template <>
+__device__ __forceinline__ void vld<float, LdPlain>(const float* v, int i, float o[3])
+{
+	const float4 t = *(const float4*)(v + 4 * (size_t)i);
+	o[0] = t.x;
+	o[1] = t.y;
+	o[2] = t.z;
+}
+template <>
+__device__ __forceinline__ void vld<float, LdCG>(const float* v, int i, float o[3])
+{
+	const float4 t = __ldcg((const float4*)(v + 4 * (size_t)i));
+	o[0] = t.x;
+	o[1] = t.y;
+	o[2] = t.z;
+}
+template <>
+__device__ __forceinline__ void vld<double, LdPlain>(const double* v, int i, double o[3])
+{
+	const double2 a = *(const double2*)(v + 4 * (size_t)i), b = *(const double2*)(v + 4 * (size_t)i + 2);
+	o[0] = a.x;
+	o[1] = a.y;
+	o[2] = b.x;
+}
+template <>
+__device__ __forceinline__ void vld<double, LdCG>(const double* v, int i, double o[3])
+{
+	const double2 a = __ldcg((const double2*)(v + 4 * (size_t)i)), b = __ldcg((const double2*)(v + 4 * (size_t)i + 2));
+	o[0] = a.x;
+	o[1] = a.y;
+	o[2] = b.x;
+}
+__device__ __forceinline__ void vst(float* v, int i, const float o[3])
+{
+	*(float4*)(v + 4 * (size_t)i) = make_float4(o[0], o[1], o[2], 0.0f);
+}
+__device__ __forceinline__ void vst(double* v, int i, const double o[3])
+{
+	*(double2*)(v + 4 * (size_t)i) = make_double2(o[0], o[1]);
+	*(double2*)(v + 4 * (size_t)i + 2) = make_double2(o[2], 0.0);
+}
+
 // ------------------------------------------------------------------ storage conversions
 template <class T> __device__ __forceinline__ float to_f(T v);
 template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
@@ -595,8 +641,9 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	float diag[9];
 	for (int k = 0; k < w; ++k)
 	{
-		const int slot = base + k * kSlice + lane;
-		const int j = B.col[slot];
+		const int slot = base + k * kSlice + lane;           // contribution-list item
+		const size_t bs = block_slot((size_t)base, k, lane); // block storage
+		const int j = B.col[bs];
 		float a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 		{
 			// tetrahedron contributions of this slot, four in flight at a time
@@ -658,21 +705,20 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 			for (int q = 0; q < 9; ++q) a[q] = 0.0f;
 		}
 #pragma unroll
-		for (int q = 0; q < 9; ++q) B.A32[(size_t)q * B.nslots + slot] = a[q];
+		for (int q = 0; q < 9; ++q) B.A32[(size_t)q * B.nslots + bs] = a[q];
 		if (B.Alo)
 		{
 #pragma unroll
-			for (int q = 0; q < 9; ++q) ((TA*)B.Alo)[(size_t)q * B.nslots + slot] = from_f<TA>(a[q]);
+			for (int q = 0; q < 9; ++q) ((TA*)B.Alo)[(size_t)q * B.nslots + bs] = from_f<TA>(a[q]);
 		}
 	}
 	if (!Si) bi = f3(0, 0, 0);
 	TV* pb = vp<TV>(B.pb);
-	const int np = B.npad;
-	pb[i] = (TV)bi.x;
-	pb[np + i] = (TV)bi.y;
-	pb[2 * np + i] = (TV)bi.z;
+	const TV bv[3] = {(TV)bi.x, (TV)bi.y, (TV)bi.z};
+	vst(pb, i, bv);
 
-	// preconditioner
+	// preconditioner: scalar Jacobi (sparse_solver.cpp:38-55) as one 4-wide value, or the rows of
+	// the inverted 3x3 diagonal block as three
 	TV* Mv = vp<TV>(B.Minv);
 	TV m3[9];
 	if (B.precond == B3G_PRECOND_BLOCK_JACOBI)
@@ -686,101 +732,117 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		double id = 1.0 / det;
 		double inv[9] = {c00 * id, c01 * id, c02 * id, c10 * id, c11 * id, c12 * id, c20 * id, c21 * id, c22 * id};
 #pragma unroll
-		for (int q = 0; q < 9; ++q)
-		{
-			m3[q] = (TV)inv[q];
-			Mv[(size_t)q * np + i] = m3[q];
-		}
+		for (int q = 0; q < 9; ++q) m3[q] = (TV)inv[q];
+		vst(Mv, 3 * i, m3);
+		vst(Mv, 3 * i + 1, m3 + 3);
+		vst(Mv, 3 * i + 2, m3 + 6);
 	}
 	else
 	{
-		// sparse_solver.cpp:38-55
 		m3[0] = (TV)(1.0f / diag[0]);
 		m3[4] = (TV)(1.0f / diag[4]);
 		m3[8] = (TV)(1.0f / diag[8]);
-		Mv[i] = m3[0];
-		Mv[np + i] = m3[4];
-		Mv[2 * np + i] = m3[8];
+		const TV md[3] = {m3[0], m3[4], m3[8]};
+		vst(Mv, i, md);
 	}
 	if (!init_pcg) return 0.0;
-	TV r0 = pb[i], r1 = pb[np + i], r2 = pb[2 * np + i];
-	TV s0, s1, s2;
+	const TV r0 = bv[0], r1 = bv[1], r2 = bv[2];
+	TV sv[3];
 	if (B.precond == B3G_PRECOND_BLOCK_JACOBI)
 	{
-		s0 = m3[0] * r0 + m3[1] * r1 + m3[2] * r2;
-		s1 = m3[3] * r0 + m3[4] * r1 + m3[5] * r2;
-		s2 = m3[6] * r0 + m3[7] * r1 + m3[8] * r2;
+		sv[0] = m3[0] * r0 + m3[1] * r1 + m3[2] * r2;
+		sv[1] = m3[3] * r0 + m3[4] * r1 + m3[5] * r2;
+		sv[2] = m3[6] * r0 + m3[7] * r1 + m3[8] * r2;
 	}
 	else
 	{
-		s0 = m3[0] * r0;
-		s1 = m3[4] * r1;
-		s2 = m3[8] * r2;
+		sv[0] = m3[0] * r0;
+		sv[1] = m3[4] * r1;
+		sv[2] = m3[8] * r2;
 	}
-	TV* rr = vp<TV>(B.r);
-	TV* dd = vp<TV>(B.d);
-	TV* ss = vp<TV>(B.s);
-	TV* yy = vp<TV>(B.py);
-	rr[i] = r0; rr[np + i] = r1; rr[2 * np + i] = r2;
-	ss[i] = s0; ss[np + i] = s1; ss[2 * np + i] = s2;
-	dd[i] = s0; dd[np + i] = s1; dd[2 * np + i] = s2;
-	yy[i] = 0; yy[np + i] = 0; yy[2 * np + i] = 0;
-	return (double)r0 * (double)s0 + (double)r1 * (double)s1 + (double)r2 * (double)s2;
+	const TV zero[3] = {0, 0, 0};
+	vst(vp<TV>(B.r), i, bv);
+	vst(vp<TV>(B.s), i, sv);
+	vst(vp<TV>(B.d), i, sv);
+	vst(vp<TV>(B.py), i, zero);
+	return (double)r0 * (double)sv[0] + (double)r1 * (double)sv[1] + (double)r2 * (double)sv[2];
 }
 
-// q_i = (A x)_i for row i over a SELL-32 slice; TA = block storage, TV = vector type.
-// Every lane runs the slice width w (warp-uniform trip count): slots past the end of a row hold
-// zero blocks whose column is a valid vertex, so no per-row bound is needed. The loads of four
-// consecutive blocks (9 planes, column ids, then the gathered x) are issued before their FMAs so
-// each warp keeps about 5 KB of loads in flight.
+// Four consecutive blocks of one lane in one plane, widened to the arithmetic type.
+template <class TA, class L>
+__device__ __forceinline__ void load4(const TA* p, typename Acc<TA>::type o[4]);
+template <>
+__device__ __forceinline__ void load4<float, LdPlain>(const float* p, float o[4])
+{
+	const float4 t = *(const float4*)p;
+	o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+}
+template <>
+__device__ __forceinline__ void load4<float, LdCG>(const float* p, float o[4])
+{
+	const float4 t = __ldcg((const float4*)p);
+	o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+}
+template <>
+__device__ __forceinline__ void load4<double, LdPlain>(const double* p, double o[4])
+{
+	const double2 a = *(const double2*)p, b = *(const double2*)(p + 2);
+	o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+template <>
+__device__ __forceinline__ void load4<double, LdCG>(const double* p, double o[4])
+{
+	const double2 a = __ldcg((const double2*)p), b = __ldcg((const double2*)(p + 2));
+	o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+__device__ __forceinline__ void unpack_bf16x4(uint2 t, float o[4])
+{
+	o[0] = __uint_as_float(t.x << 16);
+	o[1] = __uint_as_float(t.x & 0xffff0000u);
+	o[2] = __uint_as_float(t.y << 16);
+	o[3] = __uint_as_float(t.y & 0xffff0000u);
+}
+template <>
+__device__ __forceinline__ void load4<__nv_bfloat16, LdPlain>(const __nv_bfloat16* p, float o[4])
+{
+	unpack_bf16x4(*(const uint2*)p, o);
+}
+template <>
+__device__ __forceinline__ void load4<__nv_bfloat16, LdCG>(const __nv_bfloat16* p, float o[4])
+{
+	unpack_bf16x4(__ldcg((const uint2*)p), o);
+}
+
+// q_i = (A x)_i for row i = 32 s + lane of a slice of width w (a multiple of 4). Per group of
+// four blocks a lane issues one 16-byte load of column ids, one vector load per value plane and
+// four 16-byte gathers of x, all before the first FMA. Padding blocks are zero.
 template <class TA, class TV, class L = LdPlain>
 __device__ __forceinline__ void spmv_row(const TA* A, const int* __restrict__ col, int nslots, int base, int w,
-                                         int lane, const TV* x, int np, TV out[3])
+                                         int lane, const TV* x, TV out[3])
 {
 	typedef typename Acc<TA>::type AT;
 	AT o0 = 0, o1 = 0, o2 = 0;
 	const size_t ns = (size_t)nslots;
-	int k = 0;
-	for (; k + 4 <= w; k += 4)
+	for (int k = 0; k < w; k += kGroup)
 	{
-		int slot[4], j[4];
-		AT a[4][9], xv[4][3];
+		const size_t off = block_slot((size_t)base, k, lane);
+		const int4 jj = __ldg((const int4*)(col + off));
+		AT a[9][4];
+#pragma unroll
+		for (int p = 0; p < 9; ++p) load4<TA, L>(A + p * ns + off, a[p]);
+		TV xv[4][3];
+		vld<TV, L>(x, jj.x, xv[0]);
+		vld<TV, L>(x, jj.y, xv[1]);
+		vld<TV, L>(x, jj.z, xv[2]);
+		vld<TV, L>(x, jj.w, xv[3]);
 #pragma unroll
 		for (int u = 0; u < 4; ++u)
 		{
-			slot[u] = base + (k + u) * kSlice + lane;
-			j[u] = __ldg(col + slot[u]);
+			const AT x0 = (AT)xv[u][0], x1 = (AT)xv[u][1], x2 = (AT)xv[u][2];
+			o0 += a[0][u] * x0 + a[1][u] * x1 + a[2][u] * x2;
+			o1 += a[3][u] * x0 + a[4][u] * x1 + a[5][u] * x2;
+			o2 += a[6][u] * x0 + a[7][u] * x1 + a[8][u] * x2;
 		}
-#pragma unroll
-		for (int u = 0; u < 4; ++u)
-#pragma unroll
-			for (int p = 0; p < 9; ++p) a[u][p] = widen(L::ld(A + p * ns + slot[u]));
-#pragma unroll
-		for (int u = 0; u < 4; ++u)
-		{
-			xv[u][0] = (AT)L::ld(x + j[u]);
-			xv[u][1] = (AT)L::ld(x + np + j[u]);
-			xv[u][2] = (AT)L::ld(x + 2 * np + j[u]);
-		}
-#pragma unroll
-		for (int u = 0; u < 4; ++u)
-		{
-			o0 += a[u][0] * xv[u][0] + a[u][1] * xv[u][1] + a[u][2] * xv[u][2];
-			o1 += a[u][3] * xv[u][0] + a[u][4] * xv[u][1] + a[u][5] * xv[u][2];
-			o2 += a[u][6] * xv[u][0] + a[u][7] * xv[u][1] + a[u][8] * xv[u][2];
-		}
-	}
-	for (; k < w; ++k)
-	{
-		const int slot = base + k * kSlice + lane;
-		const int j = __ldg(col + slot);
-		AT a[9];
-#pragma unroll
-		for (int p = 0; p < 9; ++p) a[p] = widen(L::ld(A + p * ns + slot));
-		AT x0 = (AT)L::ld(x + j), x1 = (AT)L::ld(x + np + j), x2 = (AT)L::ld(x + 2 * np + j);
-		o0 += a[0] * x0 + a[1] * x1 + a[2] * x2;
-		o1 += a[3] * x0 + a[4] * x1 + a[5] * x2;
-		o2 += a[6] * x0 + a[7] * x1 + a[8] * x2;
 	}
 	out[0] = (TV)o0;
 	out[1] = (TV)o1;
@@ -792,19 +854,23 @@ template <class TV, class L = LdPlain>
 __device__ __forceinline__ void precond_row(const DevBody& B, int i, const TV r[3], TV s[3])
 {
 	const TV* M = (const TV*)B.Minv;
-	const int np = B.npad;
 	if (B.precond == B3G_PRECOND_BLOCK_JACOBI)
 	{
-#pragma unroll
-		for (int a = 0; a < 3; ++a)
-			s[a] = L::ld(M + (size_t)(3 * a) * np + i) * r[0] + L::ld(M + (size_t)(3 * a + 1) * np + i) * r[1] +
-			       L::ld(M + (size_t)(3 * a + 2) * np + i) * r[2];
+		TV m0[3], m1[3], m2[3];
+		vld<TV, L>(M, 3 * i, m0);
+		vld<TV, L>(M, 3 * i + 1, m1);
+		vld<TV, L>(M, 3 * i + 2, m2);
+		s[0] = m0[0] * r[0] + m0[1] * r[1] + m0[2] * r[2];
+		s[1] = m1[0] * r[0] + m1[1] * r[1] + m1[2] * r[2];
+		s[2] = m2[0] * r[0] + m2[1] * r[1] + m2[2] * r[2];
 	}
 	else
 	{
-		s[0] = L::ld(M + i) * r[0];
-		s[1] = L::ld(M + np + i) * r[1];
-		s[2] = L::ld(M + 2 * np + i) * r[2];
+		TV m[3];
+		vld<TV, L>(M, i, m);
+		s[0] = m[0] * r[0];
+		s[1] = m[1] * r[1];
+		s[2] = m[2] * r[2];
 	}
 }
 
@@ -867,9 +933,9 @@ __device__ __forceinline__ void find_new_contacts(const DevBody& B, int i, float
 template <class TV, class L = LdPlain>
 __device__ __forceinline__ double final_vertex(const DevBody& B, int i, float h, bool first_newton, bool finish)
 {
-	const int np = B.npad;
-	const TV* py = (const TV*)B.py;
-	float3 dv = f3((float)L::ld(py + i), (float)L::ld(py + np + i), (float)L::ld(py + 2 * np + i));
+	TV y3[3];
+	vld<TV, L>((const TV*)B.py, i, y3);
+	float3 dv = f3((float)y3[0], (float)y3[1], (float)y3[2]);
 	float3 v = ldl3<L>(first_newton ? B.v : B.vi, i) + dv;
 	float3 x = ldl3<L>(B.x, i) + h * v + ldl3<L>(B.trans, i);
 	if (finish)

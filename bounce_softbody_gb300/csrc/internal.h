@@ -2,14 +2,21 @@
 // kernels (kernels.cu, persistent.cu) and the C ABI (api.cu).
 //
 // Matrix storage: sliced block-ELL with 32 rows per slice ("SELL-32", one warp per slice, one
-// lane per block row). Slice s owns slots [slice_ptr[s], slice_ptr[s+1]) = width_s * 32 slots;
-// the k-th block of row i = 32 s + lane sits in slot slice_ptr[s] + 32 k + lane. The 3x3 block
-// values live in 9 planes (plane p holds entry p = 3 * row + col of every slot), so a warp reads
-// 32 consecutive values per plane per k: fully coalesced, no reduction across lanes, no padding
-// bytes read (rowlen predicates the tail). The diagonal block is always slot k = 0 of its row.
+// lane per block row). Slice s owns slots [slice_ptr[s], slice_ptr[s+1]) = width_s * 32 slots,
+// width_s a multiple of kGroup = 4. The k-th block of row i = 32 s + lane sits in
+//   block_slot(s, k, lane) = slice_ptr[s] + 128 (k / 4) + 4 lane + k % 4,
+// so one lane's four consecutive blocks are adjacent: a lane loads each of the 9 value planes of
+// a group of four blocks, and their column ids, as single 16-byte vectors, and a warp's loads
+// cover 512 consecutive bytes. Plane p (entry p = 3 * row + col of a 3x3 block) of every slot
+// lives at p * nslots + slot. Slots past the end of a row hold zero blocks whose column is the
+// row itself. The diagonal block is always k = 0.
+// Per-slot contribution lists use the item index list_item(s, k, lane) = slice_ptr[s] + 32 k +
+// lane (same range, different order) so that a warp reading the lists of its 32 rows at one k
+// touches consecutive words.
 //
-// Solver vectors are planar too: component c of vertex i at c * npad + i (npad = 32 * nslices).
-// Vertex state (x, v, external force, translation) stays 3 floats per vertex, like b3Vec3 arrays.
+// Solver vectors are 4-wide per vertex (x, y, z, unused) so a neighbour's value is one 16-byte
+// load: component c of vertex i at 4 i + c. Vertex state (x, v, external force, translation)
+// stays 3 floats per vertex, like b3Vec3 arrays.
 #pragma once
 
 #include <stdint.h>
@@ -30,6 +37,9 @@
 namespace b3g {
 
 constexpr int kSlice = 32;
+constexpr int kGroup = 4;
+
+B3G_HD size_t block_slot(size_t base, int k, int lane) { return base + 128 * (size_t)(k >> 2) + 4 * lane + (k & 3); }
 constexpr int kMaxWorld = 4;
 constexpr int kMaxTeamCtas = 16;
 
@@ -53,7 +63,7 @@ struct Scalars
 	int refresh;       // refresh period
 	unsigned counter;  // arrival counter of the deterministic grid reduction (plain path)
 	int pending_check; // bf16 mode: recursive residual met the tolerance, confirm with a refresh
-	int pad;
+	int fault;         // a bounded device wait expired (the step's results are not valid)
 	unsigned long long total_iters;  // PCG iterations of every step since creation
 	unsigned long long total_steps;
 };
@@ -73,7 +83,7 @@ struct DevBody
 	const uint8_t* rowlen;      // npad (0 for padding rows)
 	float* A32;                 // 9 * nslots
 	void* Alo;                  // 9 * nslots of the precision's storage type (double / bf16), or null
-	void* Minv;                 // 3 * npad (scalar Jacobi) or 9 * npad (block Jacobi), vector type
+	void* Minv;                 // 4 per vertex (scalar Jacobi) or 12 (three rows, block Jacobi), vector type
 
 	// contribution lists in element order (deterministic), interleaved across the 32 lanes of a
 	// slice: entry t of item j (a slot, or a row) sits at start[j] + 32 t, so a warp reading entry

@@ -4,6 +4,8 @@
 #include "device.cuh"
 #include "ops.h"
 
+#include <algorithm>
+
 namespace b3g {
 
 namespace {
@@ -118,6 +120,7 @@ __global__ void k_begin(Scalars* sc, int max_it, double tol2, int refresh, doubl
 	sc->max_it = 0;
 	sc->counter = 0u;
 	sc->pending_check = 0;
+	sc->fault = 0;
 	sc->delta = sc->delta0 = 0.0;
 	sc->alpha = sc->beta = sc->dq = 0.0;
 }
@@ -187,31 +190,23 @@ template <class TA, class TV>
 __global__ void __launch_bounds__(kThreads) k_pcg_init(DevBody B, const TA* A)
 {
 	const int lane = threadIdx.x & 31;
-	const int np = B.npad;
 	double part = 0.0;
-	const TV* py = (const TV*)B.py;
-	TV* pb = (TV*)B.pb;
-	TV* r = (TV*)B.r;
-	TV* s = (TV*)B.s;
-	TV* d = (TV*)B.d;
 	for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < B.nslices; sl += (gridDim.x * blockDim.x) >> 5)
 	{
-		int i = sl * kSlice + lane;
+		const int i = sl * kSlice + lane;
 		if (i >= B.n) continue;
-		int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-		TV q[3];
-		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, py, np, q);
-		TV rr[3] = {pb[i] - q[0], pb[np + i] - q[1], pb[2 * np + i] - q[2]};
-		TV ss[3];
-		precond_row<TV>(B, i, rr, ss);
+		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
+		TV q[3], b[3], rr[3], ss[3];
+		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, (const TV*)B.py, q);
+		vld<TV, LdPlain>((const TV*)B.pb, i, b);
 #pragma unroll
-		for (int c = 0; c < 3; ++c)
-		{
-			r[c * np + i] = rr[c];
-			s[c * np + i] = ss[c];
-			d[c * np + i] = ss[c];
-			part += (double)rr[c] * (double)ss[c];
-		}
+		for (int c = 0; c < 3; ++c) rr[c] = b[c] - q[c];
+		precond_row<TV>(B, i, rr, ss);
+		vst((TV*)B.r, i, rr);
+		vst((TV*)B.s, i, ss);
+		vst((TV*)B.d, i, ss);
+#pragma unroll
+		for (int c = 0; c < 3; ++c) part += (double)rr[c] * (double)ss[c];
 	}
 	double total;
 	if (grid_reduce(part, B.partials, &B.sc->counter, &total)) pcg_start(B.sc, total);
@@ -223,23 +218,19 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(DevBody B, const TA* A)
 {
 	if (B.sc->done) return;
 	const int lane = threadIdx.x & 31;
-	const int np = B.npad;
 	const TV* d = (const TV*)B.d;
-	TV* q = (TV*)B.q;
 	double part = 0.0;
 	for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < B.nslices; sl += (gridDim.x * blockDim.x) >> 5)
 	{
-		int i = sl * kSlice + lane;
+		const int i = sl * kSlice + lane;
 		if (i >= B.n) continue;
-		int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-		TV o[3];
-		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, d, np, o);
+		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
+		TV o[3], dd[3];
+		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, d, o);
+		vst((TV*)B.q, i, o);
+		vld<TV, LdPlain>(d, i, dd);
 #pragma unroll
-		for (int c = 0; c < 3; ++c)
-		{
-			q[c * np + i] = o[c];
-			part += (double)d[c * np + i] * (double)o[c];
-		}
+		for (int c = 0; c < 3; ++c) part += (double)dd[c] * (double)o[c];
 	}
 	double total;
 	if (grid_reduce(part, B.partials, &B.sc->counter, &total))
@@ -268,33 +259,29 @@ __global__ void __launch_bounds__(kThreads) k_update(DevBody B, int bf16_mode)
 	Scalars* sc = B.sc;
 	if (sc->done) return;
 	const bool refresh = refresh_now(sc);
-	const int np = B.npad;
 	const TV alpha = (TV)sc->alpha;
-	TV* x = (TV*)B.py;
-	const TV* d = (const TV*)B.d;
-	const TV* q = (const TV*)B.q;
-	TV* r = (TV*)B.r;
-	TV* s = (TV*)B.s;
 	double part = 0.0;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
 	{
+		TV x[3], d[3], r[3], q[3], s[3];
+		vld<TV, LdPlain>((const TV*)B.py, i, x);
+		vld<TV, LdPlain>((const TV*)B.d, i, d);
+		if (!refresh)
+		{
+			vld<TV, LdPlain>((const TV*)B.r, i, r);
+			vld<TV, LdPlain>((const TV*)B.q, i, q);
+		}
 #pragma unroll
-		for (int c = 0; c < 3; ++c) x[c * np + i] += alpha * d[c * np + i];
+		for (int c = 0; c < 3; ++c) x[c] += alpha * d[c];
+		vst((TV*)B.py, i, x);
 		if (refresh) continue;
-		TV rr[3], ss[3];
 #pragma unroll
-		for (int c = 0; c < 3; ++c)
-		{
-			rr[c] = r[c * np + i] - alpha * q[c * np + i];
-			r[c * np + i] = rr[c];
-		}
-		precond_row<TV>(B, i, rr, ss);
+		for (int c = 0; c < 3; ++c) r[c] -= alpha * q[c];
+		precond_row<TV>(B, i, r, s);
+		vst((TV*)B.r, i, r);
+		vst((TV*)B.s, i, s);
 #pragma unroll
-		for (int c = 0; c < 3; ++c)
-		{
-			s[c * np + i] = ss[c];
-			part += (double)rr[c] * (double)ss[c];
-		}
+		for (int c = 0; c < 3; ++c) part += (double)r[c] * (double)s[c];
 	}
 	if (refresh) return;
 	double total;
@@ -309,29 +296,22 @@ __global__ void __launch_bounds__(kThreads) k_resid(DevBody B, const TA* A, int 
 	if (sc->done) return;
 	if (!refresh_now(sc)) return;
 	const int lane = threadIdx.x & 31;
-	const int np = B.npad;
-	const TV* py = (const TV*)B.py;
-	const TV* pb = (const TV*)B.pb;
-	TV* r = (TV*)B.r;
-	TV* s = (TV*)B.s;
 	double part = 0.0;
 	for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < B.nslices; sl += (gridDim.x * blockDim.x) >> 5)
 	{
-		int i = sl * kSlice + lane;
+		const int i = sl * kSlice + lane;
 		if (i >= B.n) continue;
-		int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-		TV q[3];
-		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, py, np, q);
-		TV rr[3] = {pb[i] - q[0], pb[np + i] - q[1], pb[2 * np + i] - q[2]};
-		TV ss[3];
-		precond_row<TV>(B, i, rr, ss);
+		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
+		TV q[3], b[3], rr[3], ss[3];
+		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, (const TV*)B.py, q);
+		vld<TV, LdPlain>((const TV*)B.pb, i, b);
 #pragma unroll
-		for (int c = 0; c < 3; ++c)
-		{
-			r[c * np + i] = rr[c];
-			s[c * np + i] = ss[c];
-			part += (double)rr[c] * (double)ss[c];
-		}
+		for (int c = 0; c < 3; ++c) rr[c] = b[c] - q[c];
+		precond_row<TV>(B, i, rr, ss);
+		vst((TV*)B.r, i, rr);
+		vst((TV*)B.s, i, ss);
+#pragma unroll
+		for (int c = 0; c < 3; ++c) part += (double)rr[c] * (double)ss[c];
 	}
 	double total;
 	if (grid_reduce(part, B.partials, &sc->counter, &total)) decide_after_reduction(sc, total, bf16_mode != 0, true);
@@ -343,14 +323,15 @@ __global__ void __launch_bounds__(kThreads) k_direction(DevBody B)
 {
 	Scalars* sc = B.sc;
 	if (sc->done) return;
-	const int np = B.npad;
 	const TV beta = (TV)sc->beta;
-	TV* d = (TV*)B.d;
-	const TV* s = (const TV*)B.s;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
 	{
+		TV d[3], s[3];
+		vld<TV, LdPlain>((const TV*)B.d, i, d);
+		vld<TV, LdPlain>((const TV*)B.s, i, s);
 #pragma unroll
-		for (int c = 0; c < 3; ++c) d[c * np + i] = s[c * np + i] + beta * d[c * np + i];
+		for (int c = 0; c < 3; ++c) d[c] = s[c] + beta * d[c];
+		vst((TV*)B.d, i, d);
 	}
 }
 
@@ -444,7 +425,16 @@ StepParams dev_params(const StepParamsHost& P)
 }
 
 int slice_grid(const DevBody& B) { return grid_for(B.nslices, kWarps); }
+
 int vertex_grid(const DevBody& B) { return grid_for(B.n, kThreads); }
+
+// SpMV: one slice per warp, every warp in flight at once where the grid allows
+template <class TA, class TV>
+cudaError_t launch_spmv(const DevBody& B, const TA* A, cudaStream_t st)
+{
+	k_spmv_dot<TA, TV><<<slice_grid(B), kThreads, 0, st>>>(B, A);
+	return cudaGetLastError();
+}
 
 } // namespace
 
@@ -493,21 +483,24 @@ cudaError_t op_pcg_iteration(const DevBody& B, int prec, cudaStream_t st)
 	if (prec == kP64)
 	{
 		const double* A = (const double*)B.Alo;
-		k_spmv_dot<double, double><<<gs, kThreads, 0, st>>>(B, A);
+		cudaError_t e = launch_spmv<double, double>(B, A, st);
+		if (e != cudaSuccess) return e;
 		k_update<double><<<gv, kThreads, 0, st>>>(B, 0);
 		k_resid<double, double><<<gs, kThreads, 0, st>>>(B, A, 0);
 		k_direction<double><<<gv, kThreads, 0, st>>>(B);
 	}
 	else if (prec == kPBF)
 	{
-		k_spmv_dot<__nv_bfloat16, float><<<gs, kThreads, 0, st>>>(B, (const __nv_bfloat16*)B.Alo);
+		cudaError_t e = launch_spmv<__nv_bfloat16, float>(B, (const __nv_bfloat16*)B.Alo, st);
+		if (e != cudaSuccess) return e;
 		k_update<float><<<gv, kThreads, 0, st>>>(B, 1);
 		k_resid<float, float><<<gs, kThreads, 0, st>>>(B, B.A32, 1);
 		k_direction<float><<<gv, kThreads, 0, st>>>(B);
 	}
 	else
 	{
-		k_spmv_dot<float, float><<<gs, kThreads, 0, st>>>(B, B.A32);
+		cudaError_t e = launch_spmv<float, float>(B, B.A32, st);
+		if (e != cudaSuccess) return e;
 		k_update<float><<<gv, kThreads, 0, st>>>(B, 0);
 		k_resid<float, float><<<gs, kThreads, 0, st>>>(B, B.A32, 0);
 		k_direction<float><<<gv, kThreads, 0, st>>>(B);

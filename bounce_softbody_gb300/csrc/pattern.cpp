@@ -227,13 +227,16 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 	{
 		int w = 0;
 		for (int l = 0; l < kSlice; ++l) w = std::max(w, (int)rowlen[s * kSlice + l]);
+		w = (w + kGroup - 1) / kGroup * kGroup;  // whole groups of kGroup slots
 		P.maxw = std::max(P.maxw, w);
 		slice_ptr[s + 1] = slice_ptr[s] + w * kSlice;
 	}
 	P.nslots = slice_ptr[P.nslices];
+	// contribution-list item of (row i, k-th block): list_item(s, k, lane) = slice_ptr[s] + 32 k + lane
 	auto slot_of = [&](uint32_t i, uint32_t k) -> uint32_t {
 		return (uint32_t)slice_ptr[i / kSlice] + k * kSlice + (i % kSlice);
 	};
+	// block slots: block_slot(s, k, lane) = slice_ptr[s] + 128 (k / 4) + 4 lane + k % 4
 	std::vector<int> col(P.nslots, 0);
 	for (int s = 0; s < P.nslices; ++s)
 		for (int l = 0; l < kSlice; ++l)
@@ -241,7 +244,8 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 			uint32_t i = (uint32_t)(s * kSlice + l);
 			int w = (slice_ptr[s + 1] - slice_ptr[s]) / kSlice;
 			for (int k = 0; k < w; ++k)
-				col[slice_ptr[s] + k * kSlice + l] = (i < n && (uint32_t)k < rowlen[i]) ? (int)cols[rowptr[i] + k] : (int)std::min<uint32_t>(i, n - 1);
+				col[block_slot(slice_ptr[s], k, l)] =
+				    (i < n && (uint32_t)k < rowlen[i]) ? (int)cols[rowptr[i] + k] : (int)std::min<uint32_t>(i, n - 1);
 		}
 
 	// contribution counts per slot

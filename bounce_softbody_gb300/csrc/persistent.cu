@@ -128,71 +128,112 @@ __device__ __forceinline__ double update_two(const DevBody& B, TV* __restrict__ 
                                              TV* __restrict__ r, const TV* __restrict__ q, TV* __restrict__ s,
                                              int i0, int i1, bool ok1, TV alpha, bool refresh)
 {
-	const int np = B.npad;
 	const int ii[2] = {i0, i1};
 	const bool ok[2] = {true, ok1};
 	TV x[2][3], dd[2][3], rr[2][3], qq[2][3];
 #pragma unroll
 	for (int u = 0; u < 2; ++u)
-#pragma unroll
-		for (int c = 0; c < 3; ++c)
-			if (ok[u])
+		if (ok[u])
+		{
+			vld<TV, LD>(py, ii[u], x[u]);
+			vld<TV, LD>(d, ii[u], dd[u]);
+			if (!refresh)
 			{
-				x[u][c] = LD::ld(py + c * np + ii[u]);
-				dd[u][c] = LD::ld(d + c * np + ii[u]);
-				if (!refresh)
-				{
-					rr[u][c] = LD::ld(r + c * np + ii[u]);
-					qq[u][c] = LD::ld(q + c * np + ii[u]);
-				}
+				vld<TV, LD>(r, ii[u], rr[u]);
+				vld<TV, LD>(q, ii[u], qq[u]);
 			}
+		}
 	double part = 0.0;
 #pragma unroll
 	for (int u = 0; u < 2; ++u)
 	{
 		if (!ok[u]) continue;
+		TV nx[3];
 #pragma unroll
-		for (int c = 0; c < 3; ++c) py[c * np + ii[u]] = x[u][c] + alpha * dd[u][c];
+		for (int c = 0; c < 3; ++c) nx[c] = x[u][c] + alpha * dd[u][c];
+		vst(py, ii[u], nx);
 		if (refresh) continue;
 		TV nr[3], ss[3];
 #pragma unroll
 		for (int c = 0; c < 3; ++c) nr[c] = rr[u][c] - alpha * qq[u][c];
 		precond_row<TV, LD>(B, ii[u], nr, ss);
+		vst(r, ii[u], nr);
+		vst(s, ii[u], ss);
 #pragma unroll
-		for (int c = 0; c < 3; ++c)
-		{
-			r[c * np + ii[u]] = nr[c];
-			s[c * np + ii[u]] = ss[c];
-			part += (double)nr[c] * (double)ss[c];
-		}
+		for (int c = 0; c < 3; ++c) part += (double)nr[c] * (double)ss[c];
 	}
 	return part;
 }
 
 // d = s + beta d for two rows, loads first
 template <class TV, class LD>
-__device__ __forceinline__ void direction_two(const DevBody& B, TV* __restrict__ d, const TV* __restrict__ s, int i0,
-                                              int i1, bool ok1, TV beta)
+__device__ __forceinline__ void direction_two(TV* __restrict__ d, const TV* __restrict__ s, int i0, int i1, bool ok1,
+                                              TV beta)
 {
-	const int np = B.npad;
 	TV s0[3], d0[3], s1[3], d1[3];
-#pragma unroll
-	for (int c = 0; c < 3; ++c)
+	vld<TV, LD>(s, i0, s0);
+	vld<TV, LD>(d, i0, d0);
+	if (ok1)
 	{
-		s0[c] = LD::ld(s + c * np + i0);
-		d0[c] = LD::ld(d + c * np + i0);
-		if (ok1)
-		{
-			s1[c] = LD::ld(s + c * np + i1);
-			d1[c] = LD::ld(d + c * np + i1);
-		}
+		vld<TV, LD>(s, i1, s1);
+		vld<TV, LD>(d, i1, d1);
 	}
 #pragma unroll
 	for (int c = 0; c < 3; ++c)
 	{
-		d[c * np + i0] = s0[c] + beta * d0[c];
-		if (ok1) d[c * np + i1] = s1[c] + beta * d1[c];
+		d0[c] = s0[c] + beta * d0[c];
+		d1[c] = s1[c] + beta * d1[c];
 	}
+	vst(d, i0, d0);
+	if (ok1) vst(d, i1, d1);
+}
+
+// r = pb - A x, s = M^-1 r for the rows of one warp's slices (init / refresh); optionally d = s
+template <class TA, class TV, class LD>
+__device__ __forceinline__ double residual_rows(const DevBody& B, const TA* A, const TV* x, int s0, int stride,
+                                                bool set_d)
+{
+	const int lane = threadIdx.x & 31;
+	double part = 0.0;
+	for (int sl = s0; sl < B.nslices; sl += stride)
+	{
+		const int i = sl * kSlice + lane;
+		if (i >= B.n) continue;
+		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
+		TV o[3], b[3], rr[3], ss[3];
+		spmv_row<TA, TV, LD>(A, B.col, B.nslots, base, w, lane, x, o);
+		vld<TV, LD>((const TV*)B.pb, i, b);
+#pragma unroll
+		for (int c = 0; c < 3; ++c) rr[c] = b[c] - o[c];
+		precond_row<TV, LD>(B, i, rr, ss);
+		vst((TV*)B.r, i, rr);
+		vst((TV*)B.s, i, ss);
+		if (set_d) vst((TV*)B.d, i, ss);
+#pragma unroll
+		for (int c = 0; c < 3; ++c) part += (double)rr[c] * (double)ss[c];
+	}
+	return part;
+}
+
+// q = A d and this warp's part of d.q
+template <class TA, class TV, class LD>
+__device__ __forceinline__ double spmv_dot_rows(const DevBody& B, const TA* A, const TV* d, TV* q, int s0, int stride)
+{
+	const int lane = threadIdx.x & 31;
+	double part = 0.0;
+	for (int sl = s0; sl < B.nslices; sl += stride)
+	{
+		const int i = sl * kSlice + lane;
+		if (i >= B.n) continue;
+		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
+		TV o[3], dd[3];
+		spmv_row<TA, TV, LD>(A, B.col, B.nslots, base, w, lane, d, o);
+		vst(q, i, o);
+		vld<TV, LD>(d, i, dd);
+#pragma unroll
+		for (int c = 0; c < 3; ++c) part += (double)dd[c] * (double)o[c];
+	}
+	return part;
 }
 
 // The implicit step of one body by one team; mirrors the per-op path of kernels.cu phase for
@@ -204,7 +245,6 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 	// loads are coherent there. Cluster teams read other SMs' writes: L2-coherent loads.
 	typedef typename std::conditional<CL == 1, LdPlain, LdCG>::type LD;
 	const int lane = threadIdx.x & 31;
-	const int np = B.npad;
 	const TA* Asp = (sizeof(TA) == sizeof(float) && !bf16) ? (const TA*)B.A32 : (const TA*)B.Alo;
 	const float h = P.h;
 	TV* py = (TV*)B.py;
@@ -219,6 +259,7 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 	unsigned long long iters_all = 0ull;
 	PhaseClock pc;
 	pc.start(P.prof);
+	if (T.tid() == 0) B.sc->fault = 0;  // ordered before any SpMV by the element-phase barrier
 	for (int k = 0; k < P.newton; ++k)
 	{
 		StepParams sp;
@@ -237,29 +278,9 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 		{
 			// warm start from the previous solution: r = pb - A py
 			T.sync();
-			part = 0.0;
-			for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
-			{
-				const int i = sl * kSlice + lane;
-				if (i >= B.n) continue;
-				const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-				TV o[3], rr[3], ss[3];
-				if (sizeof(TA) == sizeof(double))
-					spmv_row<TA, TV, LD>(Asp, B.col, B.nslots, base, w, lane, py, np, o);
-				else
-					spmv_row<float, TV, LD>(B.A32, B.col, B.nslots, base, w, lane, py, np, o);
-#pragma unroll
-				for (int c = 0; c < 3; ++c) rr[c] = LD::ld(pb + c * np + i) - o[c];
-				precond_row<TV, LD>(B, i, rr, ss);
-#pragma unroll
-				for (int c = 0; c < 3; ++c)
-				{
-					r[c * np + i] = rr[c];
-					s[c * np + i] = ss[c];
-					d[c * np + i] = ss[c];
-					part += (double)rr[c] * (double)ss[c];
-				}
-			}
+			part = (sizeof(TA) == sizeof(double))
+			           ? residual_rows<TA, TV, LD>(B, Asp, py, T.warp(), T.nwarps(), true)
+			           : residual_rows<float, TV, LD>(B, B.A32, py, T.warp(), T.nwarps(), true);
 		}
 		delta0 = T.reduce(part);
 		pc.tick(kPhAsm);
@@ -286,22 +307,8 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 			done = false;
 		while (!done)
 		{
-			// q = A d, alpha = delta / d.q
-			part = 0.0;
-			for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
-			{
-				const int i = sl * kSlice + lane;
-				if (i >= B.n) continue;
-				const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-				TV o[3];
-				spmv_row<TA, TV, LD>(Asp, B.col, B.nslots, base, w, lane, d, np, o);
-#pragma unroll
-				for (int c = 0; c < 3; ++c)
-				{
-					q[c * np + i] = o[c];
-					part += (double)LD::ld(d + c * np + i) * (double)o[c];
-				}
-			}
+			// q = A d (block planes staged through shared memory), alpha = delta / d.q
+			part = spmv_dot_rows<TA, TV, LD>(B, Asp, d, q, T.warp(), T.nwarps());
 			const double dq = T.reduce(part);
 			pc.tick(kPhSpmv);
 			if (!isfinite(dq))
@@ -329,27 +336,9 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 			{
 				// sparse_solver.cpp:83-90: r = b - A x with the full-precision blocks
 				T.sync();
-				for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
-				{
-					const int i = sl * kSlice + lane;
-					if (i >= B.n) continue;
-					const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-					TV o[3], rr[3], ss[3];
-					if (sizeof(TA) == sizeof(double))
-						spmv_row<TA, TV, LD>(Asp, B.col, B.nslots, base, w, lane, py, np, o);
-					else
-						spmv_row<float, TV, LD>(B.A32, B.col, B.nslots, base, w, lane, py, np, o);
-#pragma unroll
-					for (int c = 0; c < 3; ++c) rr[c] = LD::ld(pb + c * np + i) - o[c];
-					precond_row<TV, LD>(B, i, rr, ss);
-#pragma unroll
-					for (int c = 0; c < 3; ++c)
-					{
-						r[c * np + i] = rr[c];
-						s[c * np + i] = ss[c];
-						part += (double)rr[c] * (double)ss[c];
-					}
-				}
+				part = (sizeof(TA) == sizeof(double))
+				           ? residual_rows<TA, TV, LD>(B, Asp, py, T.warp(), T.nwarps(), false)
+				           : residual_rows<float, TV, LD>(B, B.A32, py, T.warp(), T.nwarps(), false);
 			}
 			const double dn = T.reduce(part);
 			pc.tick(kPhUpdate);
@@ -385,7 +374,7 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 				const int sl1 = sl + T.nwarps();
 				const int i1 = sl1 * kSlice + lane;
 				if (i0 >= B.n) continue;
-				direction_two<TV, LD>(B, d, s, i0, i1, sl1 < B.nslices && i1 < B.n, bt);
+				direction_two<TV, LD>(d, s, i0, i1, sl1 < B.nslices && i1 < B.n, bt);
 			}
 			T.sync();
 			pc.tick(kPhDir);
@@ -431,6 +420,7 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 		sc->newton_iter = newton_done_at;
 		sc->newton_err = err;
 		sc->done = 1;
+		if (sc->fault) sc->status = B3G_SOLVE_DEVICE_TIMEOUT;
 		sc->total_iters += iters_all;
 		sc->total_steps += 1ull;
 	}
@@ -449,6 +439,7 @@ __global__ void __launch_bounds__(kPThreads, B3G_BATCH_MIN_BLOCKS) k_batch(Batch
 {
 	__shared__ TeamShared sh;
 	__shared__ __align__(16) DevBody sb;
+
 	if (CL > 1)
 	{
 		cg::cluster_group cl = cg::this_cluster();
@@ -524,6 +515,7 @@ int max_clusters()
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(CL * 64, 1, 1);
 	cfg.blockDim = dim3(kPThreads, 1, 1);
+	cfg.dynamicSmemBytes = 0;
 	cudaLaunchAttribute attr[1];
 	attr[0].id = cudaLaunchAttributeClusterDimension;
 	attr[0].val.clusterDim.x = CL;

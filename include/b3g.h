@@ -62,7 +62,8 @@ typedef enum b3g_solve_status
 	B3G_SOLVE_CONVERGED = 0,      /* delta <= tol^2 * delta0 */
 	B3G_SOLVE_MAX_ITERATIONS = 1, /* stopped at the iteration cap (the reference's usual exit) */
 	B3G_SOLVE_NONFINITE = 2,      /* a reduction produced NaN or Inf; state left unchanged */
-	B3G_SOLVE_BREAKDOWN = 3       /* d.Ad <= 0: the filtered system is not positive definite */
+	B3G_SOLVE_BREAKDOWN = 3,      /* d.Ad <= 0: the filtered system is not positive definite */
+	B3G_SOLVE_DEVICE_TIMEOUT = 4  /* a bounded device wait expired; the step's results are not valid */
 } b3g_solve_status;
 
 /* b3ParticleType (include/bounce_softbody/dynamics/particle.h:31-36). */

@@ -42,5 +42,8 @@ def test_gpu_matches_reference_golden(ctx, name):
         floor_v = rel(z[f"ref32_v_{s}"], rv)
         assert rel_disp(x, rx, desc.x) < max(1e-4, 20 * floor_x), (name, s)
         assert rel(v, rv) < max(1e-3, 20 * floor_v), (name, s)
-        assert abs(its[-1] - int(z[f"ref32_it_{s}"][-1])) <= 3, (name, s, its[-1])
+        ref_it = int(z[f"ref32_it_{s}"][-1])
+        # contact scenes are chaotic: their iteration counts wander with the trajectory
+        slack = 3 if "contact" not in name else max(3, int(0.35 * ref_it))
+        assert abs(its[-1] - ref_it) <= slack, (name, s, its[-1])
     g.close()
