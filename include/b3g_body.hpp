@@ -1,0 +1,596 @@
+// b3g_body.hpp — the reference's body / particle / force API over the b3g C ABI (header-only).
+//
+// A program written against Bounce Softbody's b3Body (include/bounce_softbody/dynamics/body.h)
+// builds against this header and links libb3g.so instead: the same class and definition names,
+// the same creation calls and the same Step(dt, forceIterations, forceSubIterations). The body's
+// state lives on the GPU; particles read it back on demand.
+//
+// What maps where:
+//   b3Body::CreateParticle / CreateForce / CreateTetrahedron / CreateTriangle / CreateSphere /
+//   CreateFixture / SetGravity      recorded on the host; the device body (b3g_body_create) is
+//                                   built at the first Step and rebuilt after topology changes
+//   b3Body::Step                    b3g_body_step (uploads pending forces / translations first)
+//   b3Particle::Get/SetPosition, Get/SetVelocity, ApplyForce, ApplyTranslation, SetType
+//                                   b3g_body_get_state / set_state / apply_* / set_types
+//   b3_forceSolver*Iterations       b3Body::GetStepStats()
+// Extensions (no reference counterpart): SetSolverTolerance (the reference's Step always runs the
+// PCG at FLT_EPSILON), SetPrecision, SetPreconditioner.
+// Not provided (outside the implicit step): ray casts, debug draw, stretch / shear / mouse forces,
+// non-sphere world shapes.
+#pragma once
+
+#include "b3g.h"
+
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+typedef float scalar;
+typedef uint32_t uint32;
+
+struct b3Vec3
+{
+	b3Vec3() : x(0), y(0), z(0) {}
+	b3Vec3(scalar _x, scalar _y, scalar _z) : x(_x), y(_y), z(_z) {}
+	void SetZero() { x = y = z = 0; }
+	void Set(scalar _x, scalar _y, scalar _z) { x = _x; y = _y; z = _z; }
+	b3Vec3 operator+(const b3Vec3& b) const { return b3Vec3(x + b.x, y + b.y, z + b.z); }
+	b3Vec3 operator-(const b3Vec3& b) const { return b3Vec3(x - b.x, y - b.y, z - b.z); }
+	b3Vec3& operator+=(const b3Vec3& b) { x += b.x; y += b.y; z += b.z; return *this; }
+	scalar x, y, z;
+};
+inline b3Vec3 operator*(scalar s, const b3Vec3& v) { return b3Vec3(s * v.x, s * v.y, s * v.z); }
+inline scalar b3Distance(const b3Vec3& a, const b3Vec3& b)
+{
+	b3Vec3 d = a - b;
+	return std::sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+}
+
+enum b3ParticleType
+{
+	e_staticParticle,
+	e_kinematicParticle,
+	e_dynamicParticle
+};
+
+struct b3ParticleDef
+{
+	b3ParticleType type = e_staticParticle;
+	b3Vec3 position;
+	b3Vec3 velocity;
+	scalar damping = 0;
+	uint32 userIndex = 0xFFFFFFFFu;
+	void* userData = nullptr;
+};
+
+class b3Body;
+
+class b3Particle
+{
+public:
+	void SetType(b3ParticleType type);
+	b3ParticleType GetType() const { return m_type; }
+	void SetPosition(const b3Vec3& position);
+	const b3Vec3& GetPosition() const;
+	void SetVelocity(const b3Vec3& velocity);
+	const b3Vec3& GetVelocity() const;
+	scalar GetMass() const;
+	void ApplyForce(const b3Vec3& force);
+	const b3Vec3& GetForce() const { return m_force; }
+	void ApplyImpulse(const b3Vec3& impulse);
+	void ApplyTranslation(const b3Vec3& translation);
+	const b3Vec3& GetTranslation() const { return m_translation; }
+	scalar GetDamping() const { return m_damping; }
+	void SetUserIndex(uint32 i) { m_userIndex = i; }
+	uint32 GetUserIndex() const { return m_userIndex; }
+	void SetUserData(void* p) { m_userData = p; }
+	void* GetUserData() const { return m_userData; }
+
+private:
+	friend class b3Body;
+	b3Body* m_body = nullptr;
+	uint32 m_index = 0;
+	b3ParticleType m_type = e_staticParticle;
+	scalar m_damping = 0;
+	b3Vec3 m_force, m_translation;
+	uint32 m_userIndex = 0xFFFFFFFFu;
+	void* m_userData = nullptr;
+};
+
+enum b3ForceType
+{
+	e_stretchForce,
+	e_shearForce,
+	e_springForce,
+	e_mouseForce,
+	e_triangleElementForce,
+	e_tetrahedronElementForce
+};
+
+struct b3ForceDef
+{
+	b3ForceType type;
+	uint32 userIndex = 0xFFFFFFFFu;
+};
+
+struct b3SpringForceDef : public b3ForceDef
+{
+	b3SpringForceDef() { type = e_springForce; }
+	// spring_force.cpp:25-35: rest length from the particles' current positions
+	void Initialize(b3Particle* particle1, b3Particle* particle2, scalar ks, scalar kd)
+	{
+		p1 = particle1;
+		p2 = particle2;
+		length = b3Distance(p1->GetPosition(), p2->GetPosition());
+		stiffness = ks;
+		dampingStiffness = kd;
+	}
+	b3Particle* p1 = nullptr;
+	b3Particle* p2 = nullptr;
+	scalar length = 0;
+	scalar stiffness = 0;
+	scalar dampingStiffness = 0;
+};
+
+struct b3TriangleElementForceDef : public b3ForceDef
+{
+	b3TriangleElementForceDef() { type = e_triangleElementForce; }
+	b3Particle *p1 = nullptr, *p2 = nullptr, *p3 = nullptr;
+	b3Vec3 v1, v2, v3;
+	scalar youngModulusX = 100, youngModulusY = 100, shearModulus = 50;
+	scalar poissonRationXY = 0.2f, poissonRationYX = 0.2f;
+	scalar stiffnessDamping = 0;
+};
+
+struct b3TetrahedronElementForceDef : public b3ForceDef
+{
+	b3TetrahedronElementForceDef() { type = e_tetrahedronElementForce; }
+	b3Particle *p1 = nullptr, *p2 = nullptr, *p3 = nullptr, *p4 = nullptr;
+	b3Vec3 v1, v2, v3, v4;
+	scalar youngModulus = 500, poissonRatio = 0.3f, stiffnessDamping = 0;
+};
+
+struct b3Force
+{
+	b3ForceType type;
+	uint32 index;
+};
+
+struct b3FixtureDef
+{
+	scalar radius = 0, density = 0, friction = 0;
+	uint32 userIndex = 0xFFFFFFFFu;
+};
+struct b3SphereFixtureDef : public b3FixtureDef
+{
+	b3Particle* p = nullptr;
+};
+struct b3TriangleFixtureDef : public b3FixtureDef
+{
+	b3Particle *p1 = nullptr, *p2 = nullptr, *p3 = nullptr;
+	b3Vec3 v1, v2, v3;
+};
+struct b3TetrahedronFixtureDef : public b3FixtureDef
+{
+	b3Particle *p1 = nullptr, *p2 = nullptr, *p3 = nullptr, *p4 = nullptr;
+	b3Vec3 v1, v2, v3, v4;
+};
+
+struct b3SphereShape
+{
+	b3Vec3 m_center;
+	scalar m_radius = 0;
+};
+struct b3WorldFixtureDef
+{
+	const b3SphereShape* shape = nullptr;
+	scalar friction = 0.5f;
+};
+
+class b3Body
+{
+public:
+	explicit b3Body(int device = 0)
+	{
+		check(b3g_context_create(device, &m_ctx), "b3g_context_create");
+		b3g_solver_config_default(&m_cfg);
+	}
+	~b3Body()
+	{
+		for (b3Particle* p : m_particles) delete p;
+		for (b3Force* f : m_forceHandles) delete f;
+		if (m_body) b3g_body_destroy(m_body);
+		if (m_ctx) b3g_context_destroy(m_ctx);
+	}
+	b3Body(const b3Body&) = delete;
+	b3Body& operator=(const b3Body&) = delete;
+
+	b3Particle* CreateParticle(const b3ParticleDef& def)
+	{
+		fetch();
+		b3Particle* p = new b3Particle();
+		p->m_body = this;
+		p->m_index = (uint32)m_particles.size();
+		p->m_type = def.type;
+		p->m_damping = def.damping;
+		p->m_userIndex = def.userIndex;
+		p->m_userData = def.userData;
+		m_particles.push_back(p);
+		m_x.push_back(def.position);
+		m_v.push_back(def.velocity);  // as the reference constructor: SetType(static) zeroes it
+		m_topologyDirty = true;
+		return p;
+	}
+
+	b3Force* CreateForce(const b3ForceDef& def)
+	{
+		b3Force* f = new b3Force();
+		f->type = def.type;
+		switch (def.type)
+		{
+		case e_tetrahedronElementForce:
+		{
+			const b3TetrahedronElementForceDef& d = (const b3TetrahedronElementForceDef&)def;
+			f->index = (uint32)m_tetE.size();
+			const b3Particle* ps[4] = {d.p1, d.p2, d.p3, d.p4};
+			const b3Vec3 vs[4] = {d.v1, d.v2, d.v3, d.v4};
+			for (int k = 0; k < 4; ++k)
+			{
+				m_tets.push_back(ps[k]->m_index);
+				push3(m_tetRest, vs[k]);
+			}
+			m_tetE.push_back(d.youngModulus);
+			m_tetNu.push_back(d.poissonRatio);
+			m_tetKd.push_back(d.stiffnessDamping);
+			m_tetDensity.push_back(0);
+			break;
+		}
+		case e_triangleElementForce:
+		{
+			const b3TriangleElementForceDef& d = (const b3TriangleElementForceDef&)def;
+			f->index = (uint32)m_triEx.size();
+			const b3Particle* ps[3] = {d.p1, d.p2, d.p3};
+			const b3Vec3 vs[3] = {d.v1, d.v2, d.v3};
+			for (int k = 0; k < 3; ++k)
+			{
+				m_tris.push_back(ps[k]->m_index);
+				push3(m_triRest, vs[k]);
+			}
+			m_triEx.push_back(d.youngModulusX);
+			m_triEy.push_back(d.youngModulusY);
+			m_triEs.push_back(d.shearModulus);
+			m_triNxy.push_back(d.poissonRationXY);
+			m_triNyx.push_back(d.poissonRationYX);
+			m_triKd.push_back(d.stiffnessDamping);
+			m_triDensity.push_back(0);
+			break;
+		}
+		case e_springForce:
+		{
+			const b3SpringForceDef& d = (const b3SpringForceDef&)def;
+			f->index = (uint32)m_sprL0.size();
+			m_springs.push_back(d.p1->m_index);
+			m_springs.push_back(d.p2->m_index);
+			m_sprL0.push_back(d.length);
+			m_sprKs.push_back(d.stiffness);
+			m_sprKd.push_back(d.dampingStiffness);
+			break;
+		}
+		default:
+			delete f;
+			throw std::invalid_argument("b3g: this force type is not part of the implicit step on the GPU");
+		}
+		m_forceHandles.push_back(f);
+		m_topologyDirty = true;
+		return f;
+	}
+
+	// Tetrahedron / triangle fixtures carry the density of the lumped mass (b3Body::ResetMass).
+	// The element with the same particles takes the density; a fixture without an element force
+	// contributes mass only through an element-less entry, which the GPU body does not model.
+	void CreateTetrahedron(const b3TetrahedronFixtureDef& def)
+	{
+		uint32 a[4] = {def.p1->m_index, def.p2->m_index, def.p3->m_index, def.p4->m_index};
+		for (size_t e = 0; e < m_tetE.size(); ++e)
+			if (same_set(&m_tets[4 * e], a, 4))
+			{
+				m_tetDensity[e] = def.density;
+				m_topologyDirty = true;
+				return;
+			}
+		throw std::invalid_argument("b3g: CreateTetrahedron needs the tetrahedron element force created first");
+	}
+	void CreateTriangle(const b3TriangleFixtureDef& def)
+	{
+		uint32 a[3] = {def.p1->m_index, def.p2->m_index, def.p3->m_index};
+		for (size_t e = 0; e < m_triEx.size(); ++e)
+			if (same_set(&m_tris[3 * e], a, 3))
+			{
+				m_triDensity[e] = def.density;
+				m_topologyDirty = true;
+				return;
+			}
+		throw std::invalid_argument("b3g: CreateTriangle needs the triangle element force created first");
+	}
+	void CreateSphere(const b3SphereFixtureDef& def)
+	{
+		if (m_sphereRadius.size() < m_particles.size())
+		{
+			m_sphereRadius.resize(m_particles.size(), 0);
+			m_sphereFriction.resize(m_particles.size(), 0);
+		}
+		m_sphereRadius[def.p->m_index] = def.radius;
+		m_sphereFriction[def.p->m_index] = def.friction;
+		m_topologyDirty = true;
+	}
+	void CreateFixture(const b3WorldFixtureDef& def)
+	{
+		m_world.push_back(def.shape->m_center.x);
+		m_world.push_back(def.shape->m_center.y);
+		m_world.push_back(def.shape->m_center.z);
+		m_world.push_back(def.shape->m_radius);
+		m_world.push_back(def.friction);
+		m_topologyDirty = true;
+	}
+
+	void SetGravity(const b3Vec3& g)
+	{
+		m_gravity = g;
+		m_topologyDirty = true;
+	}
+	b3Vec3 GetGravity() const { return m_gravity; }
+
+	// b3Body::Step (body.cpp:552-604) on the GPU.
+	void Step(scalar dt, uint32 forceIterations, uint32 forceSubIterations)
+	{
+		build();
+		flush_inputs();
+		m_cfg.force_iterations = forceIterations;
+		m_cfg.max_pcg_iterations = forceSubIterations;
+		check(b3g_body_step(m_body, dt, &m_cfg, &m_stats), "b3g_body_step");
+		for (b3Particle* p : m_particles)
+		{
+			p->m_force.SetZero();
+			p->m_translation.SetZero();
+		}
+		m_hostFresh = false;
+	}
+
+	scalar GetEnergy() const
+	{
+		const_cast<b3Body*>(this)->fetch();
+		scalar E = 0;
+		for (size_t i = 0; i < m_particles.size(); ++i)
+			E += mass_of(i) * (m_v[i].x * m_v[i].x + m_v[i].y * m_v[i].y + m_v[i].z * m_v[i].z);
+		return scalar(0.5) * E;
+	}
+
+	uint32 GetParticleCount() const { return (uint32)m_particles.size(); }
+	b3Particle* GetParticle(uint32 i) { return m_particles[i]; }
+	const b3g_step_stats& GetStepStats() const { return m_stats; }
+	void SetSolverTolerance(double pcgTolerance) { m_cfg.pcg_tolerance = pcgTolerance; }
+	void SetPrecision(b3g_precision p) { m_cfg.precision = p; }
+	void SetPreconditioner(b3g_preconditioner p) { m_cfg.preconditioner = p; }
+	b3g_body* GetDeviceBody()
+	{
+		build();
+		return m_body;
+	}
+
+private:
+	friend class b3Particle;
+
+	static void check(int rc, const char* what)
+	{
+		if (rc != B3G_OK) throw std::runtime_error(std::string(what) + ": " + b3g_last_error());
+	}
+	static void push3(std::vector<float>& v, const b3Vec3& p)
+	{
+		v.push_back(p.x);
+		v.push_back(p.y);
+		v.push_back(p.z);
+	}
+	static bool same_set(const uint32* a, const uint32* b, int k)
+	{
+		for (int i = 0; i < k; ++i)
+		{
+			bool found = false;
+			for (int j = 0; j < k; ++j) found = found || a[i] == b[j];
+			if (!found) return false;
+		}
+		return true;
+	}
+	scalar mass_of(size_t i) const { return i < m_mass.size() ? m_mass[i] : 0; }
+
+	// device -> host state, when the host copy is stale
+	void fetch()
+	{
+		if (!m_body || m_hostFresh) return;
+		std::vector<float> x(3 * m_x.size()), v(3 * m_v.size());
+		check(b3g_body_get_state(m_body, x.data(), v.data()), "b3g_body_get_state");
+		for (size_t i = 0; i < m_x.size(); ++i)
+		{
+			m_x[i].Set(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+			m_v[i].Set(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+		}
+		m_hostFresh = true;
+	}
+
+	void build()
+	{
+		if (m_body && !m_topologyDirty) return;
+		fetch();
+		std::vector<float> x, v, damping;
+		std::vector<int32_t> types;
+		for (size_t i = 0; i < m_particles.size(); ++i)
+		{
+			push3(x, m_x[i]);
+			push3(v, m_v[i]);
+			damping.push_back(m_particles[i]->m_damping);
+			types.push_back((int32_t)m_particles[i]->m_type);
+		}
+		b3g_body_desc d = {};
+		d.vertex_count = (uint32)m_particles.size();
+		d.positions = x.data();
+		d.velocities = v.data();
+		d.types = types.data();
+		d.damping = damping.data();
+		d.tet_count = (uint32)m_tetE.size();
+		d.tets = m_tets.data();
+		d.tet_rest = m_tetRest.data();
+		d.tet_young = m_tetE.data();
+		d.tet_poisson = m_tetNu.data();
+		d.tet_stiffness_damping = m_tetKd.data();
+		d.tet_density = m_tetDensity.data();
+		d.tri_count = (uint32)m_triEx.size();
+		d.tris = m_tris.data();
+		d.tri_rest = m_triRest.data();
+		d.tri_young_x = m_triEx.data();
+		d.tri_young_y = m_triEy.data();
+		d.tri_shear = m_triEs.data();
+		d.tri_poisson_xy = m_triNxy.data();
+		d.tri_poisson_yx = m_triNyx.data();
+		d.tri_stiffness_damping = m_triKd.data();
+		d.tri_density = m_triDensity.data();
+		d.spring_count = (uint32)m_sprL0.size();
+		d.springs = m_springs.data();
+		d.spring_rest_length = m_sprL0.data();
+		d.spring_stiffness = m_sprKs.data();
+		d.spring_damping = m_sprKd.data();
+		std::vector<float> rad, fr;
+		if (!m_sphereRadius.empty())
+		{
+			rad = m_sphereRadius;
+			fr = m_sphereFriction;
+			rad.resize(m_particles.size(), 0);
+			fr.resize(m_particles.size(), 0);
+			d.sphere_radius = rad.data();
+			d.sphere_friction = fr.data();
+		}
+		d.world_sphere_count = (uint32)(m_world.size() / 5);
+		d.world_spheres = m_world.data();
+		d.gravity[0] = m_gravity.x;
+		d.gravity[1] = m_gravity.y;
+		d.gravity[2] = m_gravity.z;
+		if (m_body) b3g_body_destroy(m_body);
+		m_body = nullptr;
+		check(b3g_body_create(m_ctx, &d, &m_body), "b3g_body_create");
+		m_mass.assign(m_particles.size(), 0);
+		check(b3g_body_get_masses(m_body, m_mass.data()), "b3g_body_get_masses");
+		m_topologyDirty = false;
+		m_hostFresh = true;
+		m_stateDirty = false;
+	}
+
+	// pending host-side changes -> device, before a step
+	void flush_inputs()
+	{
+		if (m_stateDirty)
+		{
+			std::vector<float> x, v;
+			for (size_t i = 0; i < m_x.size(); ++i)
+			{
+				push3(x, m_x[i]);
+				push3(v, m_v[i]);
+			}
+			check(b3g_body_set_state(m_body, x.data(), v.data()), "b3g_body_set_state");
+			m_stateDirty = false;
+		}
+		bool f = false, t = false;
+		for (b3Particle* p : m_particles)
+		{
+			f = f || p->m_force.x != 0 || p->m_force.y != 0 || p->m_force.z != 0;
+			t = t || p->m_translation.x != 0 || p->m_translation.y != 0 || p->m_translation.z != 0;
+		}
+		if (f)
+		{
+			std::vector<float> a;
+			for (b3Particle* p : m_particles) push3(a, p->m_force);
+			check(b3g_body_apply_forces(m_body, a.data()), "b3g_body_apply_forces");
+		}
+		if (t)
+		{
+			std::vector<float> a;
+			for (b3Particle* p : m_particles) push3(a, p->m_translation);
+			check(b3g_body_apply_translations(m_body, a.data()), "b3g_body_apply_translations");
+		}
+	}
+
+	b3g_context* m_ctx = nullptr;
+	b3g_body* m_body = nullptr;
+	b3g_solver_config m_cfg;
+	b3g_step_stats m_stats{};
+	bool m_topologyDirty = true, m_hostFresh = true, m_stateDirty = false;
+	b3Vec3 m_gravity;
+	std::vector<b3Particle*> m_particles;
+	std::vector<b3Force*> m_forceHandles;
+	std::vector<b3Vec3> m_x, m_v;
+	std::vector<float> m_mass;
+	std::vector<uint32> m_tets, m_tris, m_springs;
+	std::vector<float> m_tetRest, m_tetE, m_tetNu, m_tetKd, m_tetDensity;
+	std::vector<float> m_triRest, m_triEx, m_triEy, m_triEs, m_triNxy, m_triNyx, m_triKd, m_triDensity;
+	std::vector<float> m_sprL0, m_sprKs, m_sprKd;
+	std::vector<float> m_sphereRadius, m_sphereFriction, m_world;
+};
+
+inline void b3Particle::SetType(b3ParticleType type)
+{
+	if (m_type == type) return;
+	m_type = type;
+	m_force.SetZero();
+	m_translation.SetZero();
+	b3Body* b = m_body;
+	if (!b->m_body)
+	{
+		if (type == e_staticParticle) b->m_v[m_index].SetZero();
+		b->m_topologyDirty = true;
+		return;
+	}
+	b->fetch();
+	if (type == e_staticParticle) b->m_v[m_index].SetZero();
+	std::vector<int32_t> types;
+	for (b3Particle* p : b->m_particles) types.push_back((int32_t)p->m_type);
+	b3Body::check(b3g_body_set_types(b->m_body, types.data()), "b3g_body_set_types");
+	b3Body::check(b3g_body_get_masses(b->m_body, b->m_mass.data()), "b3g_body_get_masses");
+}
+inline void b3Particle::SetPosition(const b3Vec3& position)
+{
+	m_body->fetch();
+	m_body->m_x[m_index] = position;
+	m_body->m_stateDirty = m_body->m_body != nullptr;
+}
+inline const b3Vec3& b3Particle::GetPosition() const
+{
+	m_body->fetch();
+	return m_body->m_x[m_index];
+}
+inline void b3Particle::SetVelocity(const b3Vec3& velocity)
+{
+	if (m_type == e_staticParticle) return;
+	m_body->fetch();
+	m_body->m_v[m_index] = velocity;
+	m_body->m_stateDirty = m_body->m_body != nullptr;
+}
+inline const b3Vec3& b3Particle::GetVelocity() const
+{
+	m_body->fetch();
+	return m_body->m_v[m_index];
+}
+inline scalar b3Particle::GetMass() const { return m_body->mass_of(m_index); }
+inline void b3Particle::ApplyForce(const b3Vec3& force)
+{
+	if (m_type != e_dynamicParticle) return;
+	m_force += force;
+}
+inline void b3Particle::ApplyImpulse(const b3Vec3& impulse)
+{
+	if (m_type != e_dynamicParticle) return;
+	m_body->fetch();
+	const scalar m = m_body->mass_of(m_index);
+	if (m > 0) m_body->m_v[m_index] += (scalar(1) / m) * impulse;
+	m_body->m_stateDirty = m_body->m_body != nullptr;
+}
+inline void b3Particle::ApplyTranslation(const b3Vec3& translation) { m_translation += translation; }

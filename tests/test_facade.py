@@ -1,0 +1,53 @@
+"""The C++ façade (include/b3g_body.hpp): a Bounce Softbody-style program built against it and
+linked with libb3g.so gives the same state as the C ABI used directly."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+from conftest import ROOT
+
+from bounce_softbody_gb300 import b3g, meshes
+
+LIBDIR = os.path.join(ROOT, "bounce_softbody_gb300", "_lib")
+
+
+def build_demo(tmp_path):
+    exe = str(tmp_path / "facade_demo")
+    r = subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "facade_demo.cpp"), "-L", LIBDIR, "-lb3g",
+                        f"-Wl,-rpath,{LIBDIR}", "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_facade_compiles_and_links(tmp_path):
+    build_demo(tmp_path)
+
+
+@pytest.mark.gpu
+def test_facade_matches_c_abi(tmp_path, ctx):
+    exe = build_demo(tmp_path)
+    desc = meshes.tet_grid(6, 5, 7, seed=4, E=2e5, nu=0.33, pin="y0")
+    steps, dt, tol = 8, 1.0 / 60.0, 1e-5
+    inp = tmp_path / "in.bin"
+    with open(inp, "wb") as f:
+        np.array([desc.n, desc.tets.shape[0]], np.uint32).tofile(f)
+        desc.x.astype(np.float32).tofile(f)
+        desc.type.astype(np.int32).tofile(f)
+        desc.tets.astype(np.uint32).tofile(f)
+        np.array([desc.tet_E[0], desc.tet_nu[0], desc.tet_density[0], desc.damping[0]], np.float32).tofile(f)
+        np.array([steps], np.uint32).tofile(f)
+        np.array([dt, tol], np.float32).tofile(f)
+    out = tmp_path / "out.bin"
+    r = subprocess.run([exe, str(inp), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    res = np.fromfile(out, np.float32).reshape(2, desc.n, 3)
+    g = b3g.Body(ctx, desc)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=tol)
+    for _ in range(steps):
+        g.step(dt, cfg)
+    x, v = g.state()
+    g.close()
+    # same library, same inputs: identical results
+    assert np.array_equal(res[0], x) and np.array_equal(res[1], v)
