@@ -83,6 +83,8 @@ SIGNATURES = {
     "b3g_step_batch": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.c_float,
                                  C.POINTER(SolverConfig), C.c_uint32, C.POINTER(StepStats)]),
     "b3g_batch_schedule": (C.c_int, [C.c_void_p, _ip, C.c_uint32]),
+    "b3g_step_batch_noalloc": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.c_float,
+                                         C.POINTER(SolverConfig), C.c_uint32, C.POINTER(StepStats)]),
     "b3g_batch_phase_cycles": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int]),
     "b3g_batch_apply_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp]),
     "b3g_batch_get_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp, _fp]),
@@ -319,6 +321,18 @@ def step_batch(ctx: Context, bodies: Sequence[Body], dt: float, steps: int = 1,
     _check(lib.b3g_step_batch(ctx.handle, arr, len(bodies), dt, C.byref(cfg), steps, st if stats else None),
            "b3g_step_batch")
     return [s.as_dict() for s in st] if stats else None
+
+
+def step_batch_noalloc(ctx: Context, bodies: Sequence[Body], dt: float, steps: int = 1,
+                       config: Optional[SolverConfig] = None, stats: bool = True):
+    """b3g_step_batch_noalloc: the batched step with no device (or host) allocation in the call."""
+    lib = load_library()
+    cfg = config if config is not None else solver_config()
+    arr = (C.c_void_p * len(bodies))(*[b.handle for b in bodies])
+    st = (StepStats * max(len(bodies), 1))()
+    _check(lib.b3g_step_batch_noalloc(ctx.handle, arr, len(bodies), dt, C.byref(cfg), steps, st if stats else None),
+           "b3g_step_batch_noalloc")
+    return [s.as_dict() for s in st[:len(bodies)]] if stats else None
 
 
 def batch_schedule(ctx: Context) -> dict:

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
@@ -428,5 +429,143 @@ extern "C" int b3g_batch_phase_cycles(b3g_context* ctx, uint64_t out[8], int res
 	if (e == cudaSuccess && reset) e = cudaMemsetAsync(c->d_prof, 0, h.size() * sizeof(unsigned long long), ctx->stream);
 	if (e != cudaSuccess) return cuda_fail(e, "phase cycles");
 	for (size_t k = 0; k < h.size(); ++k) out[k % 8] += h[k];
+	return B3G_OK;
+}
+
+// ------------------------------------------------------------------ allocation-free batch step
+// b3g_step_batch allocates its per-batch tables (body descriptors, size order, work counters) with
+// cudaMalloc on first use. Some callers cannot allocate device memory when they step: a frame
+// being captured into a CUDA graph (cudaMalloc is not allowed while a stream is capturing),
+// engines that forbid allocation after load or run under a fixed device-memory budget (and
+// cudaMalloc / cudaFree synchronise the device, stalling a frame). b3g_step_batch_noalloc keeps
+// those tables in this file-scope device array instead: room for kNoAllocMaxBodies bodies per
+// call, held by every GPU that loads the library until the process exits.
+constexpr uint32_t kNoAllocMaxBodies = 512;
+constexpr size_t noalloc_round(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t kNoAllocOrderOffset = noalloc_round(kNoAllocMaxBodies * sizeof(DevBody));
+constexpr size_t kNoAllocQueueOffset = kNoAllocOrderOffset + noalloc_round(kNoAllocMaxBodies * sizeof(int));
+constexpr size_t kNoAllocScratchBytes = kNoAllocQueueOffset + 256;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Host side: the array's name is only a host stand-in for the device copy, so each device's real
+// address is looked up once (with that device current) and kept here. The host staging arrays are
+// static too, so a call allocates nothing on the host either.
+static std::mutex g_noalloc_mutex;
+static unsigned char* g_noalloc_dev[kNoAllocMaxDevices] = {};
+static DevBody g_noalloc_host_bodies[kNoAllocMaxBodies];
+static int g_noalloc_host_order[kNoAllocMaxBodies];
+
+static int noalloc_setup(int device, unsigned char** out)
+{
+	if (device < 0 || device >= kNoAllocMaxDevices) return fail(B3G_ERROR_UNSUPPORTED, "device %d out of range", device);
+	if (!g_noalloc_dev[device])
+	{
+		unsigned char* ptr = nullptr;
+		cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
+		if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress of the allocation-free scratch");
+		e = cudaMemset(ptr + kNoAllocQueueOffset, 0, 256);
+		if (e != cudaSuccess) return cuda_fail(e, "clearing the allocation-free scratch");
+		g_noalloc_dev[device] = ptr;
+	}
+	*out = g_noalloc_dev[device];
+	return B3G_OK;
+}
+
+extern "C" int b3g_step_batch_noalloc(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float dt,
+                                      const b3g_solver_config* cfg_in, uint32_t steps, b3g_step_stats* stats)
+{
+	if (!ctx || (!bodies && count)) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	if (count > kNoAllocMaxBodies)
+		return fail(B3G_ERROR_UNSUPPORTED, "b3g_step_batch_noalloc takes at most %u bodies per call (got %u)",
+		            kNoAllocMaxBodies, count);
+	if (count == 0 || steps == 0) return B3G_OK;
+	if (!(dt > 0.0f)) return fail(B3G_ERROR_INVALID_ARGUMENT, "b3g_step_batch_noalloc needs dt > 0");
+	b3g_solver_config cfg;
+	if (cfg_in) cfg = *cfg_in;
+	else b3g_solver_config_default(&cfg);
+	int rc = check_config(&cfg);
+	if (rc != B3G_OK) return rc;
+	const int prec = prec_of(&cfg);
+	for (uint32_t k = 0; k < count; ++k)
+	{
+		const b3g_body* b = bodies[k];
+		if (!b) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u is null", k);
+		if (b->ctx != ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u belongs to another context", k);
+		if (!b->prec[prec].mem)
+			return fail(B3G_ERROR_INVALID_ARGUMENT,
+			            "body %u has no solver buffers for this precision yet; step it once with this precision "
+			            "through b3g_body_step or b3g_step_batch first",
+			            k);
+		for (uint32_t j = 0; j < k; ++j)
+			if (bodies[j] == bodies[k]) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u is listed twice", k);
+	}
+	if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(B3G_ERROR_CUDA, "cudaSetDevice");
+	std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+	unsigned char* scratch = nullptr;
+	rc = noalloc_setup(ctx->device, &scratch);
+	if (rc != B3G_OK) return rc;
+	cudaStream_t st = ctx->stream;
+
+	// descriptors and the size order (largest first), staged through the static host arrays
+	int maxn = 0;
+	for (uint32_t k = 0; k < count; ++k)
+	{
+		g_noalloc_host_bodies[k] = dev_for(bodies[k], prec, cfg.preconditioner);
+		g_noalloc_host_order[k] = (int)k;
+		maxn = std::max(maxn, (int)bodies[k]->n);
+	}
+	std::stable_sort(g_noalloc_host_order, g_noalloc_host_order + count,
+	                 [&](int a, int b) { return bodies[a]->n > bodies[b]->n; });
+	DevBody* d_bodies = (DevBody*)scratch;
+	int* d_order = (int*)(scratch + kNoAllocOrderOffset);
+	unsigned* d_queue = (unsigned*)(scratch + kNoAllocQueueOffset);
+	cudaError_t e = cudaMemcpyAsync(d_bodies, g_noalloc_host_bodies, count * sizeof(DevBody), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(d_order, g_noalloc_host_order, count * sizeof(int), cudaMemcpyHostToDevice, st);
+	if (e != cudaSuccess) return cuda_fail(e, "b3g_step_batch_noalloc upload");
+
+	// the size heuristic of b3g_step_batch (no autotuning: it would need a state snapshot)
+	const int cluster = maxn >= 4096 ? 4 : 1;
+	const int threshold = 4096;
+	int nbig = 0;
+	if (cluster > 1)
+		for (uint32_t k = 0; k < count; ++k)
+			if ((int)bodies[k]->n >= threshold) ++nbig;
+	int m = batch_max_clusters(prec, cluster);
+	if (m <= 0) m = std::max(1, ctx->sm_count / cluster);
+	BatchArgs A;
+	A.bodies = d_bodies;
+	A.big = d_order;
+	A.nbig = nbig;
+	A.small = d_order + nbig;
+	A.nsmall = (int)count - nbig;
+	A.queue = d_queue;  // op_batch clears the two counters before the launch
+	A.steps = (int)steps;
+	A.h = dt;
+	A.newton = (int)std::max<uint32_t>(1u, cfg.force_iterations);
+	A.max_iter = (int)cfg.max_pcg_iterations;
+	A.tol2 = cfg.pcg_tolerance * cfg.pcg_tolerance;
+	A.refresh = (int)cfg.refresh_period;
+	A.newton_tol2 = cfg.newton_tolerance * cfg.newton_tolerance;
+	A.prec = prec;
+	A.cluster = cluster;
+	A.ctas = m * cluster;
+	A.prof = nullptr;
+	e = op_batch(A, st);
+	if (e != cudaSuccess) return cuda_fail(e, "b3g_step_batch_noalloc launch");
+	if (stats)
+	{
+		for (uint32_t k0 = 0; k0 < count && e == cudaSuccess; k0 += 1024)
+		{
+			uint32_t mm = std::min<uint32_t>(1024, count - k0);
+			for (uint32_t k = 0; k < mm && e == cudaSuccess; ++k)
+				e = cudaMemcpyAsync(ctx->h_scalars + k, bodies[k0 + k]->d.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st);
+			if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+			for (uint32_t k = 0; k < mm && e == cudaSuccess; ++k) stats_from(ctx->h_scalars[k], stats + k0 + k);
+		}
+		if (e != cudaSuccess) return cuda_fail(e, "b3g_step_batch_noalloc stats");
+	}
 	return B3G_OK;
 }

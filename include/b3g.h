@@ -181,6 +181,22 @@ B3G_API int b3g_body_step(b3g_body* body, float dt, const b3g_solver_config* con
 B3G_API int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float dt,
                    const b3g_solver_config* config, uint32_t steps, b3g_step_stats* stats);
 
+/* Like b3g_step_batch, without allocating anything. No counterpart in the reference.
+ * For callers that cannot allocate device memory while they step: a frame captured into a CUDA
+ * graph (cudaMalloc is not permitted during stream capture), engines that forbid allocation after
+ * load or keep a fixed device-memory budget (cudaMalloc / cudaFree also synchronise the device).
+ * b3g_step_batch allocates per-batch tables on first use; this entry point keeps them in a fixed
+ * device array of the library instead (held by every GPU that loads the library until exit), for
+ * at most 512 bodies per call (more fails with B3G_ERROR_UNSUPPORTED). The bodies bring their own
+ * state and solver buffers: each must already have buffers for the requested precision (FP32
+ * always does; FP64 / BF16 after a first step in that precision). The schedule is the size
+ * heuristic (clusters of 4 CTAs for bodies of 4096 vertices or more), not autotuned; dt must be
+ * > 0. The first call on a device looks the array up and clears it (set-up): make that first call
+ * before any stream capture. Every call reuses the same array, so calls whose work overlaps on the
+ * GPU (other streams, other contexts on the same device) race; calls on one stream are ordered. */
+B3G_API int b3g_step_batch_noalloc(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float dt,
+                                   const b3g_solver_config* config, uint32_t steps, b3g_step_stats* stats);
+
 /* Schedule of the context's current batch: cluster size, size threshold of cluster-stepped bodies
  * (-1 = none), bodies stepped by clusters, CTAs per launch, autotuned (0/1), number of timed
  * candidates, then (candidate code = cluster * 1e6 + threshold, microseconds) per candidate. */
