@@ -303,8 +303,11 @@ def ours(args, world, rank, local, pg):
     alg = sum(args.steps * assembly_bytes(i) + it * iteration_bytes(i, vsz, bs) for i, it in zip(infos, iters))
     achieved = alg / (total_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
+    # DRAM traffic per launch: ncu on a 128-body launch measured 1.21 x its algorithmic bytes
+    # (profiles/k_batch_batch512.md); traffic grows with the vertex-steps, so it is scaled by them
+    traffic = 1.21 * alg / args.steps if args.workload == "batch" and args.precision == "fp32" else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": "k_batch (persistent, one launch per step)",
+            "traffic": traffic, "kernel": "k_batch (persistent, one launch per step)",
             "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_step": alg / args.steps,
             "pcg_iterations_per_step_mean": float(np.mean(iters)) / args.steps if iters else 0.0}
     sched = b3g.batch_schedule(ctx) if not single else None
