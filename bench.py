@@ -44,10 +44,18 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="batch", choices=["batch", "tet64", "cloth128", "tet10"])
+    p.add_argument("--workload", default="batch", choices=["batch", "tet64", "cloth128", "tet10", "serve"])
     p.add_argument("--bodies", type=int, default=512)
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "bf16"])
     p.add_argument("--no-extras", action="store_true", help="skip e2e, plain path and CPU baseline")
+    # serving (--workload serve): Poisson arrivals over a pool of bodies
+    p.add_argument("--serve-rate", type=float, default=2000.0, help="requests per second")
+    p.add_argument("--serve-seconds", type=float, default=10.0, help="length of the arrival stream")
+    p.add_argument("--serve-grace", type=float, default=5.0, help="seconds to keep serving after the stream")
+    p.add_argument("--serve-pool", type=int, default=256, help="distinct bodies of the stream")
+    p.add_argument("--serve-max-active", type=int, default=256, help="bodies per launch at most")
+    p.add_argument("--serve-budget-gb", type=float, default=64.0, help="device memory for resident bodies")
+    p.add_argument("--serve-plain-seconds", type=float, default=10.0, help="plain-path sample length")
     return p.parse_args()
 
 
@@ -380,10 +388,118 @@ def ours(args, world, rank, local, pg):
     return 0
 
 
+# ------------------------------------------------------------------ serving
+def serve_arm(args, rank, local):
+    """Continuous-batching server under a Poisson request stream; the same stream through the
+    plain one-body-at-a-time path on a bounded sample."""
+    from bounce_softbody_gb300 import b3g, meshes
+
+    pool = meshes.serving_bodies(args.serve_pool, seed=5 + 1000 * rank)
+    scfg = b3g.solver_config(max_pcg_iterations=PCG_MAX, pcg_tolerance=PCG_TOL)
+    rng = np.random.default_rng(7 + 1000 * rank)
+    gaps = rng.exponential(1.0 / args.serve_rate, size=int(args.serve_rate * args.serve_seconds * 1.5) + 16)
+    arrival = np.cumsum(gaps)
+    arrival = arrival[arrival < args.serve_seconds]
+    req_body = rng.integers(0, len(pool), size=arrival.size)
+    req_steps = rng.integers(1, 31, size=arrival.size)
+    demand = float(sum(pool[b].n * s for b, s in zip(req_body, req_steps))) / args.serve_seconds
+
+    ctx = b3g.Context(local)
+    srv = b3g.Server(ctx, int(args.serve_budget_gb * (1 << 30)), args.serve_max_active, DT, scfg)
+    for d in pool:
+        srv.add_body(d)
+    srv.start()
+    t0 = time.perf_counter()
+    for k in range(len(pool)):  # warm-up: every body created on the device and stepped once
+        srv.submit(k, 1)
+    srv.drain(timeout=1800)
+    setup_s = time.perf_counter() - t0
+    srv.reset_stats()
+
+    clocks = Clocks(local)
+    results = []
+    t0 = time.perf_counter()
+    i = 0
+    while i < arrival.size:
+        now = time.perf_counter() - t0
+        while i < arrival.size and arrival[i] <= now:
+            srv.submit(int(req_body[i]), int(req_steps[i]))
+            i += 1
+        results += srv.poll()
+        time.sleep(0.0002)
+    end = t0 + args.serve_seconds + args.serve_grace
+    while time.perf_counter() < end and srv.pending() > 0:
+        results += srv.poll()
+        time.sleep(0.001)
+    results += srv.poll()
+    st = srv.stats()
+    queued = srv.pending()
+    clk = clocks.stop()
+    srv.close()
+
+    done = [r for r in results if r["status"] == "done"]
+    lat = np.array([r["latency_seconds"] for r in done]) * 1e3
+    per_step = np.array([r["latency_seconds"] / r["steps"] for r in done]) * 1e3
+    value = st["vertex_steps"] / st["wall_seconds"] if st["wall_seconds"] > 0 else 0.0
+
+    # plain path: the same stream, one request after another, one body step per call
+    plain = {}
+    if args.serve_plain_seconds > 0:
+        cache = {}
+        order = list(range(arrival.size))
+        for k in order[:64]:  # create the sample's bodies outside the timed region
+            b = int(req_body[k])
+            if b not in cache:
+                cache[b] = b3g.Body(ctx, pool[b])
+        step_ms, vsteps = [], 0
+        p0 = time.perf_counter()
+        for k in order[:64]:
+            body = cache[int(req_body[k])]
+            for _ in range(int(req_steps[k])):
+                s0 = time.perf_counter()
+                body.step(DT, scfg, stats=True)  # waits for the step
+                step_ms.append(1e3 * (time.perf_counter() - s0))
+                vsteps += body.n
+            if time.perf_counter() - p0 > args.serve_plain_seconds:
+                break
+        psec = time.perf_counter() - p0
+        plain = {"value": vsteps / psec, "unit": "vertex-steps/s", "requests": k + 1,
+                 "p50_step_ms": float(np.median(step_ms)), "p99_step_ms": float(np.percentile(step_ms, 99)),
+                 "note": "same request stream served one request after another by b3g_body_step"}
+        for b in cache.values():
+            b.close()
+    ctx.close()
+
+    line = {"metric": "serving: vertex-steps/s and p50/p99 step latency under Poisson arrivals", "value": value,
+            "unit": "vertex-steps/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (seeded meshes and arrivals)",
+            "config": {"workload": f"Poisson arrivals {args.serve_rate:g} req/s for {args.serve_seconds:g} s over "
+                                   f"{len(pool)} bodies (tet 1e3..1e5 vertices log-uniform / cloth 32^2..256^2), "
+                                   f"1..30 steps per request, h=1/60",
+                       "pool_vertices": int(sum(d.n for d in pool)), "max_active": args.serve_max_active,
+                       "budget_gb": args.serve_budget_gb, "pcg_tol": PCG_TOL, "pcg_max_iter": PCG_MAX,
+                       "setup_s": round(setup_s, 1)},
+            "demand_vertex_steps_per_s": demand,
+            "requests": {"submitted": int(arrival.size), "completed": len(done), "queued_at_end": queued,
+                         "rejected": int(st["rejected"]), "evictions": int(st["evictions"])},
+            "request_latency_ms": {"p50": float(np.median(lat)) if lat.size else None,
+                                   "p99": float(np.percentile(lat, 99)) if lat.size else None},
+            "request_latency_per_step_ms": {"p50": float(np.median(per_step)) if per_step.size else None,
+                                            "p99": float(np.percentile(per_step, 99)) if per_step.size else None},
+            "p50_step_ms": st["step_ms_p50"], "p99_step_ms": st["step_ms_p99"],
+            "launches": int(st["iterations"]), "gpu_busy_frac": st["gpu_seconds"] / st["wall_seconds"] if st["wall_seconds"] else None,
+            "clocks": clk, "gpu_launches": int(st["iterations"]), "plain": plain}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     world, rank, local, pg = dist_setup(args)
-    if args.impl == "reference":
+    if args.impl == "ours" and args.workload == "serve":
+        rc = serve_arm(args, rank, local)
+    elif args.impl == "reference":
         rc = reference_arm(args, world, rank, pg)
     else:
         rc = ours(args, world, rank, local, pg)

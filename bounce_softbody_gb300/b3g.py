@@ -66,6 +66,25 @@ class StepStats(C.Structure):
                 "total_pcg_iterations": int(self.total_pcg_iterations), "total_steps": int(self.total_steps)}
 
 
+class RequestResult(C.Structure):
+    _fields_ = [
+        ("request_id", C.c_uint64), ("body_id", C.c_uint32), ("steps", C.c_uint32),
+        ("status", C.c_int32), ("reserved", C.c_int32), ("pcg_iterations", C.c_uint64),
+        ("queue_seconds", C.c_double), ("latency_seconds", C.c_double),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_uint64), ("vertex_steps", C.c_uint64), ("admitted", C.c_uint64),
+        ("completed", C.c_uint64), ("rejected", C.c_uint64), ("evictions", C.c_uint64),
+        ("resident_bytes", C.c_uint64), ("waiting", C.c_uint64), ("gpu_seconds", C.c_double),
+        ("wall_seconds", C.c_double), ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double),
+    ]
+
+
+REQUEST_STATUS = {0: "done", 1: "rejected", 2: "device_timeout"}
+
 # every entry point of include/b3g.h with its ctypes signature
 SIGNATURES = {
     "b3g_solver_config_default": (None, [C.POINTER(SolverConfig)]),
@@ -97,6 +116,17 @@ SIGNATURES = {
     "b3g_body_set_rotations": (C.c_int, [C.c_void_p, _fp]),
     "b3g_body_get_masses": (C.c_int, [C.c_void_p, _fp]),
     "b3g_body_get_stats": (C.c_int, [C.c_void_p, C.POINTER(StepStats)]),
+    "b3g_server_create": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_float, C.POINTER(SolverConfig),
+                                    C.POINTER(C.c_void_p)]),
+    "b3g_server_add_body": (C.c_int, [C.c_void_p, C.POINTER(BodyDescC), _up]),
+    "b3g_server_start": (C.c_int, [C.c_void_p]),
+    "b3g_server_submit": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint64)]),
+    "b3g_server_poll": (C.c_int, [C.c_void_p, C.POINTER(RequestResult), C.c_uint32, _up]),
+    "b3g_server_pending": (C.c_int, [C.c_void_p, _up]),
+    "b3g_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    "b3g_server_reset_stats": (C.c_int, [C.c_void_p]),
+    "b3g_server_get_state": (C.c_int, [C.c_void_p, C.c_uint32, _fp, _fp]),
+    "b3g_server_destroy": (C.c_int, [C.c_void_p]),
 }
 
 _lib = None
@@ -183,54 +213,60 @@ def _ptr(a, t):
     return a.ctypes.data_as(t)
 
 
+def _desc_struct(desc, masses=None):
+    """A b3g_body_desc pointing into numpy copies of a meshes.BodyDesc; returns (struct, arrays to keep alive)."""
+    keep = []
+
+    def f(a):
+        a = _f32(a)
+        keep.append(a)
+        return _ptr(a, _fp)
+
+    def u(a):
+        a = np.ascontiguousarray(a, dtype=np.uint32)
+        keep.append(a)
+        return _ptr(a, _up)
+
+    d = BodyDescC()
+    d.vertex_count = desc.n
+    d.positions = f(desc.x)
+    d.velocities = f(desc.v)
+    types = np.ascontiguousarray(desc.type, dtype=np.int32)
+    keep.append(types)
+    d.types = types.ctypes.data_as(_ip)
+    d.damping = f(desc.damping)
+    d.masses = f(masses) if masses is not None else C.cast(None, _fp)
+    d.tet_count = desc.tets.shape[0]
+    d.tets = u(desc.tets)
+    d.tet_rest = C.cast(None, _fp)
+    d.tet_young, d.tet_poisson = f(desc.tet_E), f(desc.tet_nu)
+    d.tet_stiffness_damping, d.tet_density = f(desc.tet_kdamp), f(desc.tet_density)
+    d.tri_count = desc.tris.shape[0]
+    d.tris = u(desc.tris)
+    d.tri_rest = C.cast(None, _fp)
+    d.tri_young_x, d.tri_young_y, d.tri_shear = f(desc.tri_Ex), f(desc.tri_Ey), f(desc.tri_Es)
+    d.tri_poisson_xy, d.tri_poisson_yx = f(desc.tri_nuxy), f(desc.tri_nuyx)
+    d.tri_stiffness_damping, d.tri_density = f(desc.tri_kdamp), f(desc.tri_density)
+    d.spring_count = desc.springs.shape[0]
+    d.springs = u(desc.springs)
+    d.spring_rest_length, d.spring_stiffness, d.spring_damping = (
+        f(desc.spring_L0), f(desc.spring_ks), f(desc.spring_kd))
+    d.sphere_radius = f(desc.sphere_radius) if desc.sphere_radius is not None else C.cast(None, _fp)
+    d.sphere_friction = f(desc.sphere_friction) if desc.sphere_friction is not None else C.cast(None, _fp)
+    d.world_sphere_count = desc.world_spheres.shape[0]
+    d.world_spheres = f(desc.world_spheres)
+    for k in range(3):
+        d.gravity[k] = float(desc.gravity[k])
+    return d, keep
+
+
 class Body:
     """One body on the GPU, created from a meshes.BodyDesc (or anything with its fields)."""
 
     def __init__(self, ctx: Context, desc, masses=None):
         lib = load_library()
         self.ctx = ctx
-        keep = []
-
-        def f(a):
-            a = _f32(a)
-            keep.append(a)
-            return _ptr(a, _fp)
-
-        def u(a):
-            a = np.ascontiguousarray(a, dtype=np.uint32)
-            keep.append(a)
-            return _ptr(a, _up)
-
-        d = BodyDescC()
-        d.vertex_count = desc.n
-        d.positions = f(desc.x)
-        d.velocities = f(desc.v)
-        types = np.ascontiguousarray(desc.type, dtype=np.int32)
-        keep.append(types)
-        d.types = types.ctypes.data_as(_ip)
-        d.damping = f(desc.damping)
-        d.masses = f(masses) if masses is not None else C.cast(None, _fp)
-        d.tet_count = desc.tets.shape[0]
-        d.tets = u(desc.tets)
-        d.tet_rest = C.cast(None, _fp)
-        d.tet_young, d.tet_poisson = f(desc.tet_E), f(desc.tet_nu)
-        d.tet_stiffness_damping, d.tet_density = f(desc.tet_kdamp), f(desc.tet_density)
-        d.tri_count = desc.tris.shape[0]
-        d.tris = u(desc.tris)
-        d.tri_rest = C.cast(None, _fp)
-        d.tri_young_x, d.tri_young_y, d.tri_shear = f(desc.tri_Ex), f(desc.tri_Ey), f(desc.tri_Es)
-        d.tri_poisson_xy, d.tri_poisson_yx = f(desc.tri_nuxy), f(desc.tri_nuyx)
-        d.tri_stiffness_damping, d.tri_density = f(desc.tri_kdamp), f(desc.tri_density)
-        d.spring_count = desc.springs.shape[0]
-        d.springs = u(desc.springs)
-        d.spring_rest_length, d.spring_stiffness, d.spring_damping = (
-            f(desc.spring_L0), f(desc.spring_ks), f(desc.spring_kd))
-        d.sphere_radius = f(desc.sphere_radius) if desc.sphere_radius is not None else C.cast(None, _fp)
-        d.sphere_friction = f(desc.sphere_friction) if desc.sphere_friction is not None else C.cast(None, _fp)
-        d.world_sphere_count = desc.world_spheres.shape[0]
-        d.world_spheres = f(desc.world_spheres)
-        for k in range(3):
-            d.gravity[k] = float(desc.gravity[k])
+        d, keep = _desc_struct(desc, masses)
         h = C.c_void_p()
         _check(lib.b3g_body_create(ctx.handle, C.byref(d), C.byref(h)), "b3g_body_create")
         del keep
@@ -366,3 +402,92 @@ def batch_phase_cycles(ctx: Context, reset: bool = True) -> dict:
     a = (C.c_uint64 * 8)()
     _check(load_library().b3g_batch_phase_cycles(ctx.handle, a, 1 if reset else 0), "b3g_batch_phase_cycles")
     return {PHASES[k]: int(a[k]) for k in range(6)}
+
+
+class Server:
+    """Continuous-batching request loop over many bodies (b3g_server_*).
+
+    Register bodies with add_body, start the worker, submit (body, steps) requests from any
+    thread and poll finished ones. Close before the context."""
+
+    def __init__(self, ctx: Context, memory_budget_bytes: int, max_active: int, dt: float,
+                 config: Optional[SolverConfig] = None):
+        lib = load_library()
+        self.ctx = ctx
+        cfg = config if config is not None else solver_config()
+        h = C.c_void_p()
+        _check(lib.b3g_server_create(ctx.handle, int(memory_budget_bytes), int(max_active), float(dt),
+                                     C.byref(cfg), C.byref(h)), "b3g_server_create")
+        self.handle = h
+        self.sizes = []
+
+    def add_body(self, desc, masses=None) -> int:
+        d, keep = _desc_struct(desc, masses)
+        out = C.c_uint32()
+        _check(load_library().b3g_server_add_body(self.handle, C.byref(d), C.byref(out)), "b3g_server_add_body")
+        del keep
+        self.sizes.append(desc.n)
+        return int(out.value)
+
+    def start(self):
+        _check(load_library().b3g_server_start(self.handle), "b3g_server_start")
+
+    def submit(self, body_id: int, steps: int) -> int:
+        rid = C.c_uint64()
+        _check(load_library().b3g_server_submit(self.handle, int(body_id), int(steps), C.byref(rid)),
+               "b3g_server_submit")
+        return int(rid.value)
+
+    def poll(self, capacity: int = 1024) -> list:
+        buf = (RequestResult * capacity)()
+        n = C.c_uint32()
+        _check(load_library().b3g_server_poll(self.handle, buf, capacity, C.byref(n)), "b3g_server_poll")
+        return [{"request_id": int(r.request_id), "body_id": int(r.body_id), "steps": int(r.steps),
+                 "status": REQUEST_STATUS.get(r.status, str(r.status)), "pcg_iterations": int(r.pcg_iterations),
+                 "queue_seconds": r.queue_seconds, "latency_seconds": r.latency_seconds}
+                for r in buf[:n.value]]
+
+    def pending(self) -> int:
+        n = C.c_uint32()
+        _check(load_library().b3g_server_pending(self.handle, C.byref(n)), "b3g_server_pending")
+        return int(n.value)
+
+    def drain(self, timeout: float = 600.0, poll_interval: float = 0.001) -> list:
+        """Wait until every submitted request has finished; return the finished requests."""
+        import time
+        out = []
+        t0 = time.monotonic()
+        while True:
+            out += self.poll()
+            if self.pending() == 0:
+                return out + self.poll()
+            if time.monotonic() - t0 > timeout:
+                raise B3gError(f"server requests not finished after {timeout} s")
+            time.sleep(poll_interval)
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(load_library().b3g_server_get_stats(self.handle, C.byref(st)), "b3g_server_get_stats")
+        return {name: getattr(st, name) for name, _ in ServerStats._fields_}
+
+    def reset_stats(self):
+        _check(load_library().b3g_server_reset_stats(self.handle), "b3g_server_reset_stats")
+
+    def state(self, body_id: int):
+        n = self.sizes[body_id]
+        x = np.empty((n, 3), np.float32)
+        v = np.empty((n, 3), np.float32)
+        _check(load_library().b3g_server_get_state(self.handle, int(body_id), _ptr(x, _fp), _ptr(v, _fp)),
+               "b3g_server_get_state")
+        return x, v
+
+    def close(self):
+        if self.handle:
+            load_library().b3g_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -20,7 +20,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libb3g.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "kernels.cu", "batch.cu", "persistent.cu", "pattern.cpp"]
+SOURCES = ["api.cu", "kernels.cu", "batch.cu", "persistent.cu", "server.cu", "pattern.cpp"]
 
 
 def nvcc() -> str:

@@ -226,3 +226,32 @@ def config_tet64(seed: int = 0) -> BodyDesc:
 def config_cloth128() -> BodyDesc:
     """128^2 cloth (16,384 vertices, 32,258 triangles, 64,768 springs) over a r=0.5 sphere."""
     return cloth_grid(128, name="cloth128")
+
+
+def serving_bodies(count: int = 256, seed: int = 5) -> list[BodyDesc]:
+    """Bodies of a serving stream: half tetrahedral blocks, half cloths (seeded).
+
+    A block has a vertex count log-uniform in [1e3, 1e5], split into a x b x c with aspect ratios
+    up to about 1.4, Young modulus log-uniform in [1e4, 1e6], Poisson ratio U[0.2, 0.45] and one
+    random face pinned. A cloth is an m x m grid with m log-uniform in [32, 256], membrane
+    stiffness E*t U[25, 100], springs of stiffness 1e3 and damping 5, two corners pinned, over a
+    static sphere with contacts and friction 0.3.
+    """
+    rng = np.random.default_rng(seed)
+    faces = ["x0", "x1", "y0", "y1", "z0", "z1"]
+    out = []
+    for k in range(count):
+        if rng.random() < 0.5:
+            nv = float(np.exp(rng.uniform(np.log(1e3), np.log(1e5))))
+            f = np.exp(rng.uniform(-0.33, 0.33, size=3))
+            f /= np.cbrt(np.prod(f))
+            a, b, c = (max(4, int(round(np.cbrt(nv) * s))) for s in f)
+            E = float(10.0 ** rng.uniform(4.0, 6.0))
+            nu = float(rng.uniform(0.2, 0.45))
+            face = faces[int(rng.integers(0, 6))]
+            out.append(tet_grid(a, b, c, E=E, nu=nu, pin=face, rng=rng, name=f"serve{k}_tet{a}x{b}x{c}"))
+        else:
+            m = int(round(np.exp(rng.uniform(np.log(32), np.log(256)))))
+            E_t = float(rng.uniform(25.0, 100.0))
+            out.append(cloth_grid(m, E_t=E_t, name=f"serve{k}_cloth{m}"))
+    return out

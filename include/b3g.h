@@ -231,6 +231,71 @@ B3G_API int b3g_body_get_masses(b3g_body* body, float* masses);
 /* Statistics of the body's last step (waits for it). */
 B3G_API int b3g_body_get_stats(b3g_body* body, b3g_step_stats* stats);
 
+/* ---------------------------------------------------------------- serving
+ * A server steps many bodies on request, continuously batched: a worker thread repeatedly admits
+ * waiting requests, steps every body with an active request once in one batched launch (the
+ * kernel of b3g_step_batch) and retires finished requests; requests that arrive meanwhile join at
+ * the next launch. Bodies stay resident on the device between requests while their device
+ * footprint fits `memory_budget_bytes`; beyond it idle bodies are evicted least recently used
+ * first (their state is kept on the host and restored exactly when they return) and requests wait
+ * for room. A body serves its requests one at a time in arrival order. Team sizes depend only on
+ * each body's own size, so a body's results do not depend on the mix it is stepped in.
+ * No reference counterpart: the reference steps one body per b3Body::Step call
+ * (src/bounce_softbody/dynamics/body.cpp:552); this is the request loop a service would put around it. */
+typedef struct b3g_server b3g_server;
+
+typedef enum b3g_request_status
+{
+	B3G_REQUEST_DONE = 0,
+	B3G_REQUEST_REJECTED = 1,          /* the body alone exceeds the memory budget */
+	B3G_REQUEST_DEVICE_TIMEOUT = 2     /* a bounded device wait expired during one of its steps */
+} b3g_request_status;
+
+typedef struct b3g_request_result
+{
+	uint64_t request_id;
+	uint32_t body_id;
+	uint32_t steps;
+	int32_t status;                /* b3g_request_status */
+	int32_t reserved;
+	uint64_t pcg_iterations;       /* PCG iterations of the request's steps */
+	double queue_seconds;          /* arrival to first step */
+	double latency_seconds;        /* arrival to completion */
+} b3g_request_result;
+
+typedef struct b3g_server_stats
+{
+	uint64_t iterations;           /* batched launches */
+	uint64_t vertex_steps;         /* vertices x steps completed */
+	uint64_t admitted, completed, rejected, evictions;
+	uint64_t resident_bytes;       /* device bytes of the resident bodies */
+	uint64_t waiting;              /* requests not yet started */
+	double gpu_seconds;            /* summed device time of the launches */
+	double wall_seconds;           /* first arrival to last completed launch */
+	double step_ms_p50, step_ms_p99; /* device time per launch */
+} b3g_server_stats;
+
+/* config NULL = b3g_solver_config_default; max_active bounds the bodies of one launch. */
+B3G_API int b3g_server_create(b3g_context* ctx, uint64_t memory_budget_bytes, uint32_t max_active, float dt,
+                              const b3g_solver_config* config, b3g_server** out);
+/* Register a body (its arrays are copied; nothing is allocated on the device yet). */
+B3G_API int b3g_server_add_body(b3g_server* server, const b3g_body_desc* desc, uint32_t* body_id);
+/* Start the worker thread. Requests submitted before it starts wait. */
+B3G_API int b3g_server_start(b3g_server* server);
+/* Queue `steps` steps of a body; thread-safe. */
+B3G_API int b3g_server_submit(b3g_server* server, uint32_t body_id, uint32_t steps, uint64_t* request_id);
+/* Take up to `capacity` finished requests in completion order. */
+B3G_API int b3g_server_poll(b3g_server* server, b3g_request_result* out, uint32_t capacity, uint32_t* count);
+/* Requests submitted and not yet finished. */
+B3G_API int b3g_server_pending(b3g_server* server, uint32_t* pending);
+B3G_API int b3g_server_get_stats(b3g_server* server, b3g_server_stats* stats);
+/* Restart the statistics (counters, launch times, the wall clock from the next arrival). */
+B3G_API int b3g_server_reset_stats(b3g_server* server);
+/* State of a body that has no active request (3 floats per vertex each; either may be NULL). */
+B3G_API int b3g_server_get_state(b3g_server* server, uint32_t body_id, float* positions, float* velocities);
+/* Stop the worker after its current launch and free every body of the server. */
+B3G_API int b3g_server_destroy(b3g_server* server);
+
 #ifdef __cplusplus
 }
 #endif
