@@ -478,6 +478,7 @@ def serve_arm(args, rank, local):
                                    f"1..30 steps per request, h=1/60",
                        "pool_vertices": int(sum(d.n for d in pool)), "max_active": args.serve_max_active,
                        "budget_gb": args.serve_budget_gb, "pcg_tol": PCG_TOL, "pcg_max_iter": PCG_MAX,
+                       "team": f"clusters of {st['cluster_ctas']} CTAs from {st['cluster_threshold']} vertices",
                        "setup_s": round(setup_s, 1)},
             "demand_vertex_steps_per_s": demand,
             "requests": {"submitted": int(arrival.size), "completed": len(done), "queued_at_end": queued,

@@ -80,6 +80,7 @@ class ServerStats(C.Structure):
         ("completed", C.c_uint64), ("rejected", C.c_uint64), ("evictions", C.c_uint64),
         ("resident_bytes", C.c_uint64), ("waiting", C.c_uint64), ("gpu_seconds", C.c_double),
         ("wall_seconds", C.c_double), ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double),
+        ("cluster_ctas", C.c_uint32), ("cluster_threshold", C.c_uint32),
     ]
 
 

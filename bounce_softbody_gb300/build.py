@@ -20,7 +20,8 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libb3g.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "kernels.cu", "batch.cu", "persistent.cu", "server.cu", "pattern.cpp"]
+SOURCES = ["api.cu", "kernels.cu", "batch.cu", "persistent.cu", "persistent_f32.cu", "persistent_f64.cu",
+           "persistent_bf16.cu", "server.cu", "pattern.cpp"]
 
 
 def nvcc() -> str:

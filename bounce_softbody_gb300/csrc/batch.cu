@@ -159,10 +159,11 @@ int autotune(b3g_context* ctx, BatchCache* c, float h, const b3g_solver_config& 
 	std::vector<std::pair<int, int>> cands;
 	cands.push_back({1, 1 << 30});
 	const int thresholds[] = {4096, 8192, 16384, 32768};
-	const int clusters[] = {2, 4, 8};
+	const int clusters[] = {2, 4, 8, 16};
 	for (int cl : clusters)
-		for (int t : thresholds)
-			if (t <= maxn) cands.push_back({cl, t});
+		if (batch_max_clusters(c->prec, cl) > 0)  // 16-CTA clusters need hardware support
+			for (int t : thresholds)
+				if (t <= maxn) cands.push_back({cl, t});
 	cudaEvent_t e0, e1;
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
@@ -306,7 +307,7 @@ extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_
 		const char* env = std::getenv("B3G_AUTOTUNE");
 		const char* forced = std::getenv("B3G_BATCH_SCHEDULE");  // "cluster,threshold"
 		int fc = 0, ft = 0;
-		if (forced && std::sscanf(forced, "%d,%d", &fc, &ft) == 2 && (fc == 1 || fc == 2 || fc == 4 || fc == 8))
+		if (forced && std::sscanf(forced, "%d,%d", &fc, &ft) == 2 && (fc == 1 || fc == 2 || fc == 4 || fc == 8 || fc == 16))
 			set_schedule(c, fc, ft > 0 ? ft : (1 << 30), ctx->sm_count);
 		else if (!(env && env[0] == '0'))
 		{

@@ -1,553 +1,13 @@
-// Persistent batch kernel: many independent bodies step in one launch.
-//
-// A body is owned by a team: either a thread-block cluster of CL CTAs (large bodies) or a
-// single CTA (small bodies). The team runs the whole implicit step of its body without leaving
-// the kernel: element phase, row assembly, PCG, final update. Team-wide synchronisation is the
-// hardware cluster barrier (or __syncthreads for one CTA); dot products are reduced per warp by
-// shuffles, per CTA through shared memory and across the cluster through distributed shared
-// memory, always in the same order, so every thread of the team holds the same bitwise value
-// and takes the same solver decisions without a round trip to global memory. There is no
-// spin-wait anywhere: the only inter-CTA waits are hardware barriers between CTAs that the
-// cluster launch guarantees to be co-resident.
-//
-// Work distribution: bodies are sorted by size (largest first). Clusters first take large bodies
-// from a global counter; when those run out every CTA takes small bodies on its own.
-#include "device.cuh"
-#include "ops.h"
-
-#include <cooperative_groups.h>
-#include <type_traits>
-
-namespace cg = cooperative_groups;
+// Dispatch of the persistent batch kernel (persistent.cuh) to its per-precision instantiations.
+#include "persistent.cuh"
 
 namespace b3g {
 
-namespace {
-
-#ifndef B3G_BATCH_MIN_BLOCKS
-#define B3G_BATCH_MIN_BLOCKS 2   // resident CTAs per SM the register budget is sized for
-#endif
-
-constexpr int kPThreads = 256;
-constexpr int kPWarps = kPThreads / 32;
-
-struct TeamShared
-{
-	double wp[2][kPWarps];
-	double slot[2];
-	int item;
-	int pad;
-};
-
-template <int CL>
-struct Team
-{
-	TeamShared* sh;
-	int parity;
-	int rank;
-
-	__device__ void sync()
-	{
-		if (CL == 1) __syncthreads();
-		else cg::this_cluster().sync();
-	}
-	__device__ int tid() const { return rank * kPThreads + (int)threadIdx.x; }
-	__device__ int nthreads() const { return CL * kPThreads; }
-	__device__ int warp() const { return rank * kPWarps + ((int)threadIdx.x >> 5); }
-	__device__ int nwarps() const { return CL * kPWarps; }
-
-	// Team-wide sum; every thread of the team returns the same value (fixed summation order).
-	__device__ double reduce(double v)
-	{
-		const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-		v = warp_sum(v);
-		if (lane == 0) sh->wp[parity][w] = v;
-		__syncthreads();
-		double t = 0.0;
-#pragma unroll
-		for (int k = 0; k < kPWarps; ++k) t += sh->wp[parity][k];
-		if (CL > 1)
-		{
-			if (threadIdx.x == 0) sh->slot[parity] = t;
-			cg::cluster_group cl = cg::this_cluster();
-			cl.sync();
-			double u = 0.0;
-			if (lane < CL) u = *cl.map_shared_rank(&sh->slot[parity], lane);
-			t = warp_sum(u);
-		}
-		parity ^= 1;
-		return t;
-	}
-};
-
-struct BatchParams
-{
-	const DevBody* bodies;
-	const int* big;
-	int nbig;
-	const int* small;
-	int nsmall;
-	unsigned* queue;
-	int steps;
-	float h;
-	int newton;
-	int max_iter;
-	double tol2;
-	int refresh;
-	double newton_tol2;
-	unsigned long long* prof;  // optional: kPhases cycle counters per CTA
-};
-
-// Phases timed by the optional instrumentation (cycles of thread 0 of each CTA, barriers and
-// reductions included in the phase that ends with them).
-enum { kPhElem = 0, kPhAsm = 1, kPhSpmv = 2, kPhUpdate = 3, kPhDir = 4, kPhFinal = 5, kPhIdle = 6, kPhases = 8 };
-
-struct PhaseClock
-{
-	unsigned long long* slot;
-	long long t;
-	__device__ void start(unsigned long long* p)
-	{
-		slot = p ? p + (size_t)blockIdx.x * kPhases : nullptr;
-		if (slot) t = clock64();
-	}
-	__device__ void tick(int phase)
-	{
-		if (!slot) return;
-		long long now = clock64();
-		if (threadIdx.x == 0) slot[phase] += (unsigned long long)(now - t);
-		t = now;
-	}
-};
-
-// PCG update of two rows (slices sl and sl + stride of one warp) with every load issued before
-// the first store: x += alpha d and, unless this is a refresh iteration, r -= alpha q,
-// s = M^-1 r. Returns the rows' r.s.
-template <class TV, class LD>
-__device__ __forceinline__ double update_two(const DevBody& B, TV* __restrict__ py, const TV* __restrict__ d,
-                                             TV* __restrict__ r, const TV* __restrict__ q, TV* __restrict__ s,
-                                             int i0, int i1, bool ok1, TV alpha, bool refresh)
-{
-	const int ii[2] = {i0, i1};
-	const bool ok[2] = {true, ok1};
-	TV x[2][3], dd[2][3], rr[2][3], qq[2][3];
-#pragma unroll
-	for (int u = 0; u < 2; ++u)
-		if (ok[u])
-		{
-			vld<TV, LD>(py, ii[u], x[u]);
-			vld<TV, LD>(d, ii[u], dd[u]);
-			if (!refresh)
-			{
-				vld<TV, LD>(r, ii[u], rr[u]);
-				vld<TV, LD>(q, ii[u], qq[u]);
-			}
-		}
-	double part = 0.0;
-#pragma unroll
-	for (int u = 0; u < 2; ++u)
-	{
-		if (!ok[u]) continue;
-		TV nx[3];
-#pragma unroll
-		for (int c = 0; c < 3; ++c) nx[c] = x[u][c] + alpha * dd[u][c];
-		vst(py, ii[u], nx);
-		if (refresh) continue;
-		TV nr[3], ss[3];
-#pragma unroll
-		for (int c = 0; c < 3; ++c) nr[c] = rr[u][c] - alpha * qq[u][c];
-		precond_row<TV, LD>(B, ii[u], nr, ss);
-		vst(r, ii[u], nr);
-		vst(s, ii[u], ss);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)nr[c] * (double)ss[c];
-	}
-	return part;
-}
-
-// d = s + beta d for two rows, loads first
-template <class TV, class LD>
-__device__ __forceinline__ void direction_two(TV* __restrict__ d, const TV* __restrict__ s, int i0, int i1, bool ok1,
-                                              TV beta)
-{
-	TV s0[3], d0[3], s1[3], d1[3];
-	vld<TV, LD>(s, i0, s0);
-	vld<TV, LD>(d, i0, d0);
-	if (ok1)
-	{
-		vld<TV, LD>(s, i1, s1);
-		vld<TV, LD>(d, i1, d1);
-	}
-#pragma unroll
-	for (int c = 0; c < 3; ++c)
-	{
-		d0[c] = s0[c] + beta * d0[c];
-		d1[c] = s1[c] + beta * d1[c];
-	}
-	vst(d, i0, d0);
-	if (ok1) vst(d, i1, d1);
-}
-
-// r = pb - A x, s = M^-1 r for the rows of one warp's slices (init / refresh); optionally d = s
-template <class TA, class TV, class LD>
-__device__ __forceinline__ double residual_rows(const DevBody& B, const TA* A, const TV* x, int s0, int stride,
-                                                bool set_d)
-{
-	const int lane = threadIdx.x & 31;
-	double part = 0.0;
-	for (int sl = s0; sl < B.nslices; sl += stride)
-	{
-		const int i = sl * kSlice + lane;
-		if (i >= B.n) continue;
-		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-		TV o[3], b[3], rr[3], ss[3];
-		spmv_row<TA, TV, LD>(A, B.col, B.nslots, base, w, lane, x, o);
-		vld<TV, LD>((const TV*)B.pb, i, b);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) rr[c] = b[c] - o[c];
-		precond_row<TV, LD>(B, i, rr, ss);
-		vst((TV*)B.r, i, rr);
-		vst((TV*)B.s, i, ss);
-		if (set_d) vst((TV*)B.d, i, ss);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)rr[c] * (double)ss[c];
-	}
-	return part;
-}
-
-// q = A d and this warp's part of d.q
-template <class TA, class TV, class LD>
-__device__ __forceinline__ double spmv_dot_rows(const DevBody& B, const TA* A, const TV* d, TV* q, int s0, int stride)
-{
-	const int lane = threadIdx.x & 31;
-	double part = 0.0;
-	for (int sl = s0; sl < B.nslices; sl += stride)
-	{
-		const int i = sl * kSlice + lane;
-		if (i >= B.n) continue;
-		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-		TV o[3], dd[3];
-		spmv_row<TA, TV, LD>(A, B.col, B.nslots, base, w, lane, d, o);
-		vst(q, i, o);
-		vld<TV, LD>(d, i, dd);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)dd[c] * (double)o[c];
-	}
-	return part;
-}
-
-// The implicit step of one body by one team; mirrors the per-op path of kernels.cu phase for
-// phase (same device functions, same reduction decisions).
-template <int CL, class TA, class TV>
-__device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, bool bf16)
-{
-	// A single-CTA team reads what its own threads wrote behind __syncthreads: ordinary (L1)
-	// loads are coherent there. Cluster teams read other SMs' writes: L2-coherent loads.
-	typedef typename std::conditional<CL == 1, LdPlain, LdCG>::type LD;
-	const int lane = threadIdx.x & 31;
-	const TA* Asp = (sizeof(TA) == sizeof(float) && !bf16) ? (const TA*)B.A32 : (const TA*)B.Alo;
-	const float h = P.h;
-	TV* py = (TV*)B.py;
-	TV* pb = (TV*)B.pb;
-	TV* r = (TV*)B.r;
-	TV* s = (TV*)B.s;
-	TV* d = (TV*)B.d;
-	TV* q = (TV*)B.q;
-	int min_it = 0x7fffffff, max_it = 0, status = B3G_SOLVE_CONVERGED, newton_done_at = 0;
-	double delta = 0.0, delta0 = 0.0, err = 0.0, err0 = 0.0;
-	int iter = 0;
-	unsigned long long iters_all = 0ull;
-	PhaseClock pc;
-	pc.start(P.prof);
-	if (T.tid() == 0) B.sc->fault = 0;  // ordered before any SpMV by the element-phase barrier
-	for (int k = 0; k < P.newton; ++k)
-	{
-		StepParams sp;
-		sp.h = h;
-		sp.first_newton = k == 0 ? 1 : 0;
-		const bool finish = P.newton == 1;
-		for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LD>(B, e, sp);
-		for (int e = T.tid(); e < B.ntr; e += T.nthreads()) tri_element<LD>(B, e, sp);
-		for (int e = T.tid(); e < B.ns; e += T.nthreads()) spring_element<LD>(B, e, sp);
-		T.sync();
-		pc.tick(kPhElem);
-		double part = 0.0;
-		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
-			part += assemble_row<TA, TV, LD>(B, sl, lane, sp, k == 0);
-		if (k > 0)
-		{
-			// warm start from the previous solution: r = pb - A py
-			T.sync();
-			part = (sizeof(TA) == sizeof(double))
-			           ? residual_rows<TA, TV, LD>(B, Asp, py, T.warp(), T.nwarps(), true)
-			           : residual_rows<float, TV, LD>(B, B.A32, py, T.warp(), T.nwarps(), true);
-		}
-		delta0 = T.reduce(part);
-		pc.tick(kPhAsm);
-		delta = delta0;
-		iter = 0;
-		bool pending = false;
-		bool done;
-		if (!isfinite(delta0))
-		{
-			status = B3G_SOLVE_NONFINITE;
-			done = true;
-		}
-		else if (delta0 <= P.tol2 * delta0)
-		{
-			status = B3G_SOLVE_CONVERGED;
-			done = true;
-		}
-		else if (P.max_iter <= 0)
-		{
-			status = B3G_SOLVE_MAX_ITERATIONS;
-			done = true;
-		}
-		else
-			done = false;
-		while (!done)
-		{
-			// q = A d (block planes staged through shared memory), alpha = delta / d.q
-			part = spmv_dot_rows<TA, TV, LD>(B, Asp, d, q, T.warp(), T.nwarps());
-			const double dq = T.reduce(part);
-			pc.tick(kPhSpmv);
-			if (!isfinite(dq))
-			{
-				status = B3G_SOLVE_NONFINITE;
-				break;
-			}
-			if (!(dq > 0.0))
-			{
-				status = B3G_SOLVE_BREAKDOWN;
-				break;
-			}
-			const TV alpha = (TV)(delta / dq);
-			const bool refresh = (P.refresh > 0 && (iter % P.refresh) == 0) || pending;
-			part = 0.0;
-			for (int sl = T.warp(); sl < B.nslices; sl += 2 * T.nwarps())
-			{
-				const int i0 = sl * kSlice + lane;
-				const int sl1 = sl + T.nwarps();
-				const int i1 = sl1 * kSlice + lane;
-				if (i0 >= B.n) continue;
-				part += update_two<TV, LD>(B, py, d, r, q, s, i0, i1, sl1 < B.nslices && i1 < B.n, alpha, refresh);
-			}
-			if (refresh)
-			{
-				// sparse_solver.cpp:83-90: r = b - A x with the full-precision blocks
-				T.sync();
-				part = (sizeof(TA) == sizeof(double))
-				           ? residual_rows<TA, TV, LD>(B, Asp, py, T.warp(), T.nwarps(), false)
-				           : residual_rows<float, TV, LD>(B, B.A32, py, T.warp(), T.nwarps(), false);
-			}
-			const double dn = T.reduce(part);
-			pc.tick(kPhUpdate);
-			const double beta = dn / delta;
-			delta = dn;
-			iter += 1;
-			if (!isfinite(dn))
-			{
-				status = B3G_SOLVE_NONFINITE;
-				break;
-			}
-			bool conv = dn <= P.tol2 * delta0;
-			if (bf16 && conv && !refresh)
-			{
-				pending = true;
-				conv = false;
-			}
-			if (refresh) pending = false;
-			if (conv)
-			{
-				status = B3G_SOLVE_CONVERGED;
-				break;
-			}
-			if (iter >= P.max_iter)
-			{
-				status = B3G_SOLVE_MAX_ITERATIONS;
-				break;
-			}
-			const TV bt = (TV)beta;
-			for (int sl = T.warp(); sl < B.nslices; sl += 2 * T.nwarps())
-			{
-				const int i0 = sl * kSlice + lane;
-				const int sl1 = sl + T.nwarps();
-				const int i1 = sl1 * kSlice + lane;
-				if (i0 >= B.n) continue;
-				direction_two<TV, LD>(d, s, i0, i1, sl1 < B.nslices && i1 < B.n, bt);
-			}
-			T.sync();
-			pc.tick(kPhDir);
-		}
-		min_it = iter < min_it ? iter : min_it;
-		max_it = iter > max_it ? iter : max_it;
-		iters_all += (unsigned long long)iter;
-		// every thread finished its PCG reads before the final update rewrites x / v
-		T.sync();
-		part = 0.0;
-		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
-		{
-			const int i = sl * kSlice + lane;
-			if (i < B.n) part += final_vertex<TV, LD>(B, i, h, k == 0, finish);
-		}
-		err = T.reduce(part);
-		pc.tick(kPhFinal);
-		if (k == 0) err0 = err;
-		newton_done_at = k + 1;
-		if (finish) break;
-		const bool ndone = k == 0 ? err <= P.newton_tol2 : err <= P.newton_tol2 * err0;
-		if (ndone || k == P.newton - 1)
-		{
-			T.sync();
-			for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
-			{
-				const int i = sl * kSlice + lane;
-				if (i < B.n) post_vertex<LD>(B, i, h);
-			}
-			break;
-		}
-	}
-	T.sync();
-	if (T.tid() == 0)
-	{
-		Scalars* sc = B.sc;
-		sc->iter = iter;
-		sc->delta = delta;
-		sc->delta0 = delta0;
-		sc->status = status;
-		sc->min_it = min_it;
-		sc->max_it = max_it;
-		sc->newton_iter = newton_done_at;
-		sc->newton_err = err;
-		sc->done = 1;
-		if (sc->fault) sc->status = B3G_SOLVE_DEVICE_TIMEOUT;
-		sc->total_iters += iters_all;
-		sc->total_steps += 1ull;
-	}
-}
-
-__device__ void load_body(DevBody* dst, const DevBody* src)
-{
-	const int words = (int)(sizeof(DevBody) / sizeof(int));
-	const int* s = (const int*)src;
-	int* d = (int*)dst;
-	for (int k = threadIdx.x; k < words; k += blockDim.x) d[k] = __ldcg(s + k);
-}
-
-template <int CL, class TA, class TV>
-__global__ void __launch_bounds__(kPThreads, B3G_BATCH_MIN_BLOCKS) k_batch(BatchParams P, int bf16)
-{
-	__shared__ TeamShared sh;
-	__shared__ __align__(16) DevBody sb;
-
-	if (CL > 1)
-	{
-		cg::cluster_group cl = cg::this_cluster();
-		Team<CL> T;
-		T.sh = &sh;
-		T.parity = 0;
-		T.rank = (int)cl.block_rank();
-		for (;;)
-		{
-			if (T.rank == 0 && threadIdx.x == 0) sh.item = (int)atomicAdd(P.queue, 1u);
-			cl.sync();
-			const int item = *cl.map_shared_rank(&sh.item, 0);
-			cl.sync();
-			if (item >= P.nbig) break;
-			load_body(&sb, P.bodies + P.big[item]);
-			__syncthreads();
-			for (int st = 0; st < P.steps; ++st) team_step<CL, TA, TV>(T, sb, P, bf16 != 0);
-			cl.sync();
-		}
-	}
-	Team<1> T1;
-	T1.sh = &sh;
-	T1.parity = 0;
-	T1.rank = 0;
-	for (;;)
-	{
-		if (threadIdx.x == 0) sh.item = (int)atomicAdd(P.queue + 1, 1u);
-		__syncthreads();
-		const int item = sh.item;
-		__syncthreads();
-		if (item >= P.nsmall) break;
-		load_body(&sb, P.bodies + P.small[item]);
-		__syncthreads();
-		for (int st = 0; st < P.steps; ++st) team_step<1, TA, TV>(T1, sb, P, bf16 != 0);
-		__syncthreads();
-	}
-}
-
-template <int CL, class TA, class TV>
-cudaError_t launch_cl(const BatchParams& P, int ctas, int bf16, cudaStream_t st)
-{
-	cudaLaunchConfig_t cfg = {};
-	cfg.gridDim = dim3((unsigned)ctas, 1, 1);
-	cfg.blockDim = dim3(kPThreads, 1, 1);
-	cfg.dynamicSmemBytes = 0;
-	cfg.stream = st;
-	cudaLaunchAttribute attr[1];
-	attr[0].id = cudaLaunchAttributeClusterDimension;
-	attr[0].val.clusterDim.x = CL;
-	attr[0].val.clusterDim.y = 1;
-	attr[0].val.clusterDim.z = 1;
-	cfg.attrs = attr;
-	cfg.numAttrs = 1;
-	return cudaLaunchKernelEx(&cfg, k_batch<CL, TA, TV>, P, bf16);
-}
-
-template <class TA, class TV>
-cudaError_t launch_prec(const BatchParams& P, int cluster, int ctas, int bf16, cudaStream_t st)
-{
-	switch (cluster)
-	{
-	case 1: return launch_cl<1, TA, TV>(P, ctas, bf16, st);
-	case 2: return launch_cl<2, TA, TV>(P, ctas, bf16, st);
-	case 4: return launch_cl<4, TA, TV>(P, ctas, bf16, st);
-	case 8: return launch_cl<8, TA, TV>(P, ctas, bf16, st);
-	default: return cudaErrorInvalidValue;
-	}
-}
-
-template <int CL, class TA, class TV>
-int max_clusters()
-{
-	cudaLaunchConfig_t cfg = {};
-	cfg.gridDim = dim3(CL * 64, 1, 1);
-	cfg.blockDim = dim3(kPThreads, 1, 1);
-	cfg.dynamicSmemBytes = 0;
-	cudaLaunchAttribute attr[1];
-	attr[0].id = cudaLaunchAttributeClusterDimension;
-	attr[0].val.clusterDim.x = CL;
-	attr[0].val.clusterDim.y = 1;
-	attr[0].val.clusterDim.z = 1;
-	cfg.attrs = attr;
-	cfg.numAttrs = 1;
-	int n = 0;
-	if (cudaOccupancyMaxActiveClusters(&n, k_batch<CL, TA, TV>, &cfg) != cudaSuccess) return 0;
-	return n;
-}
-
-template <class TA, class TV>
-int max_clusters_prec(int cluster)
-{
-	switch (cluster)
-	{
-	case 1: return max_clusters<1, TA, TV>();
-	case 2: return max_clusters<2, TA, TV>();
-	case 4: return max_clusters<4, TA, TV>();
-	case 8: return max_clusters<8, TA, TV>();
-	default: return 0;
-	}
-}
-
-} // namespace
-
 int batch_max_clusters(int prec, int cluster)
 {
-	if (prec == kP64) return max_clusters_prec<double, double>(cluster);
-	if (prec == kPBF) return max_clusters_prec<__nv_bfloat16, float>(cluster);
-	return max_clusters_prec<float, float>(cluster);
+	if (prec == kP64) return max_clusters_f64(cluster);
+	if (prec == kPBF) return max_clusters_bf16(cluster);
+	return max_clusters_f32(cluster);
 }
 
 cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
@@ -569,9 +29,9 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 	P.prof = A.prof;
 	cudaError_t e = cudaMemsetAsync(A.queue, 0, 2 * sizeof(unsigned), st);
 	if (e != cudaSuccess) return e;
-	if (A.prec == kP64) return launch_prec<double, double>(P, A.cluster, A.ctas, 0, st);
-	if (A.prec == kPBF) return launch_prec<__nv_bfloat16, float>(P, A.cluster, A.ctas, 1, st);
-	return launch_prec<float, float>(P, A.cluster, A.ctas, 0, st);
+	if (A.prec == kP64) return launch_batch_f64(P, A.cluster, A.ctas, st);
+	if (A.prec == kPBF) return launch_batch_bf16(P, A.cluster, A.ctas, st);
+	return launch_batch_f32(P, A.cluster, A.ctas, st);
 }
 
 } // namespace b3g

@@ -17,6 +17,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -178,7 +179,7 @@ uint64_t estimate_bytes(const HostDesc& h)
 	return (uint64_t)(1.15 * b) + (64u << 10);
 }
 
-constexpr int kServerCluster = 4;
+constexpr int kServerCluster = 8;  // default team size of large bodies (B3G_SERVER_CLUSTER overrides)
 constexpr uint32_t kServerThreshold = 4096;
 
 struct Request
@@ -212,6 +213,7 @@ struct b3g_server
 	float dt = 0;
 	uint64_t budget = 0, resident_bytes = 0;
 	uint32_t max_active = 0;
+	int cluster = kServerCluster;
 	std::mutex mu;
 	std::condition_variable cv;
 	std::vector<SBody> bodies;
@@ -413,8 +415,8 @@ int prepare(b3g_server* s, const std::vector<uint32_t>& act, int* nbig)
 	std::stable_sort(s->h_order, s->h_order + act.size(),
 	                 [&](int a, int b) { return s->bodies[act[a]].h.n > s->bodies[act[b]].h.n; });
 	// One schedule for every launch: bodies of kServerThreshold vertices or more are stepped by
-	// clusters of kServerCluster CTAs, the rest by single CTAs, always by the same kernel, so a
-	// body's arithmetic does not depend on which other bodies share the launch.
+	// clusters of s->cluster CTAs, the rest by single CTAs, always by the same kernel, so a body's
+	// arithmetic does not depend on which other bodies share the launch.
 	*nbig = 0;
 	for (uint32_t k : act)
 		if (s->bodies[k].h.n >= kServerThreshold) ++*nbig;
@@ -429,8 +431,8 @@ int step_active(b3g_server* s, int count, int nbig)
 	cudaError_t e = cudaMemcpyAsync(s->d_table, s->h_table, count * sizeof(DevBody), cudaMemcpyHostToDevice, st);
 	if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_order, s->h_order, count * sizeof(int), cudaMemcpyHostToDevice, st);
 	if (e != cudaSuccess) return cuda_fail(e, "server upload");
-	int m = batch_max_clusters(prec, kServerCluster);
-	if (m <= 0) m = std::max(1, s->ctx->sm_count / kServerCluster);
+	int m = batch_max_clusters(prec, s->cluster);
+	if (m <= 0) m = std::max(1, s->ctx->sm_count / s->cluster);
 	BatchArgs A;
 	A.bodies = s->d_table;
 	A.big = s->d_order;
@@ -446,8 +448,8 @@ int step_active(b3g_server* s, int count, int nbig)
 	A.refresh = (int)s->cfg.refresh_period;
 	A.newton_tol2 = s->cfg.newton_tolerance * s->cfg.newton_tolerance;
 	A.prec = prec;
-	A.cluster = kServerCluster;
-	A.ctas = m * kServerCluster;
+	A.cluster = s->cluster;
+	A.ctas = m * s->cluster;
 	A.prof = nullptr;
 	cudaEventRecord(s->ev0, st);
 	e = op_batch(A, st);
@@ -551,6 +553,12 @@ int b3g_server_create(b3g_context* ctx, uint64_t memory_budget_bytes, uint32_t m
 	s->budget = memory_budget_bytes;
 	s->max_active = max_active;
 	cudaSetDevice(ctx->device);
+	if (const char* env = std::getenv("B3G_SERVER_CLUSTER"))
+	{
+		const int c = std::atoi(env);
+		if (c == 1 || c == 2 || c == 4 || c == 8 || c == 16) s->cluster = c;
+	}
+	while (s->cluster > 1 && batch_max_clusters(prec_of(&s->cfg), s->cluster) <= 0) s->cluster /= 2;
 	cudaError_t e = cudaMalloc(&s->d_table, max_active * sizeof(DevBody));
 	if (e == cudaSuccess) e = cudaMalloc(&s->d_order, max_active * sizeof(int));
 	if (e == cudaSuccess) e = cudaMalloc(&s->d_queue, 4 * sizeof(unsigned));
@@ -656,6 +664,8 @@ int b3g_server_get_stats(b3g_server* s, b3g_server_stats* out)
 	std::lock_guard<std::mutex> lk(s->mu);
 	std::memset(out, 0, sizeof(*out));
 	out->iterations = s->iteration - s->iteration_base;
+	out->cluster_ctas = (uint32_t)s->cluster;
+	out->cluster_threshold = kServerThreshold;
 	out->vertex_steps = s->vertex_steps;
 	out->admitted = s->admitted;
 	out->completed = s->completed;

@@ -273,6 +273,8 @@ typedef struct b3g_server_stats
 	double gpu_seconds;            /* summed device time of the launches */
 	double wall_seconds;           /* first arrival to last completed launch */
 	double step_ms_p50, step_ms_p99; /* device time per launch */
+	uint32_t cluster_ctas;         /* CTAs of the team of a large body */
+	uint32_t cluster_threshold;    /* vertices from which a body is large */
 } b3g_server_stats;
 
 /* config NULL = b3g_solver_config_default; max_active bounds the bodies of one launch. */
