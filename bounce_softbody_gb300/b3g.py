@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from typing import Optional, Sequence
 
 import numpy as np
@@ -177,12 +178,16 @@ def solver_config(force_iterations: int = 1, max_pcg_iterations: int = 200, pcg_
 
 
 class Context:
+    """A b3g context. Bodies and servers made on it register here; close() closes them first, so a
+    body never outlives the context its device memory and stream belong to."""
+
     def __init__(self, device: int = 0):
         lib = load_library()
         h = C.c_void_p()
         _check(lib.b3g_context_create(device, C.byref(h)), "b3g_context_create")
         self.handle = h
         self.device = device
+        self._dependents = weakref.WeakSet()
 
     def stream(self) -> int:
         s = C.c_void_p()
@@ -194,6 +199,10 @@ class Context:
 
     def close(self):
         if self.handle:
+            # servers first (their worker thread steps bodies of this context), then bodies
+            deps = sorted(list(self._dependents), key=lambda o: 0 if isinstance(o, Server) else 1)
+            for o in deps:
+                o.close()
             load_library().b3g_context_destroy(self.handle)
             self.handle = None
 
@@ -272,6 +281,7 @@ class Body:
         _check(lib.b3g_body_create(ctx.handle, C.byref(d), C.byref(h)), "b3g_body_create")
         del keep
         self.handle = h
+        ctx._dependents.add(self)
         self.n = desc.n
         self.tet_count = desc.tets.shape[0]
 
@@ -420,6 +430,7 @@ class Server:
         _check(lib.b3g_server_create(ctx.handle, int(memory_budget_bytes), int(max_active), float(dt),
                                      C.byref(cfg), C.byref(h)), "b3g_server_create")
         self.handle = h
+        ctx._dependents.add(self)
         self.sizes = []
 
     def add_body(self, desc, masses=None) -> int:

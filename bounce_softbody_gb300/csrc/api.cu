@@ -236,6 +236,8 @@ int ensure_precision(b3g_body* b, int prec)
 	if (prec == kP64) alo = 9 * (size_t)b->d.nslots * sizeof(double);
 	if (prec == kPBF) alo = 9 * (size_t)b->d.nslots * sizeof(__nv_bfloat16);
 	bytes += align_up(alo);
+	const size_t xd = prec == kP64 ? 0 : 4 * np * sizeof(double);  // FP64 solution for refinement
+	bytes += align_up(xd);
 	char* mem = nullptr;
 	cudaError_t e = cudaMalloc(&mem, bytes);
 	if (e != cudaSuccess) return cuda_fail(e, "allocating solver vectors");
@@ -257,10 +259,12 @@ int ensure_precision(b3g_body* b, int prec)
 	pb.minv = p;
 	p += align_up(12 * np * vs);
 	pb.alo = alo ? p : nullptr;
+	p += align_up(alo);
+	pb.xd = xd ? (double*)p : nullptr;
 	return B3G_OK;
 }
 
-DevBody dev_for(const b3g_body* b, int prec, int precond)
+DevBody dev_for(const b3g_body* b, int prec, int precond, bool refine)
 {
 	DevBody d = b->d;
 	const PrecBuffers& pb = b->prec[prec];
@@ -273,6 +277,7 @@ DevBody dev_for(const b3g_body* b, int prec, int precond)
 	d.py = pb.vec[6];
 	d.Minv = pb.minv;
 	d.Alo = pb.alo;
+	d.xd = refine ? pb.xd : nullptr;
 	d.precond = precond;
 	return d;
 }
@@ -714,7 +719,7 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 	const int prec = prec_of(&cfg);
 	rc = ensure_precision(b, prec);
 	if (rc != B3G_OK) return rc;
-	DevBody D = dev_for(b, prec, cfg.preconditioner);
+	DevBody D = dev_for(b, prec, cfg.preconditioner, true);
 	const int newton = (int)std::max<uint32_t>(1u, cfg.force_iterations);
 	e = op_begin(D, st, (int)cfg.max_pcg_iterations, cfg.pcg_tolerance * cfg.pcg_tolerance, (int)cfg.refresh_period,
 	             cfg.newton_tolerance * cfg.newton_tolerance);
@@ -730,7 +735,7 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 		for (int it = 0; it < (int)cfg.max_pcg_iterations && e == cudaSuccess; it += chunk)
 		{
 			for (int j = 0; j < chunk && it + j < (int)cfg.max_pcg_iterations && e == cudaSuccess; ++j)
-				e = op_pcg_iteration(D, prec, st);
+				e = op_pcg_iteration(D, prec, it + j, (int)cfg.refresh_period, st);
 			if (e != cudaSuccess) break;
 			e = cudaMemcpyAsync(&hs->done, &D.sc->done, sizeof(int), cudaMemcpyDeviceToHost, st);
 			if (e == cudaSuccess) e = cudaStreamSynchronize(st);

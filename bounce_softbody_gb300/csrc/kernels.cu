@@ -4,6 +4,8 @@
 #include "device.cuh"
 #include "ops.h"
 
+#include <utility>
+
 #include <algorithm>
 
 namespace b3g {
@@ -196,11 +198,22 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(DevBody B, const TA* A)
 		const int i = sl * kSlice + lane;
 		if (i >= B.n) continue;
 		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-		TV q[3], b[3], rr[3], ss[3];
-		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, (const TV*)B.py, q);
+		TV b[3], rr[3], ss[3];
 		vld<TV, LdPlain>((const TV*)B.pb, i, b);
+		if (B.xd)
+		{
+			double q[3];
+			spmv_row_x64(B.A32, B.col, B.nslots, base, w, lane, B.xd, q);
 #pragma unroll
-		for (int c = 0; c < 3; ++c) rr[c] = b[c] - q[c];
+			for (int c = 0; c < 3; ++c) rr[c] = (TV)((double)b[c] - q[c]);
+		}
+		else
+		{
+			TV q[3];
+			spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, (const TV*)B.py, q);
+#pragma unroll
+			for (int c = 0; c < 3; ++c) rr[c] = b[c] - q[c];
+		}
 		precond_row<TV>(B, i, rr, ss);
 		vst((TV*)B.r, i, rr);
 		vst((TV*)B.s, i, ss);
@@ -212,25 +225,28 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(DevBody B, const TA* A)
 	if (grid_reduce(part, B.partials, &B.sc->counter, &total)) pcg_start(B.sc, total);
 }
 
-// q = A d and alpha = delta / d.q
+// d' = s + beta d (d' = s on a solve's first iteration), q = A d' and alpha = delta / d'.q.
+// Reads the direction from B.d and writes the new one to B.d2; the host swaps the two buffers
+// every iteration.
 template <class TA, class TV>
-__global__ void __launch_bounds__(kThreads) k_spmv_dot(DevBody B, const TA* A)
+__global__ void __launch_bounds__(kThreads) k_dir_spmv_dot(DevBody B, const TA* A)
 {
 	if (B.sc->done) return;
 	const int lane = threadIdx.x & 31;
-	const TV* d = (const TV*)B.d;
+	const bool first = B.sc->iter == 0;
+	const TV beta = (TV)B.sc->beta;
 	double part = 0.0;
 	for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < B.nslices; sl += (gridDim.x * blockDim.x) >> 5)
 	{
 		const int i = sl * kSlice + lane;
 		if (i >= B.n) continue;
 		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-		TV o[3], dd[3];
-		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, d, o);
+		TV o[3], dn[3];
+		spmv_row_dir<TA, TV>(A, B.col, B.nslots, base, w, lane, (const TV*)B.s, (const TV*)B.d, beta, first, o, dn);
 		vst((TV*)B.q, i, o);
-		vld<TV, LdPlain>(d, i, dd);
+		vst((TV*)B.d2, i, dn);
 #pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)dd[c] * (double)o[c];
+		for (int c = 0; c < 3; ++c) part += (double)dn[c] * (double)o[c];
 	}
 	double total;
 	if (grid_reduce(part, B.partials, &B.sc->counter, &total))
@@ -252,7 +268,7 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(DevBody B, const TA* A)
 	}
 }
 
-// x += alpha d; unless this is a refresh iteration: r -= alpha q, s = M^-1 r, delta = r.s
+// x += alpha d' (d' in B.d2); unless this is a refresh iteration: r -= alpha q, s = M^-1 r, delta = r.s
 template <class TV>
 __global__ void __launch_bounds__(kThreads) k_update(DevBody B, int bf16_mode)
 {
@@ -260,20 +276,34 @@ __global__ void __launch_bounds__(kThreads) k_update(DevBody B, int bf16_mode)
 	if (sc->done) return;
 	const bool refresh = refresh_now(sc);
 	const TV alpha = (TV)sc->alpha;
+	const double alpha_d = sc->alpha;
 	double part = 0.0;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
 	{
-		TV x[3], d[3], r[3], q[3], s[3];
-		vld<TV, LdPlain>((const TV*)B.py, i, x);
-		vld<TV, LdPlain>((const TV*)B.d, i, d);
+		TV d[3], r[3], q[3], s[3];
+		vld<TV, LdPlain>((const TV*)B.d2, i, d);  // this iteration's direction
 		if (!refresh)
 		{
 			vld<TV, LdPlain>((const TV*)B.r, i, r);
 			vld<TV, LdPlain>((const TV*)B.q, i, q);
 		}
+		if (B.xd)
+		{
+			// refinement: the solution accumulates in FP64
+			double x[3];
+			vld<double, LdPlain>(B.xd, i, x);
 #pragma unroll
-		for (int c = 0; c < 3; ++c) x[c] += alpha * d[c];
-		vst((TV*)B.py, i, x);
+			for (int c = 0; c < 3; ++c) x[c] += alpha_d * (double)d[c];
+			vst(B.xd, i, x);
+		}
+		else
+		{
+			TV x[3];
+			vld<TV, LdPlain>((const TV*)B.py, i, x);
+#pragma unroll
+			for (int c = 0; c < 3; ++c) x[c] += alpha * d[c];
+			vst((TV*)B.py, i, x);
+		}
 		if (refresh) continue;
 #pragma unroll
 		for (int c = 0; c < 3; ++c) r[c] -= alpha * q[c];
@@ -302,11 +332,23 @@ __global__ void __launch_bounds__(kThreads) k_resid(DevBody B, const TA* A, int 
 		const int i = sl * kSlice + lane;
 		if (i >= B.n) continue;
 		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
-		TV q[3], b[3], rr[3], ss[3];
-		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, (const TV*)B.py, q);
+		TV b[3], rr[3], ss[3];
 		vld<TV, LdPlain>((const TV*)B.pb, i, b);
+		if (B.xd)
+		{
+			// refinement: b - A x from the FP64 solution with FP64 sums, rounded once
+			double q[3];
+			spmv_row_x64(B.A32, B.col, B.nslots, base, w, lane, B.xd, q);
 #pragma unroll
-		for (int c = 0; c < 3; ++c) rr[c] = b[c] - q[c];
+			for (int c = 0; c < 3; ++c) rr[c] = (TV)((double)b[c] - q[c]);
+		}
+		else
+		{
+			TV q[3];
+			spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, (const TV*)B.py, q);
+#pragma unroll
+			for (int c = 0; c < 3; ++c) rr[c] = b[c] - q[c];
+		}
 		precond_row<TV>(B, i, rr, ss);
 		vst((TV*)B.r, i, rr);
 		vst((TV*)B.s, i, ss);
@@ -315,24 +357,6 @@ __global__ void __launch_bounds__(kThreads) k_resid(DevBody B, const TA* A, int 
 	}
 	double total;
 	if (grid_reduce(part, B.partials, &sc->counter, &total)) decide_after_reduction(sc, total, bf16_mode != 0, true);
-}
-
-// d = s + beta d
-template <class TV>
-__global__ void __launch_bounds__(kThreads) k_direction(DevBody B)
-{
-	Scalars* sc = B.sc;
-	if (sc->done) return;
-	const TV beta = (TV)sc->beta;
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
-	{
-		TV d[3], s[3];
-		vld<TV, LdPlain>((const TV*)B.d, i, d);
-		vld<TV, LdPlain>((const TV*)B.s, i, s);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) d[c] = s[c] + beta * d[c];
-		vst((TV*)B.d, i, d);
-	}
 }
 
 // v = v + dv, x = x0 + h v + y, Newton error |dv|^2 (sparse_force_solver.cpp:194-223).
@@ -432,7 +456,7 @@ int vertex_grid(const DevBody& B) { return grid_for(B.n, kThreads); }
 template <class TA, class TV>
 cudaError_t launch_spmv(const DevBody& B, const TA* A, cudaStream_t st)
 {
-	k_spmv_dot<TA, TV><<<slice_grid(B), kThreads, 0, st>>>(B, A);
+	k_dir_spmv_dot<TA, TV><<<slice_grid(B), kThreads, 0, st>>>(B, A);
 	return cudaGetLastError();
 }
 
@@ -477,8 +501,15 @@ cudaError_t op_pcg_init(const DevBody& B, int prec, cudaStream_t st)
 	return cudaGetLastError();
 }
 
-cudaError_t op_pcg_iteration(const DevBody& B, int prec, cudaStream_t st)
+cudaError_t op_pcg_iteration(const DevBody& D, int prec, int j, int refresh, cudaStream_t st)
 {
+	// direction buffers alternate: iteration j reads the direction from one and writes the new
+	// one to the other
+	DevBody B = D;
+	if (j & 1) std::swap(B.d, B.d2);
+	// the true-residual refresh runs when the iteration counter is a multiple of the period; in
+	// bf16 mode it may also be requested by a pending convergence check, so it is always launched
+	const bool resid = prec == kPBF || (refresh > 0 && j % refresh == 0);
 	int gs = slice_grid(B), gv = vertex_grid(B);
 	if (prec == kP64)
 	{
@@ -486,8 +517,7 @@ cudaError_t op_pcg_iteration(const DevBody& B, int prec, cudaStream_t st)
 		cudaError_t e = launch_spmv<double, double>(B, A, st);
 		if (e != cudaSuccess) return e;
 		k_update<double><<<gv, kThreads, 0, st>>>(B, 0);
-		k_resid<double, double><<<gs, kThreads, 0, st>>>(B, A, 0);
-		k_direction<double><<<gv, kThreads, 0, st>>>(B);
+		if (resid) k_resid<double, double><<<gs, kThreads, 0, st>>>(B, A, 0);
 	}
 	else if (prec == kPBF)
 	{
@@ -495,15 +525,13 @@ cudaError_t op_pcg_iteration(const DevBody& B, int prec, cudaStream_t st)
 		if (e != cudaSuccess) return e;
 		k_update<float><<<gv, kThreads, 0, st>>>(B, 1);
 		k_resid<float, float><<<gs, kThreads, 0, st>>>(B, B.A32, 1);
-		k_direction<float><<<gv, kThreads, 0, st>>>(B);
 	}
 	else
 	{
 		cudaError_t e = launch_spmv<float, float>(B, B.A32, st);
 		if (e != cudaSuccess) return e;
 		k_update<float><<<gv, kThreads, 0, st>>>(B, 0);
-		k_resid<float, float><<<gs, kThreads, 0, st>>>(B, B.A32, 0);
-		k_direction<float><<<gv, kThreads, 0, st>>>(B);
+		if (resid) k_resid<float, float><<<gs, kThreads, 0, st>>>(B, B.A32, 0);
 	}
 	return cudaGetLastError();
 }

@@ -27,7 +27,8 @@ cudaError_t op_newton_begin(const DevBody& B, cudaStream_t st);
 cudaError_t op_elements(const DevBody& B, const StepParamsHost& P, cudaStream_t st);
 cudaError_t op_assemble(const DevBody& B, const StepParamsHost& P, int prec, bool init, cudaStream_t st);
 cudaError_t op_pcg_init(const DevBody& B, int prec, cudaStream_t st);
-cudaError_t op_pcg_iteration(const DevBody& B, int prec, cudaStream_t st);
+// iteration j (0-based) of the current solve; refresh = the true-residual refresh period
+cudaError_t op_pcg_iteration(const DevBody& B, int prec, int j, int refresh, cudaStream_t st);
 // mode 0: write the Newton iterate (xi, vi); mode 1: write the state and finish the step
 cudaError_t op_final(const DevBody& B, const StepParamsHost& P, int prec, int mode, cudaStream_t st);
 // finish a multi-Newton step: iterate -> state, friction, clear, new contacts

@@ -207,7 +207,7 @@ __device__ __forceinline__ double residual_rows(const DevBody& B, const TA* A, c
 		if (i >= B.n) continue;
 		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 		TV o[3], b[3], rr[3], ss[3];
-		spmv_row<TA, TV, LD>(A, B.col, B.nslots, base, w, lane, x, o);
+		spmv_row<TA, TV, LD, MatVia<LD>>(A, B.col, B.nslots, base, w, lane, x, o);
 		vld<TV, LD>((const TV*)B.pb, i, b);
 #pragma unroll
 		for (int c = 0; c < 3; ++c) rr[c] = b[c] - o[c];
@@ -233,7 +233,7 @@ __device__ __forceinline__ double spmv_dot_rows(const DevBody& B, const TA* A, c
 		if (i >= B.n) continue;
 		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 		TV o[3], dd[3];
-		spmv_row<TA, TV, LD>(A, B.col, B.nslots, base, w, lane, d, o);
+		spmv_row<TA, TV, LD, MatVia<LD>>(A, B.col, B.nslots, base, w, lane, d, o);
 		vst(q, i, o);
 		vld<TV, LD>(d, i, dd);
 #pragma unroll
