@@ -1005,18 +1005,18 @@ __device__ __forceinline__ void spmv_row_x64(const float* A, const int* __restri
 // (first iteration of a solve: d' = s). The diagonal block leads every row, so the first gathered
 // column is the row itself and its d'_i is returned in dn. Every lane forms d'_j with the same
 // expression as the owner of row j, so all copies of a value agree bitwise.
-template <class TV>
+template <class TV, class L = LdPlain>
 __device__ __forceinline__ void gather_dir(const TV* s, const TV* d, TV beta, bool first, int j, TV o[3])
 {
-	vld<TV, LdPlain>(s, j, o);
+	vld<TV, L>(s, j, o);
 	if (first) return;
 	TV dj[3];
-	vld<TV, LdPlain>(d, j, dj);
+	vld<TV, L>(d, j, dj);
 #pragma unroll
 	for (int c = 0; c < 3; ++c) o[c] = o[c] + beta * dj[c];
 }
 
-template <class TA, class TV, class M = MatNC>
+template <class TA, class TV, class L = LdPlain, class M = MatNC>
 __device__ __forceinline__ void spmv_row_dir(const TA* A, const int* __restrict__ col, int nslots, int base, int w,
                                              int lane, const TV* s, const TV* d, TV beta, bool first, TV out[3],
                                              TV dn[3])
@@ -1033,10 +1033,10 @@ __device__ __forceinline__ void spmv_row_dir(const TA* A, const int* __restrict_
 #pragma unroll
 		for (int p = 0; p < 9; ++p) mat_load4(A + p * ns + off, a[p], pol, (M*)nullptr);
 		TV xv[4][3];
-		gather_dir<TV>(s, d, beta, first, jj.x, xv[0]);
-		gather_dir<TV>(s, d, beta, first, jj.y, xv[1]);
-		gather_dir<TV>(s, d, beta, first, jj.z, xv[2]);
-		gather_dir<TV>(s, d, beta, first, jj.w, xv[3]);
+		gather_dir<TV, L>(s, d, beta, first, jj.x, xv[0]);
+		gather_dir<TV, L>(s, d, beta, first, jj.y, xv[1]);
+		gather_dir<TV, L>(s, d, beta, first, jj.z, xv[2]);
+		gather_dir<TV, L>(s, d, beta, first, jj.w, xv[3]);
 		if (k == 0)
 		{
 #pragma unroll

@@ -47,7 +47,7 @@ struct BatchArgs
 	int nbig;
 	const int* small;        // device array: indices of bodies stepped by single CTAs
 	int nsmall;
-	unsigned* queue;         // device: two work counters, cleared by op_batch
+	unsigned* queue;         // device: four work counters (two per launch), cleared by op_batch
 	int steps;
 	float h;
 	int newton;

@@ -27,7 +27,7 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 	P.refresh = A.refresh;
 	P.newton_tol2 = A.newton_tol2;
 	P.prof = A.prof;
-	cudaError_t e = cudaMemsetAsync(A.queue, 0, 2 * sizeof(unsigned), st);
+	cudaError_t e = cudaMemsetAsync(A.queue, 0, 4 * sizeof(unsigned), st);  // two counters per launch
 	if (e != cudaSuccess) return e;
 	if (A.prec == kP64) return launch_batch_f64(P, A.cluster, A.ctas, st);
 	if (A.prec == kPBF) return launch_batch_bf16(P, A.cluster, A.ctas, st);

@@ -20,6 +20,7 @@
 #include "device.cuh"
 #include "ops.h"
 
+#include <atomic>
 #include <cooperative_groups.h>
 #include <type_traits>
 
@@ -242,8 +243,192 @@ __device__ __forceinline__ double spmv_dot_rows(const DevBody& B, const TA* A, c
 	return part;
 }
 
-// The implicit step of one body by one team; mirrors the per-op path of kernels.cu phase for
-// phase (same device functions, same reduction decisions).
+// Result of one PCG solve of a team.
+struct SolveOut
+{
+	int iter;
+	int status;
+	double delta;
+};
+
+// The preconditioned CG of one body by one team, from r, s, d, py set up by the assembly (or a
+// warm start) with r.s = delta0 (sparse_solver.cpp:57-108 with the true-residual refresh).
+template <int CL, class TA, class TV, class LD>
+__device__ SolveOut team_pcg(Team<CL>& T, const DevBody& B, const BatchParams& P, bool bf16, double delta0,
+                             PhaseClock& pc)
+{
+	const int lane = threadIdx.x & 31;
+	const TA* Asp = (sizeof(TA) == sizeof(float) && !bf16) ? (const TA*)B.A32 : (const TA*)B.Alo;
+	TV* py = (TV*)B.py;
+	TV* r = (TV*)B.r;
+	TV* s = (TV*)B.s;
+	TV* d = (TV*)B.d;
+	TV* q = (TV*)B.q;
+	SolveOut out;
+	out.status = B3G_SOLVE_CONVERGED;
+	out.iter = 0;
+	double delta = delta0;
+	bool pending = false;
+	bool done;
+	if (!isfinite(delta0))
+	{
+		out.status = B3G_SOLVE_NONFINITE;
+		done = true;
+	}
+	else if (delta0 <= P.tol2 * delta0)
+	{
+		out.status = B3G_SOLVE_CONVERGED;
+		done = true;
+	}
+	else if (P.max_iter <= 0)
+	{
+		out.status = B3G_SOLVE_MAX_ITERATIONS;
+		done = true;
+	}
+	else
+		done = false;
+	int iter = 0;
+	while (!done)
+	{
+		// q = A d, alpha = delta / d.q
+		double part = spmv_dot_rows<TA, TV, LD>(B, Asp, d, q, T.warp(), T.nwarps());
+		const double dq = T.reduce(part);
+		pc.tick(kPhSpmv);
+		if (!isfinite(dq))
+		{
+			out.status = B3G_SOLVE_NONFINITE;
+			break;
+		}
+		if (!(dq > 0.0))
+		{
+			out.status = B3G_SOLVE_BREAKDOWN;
+			break;
+		}
+		const TV alpha = (TV)(delta / dq);
+		const bool refresh = (P.refresh > 0 && (iter % P.refresh) == 0) || pending;
+		part = 0.0;
+		for (int sl = T.warp(); sl < B.nslices; sl += 2 * T.nwarps())
+		{
+			const int i0 = sl * kSlice + lane;
+			const int sl1 = sl + T.nwarps();
+			const int i1 = sl1 * kSlice + lane;
+			if (i0 >= B.n) continue;
+			part += update_two<TV, LD>(B, py, d, r, q, s, i0, i1, sl1 < B.nslices && i1 < B.n, alpha, refresh);
+		}
+		if (refresh)
+		{
+			// sparse_solver.cpp:83-90: r = b - A x with the full-precision blocks
+			T.sync();
+			part = (sizeof(TA) == sizeof(double))
+			           ? residual_rows<TA, TV, LD>(B, Asp, py, T.warp(), T.nwarps(), false)
+			           : residual_rows<float, TV, LD>(B, B.A32, py, T.warp(), T.nwarps(), false);
+		}
+		const double dn = T.reduce(part);
+		pc.tick(kPhUpdate);
+		const double beta = dn / delta;
+		delta = dn;
+		iter += 1;
+		if (!isfinite(dn))
+		{
+			out.status = B3G_SOLVE_NONFINITE;
+			break;
+		}
+		bool conv = dn <= P.tol2 * delta0;
+		if (bf16 && conv && !refresh)
+		{
+			pending = true;
+			conv = false;
+		}
+		if (refresh) pending = false;
+		if (conv)
+		{
+			out.status = B3G_SOLVE_CONVERGED;
+			break;
+		}
+		if (iter >= P.max_iter)
+		{
+			out.status = B3G_SOLVE_MAX_ITERATIONS;
+			break;
+		}
+		// d = s + beta d as its own sweep: folding it into the SpMV (as the per-op path does)
+		// doubles the SpMV's vector gathers, which for the hundreds of bodies a launch runs at
+		// once come from DRAM rather than L2 (measured 4% slower on the 512-body batch)
+		const TV bt = (TV)beta;
+		for (int sl = T.warp(); sl < B.nslices; sl += 2 * T.nwarps())
+		{
+			const int i0 = sl * kSlice + lane;
+			const int sl1 = sl + T.nwarps();
+			const int i1 = sl1 * kSlice + lane;
+			if (i0 >= B.n) continue;
+			direction_two<TV, LD>(d, s, i0, i1, sl1 < B.nslices && i1 < B.n, bt);
+		}
+		T.sync();
+		pc.tick(kPhDir);
+	}
+	out.iter = iter;
+	out.delta = delta;
+	return out;
+}
+
+// Element phase and row assembly of one Newton iteration; returns the team's r.s (the PCG's
+// delta0). k > 0 warm-starts from the previous solution: r = pb - A py.
+template <int CL, class TA, class TV, class LD>
+__device__ double team_assemble(Team<CL>& T, const DevBody& B, const BatchParams& P, bool bf16, int k, PhaseClock& pc)
+{
+	const int lane = threadIdx.x & 31;
+	StepParams sp;
+	sp.h = P.h;
+	sp.first_newton = k == 0 ? 1 : 0;
+	for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LD>(B, e, sp);
+	for (int e = T.tid(); e < B.ntr; e += T.nthreads()) tri_element<LD>(B, e, sp);
+	for (int e = T.tid(); e < B.ns; e += T.nthreads()) spring_element<LD>(B, e, sp);
+	T.sync();
+	pc.tick(kPhElem);
+	double part = 0.0;
+	for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
+		part += assemble_row<TA, TV, LD>(B, sl, lane, sp, k == 0);
+	if (k > 0)
+	{
+		const TA* Asp = (sizeof(TA) == sizeof(float) && !bf16) ? (const TA*)B.A32 : (const TA*)B.Alo;
+		T.sync();
+		part = (sizeof(TA) == sizeof(double))
+		           ? residual_rows<TA, TV, LD>(B, Asp, (const TV*)B.py, T.warp(), T.nwarps(), true)
+		           : residual_rows<float, TV, LD>(B, B.A32, (const TV*)B.py, T.warp(), T.nwarps(), true);
+	}
+	const double delta0 = T.reduce(part);
+	pc.tick(kPhAsm);
+	return delta0;
+}
+
+// Final update of a single-Newton step (state, friction, clearing, new contacts) and the
+// step's statistics.
+template <int CL, class TV, class LD>
+__device__ void team_finish(Team<CL>& T, const DevBody& B, const BatchParams& P, const SolveOut& so, double delta0,
+                            int newton_iters, int min_it, int max_it, unsigned long long iters_all, double err,
+                            PhaseClock& pc)
+{
+	T.sync();
+	if (T.tid() == 0)
+	{
+		Scalars* sc = B.sc;
+		sc->iter = so.iter;
+		sc->delta = so.delta;
+		sc->delta0 = delta0;
+		sc->status = so.status;
+		sc->min_it = min_it;
+		sc->max_it = max_it;
+		sc->newton_iter = newton_iters;
+		sc->newton_err = err;
+		sc->done = 1;
+		if (sc->fault) sc->status = B3G_SOLVE_DEVICE_TIMEOUT;
+		sc->total_iters += iters_all;
+		sc->total_steps += 1ull;
+	}
+}
+
+// The whole implicit step of one body by one team (any number of Newton iterations); mirrors
+// the per-op path of kernels.cu phase for phase (same device functions, same reduction
+// decisions).
 template <int CL, class TA, class TV>
 __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, bool bf16)
 {
@@ -251,146 +436,28 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 	// loads are coherent there. Cluster teams read other SMs' writes: L2-coherent loads.
 	typedef typename std::conditional<CL == 1, LdPlain, LdCG>::type LD;
 	const int lane = threadIdx.x & 31;
-	const TA* Asp = (sizeof(TA) == sizeof(float) && !bf16) ? (const TA*)B.A32 : (const TA*)B.Alo;
 	const float h = P.h;
-	TV* py = (TV*)B.py;
-	TV* pb = (TV*)B.pb;
-	TV* r = (TV*)B.r;
-	TV* s = (TV*)B.s;
-	TV* d = (TV*)B.d;
-	TV* q = (TV*)B.q;
-	int min_it = 0x7fffffff, max_it = 0, status = B3G_SOLVE_CONVERGED, newton_done_at = 0;
-	double delta = 0.0, delta0 = 0.0, err = 0.0, err0 = 0.0;
-	int iter = 0;
+	int min_it = 0x7fffffff, max_it = 0, newton_done_at = 0;
+	double delta0 = 0.0, err = 0.0, err0 = 0.0;
 	unsigned long long iters_all = 0ull;
+	SolveOut so;
+	so.iter = 0;
+	so.status = B3G_SOLVE_CONVERGED;
+	so.delta = 0.0;
 	PhaseClock pc;
 	pc.start(P.prof);
 	if (T.tid() == 0) B.sc->fault = 0;  // ordered before any SpMV by the element-phase barrier
 	for (int k = 0; k < P.newton; ++k)
 	{
-		StepParams sp;
-		sp.h = h;
-		sp.first_newton = k == 0 ? 1 : 0;
 		const bool finish = P.newton == 1;
-		for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LD>(B, e, sp);
-		for (int e = T.tid(); e < B.ntr; e += T.nthreads()) tri_element<LD>(B, e, sp);
-		for (int e = T.tid(); e < B.ns; e += T.nthreads()) spring_element<LD>(B, e, sp);
-		T.sync();
-		pc.tick(kPhElem);
-		double part = 0.0;
-		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
-			part += assemble_row<TA, TV, LD>(B, sl, lane, sp, k == 0);
-		if (k > 0)
-		{
-			// warm start from the previous solution: r = pb - A py
-			T.sync();
-			part = (sizeof(TA) == sizeof(double))
-			           ? residual_rows<TA, TV, LD>(B, Asp, py, T.warp(), T.nwarps(), true)
-			           : residual_rows<float, TV, LD>(B, B.A32, py, T.warp(), T.nwarps(), true);
-		}
-		delta0 = T.reduce(part);
-		pc.tick(kPhAsm);
-		delta = delta0;
-		iter = 0;
-		bool pending = false;
-		bool done;
-		if (!isfinite(delta0))
-		{
-			status = B3G_SOLVE_NONFINITE;
-			done = true;
-		}
-		else if (delta0 <= P.tol2 * delta0)
-		{
-			status = B3G_SOLVE_CONVERGED;
-			done = true;
-		}
-		else if (P.max_iter <= 0)
-		{
-			status = B3G_SOLVE_MAX_ITERATIONS;
-			done = true;
-		}
-		else
-			done = false;
-		while (!done)
-		{
-			// q = A d (block planes staged through shared memory), alpha = delta / d.q
-			part = spmv_dot_rows<TA, TV, LD>(B, Asp, d, q, T.warp(), T.nwarps());
-			const double dq = T.reduce(part);
-			pc.tick(kPhSpmv);
-			if (!isfinite(dq))
-			{
-				status = B3G_SOLVE_NONFINITE;
-				break;
-			}
-			if (!(dq > 0.0))
-			{
-				status = B3G_SOLVE_BREAKDOWN;
-				break;
-			}
-			const TV alpha = (TV)(delta / dq);
-			const bool refresh = (P.refresh > 0 && (iter % P.refresh) == 0) || pending;
-			part = 0.0;
-			for (int sl = T.warp(); sl < B.nslices; sl += 2 * T.nwarps())
-			{
-				const int i0 = sl * kSlice + lane;
-				const int sl1 = sl + T.nwarps();
-				const int i1 = sl1 * kSlice + lane;
-				if (i0 >= B.n) continue;
-				part += update_two<TV, LD>(B, py, d, r, q, s, i0, i1, sl1 < B.nslices && i1 < B.n, alpha, refresh);
-			}
-			if (refresh)
-			{
-				// sparse_solver.cpp:83-90: r = b - A x with the full-precision blocks
-				T.sync();
-				part = (sizeof(TA) == sizeof(double))
-				           ? residual_rows<TA, TV, LD>(B, Asp, py, T.warp(), T.nwarps(), false)
-				           : residual_rows<float, TV, LD>(B, B.A32, py, T.warp(), T.nwarps(), false);
-			}
-			const double dn = T.reduce(part);
-			pc.tick(kPhUpdate);
-			const double beta = dn / delta;
-			delta = dn;
-			iter += 1;
-			if (!isfinite(dn))
-			{
-				status = B3G_SOLVE_NONFINITE;
-				break;
-			}
-			bool conv = dn <= P.tol2 * delta0;
-			if (bf16 && conv && !refresh)
-			{
-				pending = true;
-				conv = false;
-			}
-			if (refresh) pending = false;
-			if (conv)
-			{
-				status = B3G_SOLVE_CONVERGED;
-				break;
-			}
-			if (iter >= P.max_iter)
-			{
-				status = B3G_SOLVE_MAX_ITERATIONS;
-				break;
-			}
-			const TV bt = (TV)beta;
-			for (int sl = T.warp(); sl < B.nslices; sl += 2 * T.nwarps())
-			{
-				const int i0 = sl * kSlice + lane;
-				const int sl1 = sl + T.nwarps();
-				const int i1 = sl1 * kSlice + lane;
-				if (i0 >= B.n) continue;
-				direction_two<TV, LD>(d, s, i0, i1, sl1 < B.nslices && i1 < B.n, bt);
-			}
-			T.sync();
-			pc.tick(kPhDir);
-		}
-		min_it = iter < min_it ? iter : min_it;
-		max_it = iter > max_it ? iter : max_it;
-		iters_all += (unsigned long long)iter;
+		delta0 = team_assemble<CL, TA, TV, LD>(T, B, P, bf16, k, pc);
+		so = team_pcg<CL, TA, TV, LD>(T, B, P, bf16, delta0, pc);
+		min_it = so.iter < min_it ? so.iter : min_it;
+		max_it = so.iter > max_it ? so.iter : max_it;
+		iters_all += (unsigned long long)so.iter;
 		// every thread finished its PCG reads before the final update rewrites x / v
 		T.sync();
-		part = 0.0;
+		double part = 0.0;
 		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
 		{
 			const int i = sl * kSlice + lane;
@@ -413,23 +480,44 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 			break;
 		}
 	}
+	team_finish<CL, TV, LD>(T, B, P, so, delta0, newton_done_at, min_it, max_it, iters_all, err, pc);
+}
+
+// Single-Newton step split in two launches so that each part runs with its own register budget
+// (the element and assembly code needs 128 registers a thread, the PCG far fewer, and more warps
+// per SM hide more of its memory latency). Part 1: elements and assembly; the PCG's delta0 goes
+// to the body's scalars.
+template <int CL, class TA, class TV>
+__device__ void team_step_assemble(Team<CL>& T, const DevBody& B, const BatchParams& P, bool bf16)
+{
+	typedef typename std::conditional<CL == 1, LdPlain, LdCG>::type LD;
+	PhaseClock pc;
+	pc.start(P.prof);
+	if (T.tid() == 0) B.sc->fault = 0;
+	const double delta0 = team_assemble<CL, TA, TV, LD>(T, B, P, bf16, 0, pc);
+	if (T.tid() == 0) B.sc->delta0 = delta0;
+}
+
+// Part 2: the PCG, the final update and the statistics.
+template <int CL, class TA, class TV>
+__device__ void team_step_solve(Team<CL>& T, const DevBody& B, const BatchParams& P, bool bf16)
+{
+	typedef typename std::conditional<CL == 1, LdPlain, LdCG>::type LD;
+	const int lane = threadIdx.x & 31;
+	PhaseClock pc;
+	pc.start(P.prof);
+	const double delta0 = __ldcg(&B.sc->delta0);
+	const SolveOut so = team_pcg<CL, TA, TV, LD>(T, B, P, bf16, delta0, pc);
 	T.sync();
-	if (T.tid() == 0)
+	double part = 0.0;
+	for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
 	{
-		Scalars* sc = B.sc;
-		sc->iter = iter;
-		sc->delta = delta;
-		sc->delta0 = delta0;
-		sc->status = status;
-		sc->min_it = min_it;
-		sc->max_it = max_it;
-		sc->newton_iter = newton_done_at;
-		sc->newton_err = err;
-		sc->done = 1;
-		if (sc->fault) sc->status = B3G_SOLVE_DEVICE_TIMEOUT;
-		sc->total_iters += iters_all;
-		sc->total_steps += 1ull;
+		const int i = sl * kSlice + lane;
+		if (i < B.n) part += final_vertex<TV, LD>(B, i, P.h, true, true);
 	}
+	const double err = T.reduce(part);
+	pc.tick(kPhFinal);
+	team_finish<CL, TV, LD>(T, B, P, so, delta0, 1, so.iter, so.iter, (unsigned long long)so.iter, err, pc);
 }
 
 __device__ void load_body(DevBody* dst, const DevBody* src)
@@ -440,11 +528,29 @@ __device__ void load_body(DevBody* dst, const DevBody* src)
 	for (int k = threadIdx.x; k < words; k += blockDim.x) d[k] = __ldcg(s + k);
 }
 
-template <int CL, class TA, class TV>
-__global__ void __launch_bounds__(kPThreads, B3G_BATCH_MIN_BLOCKS) k_batch(BatchParams P, int bf16)
+#ifndef B3G_SOLVE_MIN_BLOCKS
+#define B3G_SOLVE_MIN_BLOCKS 4   // resident CTAs per SM of the PCG launch (64 registers a thread)
+#endif
+
+// Launch phases: the whole step (any number of Newton iterations), or the two parts of a
+// single-Newton step. Each part takes its work from its own pair of counters.
+enum { kPhaseWhole = 0, kPhaseAssemble = 1, kPhaseSolve = 2 };
+
+template <int CL, class TA, class TV, int PH>
+__device__ __forceinline__ void team_run(Team<CL>& T, const DevBody& B, const BatchParams& P, bool bf16)
+{
+	if (PH == kPhaseWhole) team_step<CL, TA, TV>(T, B, P, bf16);
+	else if (PH == kPhaseAssemble) team_step_assemble<CL, TA, TV>(T, B, P, bf16);
+	else team_step_solve<CL, TA, TV>(T, B, P, bf16);
+}
+
+template <int CL, class TA, class TV, int PH>
+__global__ void __launch_bounds__(kPThreads, PH == kPhaseSolve ? B3G_SOLVE_MIN_BLOCKS : B3G_BATCH_MIN_BLOCKS)
+k_batch(BatchParams P, int bf16)
 {
 	__shared__ TeamShared sh;
 	__shared__ __align__(16) DevBody sb;
+	unsigned* queue = P.queue + (PH == kPhaseSolve ? 2 : 0);
 
 	if (CL > 1)
 	{
@@ -455,14 +561,14 @@ __global__ void __launch_bounds__(kPThreads, B3G_BATCH_MIN_BLOCKS) k_batch(Batch
 		T.rank = (int)cl.block_rank();
 		for (;;)
 		{
-			if (T.rank == 0 && threadIdx.x == 0) sh.item = (int)atomicAdd(P.queue, 1u);
+			if (T.rank == 0 && threadIdx.x == 0) sh.item = (int)atomicAdd(queue, 1u);
 			cl.sync();
 			const int item = *cl.map_shared_rank(&sh.item, 0);
 			cl.sync();
 			if (item >= P.nbig) break;
 			load_body(&sb, P.bodies + P.big[item]);
 			__syncthreads();
-			for (int st = 0; st < P.steps; ++st) team_step<CL, TA, TV>(T, sb, P, bf16 != 0);
+			for (int st = 0; st < P.steps; ++st) team_run<CL, TA, TV, PH>(T, sb, P, bf16 != 0);
 			cl.sync();
 		}
 	}
@@ -472,30 +578,30 @@ __global__ void __launch_bounds__(kPThreads, B3G_BATCH_MIN_BLOCKS) k_batch(Batch
 	T1.rank = 0;
 	for (;;)
 	{
-		if (threadIdx.x == 0) sh.item = (int)atomicAdd(P.queue + 1, 1u);
+		if (threadIdx.x == 0) sh.item = (int)atomicAdd(queue + 1, 1u);
 		__syncthreads();
 		const int item = sh.item;
 		__syncthreads();
 		if (item >= P.nsmall) break;
 		load_body(&sb, P.bodies + P.small[item]);
 		__syncthreads();
-		for (int st = 0; st < P.steps; ++st) team_step<1, TA, TV>(T1, sb, P, bf16 != 0);
+		for (int st = 0; st < P.steps; ++st) team_run<1, TA, TV, PH>(T1, sb, P, bf16 != 0);
 		__syncthreads();
 	}
 }
 
 // Clusters of more than 8 CTAs are a non-portable size the kernel has to opt in to.
-template <int CL, class TA, class TV>
+template <int CL, class TA, class TV, int PH>
 cudaError_t allow_cluster()
 {
 	if (CL <= 8) return cudaSuccess;
-	return cudaFuncSetAttribute(k_batch<CL, TA, TV>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+	return cudaFuncSetAttribute(k_batch<CL, TA, TV, PH>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 }
 
-template <int CL, class TA, class TV>
-cudaError_t launch_cl(const BatchParams& P, int ctas, int bf16, cudaStream_t st)
+template <int CL, class TA, class TV, int PH>
+cudaError_t launch_ph(const BatchParams& P, int ctas, int bf16, cudaStream_t st)
 {
-	cudaError_t e = allow_cluster<CL, TA, TV>();
+	cudaError_t e = allow_cluster<CL, TA, TV, PH>();
 	if (e != cudaSuccess) return e;
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3((unsigned)ctas, 1, 1);
@@ -509,7 +615,54 @@ cudaError_t launch_cl(const BatchParams& P, int ctas, int bf16, cudaStream_t st)
 	attr[0].val.clusterDim.z = 1;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
-	return cudaLaunchKernelEx(&cfg, k_batch<CL, TA, TV>, P, bf16);
+	return cudaLaunchKernelEx(&cfg, k_batch<CL, TA, TV, PH>, P, bf16);
+}
+
+template <int CL, class TA, class TV, int PH>
+int max_clusters_ph()
+{
+	if (allow_cluster<CL, TA, TV, PH>() != cudaSuccess) return 0;
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(CL * 64, 1, 1);
+	cfg.blockDim = dim3(kPThreads, 1, 1);
+	cfg.dynamicSmemBytes = 0;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeClusterDimension;
+	attr[0].val.clusterDim.x = CL;
+	attr[0].val.clusterDim.y = 1;
+	attr[0].val.clusterDim.z = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	int n = 0;
+	if (cudaOccupancyMaxActiveClusters(&n, k_batch<CL, TA, TV, PH>, &cfg) != cudaSuccess) return 0;
+	return n;
+}
+
+// Co-resident clusters of the solve launch (more CTAs per SM than the assembly launch), queried
+// once per instantiation.
+template <int CL, class TA, class TV>
+int solve_clusters()
+{
+	static std::atomic<int> cached(-1);
+	int m = cached.load(std::memory_order_relaxed);
+	if (m < 0)
+	{
+		m = max_clusters_ph<CL, TA, TV, kPhaseSolve>();
+		cached.store(m, std::memory_order_relaxed);
+	}
+	return m;
+}
+
+// One step: the whole-step kernel for several Newton iterations, else the assembly launch
+// (`ctas` CTAs) followed by the solve launch (as many CTAs as fit).
+template <int CL, class TA, class TV>
+cudaError_t launch_cl(const BatchParams& P, int ctas, int bf16, cudaStream_t st)
+{
+	if (P.newton > 1) return launch_ph<CL, TA, TV, kPhaseWhole>(P, ctas, bf16, st);
+	cudaError_t e = launch_ph<CL, TA, TV, kPhaseAssemble>(P, ctas, bf16, st);
+	if (e != cudaSuccess) return e;
+	const int m = solve_clusters<CL, TA, TV>();
+	return launch_ph<CL, TA, TV, kPhaseSolve>(P, m > 0 ? m * CL : ctas, bf16, st);
 }
 
 template <class TA, class TV>
@@ -526,24 +679,13 @@ cudaError_t launch_prec(const BatchParams& P, int cluster, int ctas, int bf16, c
 	}
 }
 
+// Co-resident clusters of the assembly (and whole-step) launch; also primes the solve launch's
+// count so that no occupancy query happens while a stream is being captured.
 template <int CL, class TA, class TV>
 int max_clusters()
 {
-	if (allow_cluster<CL, TA, TV>() != cudaSuccess) return 0;
-	cudaLaunchConfig_t cfg = {};
-	cfg.gridDim = dim3(CL * 64, 1, 1);
-	cfg.blockDim = dim3(kPThreads, 1, 1);
-	cfg.dynamicSmemBytes = 0;
-	cudaLaunchAttribute attr[1];
-	attr[0].id = cudaLaunchAttributeClusterDimension;
-	attr[0].val.clusterDim.x = CL;
-	attr[0].val.clusterDim.y = 1;
-	attr[0].val.clusterDim.z = 1;
-	cfg.attrs = attr;
-	cfg.numAttrs = 1;
-	int n = 0;
-	if (cudaOccupancyMaxActiveClusters(&n, k_batch<CL, TA, TV>, &cfg) != cudaSuccess) return 0;
-	return n;
+	solve_clusters<CL, TA, TV>();
+	return max_clusters_ph<CL, TA, TV, kPhaseAssemble>();
 }
 
 template <class TA, class TV>
