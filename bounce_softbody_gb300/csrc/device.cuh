@@ -136,6 +136,16 @@ __device__ __forceinline__ void vst(double* v, int i, const double o[3])
 	*(double2*)(v + 4 * (size_t)i + 2) = make_double2(o[2], 0.0);
 }
 
+// One vertex's term of a PCG dot product: the three products summed in the vector type (FP32
+// in the FP32 and BF16 modes, as the reference computes them), then widened, so that the sums
+// over vertices, warps and CTAs run in FP64 while the FP64 pipe (a small fraction of the FP32
+// rate on this GPU) sees one conversion and one add per vertex.
+template <class TV>
+__device__ __forceinline__ double dot3(const TV a[3], const TV b[3])
+{
+	return (double)(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
+}
+
 // ------------------------------------------------------------------ storage conversions
 template <class T> __device__ __forceinline__ float to_f(T v);
 template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
@@ -832,7 +842,7 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		const double zd[3] = {0.0, 0.0, 0.0};
 		vst(B.xd, i, zd);
 	}
-	return (double)r0 * (double)sv[0] + (double)r1 * (double)sv[1] + (double)r2 * (double)sv[2];
+	return dot3<TV>(bv, sv);
 }
 
 // Four consecutive blocks of one lane in one plane, widened to the arithmetic type.

@@ -218,8 +218,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(DevBody B, const TA* A)
 		vst((TV*)B.r, i, rr);
 		vst((TV*)B.s, i, ss);
 		vst((TV*)B.d, i, ss);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)rr[c] * (double)ss[c];
+		part += dot3<TV>(rr, ss);
 	}
 	double total;
 	if (grid_reduce(part, B.partials, &B.sc->counter, &total)) pcg_start(B.sc, total);
@@ -228,8 +227,11 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(DevBody B, const TA* A)
 // d' = s + beta d (d' = s on a solve's first iteration), q = A d' and alpha = delta / d'.q.
 // Reads the direction from B.d and writes the new one to B.d2; the host swaps the two buffers
 // every iteration.
+#ifndef B3G_SPMV_MIN_BLOCKS
+#define B3G_SPMV_MIN_BLOCKS 4   // 64 registers: 4 CTAs (32 warps) per SM hide more gather latency
+#endif
 template <class TA, class TV>
-__global__ void __launch_bounds__(kThreads) k_dir_spmv_dot(DevBody B, const TA* A)
+__global__ void __launch_bounds__(kThreads, B3G_SPMV_MIN_BLOCKS) k_dir_spmv_dot(DevBody B, const TA* A)
 {
 	if (B.sc->done) return;
 	const int lane = threadIdx.x & 31;
@@ -245,8 +247,7 @@ __global__ void __launch_bounds__(kThreads) k_dir_spmv_dot(DevBody B, const TA* 
 		spmv_row_dir<TA, TV>(A, B.col, B.nslots, base, w, lane, (const TV*)B.s, (const TV*)B.d, beta, first, o, dn);
 		vst((TV*)B.q, i, o);
 		vst((TV*)B.d2, i, dn);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)dn[c] * (double)o[c];
+		part += dot3<TV>(dn, o);
 	}
 	double total;
 	if (grid_reduce(part, B.partials, &B.sc->counter, &total))
@@ -310,8 +311,7 @@ __global__ void __launch_bounds__(kThreads) k_update(DevBody B, int bf16_mode)
 		precond_row<TV>(B, i, r, s);
 		vst((TV*)B.r, i, r);
 		vst((TV*)B.s, i, s);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)r[c] * (double)s[c];
+		part += dot3<TV>(r, s);
 	}
 	if (refresh) return;
 	double total;
@@ -352,8 +352,7 @@ __global__ void __launch_bounds__(kThreads) k_resid(DevBody B, const TA* A, int 
 		precond_row<TV>(B, i, rr, ss);
 		vst((TV*)B.r, i, rr);
 		vst((TV*)B.s, i, ss);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)rr[c] * (double)ss[c];
+		part += dot3<TV>(rr, ss);
 	}
 	double total;
 	if (grid_reduce(part, B.partials, &sc->counter, &total)) decide_after_reduction(sc, total, bf16_mode != 0, true);

@@ -166,8 +166,7 @@ __device__ __forceinline__ double update_two(const DevBody& B, TV* __restrict__ 
 		precond_row<TV, LD>(B, ii[u], nr, ss);
 		vst(r, ii[u], nr);
 		vst(s, ii[u], ss);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)nr[c] * (double)ss[c];
+		part += dot3<TV>(nr, ss);
 	}
 	return part;
 }
@@ -216,8 +215,7 @@ __device__ __forceinline__ double residual_rows(const DevBody& B, const TA* A, c
 		vst((TV*)B.r, i, rr);
 		vst((TV*)B.s, i, ss);
 		if (set_d) vst((TV*)B.d, i, ss);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)rr[c] * (double)ss[c];
+		part += dot3<TV>(rr, ss);
 	}
 	return part;
 }
@@ -237,8 +235,7 @@ __device__ __forceinline__ double spmv_dot_rows(const DevBody& B, const TA* A, c
 		spmv_row<TA, TV, LD, MatVia<LD>>(A, B.col, B.nslots, base, w, lane, d, o);
 		vst(q, i, o);
 		vld<TV, LD>(d, i, dd);
-#pragma unroll
-		for (int c = 0; c < 3; ++c) part += (double)dd[c] * (double)o[c];
+		part += dot3<TV>(dd, o);
 	}
 	return part;
 }
