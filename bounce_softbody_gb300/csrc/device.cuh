@@ -711,21 +711,53 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	}
 
 	float diag[9];
+	// Slot pipeline: the next slot's list header and its first four tetrahedron codes load while
+	// this slot's records are gathered, so a slot waits on one gather instead of three dependent
+	// loads. Contributions are added in list order, as before.
+	uint32_t st_n = __ldg(B.tet_cstart + base + lane);
+	int cnt_n = __ldg(B.tet_ccnt + base + lane);
+	uint32_t cd_n[4];
+#pragma unroll
+	for (int u = 0; u < 4; ++u) cd_n[u] = u < cnt_n ? __ldg(B.tet_clist + st_n + kSlice * u) : 0u;
 	for (int k = 0; k < w; ++k)
 	{
 		const int slot = base + k * kSlice + lane;           // contribution-list item
 		const size_t bs = block_slot((size_t)base, k, lane); // block storage
 		const int j = B.col[bs];
+		const uint32_t st = st_n;
+		const int cnt = cnt_n;
+		uint32_t cd[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) cd[u] = cd_n[u];
+		if (k + 1 < w)
+		{
+			st_n = __ldg(B.tet_cstart + slot + kSlice);
+			cnt_n = __ldg(B.tet_ccnt + slot + kSlice);
+		}
 		float a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 		{
-			// tetrahedron contributions of this slot, four in flight at a time
-			const uint32_t st = __ldg(B.tet_cstart + slot);
-			const int cnt = __ldg(B.tet_ccnt + slot);
-			int t = 0;
+			float4 ua[4], ub[4];
+#pragma unroll
+			for (int u = 0; u < 4; ++u)
+				if (u < cnt)
+				{
+					const size_t r0 = 4 * (size_t)(cd[u] >> 4);
+					ua[u] = L::ld(B.tet_rec + r0 + ((cd[u] >> 2) & 3u));
+					ub[u] = L::ld(B.tet_rec + r0 + (cd[u] & 3u));
+				}
+			if (k + 1 < w)
+			{
+#pragma unroll
+				for (int u = 0; u < 4; ++u) cd_n[u] = u < cnt_n ? __ldg(B.tet_clist + st_n + kSlice * u) : 0u;
+			}
+#pragma unroll
+			for (int u = 0; u < 4; ++u)
+				if (u < cnt) add_tet_block(a, ua[u], ub[u]);
+			// the rest of the slot's contributions, four in flight at a time
+			int t = 4;
 			for (; t + 4 <= cnt; t += 4)
 			{
 				uint32_t code[4];
-				float4 ua[4], ub[4];
 #pragma unroll
 				for (int u = 0; u < 4; ++u) code[u] = __ldg(B.tet_clist + st + kSlice * (t + u));
 #pragma unroll

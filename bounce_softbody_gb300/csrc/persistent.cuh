@@ -304,13 +304,11 @@ __device__ SolveOut team_pcg(Team<CL>& T, const DevBody& B, const BatchParams& P
 		const TV alpha = (TV)(delta / dq);
 		const bool refresh = (P.refresh > 0 && (iter % P.refresh) == 0) || pending;
 		part = 0.0;
-		for (int sl = T.warp(); sl < B.nslices; sl += 2 * T.nwarps())
+		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
 		{
 			const int i0 = sl * kSlice + lane;
-			const int sl1 = sl + T.nwarps();
-			const int i1 = sl1 * kSlice + lane;
 			if (i0 >= B.n) continue;
-			part += update_two<TV, LD>(B, py, d, r, q, s, i0, i1, sl1 < B.nslices && i1 < B.n, alpha, refresh);
+			part += update_two<TV, LD>(B, py, d, r, q, s, i0, i0, false, alpha, refresh);
 		}
 		if (refresh)
 		{
@@ -351,13 +349,11 @@ __device__ SolveOut team_pcg(Team<CL>& T, const DevBody& B, const BatchParams& P
 		// doubles the SpMV's vector gathers, which for the hundreds of bodies a launch runs at
 		// once come from DRAM rather than L2 (measured 4% slower on the 512-body batch)
 		const TV bt = (TV)beta;
-		for (int sl = T.warp(); sl < B.nslices; sl += 2 * T.nwarps())
+		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
 		{
 			const int i0 = sl * kSlice + lane;
-			const int sl1 = sl + T.nwarps();
-			const int i1 = sl1 * kSlice + lane;
 			if (i0 >= B.n) continue;
-			direction_two<TV, LD>(d, s, i0, i1, sl1 < B.nslices && i1 < B.n, bt);
+			direction_two<TV, LD>(d, s, i0, i0, false, bt);
 		}
 		T.sync();
 		pc.tick(kPhDir);
