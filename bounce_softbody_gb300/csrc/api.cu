@@ -236,8 +236,8 @@ int ensure_precision(b3g_body* b, int prec)
 	if (prec == kP64) alo = 9 * (size_t)b->d.nslots * sizeof(double);
 	if (prec == kPBF) alo = 9 * (size_t)b->d.nslots * sizeof(__nv_bfloat16);
 	bytes += align_up(alo);
-	const size_t xd = prec == kP64 ? 0 : 4 * np * sizeof(double);  // FP64 solution for refinement
-	bytes += align_up(xd);
+	const size_t xff = prec == kP64 ? 0 : 8 * np * sizeof(float);  // float-float solution for refinement
+	bytes += align_up(xff);
 	char* mem = nullptr;
 	cudaError_t e = cudaMalloc(&mem, bytes);
 	if (e != cudaSuccess) return cuda_fail(e, "allocating solver vectors");
@@ -260,7 +260,7 @@ int ensure_precision(b3g_body* b, int prec)
 	p += align_up(12 * np * vs);
 	pb.alo = alo ? p : nullptr;
 	p += align_up(alo);
-	pb.xd = xd ? (double*)p : nullptr;
+	pb.xff = xff ? (float*)p : nullptr;
 	return B3G_OK;
 }
 
@@ -277,7 +277,7 @@ DevBody dev_for(const b3g_body* b, int prec, int precond, bool refine)
 	d.py = pb.vec[6];
 	d.Minv = pb.minv;
 	d.Alo = pb.alo;
-	d.xd = refine ? pb.xd : nullptr;
+	d.xff = refine ? pb.xff : nullptr;
 	d.precond = precond;
 	return d;
 }

@@ -29,7 +29,7 @@ struct PrecBuffers
 	void* vec[7] = {};   // pb r d d2 q s py
 	void* minv = nullptr;
 	void* alo = nullptr;
-	double* xd = nullptr;  // FP64 solution (FP32 and BF16 modes)
+	float* xff = nullptr;  // float-float solution (FP32 and BF16 modes), 8 floats per vertex
 };
 
 } // namespace b3g
@@ -59,7 +59,7 @@ int cuda_fail(cudaError_t e, const char* where);
 void reset_mass(b3g_body* b);
 int upload_masses(b3g_body* b);
 int ensure_precision(b3g_body* b, int prec);
-// refine: the per-op path's iterative refinement (FP64 solution and refresh residual)
+// refine: the per-op path's iterative refinement (float-float solution and refresh residual)
 DevBody dev_for(const b3g_body* b, int prec, int precond, bool refine = false);
 int prec_of(const b3g_solver_config* c);
 int check_config(const b3g_solver_config* c);

@@ -146,6 +146,40 @@ __device__ __forceinline__ double dot3(const TV a[3], const TV b[3])
 	return (double)(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
 }
 
+// ------------------------------------------------------------------ float-float arithmetic
+// The refined PCG solution is kept as an unevaluated sum hi + lo of two floats (about 48
+// significant bits) and updated with error-free transformations: Knuth's TwoSum, and the
+// product error fma(a, b, -a*b). This runs on the FP32 pipes; this GPU's FP64 rate is a small
+// fraction of its FP32 rate.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+	// explicit round-to-nearest operations: the compiler never contracts them into FMAs, which
+	// would break the exactness of the transformation
+	s = __fadd_rn(a, b);
+	const float bb = __fsub_rn(s, a);
+	e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// (hi, lo) += p + pe, where pe is a small correction (a product's rounding error)
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float p, float pe)
+{
+	float s, e;
+	two_sum(hi, p, s, e);
+	e = __fadd_rn(e, __fadd_rn(lo, pe));
+	hi = __fadd_rn(s, e);
+	lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+__device__ __forceinline__ void ff_ld(const float* x, int i, float hi[3], float lo[3])
+{
+	const float4 h = *(const float4*)(x + 8 * (size_t)i), l = *(const float4*)(x + 8 * (size_t)i + 4);
+	hi[0] = h.x; hi[1] = h.y; hi[2] = h.z;
+	lo[0] = l.x; lo[1] = l.y; lo[2] = l.z;
+}
+__device__ __forceinline__ void ff_st(float* x, int i, const float hi[3], const float lo[3])
+{
+	*(float4*)(x + 8 * (size_t)i) = make_float4(hi[0], hi[1], hi[2], 0.0f);
+	*(float4*)(x + 8 * (size_t)i + 4) = make_float4(lo[0], lo[1], lo[2], 0.0f);
+}
+
 // ------------------------------------------------------------------ storage conversions
 template <class T> __device__ __forceinline__ float to_f(T v);
 template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
@@ -869,10 +903,10 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	vst(vp<TV>(B.s), i, sv);
 	vst(vp<TV>(B.d), i, sv);
 	vst(vp<TV>(B.py), i, zero);
-	if (B.xd)
+	if (B.xff)
 	{
-		const double zd[3] = {0.0, 0.0, 0.0};
-		vst(B.xd, i, zd);
+		const float z[3] = {0.0f, 0.0f, 0.0f};
+		ff_st(B.xff, i, z, z);
 	}
 	return dot3<TV>(bv, sv);
 }
@@ -1009,12 +1043,13 @@ __device__ __forceinline__ void spmv_row(const TA* A, const int* __restrict__ co
 	out[2] = (TV)o2;
 }
 
-// (A x)_i in FP64 for the refinement residual: FP32 blocks, the FP64 solution, FP64 products
-// and sums (FP32 blocks are exact in FP64, so the only rounding is that of the FP64 arithmetic).
-__device__ __forceinline__ void spmv_row_x64(const float* A, const int* __restrict__ col, int nslots, int base, int w,
-                                             int lane, const double* x, double out[3])
+// (A x)_i in float-float for the refinement residual: FP32 blocks times the float-float
+// solution, every product split into its float value and rounding error, summed in
+// float-float. Returns hi + lo per component.
+__device__ __forceinline__ void spmv_row_ff(const float* A, const int* __restrict__ col, int nslots, int base, int w,
+                                            int lane, const float* xff, float ohi[3], float olo[3])
 {
-	double o0 = 0, o1 = 0, o2 = 0;
+	float h0 = 0, h1 = 0, h2 = 0, l0 = 0, l1 = 0, l2 = 0;
 	const size_t ns = (size_t)nslots;
 	const unsigned long long pol = evict_first_policy();
 	for (int k = 0; k < w; k += kGroup)
@@ -1024,22 +1059,36 @@ __device__ __forceinline__ void spmv_row_x64(const float* A, const int* __restri
 		float a[9][4];
 #pragma unroll
 		for (int p = 0; p < 9; ++p) mat_load4(A + p * ns + off, a[p], pol, (MatNC*)nullptr);
-		double xv[4][3];
-		vld<double, LdPlain>(x, jj.x, xv[0]);
-		vld<double, LdPlain>(x, jj.y, xv[1]);
-		vld<double, LdPlain>(x, jj.z, xv[2]);
-		vld<double, LdPlain>(x, jj.w, xv[3]);
+		const int js[4] = {jj.x, jj.y, jj.z, jj.w};
 #pragma unroll
 		for (int u = 0; u < 4; ++u)
 		{
-			o0 += (double)a[0][u] * xv[u][0] + (double)a[1][u] * xv[u][1] + (double)a[2][u] * xv[u][2];
-			o1 += (double)a[3][u] * xv[u][0] + (double)a[4][u] * xv[u][1] + (double)a[5][u] * xv[u][2];
-			o2 += (double)a[6][u] * xv[u][0] + (double)a[7][u] * xv[u][1] + (double)a[8][u] * xv[u][2];
+			float xh[3], xl[3];
+			ff_ld(xff, js[u], xh, xl);
+#pragma unroll
+			for (int c = 0; c < 3; ++c)
+			{
+				const float a0 = a[3 * 0 + c][u], a1 = a[3 * 1 + c][u], a2 = a[3 * 2 + c][u];
+				// row 0, 1, 2 of the block times component c of x_j
+				float p = __fmul_rn(a0, xh[c]);
+				ff_add(h0, l0, p, fmaf(a0, xh[c], -p) + a0 * xl[c]);
+				p = __fmul_rn(a1, xh[c]);
+				ff_add(h1, l1, p, fmaf(a1, xh[c], -p) + a1 * xl[c]);
+				p = __fmul_rn(a2, xh[c]);
+				ff_add(h2, l2, p, fmaf(a2, xh[c], -p) + a2 * xl[c]);
+			}
 		}
 	}
-	out[0] = o0;
-	out[1] = o1;
-	out[2] = o2;
+	ohi[0] = h0; ohi[1] = h1; ohi[2] = h2;
+	olo[0] = l0; olo[1] = l1; olo[2] = l2;
+}
+
+// b - (hi + lo), rounded once to float
+__device__ __forceinline__ float ff_residual(float b, float hi, float lo)
+{
+	float t, e;
+	two_sum(b, -hi, t, e);
+	return __fadd_rn(t, __fsub_rn(e, lo));
 }
 
 // The SpMV of a PCG iteration with the direction update folded in: q_i = (A d')_i with
@@ -1183,11 +1232,11 @@ template <class TV, class L = LdPlain>
 __device__ __forceinline__ double final_vertex(const DevBody& B, int i, float h, bool first_newton, bool finish)
 {
 	float3 dv;
-	if (B.xd)
+	if (B.xff)
 	{
-		double yd[3];
-		vld<double, L>(B.xd, i, yd);
-		dv = f3((float)yd[0], (float)yd[1], (float)yd[2]);
+		float yh[3], yl[3];
+		ff_ld(B.xff, i, yh, yl);
+		dv = f3(yh[0] + yl[0], yh[1] + yl[1], yh[2] + yl[2]);
 	}
 	else
 	{

@@ -156,9 +156,9 @@ struct DevBody
 	void* q;
 	void* s;
 	void* py;
-	double* xd;                 // FP64 copy of the solution for iterative refinement (per-op path,
-	                            // FP32 and BF16 modes): x accumulates here and the true-residual
-	                            // refresh computes b - A x in FP64 from it; null = x lives in py
+	float* xff;                 // float-float solution for iterative refinement (per-op path, FP32
+	                            // and BF16 modes): 8 floats per vertex, (hi x, y, z, 0) then
+	                            // (lo x, y, z, 0); null = the solution is py
 
 	float gravity[3];
 

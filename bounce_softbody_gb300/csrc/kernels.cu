@@ -200,12 +200,13 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(DevBody B, const TA* A)
 		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 		TV b[3], rr[3], ss[3];
 		vld<TV, LdPlain>((const TV*)B.pb, i, b);
-		if (B.xd)
+		if (B.xff)
 		{
-			double q[3];
-			spmv_row_x64(B.A32, B.col, B.nslots, base, w, lane, B.xd, q);
+			// refinement: b - A x from the float-float solution in float-float, rounded once
+			float qh[3], ql[3];
+			spmv_row_ff(B.A32, B.col, B.nslots, base, w, lane, B.xff, qh, ql);
 #pragma unroll
-			for (int c = 0; c < 3; ++c) rr[c] = (TV)((double)b[c] - q[c]);
+			for (int c = 0; c < 3; ++c) rr[c] = (TV)ff_residual((float)b[c], qh[c], ql[c]);
 		}
 		else
 		{
@@ -277,7 +278,6 @@ __global__ void __launch_bounds__(kThreads) k_update(DevBody B, int bf16_mode)
 	if (sc->done) return;
 	const bool refresh = refresh_now(sc);
 	const TV alpha = (TV)sc->alpha;
-	const double alpha_d = sc->alpha;
 	double part = 0.0;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
 	{
@@ -288,14 +288,19 @@ __global__ void __launch_bounds__(kThreads) k_update(DevBody B, int bf16_mode)
 			vld<TV, LdPlain>((const TV*)B.r, i, r);
 			vld<TV, LdPlain>((const TV*)B.q, i, q);
 		}
-		if (B.xd)
+		if (B.xff)
 		{
-			// refinement: the solution accumulates in FP64
-			double x[3];
-			vld<double, LdPlain>(B.xd, i, x);
+			// refinement: the solution accumulates in float-float (the product alpha d and its
+			// rounding error are both added)
+			float xh[3], xl[3];
+			ff_ld(B.xff, i, xh, xl);
 #pragma unroll
-			for (int c = 0; c < 3; ++c) x[c] += alpha_d * (double)d[c];
-			vst(B.xd, i, x);
+			for (int c = 0; c < 3; ++c)
+			{
+				const float p = __fmul_rn((float)alpha, (float)d[c]);
+				ff_add(xh[c], xl[c], p, fmaf((float)alpha, (float)d[c], -p));
+			}
+			ff_st(B.xff, i, xh, xl);
 		}
 		else
 		{
@@ -334,13 +339,13 @@ __global__ void __launch_bounds__(kThreads) k_resid(DevBody B, const TA* A, int 
 		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 		TV b[3], rr[3], ss[3];
 		vld<TV, LdPlain>((const TV*)B.pb, i, b);
-		if (B.xd)
+		if (B.xff)
 		{
-			// refinement: b - A x from the FP64 solution with FP64 sums, rounded once
-			double q[3];
-			spmv_row_x64(B.A32, B.col, B.nslots, base, w, lane, B.xd, q);
+			// refinement: b - A x from the float-float solution in float-float, rounded once
+			float qh[3], ql[3];
+			spmv_row_ff(B.A32, B.col, B.nslots, base, w, lane, B.xff, qh, ql);
 #pragma unroll
-			for (int c = 0; c < 3; ++c) rr[c] = (TV)((double)b[c] - q[c]);
+			for (int c = 0; c < 3; ++c) rr[c] = (TV)ff_residual((float)b[c], qh[c], ql[c]);
 		}
 		else
 		{
