@@ -36,6 +36,9 @@ METRIC = "vertex-steps/s batched vs plain at resid 1e-5; p50/p99 step latency"
 DT = 1.0 / 60.0
 PCG_TOL = 1e-5
 PCG_MAX = 200
+# DRAM traffic / algorithmic bytes of the batch PCG launch, from the ncu capture of the
+# 128-body case (profiles/k_batch_batch512.md)
+PCG_TRAFFIC_RATIO = 1.03
 
 
 def parse():
@@ -48,6 +51,8 @@ def parse():
     p.add_argument("--bodies", type=int, default=512)
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "bf16"])
     p.add_argument("--no-extras", action="store_true", help="skip e2e, plain path and CPU baseline")
+    p.add_argument("--path", default="plain", choices=["plain", "batch"],
+                   help="single-body workloads: the per-op kernels (plain) or the persistent kernel with one body")
     # serving (--workload serve): Poisson arrivals over a pool of bodies
     p.add_argument("--serve-rate", type=float, default=2000.0, help="requests per second")
     p.add_argument("--serve-seconds", type=float, default=10.0, help="length of the arrival stream")
@@ -152,6 +157,12 @@ def iteration_bytes(info, vs=4, bs=36):
     """One PCG iteration: SpMV + (x, r, d, q, Minv read; x, r, s written) + (s, d read; d written)."""
     n = info["vertices"]
     return spmv_bytes(info, vs, bs) + 8 * 3 * vs * n + 3 * 3 * vs * n
+
+
+def final_bytes(info):
+    """Final update of one step: solution read (16 B), state x, v, translation, external force
+    read and x, v, external force, translation written (12 B each)."""
+    return info["vertices"] * (16 + 4 * 12 + 4 * 12)
 
 
 def assembly_bytes(info):
@@ -275,9 +286,10 @@ def ours(args, world, rank, local, pg):
     stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
 
     single = args.workload != "batch"
+    per_op = single and args.path == "plain"
 
     def step_once():
-        if single:
+        if per_op:
             # one body: the per-op kernels of the single-body path (grid-wide SpMV / reductions)
             bodies[0].step(dt, scfg, stats=False)
         else:
@@ -306,19 +318,45 @@ def ours(args, world, rank, local, pg):
     t_max = max_over_ranks(pg, total_ms / 1e3, local)
     value = sum_over_ranks(pg, nverts * args.steps, local) / t_max
 
-    # roofline of the batch kernel (the only kernel of a step besides a 8-byte memset)
+    # rooflines. Whole step: every kernel of the timed region. Persistent path: the PCG launch
+    # (the dominant kernel, 78 % of a step) and the assembly launch, each timed live with CUDA
+    # events around its own launch on the context's stream (b3g_batch_set_launch_timing) over
+    # extra steps run after the timed region.
     bs, vsz = {"fp32": (36, 4), "fp64": (72, 8), "bf16": (18, 4)}[args.precision]
-    alg = sum(args.steps * assembly_bytes(i) + it * iteration_bytes(i, vsz, bs) for i, it in zip(infos, iters))
+    alg_asm = sum(args.steps * assembly_bytes(i) for i in infos)
+    alg_pcg = sum(it * iteration_bytes(i, vsz, bs) + args.steps * final_bytes(i) for i, it in zip(infos, iters))
+    alg = alg_asm + alg_pcg
     achieved = alg / (total_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
-    # DRAM traffic per launch: ncu on a 128-body launch measured 1.21 x its algorithmic bytes
-    # (profiles/k_batch_batch512.md); traffic grows with the vertex-steps, so it is scaled by them
-    traffic = 1.21 * alg / args.steps if args.workload == "batch" and args.precision == "fp32" else None
+    step_roof = {"achieved": achieved, "frac": achieved / peak, "algorithmic_bytes_per_step": alg / args.steps}
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": "k_batch (persistent, one launch per step)",
-            "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_step": alg / args.steps,
+            "traffic": None, "kernel": "", "peak_source": f"{peak_kind} hbm_gbs",
+            "algorithmic_bytes_per_step": alg / args.steps,
             "pcg_iterations_per_step_mean": float(np.mean(iters)) / args.steps if iters else 0.0}
-    sched = b3g.batch_schedule(ctx) if not single else None
+    if not per_op:
+        tsteps = max(3, min(args.steps, 5))
+        b3g.batch_set_launch_timing(ctx, True)
+        b3g.batch_launch_times(ctx, reset=True)
+        before_t = [b.stats()["total_pcg_iterations"] for b in bodies]
+        b3g.step_batch(ctx, bodies, dt, tsteps, scfg, stats=False)
+        lt = b3g.batch_launch_times(ctx, reset=True)
+        b3g.batch_set_launch_timing(ctx, False)
+        its_t = [b.stats()["total_pcg_iterations"] - x for b, x in zip(bodies, before_t)]
+        pcg_b = sum(it * iteration_bytes(i, vsz, bs) + tsteps * final_bytes(i) for i, it in zip(infos, its_t)) / tsteps
+        asm_b = sum(assembly_bytes(i) for i in infos)
+        pcg_ms, asm_ms = lt["pcg_ms"] / lt["steps"], lt["assembly_ms"] / lt["steps"]
+        ach = pcg_b / (pcg_ms / 1e3) / 1e9
+        roof.update({"achieved": ach, "frac": ach / peak, "kernel": "k_batch PCG launch (PCG + final update)",
+                     "algorithmic_bytes_per_launch": pcg_b, "launch_ms": pcg_ms, "launches_timed": lt["steps"]})
+        # DRAM traffic of the PCG launch: ncu on the 128-body case measured 37.94 GB for
+        # PCG_TRAFFIC_RATIO x its algorithmic bytes; traffic grows with the work, so the ratio
+        # scales it to this launch
+        if args.precision == "fp32":
+            roof["traffic"] = PCG_TRAFFIC_RATIO * pcg_b
+        roof["assembly_launch"] = {"achieved": asm_b / (asm_ms / 1e3) / 1e9, "frac": asm_b / (asm_ms / 1e3) / 1e9 / peak,
+                                   "algorithmic_bytes_per_launch": asm_b, "launch_ms": asm_ms}
+    roof["whole_step"] = step_roof
+    sched = b3g.batch_schedule(ctx) if not per_op else None
 
     extras = {}
     if not args.no_extras and rank == 0 and not single:
@@ -360,15 +398,26 @@ def ours(args, world, rank, local, pg):
                                   "sample": f"{len(cs)} of {len(descs)} bodies ({sum(d.n for d in cs)} vertices), "
                                             f"1 step, oracle C restatement FP32, {csec:.2f} s"}
 
-    # batch: one persistent kernel per step (graph: memset node + kernel node); single body:
-    # begin + elements + assembly + 4 per PCG iteration (launched in chunks of 8) + final
-    if single:
-        chunks = [-(-int(it) // 8) * 8 for it in iters]
-        launches = int(args.steps * 4 + 4 * sum(chunks) + (args.steps if infos[0]["tris"] else 0)
-                       + (args.steps if infos[0]["springs"] else 0))
-        roof["kernel"] = "k_spmv_dot (per-op path)"
+    # persistent path: two launches per step (elements + assembly, then PCG + final update), plus
+    # a 16-byte memset of the work counters that is not a kernel. Per-op path per step: begin,
+    # one element kernel per element kind, assembly, then per PCG iteration the fused
+    # direction/SpMV/dot kernel and the update kernel (launched in chunks of 8 iterations between
+    # convergence checks), the true-residual refresh when due (every iteration in bf16 mode), and
+    # the final update.
+    if per_op:
+        i0 = infos[0]
+        per_step = 1 + (1 if i0["tets"] else 0) + (1 if i0["tris"] else 0) + (1 if i0["springs"] else 0) + 1 + 1
+        launches = per_step * args.steps
+        refresh = scfg.refresh_period
+        for it in iters:  # total over the timed steps; every step of a run takes about the same
+            per = int(it) / max(args.steps, 1)
+            launched = min(-(-int(round(per)) // 8) * 8, mx)
+            resid = launched if args.precision == "bf16" else (
+                sum(1 for j in range(launched) if refresh > 0 and j % refresh == 0))
+            launches += args.steps * (2 * launched + resid)
+        roof["kernel"] = "per-op step: k_dir_spmv_dot (70 % of the kernel time) + k_update + refresh"
     else:
-        launches = args.steps
+        launches = 2 * args.steps
     line = {"metric": METRIC, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "fp64": "f64", "bf16": "bf16+f32"}[args.precision],

@@ -107,6 +107,8 @@ SIGNATURES = {
     "b3g_step_batch_noalloc": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.c_float,
                                          C.POINTER(SolverConfig), C.c_uint32, C.POINTER(StepStats)]),
     "b3g_batch_phase_cycles": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int]),
+    "b3g_batch_set_launch_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "b3g_batch_launch_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int]),
     "b3g_batch_apply_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp]),
     "b3g_batch_get_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp, _fp]),
     "b3g_body_get_state": (C.c_int, [C.c_void_p, _fp, _fp]),
@@ -404,6 +406,17 @@ def batch_get_state(ctx: Context, bodies: Sequence[Body], x_ptr: int, v_ptr: int
     arr = (C.c_void_p * len(bodies))(*[b.handle for b in bodies])
     _check(load_library().b3g_batch_get_state(ctx.handle, arr, len(bodies), C.cast(x_ptr, _fp), C.cast(v_ptr, _fp)),
            "b3g_batch_get_state")
+
+
+def batch_set_launch_timing(ctx: Context, on: bool):
+    _check(load_library().b3g_batch_set_launch_timing(ctx.handle, 1 if on else 0), "b3g_batch_set_launch_timing")
+
+
+def batch_launch_times(ctx: Context, reset: bool = True) -> dict:
+    """Accumulated device ms of the assembly and PCG launches of timed batched steps."""
+    a = (C.c_double * 3)()
+    _check(load_library().b3g_batch_launch_times(ctx.handle, a, 1 if reset else 0), "b3g_batch_launch_times")
+    return {"assembly_ms": a[0], "pcg_ms": a[1], "steps": int(a[2])}
 
 
 PHASES = ["elements", "assembly", "spmv", "update", "direction", "final", "-", "-"]

@@ -376,6 +376,8 @@ int b3g_context_destroy(b3g_context* c)
 	cudaSetDevice(c->device);
 	cudaStreamSynchronize(c->stream);
 	destroy_batch_cache(c);
+	for (cudaEvent_t& e : c->tev)
+		if (e) cudaEventDestroy(e);
 	if (c->h_scalars) cudaFreeHost(c->h_scalars);
 	cudaStreamDestroy(c->stream);
 	delete c;

@@ -17,6 +17,12 @@ struct b3g_context
 	cudaStream_t stream = nullptr;
 	b3g::Scalars* h_scalars = nullptr;   // pinned, 1024 entries
 	BatchCache* batch = nullptr;
+	// b3g_batch_set_launch_timing: batched steps launch directly (no graph) with events around
+	// the assembly and PCG launches; device milliseconds accumulate here
+	bool launch_timing = false;
+	cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
+	double t_assembly_ms = 0.0, t_pcg_ms = 0.0;
+	unsigned long long t_steps = 0;
 };
 
 namespace b3g {

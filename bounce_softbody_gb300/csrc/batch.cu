@@ -259,6 +259,22 @@ void forget_body_in_batch_cache(b3g_context* c, b3g_body* b)
 		}
 }
 
+// each body's solver scalars through the context's pinned buffer, 1024 at a time
+static int read_batch_stats(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, b3g_step_stats* stats)
+{
+	cudaStream_t st = ctx->stream;
+	cudaError_t e = cudaSuccess;
+	for (uint32_t k0 = 0; k0 < count && e == cudaSuccess; k0 += 1024)
+	{
+		uint32_t m = std::min<uint32_t>(1024, count - k0);
+		for (uint32_t k = 0; k < m && e == cudaSuccess; ++k)
+			e = cudaMemcpyAsync(ctx->h_scalars + k, bodies[k0 + k]->d.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+		for (uint32_t k = 0; k < m && e == cudaSuccess; ++k) stats_from(ctx->h_scalars[k], stats + k0 + k);
+	}
+	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch stats");
+}
+
 extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float dt,
                               const b3g_solver_config* cfg_in, uint32_t steps, b3g_step_stats* stats)
 {
@@ -316,6 +332,32 @@ extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_
 		}
 	}
 	BatchArgs A = make_args(c, dt, 1, cfg);
+	if (ctx->launch_timing && A.newton == 1)
+	{
+		// timed steps: the two launches of each step bracketed by events, no graph
+		for (cudaEvent_t& ev : ctx->tev)
+			if (!ev && cudaEventCreate(&ev) != cudaSuccess) return cuda_fail(cudaGetLastError(), "timing events");
+		for (uint32_t s = 0; s < steps; ++s)
+		{
+			cudaError_t e = cudaEventRecord(ctx->tev[0], st);
+			A.part = 1;
+			if (e == cudaSuccess) e = op_batch(A, st);
+			if (e == cudaSuccess) e = cudaEventRecord(ctx->tev[1], st);
+			A.part = 2;
+			if (e == cudaSuccess) e = op_batch(A, st);
+			if (e == cudaSuccess) e = cudaEventRecord(ctx->tev[2], st);
+			if (e == cudaSuccess) e = cudaEventSynchronize(ctx->tev[2]);
+			if (e != cudaSuccess) return cuda_fail(e, "timed batch step");
+			float m1 = 0.0f, m2 = 0.0f;
+			cudaEventElapsedTime(&m1, ctx->tev[0], ctx->tev[1]);
+			cudaEventElapsedTime(&m2, ctx->tev[1], ctx->tev[2]);
+			ctx->t_assembly_ms += m1;
+			ctx->t_pcg_ms += m2;
+			ctx->t_steps += 1;
+		}
+		A.part = 0;
+		return stats ? read_batch_stats(ctx, bodies, count, stats) : B3G_OK;
+	}
 	const bool graph_ok = c->graph && c->g_h == dt && c->g_newton == A.newton && c->g_max_iter == A.max_iter &&
 	                      c->g_tol2 == A.tol2 && c->g_refresh == A.refresh && c->g_ntol2 == A.newton_tol2;
 	cudaError_t e = cudaSuccess;
@@ -346,18 +388,27 @@ extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_
 	}
 	for (uint32_t s = 0; s < steps && e == cudaSuccess; ++s) e = cudaGraphLaunch(c->graph, st);
 	if (e != cudaSuccess) return cuda_fail(e, "batch launch");
-	if (stats)
+	if (stats) return read_batch_stats(ctx, bodies, count, stats);
+	return B3G_OK;
+}
+
+extern "C" int b3g_batch_set_launch_timing(b3g_context* ctx, int on)
+{
+	if (!ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "null context");
+	ctx->launch_timing = on != 0;
+	return B3G_OK;
+}
+
+extern "C" int b3g_batch_launch_times(b3g_context* ctx, double out[3], int reset)
+{
+	if (!ctx || !out) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	out[0] = ctx->t_assembly_ms;
+	out[1] = ctx->t_pcg_ms;
+	out[2] = (double)ctx->t_steps;
+	if (reset)
 	{
-		// read back each body's solver scalars through the pinned buffer, 1024 at a time
-		for (uint32_t k0 = 0; k0 < count && e == cudaSuccess; k0 += 1024)
-		{
-			uint32_t m = std::min<uint32_t>(1024, count - k0);
-			for (uint32_t k = 0; k < m && e == cudaSuccess; ++k)
-				e = cudaMemcpyAsync(ctx->h_scalars + k, bodies[k0 + k]->d.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st);
-			if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-			for (uint32_t k = 0; k < m && e == cudaSuccess; ++k) stats_from(ctx->h_scalars[k], stats + k0 + k);
-		}
-		if (e != cudaSuccess) return cuda_fail(e, "batch stats");
+		ctx->t_assembly_ms = ctx->t_pcg_ms = 0.0;
+		ctx->t_steps = 0;
 	}
 	return B3G_OK;
 }

@@ -59,6 +59,7 @@ struct BatchArgs
 	int cluster;             // CTAs per cluster: 1, 2, 4 or 8
 	int ctas;                // CTAs of the launch (multiple of cluster)
 	unsigned long long* prof; // optional phase cycle counters (8 per CTA), null = off
+	int part = 0;            // single-Newton steps: 0 both launches, 1 assembly only, 2 PCG only
 };
 cudaError_t op_batch(const BatchArgs& A, cudaStream_t st);
 // Co-resident clusters of the batch kernel for this precision and cluster size (0 on error).

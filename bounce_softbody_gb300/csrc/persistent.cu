@@ -27,11 +27,15 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 	P.refresh = A.refresh;
 	P.newton_tol2 = A.newton_tol2;
 	P.prof = A.prof;
-	cudaError_t e = cudaMemsetAsync(A.queue, 0, 4 * sizeof(unsigned), st);  // two counters per launch
-	if (e != cudaSuccess) return e;
-	if (A.prec == kP64) return launch_batch_f64(P, A.cluster, A.ctas, st);
-	if (A.prec == kPBF) return launch_batch_bf16(P, A.cluster, A.ctas, st);
-	return launch_batch_f32(P, A.cluster, A.ctas, st);
+	if (A.part != 2)
+	{
+		// two counters per launch; the solve-only part reuses what the assembly part cleared
+		cudaError_t e = cudaMemsetAsync(A.queue, 0, 4 * sizeof(unsigned), st);
+		if (e != cudaSuccess) return e;
+	}
+	if (A.prec == kP64) return launch_batch_f64(P, A.cluster, A.ctas, A.part, st);
+	if (A.prec == kPBF) return launch_batch_bf16(P, A.cluster, A.ctas, A.part, st);
+	return launch_batch_f32(P, A.cluster, A.ctas, A.part, st);
 }
 
 } // namespace b3g

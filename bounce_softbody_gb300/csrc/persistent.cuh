@@ -647,27 +647,31 @@ int solve_clusters()
 }
 
 // One step: the whole-step kernel for several Newton iterations, else the assembly launch
-// (`ctas` CTAs) followed by the solve launch (as many CTAs as fit).
+// (`ctas` CTAs) followed by the solve launch (as many CTAs as fit). part 1 / 2 issues only the
+// assembly / solve launch of a single-Newton step (timed separately), 0 both.
 template <int CL, class TA, class TV>
-cudaError_t launch_cl(const BatchParams& P, int ctas, int bf16, cudaStream_t st)
+cudaError_t launch_cl(const BatchParams& P, int ctas, int bf16, int part, cudaStream_t st)
 {
 	if (P.newton > 1) return launch_ph<CL, TA, TV, kPhaseWhole>(P, ctas, bf16, st);
-	cudaError_t e = launch_ph<CL, TA, TV, kPhaseAssemble>(P, ctas, bf16, st);
-	if (e != cudaSuccess) return e;
+	if (part != 2)
+	{
+		cudaError_t e = launch_ph<CL, TA, TV, kPhaseAssemble>(P, ctas, bf16, st);
+		if (e != cudaSuccess || part == 1) return e;
+	}
 	const int m = solve_clusters<CL, TA, TV>();
 	return launch_ph<CL, TA, TV, kPhaseSolve>(P, m > 0 ? m * CL : ctas, bf16, st);
 }
 
 template <class TA, class TV>
-cudaError_t launch_prec(const BatchParams& P, int cluster, int ctas, int bf16, cudaStream_t st)
+cudaError_t launch_prec(const BatchParams& P, int cluster, int ctas, int bf16, int part, cudaStream_t st)
 {
 	switch (cluster)
 	{
-	case 1: return launch_cl<1, TA, TV>(P, ctas, bf16, st);
-	case 2: return launch_cl<2, TA, TV>(P, ctas, bf16, st);
-	case 4: return launch_cl<4, TA, TV>(P, ctas, bf16, st);
-	case 8: return launch_cl<8, TA, TV>(P, ctas, bf16, st);
-	case 16: return launch_cl<16, TA, TV>(P, ctas, bf16, st);
+	case 1: return launch_cl<1, TA, TV>(P, ctas, bf16, part, st);
+	case 2: return launch_cl<2, TA, TV>(P, ctas, bf16, part, st);
+	case 4: return launch_cl<4, TA, TV>(P, ctas, bf16, part, st);
+	case 8: return launch_cl<8, TA, TV>(P, ctas, bf16, part, st);
+	case 16: return launch_cl<16, TA, TV>(P, ctas, bf16, part, st);
 	default: return cudaErrorInvalidValue;
 	}
 }
@@ -698,9 +702,9 @@ int max_clusters_prec(int cluster)
 } // namespace
 
 // per-precision entry points (persistent_f32.cu, persistent_f64.cu, persistent_bf16.cu)
-cudaError_t launch_batch_f32(const BatchParams& P, int cluster, int ctas, cudaStream_t st);
-cudaError_t launch_batch_f64(const BatchParams& P, int cluster, int ctas, cudaStream_t st);
-cudaError_t launch_batch_bf16(const BatchParams& P, int cluster, int ctas, cudaStream_t st);
+cudaError_t launch_batch_f32(const BatchParams& P, int cluster, int ctas, int part, cudaStream_t st);
+cudaError_t launch_batch_f64(const BatchParams& P, int cluster, int ctas, int part, cudaStream_t st);
+cudaError_t launch_batch_bf16(const BatchParams& P, int cluster, int ctas, int part, cudaStream_t st);
 int max_clusters_f32(int cluster);
 int max_clusters_f64(int cluster);
 int max_clusters_bf16(int cluster);

@@ -3,9 +3,9 @@
 
 namespace b3g {
 
-cudaError_t launch_batch_bf16(const BatchParams& P, int cluster, int ctas, cudaStream_t st)
+cudaError_t launch_batch_bf16(const BatchParams& P, int cluster, int ctas, int part, cudaStream_t st)
 {
-	return launch_prec<__nv_bfloat16, float>(P, cluster, ctas, 1, st);
+	return launch_prec<__nv_bfloat16, float>(P, cluster, ctas, 1, part, st);
 }
 
 int max_clusters_bf16(int cluster) { return max_clusters_prec<__nv_bfloat16, float>(cluster); }

@@ -3,9 +3,9 @@
 
 namespace b3g {
 
-cudaError_t launch_batch_f32(const BatchParams& P, int cluster, int ctas, cudaStream_t st)
+cudaError_t launch_batch_f32(const BatchParams& P, int cluster, int ctas, int part, cudaStream_t st)
 {
-	return launch_prec<float, float>(P, cluster, ctas, 0, st);
+	return launch_prec<float, float>(P, cluster, ctas, 0, part, st);
 }
 
 int max_clusters_f32(int cluster) { return max_clusters_prec<float, float>(cluster); }

@@ -3,9 +3,9 @@
 
 namespace b3g {
 
-cudaError_t launch_batch_f64(const BatchParams& P, int cluster, int ctas, cudaStream_t st)
+cudaError_t launch_batch_f64(const BatchParams& P, int cluster, int ctas, int part, cudaStream_t st)
 {
-	return launch_prec<double, double>(P, cluster, ctas, 0, st);
+	return launch_prec<double, double>(P, cluster, ctas, 0, part, st);
 }
 
 int max_clusters_f64(int cluster) { return max_clusters_prec<double, double>(cluster); }

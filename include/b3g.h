@@ -207,6 +207,14 @@ B3G_API int b3g_batch_schedule(b3g_context* ctx, int32_t* out, uint32_t capacity
  * is set when the batch is first stepped; zeros otherwise. reset != 0 clears the counters. */
 B3G_API int b3g_batch_phase_cycles(b3g_context* ctx, uint64_t out[8], int reset);
 
+/* Launch timing of batched steps (measurement aid, no reference counterpart). While on, a
+ * single-Newton b3g_step_batch launches its two kernels (elements + assembly, then PCG + final
+ * update) directly instead of replaying its graph, records CUDA events around each and waits
+ * for them; b3g_batch_launch_times returns the accumulated device milliseconds of the assembly
+ * launches and of the PCG launches and the number of timed steps (out[0..2]). */
+B3G_API int b3g_batch_set_launch_timing(b3g_context* ctx, int on);
+B3G_API int b3g_batch_launch_times(b3g_context* ctx, double out[3], int reset);
+
 /* Host-buffer transfers for a list of bodies of one context; the host arrays are the bodies'
  * arrays concatenated in list order (3 floats per vertex). Pinned host memory makes them
  * asynchronous copies; get waits for the copies. */

@@ -96,3 +96,25 @@ def test_batch_is_deterministic(ctx, cluster_env, monkeypatch):
             b.close()
     for (x1, v1), (x2, v2) in zip(out[0], out[1]):
         assert np.array_equal(x1, x2) and np.array_equal(v1, v2)
+
+
+def test_launch_timing_mode_same_results(ctx):
+    """Timed batched steps (direct launches with events around the assembly and PCG launches)
+    compute exactly what the graph-replayed steps compute, and report positive launch times."""
+    descs = small_batch(count=8, seed=23)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    ref = [b3g.Body(ctx, d) for d in descs]
+    tim = [b3g.Body(ctx, d) for d in descs]
+    b3g.step_batch(ctx, ref, DT, 3, cfg, stats=False)
+    b3g.batch_set_launch_timing(ctx, True)
+    b3g.batch_launch_times(ctx, reset=True)
+    b3g.step_batch(ctx, tim, DT, 3, cfg, stats=False)
+    t = b3g.batch_launch_times(ctx, reset=True)
+    b3g.batch_set_launch_timing(ctx, False)
+    assert t["steps"] == 3 and t["assembly_ms"] > 0 and t["pcg_ms"] > 0
+    for a, b in zip(ref, tim):
+        xa, va = a.state()
+        xb, vb = b.state()
+        assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    for b in ref + tim:
+        b.close()
