@@ -25,6 +25,16 @@ _up = C.POINTER(C.c_uint32)
 _ip = C.POINTER(C.c_int32)
 
 
+class WorldShapeC(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32), ("radius", C.c_float), ("friction", C.c_float), ("p", C.c_float * 9),
+        ("rotation", C.c_float * 4), ("translation", C.c_float * 3), ("scale", C.c_float * 3),
+        ("vertex_count", C.c_uint32), ("vertices", _fp), ("triangle_count", C.c_uint32), ("triangles", _up),
+        ("wings", _up), ("grid", C.c_uint32 * 3), ("voxels", _fp), ("grid_lower", C.c_float * 3),
+        ("grid_upper", C.c_float * 3), ("invert", C.c_int32),
+    ]
+
+
 class BodyDescC(C.Structure):
     _fields_ = [
         ("vertex_count", C.c_uint32), ("positions", _fp), ("velocities", _fp), ("types", _ip),
@@ -39,6 +49,7 @@ class BodyDescC(C.Structure):
         ("sphere_radius", _fp), ("sphere_friction", _fp),
         ("world_sphere_count", C.c_uint32), ("world_spheres", _fp),
         ("gravity", C.c_float * 3),
+        ("world_shape_count", C.c_uint32), ("world_shapes", C.POINTER(WorldShapeC)),
     ]
 
 
@@ -269,6 +280,41 @@ def _desc_struct(desc, masses=None):
     d.world_spheres = f(desc.world_spheres)
     for k in range(3):
         d.gravity[k] = float(desc.gravity[k])
+    shapes = list(getattr(desc, "world_shapes", []) or [])
+    d.world_shape_count = len(shapes)
+    if shapes:
+        arr = (WorldShapeC * len(shapes))()
+        keep.append(arr)
+        for w, sh in zip(arr, shapes):
+            w.type = int(sh.type)
+            w.radius, w.friction = float(sh.radius), float(sh.friction)
+            p = np.zeros(9)
+            p[:len(np.ravel(sh.p))] = np.ravel(sh.p)
+            for k in range(9):
+                w.p[k] = float(p[k])
+            for k in range(4):
+                w.rotation[k] = float(sh.rotation[k])
+            for k in range(3):
+                w.translation[k] = float(sh.translation[k])
+                w.scale[k] = float(sh.scale[k])
+                w.grid_lower[k] = float(sh.grid_lower[k])
+                w.grid_upper[k] = float(sh.grid_upper[k])
+            if sh.vertices is not None:
+                w.vertex_count = int(np.asarray(sh.vertices).shape[0])
+                w.vertices = f(np.asarray(sh.vertices))
+            if sh.triangles is not None:
+                w.triangle_count = int(np.asarray(sh.triangles).shape[0])
+                w.triangles = u(np.asarray(sh.triangles))
+            if sh.wings is not None:
+                w.wings = u(np.asarray(sh.wings))
+            if sh.voxels is not None:
+                vox = np.asarray(sh.voxels)
+                w.grid[0], w.grid[1], w.grid[2] = vox.shape[2], vox.shape[1], vox.shape[0]
+                w.voxels = f(vox)
+            w.invert = 1 if sh.invert else 0
+        d.world_shapes = C.cast(arr, C.POINTER(WorldShapeC))
+    else:
+        d.world_shapes = C.cast(None, C.POINTER(WorldShapeC))
     return d, keep
 
 

@@ -1,6 +1,7 @@
 // C ABI of b3g (include/b3g.h): contexts, bodies, the single-body step (per-op kernels) and
 // state transfer. The batch entry point lives in batch.cu.
 #include "api_internal.h"
+#include "shapes.h"
 
 #include <algorithm>
 #include <cmath>
@@ -410,9 +411,13 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 		return fail(B3G_ERROR_INVALID_ARGUMENT, "triangles need tris and their five material arrays");
 	if (d->spring_count && (!d->springs || !d->spring_rest_length || !d->spring_stiffness || !d->spring_damping))
 		return fail(B3G_ERROR_INVALID_ARGUMENT, "springs need springs, rest lengths, stiffness and damping");
-	if (d->world_sphere_count > (uint32_t)kMaxWorld)
-		return fail(B3G_ERROR_UNSUPPORTED, "at most %d world spheres", kMaxWorld);
-	if (d->world_sphere_count && !d->world_spheres) return fail(B3G_ERROR_INVALID_ARGUMENT, "world_spheres is null");
+	std::vector<DevShape> shapes;
+	std::vector<float> shape_data;
+	{
+		char msg[256];
+		if (build_shapes(d, shapes, shape_data, msg, sizeof(msg)) != 0)
+			return fail(B3G_ERROR_INVALID_ARGUMENT, "%s", msg);
+	}
 	for (uint32_t i = 0; i < n; ++i)
 		if (d->types[i] < 0 || d->types[i] > 2) return fail(B3G_ERROR_INVALID_ARGUMENT, "vertex %u has type %d", i, d->types[i]);
 	if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(B3G_ERROR_CUDA, "cudaSetDevice");
@@ -424,7 +429,7 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	b->nt = d->tet_count;
 	b->ntr = d->tri_count;
 	b->ns = d->spring_count;
-	b->nw = d->sphere_radius ? d->world_sphere_count : 0;
+	b->nw = d->sphere_radius ? (uint32_t)shapes.size() : 0;
 
 	char err[256];
 	Pattern P;
@@ -495,6 +500,7 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 
 	// device arena
 	const int np = P.npad;
+	float* shape_dev = nullptr;  // mesh triangles and SDF voxels of the world shapes
 	auto carve = [&](Carver& C, DevBody& D) {
 		D.slice_ptr = C.take<int>(P.nslices + 1);
 		D.col = C.take<int>(P.nslots);
@@ -545,6 +551,8 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 		D.c_apply = C.take<uint8_t>((size_t)n * b->nw);
 		D.c_nf = C.take<float>((size_t)n * b->nw);
 		D.c_normal = C.take<float>(3 * (size_t)n * b->nw);
+		D.shapes = C.take<DevShape>(b->nw);
+		shape_dev = C.take<float>(b->nw ? shape_data.size() : 0);
 		D.sc = C.take<Scalars>(1);
 		D.partials = C.take<double>(kMaxPartials);
 		D.team_partials = C.take<double>(kMaxPartials);
@@ -576,17 +584,7 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	D.nw = (int)b->nw;
 	D.maxw = P.maxw;
 	D.contacts = b->nw > 0 ? 1 : 0;
-	for (int k = 0; k < kMaxWorld; ++k)
-	{
-		D.world[k] = make_float4(0, 0, 0, 0);
-		D.wfric[k] = 0.0f;
-	}
-	for (uint32_t k = 0; k < b->nw; ++k)
-	{
-		const float* w = d->world_spheres + 5 * k;
-		D.world[k] = make_float4(w[0], w[1], w[2], w[3]);
-		D.wfric[k] = w[4];
-	}
+	if (b->nw) bind_shape_data(shapes, shape_dev);
 	D.gravity[0] = d->gravity[0];
 	D.gravity[1] = d->gravity[1];
 	D.gravity[2] = d->gravity[2];
@@ -641,6 +639,8 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	{
 		up(D.srad, d->sphere_radius, n * sizeof(float));
 		if (d->sphere_friction) up(D.sfric, d->sphere_friction, n * sizeof(float));
+		up(D.shapes, shapes.data(), shapes.size() * sizeof(DevShape));
+		up(shape_dev, shape_data.data(), shape_data.size() * sizeof(float));
 	}
 	if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
 	free_pattern(&P);

@@ -584,32 +584,284 @@ __device__ __forceinline__ void spring_element(const DevBody& B, int s, const St
 }
 
 // ------------------------------------------------------------------ row assembly
-// sphere_shape.cpp:50-77 against one static sphere
-__device__ __forceinline__ bool sphere_collide(float4 sh, float3 x, float r1, float3& normal)
+// ------------------------------------------------------------------ world shapes
+// The closest point of each static world shape to a vertex sphere (b3Shape::Collide): the
+// manifold point on the shape's core and the normal from the shape to the sphere, or no contact.
+__device__ __forceinline__ float3 f3p(const float* p) { return f3(p[0], p[1], p[2]); }
+
+// quat.h:75-79 b3Quat::Rotate, and the rotation by the conjugate (b3MulC)
+__device__ __forceinline__ float3 qrot(const float q[4], float3 v, float sign = 1.0f)
 {
-	float radius = sh.w + r1;
-	float rr = radius * radius;
-	float3 d = x - f3(sh.x, sh.y, sh.z);
-	float dd = dot3(d, d);
-	if (dd <= rr)
-	{
-		if (dd > kFltEps * kFltEps)
-		{
-			float dist = sqrtf(dd);
-			normal = f3(d.x / dist, d.y / dist, d.z / dist);
-		}
-		else normal = f3(0.0f, 1.0f, 0.0f);
-		return true;
-	}
-	return false;
+	const float3 u = f3(sign * q[0], sign * q[1], sign * q[2]);
+	const float3 t = 2.0f * cross3(u, v);
+	return v + q[3] * t + cross3(u, t);
 }
 
-// aabb.h:371 b3TestOverlap of AABB(vertex, r) and the sphere's AABB
-__device__ __forceinline__ bool aabb_overlap(float3 p, float r, float4 sh)
+// sphere_shape.cpp:50-77
+__device__ __forceinline__ bool collide_sphere(const DevShape& S, float3 Q, float r1, float3& P, float3& n)
 {
-	if (p.x + r < sh.x - sh.w || p.x - r > sh.x + sh.w) return false;
-	if (p.y + r < sh.y - sh.w || p.y - r > sh.y + sh.w) return false;
-	if (p.z + r < sh.z - sh.w || p.z - r > sh.z + sh.w) return false;
+	const float radius = S.radius + r1;
+	const float3 c = f3p(S.a);
+	const float3 d = Q - c;
+	const float dd = dot3(d, d);
+	if (!(dd <= radius * radius)) return false;
+	P = c;
+	if (dd > kFltEps * kFltEps)
+	{
+		const float dist = sqrtf(dd);
+		n = f3(d.x / dist, d.y / dist, d.z / dist);
+	}
+	else n = f3(0.0f, 1.0f, 0.0f);
+	return true;
+}
+
+// closest point P of a feature, normal from it to Q unless Q is on it (then `fallback`)
+__device__ __forceinline__ bool point_feature(float3 Q, float3 Pf, float radius, float3 fallback, float3& P, float3& n)
+{
+	const float3 d = Q - Pf;
+	const float dd = dot3(d, d);
+	if (dd > radius * radius) return false;
+	n = fallback;
+	const float l = sqrtf(dd);
+	if (l > kFltEps) n = f3(d.x / l, d.y / l, d.z / l);
+	P = Pf;
+	return true;
+}
+
+// capsule_shape.cpp:52-136
+__device__ __forceinline__ bool collide_capsule(const DevShape& S, float3 Q, float r1, float3& P, float3& n)
+{
+	const float3 A = f3p(S.a), B = f3p(S.b);
+	const float3 AB = B - A;
+	const float u = dot3(B - Q, AB), v = dot3(Q - A, AB);
+	const float radius = S.radius + r1;
+	if (v <= 0.0f) return point_feature(Q, A, radius, f3(0.0f, 1.0f, 0.0f), P, n);
+	if (u <= 0.0f) return point_feature(Q, B, radius, f3(0.0f, 1.0f, 0.0f), P, n);
+	const float ss = dot3(AB, AB);
+	const float3 Pm = (u * A + v * B);
+	const float3 Pc = f3(Pm.x / ss, Pm.y / ss, Pm.z / ss);
+	const float3 d = Q - Pc;
+	if (dot3(d, d) > radius * radius) return false;
+	const float3 AQ = Q - A;
+	float3 nn = cross3(cross3(AB, AQ), AB);
+	if (dot3(nn, AQ) < 0.0f) nn = -nn;
+	n = normalize3(nn);
+	P = Pc;
+	return true;
+}
+
+// box_shape.cpp:63-140: planes (+-x, +-y, +-z) at the extents in the box frame
+__device__ __forceinline__ bool collide_box(const DevShape& S, float3 Q, float r1, float3& P, float3& n)
+{
+	const float3 e = f3p(S.a);
+	const float radius = S.radius + r1;
+	const float3 cl = qrot(S.q, Q - f3p(S.t), -1.0f);  // b3MulT(xf, Q)
+	const float3 normals[6] = {f3(1, 0, 0), f3(-1, 0, 0), f3(0, 1, 0), f3(0, -1, 0), f3(0, 0, 1), f3(0, 0, -1)};
+	const float offsets[6] = {e.x, e.x, e.y, e.y, e.z, e.z};
+	int face = 0;
+	float sep = -3.402823466e+38f;
+	for (int k = 0; k < 6; ++k)
+	{
+		const float sk = dot3(normals[k], cl) - offsets[k];
+		if (sk > radius) return false;
+		if (sk > sep)
+		{
+			face = k;
+			sep = sk;
+		}
+	}
+	if (sep < 0.0f)
+	{
+		// the sphere center is inside the box: the closest face
+		const float3 cb = cl - sep * normals[face];
+		P = qrot(S.q, cb) + f3p(S.t);
+		n = qrot(S.q, normals[face]);
+		return true;
+	}
+	const float3 cb = f3(fmaxf(-e.x, fminf(cl.x, e.x)), fmaxf(-e.y, fminf(cl.y, e.y)), fmaxf(-e.z, fminf(cl.z, e.z)));
+	const float3 d = cl - cb;
+	const float dd = dot3(d, d);
+	if (dd > radius * radius) return false;
+	if (!(dd > kFltEps * kFltEps)) return false;
+	const float dist = sqrtf(dd);
+	P = qrot(S.q, cb) + f3p(S.t);
+	n = qrot(S.q, f3(d.x / dist, d.y / dist, d.z / dist));
+	return true;
+}
+
+// geometry.h:27-70 b3BarycentricCoordinates of Q on segment AB (u, v, divisor) and on
+// triangle ABC (u, v, w, divisor)
+__device__ __forceinline__ void bary2(float out[3], float3 A, float3 B, float3 Q)
+{
+	const float3 AB = B - A, QA = A - Q, QB = B - Q;
+	out[0] = dot3(QB, AB);
+	out[1] = -dot3(QA, AB);
+	out[2] = dot3(AB, AB);
+}
+__device__ __forceinline__ void bary3(float out[4], float3 A, float3 B, float3 C, float3 Q)
+{
+	const float3 AB = B - A, AC = C - A, QA = A - Q, QB = B - Q, QC = C - Q;
+	const float3 ABxAC = cross3(AB, AC);
+	out[0] = dot3(cross3(QB, QC), ABxAC);
+	out[1] = dot3(cross3(QC, QA), ABxAC);
+	out[2] = dot3(cross3(QA, QB), ABxAC);
+	out[3] = dot3(ABxAC, ABxAC);
+}
+
+// triangle_shape.cpp:65-311 with optional wing vertices (mesh children)
+__device__ __forceinline__ bool collide_triangle(float3 A, float3 B, float3 C, const float3* wing, const bool* has_wing,
+                                                 float shape_radius, float3 Q, float r1, float3& P, float3& n)
+{
+	const float radius = shape_radius + r1;
+	const float3 tn = normalize3(cross3(B - A, C - A));
+	float wAB[3], wBC[3], wCA[3];
+	bary2(wAB, A, B, Q);
+	bary2(wBC, B, C, Q);
+	bary2(wCA, C, A, Q);
+	if (wAB[1] <= 0.0f && wCA[0] <= 0.0f) return point_feature(Q, A, radius, tn, P, n);
+	if (wAB[0] <= 0.0f && wBC[1] <= 0.0f) return point_feature(Q, B, radius, tn, P, n);
+	if (wBC[0] <= 0.0f && wCA[1] <= 0.0f) return point_feature(Q, C, radius, tn, P, n);
+	float wABC[4];
+	bary3(wABC, A, B, C, Q);
+	// edge regions: AB (wing 0: face wing, B, A), BC (wing 1: wing, C, B), CA (wing 2: wing, A, C)
+	const float* wedge[3] = {wAB, wBC, wCA};
+	const float3 E0[3] = {A, B, C}, E1[3] = {B, C, A};
+	const float opp[3] = {wABC[2], wABC[0], wABC[1]};
+	for (int e = 0; e < 3; ++e)
+	{
+		const float* w = wedge[e];
+		if (w[0] > 0.0f && w[1] > 0.0f && wABC[3] * opp[e] <= 0.0f)
+		{
+			const float3 Pm = w[0] * E0[e] + w[1] * E1[e];
+			const float3 Pe = f3(Pm.x / w[2], Pm.y / w[2], Pm.z / w[2]);
+			const float3 d = Q - Pe;
+			if (dot3(d, d) > radius * radius) return false;
+			if (wing && has_wing[e])
+			{
+				// is the sphere in the face region of the adjacent triangle (wing, E1, E0)?
+				float w1[4];
+				bary3(w1, wing[e], E1[e], E0[e], Q);
+				if (w1[0] > 0.0f && w1[1] > 0.0f && w1[2] > 0.0f) return false;
+			}
+			n = tn;
+			const float l = len3(d);
+			if (l > kFltEps) n = f3(d.x / l, d.y / l, d.z / l);
+			P = Pe;
+			return true;
+		}
+	}
+	// face region
+	const float3 Pm = wABC[0] * A + wABC[1] * B + wABC[2] * C;
+	const float3 Pf = f3(Pm.x / wABC[3], Pm.y / wABC[3], Pm.z / wABC[3]);
+	return point_feature(Q, Pf, radius, tn, P, n);
+}
+
+// mesh_shape.cpp:87-124: the closest child-triangle manifold among the triangles whose mesh-frame
+// AABB overlaps the sphere's query box (center in the unscaled mesh frame, radius unscaled)
+__device__ __forceinline__ bool collide_mesh(const DevShape& S, float3 Q, float r1, float3& P, float3& n)
+{
+	const float3 cl0 = qrot(S.q, Q - f3p(S.t), -1.0f);
+	const float3 c = f3(S.inv_scale[0] * cl0.x, S.inv_scale[1] * cl0.y, S.inv_scale[2] * cl0.z);
+	const float qr = r1 + S.radius;
+	float dd0 = 3.402823466e+38f;
+	bool found = false;
+	for (int k = 0; k < S.count; ++k)
+	{
+		const float* T = S.data + (size_t)kMeshTriFloats * k;
+		if (c.x + qr < T[21] || c.x - qr > T[24] || c.y + qr < T[22] || c.y - qr > T[25] || c.z + qr < T[23] ||
+		    c.z - qr > T[26])
+			continue;
+		const float3 wing[3] = {f3p(T + 9), f3p(T + 12), f3p(T + 15)};
+		const bool has[3] = {T[18] != 0.0f, T[19] != 0.0f, T[20] != 0.0f};
+		float3 Pk, nk;
+		if (!collide_triangle(f3p(T), f3p(T + 3), f3p(T + 6), wing, has, S.radius, Q, r1, Pk, nk)) continue;
+		const float3 d = Q - Pk;
+		const float dd = dot3(d, d);
+		if (dd < dd0)
+		{
+			dd0 = dd;
+			P = Pk;
+			n = nk;
+			found = true;
+		}
+	}
+	return found;
+}
+
+// voxel_grid.h:166-206 trilinear sample of the grid cell around point p (shape frame); grad
+// also returns the interpolated gradient (differences across the cell)
+__device__ __forceinline__ bool sdf_sample(const DevShape& S, float3 p, float& value, float3& grad)
+{
+	const float3 lo = f3p(S.glo), hi = f3p(S.ghi);
+	const float3 dims = f3((float)(S.dims[0] - 1), (float)(S.dims[1] - 1), (float)(S.dims[2] - 1));
+	const float3 ext = hi - lo;
+	const float3 cs = f3(ext.x / dims.x, ext.y / dims.y, ext.z / dims.z);
+	const float3 lp = p - lo;
+	const int i = (int)floorf(lp.x / cs.x), j = (int)floorf(lp.y / cs.y), k = (int)floorf(lp.z / cs.z);
+	if (i < 0 || i >= S.dims[0] - 1 || j < 0 || j >= S.dims[1] - 1 || k < 0 || k >= S.dims[2] - 1) return false;
+	// regular_grid_indexer.h: the cell AABB from its center and half size
+	const float3 half = 0.5f * cs;
+	const float3 center = lo + f3(i * cs.x, j * cs.y, k * cs.z) + half;
+	const float3 clo = center - half, chi = center + half;
+	const float3 cd = chi - clo;
+	const float3 rel = f3((p.x - clo.x) / cd.x, (p.y - clo.y) / cd.y, (p.z - clo.z) / cd.z);
+	const int W = S.dims[0], H = S.dims[1];
+	const float* V = S.data;
+	auto vox = [&](int a, int b, int c) { return V[(size_t)a + (size_t)W * ((size_t)b + (size_t)H * (size_t)c)]; };
+	const float v[8] = {vox(i, j, k),         vox(i, j, k + 1),     vox(i, j + 1, k),     vox(i, j + 1, k + 1),
+	                    vox(i + 1, j, k),     vox(i + 1, j, k + 1), vox(i + 1, j + 1, k), vox(i + 1, j + 1, k + 1)};
+	auto lerp = [](float x, float a, float b) { return (1.0f - x) * a + x * b; };
+	auto interp = [&](float x, float y, float z) {
+		x = fminf(fmaxf(x, 0.0f), 1.0f);
+		y = fminf(fmaxf(y, 0.0f), 1.0f);
+		z = fminf(fmaxf(z, 0.0f), 1.0f);
+		const float c00 = lerp(x, v[0], v[4]), c10 = lerp(x, v[2], v[6]), c01 = lerp(x, v[1], v[5]),
+		            c11 = lerp(x, v[3], v[7]);
+		return lerp(z, lerp(y, c00, c10), lerp(y, c01, c11));
+	};
+	value = interp(rel.x, rel.y, rel.z);
+	grad = f3(interp(1.0f, rel.y, rel.z) - interp(0.0f, rel.y, rel.z), interp(rel.x, 1.0f, rel.z) - interp(rel.x, 0.0f, rel.z),
+	          interp(rel.x, rel.y, 1.0f) - interp(rel.x, rel.y, 0.0f));
+	return true;
+}
+
+// sdf_shape.cpp:50-84
+__device__ __forceinline__ bool collide_sdf(const DevShape& S, float3 Q, float r1, float3& P, float3& n)
+{
+	const float3 pl = qrot(S.q, Q - f3p(S.t), -1.0f);
+	const float radius = r1 + S.radius;
+	float dist;
+	float3 g;
+	if (!sdf_sample(S, pl, dist, g)) return false;
+	if (S.invert) dist = -dist;
+	if (dist > radius) return false;
+	float3 nl = normalize3(g);
+	if (S.invert) nl = -nl;
+	n = qrot(S.q, nl);
+	P = Q - dist * n;
+	return true;
+}
+
+__device__ __forceinline__ bool world_collide(const DevShape& S, float3 Q, float r1, float3& P, float3& n)
+{
+	switch (S.type)
+	{
+	case B3G_SHAPE_SPHERE: return collide_sphere(S, Q, r1, P, n);
+	case B3G_SHAPE_CAPSULE: return collide_capsule(S, Q, r1, P, n);
+	case B3G_SHAPE_BOX: return collide_box(S, Q, r1, P, n);
+	case B3G_SHAPE_TRIANGLE: return collide_triangle(f3p(S.a), f3p(S.b), f3p(S.c), nullptr, nullptr, S.radius, Q, r1, P, n);
+	case B3G_SHAPE_MESH: return collide_mesh(S, Q, r1, P, n);
+	case B3G_SHAPE_SDF: return collide_sdf(S, Q, r1, P, n);
+	default: return false;
+	}
+}
+
+// aabb.h:371 b3TestOverlap of the vertex sphere's AABB and the world fixture's AABB
+__device__ __forceinline__ bool aabb_overlap(float3 p, float r, const DevShape& S)
+{
+	if (p.x + r < S.lo[0] || p.x - r > S.hi[0]) return false;
+	if (p.y + r < S.lo[1] || p.y - r > S.hi[1]) return false;
+	if (p.z + r < S.lo[2] || p.z - r > S.hi[2]) return false;
 	return true;
 }
 
@@ -669,7 +921,7 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		for (int k = 0; k < B.nw; ++k)
 		{
 			const int c = i * B.nw + k;
-			const float4 sh = B.world[k];
+			const DevShape& sh = B.shapes[k];
 			if (P.first_newton)
 			{
 				// contact_manager.cpp:108-146 UpdateContacts at the start of the step
@@ -684,8 +936,8 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 				}
 			}
 			if (!B.c_exists[c]) continue;
-			float3 n2;
-			if (!sphere_collide(sh, xi, r1, n2)) continue;
+			float3 p2, n2;
+			if (!world_collide(sh, xi, r1, p2, n2)) continue;
 			if (!B.c_apply[c])
 			{
 				st3(B.c_normal, c, n2);
@@ -694,7 +946,7 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 			// sphere_shape_contact.cpp:98-126
 			float3 n1 = -n2;
 			float3 c1 = xi + r1 * n1;
-			float3 c2 = f3(sh.x, sh.y, sh.z) + sh.w * n2;
+			float3 c2 = p2 + sh.radius * n2;
 			float C = len3(c2 - c1);
 			C = fminf(kBaumgarte * C, kMaxContactCorrection);
 			float3 f1 = (-kContactStiffness * C) * n1;
@@ -1187,7 +1439,7 @@ __device__ __forceinline__ void apply_friction(const DevBody& B, int i, float h,
 		t1 = normalize3(t1);
 		float3 t2 = cross3(t1, normal);
 		float im1 = B.invmass[i];
-		float fr = sqrtf(B.sfric[i] * B.wfric[k]);
+		float fr = sqrtf(B.sfric[i] * B.shapes[k].friction);
 		float tm = im1 > 0.0f ? 1.0f / im1 : 0.0f;
 		float cx = dot3(v, t1), cy = dot3(v, t2);
 		float ix = tm * -cx, iy = tm * -cy;
@@ -1216,7 +1468,7 @@ __device__ __forceinline__ void find_new_contacts(const DevBody& B, int i, float
 	{
 		const int c = i * B.nw + k;
 		if (B.c_exists[c]) continue;
-		if (aabb_overlap(x, B.srad[i], B.world[k]))
+		if (aabb_overlap(x, B.srad[i], B.shapes[k]))
 		{
 			B.c_exists[c] = 1;
 			B.c_nf[c] = 0.0f;

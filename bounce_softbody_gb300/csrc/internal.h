@@ -40,7 +40,7 @@ constexpr int kSlice = 32;
 constexpr int kGroup = 4;
 
 B3G_HD size_t block_slot(size_t base, int k, int lane) { return base + 128 * (size_t)(k >> 2) + 4 * lane + (k & 3); }
-constexpr int kMaxWorld = 4;
+constexpr int kMaxWorld = 16;   // world fixtures per body
 constexpr int kMaxTeamCtas = 16;
 
 // Device-resident solver scalars of one body; everything the PCG decides is taken here.
@@ -67,6 +67,31 @@ struct Scalars
 	unsigned long long total_iters;  // PCG iterations of every step since creation
 	unsigned long long total_steps;
 };
+
+// One static world shape (b3WorldFixture + b3Shape) on the device. Geometry is in world space
+// except where the shape keeps a frame (box, sdf: rotation q, translation t; mesh triangles are
+// stored transformed). lo / hi: the fixture's AABB as the reference computes it, for contact
+// creation and persistence.
+struct DevShape
+{
+	int type;                   // b3g_shape_type
+	float radius;               // b3Shape::m_radius
+	float friction;
+	int count;                  // mesh: triangles
+	float a[3], b[3], c[3];     // sphere: a center; capsule: a, b; triangle: a, b, c; box: a extents
+	float q[4];                 // box, sdf, mesh: rotation (x, y, z, w)
+	float t[3];                 // box, sdf, mesh: translation
+	float lo[3], hi[3];         // fixture AABB
+	float inv_scale[3];         // mesh: 1 / scale (query box in the unscaled mesh frame)
+	int dims[3];                // sdf: voxels along x, y, z
+	int invert;                 // sdf
+	float glo[3], ghi[3];       // sdf: grid AABB in the shape frame
+	const float* data;          // mesh: kMeshTriFloats per triangle; sdf: voxels
+};
+
+// Per mesh triangle: world-space vertices (9), world-space wing vertices (9), wing flags (3),
+// unscaled mesh-frame AABB lower and upper (6), pad (1)
+constexpr int kMeshTriFloats = 28;
 
 // Everything a kernel needs about one body. Passed by value to the per-op kernels and read
 // from a device array by the persistent batch kernel.
@@ -141,8 +166,7 @@ struct DevBody
 	// contacts
 	const float* srad;
 	const float* sfric;
-	float4 world[kMaxWorld];    // centre, radius
-	float wfric[kMaxWorld];
+	const struct DevShape* shapes; // nw static world shapes (device array)
 	uint8_t* c_exists;          // n * nw
 	uint8_t* c_apply;
 	float* c_nf;                // accumulated normal force

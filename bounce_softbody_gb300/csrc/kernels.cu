@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(kThreads) k_nostep(DevBody B)
 			for (int k = 0; k < B.nw; ++k)
 			{
 				const int c = i * B.nw + k;
-				if (B.c_exists[c] && (B.type[i] != B3G_DYNAMIC || !aabb_overlap(x, B.srad[i], B.world[k]))) B.c_exists[c] = 0;
+				if (B.c_exists[c] && (B.type[i] != B3G_DYNAMIC || !aabb_overlap(x, B.srad[i], B.shapes[k]))) B.c_exists[c] = 0;
 				else if (B.c_exists[c])
 				{
 					B.c_nf[c] = 0.0f;

@@ -46,6 +46,15 @@ struct HostDesc
 	std::vector<float> spr_L0, spr_ks, spr_kd;
 	std::vector<float> srad, sfric, world;
 	float gravity[3] = {0, 0, 0};
+	// world shapes; their arrays are owned by `owned`, and the pointers in `shapes` point into
+	// those arrays' heap buffers (which stay put when a HostDesc is moved)
+	struct Owned
+	{
+		std::vector<float> vertices, voxels;
+		std::vector<uint32_t> triangles, wings;
+	};
+	std::vector<b3g_world_shape> shapes;
+	std::vector<Owned> owned;
 };
 
 template <class T>
@@ -111,6 +120,27 @@ void capture(HostDesc& h, const b3g_body_desc* d)
 	}
 	copy_opt(h.world, d->world_spheres, 5 * (size_t)h.nw);
 	for (int k = 0; k < 3; ++k) h.gravity[k] = d->gravity[k];
+	h.shapes.clear();
+	h.owned.clear();
+	if (d->world_shapes)
+	{
+		h.owned.resize(d->world_shape_count);
+		for (uint32_t k = 0; k < d->world_shape_count; ++k)
+		{
+			b3g_world_shape w = d->world_shapes[k];
+			HostDesc::Owned& o = h.owned[k];
+			const size_t nvox = (size_t)w.grid[0] * w.grid[1] * w.grid[2];
+			if (w.vertices) o.vertices.assign(w.vertices, w.vertices + 3 * (size_t)w.vertex_count);
+			if (w.triangles) o.triangles.assign(w.triangles, w.triangles + 3 * (size_t)w.triangle_count);
+			if (w.wings) o.wings.assign(w.wings, w.wings + 3 * (size_t)w.triangle_count);
+			if (w.voxels) o.voxels.assign(w.voxels, w.voxels + nvox);
+			w.vertices = w.vertices ? o.vertices.data() : nullptr;
+			w.triangles = w.triangles ? o.triangles.data() : nullptr;
+			w.wings = w.wings ? o.wings.data() : nullptr;
+			w.voxels = w.voxels ? o.voxels.data() : nullptr;
+			h.shapes.push_back(w);
+		}
+	}
 }
 
 template <class T>
@@ -155,6 +185,8 @@ b3g_body_desc make_desc(const HostDesc& h)
 	d.world_sphere_count = h.nw;
 	d.world_spheres = ptr_or_null(h.world);
 	for (int k = 0; k < 3; ++k) d.gravity[k] = h.gravity[k];
+	d.world_shape_count = (uint32_t)h.shapes.size();
+	d.world_shapes = ptr_or_null(h.shapes);
 	return d;
 }
 
@@ -176,6 +208,8 @@ uint64_t estimate_bytes(const HostDesc& h)
 	b += 36 * (9 * ntr + ns) + 12 * (3 * ntr + ns);                                     // explicit blocks
 	b += nw * n * 18 + (nw ? 8 * n : 0);                                                // contacts
 	b += 160 * npad;                                                                    // FP32 solver vectors
+	for (const b3g_world_shape& w : h.shapes)                                           // mesh triangles, voxels
+		b += 4.0 * kMeshTriFloats * w.triangle_count + 4.0 * w.grid[0] * w.grid[1] * w.grid[2];
 	return (uint64_t)(1.15 * b) + (64u << 10);
 }
 

@@ -23,6 +23,52 @@ import numpy as np
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2  # b3ParticleType (include/bounce_softbody/dynamics/particle.h:31-36)
 
 
+SHAPE_SPHERE, SHAPE_CAPSULE, SHAPE_BOX, SHAPE_TRIANGLE, SHAPE_MESH, SHAPE_SDF = range(6)
+NULL_VERTEX = 0xFFFFFFFF
+
+
+@dataclasses.dataclass
+class WorldShape:
+    """A static world fixture's shape (b3g_world_shape). `p` per type: sphere center; capsule
+    center1, center2; box half extents; triangle vertex1..3. Box, mesh and SDF carry a transform
+    (rotation quaternion x, y, z, w and translation); a mesh its vertices, triangles, optional
+    wing vertices (NULL_VERTEX = open edge) and scale; an SDF its voxel grid (grid[0] fastest),
+    grid AABB in the shape frame and the invert flag."""
+    type: int
+    radius: float = 0.0
+    friction: float = 0.0
+    p: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(9))
+    rotation: np.ndarray = dataclasses.field(default_factory=lambda: np.array([0.0, 0.0, 0.0, 1.0]))
+    translation: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(3))
+    scale: np.ndarray = dataclasses.field(default_factory=lambda: np.ones(3))
+    vertices: Optional[np.ndarray] = None     # (V, 3)
+    triangles: Optional[np.ndarray] = None    # (T, 3) uint32
+    wings: Optional[np.ndarray] = None        # (T, 3) uint32
+    voxels: Optional[np.ndarray] = None       # (D, H, W) signed distances
+    grid_lower: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(3))
+    grid_upper: np.ndarray = dataclasses.field(default_factory=lambda: np.ones(3))
+    invert: bool = False
+
+
+def mesh_wings(triangles: np.ndarray) -> np.ndarray:
+    """Wing vertex of every triangle edge as b3Mesh::BuildAdjacency sets it (mesh.cpp:40-94):
+    for edge (v_j, v_j+1) of triangle t the vertex opposite the shared edge of the first other
+    triangle, in index order, that holds the reversed edge; NULL_VERTEX when there is none."""
+    T = np.asarray(triangles, np.int64)
+    holders = {}  # directed edge -> triangles holding it, ascending, with the edge's position
+    for t in range(T.shape[0]):
+        for j in range(3):
+            holders.setdefault((int(T[t, j]), int(T[t, (j + 1) % 3])), []).append((t, j))
+    wings = np.full(T.shape, NULL_VERTEX, np.uint32)
+    for t in range(T.shape[0]):
+        for j in range(3):
+            for t2, j2 in holders.get((int(T[t, (j + 1) % 3]), int(T[t, j])), []):
+                if t2 != t:
+                    wings[t, j] = T[t2, (j2 + 2) % 3]
+                    break
+    return wings
+
+
 @dataclasses.dataclass
 class BodyDesc:
     x: np.ndarray                      # (n, 3) float64 positions (also the rest state)
@@ -51,6 +97,7 @@ class BodyDesc:
     world_spheres: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 5)))
     gravity: np.ndarray = dataclasses.field(default_factory=lambda: np.array([0.0, -9.8, 0.0]))
     name: str = "body"
+    world_shapes: list = dataclasses.field(default_factory=list)   # WorldShape, after the spheres
 
     @property
     def n(self) -> int:
@@ -255,3 +302,63 @@ def serving_bodies(count: int = 256, seed: int = 5) -> list[BodyDesc]:
             E_t = float(rng.uniform(25.0, 100.0))
             out.append(cloth_grid(m, E_t=E_t, name=f"serve{k}_cloth{m}"))
     return out
+
+
+def _quat_axis_angle(axis, angle):
+    axis = np.asarray(axis, np.float64)
+    axis = axis / np.linalg.norm(axis)
+    return np.array([*(np.sin(0.5 * angle) * axis), np.cos(0.5 * angle)])
+
+
+def shape_scene(kind: str, m: int = 12, height: float = 0.05) -> BodyDesc:
+    """An m x m cloth (side 0.8, contact radius 0.01, friction 0.3, two corners pinned) hanging
+    just above one static world shape of the given kind: "capsule" (horizontal, r = 0.2), "box"
+    (0.4 x 0.1 x 0.4 half extents, tilted 0.3 rad about z), "triangle" (a large tilted
+    triangle), "mesh" (a 6 x 6 bumpy height-field mesh with wing vertices, scaled and rotated)
+    or "sdf" (a 16^3 voxel grid of the signed distance to a sphere of radius 0.3). The cloth's
+    lowest vertex starts `height` above the shape's top."""
+    cloth = cloth_grid(m, side=0.8, height=0.0, contact_radius=0.01, friction=0.3, name=f"{kind}{m}")
+    cloth.world_spheres = np.zeros((0, 5))
+    fr = 0.4
+    if kind == "capsule":
+        sh = WorldShape(SHAPE_CAPSULE, radius=0.2, friction=fr, p=np.array([-0.5, 0, 0.05, 0.5, 0, -0.05, 0, 0, 0]))
+        top = 0.2
+    elif kind == "box":
+        sh = WorldShape(SHAPE_BOX, radius=0.0, friction=fr, p=np.array([0.4, 0.1, 0.4, 0, 0, 0, 0, 0, 0]),
+                        rotation=_quat_axis_angle([0, 0, 1], 0.3), translation=np.array([0.0, 0.0, 0.0]))
+        top = 0.1 * np.cos(0.3) + 0.4 * np.sin(0.3)
+    elif kind == "triangle":
+        sh = WorldShape(SHAPE_TRIANGLE, radius=0.0, friction=fr,
+                        p=np.array([-1.2, -0.05, -1.0, 1.2, 0.05, -1.0, 0.0, 0.0, 1.3]))
+        top = 0.05 * 0.4 / 1.2  # the plane's height under the cloth's highest corner
+    elif kind == "mesh":
+        g = 6
+        xs = np.linspace(-0.6, 0.6, g)
+        X, Z = np.meshgrid(xs, xs, indexing="ij")
+        Y = 0.05 * np.sin(3.0 * X) * np.cos(2.0 * Z)
+        verts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+        tris = []
+        for i in range(g - 1):
+            for j in range(g - 1):
+                a, b, c, d = i * g + j, (i + 1) * g + j, i * g + j + 1, (i + 1) * g + j + 1
+                tris += [[a, c, b], [b, c, d]]
+        tris = np.array(tris, np.uint32)
+        sh = WorldShape(SHAPE_MESH, radius=0.0, friction=fr, vertices=verts, triangles=tris, wings=mesh_wings(tris),
+                        scale=np.array([1.1, 1.0, 0.9]), rotation=_quat_axis_angle([0, 1, 0], 0.2),
+                        translation=np.array([0.0, -0.02, 0.0]))
+        top = 0.05 - 0.02
+    elif kind == "sdf":
+        n = 16
+        lo, hi = -0.5, 0.5
+        ax = np.linspace(lo, hi, n)
+        Z, Y, X = np.meshgrid(ax, ax, ax, indexing="ij")  # voxels (k, j, i): x fastest
+        vox = np.sqrt(X ** 2 + Y ** 2 + Z ** 2) - 0.3
+        sh = WorldShape(SHAPE_SDF, radius=0.0, friction=fr, voxels=vox, grid_lower=np.full(3, lo),
+                        grid_upper=np.full(3, hi), rotation=np.array([0.0, 0.0, 0.0, 1.0]))
+        top = 0.3
+    else:
+        raise ValueError(kind)
+    cloth.x = cloth.x.copy()
+    cloth.x[:, 1] = top + 0.01 + height
+    cloth.world_shapes = [sh]
+    return cloth

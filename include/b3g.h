@@ -82,6 +82,40 @@ typedef enum b3g_preconditioner
 	B3G_PRECOND_BLOCK_JACOBI = 1   /* inverse of each 3x3 diagonal block */
 } b3g_preconditioner;
 
+/* Static world shapes the body's vertex spheres collide with (b3WorldFixture with a b3Shape,
+ * include/bounce_softbody/collision/shapes/). All in world space unless noted. */
+typedef enum b3g_shape_type
+{
+	B3G_SHAPE_SPHERE = 0,     /* b3SphereShape: p[0..2] center */
+	B3G_SHAPE_CAPSULE = 1,    /* b3CapsuleShape: p[0..2] center1, p[3..5] center2 */
+	B3G_SHAPE_BOX = 2,        /* b3BoxShape: p[0..2] extents, transform */
+	B3G_SHAPE_TRIANGLE = 3,   /* b3TriangleShape: p[0..8] vertex1..3 (no wing vertices) */
+	B3G_SHAPE_MESH = 4,       /* b3MeshShape: mesh, scale, transform */
+	B3G_SHAPE_SDF = 5         /* b3SDFShape: voxel grid of signed distances, transform, invert */
+} b3g_shape_type;
+
+typedef struct b3g_world_shape
+{
+	int32_t type;             /* b3g_shape_type */
+	float radius;             /* b3Shape::m_radius */
+	float friction;           /* b3WorldFixtureDef::friction */
+	float p[9];               /* per type, see b3g_shape_type */
+	float rotation[4];        /* box, mesh, sdf: b3Transform::rotation quaternion (x, y, z, w) */
+	float translation[3];     /* box, mesh, sdf: b3Transform::translation */
+	float scale[3];           /* mesh: b3MeshShape::m_scale */
+	uint32_t vertex_count;    /* mesh: b3Mesh::vertexCount */
+	const float* vertices;    /* mesh: 3 per vertex, mesh frame */
+	uint32_t triangle_count;  /* mesh: b3Mesh::triangleCount (at most 1,048,576) */
+	const uint32_t* triangles; /* mesh: v1, v2, v3 per triangle (b3Triangle) */
+	const uint32_t* wings;    /* mesh: u1, u2, u3 per triangle, the wing vertex of edge v1v2 / v2v3 /
+	                             v3v1 or 0xFFFFFFFF (b3Mesh::BuildAdjacency); NULL = all edges open */
+	uint32_t grid[3];         /* sdf: voxels along x, y, z (b3VoxelGrid width, height, depth), >= 2 */
+	const float* voxels;      /* sdf: grid[0]*grid[1]*grid[2] signed distances, x fastest */
+	float grid_lower[3];      /* sdf: the grid's AABB in the shape frame */
+	float grid_upper[3];
+	int32_t invert;           /* sdf: b3SDFShape::m_invert */
+} b3g_world_shape;
+
 /* One body. Arrays are host memory, read once by b3g_body_create. Per-element material arrays
  * hold one value per element. Vertex ids index the arrays of this body. */
 typedef struct b3g_body_desc
@@ -120,10 +154,14 @@ typedef struct b3g_body_desc
 
 	const float* sphere_radius;    /* per-vertex b3SphereFixture radius, NULL = no contacts */
 	const float* sphere_friction;  /* per-vertex friction */
-	uint32_t world_sphere_count;   /* static b3SphereShape world fixtures (at most 4) */
+	uint32_t world_sphere_count;   /* static b3SphereShape world fixtures (shorthand, see below) */
 	const float* world_spheres;    /* 5 per shape: center x, y, z, radius, friction */
 
 	float gravity[3];              /* b3Body::SetGravity */
+
+	uint32_t world_shape_count;    /* further static world fixtures of any shape; together with the
+	                                  world spheres at most 16 fixtures, spheres first */
+	const b3g_world_shape* world_shapes;
 } b3g_body_desc;
 
 /* Solver settings of one step. b3g_solver_config_default() gives the reference's: one Newton

@@ -179,14 +179,98 @@ struct b3TetrahedronFixtureDef : public b3FixtureDef
 	b3Vec3 v1, v2, v3, v4;
 };
 
-struct b3SphereShape
+// Static world shapes (include/bounce_softbody/collision/shapes/): the same member names; the
+// geometry is read when the fixture is created.
+struct b3Quat
 {
-	b3Vec3 m_center;
+	b3Vec3 v;
+	scalar s = 1;
+	b3Quat() {}
+	b3Quat(const b3Vec3& _v, scalar _s) : v(_v), s(_s) {}
+};
+struct b3Transform
+{
+	b3Vec3 translation;
+	b3Quat rotation;
+	void SetIdentity()
+	{
+		translation = b3Vec3(0, 0, 0);
+		rotation = b3Quat();
+	}
+};
+class b3Shape
+{
+public:
+	enum Type { e_sphere = 0, e_capsule = 1, e_triangle = 2, e_box = 3, e_mesh = 4, e_sdf = 5 };
+	virtual ~b3Shape() {}
+	Type GetType() const { return m_type; }
+	Type m_type = e_sphere;
 	scalar m_radius = 0;
+};
+struct b3SphereShape : public b3Shape
+{
+	b3SphereShape() { m_type = e_sphere; }
+	b3Vec3 m_center;
+};
+struct b3CapsuleShape : public b3Shape
+{
+	b3CapsuleShape() : m_center1(0, 1, 0), m_center2(0, -1, 0) { m_type = e_capsule; }
+	b3Vec3 m_center1, m_center2;
+};
+struct b3BoxShape : public b3Shape
+{
+	b3BoxShape() { m_type = e_box; m_xf.SetIdentity(); }
+	b3Vec3 m_extents;
+	b3Transform m_xf;
+};
+struct b3TriangleShape : public b3Shape
+{
+	b3TriangleShape() { m_type = e_triangle; }
+	void Set(const b3Vec3& v1, const b3Vec3& v2, const b3Vec3& v3)
+	{
+		m_vertex1 = v1;
+		m_vertex2 = v2;
+		m_vertex3 = v3;
+	}
+	b3Vec3 m_vertex1, m_vertex2, m_vertex3;
+};
+// b3Triangle / b3Mesh (collision/geometry/mesh.h): wing vertex 0xFFFFFFFF = open edge
+struct b3Triangle
+{
+	uint32 v1, v2, v3;
+	uint32 u1 = 0xFFFFFFFFu, u2 = 0xFFFFFFFFu, u3 = 0xFFFFFFFFu;
+};
+struct b3Mesh
+{
+	uint32 vertexCount = 0;
+	b3Vec3* vertices = nullptr;
+	uint32 triangleCount = 0;
+	b3Triangle* triangles = nullptr;
+};
+struct b3MeshShape : public b3Shape
+{
+	b3MeshShape() : m_scale(1, 1, 1) { m_type = e_mesh; m_xf.SetIdentity(); }
+	const b3Mesh* m_mesh = nullptr;
+	b3Transform m_xf;
+	b3Vec3 m_scale;
+};
+// b3SDF (collision/geometry/sdf.h): a voxel grid of signed distances over an AABB, x fastest
+struct b3SDF
+{
+	uint32 width = 0, height = 0, depth = 0;
+	const scalar* voxels = nullptr;
+	b3Vec3 lowerBound, upperBound;
+};
+struct b3SDFShape : public b3Shape
+{
+	b3SDFShape() { m_type = e_sdf; m_xf.SetIdentity(); }
+	const b3SDF* m_sdf = nullptr;
+	b3Transform m_xf;
+	bool m_invert = false;
 };
 struct b3WorldFixtureDef
 {
-	const b3SphereShape* shape = nullptr;
+	const b3Shape* shape = nullptr;
 	scalar friction = 0.5f;
 };
 
@@ -328,11 +412,106 @@ public:
 	}
 	void CreateFixture(const b3WorldFixtureDef& def)
 	{
-		m_world.push_back(def.shape->m_center.x);
-		m_world.push_back(def.shape->m_center.y);
-		m_world.push_back(def.shape->m_center.z);
-		m_world.push_back(def.shape->m_radius);
-		m_world.push_back(def.friction);
+		const b3Shape* sh = def.shape;
+		if (sh->m_type == b3Shape::e_sphere)
+		{
+			const b3SphereShape* sp = static_cast<const b3SphereShape*>(sh);
+			m_world.push_back(sp->m_center.x);
+			m_world.push_back(sp->m_center.y);
+			m_world.push_back(sp->m_center.z);
+			m_world.push_back(sp->m_radius);
+			m_world.push_back(def.friction);
+			m_topologyDirty = true;
+			return;
+		}
+		b3g_world_shape w{};
+		w.radius = sh->m_radius;
+		w.friction = def.friction;
+		w.rotation[3] = 1;
+		auto set_xf = [&](const b3Transform& xf) {
+			w.rotation[0] = xf.rotation.v.x;
+			w.rotation[1] = xf.rotation.v.y;
+			w.rotation[2] = xf.rotation.v.z;
+			w.rotation[3] = xf.rotation.s;
+			w.translation[0] = xf.translation.x;
+			w.translation[1] = xf.translation.y;
+			w.translation[2] = xf.translation.z;
+		};
+		auto set_p = [&](int at, const b3Vec3& v) {
+			w.p[at] = v.x;
+			w.p[at + 1] = v.y;
+			w.p[at + 2] = v.z;
+		};
+		m_shapeData.emplace_back();
+		ShapeData& own = m_shapeData.back();
+		switch (sh->m_type)
+		{
+		case b3Shape::e_capsule:
+		{
+			const b3CapsuleShape* c = static_cast<const b3CapsuleShape*>(sh);
+			w.type = B3G_SHAPE_CAPSULE;
+			set_p(0, c->m_center1);
+			set_p(3, c->m_center2);
+			break;
+		}
+		case b3Shape::e_box:
+		{
+			const b3BoxShape* b = static_cast<const b3BoxShape*>(sh);
+			w.type = B3G_SHAPE_BOX;
+			set_p(0, b->m_extents);
+			set_xf(b->m_xf);
+			break;
+		}
+		case b3Shape::e_triangle:
+		{
+			const b3TriangleShape* t = static_cast<const b3TriangleShape*>(sh);
+			w.type = B3G_SHAPE_TRIANGLE;
+			set_p(0, t->m_vertex1);
+			set_p(3, t->m_vertex2);
+			set_p(6, t->m_vertex3);
+			break;
+		}
+		case b3Shape::e_mesh:
+		{
+			const b3MeshShape* m = static_cast<const b3MeshShape*>(sh);
+			w.type = B3G_SHAPE_MESH;
+			set_xf(m->m_xf);
+			w.scale[0] = m->m_scale.x;
+			w.scale[1] = m->m_scale.y;
+			w.scale[2] = m->m_scale.z;
+			for (uint32 v = 0; v < m->m_mesh->vertexCount; ++v) push3(own.f, m->m_mesh->vertices[v]);
+			for (uint32 t = 0; t < m->m_mesh->triangleCount; ++t)
+			{
+				const b3Triangle& T = m->m_mesh->triangles[t];
+				own.u.insert(own.u.end(), {T.v1, T.v2, T.v3});
+				own.u2.insert(own.u2.end(), {T.u1, T.u2, T.u3});
+			}
+			w.vertex_count = m->m_mesh->vertexCount;
+			w.triangle_count = m->m_mesh->triangleCount;
+			break;
+		}
+		case b3Shape::e_sdf:
+		{
+			const b3SDFShape* f = static_cast<const b3SDFShape*>(sh);
+			w.type = B3G_SHAPE_SDF;
+			set_xf(f->m_xf);
+			const b3SDF* g = f->m_sdf;
+			w.grid[0] = g->width;
+			w.grid[1] = g->height;
+			w.grid[2] = g->depth;
+			own.f.assign(g->voxels, g->voxels + (size_t)g->width * g->height * g->depth);
+			w.grid_lower[0] = g->lowerBound.x;
+			w.grid_lower[1] = g->lowerBound.y;
+			w.grid_lower[2] = g->lowerBound.z;
+			w.grid_upper[0] = g->upperBound.x;
+			w.grid_upper[1] = g->upperBound.y;
+			w.grid_upper[2] = g->upperBound.z;
+			w.invert = f->m_invert ? 1 : 0;
+			break;
+		}
+		default: break;
+		}
+		m_shapes.push_back(w);
 		m_topologyDirty = true;
 	}
 
@@ -472,6 +651,21 @@ private:
 		}
 		d.world_sphere_count = (uint32)(m_world.size() / 5);
 		d.world_spheres = m_world.data();
+		// shape arrays point into m_shapeData (kept beside m_shapes, in the same order)
+		for (size_t k = 0; k < m_shapes.size(); ++k)
+		{
+			b3g_world_shape& w = m_shapes[k];
+			ShapeData& own = m_shapeData[k];
+			if (w.type == B3G_SHAPE_MESH)
+			{
+				w.vertices = own.f.data();
+				w.triangles = own.u.data();
+				w.wings = own.u2.data();
+			}
+			if (w.type == B3G_SHAPE_SDF) w.voxels = own.f.data();
+		}
+		d.world_shape_count = (uint32)m_shapes.size();
+		d.world_shapes = m_shapes.data();
 		d.gravity[0] = m_gravity.x;
 		d.gravity[1] = m_gravity.y;
 		d.gravity[2] = m_gravity.z;
@@ -534,6 +728,13 @@ private:
 	std::vector<float> m_triRest, m_triEx, m_triEy, m_triEs, m_triNxy, m_triNyx, m_triKd, m_triDensity;
 	std::vector<float> m_sprL0, m_sprKs, m_sprKd;
 	std::vector<float> m_sphereRadius, m_sphereFriction, m_world;
+	struct ShapeData
+	{
+		std::vector<float> f;          // mesh vertices or SDF voxels
+		std::vector<uint32_t> u, u2;   // mesh triangles and wing vertices
+	};
+	std::vector<b3g_world_shape> m_shapes;
+	std::vector<ShapeData> m_shapeData;
 };
 
 inline void b3Particle::SetType(b3ParticleType type)

@@ -179,6 +179,25 @@ static void dtr(real* out, const real* A, int m, int n)
 }
 
 /* ------------------------------------------------------------------ body */
+/* A static world fixture's shape (the b3Shape types of collision/shapes/): p per type: sphere
+ * center; capsule center1, center2; box half extents; triangle vertex1..3. */
+typedef struct b3o_shape
+{
+	int32_t type; /* 0 sphere, 1 capsule, 2 box, 3 triangle, 4 mesh, 5 sdf */
+	double radius, friction;
+	double p[9];
+	double rotation[4], translation[3], scale[3];
+	uint32_t vertex_count;
+	const double* vertices;
+	uint32_t triangle_count;
+	const uint32_t* triangles;
+	const uint32_t* wings; /* null = all edges open */
+	uint32_t grid[3];
+	const double* voxels;
+	double grid_lower[3], grid_upper[3];
+	int32_t invert;
+} b3o_shape;
+
 typedef struct
 {
 	uint32_t n;
@@ -198,7 +217,29 @@ typedef struct
 	uint32_t world_sphere_count;
 	const double* world_spheres;
 	double gravity[3];
+	uint32_t world_shape_count;
+	const struct b3o_shape* world_shapes;
 } b3o_desc;
+
+/* a world shape in the restatement's precision; lo / hi is the fixture AABB */
+typedef struct oshape
+{
+	int type;
+	real radius, friction;
+	v3 a, b, c;
+	quat q;
+	v3 t;
+	v3 lo, hi;
+	v3 inv_scale;
+	int dims[3];
+	int invert;
+	v3 glo, ghi;
+	uint32_t count;
+	real* tri; /* mesh: 28 per triangle (vertices, wing vertices, wing flags, mesh-frame AABB) */
+	real* vox; /* sdf */
+} oshape;
+
+static void shape_setup(oshape* S, const b3o_shape* W);
 
 typedef struct
 {
@@ -245,8 +286,7 @@ typedef struct
 
 	real *srad, *sfric;
 	uint32_t nw;
-	v3* wc;
-	real *wr, *wf;
+	struct oshape* ws;
 	/* contacts: one slot per (vertex, world fixture), index i*nw + k */
 	uint8_t* c_exists;
 	uint8_t* c_apply;
@@ -493,16 +533,20 @@ static body_t* body_create(const b3o_desc* d)
 			B->sfric[i] = (real)d->sphere_friction[i];
 		}
 	}
-	B->nw = d->world_sphere_count;
-	B->wc = xcalloc(B->nw, sizeof(v3));
-	B->wr = xcalloc(B->nw, sizeof(real));
-	B->wf = xcalloc(B->nw, sizeof(real));
-	for (uint32_t k = 0; k < B->nw; ++k)
+	B->nw = d->world_sphere_count + d->world_shape_count;
+	B->ws = xcalloc(B->nw ? B->nw : 1, sizeof(oshape));
+	for (uint32_t k = 0; k < d->world_sphere_count; ++k)
 	{
-		B->wc[k] = D3(d->world_spheres + 5 * k);
-		B->wr[k] = (real)d->world_spheres[5 * k + 3];
-		B->wf[k] = (real)d->world_spheres[5 * k + 4];
+		b3o_shape sh;
+		memset(&sh, 0, sizeof(sh));
+		sh.type = 0;
+		memcpy(sh.p, d->world_spheres + 5 * k, 3 * sizeof(double));
+		sh.radius = d->world_spheres[5 * k + 3];
+		sh.friction = d->world_spheres[5 * k + 4];
+		sh.rotation[3] = 1;
+		shape_setup(&B->ws[k], &sh);
 	}
+	for (uint32_t k = 0; k < d->world_shape_count; ++k) shape_setup(&B->ws[d->world_sphere_count + k], d->world_shapes + k);
 	size_t nc = (size_t)n * (B->nw ? B->nw : 1);
 	B->c_exists = xcalloc(nc, 1);
 	B->c_apply = xcalloc(nc, 1);
@@ -573,9 +617,15 @@ static body_t* body_create(const b3o_desc* d)
 static void body_free(body_t* B)
 {
 	if (!B) return;
+	for (uint32_t k = 0; k < B->nw; ++k)
+	{
+		free(B->ws[k].tri);
+		free(B->ws[k].vox);
+	}
+	free(B->ws);
 	void* ptrs[] = {B->x, B->v, B->fext, B->trans, B->type, B->mass, B->invmass, B->damping, B->tet,
 	                B->tet_rest, B->invE, B->K, B->q, B->tkd, B->tri, B->tri_x, B->invS, B->K2, B->trkd,
-	                B->spr, B->L0, B->ks, B->kd, B->srad, B->sfric, B->wc, B->wr, B->wf, B->c_exists,
+	                B->spr, B->L0, B->ks, B->kd, B->srad, B->sfric, B->c_exists,
 	                B->c_apply, B->c_normalForce, B->c_normal, B->rowptr, B->col, B->tet_slot, B->tri_slot,
 	                B->spr_slot, B->diag, B->dfdx, B->dfdv, B->A, B->x0, B->v0, B->fe, B->y, B->xx, B->vv,
 	                B->fi, B->b, B->pb, B->py, B->w, B->tmp, B->r, B->d, B->qv, B->s, B->Minv, B->Mval, B->S};
@@ -778,25 +828,347 @@ static void spring_apply(body_t* B, uint32_t e)
 	}
 }
 
-/* sphere_shape.cpp:50-77 */
-static int sphere_collide(v3 center, real rshape, v3 vertex, real rsphere, v3* point, v3* normal)
+/* ------------------------------------------------------------------ world shapes */
+/* quat.h:75-79 b3Quat::Rotate; sign -1 rotates by the conjugate (b3MulC) */
+static v3 qrot(quat q, v3 v, real sign)
 {
-	real radius = rshape + rsphere;
-	real rr = radius * radius;
-	v3 dd = sub(vertex, center);
-	real d2 = dot(dd, dd);
-	if (d2 <= rr)
+	v3 u = scl(sign, q.v);
+	v3 t = scl(2, cross(u, v));
+	return add(add(v, scl(q.s, t)), cross(u, t));
+}
+static v3 vmin3(v3 a, v3 b) { return V(a.x < b.x ? a.x : b.x, a.y < b.y ? a.y : b.y, a.z < b.z ? a.z : b.z); }
+static v3 vmax3(v3 a, v3 b) { return V(a.x > b.x ? a.x : b.x, a.y > b.y ? a.y : b.y, a.z > b.z ? a.z : b.z); }
+static v3 vdiv(v3 a, real s) { return V(a.x / s, a.y / s, a.z / s); }
+static v3 P3(const double* p) { return V((real)p[0], (real)p[1], (real)p[2]); }
+static v3 xform(const oshape* S, v3 v) { return add(qrot(S->q, v, 1), S->t); }
+
+/* settings.h:70 B3_LINEAR_SLOP */
+#define B3O_LINEAR_SLOP ((real)0.005)
+#define B3O_NULL_VERTEX 0xFFFFFFFFu
+
+/* the fixture AABBs of the shapes' ComputeAABB, mesh triangles in world space with their wing
+ * vertices and mesh-frame AABBs (mesh.h:102-117), SDF voxels */
+static void shape_setup(oshape* S, const b3o_shape* W)
+{
+	memset(S, 0, sizeof(*S));
+	S->type = W->type;
+	S->radius = (real)W->radius;
+	S->friction = (real)W->friction;
+	S->a = P3(W->p);
+	S->b = P3(W->p + 3);
+	S->c = P3(W->p + 6);
+	S->q.v = P3(W->rotation);
+	S->q.s = (real)W->rotation[3];
+	S->t = P3(W->translation);
+	v3 r = V(S->radius, S->radius, S->radius);
+	v3 lo = V(0, 0, 0), hi = V(0, 0, 0);
+	switch (W->type)
 	{
-		*point = center;
-		if (d2 > B3O_EPS * B3O_EPS)
+	case 0: lo = sub(S->a, r); hi = add(S->a, r); break;                                    /* sphere_shape.cpp:42-48 */
+	case 1: lo = sub(vmin3(S->a, S->b), r); hi = add(vmax3(S->a, S->b), r); break;           /* capsule_shape.cpp:40-50 */
+	case 2:                                                                                   /* box_shape.cpp:40-61 */
+	{
+		v3 e = S->a;
+		for (int c = 0; c < 8; ++c)
 		{
-			real dist = rsqrt_(d2);
-			*normal = V(dd.x / dist, dd.y / dist, dd.z / dist);
+			v3 v = V((c & 4) ? e.x : -e.x, (c & 2) ? e.y : -e.y, (c & 1) ? e.z : -e.z);
+			v3 w = xform(S, v);
+			lo = c ? vmin3(lo, w) : w;
+			hi = c ? vmax3(hi, w) : w;
 		}
-		else *normal = V(0, 1, 0);
+		lo = sub(lo, r);
+		hi = add(hi, r);
+		break;
+	}
+	case 3: lo = sub(vmin3(S->a, vmin3(S->b, S->c)), r); hi = add(vmax3(S->a, vmax3(S->b, S->c)), r); break; /* triangle_shape.cpp:51-63 */
+	case 4:                                                                                   /* mesh_shape.cpp:46-52, 129-162 */
+	{
+		v3 sc = P3(W->scale);
+		S->inv_scale = V(1 / sc.x, 1 / sc.y, 1 / sc.z);
+		S->count = W->triangle_count;
+		S->tri = xcalloc((size_t)28 * W->triangle_count, sizeof(real));
+		for (uint32_t t = 0; t < W->triangle_count; ++t)
+		{
+			real* R = S->tri + (size_t)28 * t;
+			const uint32_t* tv = W->triangles + 3 * t;
+			v3 loc[3];
+			for (int c = 0; c < 3; ++c)
+			{
+				loc[c] = P3(W->vertices + 3 * tv[c]);
+				v3 w = xform(S, V(sc.x * loc[c].x, sc.y * loc[c].y, sc.z * loc[c].z));
+				R[3 * c] = w.x; R[3 * c + 1] = w.y; R[3 * c + 2] = w.z;
+				uint32_t u = W->wings ? W->wings[3 * t + c] : B3O_NULL_VERTEX;
+				if (u != B3O_NULL_VERTEX)
+				{
+					v3 lu = P3(W->vertices + 3 * u);
+					v3 wu = xform(S, V(sc.x * lu.x, sc.y * lu.y, sc.z * lu.z));
+					R[9 + 3 * c] = wu.x; R[10 + 3 * c] = wu.y; R[11 + 3 * c] = wu.z;
+					R[18 + c] = 1;
+				}
+			}
+			v3 tl = sub(vmin3(loc[0], vmin3(loc[1], loc[2])), V(B3O_LINEAR_SLOP, B3O_LINEAR_SLOP, B3O_LINEAR_SLOP));
+			v3 th = add(vmax3(loc[0], vmax3(loc[1], loc[2])), V(B3O_LINEAR_SLOP, B3O_LINEAR_SLOP, B3O_LINEAR_SLOP));
+			R[21] = tl.x; R[22] = tl.y; R[23] = tl.z; R[24] = th.x; R[25] = th.y; R[26] = th.z;
+		}
+		for (uint32_t v = 0; v < W->vertex_count; ++v)
+		{
+			v3 lv = P3(W->vertices + 3 * v);
+			v3 w = xform(S, V(sc.x * lv.x, sc.y * lv.y, sc.z * lv.z));
+			lo = v ? vmin3(lo, w) : w;
+			hi = v ? vmax3(hi, w) : w;
+		}
+		lo = sub(lo, r);
+		hi = add(hi, r);
+		break;
+	}
+	case 5:                                                                                   /* sdf_shape.cpp:40-46, aabb.h:321-336 */
+	{
+		for (int c = 0; c < 3; ++c) S->dims[c] = (int)W->grid[c];
+		S->invert = W->invert ? 1 : 0;
+		S->glo = P3(W->grid_lower);
+		S->ghi = P3(W->grid_upper);
+		size_t nv = (size_t)W->grid[0] * W->grid[1] * W->grid[2];
+		S->vox = xcalloc(nv, sizeof(real));
+		for (size_t k = 0; k < nv; ++k) S->vox[k] = (real)W->voxels[k];
+		v3 lc = scl((real)0.5, add(S->glo, S->ghi)), lr = scl((real)0.5, sub(S->ghi, S->glo));
+		v3 cc = xform(S, lc);
+		m33 R = qmat(S->q);
+		v3 ax = V(fabs((double)R.c[0].x), fabs((double)R.c[0].y), fabs((double)R.c[0].z));
+		v3 ay = V(fabs((double)R.c[1].x), fabs((double)R.c[1].y), fabs((double)R.c[1].z));
+		v3 az = V(fabs((double)R.c[2].x), fabs((double)R.c[2].y), fabs((double)R.c[2].z));
+		v3 rr = V(dot(lr, ax), dot(lr, ay), dot(lr, az));
+		lo = sub(sub(cc, rr), r);
+		hi = add(add(cc, rr), r);
+		break;
+	}
+	default: break;
+	}
+	S->lo = lo;
+	S->hi = hi;
+}
+
+/* the closest feature point Pf: contact if within radius; normal toward Q unless Q is on it */
+static int point_feature(v3 Q, v3 Pf, real radius, v3 fallback, v3* P, v3* n)
+{
+	v3 d = sub(Q, Pf);
+	real dd = dot(d, d);
+	if (dd > radius * radius) return 0;
+	*n = fallback;
+	real l = rsqrt_(dd);
+	if (l > B3O_EPS) *n = vdiv(d, l);
+	*P = Pf;
+	return 1;
+}
+
+/* sphere_shape.cpp:50-77 */
+static int collide_sphere(const oshape* S, v3 Q, real r1, v3* P, v3* n)
+{
+	real radius = S->radius + r1;
+	v3 d = sub(Q, S->a);
+	real dd = dot(d, d);
+	if (!(dd <= radius * radius)) return 0;
+	*P = S->a;
+	if (dd > B3O_EPS * B3O_EPS) *n = vdiv(d, rsqrt_(dd));
+	else *n = V(0, 1, 0);
+	return 1;
+}
+
+/* capsule_shape.cpp:52-136 */
+static int collide_capsule(const oshape* S, v3 Q, real r1, v3* P, v3* n)
+{
+	v3 A = S->a, B = S->b, AB = sub(B, A);
+	real u = dot(sub(B, Q), AB), v = dot(sub(Q, A), AB);
+	real radius = S->radius + r1;
+	if (v <= 0) return point_feature(Q, A, radius, V(0, 1, 0), P, n);
+	if (u <= 0) return point_feature(Q, B, radius, V(0, 1, 0), P, n);
+	real ss = dot(AB, AB);
+	v3 Pc = vdiv(add(scl(u, A), scl(v, B)), ss);
+	v3 d = sub(Q, Pc);
+	if (dot(d, d) > radius * radius) return 0;
+	v3 AQ = sub(Q, A);
+	v3 nn = cross(cross(AB, AQ), AB);
+	if (dot(nn, AQ) < 0) nn = neg(nn);
+	*n = normalize(nn);
+	*P = Pc;
+	return 1;
+}
+
+/* box_shape.cpp:63-140 */
+static int collide_box(const oshape* S, v3 Q, real r1, v3* P, v3* n)
+{
+	v3 e = S->a;
+	real radius = S->radius + r1;
+	v3 cl = qrot(S->q, sub(Q, S->t), -1);
+	v3 normals[6] = {V(1, 0, 0), V(-1, 0, 0), V(0, 1, 0), V(0, -1, 0), V(0, 0, 1), V(0, 0, -1)};
+	real offsets[6] = {e.x, e.x, e.y, e.y, e.z, e.z};
+	int face = 0;
+	real sep = -(real)3.402823466e+38;
+	for (int k = 0; k < 6; ++k)
+	{
+		real sk = dot(normals[k], cl) - offsets[k];
+		if (sk > radius) return 0;
+		if (sk > sep) { face = k; sep = sk; }
+	}
+	if (sep < 0)
+	{
+		v3 cb = sub(cl, scl(sep, normals[face]));
+		*P = xform(S, cb);
+		*n = qrot(S->q, normals[face], 1);
 		return 1;
 	}
-	return 0;
+	v3 cb = vmax3(neg(e), vmin3(cl, e));
+	v3 d = sub(cl, cb);
+	real dd = dot(d, d);
+	if (dd > radius * radius) return 0;
+	if (!(dd > B3O_EPS * B3O_EPS)) return 0;
+	*P = xform(S, cb);
+	*n = qrot(S->q, vdiv(d, rsqrt_(dd)), 1);
+	return 1;
+}
+
+/* geometry.h:27-70 b3BarycentricCoordinates */
+static void bary2(real out[3], v3 A, v3 B, v3 Q)
+{
+	v3 AB = sub(B, A), QA = sub(A, Q), QB = sub(B, Q);
+	out[0] = dot(QB, AB);
+	out[1] = -dot(QA, AB);
+	out[2] = dot(AB, AB);
+}
+static void bary3(real out[4], v3 A, v3 B, v3 C, v3 Q)
+{
+	v3 AB = sub(B, A), AC = sub(C, A), QA = sub(A, Q), QB = sub(B, Q), QC = sub(C, Q);
+	v3 ABxAC = cross(AB, AC);
+	out[0] = dot(cross(QB, QC), ABxAC);
+	out[1] = dot(cross(QC, QA), ABxAC);
+	out[2] = dot(cross(QA, QB), ABxAC);
+	out[3] = dot(ABxAC, ABxAC);
+}
+
+/* triangle_shape.cpp:65-311 with optional wing vertices (mesh children) */
+static int collide_triangle(v3 A, v3 B, v3 C, const v3* wing, const int* has, real rshape, v3 Q, real r1, v3* P, v3* n)
+{
+	real radius = rshape + r1;
+	v3 tn = normalize(cross(sub(B, A), sub(C, A)));
+	real wAB[3], wBC[3], wCA[3], wABC[4];
+	bary2(wAB, A, B, Q);
+	bary2(wBC, B, C, Q);
+	bary2(wCA, C, A, Q);
+	if (wAB[1] <= 0 && wCA[0] <= 0) return point_feature(Q, A, radius, tn, P, n);
+	if (wAB[0] <= 0 && wBC[1] <= 0) return point_feature(Q, B, radius, tn, P, n);
+	if (wBC[0] <= 0 && wCA[1] <= 0) return point_feature(Q, C, radius, tn, P, n);
+	bary3(wABC, A, B, C, Q);
+	const real* wedge[3] = {wAB, wBC, wCA};
+	v3 E0[3] = {A, B, C}, E1[3] = {B, C, A};
+	real opp[3] = {wABC[2], wABC[0], wABC[1]};
+	for (int e = 0; e < 3; ++e)
+	{
+		const real* w = wedge[e];
+		if (w[0] > 0 && w[1] > 0 && wABC[3] * opp[e] <= 0)
+		{
+			v3 Pe = vdiv(add(scl(w[0], E0[e]), scl(w[1], E1[e])), w[2]);
+			v3 d = sub(Q, Pe);
+			if (dot(d, d) > radius * radius) return 0;
+			if (wing && has[e])
+			{
+				real w1[4];
+				bary3(w1, wing[e], E1[e], E0[e], Q);
+				if (w1[0] > 0 && w1[1] > 0 && w1[2] > 0) return 0;
+			}
+			*n = tn;
+			real l = len(d);
+			if (l > B3O_EPS) *n = vdiv(d, l);
+			*P = Pe;
+			return 1;
+		}
+	}
+	v3 Pf = vdiv(add(add(scl(wABC[0], A), scl(wABC[1], B)), scl(wABC[2], C)), wABC[3]);
+	return point_feature(Q, Pf, radius, tn, P, n);
+}
+
+/* mesh_shape.cpp:87-124 */
+static int collide_mesh(const oshape* S, v3 Q, real r1, v3* P, v3* n)
+{
+	v3 cl0 = qrot(S->q, sub(Q, S->t), -1);
+	v3 c = V(S->inv_scale.x * cl0.x, S->inv_scale.y * cl0.y, S->inv_scale.z * cl0.z);
+	real qr = r1 + S->radius;
+	real dd0 = (real)3.402823466e+38;
+	int found = 0;
+	for (uint32_t k = 0; k < S->count; ++k)
+	{
+		const real* T = S->tri + (size_t)28 * k;
+		if (c.x + qr < T[21] || c.x - qr > T[24] || c.y + qr < T[22] || c.y - qr > T[25] || c.z + qr < T[23] || c.z - qr > T[26]) continue;
+		v3 wing[3] = {V(T[9], T[10], T[11]), V(T[12], T[13], T[14]), V(T[15], T[16], T[17])};
+		int has[3] = {T[18] != 0, T[19] != 0, T[20] != 0};
+		v3 Pk, nk;
+		if (!collide_triangle(V(T[0], T[1], T[2]), V(T[3], T[4], T[5]), V(T[6], T[7], T[8]), wing, has, S->radius, Q, r1, &Pk, &nk)) continue;
+		v3 d = sub(Q, Pk);
+		real dd = dot(d, d);
+		if (dd < dd0) { dd0 = dd; *P = Pk; *n = nk; found = 1; }
+	}
+	return found;
+}
+
+/* voxel_grid.h:166-206, regular_grid_indexer.h */
+static real lerp_(real x, real a, real b) { return (1 - x) * a + x * b; }
+static real interp(const real v[8], real x, real y, real z)
+{
+	x = x < 0 ? 0 : (x > 1 ? 1 : x);
+	y = y < 0 ? 0 : (y > 1 ? 1 : y);
+	z = z < 0 ? 0 : (z > 1 ? 1 : z);
+	real c00 = lerp_(x, v[0], v[4]), c10 = lerp_(x, v[2], v[6]), c01 = lerp_(x, v[1], v[5]), c11 = lerp_(x, v[3], v[7]);
+	return lerp_(z, lerp_(y, c00, c10), lerp_(y, c01, c11));
+}
+static int sdf_sample(const oshape* S, v3 p, real* value, v3* grad)
+{
+	v3 ext = sub(S->ghi, S->glo);
+	v3 cs = V(ext.x / (real)(S->dims[0] - 1), ext.y / (real)(S->dims[1] - 1), ext.z / (real)(S->dims[2] - 1));
+	v3 lp = sub(p, S->glo);
+	long i = (long)floor((double)(lp.x / cs.x)), j = (long)floor((double)(lp.y / cs.y)), k = (long)floor((double)(lp.z / cs.z));
+	if (i < 0 || i >= S->dims[0] - 1 || j < 0 || j >= S->dims[1] - 1 || k < 0 || k >= S->dims[2] - 1) return 0;
+	v3 half = vdiv(cs, 2);
+	v3 center = add(add(S->glo, V((real)i * cs.x, (real)j * cs.y, (real)k * cs.z)), half);
+	v3 clo = sub(center, half), chi = add(center, half), cd = sub(chi, clo);
+	v3 rel = V((p.x - clo.x) / cd.x, (p.y - clo.y) / cd.y, (p.z - clo.z) / cd.z);
+	size_t W = (size_t)S->dims[0], H = (size_t)S->dims[1];
+#define VOX(a, b, c) S->vox[(size_t)(a) + W * ((size_t)(b) + H * (size_t)(c))]
+	real v[8] = {VOX(i, j, k), VOX(i, j, k + 1), VOX(i, j + 1, k), VOX(i, j + 1, k + 1),
+	             VOX(i + 1, j, k), VOX(i + 1, j, k + 1), VOX(i + 1, j + 1, k), VOX(i + 1, j + 1, k + 1)};
+#undef VOX
+	*value = interp(v, rel.x, rel.y, rel.z);
+	*grad = V(interp(v, 1, rel.y, rel.z) - interp(v, 0, rel.y, rel.z), interp(v, rel.x, 1, rel.z) - interp(v, rel.x, 0, rel.z),
+	          interp(v, rel.x, rel.y, 1) - interp(v, rel.x, rel.y, 0));
+	return 1;
+}
+
+/* sdf_shape.cpp:50-84 */
+static int collide_sdf(const oshape* S, v3 Q, real r1, v3* P, v3* n)
+{
+	v3 pl = qrot(S->q, sub(Q, S->t), -1);
+	real radius = r1 + S->radius;
+	real dist;
+	v3 g;
+	if (!sdf_sample(S, pl, &dist, &g)) return 0;
+	if (S->invert) dist = -dist;
+	if (dist > radius) return 0;
+	v3 nl = normalize(g);
+	if (S->invert) nl = neg(nl);
+	*n = qrot(S->q, nl, 1);
+	*P = sub(Q, scl(dist, *n));
+	return 1;
+}
+
+static int world_collide(const oshape* S, v3 Q, real r1, v3* P, v3* n)
+{
+	switch (S->type)
+	{
+	case 0: return collide_sphere(S, Q, r1, P, n);
+	case 1: return collide_capsule(S, Q, r1, P, n);
+	case 2: return collide_box(S, Q, r1, P, n);
+	case 3: return collide_triangle(S->a, S->b, S->c, NULL, NULL, S->radius, Q, r1, P, n);
+	case 4: return collide_mesh(S, Q, r1, P, n);
+	case 5: return collide_sdf(S, Q, r1, P, n);
+	default: return 0;
+	}
 }
 
 /* sphere_shape_contact.cpp:53-143 (contact damping stiffness is 0 in settings.h) */
@@ -804,9 +1176,9 @@ static void contact_apply(body_t* B, uint32_t i, uint32_t k)
 {
 	size_t c = (size_t)i * B->nw + k;
 	v3 x1 = B->xx[i];
-	real r1 = B->srad[i], r2 = B->wr[k];
+	real r1 = B->srad[i], r2 = B->ws[k].radius;
 	v3 x2, n2;
-	if (!sphere_collide(B->wc[k], r2, x1, r1, &x2, &n2)) return;
+	if (!world_collide(&B->ws[k], x1, r1, &x2, &n2)) return;
 	if (!B->c_apply[c]) { B->c_normal[c] = n2; B->c_apply[c] = 1; }
 	v3 n1 = neg(n2);
 	v3 c1 = add(x1, scl(r1, n1));
@@ -972,12 +1344,12 @@ static uint32_t solve_be(body_t* B, real h, uint32_t maxIt, uint32_t maxSub, rea
 	return maxSubIt;
 }
 
-static int aabb_overlap_sphere(v3 p, real r, v3 c, real R)
+static int aabb_overlap_shape(v3 p, real r, const oshape* S)
 {
-	/* aabb.h:371 b3TestOverlap of AABB(p, r) and AABB(c, R) */
-	if (p.x + r < c.x - R || p.x - r > c.x + R) return 0;
-	if (p.y + r < c.y - R || p.y - r > c.y + R) return 0;
-	if (p.z + r < c.z - R || p.z - r > c.z + R) return 0;
+	/* aabb.h:371 b3TestOverlap of AABB(p, r) and the fixture's AABB */
+	if (p.x + r < S->lo.x || p.x - r > S->hi.x) return 0;
+	if (p.y + r < S->lo.y || p.y - r > S->hi.y) return 0;
+	if (p.z + r < S->lo.z || p.z - r > S->hi.z) return 0;
 	return 1;
 }
 
@@ -992,7 +1364,7 @@ static uint32_t body_step(body_t* B, real dt, uint32_t newtonIt, uint32_t maxSub
 			{
 				size_t c = (size_t)i * B->nw + k;
 				if (!B->c_exists[c]) continue;
-				if (B->type[i] != DYNAMIC || !aabb_overlap_sphere(B->x[i], B->srad[i], B->wc[k], B->wr[k]))
+				if (B->type[i] != DYNAMIC || !aabb_overlap_shape(B->x[i], B->srad[i], &B->ws[k]))
 				{
 					B->c_exists[c] = 0;
 					continue;
@@ -1040,7 +1412,7 @@ static uint32_t body_step(body_t* B, real dt, uint32_t newtonIt, uint32_t maxSub
 					v3 t2 = cross(t1, normal);
 					v3 v1 = B->v[i];
 					real im1 = B->invmass[i];
-					real fr = rsqrt_(B->sfric[i] * B->wf[k]);
+					real fr = rsqrt_(B->sfric[i] * B->ws[k].friction);
 					real tm = im1 > 0 ? (real)1 / im1 : 0;
 					v2 Cdot = V2(dot(v1, t1), dot(v1, t2));
 					v2 imp = scl2(tm, V2(-Cdot.x, -Cdot.y));
@@ -1067,7 +1439,7 @@ static uint32_t body_step(body_t* B, real dt, uint32_t newtonIt, uint32_t maxSub
 				size_t c = (size_t)i * B->nw + k;
 				if (B->c_exists[c]) continue;
 				if (B->type[i] != DYNAMIC) continue;
-				if (aabb_overlap_sphere(B->x[i], B->srad[i], B->wc[k], B->wr[k]))
+				if (aabb_overlap_shape(B->x[i], B->srad[i], &B->ws[k]))
 				{
 					B->c_exists[c] = 1;
 					B->c_normalForce[c] = 0;

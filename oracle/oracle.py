@@ -30,6 +30,17 @@ _up = C.POINTER(C.c_uint32)
 _ip = C.POINTER(C.c_int32)
 
 
+class _Shape(C.Structure):
+    """Mirror of RefShape (oracle/ref_harness.cpp) and b3o_shape (oracle/b3_oracle.c)."""
+    _fields_ = [
+        ("type", C.c_int32), ("radius", C.c_double), ("friction", C.c_double), ("p", C.c_double * 9),
+        ("rotation", C.c_double * 4), ("translation", C.c_double * 3), ("scale", C.c_double * 3),
+        ("vertex_count", C.c_uint32), ("vertices", _dp), ("triangle_count", C.c_uint32), ("triangles", _up),
+        ("wings", _up), ("grid", C.c_uint32 * 3), ("voxels", _dp), ("grid_lower", C.c_double * 3),
+        ("grid_upper", C.c_double * 3), ("invert", C.c_int32),
+    ]
+
+
 class _Desc(C.Structure):
     """Mirror of RefDesc (oracle/ref_harness.cpp) and b3o_desc (oracle/b3_oracle.c)."""
     _fields_ = [
@@ -43,6 +54,7 @@ class _Desc(C.Structure):
         ("sphere_radius", _dp), ("sphere_friction", _dp),
         ("world_sphere_count", C.c_uint32), ("world_spheres", _dp),
         ("gravity", C.c_double * 3),
+        ("world_shape_count", C.c_uint32), ("world_shapes", C.POINTER(_Shape)),
     ]
 
 
@@ -156,6 +168,41 @@ def _make_desc(body):
     desc.world_spheres = d(body.world_spheres)
     for k in range(3):
         desc.gravity[k] = float(body.gravity[k])
+    shapes = list(getattr(body, "world_shapes", []) or [])
+    desc.world_shape_count = len(shapes)
+    if shapes:
+        arr = (_Shape * len(shapes))()
+        keep.append(arr)
+        for w, sh in zip(arr, shapes):
+            w.type = int(sh.type)
+            w.radius, w.friction = float(sh.radius), float(sh.friction)
+            p = np.zeros(9)
+            p[:len(np.ravel(sh.p))] = np.ravel(sh.p)
+            for k in range(9):
+                w.p[k] = float(p[k])
+            for k in range(4):
+                w.rotation[k] = float(sh.rotation[k])
+            for k in range(3):
+                w.translation[k] = float(sh.translation[k])
+                w.scale[k] = float(sh.scale[k])
+                w.grid_lower[k] = float(sh.grid_lower[k])
+                w.grid_upper[k] = float(sh.grid_upper[k])
+            if sh.vertices is not None:
+                w.vertex_count = int(np.asarray(sh.vertices).shape[0])
+                w.vertices = d(np.asarray(sh.vertices))
+            if sh.triangles is not None:
+                w.triangle_count = int(np.asarray(sh.triangles).shape[0])
+                w.triangles = u(np.asarray(sh.triangles))
+            if sh.wings is not None:
+                w.wings = u(np.asarray(sh.wings))
+            if sh.voxels is not None:
+                vox = np.asarray(sh.voxels)
+                w.grid[0], w.grid[1], w.grid[2] = vox.shape[2], vox.shape[1], vox.shape[0]
+                w.voxels = d(vox)
+            w.invert = 1 if sh.invert else 0
+        desc.world_shapes = C.cast(arr, C.POINTER(_Shape))
+    else:
+        desc.world_shapes = C.cast(None, C.POINTER(_Shape))
     return desc, keep
 
 

@@ -22,6 +22,14 @@
 #include <bounce_softbody/sparse/dense_vec3.h>
 #include <bounce_softbody/sparse/diag_mat33.h>
 #include <bounce_softbody/sparse/sparse_mat33.h>
+#include <bounce_softbody/collision/shapes/sphere_shape.h>
+#include <bounce_softbody/collision/shapes/capsule_shape.h>
+#include <bounce_softbody/collision/shapes/box_shape.h>
+#include <bounce_softbody/collision/shapes/triangle_shape.h>
+#include <bounce_softbody/collision/shapes/mesh_shape.h>
+#include <bounce_softbody/collision/shapes/sdf_shape.h>
+#include <bounce_softbody/collision/geometry/mesh.h>
+#include <bounce_softbody/collision/geometry/sdf.h>
 
 #include <chrono>
 #include <new>
@@ -30,6 +38,25 @@
 #include <string.h>
 
 extern "C" {
+
+// A static world fixture's shape; p per type: sphere center; capsule center1, center2; box half
+// extents; triangle vertex1..3 (mirror of b3o_shape in b3_oracle.c).
+struct RefShape
+{
+	int32_t type;  // 0 sphere, 1 capsule, 2 box, 3 triangle, 4 mesh, 5 sdf
+	double radius, friction;
+	double p[9];
+	double rotation[4], translation[3], scale[3];
+	uint32_t vertex_count;
+	const double* vertices;
+	uint32_t triangle_count;
+	const uint32_t* triangles;
+	const uint32_t* wings;  // null = all edges open
+	uint32_t grid[3];
+	const double* voxels;
+	double grid_lower[3], grid_upper[3];
+	int32_t invert;
+};
 
 // Flat description of one body. Arrays are double on this boundary whatever `scalar` is.
 struct RefDesc
@@ -72,6 +99,9 @@ struct RefDesc
 	const double* world_spheres;   // 5 per shape: cx, cy, cz, radius, friction
 
 	double gravity[3];
+
+	uint32_t world_shape_count;
+	const RefShape* world_shapes;
 };
 
 struct RefRun
@@ -225,7 +255,123 @@ uint32 HarnessStep(b3Body* body, scalar dt, uint32 newtonIters, uint32 maxSub, s
 
 inline b3Vec3 V3(const double* p) { return b3Vec3(scalar(p[0]), scalar(p[1]), scalar(p[2])); }
 
-b3Body* BuildBody(const RefDesc* d, std::vector<b3Particle*>& ps, std::vector<b3Shape*>& shapes)
+// Owns the shapes a body's world fixtures were cloned from and the meshes and SDFs the clones
+// point to.
+struct ShapeStore
+{
+	std::vector<b3Shape*> shapes;
+	std::vector<b3Mesh*> meshes;
+	std::vector<b3SDF*> sdfs;
+	~ShapeStore()
+	{
+	
+		for (b3Mesh* m : meshes)
+		{
+			delete[] m->vertices;
+			delete[] m->triangles;
+			delete m;
+		}
+		for (b3SDF* f : sdfs) delete f;
+	}
+};
+
+static b3Transform Xf(const RefShape& w)
+{
+	b3Transform xf;
+	xf.translation = V3(w.translation);
+	xf.rotation = b3Quat(b3Vec3(scalar(w.rotation[0]), scalar(w.rotation[1]), scalar(w.rotation[2])), scalar(w.rotation[3]));
+	return xf;
+}
+
+// The reference's own shape objects for one world shape description.
+static b3Shape* MakeShape(const RefShape& w, ShapeStore& store)
+{
+	b3Shape* out = nullptr;
+	switch (w.type)
+	{
+	case 0:
+	{
+		b3SphereShape* sh = new b3SphereShape();
+		sh->m_center = V3(w.p);
+		out = sh;
+		break;
+	}
+	case 1:
+	{
+		b3CapsuleShape* sh = new b3CapsuleShape();
+		sh->m_center1 = V3(w.p);
+		sh->m_center2 = V3(w.p + 3);
+		out = sh;
+		break;
+	}
+	case 2:
+	{
+		b3BoxShape* sh = new b3BoxShape();
+		sh->m_extents = V3(w.p);
+		sh->m_xf = Xf(w);
+		out = sh;
+		break;
+	}
+	case 3:
+	{
+		b3TriangleShape* sh = new b3TriangleShape();
+		sh->Set(V3(w.p), V3(w.p + 3), V3(w.p + 6));
+		out = sh;
+		break;
+	}
+	case 4:
+	{
+		b3Mesh* m = new b3Mesh();
+		m->vertexCount = w.vertex_count;
+		m->vertices = new b3Vec3[w.vertex_count];
+		for (uint32_t v = 0; v < w.vertex_count; ++v) m->vertices[v] = V3(w.vertices + 3 * v);
+		m->triangleCount = w.triangle_count;
+		m->triangles = new b3Triangle[w.triangle_count];
+		for (uint32_t t = 0; t < w.triangle_count; ++t)
+		{
+			b3Triangle& T = m->triangles[t];
+			T.v1 = w.triangles[3 * t];
+			T.v2 = w.triangles[3 * t + 1];
+			T.v3 = w.triangles[3 * t + 2];
+			T.u1 = w.wings ? w.wings[3 * t] : B3_NULL_VERTEX;
+			T.u2 = w.wings ? w.wings[3 * t + 1] : B3_NULL_VERTEX;
+			T.u3 = w.wings ? w.wings[3 * t + 2] : B3_NULL_VERTEX;
+		}
+		m->BuildTree();
+		store.meshes.push_back(m);
+		b3MeshShape* sh = new b3MeshShape();
+		sh->m_mesh = m;
+		sh->m_scale = V3(w.scale);
+		sh->m_xf = Xf(w);
+		out = sh;
+		break;
+	}
+	case 5:
+	{
+		b3SDF* f = new b3SDF();
+		f->mesh = nullptr;
+		b3AABB aabb;
+		aabb.lowerBound = V3(w.grid_lower);
+		aabb.upperBound = V3(w.grid_upper);
+		f->voxelGrid.Create(aabb, w.grid[0], w.grid[1], w.grid[2]);
+		const uint32_t nv = w.grid[0] * w.grid[1] * w.grid[2];
+		for (uint32_t k = 0; k < nv; ++k) f->voxelGrid.SetVoxel(k, scalar(w.voxels[k]));
+		store.sdfs.push_back(f);
+		b3SDFShape* sh = new b3SDFShape();
+		sh->m_sdf = f;
+		sh->m_xf = Xf(w);
+		sh->m_invert = w.invert != 0;
+		out = sh;
+		break;
+	}
+	default: return nullptr;
+	}
+	out->m_radius = scalar(w.radius);
+	store.shapes.push_back(out);
+	return out;
+}
+
+b3Body* BuildBody(const RefDesc* d, std::vector<b3Particle*>& ps, ShapeStore& store)
 {
 	// b3Body embeds a 1 MiB stack allocator: keep it on the heap.
 	b3Body* body = new b3Body();
@@ -339,10 +485,19 @@ b3Body* BuildBody(const RefDesc* d, std::vector<b3Particle*>& ps, std::vector<b3
 		b3SphereShape* shape = new b3SphereShape();
 		shape->m_center = V3(w);
 		shape->m_radius = scalar(w[3]);
-		shapes.push_back(shape);
+		store.shapes.push_back(shape);
 		b3WorldFixtureDef wd;
 		wd.shape = shape;
 		wd.friction = scalar(w[4]);
+		body->CreateFixture(wd);
+	}
+	for (uint32_t k = 0; k < d->world_shape_count; ++k)
+	{
+		b3Shape* shape = MakeShape(d->world_shapes[k], store);
+		if (!shape) continue;
+		b3WorldFixtureDef wd;
+		wd.shape = shape;
+		wd.friction = scalar(d->world_shapes[k].friction);
 		body->CreateFixture(wd);
 	}
 	return body;
@@ -356,7 +511,7 @@ extern "C" {
 int ref_simulate(const RefDesc* d, RefRun* run)
 {
 	std::vector<b3Particle*> ps;
-	std::vector<b3Shape*> shapes;
+	ShapeStore shapes;
 	b3Body* body = BuildBody(d, ps, shapes);
 
 	auto t0 = std::chrono::steady_clock::now();
@@ -388,7 +543,7 @@ int ref_simulate(const RefDesc* d, RefRun* run)
 	}
 
 	delete body;
-	for (b3Shape* s : shapes) delete s;
+
 	return 0;
 }
 

@@ -32,7 +32,9 @@ def ctx():
 
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-GOLDEN_CASES = ["tet10", "tet10_bodystep", "tet4", "tet6_newton", "single_tet", "cloth12", "cloth12_contact"]
+GOLDEN_CASES = ["tet10", "tet10_bodystep", "tet4", "tet6_newton", "single_tet", "cloth12", "cloth12_contact",
+                "shape_capsule", "shape_box", "shape_triangle", "shape_mesh", "shape_sdf"]
+SHAPE_CASES = ["shape_capsule", "shape_box", "shape_triangle", "shape_mesh", "shape_sdf"]
 
 
 def load_golden(name):
@@ -47,7 +49,18 @@ def load_golden(name):
     world = kw.pop("world_spheres")
     sr = kw.pop("sphere_radius", None)
     sf = kw.pop("sphere_friction", None)
-    desc = meshes.BodyDesc(**kw, sphere_radius=sr, sphere_friction=sf, world_spheres=world, gravity=gravity, name=name)
+    shapes = []
+    k = 0
+    while f"shape{k}_type" in z.files:
+        fields = {f[len(f"shape{k}_"):]: z[f] for f in z.files if f.startswith(f"shape{k}_")}
+        t = int(fields.pop("type"))
+        for f in ("radius", "friction", "invert"):
+            if f in fields:
+                fields[f] = fields[f].item()
+        shapes.append(meshes.WorldShape(t, **fields))
+        k += 1
+    desc = meshes.BodyDesc(**kw, sphere_radius=sr, sphere_friction=sf, world_spheres=world, gravity=gravity, name=name,
+                           world_shapes=shapes)
     st = z["settings"]
     settings = dict(max_sub=int(st[0]), sub_tol=float(st[1]), newton_iters=int(st[2]))
     return desc, z, settings

@@ -1,10 +1,13 @@
 // Drives the implicit step through include/b3g_body.hpp the way a Bounce Softbody program does:
 // CreateParticle / CreateForce / CreateTetrahedron / SetGravity / Step. Reads a tetrahedral mesh
 // (binary: n, T, positions, types, tets, E, nu, density, damping, steps, dt, tol) from argv[1],
-// writes the final positions and velocities (binary floats) to argv[2].
+// writes the final positions and velocities (binary floats) to argv[2]. With a third argument
+// "shapes" every particle also gets a contact sphere (radius 0.03, friction 0.3) and the body
+// collides with a static b3BoxShape floor and a b3CapsuleShape.
 #include "b3g_body.hpp"
 
 #include <cstdio>
+#include <string>
 #include <vector>
 
 int main(int argc, char** argv)
@@ -49,6 +52,32 @@ int main(int argc, char** argv)
 		td.v1 = fd.v1; td.v2 = fd.v2; td.v3 = fd.v3; td.v4 = fd.v4;
 		td.density = density;
 		body.CreateTetrahedron(td);
+	}
+	if (argc > 3 && std::string(argv[3]) == "shapes")
+	{
+		for (uint32 i = 0; i < n; ++i)
+		{
+			b3SphereFixtureDef sd;
+			sd.p = ps[i];
+			sd.radius = 0.03f;
+			sd.friction = 0.3f;
+			body.CreateSphere(sd);
+		}
+		b3BoxShape floor;
+		floor.m_extents = b3Vec3(1.0f, 0.05f, 1.0f);
+		floor.m_xf.translation = b3Vec3(0.2f, -0.07f, 0.2f);
+		floor.m_xf.rotation = b3Quat(b3Vec3(0.0f, 0.0f, 0.0499792f), 0.9987503f);
+		b3WorldFixtureDef fd;
+		fd.shape = &floor;
+		fd.friction = 0.5f;
+		body.CreateFixture(fd);
+		b3CapsuleShape pole;
+		pole.m_center1 = b3Vec3(0.6f, 0.0f, -0.1f);
+		pole.m_center2 = b3Vec3(0.6f, 0.0f, 0.8f);
+		pole.m_radius = 0.12f;
+		fd.shape = &pole;
+		fd.friction = 0.2f;
+		body.CreateFixture(fd);
 	}
 	body.SetSolverTolerance(tol);
 	for (uint32 s = 0; s < steps; ++s) body.Step(dt, 1, 200);

@@ -50,7 +50,14 @@ CASES = [
      dict(max_sub=200, sub_tol=1e-5)),
     ("cloth12_contact", lambda: meshes.cloth_grid(12, side=1.2, height=0.52, sphere_radius=0.5, contact_radius=0.05),
      [3, 6], dict(max_sub=200, sub_tol=1e-5)),
-]
+    # a 10 x 10 cloth falling onto each kind of static world shape (the reference's own
+    # b3CapsuleShape, b3BoxShape, b3TriangleShape, b3MeshShape with wing vertices and b3SDFShape),
+    # in contact from step 2; short horizon for the same reason as the sphere cloth
+] + [(f"shape_{k}", (lambda k=k: meshes.shape_scene(k, m=10, height=0.002)), [2, 4], dict(max_sub=200, sub_tol=1e-5))
+     for k in ("capsule", "box", "triangle", "mesh", "sdf")]
+
+SHAPE_FIELDS = ["type", "radius", "friction", "p", "rotation", "translation", "scale", "vertices", "triangles",
+                "wings", "voxels", "grid_lower", "grid_upper", "invert"]
 
 FIELDS = ["x", "v", "type", "damping", "tets", "tet_E", "tet_nu", "tet_kdamp", "tet_density", "tris", "tri_Ex",
           "tri_Ey", "tri_Es", "tri_nuxy", "tri_nuyx", "tri_kdamp", "tri_density", "springs", "spring_L0",
@@ -66,6 +73,11 @@ def main():
         if body.sphere_radius is not None:
             out["in_sphere_radius"] = body.sphere_radius
             out["in_sphere_friction"] = body.sphere_friction
+        for k, sh in enumerate(body.world_shapes):
+            for f in SHAPE_FIELDS:
+                val = getattr(sh, f)
+                if val is not None:
+                    out[f"shape{k}_{f}"] = np.asarray(val)
         out["steps"] = np.array(snaps)
         out["settings"] = np.array([kw.get("max_sub", 200), kw.get("sub_tol", 1.1920928955078125e-07),
                                     kw.get("newton_iters", 1), 1 if kw.get("use_body_step") else 0], np.float64)

@@ -26,9 +26,20 @@ def test_facade_compiles_and_links(tmp_path):
 
 
 @pytest.mark.gpu
-def test_facade_matches_c_abi(tmp_path, ctx):
+@pytest.mark.parametrize("shapes", [False, True])
+def test_facade_matches_c_abi(tmp_path, ctx, shapes):
     exe = build_demo(tmp_path)
-    desc = meshes.tet_grid(6, 5, 7, seed=4, E=2e5, nu=0.33, pin="y0")
+    desc = meshes.tet_grid(6, 5, 7, seed=4, E=2e5, nu=0.33, pin="none" if shapes else "y0")
+    if shapes:
+        # what facade_demo.cpp builds with "shapes": contact spheres, a box floor, a capsule
+        desc.sphere_radius = np.full(desc.n, 0.03)
+        desc.sphere_friction = np.full(desc.n, 0.3)
+        desc.world_shapes = [
+            meshes.WorldShape(meshes.SHAPE_BOX, radius=0.0, friction=0.5, p=np.array([1.0, 0.05, 1.0, 0, 0, 0, 0, 0, 0]),
+                              rotation=np.array([0.0, 0.0, 0.0499792, 0.9987503]), translation=np.array([0.2, -0.07, 0.2])),
+            meshes.WorldShape(meshes.SHAPE_CAPSULE, radius=0.12, friction=0.2,
+                              p=np.array([0.6, 0.0, -0.1, 0.6, 0.0, 0.8, 0, 0, 0])),
+        ]
     steps, dt, tol = 8, 1.0 / 60.0, 1e-5
     inp = tmp_path / "in.bin"
     with open(inp, "wb") as f:
@@ -40,7 +51,8 @@ def test_facade_matches_c_abi(tmp_path, ctx):
         np.array([steps], np.uint32).tofile(f)
         np.array([dt, tol], np.float32).tofile(f)
     out = tmp_path / "out.bin"
-    r = subprocess.run([exe, str(inp), str(out)], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([exe, str(inp), str(out)] + (["shapes"] if shapes else []), capture_output=True, text=True,
+                       timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     res = np.fromfile(out, np.float32).reshape(2, desc.n, 3)
     g = b3g.Body(ctx, desc)

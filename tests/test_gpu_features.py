@@ -190,3 +190,27 @@ def test_zero_dt_skips_the_solve(ctx):
     x1, v1 = g.state()
     assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
     g.close()
+
+
+def test_invalid_world_shapes_are_rejected(ctx):
+    """b3g_body_create validates world shapes: fixture count, types, mesh indices, SDF grids."""
+    base = meshes.shape_scene("capsule", m=4)
+    cases = []
+    many = meshes.shape_scene("capsule", m=4)
+    many.world_shapes = [meshes.WorldShape(meshes.SHAPE_SPHERE, radius=0.1, p=np.zeros(9)) for _ in range(17)]
+    cases.append((many, "at most 16 world fixtures"))
+    bad_type = meshes.shape_scene("capsule", m=4)
+    bad_type.world_shapes = [meshes.WorldShape(9)]
+    cases.append((bad_type, "unknown shape type"))
+    bad_mesh = meshes.shape_scene("mesh", m=4)
+    sh = bad_mesh.world_shapes[0]
+    sh.triangles = sh.triangles.copy()
+    sh.triangles[0, 0] = 1000
+    cases.append((bad_mesh, "vertex out of range"))
+    bad_sdf = meshes.shape_scene("sdf", m=4)
+    bad_sdf.world_shapes[0].voxels = np.zeros((1, 4, 4))
+    cases.append((bad_sdf, "at least 2 voxels"))
+    for desc, msg in cases:
+        with pytest.raises(b3g.B3gError, match=msg):
+            b3g.Body(ctx, desc)
+    b3g.Body(ctx, base).close()

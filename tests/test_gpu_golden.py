@@ -7,7 +7,7 @@ relative (or 20x that spread); PCG iteration counts within 3 of the FP32 referen
 """
 import numpy as np
 import pytest
-from conftest import GOLDEN_CASES, load_golden
+from conftest import GOLDEN_CASES, SHAPE_CASES, load_golden
 
 from bounce_softbody_gb300 import b3g
 
@@ -44,6 +44,28 @@ def test_gpu_matches_reference_golden(ctx, name):
         assert rel(v, rv) < max(1e-3, 20 * floor_v), (name, s)
         ref_it = int(z[f"ref32_it_{s}"][-1])
         # contact scenes are chaotic: their iteration counts wander with the trajectory
-        slack = 3 if "contact" not in name else max(3, int(0.35 * ref_it))
+        slack = max(3, int(0.35 * ref_it)) if ("contact" in name or name.startswith("shape_")) else 3
         assert abs(its[-1] - ref_it) <= slack, (name, s, its[-1])
     g.close()
+
+
+def test_batched_shapes_match_reference_golden(ctx):
+    """The cloth-on-shape scenes stepped together by the persistent batch kernels (one launch for
+    all five shape kinds) against the same golden vectors."""
+    loaded = [load_golden(name) for name in SHAPE_CASES]
+    st = loaded[0][2]
+    cfg = b3g.solver_config(max_pcg_iterations=st["max_sub"], pcg_tolerance=st["sub_tol"])
+    bodies = [b3g.Body(ctx, desc) for desc, _, _ in loaded]
+    done = 0
+    for s in [int(k) for k in loaded[0][1]["steps"]]:
+        b3g.step_batch(ctx, bodies, DT, s - done, cfg, stats=False)
+        done = s
+        for (desc, z, _), g, name in zip(loaded, bodies, SHAPE_CASES):
+            x, v = g.state()
+            rx, rv = z[f"ref64_x_{s}"], z[f"ref64_v_{s}"]
+            floor_x = rel_disp(z[f"ref32_x_{s}"], rx, desc.x)
+            floor_v = rel(z[f"ref32_v_{s}"], rv)
+            assert rel_disp(x, rx, desc.x) < max(1e-4, 20 * floor_x), (name, s)
+            assert rel(v, rv) < max(1e-3, 20 * floor_v), (name, s)
+    for g in bodies:
+        g.close()
