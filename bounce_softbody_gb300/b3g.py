@@ -50,6 +50,9 @@ class BodyDescC(C.Structure):
         ("world_sphere_count", C.c_uint32), ("world_spheres", _fp),
         ("gravity", C.c_float * 3),
         ("world_shape_count", C.c_uint32), ("world_shapes", C.POINTER(WorldShapeC)),
+        ("stretch_count", C.c_uint32), ("stretch_tris", _up), ("stretch_uv", _fp), ("stretch_params", _fp),
+        ("shear_count", C.c_uint32), ("shear_tris", _up), ("shear_uv", _fp), ("shear_params", _fp),
+        ("mouse_count", C.c_uint32), ("mouse_ids", _up), ("mouse_params", _fp),
     ]
 
 
@@ -315,6 +318,23 @@ def _desc_struct(desc, masses=None):
         d.world_shapes = C.cast(arr, C.POINTER(WorldShapeC))
     else:
         d.world_shapes = C.cast(None, C.POINTER(WorldShapeC))
+    st = getattr(desc, "stretch_tris", None)
+    if st is not None and len(st):
+        d.stretch_count = len(st)
+        d.stretch_tris = u(st)
+        d.stretch_uv = f(desc.stretch_uv)
+        d.stretch_params = f(desc.stretch_params)
+    sh = getattr(desc, "shear_tris", None)
+    if sh is not None and len(sh):
+        d.shear_count = len(sh)
+        d.shear_tris = u(sh)
+        d.shear_uv = f(desc.shear_uv)
+        d.shear_params = f(desc.shear_params)
+    ms = getattr(desc, "mouse_ids", None)
+    if ms is not None and len(ms):
+        d.mouse_count = len(ms)
+        d.mouse_ids = u(ms)
+        d.mouse_params = f(desc.mouse_params)
     return d, keep
 
 

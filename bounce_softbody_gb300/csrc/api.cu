@@ -1,6 +1,7 @@
 // C ABI of b3g (include/b3g.h): contexts, bodies, the single-body step (per-op kernels) and
 // state transfer. The batch entry point lives in batch.cu.
 #include "api_internal.h"
+#include "forces.h"
 #include "shapes.h"
 
 #include <algorithm>
@@ -190,12 +191,12 @@ void reset_mass(b3g_body* b)
 		}
 		return;
 	}
-	for (uint32_t e = 0; e < b->ntr; ++e)
+	for (uint32_t e = 0; e < b->ntr_fix; ++e)
 		for (int k = 0; k < 3; ++k) m[b->h_tris[3 * e + k]] = 0.0f;
 	for (uint32_t e = 0; e < b->nt; ++e)
 		for (int k = 0; k < 4; ++k) m[b->h_tets[4 * e + k]] = 0.0f;
 	const float inv3 = 1.0f / 3.0f, inv4 = 1.0f / 4.0f;
-	for (uint32_t e = b->ntr; e-- > 0;)
+	for (uint32_t e = b->ntr_fix; e-- > 0;)
 	{
 		float mm = b->h_tri_mass[e];
 		for (int k = 0; k < 3; ++k) m[b->h_tris[3 * e + k]] += inv3 * mm;
@@ -407,17 +408,28 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	if (n == 0 || !d->positions || !d->types) return fail(B3G_ERROR_INVALID_ARGUMENT, "positions and types are required");
 	if (d->tet_count && (!d->tets || !d->tet_young || !d->tet_poisson))
 		return fail(B3G_ERROR_INVALID_ARGUMENT, "tetrahedra need tets, tet_young and tet_poisson");
-	if (d->tri_count && (!d->tris || !d->tri_young_x || !d->tri_young_y || !d->tri_shear || !d->tri_poisson_xy || !d->tri_poisson_yx))
-		return fail(B3G_ERROR_INVALID_ARGUMENT, "triangles need tris and their five material arrays");
+	// triangles are mass fixtures (b3TriangleFixture) and, when the five material arrays are
+	// given, membrane elements (b3TriangleElementForce) too
+	const bool tri_elements = d->tri_young_x || d->tri_young_y || d->tri_shear || d->tri_poisson_xy || d->tri_poisson_yx;
+	if (d->tri_count && (!d->tris || (tri_elements && !(d->tri_young_x && d->tri_young_y && d->tri_shear &&
+	                                                   d->tri_poisson_xy && d->tri_poisson_yx))))
+		return fail(B3G_ERROR_INVALID_ARGUMENT, "triangles need tris and all or none of their five material arrays");
+	for (uint64_t k = 0; k < 3 * (uint64_t)d->tri_count; ++k)
+		if (d->tris[k] >= n)
+			return fail(B3G_ERROR_INVALID_ARGUMENT, "triangle %u references vertex %u >= vertex_count %u",
+			            (uint32_t)(k / 3), d->tris[k], n);
 	if (d->spring_count && (!d->springs || !d->spring_rest_length || !d->spring_stiffness || !d->spring_damping))
 		return fail(B3G_ERROR_INVALID_ARGUMENT, "springs need springs, rest lengths, stiffness and damping");
 	std::vector<DevShape> shapes;
 	std::vector<float> shape_data;
+	ClothForces cf;
 	{
 		char msg[256];
 		if (build_shapes(d, shapes, shape_data, msg, sizeof(msg)) != 0)
 			return fail(B3G_ERROR_INVALID_ARGUMENT, "%s", msg);
+		if (build_cloth_forces(d, cf, msg, sizeof(msg)) != 0) return fail(B3G_ERROR_INVALID_ARGUMENT, "%s", msg);
 	}
+	const uint32_t nbw = (uint32_t)cf.bw.size(), nms = (uint32_t)cf.ms.size();
 	for (uint32_t i = 0; i < n; ++i)
 		if (d->types[i] < 0 || d->types[i] > 2) return fail(B3G_ERROR_INVALID_ARGUMENT, "vertex %u has type %d", i, d->types[i]);
 	if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(B3G_ERROR_CUDA, "cudaSetDevice");
@@ -427,13 +439,15 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	b->ctx = ctx;
 	b->n = n;
 	b->nt = d->tet_count;
-	b->ntr = d->tri_count;
+	b->ntr_fix = d->tri_count;
+	b->ntr = tri_elements ? d->tri_count : 0;
 	b->ns = d->spring_count;
 	b->nw = d->sphere_radius ? (uint32_t)shapes.size() : 0;
 
 	char err[256];
 	Pattern P;
-	if (!build_pattern(n, b->nt, d->tets, b->ntr, d->tris, b->ns, d->springs, &P, err, sizeof(err)))
+	if (!build_pattern(n, b->nt, d->tets, b->ntr, d->tris, b->ns, d->springs, nbw, cf.bw_ids.data(), nms,
+	                   cf.ms_ids.data(), &P, err, sizeof(err)))
 	{
 		delete b;
 		return fail(B3G_ERROR_INVALID_ARGUMENT, "%s", err);
@@ -443,7 +457,7 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	// element constants on the host
 	b->h_type.assign(d->types, d->types + n);
 	b->h_tets.assign(d->tets, d->tets + 4 * (size_t)b->nt);
-	b->h_tris.assign(d->tris, d->tris + 3 * (size_t)b->ntr);
+	b->h_tris.assign(d->tris, d->tris + 3 * (size_t)b->ntr_fix);
 	if (d->masses) b->h_given_mass.assign(d->masses, d->masses + n);
 	std::vector<uint4> tet(b->nt);
 	std::vector<float> tet_invE(9 * (size_t)b->nt);
@@ -473,22 +487,25 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	}
 	std::vector<uint4> tri(b->ntr);
 	std::vector<float> tri_x(6 * (size_t)b->ntr), tri_invS(4 * (size_t)b->ntr), tri_K(36 * (size_t)b->ntr), tri_kd(b->ntr);
-	b->h_tri_mass.resize(b->ntr);
-	for (uint32_t e = 0; e < b->ntr; ++e)
+	b->h_tri_mass.resize(b->ntr_fix);
+	for (uint32_t e = 0; e < b->ntr_fix; ++e)
 	{
 		const uint32_t* t = d->tris + 3 * e;
-		tri[e] = make_uint4(t[0], t[1], t[2], 0);
 		float r[9];
 		for (int k = 0; k < 3; ++k)
 			for (int c = 0; c < 3; ++c) r[3 * k + c] = d->tri_rest ? d->tri_rest[9 * e + 3 * k + c] : d->positions[3 * t[k] + c];
-		if (!tri_setup(r, d->tri_young_x[e], d->tri_young_y[e], d->tri_shear[e], d->tri_poisson_xy[e], d->tri_poisson_yx[e],
-		               &tri_x[6 * (size_t)e], &tri_invS[4 * (size_t)e], &tri_K[36 * (size_t)e]))
+		if (tri_elements)
 		{
-			free_pattern(&P);
-			delete b;
-			return fail(B3G_ERROR_INVALID_ARGUMENT, "triangle %u is degenerate", e);
+			tri[e] = make_uint4(t[0], t[1], t[2], 0);
+			if (!tri_setup(r, d->tri_young_x[e], d->tri_young_y[e], d->tri_shear[e], d->tri_poisson_xy[e],
+			               d->tri_poisson_yx[e], &tri_x[6 * (size_t)e], &tri_invS[4 * (size_t)e], &tri_K[36 * (size_t)e]))
+			{
+				free_pattern(&P);
+				delete b;
+				return fail(B3G_ERROR_INVALID_ARGUMENT, "triangle %u is degenerate", e);
+			}
+			tri_kd[e] = d->tri_stiffness_damping ? d->tri_stiffness_damping[e] : 0.0f;
 		}
-		tri_kd[e] = d->tri_stiffness_damping ? d->tri_stiffness_damping[e] : 0.0f;
 		// triangle_fixture.cpp:33-36 area = |cross| / 2
 		V3h a = ld(r), bb = ld(r + 3), c = ld(r + 6);
 		V3h N = cross(sub(bb, a), sub(c, a));
@@ -543,8 +560,12 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 		D.spr_L0 = C.take<float>(b->ns);
 		D.spr_ks = C.take<float>(b->ns);
 		D.spr_kd = C.take<float>(b->ns);
-		D.blocks = C.take<float>(9 * (9 * (size_t)b->ntr + b->ns));
-		D.bvec = C.take<float>(3 * (3 * (size_t)b->ntr + b->ns));
+		D.bw = C.take<uint4>(nbw);
+		D.bw_c = C.take<float>((size_t)kBwFloats * nbw);
+		D.ms = C.take<uint4>(nms);
+		D.ms_c = C.take<float>((size_t)kMouseFloats * nms);
+		D.blocks = C.take<float>(9 * (9 * (size_t)b->ntr + b->ns + 9 * (size_t)nbw + 16 * (size_t)nms));
+		D.bvec = C.take<float>(3 * (3 * (size_t)b->ntr + b->ns + 3 * (size_t)nbw + 4 * (size_t)nms));
 		D.srad = C.take<float>(b->nw ? n : 0);
 		D.sfric = C.take<float>(b->nw ? n : 0);
 		D.c_exists = C.take<uint8_t>((size_t)n * b->nw);
@@ -582,6 +603,8 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	D.ntr = (int)b->ntr;
 	D.ns = (int)b->ns;
 	D.nw = (int)b->nw;
+	D.nbw = (int)nbw;
+	D.nms = (int)nms;
 	D.maxw = P.maxw;
 	D.contacts = b->nw > 0 ? 1 : 0;
 	if (b->nw) bind_shape_data(shapes, shape_dev);
@@ -635,6 +658,10 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	up(D.spr_L0, d->spring_rest_length, b->ns * sizeof(float));
 	up(D.spr_ks, d->spring_stiffness, b->ns * sizeof(float));
 	up(D.spr_kd, d->spring_damping, b->ns * sizeof(float));
+	up(D.bw, cf.bw.data(), nbw * sizeof(uint4));
+	up(D.bw_c, cf.bw_c.data(), cf.bw_c.size() * sizeof(float));
+	up(D.ms, cf.ms.data(), nms * sizeof(uint4));
+	up(D.ms_c, cf.ms_c.data(), cf.ms_c.size() * sizeof(float));
 	if (b->nw)
 	{
 		up(D.srad, d->sphere_radius, n * sizeof(float));

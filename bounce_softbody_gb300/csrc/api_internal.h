@@ -44,6 +44,7 @@ struct b3g_body
 {
 	b3g_context* ctx = nullptr;
 	uint32_t n = 0, nt = 0, ntr = 0, ns = 0, nw = 0;
+	uint32_t ntr_fix = 0;  // triangle mass fixtures (ntr of them are also membrane elements)
 	uint64_t nnzb = 0;
 	b3g::DevBody d{};
 	char* arena = nullptr;

@@ -583,6 +583,228 @@ __device__ __forceinline__ void spring_element(const DevBody& B, int s, const St
 	st3(B.bvec, 3 * B.ntr + s, bvv);
 }
 
+// ------------------------------------------------------------------ cloth forces
+// Velocity-level displacement w_k = h v_k + y_k (+ x_k - iterate on later Newton iterates) of an
+// element's vertex, the vector the implicit right-hand side h (f + dfdx w) multiplies dfdx by.
+template <class LP>
+__device__ __forceinline__ float3 element_w(const DevBody& B, const StepParams& P, int id, float3 xk, float3 vk)
+{
+	float3 w = P.h * vk + ldl3<LP>(B.trans, id);
+	if (!P.first_newton) w = w + (ldl3<LP>(B.x, id) - xk);
+	return w;
+}
+
+// Symmetric 3x3 (xx, xy, xz, yy, yz, zz): s nn^T + t I.
+__device__ __forceinline__ void sym_nn(float3 n, float s, float t, float M[6])
+{
+	M[0] = s * n.x * n.x + t; M[1] = s * n.x * n.y; M[2] = s * n.x * n.z;
+	M[3] = s * n.y * n.y + t; M[4] = s * n.y * n.z; M[5] = s * n.z * n.z + t;
+}
+__device__ __forceinline__ float3 sym_mv(const float M[6], float3 v)
+{
+	return f3(M[0] * v.x + M[1] * v.y + M[2] * v.z, M[1] * v.x + M[3] * v.y + M[4] * v.z,
+	          M[2] * v.x + M[4] * v.y + M[5] * v.z);
+}
+// o (9 floats, row-major) = s M
+__device__ __forceinline__ void sym_store(float* o, const float M[6], float s)
+{
+	o[0] = s * M[0]; o[1] = s * M[1]; o[2] = s * M[2];
+	o[3] = s * M[1]; o[4] = s * M[3]; o[5] = s * M[4];
+	o[6] = s * M[2]; o[7] = s * M[4]; o[8] = s * M[5];
+}
+
+// One direction (u or v) of the Baraff-Witkin stretch condition
+// (stretch_force.cpp:142-270 for u, 272-387 for v): C = alpha (|w_dir| - b), dC_a = alpha g_a n
+// with n = w_dir / |w_dir|. Every Jacobian block of the direction is g_a g_b times one symmetric
+// matrix, so the direction yields
+//   M   = h^2 Ks + h kd alpha^2 nn^T   (the A blocks are g_a g_b M),
+//   Ks  = ks (alpha^2 nn^T + [|w_dir| > b] C alpha / |w_dir| (I - nn^T))   (dfdx_ab = -g_a g_b Ks),
+// and adds to f_a the stiffness and damping forces and -g_a Ks sum_b g_b w_b.
+__device__ __forceinline__ void stretch_direction(float3 wd, const float g[3], float alpha, float ks, float kd,
+                                                  float b, const float3 v[3], const float3 w[3], float h,
+                                                  float3 f[3], float M[6])
+{
+#pragma unroll
+	for (int q = 0; q < 6; ++q) M[q] = 0.0f;
+	const float len = len3(wd);
+	if (!(len > 0.0f)) return;
+	const float inv_len = 1.0f / len;
+	const float3 n = inv_len * wd;
+	if (ks > 0.0f)
+	{
+		const float C = alpha * (len - b);
+		const float t = len > b ? C * alpha * inv_len : 0.0f;
+		float Ks[6];
+		sym_nn(n, ks * (alpha * alpha - t), ks * t, Ks);
+		const float3 W = g[0] * w[0] + g[1] * w[1] + g[2] * w[2];
+		const float3 KW = sym_mv(Ks, W);
+#pragma unroll
+		for (int a = 0; a < 3; ++a) f[a] = f[a] - (ks * C * alpha * g[a]) * n - g[a] * KW;
+#pragma unroll
+		for (int q = 0; q < 6; ++q) M[q] = h * h * Ks[q];
+	}
+	if (kd > 0.0f)
+	{
+		const float dCdt = alpha * dot3(g[0] * v[0] + g[1] * v[1] + g[2] * v[2], n);
+#pragma unroll
+		for (int a = 0; a < 3; ++a) f[a] = f[a] - (kd * dCdt * alpha * g[a]) * n;
+		float Md[6];
+		sym_nn(n, h * kd * alpha * alpha, 0.0f, Md);
+#pragma unroll
+		for (int q = 0; q < 6; ++q) M[q] += Md[q];
+	}
+}
+
+// Baraff-Witkin stretch (stretch_force.cpp:121-388) or shear (shear_force.cpp:106-244) triangle.
+// With dx1 = x2 - x1, dx2 = x3 - x1: w_u = (dv2 dx1 - dv1 dx2) / det, w_v = (du1 dx2 - du2 dx1) / det.
+// Writes the 9 blocks -h^2 dfdx_ab - h dfdv_ab of A and the 3 vectors h (f_a + sum_b dfdx_ab w_b).
+// Shear: C = alpha w_u . w_v, dC_a = alpha (dwu_a w_v + dwv_a w_u), dfdx_ab = -ks dC_a dC_b^T
+// (the reference drops the second-derivative term), dfdv_ab = -kd dC_a dC_b^T.
+template <class LP = LdPlain>
+__device__ __forceinline__ void bw_element(const DevBody& B, int e, const StepParams& P)
+{
+	const float h = P.h;
+	const uint4 id = B.bw[e];
+	const int ids[3] = {(int)id.x, (int)id.y, (int)id.z};
+	const float* c = B.bw_c + (size_t)kBwFloats * e;
+	const float* X = P.first_newton ? B.x : B.xi;
+	const float* Vv = P.first_newton ? B.v : B.vi;
+	float3 x[3], v[3], w[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+	{
+		x[k] = ldl3<LP>(X, ids[k]);
+		v[k] = ldl3<LP>(Vv, ids[k]);
+		w[k] = element_w<LP>(B, P, ids[k], x[k], v[k]);
+	}
+	const float alpha = c[0], inv_det = c[1], du1 = c[2], dv1 = c[3], du2 = c[4], dv2 = c[5];
+	const float gu[3] = {c[6], c[7], c[8]}, gv[3] = {c[9], c[10], c[11]};
+	const float3 dx1 = x[1] - x[0], dx2 = x[2] - x[0];
+	const float3 wu = inv_det * (dv2 * dx1 - dv1 * dx2);
+	const float3 wv = inv_det * (-du2 * dx1 + du1 * dx2);
+	float3 f[3] = {f3(0, 0, 0), f3(0, 0, 0), f3(0, 0, 0)};
+	float* blk = B.blocks + 9 * ((size_t)9 * B.ntr + B.ns + 9 * (size_t)e);
+	if (id.w == kForceStretch)
+	{
+		float Mu[6], Mv[6];
+		stretch_direction(wu, gu, alpha, c[12], c[13], c[14], v, w, h, f, Mu);
+		stretch_direction(wv, gv, alpha, c[15], c[16], c[17], v, w, h, f, Mv);
+#pragma unroll
+		for (int a = 0; a < 3; ++a)
+#pragma unroll
+			for (int b = 0; b < 3; ++b)
+			{
+				const float su = gu[a] * gu[b], sv = gv[a] * gv[b];
+				float M[6];
+#pragma unroll
+				for (int q = 0; q < 6; ++q) M[q] = su * Mu[q] + sv * Mv[q];
+				sym_store(blk + 9 * (3 * a + b), M, 1.0f);
+			}
+	}
+	else
+	{
+		const float ks = c[12], kd = c[13];
+		float3 dC[3];
+#pragma unroll
+		for (int a = 0; a < 3; ++a) dC[a] = alpha * (gu[a] * wv + gv[a] * wu);
+		float sA = 0.0f;
+		if (ks > 0.0f)
+		{
+			const float C = alpha * dot3(wu, wv);
+			const float S = dot3(dC[0], w[0]) + dot3(dC[1], w[1]) + dot3(dC[2], w[2]);
+#pragma unroll
+			for (int a = 0; a < 3; ++a) f[a] = f[a] - (ks * (C + S)) * dC[a];
+			sA += h * h * ks;
+		}
+		if (kd > 0.0f)
+		{
+			const float dCdt = dot3(dC[0], v[0]) + dot3(dC[1], v[1]) + dot3(dC[2], v[2]);
+#pragma unroll
+			for (int a = 0; a < 3; ++a) f[a] = f[a] - (kd * dCdt) * dC[a];
+			sA += h * kd;
+		}
+#pragma unroll
+		for (int a = 0; a < 3; ++a)
+#pragma unroll
+			for (int b = 0; b < 3; ++b)
+			{
+				float* o = blk + 9 * (3 * a + b);
+				const float ra[3] = {dC[a].x, dC[a].y, dC[a].z}, rb[3] = {dC[b].x, dC[b].y, dC[b].z};
+#pragma unroll
+				for (int r = 0; r < 3; ++r)
+#pragma unroll
+					for (int q = 0; q < 3; ++q) o[3 * r + q] = sA * ra[r] * rb[q];
+			}
+	}
+	const size_t v0 = (size_t)3 * B.ntr + B.ns + 3 * (size_t)e;
+#pragma unroll
+	for (int a = 0; a < 3; ++a) st3(B.bvec, (int)(v0 + a), h * f[a]);
+}
+
+// Mouse spring between particle 1 and the point w2 x2 + w3 x3 + w4 x4 of a triangle
+// (mouse_force.cpp:58-245): d = x1 - c2, C = |d| - L0, dC_a = c_a n with c = (1, -w2, -w3, -w4).
+// Every block is c_a c_b times one symmetric matrix:
+//   dfdx_ab = -c_a c_b ks (nn^T + C (I / |d| - dd^T / |d|^3))   (only while |d| > L0),
+//   dfdv_ab = -c_a c_b kd nn^T.
+template <class LP = LdPlain>
+__device__ __forceinline__ void mouse_element(const DevBody& B, int e, const StepParams& P)
+{
+	const float h = P.h;
+	const uint4 id = B.ms[e];
+	const int ids[4] = {(int)id.x, (int)id.y, (int)id.z, (int)id.w};
+	const float* c = B.ms_c + (size_t)kMouseFloats * e;
+	const float* X = P.first_newton ? B.x : B.xi;
+	const float* Vv = P.first_newton ? B.v : B.vi;
+	const float cw[4] = {1.0f, -c[0], -c[1], -c[2]};
+	const float ks = c[3], kd = c[4], L0 = c[5];
+	float3 x[4], v[4];
+#pragma unroll
+	for (int k = 0; k < 4; ++k)
+	{
+		x[k] = ldl3<LP>(X, ids[k]);
+		v[k] = ldl3<LP>(Vv, ids[k]);
+	}
+	const float3 d = x[0] - (c[0] * x[1] + c[1] * x[2] + c[2] * x[3]);
+	const float L = len3(d);
+	float M[6] = {0, 0, 0, 0, 0, 0};
+	float3 fd = f3(0, 0, 0);  // f_a = c_a fd
+	if (L > 0.0f)
+	{
+		const float inv_L = 1.0f / L;
+		const float3 n = inv_L * d;
+		if (ks > 0.0f && L > L0)
+		{
+			const float C = L - L0;
+			// nn^T + C (I / L - dd^T / L^3) = (1 - C / L) nn^T + (C / L) I
+			float Ks[6];
+			sym_nn(n, ks * (1.0f - C * inv_L), ks * C * inv_L, Ks);
+			float3 W = f3(0, 0, 0);
+#pragma unroll
+			for (int k = 0; k < 4; ++k) W = W + cw[k] * element_w<LP>(B, P, ids[k], x[k], v[k]);
+			fd = fd - (ks * C) * n - sym_mv(Ks, W);
+#pragma unroll
+			for (int q = 0; q < 6; ++q) M[q] = h * h * Ks[q];
+		}
+		if (kd > 0.0f)
+		{
+			const float dCdt = dot3(v[0] - (c[0] * v[1] + c[1] * v[2] + c[2] * v[3]), n);
+			fd = fd - (kd * dCdt) * n;
+			float Md[6];
+			sym_nn(n, h * kd, 0.0f, Md);
+#pragma unroll
+			for (int q = 0; q < 6; ++q) M[q] += Md[q];
+		}
+	}
+	float* blk = B.blocks + 9 * ((size_t)9 * B.ntr + B.ns + 9 * (size_t)B.nbw + 16 * (size_t)e);
+#pragma unroll
+	for (int a = 0; a < 4; ++a)
+#pragma unroll
+		for (int b = 0; b < 4; ++b) sym_store(blk + 9 * (4 * a + b), M, cw[a] * cw[b]);
+	const size_t v0 = (size_t)3 * B.ntr + B.ns + 3 * (size_t)B.nbw + 4 * (size_t)e;
+#pragma unroll
+	for (int a = 0; a < 4; ++a) st3(B.bvec, (int)(v0 + a), (h * cw[a]) * fd);
+}
+
 // ------------------------------------------------------------------ row assembly
 // ------------------------------------------------------------------ world shapes
 // The closest point of each static world shape to a vertex sphere (b3Shape::Collide): the

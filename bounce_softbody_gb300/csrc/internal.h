@@ -93,12 +93,20 @@ struct DevShape
 // unscaled mesh-frame AABB lower and upper (6), pad (1)
 constexpr int kMeshTriFloats = 28;
 
+// Baraff-Witkin triangle records (stretch_force.cpp:62-107, shear_force.cpp:51-92): alpha,
+// inv_det, du1, dv1, du2, dv2, dwu/dx (3), dwv/dx (3), then stiffness_u, damping_u, b_u,
+// stiffness_v, damping_v, b_v (stretch) or stiffness, damping (shear).
+constexpr int kBwFloats = 20;
+constexpr int kMouseFloats = 6;
+constexpr uint32_t kForceStretch = 0, kForceShear = 1;
+
 // Everything a kernel needs about one body. Passed by value to the per-op kernels and read
 // from a device array by the persistent batch kernel.
 struct DevBody
 {
 	int n, nslices, npad, nslots;
 	int nt, ntr, ns, nw;
+	int nbw, nms;               // stretch/shear triangles, mouse springs
 	int maxw;                   // widest slice
 	int contacts;               // per-vertex contact spheres present
 
@@ -159,9 +167,18 @@ struct DevBody
 	const float* spr_ks;
 	const float* spr_kd;
 
-	// explicit (non-tetrahedral) contributions
-	float* blocks;              // 9 per block: tri (a, b) at 9 e + 3 a + b, spring at 9 Tr + s
-	float* bvec;                // 3 per vector: tri (a) at 3 e + a, spring at 3 Tr + s
+	// Baraff-Witkin stretch and shear triangles, mouse springs
+	const uint4* bw;            // 3 ids, kind in w (kForceStretch / kForceShear)
+	const float* bw_c;          // kBwFloats per element (bw_setup)
+	const uint4* ms;            // 4 ids: the dragged particle, then the triangle
+	const float* ms_c;          // kMouseFloats per element: w2, w3, w4, stiffness, damping, length
+
+	// explicit (non-tetrahedral) contributions. Blocks, 9 floats each: tri (a, b) at 9 e + 3 a + b,
+	// spring at 9 Tr + s, stretch/shear (a, b) at 9 Tr + S + 9 e + 3 a + b, mouse (a, b) at
+	// 9 Tr + S + 9 Bw + 16 e + 4 a + b. Vectors, 3 floats each: tri (a) at 3 e + a, spring at
+	// 3 Tr + s, stretch/shear (a) at 3 Tr + S + 3 e + a, mouse (a) at 3 Tr + S + 3 Bw + 4 e + a.
+	float* blocks;
+	float* bvec;
 
 	// contacts
 	const float* srad;
@@ -218,7 +235,8 @@ struct Pattern
 // Builds the SELL-32 pattern and every contribution list. Returns false with a message on a
 // malformed mesh (vertex index out of range, degenerate element).
 bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, const uint32_t* tris,
-                   uint32_t ns, const uint32_t* springs, Pattern* out, char* err, size_t errlen);
+                   uint32_t ns, const uint32_t* springs, uint32_t nbw, const uint32_t* bw, uint32_t nms,
+                   const uint32_t* ms, Pattern* out, char* err, size_t errlen);
 void free_pattern(Pattern* p);
 
 } // namespace b3g

@@ -151,6 +151,17 @@ __global__ void __launch_bounds__(kThreads) k_springs(DevBody B, StepParams P)
 	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B.ns; e += gridDim.x * blockDim.x) spring_element(B, e, P);
 }
 
+// stretch/shear triangles and mouse springs in one launch: the triangles, then the springs
+__global__ void __launch_bounds__(kThreads) k_cloth_forces(DevBody B, StepParams P)
+{
+	const int total = B.nbw + B.nms;
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x)
+	{
+		if (e < B.nbw) bw_element(B, e, P);
+		else mouse_element(B, e - B.nbw, P);
+	}
+}
+
 __device__ void pcg_start(Scalars* sc, double delta0)
 {
 	sc->delta = delta0;
@@ -509,6 +520,7 @@ cudaError_t op_elements(const DevBody& B, const StepParamsHost& Ph, cudaStream_t
 	if (B.nt > 0) k_tets<<<grid_for(B.nt, kThreads), kThreads, 0, st>>>(B, P);
 	if (B.ntr > 0) k_tris<<<grid_for(B.ntr, kThreads), kThreads, 0, st>>>(B, P);
 	if (B.ns > 0) k_springs<<<grid_for(B.ns, kThreads), kThreads, 0, st>>>(B, P);
+	if (B.nbw + B.nms > 0) k_cloth_forces<<<grid_for(B.nbw + B.nms, kThreads), kThreads, 0, st>>>(B, P);
 	return cudaGetLastError();
 }
 

@@ -21,7 +21,7 @@ namespace {
 
 struct Inc
 {
-	uint32_t kind;  // 0 tet, 1 tri, 2 spring
+	uint32_t kind;  // 0 tet, 1 tri, 2 spring, 3 stretch/shear triangle, 4 mouse spring
 	uint32_t e;
 	uint32_t a;     // local index of the row vertex in the element
 };
@@ -104,7 +104,8 @@ void free_pattern(Pattern* p)
 }
 
 bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, const uint32_t* tris,
-                   uint32_t ns, const uint32_t* springs, Pattern* out, char* err, size_t errlen)
+                   uint32_t ns, const uint32_t* springs, uint32_t nbw, const uint32_t* bw, uint32_t nms,
+                   const uint32_t* ms, Pattern* out, char* err, size_t errlen)
 {
 	*out = Pattern();
 	if (n == 0)
@@ -158,6 +159,26 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 			if (!check(springs[2 * e + a], "spring", e)) return false;
 			inc_cnt[springs[2 * e + a] + 1]++;
 		}
+	for (uint32_t e = 0; e < nbw; ++e)
+		for (int a = 0; a < 3; ++a)
+		{
+			if (!check(bw[3 * e + a], "stretch/shear triangle", e)) return false;
+			for (int b = 0; b < a; ++b)
+				if (bw[3 * e + a] == bw[3 * e + b])
+				{
+					std::snprintf(err, errlen, "stretch/shear triangle %u repeats vertex %u", e, bw[3 * e + a]);
+					return false;
+				}
+			inc_cnt[bw[3 * e + a] + 1]++;
+		}
+	// a mouse spring may name a vertex twice (weights of a degenerate triangle): each local
+	// index is its own incidence and the slot lists sum both, as the reference's dfdx(i, j) += does
+	for (uint32_t e = 0; e < nms; ++e)
+		for (int a = 0; a < 4; ++a)
+		{
+			if (!check(ms[4 * e + a], "mouse spring", e)) return false;
+			inc_cnt[ms[4 * e + a] + 1]++;
+		}
 	for (uint32_t i = 0; i < n; ++i) inc_cnt[i + 1] += inc_cnt[i];
 	std::vector<Inc> inc(inc_cnt[n]);
 	{
@@ -168,14 +189,31 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 			for (uint32_t a = 0; a < 3; ++a) inc[fill[tris[3 * e + a]]++] = Inc{1, e, a};
 		for (uint32_t e = 0; e < ns; ++e)
 			for (uint32_t a = 0; a < 2; ++a) inc[fill[springs[2 * e + a]]++] = Inc{2, e, a};
+		for (uint32_t e = 0; e < nbw; ++e)
+			for (uint32_t a = 0; a < 3; ++a) inc[fill[bw[3 * e + a]]++] = Inc{3, e, a};
+		for (uint32_t e = 0; e < nms; ++e)
+			for (uint32_t a = 0; a < 4; ++a) inc[fill[ms[4 * e + a]]++] = Inc{4, e, a};
 	}
 
 	auto elem_vertex = [&](const Inc& c, uint32_t b) -> uint32_t {
 		if (c.kind == 0) return tets[4 * c.e + b];
 		if (c.kind == 1) return tris[3 * c.e + b];
-		return springs[2 * c.e + b];
+		if (c.kind == 2) return springs[2 * c.e + b];
+		if (c.kind == 3) return bw[3 * c.e + b];
+		return ms[4 * c.e + b];
 	};
-	auto elem_size = [](uint32_t kind) -> uint32_t { return kind == 0 ? 4u : (kind == 1 ? 3u : 2u); };
+	auto elem_size = [](uint32_t kind) -> uint32_t {
+		static const uint32_t size[5] = {4u, 3u, 2u, 3u, 4u};
+		return size[kind];
+	};
+	// first block and first vector of each explicit kind
+	const uint64_t blk_bw = 9ull * ntr + ns, blk_ms = blk_bw + 9ull * nbw, blk_end = blk_ms + 16ull * nms;
+	const uint64_t vec_bw = 3ull * ntr + ns, vec_ms = vec_bw + 3ull * nbw;
+	if (blk_end >= (1ull << 31))
+	{
+		std::snprintf(err, errlen, "explicit blocks exceed 2^31");
+		return false;
+	}
 
 	// rows: diagonal first, then the other columns ascending
 	std::vector<uint32_t> rowptr(n + 1, 0);
@@ -279,7 +317,9 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 					uint32_t slot = slot_of(i, find_k(i, elem_vertex(c, b)));
 					if (c.kind == 0) tlist[tf[slot]++] = (c.e << 4) | (c.a << 2) | b;
 					else if (c.kind == 1) blist[bf[slot]++] = ((9u * c.e + 3u * c.a + b) << 1);
-					else blist[bf[slot]++] = ((9u * ntr + c.e) << 1) | (c.a != b ? 1u : 0u);
+					else if (c.kind == 2) blist[bf[slot]++] = ((9u * ntr + c.e) << 1) | (c.a != b ? 1u : 0u);
+					else if (c.kind == 3) blist[bf[slot]++] = (uint32_t)(blk_bw + 9u * c.e + 3u * c.a + b) << 1;
+					else blist[bf[slot]++] = (uint32_t)(blk_ms + 16u * c.e + 4u * c.a + b) << 1;
 				}
 			}
 	}
@@ -287,7 +327,7 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 	// vertex lists of right-hand-side contributions
 	std::vector<uint32_t> vtp(P.npad + 1, 0), vbp(P.npad + 1, 0), vtl, vbl;
 	vtl.reserve(4 * (size_t)nt);
-	vbl.reserve(3 * (size_t)ntr + 2 * (size_t)ns);
+	vbl.reserve(3 * (size_t)ntr + 2 * (size_t)ns + 3 * (size_t)nbw + 4 * (size_t)nms);
 	for (uint32_t i = 0; i < n; ++i)
 	{
 		for (uint32_t k = inc_cnt[i]; k < inc_cnt[i + 1]; ++k)
@@ -295,7 +335,9 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 			const Inc& c = inc[k];
 			if (c.kind == 0) vtl.push_back(4u * c.e + c.a);
 			else if (c.kind == 1) vbl.push_back((3u * c.e + c.a) << 1);
-			else vbl.push_back(((3u * ntr + c.e) << 1) | (c.a == 1 ? 1u : 0u));
+			else if (c.kind == 2) vbl.push_back(((3u * ntr + c.e) << 1) | (c.a == 1 ? 1u : 0u));
+			else if (c.kind == 3) vbl.push_back((uint32_t)(vec_bw + 3u * c.e + c.a) << 1);
+			else vbl.push_back((uint32_t)(vec_ms + 4u * c.e + c.a) << 1);
 		}
 		vtp[i + 1] = (uint32_t)vtl.size();
 		vbp[i + 1] = (uint32_t)vbl.size();

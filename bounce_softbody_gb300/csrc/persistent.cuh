@@ -375,6 +375,8 @@ __device__ double team_assemble(Team<CL>& T, const DevBody& B, const BatchParams
 	for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LD>(B, e, sp);
 	for (int e = T.tid(); e < B.ntr; e += T.nthreads()) tri_element<LD>(B, e, sp);
 	for (int e = T.tid(); e < B.ns; e += T.nthreads()) spring_element<LD>(B, e, sp);
+	for (int e = T.tid(); e < B.nbw; e += T.nthreads()) bw_element<LD>(B, e, sp);
+	for (int e = T.tid(); e < B.nms; e += T.nthreads()) mouse_element<LD>(B, e, sp);
 	T.sync();
 	pc.tick(kPhElem);
 	double part = 0.0;

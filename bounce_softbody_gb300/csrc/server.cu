@@ -45,6 +45,9 @@ struct HostDesc
 	std::vector<float> tri_rest, tri_Ex, tri_Ey, tri_Es, tri_nxy, tri_nyx, tri_kd, tri_rho;
 	std::vector<float> spr_L0, spr_ks, spr_kd;
 	std::vector<float> srad, sfric, world;
+	uint32_t nst = 0, nsh = 0, nms = 0;
+	std::vector<uint32_t> st_tris, sh_tris, ms_ids;
+	std::vector<float> st_uv, st_par, sh_uv, sh_par, ms_par;
 	float gravity[3] = {0, 0, 0};
 	// world shapes; their arrays are owned by `owned`, and the pointers in `shapes` point into
 	// those arrays' heap buffers (which stay put when a HostDesc is moved)
@@ -119,6 +122,17 @@ void capture(HostDesc& h, const b3g_body_desc* d)
 		else h.sfric.assign(n, 0.0f);
 	}
 	copy_opt(h.world, d->world_spheres, 5 * (size_t)h.nw);
+	h.nst = d->stretch_count;
+	h.nsh = d->shear_count;
+	h.nms = d->mouse_count;
+	copy_opt(h.st_tris, d->stretch_tris, 3 * (size_t)h.nst);
+	copy_opt(h.st_uv, d->stretch_uv, 6 * (size_t)h.nst);
+	copy_opt(h.st_par, d->stretch_params, 6 * (size_t)h.nst);
+	copy_opt(h.sh_tris, d->shear_tris, 3 * (size_t)h.nsh);
+	copy_opt(h.sh_uv, d->shear_uv, 6 * (size_t)h.nsh);
+	copy_opt(h.sh_par, d->shear_params, 2 * (size_t)h.nsh);
+	copy_opt(h.ms_ids, d->mouse_ids, 4 * (size_t)h.nms);
+	copy_opt(h.ms_par, d->mouse_params, (size_t)kMouseFloats * h.nms);
 	for (int k = 0; k < 3; ++k) h.gravity[k] = d->gravity[k];
 	h.shapes.clear();
 	h.owned.clear();
@@ -187,6 +201,17 @@ b3g_body_desc make_desc(const HostDesc& h)
 	for (int k = 0; k < 3; ++k) d.gravity[k] = h.gravity[k];
 	d.world_shape_count = (uint32_t)h.shapes.size();
 	d.world_shapes = ptr_or_null(h.shapes);
+	d.stretch_count = h.nst;
+	d.stretch_tris = ptr_or_null(h.st_tris);
+	d.stretch_uv = ptr_or_null(h.st_uv);
+	d.stretch_params = ptr_or_null(h.st_par);
+	d.shear_count = h.nsh;
+	d.shear_tris = ptr_or_null(h.sh_tris);
+	d.shear_uv = ptr_or_null(h.sh_uv);
+	d.shear_params = ptr_or_null(h.sh_par);
+	d.mouse_count = h.nms;
+	d.mouse_ids = ptr_or_null(h.ms_ids);
+	d.mouse_params = ptr_or_null(h.ms_par);
 	return d;
 }
 
@@ -198,14 +223,17 @@ b3g_body_desc make_desc(const HostDesc& h)
 uint64_t estimate_bytes(const HostDesc& h)
 {
 	const double n = h.n, nt = h.nt, ntr = h.ntr, ns = h.ns, nw = h.nw;
+	const double nbw = (double)h.nst + h.nsh, nms = h.nms;
 	const double npad = 32.0 * std::ceil(n / 32.0);
-	const double nnzb = h.nt ? 15.0 * n : (h.ntr || h.ns ? 11.0 * n : n);
+	const double nnzb = (h.nt ? 15.0 * n : (h.ntr || h.ns || nbw ? 11.0 * n : n)) + 16 * nms;
 	const double slots = 1.25 * nnzb + 128.0;
 	double b = slots * (4 + 36 + 4 + 2 + 4 + 2);                                       // col, blocks, list heads
 	b += 1.4 * 4.0 * (16 * nt + 9 * ntr + 4 * ns + 4 * nt + 3 * ntr + 2 * ns);          // contribution lists
 	b += npad * (1 + 6 + 6) + n * (6 * 12 + 13 + 12);                                   // row lists, vertex state
 	b += nt * (16 + 36 + 16 + 16 + 64 + 48) + ntr * (16 + 24 + 16 + 144 + 4) + ns * 20;  // elements
 	b += 36 * (9 * ntr + ns) + 12 * (3 * ntr + ns);                                     // explicit blocks
+	b += nbw * (16 + 4 * kBwFloats + 36 * 9 + 12 * 3 + 1.4 * 4 * 12) +                  // cloth forces
+	     nms * (16 + 4 * kMouseFloats + 36 * 16 + 12 * 4 + 1.4 * 4 * 20);
 	b += nw * n * 18 + (nw ? 8 * n : 0);                                                // contacts
 	b += 160 * npad;                                                                    // FP32 solver vectors
 	for (const b3g_world_shape& w : h.shapes)                                           // mesh triangles, voxels

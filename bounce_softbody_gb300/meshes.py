@@ -81,12 +81,12 @@ class BodyDesc:
     tet_kdamp: np.ndarray              # (T,) stiffness damping
     tet_density: np.ndarray            # (T,) density of the mass fixture
     tris: np.ndarray                   # (Tr, 3) uint32
-    tri_Ex: np.ndarray
-    tri_Ey: np.ndarray
-    tri_Es: np.ndarray
-    tri_nuxy: np.ndarray
-    tri_nuyx: np.ndarray
-    tri_kdamp: np.ndarray
+    tri_Ex: Optional[np.ndarray]       # the five element arrays None = mass fixtures only
+    tri_Ey: Optional[np.ndarray]
+    tri_Es: Optional[np.ndarray]
+    tri_nuxy: Optional[np.ndarray]
+    tri_nuyx: Optional[np.ndarray]
+    tri_kdamp: Optional[np.ndarray]
     tri_density: np.ndarray
     springs: np.ndarray                # (S, 2) uint32
     spring_L0: np.ndarray
@@ -98,6 +98,16 @@ class BodyDesc:
     gravity: np.ndarray = dataclasses.field(default_factory=lambda: np.array([0.0, -9.8, 0.0]))
     name: str = "body"
     world_shapes: list = dataclasses.field(default_factory=list)   # WorldShape, after the spheres
+    # Baraff-Witkin cloth forces and mouse springs (b3StretchForceDef, b3ShearForceDef,
+    # b3MouseForceDef). uv None = the defs' Initialize from the initial positions.
+    stretch_tris: np.ndarray = dataclasses.field(default_factory=lambda: _empty_elems(3))
+    stretch_uv: Optional[np.ndarray] = None      # (St, 6): u1, v1, u2, v2, u3, v3
+    stretch_params: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 6)))
+    shear_tris: np.ndarray = dataclasses.field(default_factory=lambda: _empty_elems(3))
+    shear_uv: Optional[np.ndarray] = None
+    shear_params: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 2)))
+    mouse_ids: np.ndarray = dataclasses.field(default_factory=lambda: _empty_elems(4))
+    mouse_params: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 6)))
 
     @property
     def n(self) -> int:
@@ -236,6 +246,65 @@ def cloth_grid(m: int = 128, side: float = 2.0, height: float = 1.0, E_t: float 
         world_spheres=np.array([[*sphere_center, sphere_radius, friction]], np.float64),
         name=name or f"cloth{m}",
     )
+
+
+def bw_cloth(m: int = 10, side: float = 2.0, height: float = 1.0, density: float = 0.2,
+             stretch_ks: float = 1e5, stretch_kd: float = 0.0, shear_ks: float = 0.0, shear_kd: float = 0.0,
+             pinned: str = "edges", mouse: bool = False, mouse_ks: float = 1e5, mouse_kd: float = 1e3,
+             mouse_offset=(0.0, -0.3, 0.0), damping: float = 0.0, name: str = "") -> BodyDesc:
+    """m x m cloth of the reference testbed's kind: triangle mass fixtures of ``density`` and one
+    Baraff-Witkin stretch force per triangle (b_u = b_v = 1, rest frame from Initialize), as
+    UniformBody builds a ClothDef with createElements = false; optionally one shear force per
+    triangle and a mouse spring as BodyDragger makes it: a static particle at the centre of a
+    triangle moved by ``mouse_offset``, weights (1/3, 1/3, 1/3), length 0.
+
+    ``pinned``: "edges" (the border, as PinnedCloth), "row" (the first row, as StretchMapping),
+    "corners" (two corners) or "none".
+    """
+    h = side / (m - 1)
+    jj, ii = np.meshgrid(np.arange(m), np.arange(m), indexing="ij")
+    ii, jj = ii.ravel(), jj.ravel()  # vertex id = i + m*j
+    x = np.stack([-0.5 * side + ii * h, np.full(ii.shape, height), -0.5 * side + jj * h], axis=1)
+    n = m * m
+    types = np.full(n, DYNAMIC, np.int32)
+    if pinned == "edges":
+        types[(ii == 0) | (ii == m - 1) | (jj == 0) | (jj == m - 1)] = STATIC
+    elif pinned == "row":
+        types[jj == 0] = STATIC
+    elif pinned == "corners":
+        types[0] = STATIC
+        types[m - 1] = STATIC
+    ci, cj = np.meshgrid(np.arange(m - 1), np.arange(m - 1), indexing="ij")
+    ci, cj = ci.ravel(), cj.ravel()
+    v00 = ci + m * cj
+    v10 = v00 + 1
+    v01 = v00 + m
+    v11 = v01 + 1
+    tris = np.concatenate([np.stack([v00, v01, v10], 1), np.stack([v10, v01, v11], 1)]).astype(np.uint32)
+    Tr = tris.shape[0]
+    stretch = np.tile([stretch_ks, stretch_kd, 1.0, stretch_ks, stretch_kd, 1.0], (Tr, 1)).astype(np.float64)
+    desc = BodyDesc(
+        x=x, v=np.zeros_like(x), type=types, damping=np.full(n, damping),
+        tets=_empty_elems(4), tet_E=_z(), tet_nu=_z(), tet_kdamp=_z(), tet_density=_z(),
+        tris=tris, tri_Ex=None, tri_Ey=None, tri_Es=None, tri_nuxy=None, tri_nuyx=None, tri_kdamp=None,
+        tri_density=np.full(Tr, density),
+        springs=_empty_elems(2), spring_L0=_z(), spring_ks=_z(), spring_kd=_z(),
+        stretch_tris=tris.copy(), stretch_params=stretch,
+        name=name or f"bwcloth{m}",
+    )
+    if shear_ks > 0.0 or shear_kd > 0.0:
+        desc.shear_tris = tris.copy()
+        desc.shear_params = np.tile([shear_ks, shear_kd], (Tr, 1)).astype(np.float64)
+    if mouse:
+        t = tris[Tr // 2 + (m - 1) // 2]
+        c = x[t.astype(np.int64)].mean(axis=0) + np.asarray(mouse_offset, np.float64)
+        desc.x = np.concatenate([x, c[None, :]])
+        desc.v = np.zeros_like(desc.x)
+        desc.type = np.concatenate([types, np.array([STATIC], np.int32)])
+        desc.damping = np.full(n + 1, damping)
+        desc.mouse_ids = np.array([[n, t[0], t[1], t[2]]], np.uint32)
+        desc.mouse_params = np.array([[1.0 / 3.0, 1.0 / 3.0, 1.0 - 2.0 / 3.0, mouse_ks, mouse_kd, 0.0]])
+    return desc
 
 
 def batch_bodies(count: int = 512, lo: int = 4, hi: int = 40, seed: int = 3, spacing: float = 0.1,

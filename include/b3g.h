@@ -135,7 +135,8 @@ typedef struct b3g_body_desc
 	const float* tet_stiffness_damping; /* ::stiffnessDamping, NULL = zero */
 	const float* tet_density;      /* b3TetrahedronFixtureDef::density, NULL = zero */
 
-	uint32_t tri_count;
+	uint32_t tri_count;            /* b3TriangleFixtures; with the five material arrays also
+	                                  b3TriangleElementForces, all five NULL = mass fixtures only */
 	const uint32_t* tris;          /* 3 vertex ids per triangle */
 	const float* tri_rest;         /* 9 per triangle, NULL = positions */
 	const float* tri_young_x;      /* b3TriangleElementForceDef::youngModulusX */
@@ -162,6 +163,23 @@ typedef struct b3g_body_desc
 	uint32_t world_shape_count;    /* further static world fixtures of any shape; together with the
 	                                  world spheres at most 16 fixtures, spheres first */
 	const b3g_world_shape* world_shapes;
+
+	/* Baraff-Witkin cloth forces (src/bounce_softbody/dynamics/forces/stretch_force.cpp,
+	 * shear_force.cpp) and mouse springs (mouse_force.cpp). uv: u1, v1, u2, v2, u3, v3 per
+	 * element as b3StretchForceDef / b3ShearForceDef hold them; NULL = Initialize() from the
+	 * elements' positions. */
+	uint32_t stretch_count;
+	const uint32_t* stretch_tris;    /* 3 vertex ids per element */
+	const float* stretch_uv;         /* 6 per element or NULL */
+	const float* stretch_params;     /* 6 per element: stiffness_u, damping_stiffness_u, b_u,
+	                                    stiffness_v, damping_stiffness_v, b_v */
+	uint32_t shear_count;
+	const uint32_t* shear_tris;      /* 3 vertex ids per element */
+	const float* shear_uv;           /* 6 per element or NULL */
+	const float* shear_params;       /* 2 per element: stiffness, dampingStiffness */
+	uint32_t mouse_count;
+	const uint32_t* mouse_ids;       /* 4 per element: p1 (the dragged particle), p2, p3, p4 */
+	const float* mouse_params;       /* 6 per element: w2, w3, w4, stiffness, dampingStiffness, length */
 } b3g_body_desc;
 
 /* Solver settings of one step. b3g_solver_config_default() gives the reference's: one Newton

@@ -6,21 +6,25 @@
 // state lives on the GPU; particles read it back on demand.
 //
 // What maps where:
-//   b3Body::CreateParticle / CreateForce / CreateTetrahedron / CreateTriangle / CreateSphere /
-//   CreateFixture / SetGravity      recorded on the host; the device body (b3g_body_create) is
-//                                   built at the first Step and rebuilt after topology changes
+//   b3Body::CreateParticle / CreateForce / DestroyForce / CreateTetrahedron / CreateTriangle /
+//   CreateSphere / CreateFixture / SetGravity
+//                                   recorded on the host; the device body (b3g_body_create) is
+//                                   built at the first Step and rebuilt after topology changes.
+//                                   Forces: tetrahedron and triangle elements, springs,
+//                                   Baraff-Witkin stretch and shear, mouse springs.
 //   b3Body::Step                    b3g_body_step (uploads pending forces / translations first)
 //   b3Particle::Get/SetPosition, Get/SetVelocity, ApplyForce, ApplyTranslation, SetType
 //                                   b3g_body_get_state / set_state / apply_* / set_types
 //   b3_forceSolver*Iterations       b3Body::GetStepStats()
 // Extensions (no reference counterpart): SetSolverTolerance (the reference's Step always runs the
 // PCG at FLT_EPSILON), SetPrecision, SetPreconditioner.
-// Not provided (outside the implicit step): ray casts, debug draw, stretch / shear / mouse forces,
-// non-sphere world shapes.
+// Not provided (outside the implicit step): ray casts, debug draw, DestroyParticle and the other
+// Destroy* calls of fixtures.
 #pragma once
 
 #include "b3g.h"
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -43,6 +47,12 @@ struct b3Vec3
 	scalar x, y, z;
 };
 inline b3Vec3 operator*(scalar s, const b3Vec3& v) { return b3Vec3(s * v.x, s * v.y, s * v.z); }
+inline scalar b3Dot(const b3Vec3& a, const b3Vec3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline b3Vec3 b3Cross(const b3Vec3& a, const b3Vec3& b)
+{
+	return b3Vec3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+inline scalar b3Length(const b3Vec3& v) { return std::sqrt(b3Dot(v, v)); }
 inline scalar b3Distance(const b3Vec3& a, const b3Vec3& b)
 {
 	b3Vec3 d = a - b;
@@ -143,6 +153,54 @@ struct b3TriangleElementForceDef : public b3ForceDef
 	scalar youngModulusX = 100, youngModulusY = 100, shearModulus = 50;
 	scalar poissonRationXY = 0.2f, poissonRationYX = 0.2f;
 	scalar stiffnessDamping = 0;
+};
+
+// Baraff-Witkin stretch and shear triangles (stretch_force.h, shear_force.h): rest (u, v)
+// coordinates of the three particles, from Initialize or set directly.
+struct b3StretchForceDef : public b3ForceDef
+{
+	b3StretchForceDef() { type = e_stretchForce; }
+	// stretch_force.cpp:36-60
+	void Initialize(const b3Vec3& A, const b3Vec3& B, const b3Vec3& C)
+	{
+		b3Vec3 AB = B - A, AC = C - A;
+		u1 = 0;
+		v1 = 0;
+		u2 = b3Length(AB);
+		v2 = 0;
+		b3Vec3 n_AB(AB.x / u2, AB.y / u2, AB.z / u2);
+		u3 = b3Dot(AC, n_AB);
+		v3 = b3Length(b3Cross(AB, AC)) / u2;
+	}
+	b3Particle *p1 = nullptr, *p2 = nullptr, *p3 = nullptr;
+	scalar u1 = 0, v1 = 0, u2 = 0, v2 = 0, u3 = 0, v3 = 0;
+	scalar stiffness_u = 0, damping_stiffness_u = 0, b_u = 1;
+	scalar stiffness_v = 0, damping_stiffness_v = 0, b_v = 1;
+};
+
+struct b3ShearForceDef : public b3ForceDef
+{
+	b3ShearForceDef() { type = e_shearForce; }
+	// shear_force.cpp:25-49 (the stretch definition's frame)
+	void Initialize(const b3Vec3& A, const b3Vec3& B, const b3Vec3& C)
+	{
+		b3StretchForceDef s;
+		s.Initialize(A, B, C);
+		u1 = s.u1; v1 = s.v1; u2 = s.u2; v2 = s.v2; u3 = s.u3; v3 = s.v3;
+	}
+	b3Particle *p1 = nullptr, *p2 = nullptr, *p3 = nullptr;
+	scalar u1 = 0, v1 = 0, u2 = 0, v2 = 0, u3 = 0, v3 = 0;
+	scalar stiffness = 0, dampingStiffness = 0;
+};
+
+// Mouse spring (mouse_force.h): particle 1 held at `length` from the point with barycentric
+// weights w2, w3, w4 on the triangle (p2, p3, p4).
+struct b3MouseForceDef : public b3ForceDef
+{
+	b3MouseForceDef() { type = e_mouseForce; }
+	b3Particle *p1 = nullptr, *p2 = nullptr, *p3 = nullptr, *p4 = nullptr;
+	scalar w2 = 0, w3 = 0, w4 = 0;
+	scalar length = 0, stiffness = 0, dampingStiffness = 0;
 };
 
 struct b3TetrahedronElementForceDef : public b3ForceDef
@@ -335,21 +393,61 @@ public:
 		case e_triangleElementForce:
 		{
 			const b3TriangleElementForceDef& d = (const b3TriangleElementForceDef&)def;
-			f->index = (uint32)m_triEx.size();
-			const b3Particle* ps[3] = {d.p1, d.p2, d.p3};
+			const uint32 a[3] = {d.p1->m_index, d.p2->m_index, d.p3->m_index};
 			const b3Vec3 vs[3] = {d.v1, d.v2, d.v3};
-			for (int k = 0; k < 3; ++k)
+			size_t e = find_tri(a, true);  // a mass fixture of the same particles without an element
+			if (e == m_triEx.size())
 			{
-				m_tris.push_back(ps[k]->m_index);
-				push3(m_triRest, vs[k]);
+				for (int k = 0; k < 3; ++k) m_tris.push_back(a[k]);
+				m_triRest.resize(m_triRest.size() + 9);
+				m_triEx.push_back(0);
+				m_triEy.push_back(0);
+				m_triEs.push_back(0);
+				m_triNxy.push_back(0);
+				m_triNyx.push_back(0);
+				m_triKd.push_back(0);
+				m_triDensity.push_back(0);
+				m_triElem.push_back(0);
+				m_triFix.push_back(0);
 			}
-			m_triEx.push_back(d.youngModulusX);
-			m_triEy.push_back(d.youngModulusY);
-			m_triEs.push_back(d.shearModulus);
-			m_triNxy.push_back(d.poissonRationXY);
-			m_triNyx.push_back(d.poissonRationYX);
-			m_triKd.push_back(d.stiffnessDamping);
-			m_triDensity.push_back(0);
+			for (int k = 0; k < 3; ++k)
+				for (int c = 0; c < 3; ++c) m_triRest[9 * e + 3 * k + c] = (&vs[k].x)[c];
+			m_triEx[e] = d.youngModulusX;
+			m_triEy[e] = d.youngModulusY;
+			m_triEs[e] = d.shearModulus;
+			m_triNxy[e] = d.poissonRationXY;
+			m_triNyx[e] = d.poissonRationYX;
+			m_triKd[e] = d.stiffnessDamping;
+			m_triElem[e] = 1;
+			f->index = (uint32)e;
+			break;
+		}
+		case e_stretchForce:
+		{
+			const b3StretchForceDef& d = (const b3StretchForceDef&)def;
+			f->index = (uint32)m_stParams.size() / 6;
+			for (const b3Particle* p : {d.p1, d.p2, d.p3}) m_stTris.push_back(p->m_index);
+			for (scalar c : {d.u1, d.v1, d.u2, d.v2, d.u3, d.v3}) m_stUv.push_back(c);
+			for (scalar c : {d.stiffness_u, d.damping_stiffness_u, d.b_u, d.stiffness_v, d.damping_stiffness_v, d.b_v})
+				m_stParams.push_back(c);
+			break;
+		}
+		case e_shearForce:
+		{
+			const b3ShearForceDef& d = (const b3ShearForceDef&)def;
+			f->index = (uint32)m_shParams.size() / 2;
+			for (const b3Particle* p : {d.p1, d.p2, d.p3}) m_shTris.push_back(p->m_index);
+			for (scalar c : {d.u1, d.v1, d.u2, d.v2, d.u3, d.v3}) m_shUv.push_back(c);
+			m_shParams.push_back(d.stiffness);
+			m_shParams.push_back(d.dampingStiffness);
+			break;
+		}
+		case e_mouseForce:
+		{
+			const b3MouseForceDef& d = (const b3MouseForceDef&)def;
+			f->index = (uint32)m_msParams.size() / 6;
+			for (const b3Particle* p : {d.p1, d.p2, d.p3, d.p4}) m_msIds.push_back(p->m_index);
+			for (scalar c : {d.w2, d.w3, d.w4, d.stiffness, d.dampingStiffness, d.length}) m_msParams.push_back(c);
 			break;
 		}
 		case e_springForce:
@@ -365,16 +463,64 @@ public:
 		}
 		default:
 			delete f;
-			throw std::invalid_argument("b3g: this force type is not part of the implicit step on the GPU");
+			throw std::invalid_argument("b3g: unknown force type");
 		}
 		m_forceHandles.push_back(f);
 		m_topologyDirty = true;
 		return f;
 	}
 
-	// Tetrahedron / triangle fixtures carry the density of the lumped mass (b3Body::ResetMass).
-	// The element with the same particles takes the density; a fixture without an element force
-	// contributes mass only through an element-less entry, which the GPU body does not model.
+	// b3Body::DestroyForce: the force's entries leave the arrays; handles behind it move down.
+	void DestroyForce(b3Force* force)
+	{
+		auto it = std::find(m_forceHandles.begin(), m_forceHandles.end(), force);
+		if (it == m_forceHandles.end()) throw std::invalid_argument("b3g: DestroyForce of an unknown force");
+		const uint32 e = force->index;
+		auto drop = [e](auto& v, size_t w) { v.erase(v.begin() + w * e, v.begin() + w * (e + 1)); };
+		bool shift = true;
+		switch (force->type)
+		{
+		case e_tetrahedronElementForce:
+			drop(m_tets, 4); drop(m_tetRest, 12); drop(m_tetE, 1); drop(m_tetNu, 1); drop(m_tetKd, 1);
+			drop(m_tetDensity, 1);
+			break;
+		case e_triangleElementForce:
+			if (m_triFix[e])
+			{
+				// the mass fixture stays
+				m_triElem[e] = 0;
+				m_triEx[e] = m_triEy[e] = m_triEs[e] = m_triNxy[e] = m_triNyx[e] = m_triKd[e] = 0;
+				shift = false;
+				break;
+			}
+			drop(m_tris, 3); drop(m_triRest, 9); drop(m_triEx, 1); drop(m_triEy, 1); drop(m_triEs, 1);
+			drop(m_triNxy, 1); drop(m_triNyx, 1); drop(m_triKd, 1); drop(m_triDensity, 1); drop(m_triElem, 1);
+			drop(m_triFix, 1);
+			break;
+		case e_springForce:
+			drop(m_springs, 2); drop(m_sprL0, 1); drop(m_sprKs, 1); drop(m_sprKd, 1);
+			break;
+		case e_stretchForce:
+			drop(m_stTris, 3); drop(m_stUv, 6); drop(m_stParams, 6);
+			break;
+		case e_shearForce:
+			drop(m_shTris, 3); drop(m_shUv, 6); drop(m_shParams, 2);
+			break;
+		case e_mouseForce:
+			drop(m_msIds, 4); drop(m_msParams, 6);
+			break;
+		}
+		if (shift)
+			for (b3Force* h : m_forceHandles)
+				if (h != force && h->type == force->type && h->index > e) --h->index;
+		m_forceHandles.erase(it);
+		delete force;
+		m_topologyDirty = true;
+	}
+
+	// Tetrahedron fixtures carry the density of the lumped mass (b3Body::ResetMass) and pair with
+	// the element force of the same particles, which must exist (a tetrahedron fixture alone is
+	// not modelled; destroying the element drops its fixture's mass too).
 	void CreateTetrahedron(const b3TetrahedronFixtureDef& def)
 	{
 		uint32 a[4] = {def.p1->m_index, def.p2->m_index, def.p3->m_index, def.p4->m_index};
@@ -387,17 +533,25 @@ public:
 			}
 		throw std::invalid_argument("b3g: CreateTetrahedron needs the tetrahedron element force created first");
 	}
+	// A triangle fixture pairs with the element force of the same particles when there is one;
+	// otherwise it is a mass fixture of its own (cloth held by stretch and shear forces).
 	void CreateTriangle(const b3TriangleFixtureDef& def)
 	{
-		uint32 a[3] = {def.p1->m_index, def.p2->m_index, def.p3->m_index};
-		for (size_t e = 0; e < m_triEx.size(); ++e)
-			if (same_set(&m_tris[3 * e], a, 3))
-			{
-				m_triDensity[e] = def.density;
-				m_topologyDirty = true;
-				return;
-			}
-		throw std::invalid_argument("b3g: CreateTriangle needs the triangle element force created first");
+		const uint32 a[3] = {def.p1->m_index, def.p2->m_index, def.p3->m_index};
+		size_t e = find_tri(a, false);
+		if (e == m_triEx.size())
+		{
+			for (int k = 0; k < 3; ++k) m_tris.push_back(a[k]);
+			for (const b3Vec3* v : {&def.v1, &def.v2, &def.v3}) push3(m_triRest, *v);
+			for (std::vector<float>* v : {&m_triEx, &m_triEy, &m_triEs, &m_triNxy, &m_triNyx, &m_triKd})
+				v->push_back(0);
+			m_triDensity.push_back(0);
+			m_triElem.push_back(0);
+			m_triFix.push_back(0);
+		}
+		m_triDensity[e] = def.density;
+		m_triFix[e] = 1;
+		m_topologyDirty = true;
 	}
 	void CreateSphere(const b3SphereFixtureDef& def)
 	{
@@ -583,6 +737,14 @@ private:
 		return true;
 	}
 	scalar mass_of(size_t i) const { return i < m_mass.size() ? m_mass[i] : 0; }
+	// the triangle entry of these particles that lacks an element (want_fixture_only) or a
+	// fixture; the entry count when there is none
+	size_t find_tri(const uint32* a, bool want_fixture_only) const
+	{
+		for (size_t e = 0; e < m_triEx.size(); ++e)
+			if (same_set(&m_tris[3 * e], a, 3) && (want_fixture_only ? !m_triElem[e] : !m_triFix[e])) return e;
+		return m_triEx.size();
+	}
 
 	// device -> host state, when the host copy is stale
 	void fetch()
@@ -627,13 +789,29 @@ private:
 		d.tri_count = (uint32)m_triEx.size();
 		d.tris = m_tris.data();
 		d.tri_rest = m_triRest.data();
-		d.tri_young_x = m_triEx.data();
-		d.tri_young_y = m_triEy.data();
-		d.tri_shear = m_triEs.data();
-		d.tri_poisson_xy = m_triNxy.data();
-		d.tri_poisson_yx = m_triNyx.data();
-		d.tri_stiffness_damping = m_triKd.data();
+		// without any element the triangles are mass fixtures only (no element work on the GPU);
+		// mixed bodies give fixture-only entries zero stiffness
+		if (std::find(m_triElem.begin(), m_triElem.end(), 1) != m_triElem.end())
+		{
+			d.tri_young_x = m_triEx.data();
+			d.tri_young_y = m_triEy.data();
+			d.tri_shear = m_triEs.data();
+			d.tri_poisson_xy = m_triNxy.data();
+			d.tri_poisson_yx = m_triNyx.data();
+			d.tri_stiffness_damping = m_triKd.data();
+		}
 		d.tri_density = m_triDensity.data();
+		d.stretch_count = (uint32)m_stParams.size() / 6;
+		d.stretch_tris = m_stTris.data();
+		d.stretch_uv = m_stUv.data();
+		d.stretch_params = m_stParams.data();
+		d.shear_count = (uint32)m_shParams.size() / 2;
+		d.shear_tris = m_shTris.data();
+		d.shear_uv = m_shUv.data();
+		d.shear_params = m_shParams.data();
+		d.mouse_count = (uint32)m_msParams.size() / 6;
+		d.mouse_ids = m_msIds.data();
+		d.mouse_params = m_msParams.data();
 		d.spring_count = (uint32)m_sprL0.size();
 		d.springs = m_springs.data();
 		d.spring_rest_length = m_sprL0.data();
@@ -726,7 +904,10 @@ private:
 	std::vector<uint32> m_tets, m_tris, m_springs;
 	std::vector<float> m_tetRest, m_tetE, m_tetNu, m_tetKd, m_tetDensity;
 	std::vector<float> m_triRest, m_triEx, m_triEy, m_triEs, m_triNxy, m_triNyx, m_triKd, m_triDensity;
+	std::vector<uint8_t> m_triElem, m_triFix;  // per triangle entry: has an element / a fixture
 	std::vector<float> m_sprL0, m_sprKs, m_sprKd;
+	std::vector<uint32> m_stTris, m_shTris, m_msIds;
+	std::vector<float> m_stUv, m_stParams, m_shUv, m_shParams, m_msParams;
 	std::vector<float> m_sphereRadius, m_sphereFriction, m_world;
 	struct ShapeData
 	{

@@ -15,6 +15,9 @@
  *   - tetrahedron element (K0, rotation, forces) src/bounce_softbody/dynamics/forces/tetrahedron_element_force.cpp:37-464
  *   - triangle element                           src/bounce_softbody/dynamics/forces/triangle_element_force.cpp:30-468
  *   - spring                                     src/bounce_softbody/dynamics/forces/spring_force.cpp:61-143
+ *   - stretch (Baraff-Witkin), (u, v) Initialize src/bounce_softbody/dynamics/forces/stretch_force.cpp:36-388
+ *   - shear (Baraff-Witkin)                      src/bounce_softbody/dynamics/forces/shear_force.cpp:25-244
+ *   - mouse spring                               src/bounce_softbody/dynamics/forces/mouse_force.cpp:25-245
  *   - sphere contact force and friction          src/bounce_softbody/dynamics/contacts/sphere_shape_contact.cpp:53-189
  *   - sphere shape collide                       src/bounce_softbody/collision/shapes/sphere_shape.cpp:50-77
  *   - contact creation / destruction             src/bounce_softbody/dynamics/contact_manager.cpp:65-146
@@ -219,6 +222,16 @@ typedef struct
 	double gravity[3];
 	uint32_t world_shape_count;
 	const struct b3o_shape* world_shapes;
+	/* cloth forces; uv null = Initialize from the initial positions */
+	uint32_t stretch_count;
+	const uint32_t* stretch_tris;
+	const double *stretch_uv, *stretch_params; /* 6, 6 per force: ks_u, kd_u, b_u, ks_v, kd_v, b_v */
+	uint32_t shear_count;
+	const uint32_t* shear_tris;
+	const double *shear_uv, *shear_params;     /* 6, 2 per force: ks, kd */
+	uint32_t mouse_count;
+	const uint32_t* mouse_ids;                 /* 4 per force */
+	const double* mouse_params;                /* 6 per force: w2, w3, w4, ks, kd, length */
 } b3o_desc;
 
 /* a world shape in the restatement's precision; lo / hi is the fixture AABB */
@@ -257,6 +270,25 @@ typedef struct
 
 enum { STATIC = 0, KINEMATIC = 1, DYNAMIC = 2 };
 
+/* b3StretchForce / b3ShearForce members (stretch_force.h, shear_force.h) */
+typedef struct bwforce
+{
+	uint32_t p[3];
+	int shear;
+	real alpha, inv_det, du1, dv1, du2, dv2;
+	real dwudx[3], dwvdx[3];
+	real ks_u, kd_u, b_u, ks_v, kd_v, b_v; /* shear: ks_u, kd_u */
+	uint32_t slot[9];                      /* (row i, column j) at i + 3 j */
+} bwforce;
+
+/* b3MouseForce members (mouse_force.h) */
+typedef struct mforce
+{
+	uint32_t p[4];
+	real w2, w3, w4, ks, kd, L0;
+	uint32_t slot[16];                     /* (row i, column j) at i + 4 j */
+} mforce;
+
 typedef struct
 {
 	uint32_t n;
@@ -283,6 +315,13 @@ typedef struct
 	uint32_t ns;
 	uint32_t* spr;
 	real *L0, *ks, *kd;
+
+	int tri_elements; /* 0: triangles are mass fixtures only */
+	uint32_t nbw;     /* stretch forces first, then shear forces */
+	uint32_t nst;
+	struct bwforce* bw;
+	uint32_t nms;
+	struct mforce* ms;
 
 	real *srad, *sfric;
 	uint32_t nw;
@@ -410,6 +449,52 @@ static void tri_reset(body_t* B, uint32_t e, v3 p1, v3 p2, v3 p3, real Ex, real 
 		}
 }
 
+/* stretch_force.cpp:36-60 / shear_force.cpp:25-49 Initialize, then the constructors
+ * (stretch_force.cpp:62-107, shear_force.cpp:51-92) */
+static void bw_setup(bwforce* F, const uint32_t* ids, const double* uvin, const double* x, int shear, const double* par)
+{
+	real uv[6];
+	for (int k = 0; k < 3; ++k) F->p[k] = ids[k];
+	F->shear = shear;
+	if (uvin)
+		for (int k = 0; k < 6; ++k) uv[k] = (real)uvin[k];
+	else
+	{
+		v3 A = D3(x + 3 * ids[0]), Bv = D3(x + 3 * ids[1]), C = D3(x + 3 * ids[2]);
+		v3 AB = sub(Bv, A), AC = sub(C, A);
+		uv[0] = 0;
+		uv[1] = 0;
+		uv[2] = len(AB);
+		uv[3] = 0;
+		v3 n_AB = V(AB.x / uv[2], AB.y / uv[2], AB.z / uv[2]); /* vec3.h:152-155: per component */
+		real a2 = len(cross(AB, AC));
+		uv[4] = dot(AC, n_AB);
+		uv[5] = a2 / uv[2];
+	}
+	F->du1 = uv[2] - uv[0];
+	F->dv1 = uv[3] - uv[1];
+	F->du2 = uv[4] - uv[0];
+	F->dv2 = uv[5] - uv[1];
+	real det = F->du1 * F->dv2 - F->du2 * F->dv1;
+	F->inv_det = (real)1 / det;
+	F->dwudx[0] = F->inv_det * (F->dv1 - F->dv2);
+	F->dwudx[1] = F->inv_det * F->dv2;
+	F->dwudx[2] = -F->inv_det * F->dv1;
+	F->dwvdx[0] = F->inv_det * (F->du2 - F->du1);
+	F->dwvdx[1] = -F->inv_det * F->du2;
+	F->dwvdx[2] = F->inv_det * F->du1;
+	F->alpha = (real)0.5 * (det < 0 ? -det : det);
+	F->ks_u = (real)par[0];
+	F->kd_u = (real)par[1];
+	if (!shear)
+	{
+		F->b_u = (real)par[2];
+		F->ks_v = (real)par[3];
+		F->kd_v = (real)par[4];
+		F->b_v = (real)par[5];
+	}
+}
+
 static void body_free(body_t* B);
 
 static body_t* body_create(const b3o_desc* d)
@@ -463,6 +548,7 @@ static body_t* body_create(const b3o_desc* d)
 	}
 
 	B->ntr = d->tri_count;
+	B->tri_elements = d->tri_Ex != NULL;
 	B->tri = xcalloc(3 * (size_t)B->ntr, sizeof(uint32_t));
 	B->tri_x = xcalloc(3 * (size_t)B->ntr, sizeof(v2));
 	B->invS = xcalloc(B->ntr, sizeof(m22));
@@ -478,8 +564,9 @@ static body_t* body_create(const b3o_desc* d)
 			p[k] = d->tri_rest ? D3(d->tri_rest + 9 * e + 3 * k) : D3(d->x + 3 * d->tris[3 * e + k]);
 		}
 		B->trkd[e] = d->tri_kdamp ? (real)d->tri_kdamp[e] : 0;
-		tri_reset(B, e, p[0], p[1], p[2], (real)d->tri_Ex[e], (real)d->tri_Ey[e], (real)d->tri_Es[e],
-		          (real)d->tri_nuxy[e], (real)d->tri_nuyx[e]);
+		if (B->tri_elements)
+			tri_reset(B, e, p[0], p[1], p[2], (real)d->tri_Ex[e], (real)d->tri_Ey[e], (real)d->tri_Es[e],
+			          (real)d->tri_nuxy[e], (real)d->tri_nuyx[e]);
 		/* triangle_fixture.cpp:33-36 area = |cross| / 2 */
 		tarea[e] = (real)0.5 * len(cross(sub(p[1], p[0]), sub(p[2], p[0])));
 	}
@@ -496,6 +583,33 @@ static body_t* body_create(const b3o_desc* d)
 		B->L0[e] = (real)d->spring_L0[e];
 		B->ks[e] = (real)d->spring_ks[e];
 		B->kd[e] = (real)d->spring_kd[e];
+	}
+
+	B->nst = d->stretch_count;
+	B->nbw = d->stretch_count + d->shear_count;
+	B->bw = xcalloc(B->nbw, sizeof(bwforce));
+	for (uint32_t e = 0; e < B->nbw; ++e)
+	{
+		int shear = e >= B->nst;
+		uint32_t k = shear ? e - B->nst : e;
+		const uint32_t* ids = (shear ? d->shear_tris : d->stretch_tris) + 3 * k;
+		const double* uv = shear ? d->shear_uv : d->stretch_uv;
+		bw_setup(&B->bw[e], ids, uv ? uv + 6 * k : NULL, d->x, shear,
+		         shear ? d->shear_params + 2 * k : d->stretch_params + 6 * k);
+	}
+	B->nms = d->mouse_count;
+	B->ms = xcalloc(B->nms, sizeof(mforce));
+	for (uint32_t e = 0; e < B->nms; ++e)
+	{
+		mforce* F = &B->ms[e];
+		const double* c = d->mouse_params + 6 * e;
+		for (int k = 0; k < 4; ++k) F->p[k] = d->mouse_ids[4 * e + k];
+		F->w2 = (real)c[0];
+		F->w3 = (real)c[1];
+		F->w4 = (real)c[2];
+		F->ks = (real)c[3];
+		F->kd = (real)c[4];
+		F->L0 = (real)c[5];
 	}
 
 	/* body.cpp:394-466 ResetMass, fixture lists walked newest first */
@@ -554,7 +668,8 @@ static body_t* body_create(const b3o_desc* d)
 	B->c_normal = xcalloc(nc, sizeof(v3));
 
 	/* block pattern: diagonal + every element pair */
-	size_t npairs = (size_t)n + 16 * (size_t)B->nt + 9 * (size_t)B->ntr + 4 * (size_t)B->ns;
+	size_t npairs = (size_t)n + 16 * (size_t)B->nt + 9 * (size_t)B->ntr + 4 * (size_t)B->ns + 9 * (size_t)B->nbw +
+	                16 * (size_t)B->nms;
 	uint64_t* keys = xcalloc(npairs, sizeof(uint64_t));
 	size_t kk = 0;
 	for (uint32_t i = 0; i < n; ++i) keys[kk++] = ((uint64_t)i << 32) | i;
@@ -567,6 +682,12 @@ static body_t* body_create(const b3o_desc* d)
 	for (uint32_t e = 0; e < B->ns; ++e)
 		for (int a = 0; a < 2; ++a)
 			for (int b = 0; b < 2; ++b) keys[kk++] = ((uint64_t)B->spr[2 * e + a] << 32) | B->spr[2 * e + b];
+	for (uint32_t e = 0; e < B->nbw; ++e)
+		for (int a = 0; a < 3; ++a)
+			for (int b = 0; b < 3; ++b) keys[kk++] = ((uint64_t)B->bw[e].p[a] << 32) | B->bw[e].p[b];
+	for (uint32_t e = 0; e < B->nms; ++e)
+		for (int a = 0; a < 4; ++a)
+			for (int b = 0; b < 4; ++b) keys[kk++] = ((uint64_t)B->ms[e].p[a] << 32) | B->ms[e].p[b];
 	qsort(keys, kk, sizeof(uint64_t), cmp_u64);
 	size_t u = 0;
 	for (size_t k = 0; k < kk; ++k)
@@ -602,6 +723,12 @@ static body_t* body_create(const b3o_desc* d)
 		B->spr_slot[4 * e + 2] = find_slot(B, i2, i1);
 		B->spr_slot[4 * e + 3] = find_slot(B, i2, i2);
 	}
+	for (uint32_t e = 0; e < B->nbw; ++e)
+		for (int a = 0; a < 3; ++a)
+			for (int b = 0; b < 3; ++b) B->bw[e].slot[a + 3 * b] = find_slot(B, B->bw[e].p[a], B->bw[e].p[b]);
+	for (uint32_t e = 0; e < B->nms; ++e)
+		for (int a = 0; a < 4; ++a)
+			for (int b = 0; b < 4; ++b) B->ms[e].slot[a + 4 * b] = find_slot(B, B->ms[e].p[a], B->ms[e].p[b]);
 
 	B->dfdx = xcalloc(B->nnzb, sizeof(m33));
 	B->dfdv = xcalloc(B->nnzb, sizeof(m33));
@@ -625,7 +752,7 @@ static void body_free(body_t* B)
 	free(B->ws);
 	void* ptrs[] = {B->x, B->v, B->fext, B->trans, B->type, B->mass, B->invmass, B->damping, B->tet,
 	                B->tet_rest, B->invE, B->K, B->q, B->tkd, B->tri, B->tri_x, B->invS, B->K2, B->trkd,
-	                B->spr, B->L0, B->ks, B->kd, B->srad, B->sfric, B->c_exists,
+	                B->spr, B->L0, B->ks, B->kd, B->bw, B->ms, B->srad, B->sfric, B->c_exists,
 	                B->c_apply, B->c_normalForce, B->c_normal, B->rowptr, B->col, B->tet_slot, B->tri_slot,
 	                B->spr_slot, B->diag, B->dfdx, B->dfdv, B->A, B->x0, B->v0, B->fe, B->y, B->xx, B->vv,
 	                B->fi, B->b, B->pb, B->py, B->w, B->tmp, B->r, B->d, B->qv, B->s, B->Minv, B->Mval, B->S};
@@ -825,6 +952,145 @@ static void spring_apply(body_t* B, uint32_t e)
 		B->dfdv[sl[1]] = madd(B->dfdv[sl[1]], K12);
 		B->dfdv[sl[2]] = madd(B->dfdv[sl[2]], K12);
 		B->dfdv[sl[3]] = madd(B->dfdv[sl[3]], K11);
+	}
+}
+
+/* one direction of stretch_force.cpp:121-388: the u part (142-270) with g = dwu/dx, or the v part */
+static void stretch_dir(body_t* B, const bwforce* F, v3 w, const real* g, real ks, real kd, real b, const v3* vs)
+{
+	real L = len(w);
+	if (!(L > 0)) return;
+	real inv_len = (real)1 / L;
+	v3 n = scl(inv_len, w);
+	m33 I = mdiag(1);
+	v3 dC[3];
+	for (int i = 0; i < 3; ++i) dC[i] = scl(F->alpha * g[i], n);
+	if (ks > 0)
+	{
+		real C = F->alpha * (L - b);
+		for (int i = 0; i < 3; ++i) B->fi[F->p[i]] = add(B->fi[F->p[i]], scl(-ks * C, dC[i]));
+		for (int i = 0; i < 3; ++i)
+			for (int j = 0; j < 3; ++j)
+			{
+				m33 K = outer(dC[i], dC[j]);
+				if (L > b) /* only while the eigenvalues stay positive */
+					K = madd(K, mscl(C, mscl(F->alpha * inv_len * g[i] * g[j], msub(I, outer(n, n)))));
+				uint32_t s = F->slot[i + 3 * j];
+				B->dfdx[s] = madd(B->dfdx[s], mscl(-ks, K));
+			}
+	}
+	if (kd > 0)
+	{
+		real dCdt = 0;
+		for (int i = 0; i < 3; ++i) dCdt += dot(dC[i], vs[i]);
+		for (int i = 0; i < 3; ++i) B->fi[F->p[i]] = add(B->fi[F->p[i]], scl(-kd * dCdt, dC[i]));
+		for (int i = 0; i < 3; ++i)
+			for (int j = 0; j < 3; ++j)
+			{
+				uint32_t s = F->slot[i + 3 * j];
+				B->dfdv[s] = madd(B->dfdv[s], mscl(-kd, outer(dC[i], dC[j])));
+			}
+	}
+}
+
+/* w_u and w_v of a (u, v) triangle: the deformation's columns (stretch_force.cpp:157-161) */
+static void bw_frame(const body_t* B, const bwforce* F, v3* wu, v3* wv, v3* vs)
+{
+	v3 x1 = B->xx[F->p[0]], x2 = B->xx[F->p[1]], x3 = B->xx[F->p[2]];
+	for (int k = 0; k < 3; ++k) vs[k] = B->vv[F->p[k]];
+	v3 dx1 = sub(x2, x1), dx2 = sub(x3, x1);
+	*wu = scl(F->inv_det, sub(scl(F->dv2, dx1), scl(F->dv1, dx2)));
+	*wv = scl(F->inv_det, add(scl(-F->du2, dx1), scl(F->du1, dx2)));
+}
+
+/* stretch_force.cpp:121-388 */
+static void stretch_apply(body_t* B, const bwforce* F)
+{
+	v3 wu, wv, vs[3];
+	bw_frame(B, F, &wu, &wv, vs);
+	stretch_dir(B, F, wu, F->dwudx, F->ks_u, F->kd_u, F->b_u, vs);
+	stretch_dir(B, F, wv, F->dwvdx, F->ks_v, F->kd_v, F->b_v, vs);
+}
+
+/* shear_force.cpp:106-244: C = alpha w_u . w_v, Jacobian without the second-derivative term */
+static void shear_apply(body_t* B, const bwforce* F)
+{
+	v3 wu, wv, vs[3], dC[3];
+	bw_frame(B, F, &wu, &wv, vs);
+	for (int i = 0; i < 3; ++i) dC[i] = scl(F->alpha, add(scl(F->dwudx[i], wv), scl(F->dwvdx[i], wu)));
+	real ks = F->ks_u, kd = F->kd_u;
+	if (ks > 0)
+	{
+		real C = F->alpha * dot(wu, wv);
+		for (int i = 0; i < 3; ++i) B->fi[F->p[i]] = add(B->fi[F->p[i]], scl(-ks * C, dC[i]));
+		for (int i = 0; i < 3; ++i)
+			for (int j = 0; j < 3; ++j)
+			{
+				uint32_t s = F->slot[i + 3 * j];
+				B->dfdx[s] = madd(B->dfdx[s], mscl(-ks, outer(dC[i], dC[j])));
+			}
+	}
+	if (kd > 0)
+	{
+		real dCdt = 0;
+		for (int i = 0; i < 3; ++i) dCdt += dot(dC[i], vs[i]);
+		for (int i = 0; i < 3; ++i) B->fi[F->p[i]] = add(B->fi[F->p[i]], scl(-kd * dCdt, dC[i]));
+		for (int i = 0; i < 3; ++i)
+			for (int j = 0; j < 3; ++j)
+			{
+				uint32_t s = F->slot[i + 3 * j];
+				B->dfdv[s] = madd(B->dfdv[s], mscl(-kd, outer(dC[i], dC[j])));
+			}
+	}
+}
+
+/* mouse_force.cpp:58-245. The second derivatives d2C/dx_i dx_j are c_i c_j (I / L - d d^T / L^3)
+ * with c = (1, -w2, -w3, -w4); the reference's table of +-w products times A and B = -A is that
+ * matrix entry for entry. */
+static void mouse_apply(body_t* B, const mforce* F)
+{
+	v3 x[4], v[4];
+	for (int k = 0; k < 4; ++k)
+	{
+		x[k] = B->xx[F->p[k]];
+		v[k] = B->vv[F->p[k]];
+	}
+	v3 c2 = add(add(scl(F->w2, x[1]), scl(F->w3, x[2])), scl(F->w4, x[3]));
+	v3 d = sub(x[0], c2);
+	real L = len(d);
+	if (!(L > 0)) return;
+	real inv_L = (real)1 / L;
+	v3 n = scl(inv_L, d);
+	const real cw[4] = {1, -F->w2, -F->w3, -F->w4};
+	v3 dC[4];
+	dC[0] = n;
+	for (int i = 1; i < 4; ++i) dC[i] = scl(cw[i], n);
+	if (F->ks > 0 && L > F->L0)
+	{
+		real C = L - F->L0;
+		for (int i = 0; i < 4; ++i) B->fi[F->p[i]] = add(B->fi[F->p[i]], scl(-F->ks * C, dC[i]));
+		real L3 = L * L * L;
+		real inv_L3 = L3 > 0 ? (real)1 / L3 : 0;
+		m33 A = msub(mdiag(inv_L), mscl(inv_L3, outer(d, d)));
+		for (int i = 0; i < 4; ++i)
+			for (int j = 0; j < 4; ++j)
+			{
+				m33 K = mscl(-F->ks, madd(outer(dC[i], dC[j]), mscl(C, mscl(cw[i] * cw[j], A))));
+				uint32_t s = F->slot[i + 4 * j];
+				B->dfdx[s] = madd(B->dfdx[s], K);
+			}
+	}
+	if (F->kd > 0)
+	{
+		v3 vc2 = add(add(scl(F->w2, v[1]), scl(F->w3, v[2])), scl(F->w4, v[3]));
+		real dCdt = dot(sub(v[0], vc2), n);
+		for (int i = 0; i < 4; ++i) B->fi[F->p[i]] = add(B->fi[F->p[i]], scl(-F->kd * dCdt, dC[i]));
+		for (int i = 0; i < 4; ++i)
+			for (int j = 0; j < 4; ++j)
+			{
+				uint32_t s = F->slot[i + 4 * j];
+				B->dfdv[s] = madd(B->dfdv[s], mscl(-F->kd, outer(dC[i], dC[j])));
+			}
 	}
 }
 
@@ -1212,9 +1478,16 @@ static void apply_forces(body_t* B)
 			B->dfdv[s] = madd(B->dfdv[s], mdiag(-c * B->mass[i]));
 		}
 	}
-	/* forces, newest first: springs, then triangles, then tetrahedra (creation order) */
+	/* forces, newest first; creation order: tetrahedra, triangles, springs, stretch, shear, mouse */
+	for (uint32_t e = B->nms; e-- > 0;) mouse_apply(B, &B->ms[e]);
+	for (uint32_t e = B->nbw; e-- > 0;)
+	{
+		if (B->bw[e].shear) shear_apply(B, &B->bw[e]);
+		else stretch_apply(B, &B->bw[e]);
+	}
 	for (uint32_t e = B->ns; e-- > 0;) spring_apply(B, e);
-	for (uint32_t e = B->ntr; e-- > 0;) tri_apply(B, e);
+	if (B->tri_elements)
+		for (uint32_t e = B->ntr; e-- > 0;) tri_apply(B, e);
 	for (uint32_t e = B->nt; e-- > 0;) tet_apply(B, e);
 	if (B->srad)
 		for (uint32_t i = 0; i < n; ++i)

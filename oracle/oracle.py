@@ -55,6 +55,9 @@ class _Desc(C.Structure):
         ("world_sphere_count", C.c_uint32), ("world_spheres", _dp),
         ("gravity", C.c_double * 3),
         ("world_shape_count", C.c_uint32), ("world_shapes", C.POINTER(_Shape)),
+        ("stretch_count", C.c_uint32), ("stretch_tris", _up), ("stretch_uv", _dp), ("stretch_params", _dp),
+        ("shear_count", C.c_uint32), ("shear_tris", _up), ("shear_uv", _dp), ("shear_params", _dp),
+        ("mouse_count", C.c_uint32), ("mouse_ids", _up), ("mouse_params", _dp),
     ]
 
 
@@ -203,6 +206,23 @@ def _make_desc(body):
         desc.world_shapes = C.cast(arr, C.POINTER(_Shape))
     else:
         desc.world_shapes = C.cast(None, C.POINTER(_Shape))
+    st = getattr(body, "stretch_tris", None)
+    if st is not None and len(st):
+        desc.stretch_count = len(st)
+        desc.stretch_tris = u(st)
+        desc.stretch_uv = d(body.stretch_uv)
+        desc.stretch_params = d(body.stretch_params)
+    sh = getattr(body, "shear_tris", None)
+    if sh is not None and len(sh):
+        desc.shear_count = len(sh)
+        desc.shear_tris = u(sh)
+        desc.shear_uv = d(body.shear_uv)
+        desc.shear_params = d(body.shear_params)
+    ms = getattr(body, "mouse_ids", None)
+    if ms is not None and len(ms):
+        desc.mouse_count = len(ms)
+        desc.mouse_ids = u(ms)
+        desc.mouse_params = d(body.mouse_params)
     return desc, keep
 
 

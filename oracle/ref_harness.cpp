@@ -102,6 +102,20 @@ struct RefDesc
 
 	uint32_t world_shape_count;
 	const RefShape* world_shapes;
+
+	// cloth forces (b3StretchForceDef, b3ShearForceDef, b3MouseForceDef); uv null = the defs'
+	// Initialize from the initial positions
+	uint32_t stretch_count;
+	const uint32_t* stretch_tris;   // 3 per force
+	const double* stretch_uv;       // 6 per force: u1, v1, u2, v2, u3, v3
+	const double* stretch_params;   // 6 per force: ks_u, kd_u, b_u, ks_v, kd_v, b_v
+	uint32_t shear_count;
+	const uint32_t* shear_tris;
+	const double* shear_uv;
+	const double* shear_params;     // 2 per force: stiffness, dampingStiffness
+	uint32_t mouse_count;
+	const uint32_t* mouse_ids;      // 4 per force: p1..p4
+	const double* mouse_params;     // 6 per force: w2, w3, w4, stiffness, dampingStiffness, length
 };
 
 struct RefRun
@@ -436,6 +450,7 @@ b3Body* BuildBody(const RefDesc* d, std::vector<b3Particle*>& ps, ShapeStore& st
 		body->m_triangleList = f;
 		++body->m_triangleCount;
 
+		if (!d->tri_Ex) continue;  // a mass fixture without an element force
 		b3TriangleElementForceDef ed;
 		ed.p1 = ps[t[0]]; ed.p2 = ps[t[1]]; ed.p3 = ps[t[2]];
 		ed.v1 = r[0]; ed.v2 = r[1]; ed.v3 = r[2];
@@ -457,6 +472,64 @@ b3Body* BuildBody(const RefDesc* d, std::vector<b3Particle*>& ps, ShapeStore& st
 		sd.stiffness = scalar(d->spring_ks[e]);
 		sd.dampingStiffness = scalar(d->spring_kd[e]);
 		body->CreateForce(sd);
+	}
+
+	for (uint32_t e = 0; e < d->stretch_count; ++e)
+	{
+		const uint32_t* t = d->stretch_tris + 3 * e;
+		const double* c = d->stretch_params + 6 * e;
+		b3StretchForceDef fd;
+		if (d->stretch_uv)
+		{
+			const double* uv = d->stretch_uv + 6 * e;
+			fd.u1 = scalar(uv[0]); fd.v1 = scalar(uv[1]);
+			fd.u2 = scalar(uv[2]); fd.v2 = scalar(uv[3]);
+			fd.u3 = scalar(uv[4]); fd.v3 = scalar(uv[5]);
+		}
+		else
+			fd.Initialize(V3(d->x + 3 * t[0]), V3(d->x + 3 * t[1]), V3(d->x + 3 * t[2]));
+		fd.p1 = ps[t[0]]; fd.p2 = ps[t[1]]; fd.p3 = ps[t[2]];
+		fd.stiffness_u = scalar(c[0]);
+		fd.damping_stiffness_u = scalar(c[1]);
+		fd.b_u = scalar(c[2]);
+		fd.stiffness_v = scalar(c[3]);
+		fd.damping_stiffness_v = scalar(c[4]);
+		fd.b_v = scalar(c[5]);
+		body->CreateForce(fd);
+	}
+
+	for (uint32_t e = 0; e < d->shear_count; ++e)
+	{
+		const uint32_t* t = d->shear_tris + 3 * e;
+		b3ShearForceDef fd;
+		if (d->shear_uv)
+		{
+			const double* uv = d->shear_uv + 6 * e;
+			fd.u1 = scalar(uv[0]); fd.v1 = scalar(uv[1]);
+			fd.u2 = scalar(uv[2]); fd.v2 = scalar(uv[3]);
+			fd.u3 = scalar(uv[4]); fd.v3 = scalar(uv[5]);
+		}
+		else
+			fd.Initialize(V3(d->x + 3 * t[0]), V3(d->x + 3 * t[1]), V3(d->x + 3 * t[2]));
+		fd.p1 = ps[t[0]]; fd.p2 = ps[t[1]]; fd.p3 = ps[t[2]];
+		fd.stiffness = scalar(d->shear_params[2 * e]);
+		fd.dampingStiffness = scalar(d->shear_params[2 * e + 1]);
+		body->CreateForce(fd);
+	}
+
+	for (uint32_t e = 0; e < d->mouse_count; ++e)
+	{
+		const uint32_t* t = d->mouse_ids + 4 * e;
+		const double* c = d->mouse_params + 6 * e;
+		b3MouseForceDef fd;
+		fd.p1 = ps[t[0]]; fd.p2 = ps[t[1]]; fd.p3 = ps[t[2]]; fd.p4 = ps[t[3]];
+		fd.w2 = scalar(c[0]);
+		fd.w3 = scalar(c[1]);
+		fd.w4 = scalar(c[2]);
+		fd.stiffness = scalar(c[3]);
+		fd.dampingStiffness = scalar(c[4]);
+		fd.length = scalar(c[5]);
+		body->CreateForce(fd);
 	}
 
 	body->ResetMass();

@@ -32,9 +32,10 @@ def ctx():
 
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-GOLDEN_CASES = ["tet10", "tet10_bodystep", "tet4", "tet6_newton", "single_tet", "cloth12", "cloth12_contact",
-                "shape_capsule", "shape_box", "shape_triangle", "shape_mesh", "shape_sdf"]
 SHAPE_CASES = ["shape_capsule", "shape_box", "shape_triangle", "shape_mesh", "shape_sdf"]
+BW_CASES = ["bw_pinned", "bw_stretch_map", "bw_shear", "bw_mouse"]
+GOLDEN_CASES = ["tet10", "tet10_bodystep", "tet4", "tet6_newton", "single_tet", "cloth12", "cloth12_contact"] + \
+    SHAPE_CASES + BW_CASES
 
 
 def load_golden(name):
@@ -59,6 +60,8 @@ def load_golden(name):
                 fields[f] = fields[f].item()
         shapes.append(meshes.WorldShape(t, **fields))
         k += 1
+    for f in ("tri_Ex", "tri_Ey", "tri_Es", "tri_nuxy", "tri_nuyx", "tri_kdamp"):
+        kw.setdefault(f, None)  # mass-only triangle fixtures
     desc = meshes.BodyDesc(**kw, sphere_radius=sr, sphere_friction=sf, world_spheres=world, gravity=gravity, name=name,
                            world_shapes=shapes)
     st = z["settings"]

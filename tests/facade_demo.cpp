@@ -3,16 +3,107 @@
 // (binary: n, T, positions, types, tets, E, nu, density, damping, steps, dt, tol) from argv[1],
 // writes the final positions and velocities (binary floats) to argv[2]. With a third argument
 // "shapes" every particle also gets a contact sphere (radius 0.03, friction 0.3) and the body
-// collides with a static b3BoxShape floor and a b3CapsuleShape.
+// collides with a static b3BoxShape floor and a b3CapsuleShape; with "cloth" it runs the
+// Baraff-Witkin cloth scene below instead (argv[1] is not read).
 #include "b3g_body.hpp"
 
 #include <cstdio>
 #include <string>
 #include <vector>
 
+// The reference testbed's pinned cloth (examples/testbed/tests/pinned_cloth.h with
+// UniformBody's ClothDef, createElements = false): an m x m grid of triangle fixtures of density
+// 0.2 held by one b3StretchForce each (stiffness 1e5), border pinned, plus one b3ShearForce per
+// triangle. A BodyDragger-style b3MouseForce pulls the centre towards a static particle for
+// `drag` steps, is destroyed, and the cloth runs `steps - drag` steps more.
+static int cloth(const char* out_path, uint32 m, uint32 steps, uint32 drag, float dt, float tol)
+{
+	b3Body body;
+	body.SetGravity(b3Vec3(0, -9.8f, 0));
+	const float side = 2.0f, h = side / (m - 1);
+	std::vector<b3Particle*> ps;
+	for (uint32 j = 0; j < m; ++j)
+		for (uint32 i = 0; i < m; ++i)
+		{
+			b3ParticleDef pd;
+			pd.type = (i == 0 || j == 0 || i == m - 1 || j == m - 1) ? e_staticParticle : e_dynamicParticle;
+			pd.position.Set(-0.5f * side + i * h, 1.0f, -0.5f * side + j * h);
+			ps.push_back(body.CreateParticle(pd));
+		}
+	std::vector<uint32> tris;
+	for (uint32 j = 0; j + 1 < m; ++j)
+		for (uint32 i = 0; i + 1 < m; ++i)
+		{
+			uint32 v00 = i + m * j, v10 = v00 + 1, v01 = v00 + m, v11 = v01 + 1;
+			tris.insert(tris.end(), {v00, v01, v10});
+		}
+	for (uint32 j = 0; j + 1 < m; ++j)
+		for (uint32 i = 0; i + 1 < m; ++i)
+		{
+			uint32 v00 = i + m * j, v10 = v00 + 1, v01 = v00 + m, v11 = v01 + 1;
+			tris.insert(tris.end(), {v10, v01, v11});
+		}
+	const uint32 T = (uint32)tris.size() / 3;
+	for (uint32 e = 0; e < T; ++e)
+	{
+		b3Particle *p1 = ps[tris[3 * e]], *p2 = ps[tris[3 * e + 1]], *p3 = ps[tris[3 * e + 2]];
+		b3TriangleFixtureDef td;
+		td.p1 = p1; td.p2 = p2; td.p3 = p3;
+		td.v1 = p1->GetPosition(); td.v2 = p2->GetPosition(); td.v3 = p3->GetPosition();
+		td.density = 0.2f;
+		body.CreateTriangle(td);
+		b3StretchForceDef sd;
+		sd.Initialize(td.v1, td.v2, td.v3);
+		sd.p1 = p1; sd.p2 = p2; sd.p3 = p3;
+		sd.stiffness_u = sd.stiffness_v = 1e5f;
+		body.CreateForce(sd);
+		b3ShearForceDef hd;
+		hd.Initialize(td.v1, td.v2, td.v3);
+		hd.p1 = p1; hd.p2 = p2; hd.p3 = p3;
+		hd.stiffness = 1e3f;
+		hd.dampingStiffness = 10.0f;
+		body.CreateForce(hd);
+	}
+	// BodyDragger::StartDragging (examples/testbed/framework/body_dragger.cpp): a static particle
+	// at the picked point, tied to the triangle's barycentre
+	const uint32 t = T / 2 + (m - 1) / 2;
+	b3Particle *q1 = ps[tris[3 * t]], *q2 = ps[tris[3 * t + 1]], *q3 = ps[tris[3 * t + 2]];
+	b3Vec3 c = (1.0f / 3.0f) * (q1->GetPosition() + q2->GetPosition() + q3->GetPosition());
+	b3ParticleDef md;
+	md.type = e_staticParticle;
+	md.position = c + b3Vec3(0.0f, -0.3f, 0.0f);
+	ps.push_back(body.CreateParticle(md));
+	b3MouseForceDef mf;
+	mf.p1 = ps.back(); mf.p2 = q1; mf.p3 = q2; mf.p4 = q3;
+	mf.w2 = 1.0f / 3.0f; mf.w3 = 1.0f / 3.0f; mf.w4 = 1.0f - 2.0f / 3.0f;
+	mf.stiffness = 1e5f;
+	mf.dampingStiffness = 1e3f;
+	mf.length = 0.0f;
+	b3Force* mouse = body.CreateForce(mf);
+	body.SetSolverTolerance(tol);
+	for (uint32 s = 0; s < steps; ++s)
+	{
+		if (s == drag) body.DestroyForce(mouse);  // BodyDragger::StopDragging
+		body.Step(dt, 1, 200);
+	}
+	FILE* o = std::fopen(out_path, "wb");
+	if (!o) return 6;
+	for (int pass = 0; pass < 2; ++pass)
+		for (b3Particle* p : ps)
+		{
+			const b3Vec3& w = pass == 0 ? p->GetPosition() : p->GetVelocity();
+			float xyz[3] = {w.x, w.y, w.z};
+			std::fwrite(xyz, 4, 3, o);
+		}
+	std::fclose(o);
+	std::printf("cloth steps=%u pcg=%u\n", steps, body.GetStepStats().pcg_iterations);
+	return 0;
+}
+
 int main(int argc, char** argv)
 {
 	if (argc < 3) return 2;
+	if (argc > 3 && std::string(argv[3]) == "cloth") return cloth(argv[2], 10, 12, 6, 1.0f / 60.0f, 1e-5f);
 	FILE* f = std::fopen(argv[1], "rb");
 	if (!f) return 3;
 	uint32 n = 0, T = 0, steps = 0;

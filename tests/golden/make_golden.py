@@ -5,8 +5,9 @@ double builds) and driven through oracle/ref_harness.cpp. Each fixture stores th
 tests need neither the reference nor the mesh generators to reproduce them) and the reference's
 positions, velocities and PCG iteration counts after a number of steps.
 
-Run here, where the reference sources exist:  python tests/golden/make_golden.py
+Run here, where the reference sources exist:  python tests/golden/make_golden.py [case ...]
 """
+import copy
 import os
 import sys
 
@@ -54,22 +55,39 @@ CASES = [
     # b3CapsuleShape, b3BoxShape, b3TriangleShape, b3MeshShape with wing vertices and b3SDFShape),
     # in contact from step 2; short horizon for the same reason as the sphere cloth
 ] + [(f"shape_{k}", (lambda k=k: meshes.shape_scene(k, m=10, height=0.002)), [2, 4], dict(max_sub=200, sub_tol=1e-5))
-     for k in ("capsule", "box", "triangle", "mesh", "sdf")]
+     for k in ("capsule", "box", "triangle", "mesh", "sdf")] + [
+    # Baraff-Witkin cloth of the reference testbed (triangle mass fixtures + b3StretchForce per
+    # triangle): pinned border (PinnedCloth), pinned row with stretch damping (StretchMapping),
+    # stretch + b3ShearForce, and a BodyDragger mouse spring pulling the pinned cloth's centre
+    ("bw_pinned", lambda: meshes.bw_cloth(10, pinned="edges", stretch_ks=1e5), [10, 40],
+     dict(max_sub=200, sub_tol=1e-5)),
+    ("bw_stretch_map", lambda: meshes.bw_cloth(10, pinned="row", stretch_ks=1e4, stretch_kd=10.0), [10, 40],
+     dict(max_sub=200, sub_tol=1e-5)),
+    ("bw_shear", lambda: meshes.bw_cloth(10, pinned="row", stretch_ks=1e4, shear_ks=1e3, shear_kd=10.0), [10, 40],
+     dict(max_sub=200, sub_tol=1e-5)),
+    ("bw_mouse", lambda: meshes.bw_cloth(10, pinned="edges", stretch_ks=1e5, mouse=True), [5, 20],
+     dict(max_sub=200, sub_tol=1e-5)),
+]
 
 SHAPE_FIELDS = ["type", "radius", "friction", "p", "rotation", "translation", "scale", "vertices", "triangles",
                 "wings", "voxels", "grid_lower", "grid_upper", "invert"]
 
 FIELDS = ["x", "v", "type", "damping", "tets", "tet_E", "tet_nu", "tet_kdamp", "tet_density", "tris", "tri_Ex",
           "tri_Ey", "tri_Es", "tri_nuxy", "tri_nuyx", "tri_kdamp", "tri_density", "springs", "spring_L0",
-          "spring_ks", "spring_kd", "world_spheres", "gravity"]
+          "spring_ks", "spring_kd", "world_spheres", "gravity", "stretch_tris", "stretch_params", "shear_tris",
+          "shear_params", "mouse_ids", "mouse_params"]
 
 
 def main():
     if not oracle.build_ref():
         raise SystemExit("the reference harness could not be built (reference sources absent)")
+    only = set(sys.argv[1:])  # case names to regenerate (default: all)
     for name, make, snaps, kw in CASES:
+        if only and name not in only:
+            continue
         body = make()
-        out = {f"in_{f}": np.asarray(getattr(body, f)) for f in FIELDS}
+        # absent fields (None: mass-only triangles) stay out of the file
+        out = {f"in_{f}": np.asarray(getattr(body, f)) for f in FIELDS if getattr(body, f) is not None}
         if body.sphere_radius is not None:
             out["in_sphere_radius"] = body.sphere_radius
             out["in_sphere_friction"] = body.sphere_friction
@@ -87,6 +105,15 @@ def main():
                 out[f"ref{bits}_x_{s}"] = x
                 out[f"ref{bits}_v_{s}"] = v
                 out[f"ref{bits}_it_{s}"] = it
+        # the FP64 reference's own sensitivity to rounding: the same run from positions moved by
+        # one unit in the last place (a PCG stopped at a loose tolerance amplifies such changes)
+        rng = np.random.default_rng(7)
+        moved = copy.deepcopy(body)
+        moved.x = body.x * (1.0 + np.ldexp(1.0, -52) * rng.choice([-1.0, 1.0], size=body.x.shape))
+        for s in snaps:
+            x, v, _, _ = oracle.simulate(moved, s, kind="ref", bits=64, **kw)
+            out[f"ref64ulp_x_{s}"] = x
+            out[f"ref64ulp_v_{s}"] = v
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
         print("wrote", name, {k: v.shape for k, v in out.items() if k.startswith("ref64_x")})
 

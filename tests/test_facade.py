@@ -63,3 +63,46 @@ def test_facade_matches_c_abi(tmp_path, ctx, shapes):
     g.close()
     # same library, same inputs: identical results
     assert np.array_equal(res[0], x) and np.array_equal(res[1], v)
+
+
+@pytest.mark.gpu
+def test_facade_cloth_forces_match_c_abi(tmp_path, ctx):
+    """facade_demo.cpp "cloth": triangle mass fixtures + stretch + shear forces, a mouse spring
+    for 6 steps (then DestroyForce) and 6 steps more, against the same scene through the C ABI
+    (meshes.bw_cloth; the mouse spring dropped by rebuilding the body from the state reached,
+    with the initial rest frames and masses). The facade computes the (u, v) frames in float
+    (b3StretchForceDef::Initialize), the C ABI in double, so the two agree to float rounding
+    rather than bitwise."""
+    exe = build_demo(tmp_path)
+    out = tmp_path / "out.bin"
+    r = subprocess.run([exe, "-", str(out), "cloth"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    desc = meshes.bw_cloth(10, pinned="edges", stretch_ks=1e5, shear_ks=1e3, shear_kd=10.0, mouse=True)
+    x_init = desc.x.copy()
+    res = np.fromfile(out, np.float32).reshape(2, desc.n, 3)
+    dt, tol = 1.0 / 60.0, 1e-5
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=tol)
+    g = b3g.Body(ctx, desc)
+    masses = g.masses()
+    for _ in range(6):
+        g.step(dt, cfg)
+    x, v = g.state()
+    g.close()
+    # the rest frames of the initial cloth (what Initialize gave), then the state reached
+    tri = desc.stretch_tris.astype(np.int64)
+    ab = x_init[tri[:, 1]] - x_init[tri[:, 0]]
+    ac = x_init[tri[:, 2]] - x_init[tri[:, 0]]
+    uv = np.zeros((tri.shape[0], 6))
+    uv[:, 2] = np.linalg.norm(ab, axis=1)
+    uv[:, 4] = np.einsum("ij,ij->i", ac, ab / uv[:, 2:3])
+    uv[:, 5] = np.linalg.norm(np.cross(ab, ac), axis=1) / uv[:, 2]
+    desc.stretch_uv, desc.shear_uv = uv, uv.copy()
+    desc.x, desc.v = x.astype(np.float64), v.astype(np.float64)
+    desc.mouse_ids, desc.mouse_params = desc.mouse_ids[:0], desc.mouse_params[:0]
+    g = b3g.Body(ctx, desc, masses=masses)
+    for _ in range(6):
+        g.step(dt, cfg)
+    x, v = g.state()
+    g.close()
+    assert np.linalg.norm(res[0] - x) <= 1e-4 * np.linalg.norm(x - x_init) + 1e-6
+    assert np.linalg.norm(res[1] - v) <= 1e-3 * np.linalg.norm(v) + 1e-5

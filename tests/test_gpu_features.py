@@ -1,5 +1,6 @@
-"""Cloth (triangles, springs, sphere contact, friction), precision variants, preconditioners,
-Newton iterations and the particle API of the CUDA path, against the oracle."""
+"""Cloth (triangles, springs, sphere contact, friction), Baraff-Witkin stretch / shear forces and
+mouse springs, precision variants, preconditioners, Newton iterations and the particle API of the
+CUDA path, against the oracle."""
 import numpy as np
 import pytest
 
@@ -214,3 +215,100 @@ def test_invalid_world_shapes_are_rejected(ctx):
         with pytest.raises(b3g.B3gError, match=msg):
             b3g.Body(ctx, desc)
     b3g.Body(ctx, base).close()
+
+
+def _bw_variant(kind):
+    """Baraff-Witkin and mouse-spring scenes beyond the golden fixtures."""
+    if kind == "uv_compressed":
+        # explicit (u, v) frames: rest lengths 0.9 of the mesh along u and 1.1 along v, and b_u,
+        # b_v away from 1, so both branches of the stretch Jacobian (|w| > b or not) are taken
+        d = meshes.bw_cloth(8, pinned="row", stretch_ks=2e4, stretch_kd=5.0)
+        tri = d.stretch_tris.astype(np.int64)
+        ab = d.x[tri[:, 1]] - d.x[tri[:, 0]]
+        ac = d.x[tri[:, 2]] - d.x[tri[:, 0]]
+        u2 = np.linalg.norm(ab, axis=1)
+        uv = np.zeros((tri.shape[0], 6))
+        uv[:, 2] = 0.9 * u2
+        uv[:, 4] = 0.9 * np.einsum("ij,ij->i", ac, ab) / u2
+        uv[:, 5] = 1.1 * np.linalg.norm(np.cross(ab, ac), axis=1) / u2
+        d.stretch_uv = uv
+        d.stretch_params[:, 2] = 1.05
+        d.stretch_params[:, 5] = 0.95
+        d.stretch_params[:, 3] = 5e3
+        return d, {}
+    if kind == "mouse_repeat":
+        # a mouse spring whose triangle names one vertex twice, with a rest length
+        d = meshes.bw_cloth(8, pinned="edges", stretch_ks=5e4, mouse=True, mouse_offset=(0.1, -0.4, 0.0))
+        d.mouse_ids[0, 3] = d.mouse_ids[0, 2]
+        d.mouse_params[0, :3] = [0.5, 0.25, 0.25]
+        d.mouse_params[0, 5] = 0.1
+        return d, {}
+    if kind == "shear_newton":
+        d = meshes.bw_cloth(8, pinned="row", stretch_ks=1e4, shear_ks=2e3, shear_kd=20.0)
+        return d, dict(newton_iters=3, sub_tol=1e-6)
+    raise ValueError(kind)
+
+
+@pytest.mark.parametrize("kind", ["uv_compressed", "mouse_repeat", "shear_newton"])
+def test_cloth_forces_match_oracle(ctx, kind):
+    """Stretch / shear / mouse-spring variants against the FP64 oracle (pinned to the reference by
+    the golden fixtures), within 20x the oracle's own FP32-vs-FP64 spread."""
+    desc, kw = _bw_variant(kind)
+    steps = 12
+    cfg = b3g.solver_config(force_iterations=kw.get("newton_iters", 1), max_pcg_iterations=200,
+                            pcg_tolerance=kw.get("sub_tol", 1e-5))
+    x, v, its, _ = gpu_run(ctx, desc, steps, cfg)
+    x64, v64, _, _ = oracle.simulate(desc, steps, kind="port", bits=64, **kw)
+    x32, v32, _, _ = oracle.simulate(desc, steps, kind="port", bits=32, **kw)
+    assert np.abs(x64 - desc.x).max() > 1e-3  # the cloth moved
+    assert rel_disp(x, x64, desc.x) < max(1e-4, 20 * rel_disp(x32, x64, desc.x)), kind
+    assert rel(v, v64) < max(1e-3, 20 * rel(v32, v64)), kind
+
+
+def test_cloth_forces_fp64_precision(ctx):
+    """The FP64 solver path with stretch, shear and a mouse spring against the FP64 reference
+    golden vectors: far inside the FP32 floor."""
+    from conftest import load_golden
+
+    for name in ("bw_shear", "bw_mouse"):
+        desc, z, st = load_golden(name)
+        cfg = b3g.solver_config(max_pcg_iterations=st["max_sub"], pcg_tolerance=st["sub_tol"],
+                                precision=b3g.PRECISION_FP64)
+        s = int(z["steps"][0])
+        x, v, _, _ = gpu_run(ctx, desc, s, cfg)
+        rx = z[f"ref64_x_{s}"]
+        floor_x = rel_disp(z[f"ref32_x_{s}"], rx, desc.x)
+        ulp_x = rel_disp(z[f"ref64ulp_x_{s}"], rx, desc.x)
+        # FP32 input rounding of the positions bounds how close a float-input body can get
+        assert rel_disp(x, rx, desc.x) < max(0.2 * floor_x, 10 * ulp_x, 1e-6), name
+
+
+def test_invalid_cloth_forces_are_rejected(ctx):
+    """b3g_body_create validates stretch / shear / mouse inputs and mass-only triangles."""
+    cases = []
+    d = meshes.bw_cloth(4)
+    d.x[int(d.stretch_tris[0, 2])] = d.x[int(d.stretch_tris[0, 0])] + 0.5 * (
+        d.x[int(d.stretch_tris[0, 1])] - d.x[int(d.stretch_tris[0, 0])])
+    cases.append((d, "degenerate"))
+    d = meshes.bw_cloth(4)
+    d.stretch_tris = d.stretch_tris.copy()
+    d.stretch_tris[1, 1] = 999
+    cases.append((d, "stretch force 1 references vertex 999"))
+    d = meshes.bw_cloth(4, shear_ks=1.0)
+    d.shear_uv = np.zeros((d.shear_tris.shape[0], 6))
+    cases.append((d, "det = 0"))
+    d = meshes.bw_cloth(4, mouse=True)
+    d.mouse_ids = d.mouse_ids.copy()
+    d.mouse_ids[0, 0] = d.n
+    cases.append((d, "mouse spring 0 references vertex"))
+    d = meshes.bw_cloth(4, mouse=True)
+    d.mouse_params = d.mouse_params.copy()
+    d.mouse_params[0, 3] = np.inf
+    cases.append((d, "non-finite"))
+    d = meshes.bw_cloth(4)
+    d.tri_Ex = np.ones(d.tris.shape[0])
+    cases.append((d, "all or none"))
+    for desc, msg in cases:
+        with pytest.raises(b3g.B3gError, match=msg):
+            b3g.Body(ctx, desc)
+    b3g.Body(ctx, meshes.bw_cloth(4, mouse=True, shear_ks=1.0)).close()

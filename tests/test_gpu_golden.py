@@ -7,7 +7,7 @@ relative (or 20x that spread); PCG iteration counts within 3 of the FP32 referen
 """
 import numpy as np
 import pytest
-from conftest import GOLDEN_CASES, SHAPE_CASES, load_golden
+from conftest import BW_CASES, GOLDEN_CASES, SHAPE_CASES, load_golden
 
 from bounce_softbody_gb300 import b3g
 
@@ -49,18 +49,23 @@ def test_gpu_matches_reference_golden(ctx, name):
     g.close()
 
 
-def test_batched_shapes_match_reference_golden(ctx):
-    """The cloth-on-shape scenes stepped together by the persistent batch kernels (one launch for
-    all five shape kinds) against the same golden vectors."""
-    loaded = [load_golden(name) for name in SHAPE_CASES]
+@pytest.mark.parametrize("group", [SHAPE_CASES, BW_CASES], ids=["shapes", "cloth_forces"])
+def test_batched_group_matches_reference_golden(ctx, group):
+    """Scenes of one kind stepped together by the persistent batch kernels (one launch for the
+    group: the five world-shape kinds, or the four Baraff-Witkin / mouse-spring cloths) against
+    the same golden vectors, each at its own snapshot steps."""
+    loaded = [load_golden(name) for name in group]
     st = loaded[0][2]
     cfg = b3g.solver_config(max_pcg_iterations=st["max_sub"], pcg_tolerance=st["sub_tol"])
     bodies = [b3g.Body(ctx, desc) for desc, _, _ in loaded]
+    snaps = sorted({int(k) for _, z, _ in loaded for k in z["steps"]})
     done = 0
-    for s in [int(k) for k in loaded[0][1]["steps"]]:
+    for s in snaps:
         b3g.step_batch(ctx, bodies, DT, s - done, cfg, stats=False)
         done = s
-        for (desc, z, _), g, name in zip(loaded, bodies, SHAPE_CASES):
+        for (desc, z, _), g, name in zip(loaded, bodies, group):
+            if s not in [int(k) for k in z["steps"]]:
+                continue
             x, v = g.state()
             rx, rv = z[f"ref64_x_{s}"], z[f"ref64_v_{s}"]
             floor_x = rel_disp(z[f"ref32_x_{s}"], rx, desc.x)

@@ -1,8 +1,10 @@
 """The oracle (C restatement) against golden vectors produced by the reference library itself.
 
 FP64 restatement vs FP64 reference: the same arithmetic up to summation order, so agreement to
-~1e-9 relative. FP32 restatement vs FP32 reference: both sit on the float noise floor; the bound
-is a multiple of the reference's own FP32-vs-FP64 spread.
+~1e-9 relative, or to within 10x the reference's own FP64 spread when its input moves by one ulp
+(stored in the fixture) where the scene amplifies rounding (contacts; a PCG stopped at a loose
+tolerance on a stiff cloth). FP32 restatement vs FP32 reference: both sit on the float noise
+floor; the bound is a multiple of the reference's own FP32-vs-FP64 spread.
 """
 import numpy as np
 import pytest
@@ -27,12 +29,24 @@ def test_port_matches_reference_golden(name):
         # the reference's own FP32-vs-FP64 spread: its float noise floor on this input
         floor_x = max(rel_disp(z[f"ref32_x_{s}"], rx, desc.x), 1e-7)
         floor_v = max(rel(z[f"ref32_v_{s}"], rv), 1e-6)
+        # the FP64 reference's own spread when its input moves by one ulp: how much this scene
+        # (contacts, a PCG stopped at a loose tolerance) amplifies rounding
+        ulp_x = rel_disp(z[f"ref64ulp_x_{s}"], rx, desc.x)
+        ulp_v = rel(z[f"ref64ulp_v_{s}"], rv)
         x64, v64, it64, _ = oracle.simulate(desc, s, kind="port", bits=64, **st)
-        # FP64 restatement vs FP64 reference: summation-order rounding only, amplified at most as
-        # much as the scene amplifies it (chaotic contact scenes), far below the FP32 floor
-        assert rel_disp(x64, rx, desc.x) < max(1e-9, 1e-3 * floor_x), (name, s)
-        assert rel(v64, rv) < max(1e-7, 1e-3 * floor_v), (name, s)
-        assert np.array_equal(it64, z[f"ref64_it_{s}"]), (name, s)
+        ref_it = z[f"ref64_it_{s}"]
+        if np.array_equal(it64, ref_it):
+            # FP64 restatement vs FP64 reference: summation-order rounding only, amplified at most
+            # as much as the scene amplifies it, far below the FP32 floor
+            assert rel_disp(x64, rx, desc.x) < max(1e-9, 1e-3 * floor_x, 10 * ulp_x), (name, s)
+            assert rel(v64, rv) < max(1e-7, 1e-3 * floor_v, 10 * ulp_v), (name, s)
+        else:
+            # a step whose residual ends on the stopping threshold (delta <= tol^2 delta0) can stop
+            # one PCG iteration apart under a different summation order; the two solutions then
+            # differ by one iteration's update, a residual below the tolerance
+            assert np.abs(it64.astype(int) - ref_it.astype(int)).max() <= 1, (name, s)
+            assert rel_disp(x64, rx, desc.x) < max(1e-9, 1e-3 * floor_x, 0.1 * st["sub_tol"]), (name, s)
+            assert rel(v64, rv) < max(1e-7, 1e-3 * floor_v, st["sub_tol"]), (name, s)
         x32, v32, it32, _ = oracle.simulate(desc, s, kind="port", bits=32, **st)
         assert rel_disp(x32, rx, desc.x) < 10 * floor_x + 1e-6, (name, s)
         assert rel(v32, rv) < 10 * floor_v + 1e-5, (name, s)
