@@ -30,19 +30,16 @@ static int cloth(const char* out_path, uint32 m, uint32 steps, uint32 drag, floa
 			pd.position.Set(-0.5f * side + i * h, 1.0f, -0.5f * side + j * h);
 			ps.push_back(body.CreateParticle(pd));
 		}
+	// cells in the order of meshes.bw_cloth (cell column i outer), lower triangles first
 	std::vector<uint32> tris;
-	for (uint32 j = 0; j + 1 < m; ++j)
+	for (int upper = 0; upper < 2; ++upper)
 		for (uint32 i = 0; i + 1 < m; ++i)
-		{
-			uint32 v00 = i + m * j, v10 = v00 + 1, v01 = v00 + m, v11 = v01 + 1;
-			tris.insert(tris.end(), {v00, v01, v10});
-		}
-	for (uint32 j = 0; j + 1 < m; ++j)
-		for (uint32 i = 0; i + 1 < m; ++i)
-		{
-			uint32 v00 = i + m * j, v10 = v00 + 1, v01 = v00 + m, v11 = v01 + 1;
-			tris.insert(tris.end(), {v10, v01, v11});
-		}
+			for (uint32 j = 0; j + 1 < m; ++j)
+			{
+				uint32 v00 = i + m * j, v10 = v00 + 1, v01 = v00 + m, v11 = v01 + 1;
+				if (upper) tris.insert(tris.end(), {v10, v01, v11});
+				else tris.insert(tris.end(), {v00, v01, v10});
+			}
 	const uint32 T = (uint32)tris.size() / 3;
 	for (uint32 e = 0; e < T; ++e)
 	{
