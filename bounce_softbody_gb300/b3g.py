@@ -35,6 +35,11 @@ class WorldShapeC(C.Structure):
     ]
 
 
+class RayHit(C.Structure):
+    """b3g_ray_hit (include/b3g.h)."""
+    _fields_ = [("hit", C.c_int32), ("triangle", C.c_uint32), ("fraction", C.c_float), ("normal", C.c_float * 3)]
+
+
 class BodyDescC(C.Structure):
     _fields_ = [
         ("vertex_count", C.c_uint32), ("positions", _fp), ("velocities", _fp), ("types", _ip),
@@ -134,6 +139,7 @@ SIGNATURES = {
     "b3g_body_set_rotations": (C.c_int, [C.c_void_p, _fp]),
     "b3g_body_get_masses": (C.c_int, [C.c_void_p, _fp]),
     "b3g_body_get_stats": (C.c_int, [C.c_void_p, C.POINTER(StepStats)]),
+    "b3g_body_ray_cast": (C.c_int, [C.c_void_p, _fp, C.c_uint32, C.POINTER(RayHit)]),
     "b3g_server_create": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_float, C.POINTER(SolverConfig),
                                     C.POINTER(C.c_void_p)]),
     "b3g_server_add_body": (C.c_int, [C.c_void_p, C.POINTER(BodyDescC), _up]),
@@ -404,6 +410,18 @@ class Body:
     def set_rotations(self, q):
         qa = _f32(q)
         _check(load_library().b3g_body_set_rotations(self.handle, qa.ctypes.data_as(_fp)), "b3g_body_set_rotations")
+
+    def ray_cast(self, segments):
+        """b3Body::RayCastSingle for each row (p1, p2) of ``segments`` against the body's triangle
+        fixtures. Returns (hit bool array, triangle index array, fraction array, normal array)."""
+        seg = np.ascontiguousarray(np.asarray(segments, np.float32).reshape(-1, 6))
+        out = (RayHit * max(len(seg), 1))()
+        _check(load_library().b3g_body_ray_cast(self.handle, seg.ctypes.data_as(_fp), len(seg), out),
+               "b3g_body_ray_cast")
+        hits = list(out)[: len(seg)]
+        return (np.array([h.hit != 0 for h in hits], bool), np.array([h.triangle for h in hits], np.int64),
+                np.array([h.fraction for h in hits], np.float32),
+                np.array([list(h.normal) for h in hits], np.float32).reshape(-1, 3))
 
     def masses(self) -> np.ndarray:
         m = np.zeros(self.n, np.float32)

@@ -485,7 +485,7 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 		float dens = d->tet_density ? d->tet_density[e] : 0.0f;
 		b->h_tet_mass[e] = dens * vol;
 	}
-	std::vector<uint4> tri(b->ntr);
+	std::vector<uint4> tri(b->ntr_fix);  // every triangle fixture (the ray cast's targets)
 	std::vector<float> tri_x(6 * (size_t)b->ntr), tri_invS(4 * (size_t)b->ntr), tri_K(36 * (size_t)b->ntr), tri_kd(b->ntr);
 	b->h_tri_mass.resize(b->ntr_fix);
 	for (uint32_t e = 0; e < b->ntr_fix; ++e)
@@ -494,9 +494,9 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 		float r[9];
 		for (int k = 0; k < 3; ++k)
 			for (int c = 0; c < 3; ++c) r[3 * k + c] = d->tri_rest ? d->tri_rest[9 * e + 3 * k + c] : d->positions[3 * t[k] + c];
+		tri[e] = make_uint4(t[0], t[1], t[2], 0);
 		if (tri_elements)
 		{
-			tri[e] = make_uint4(t[0], t[1], t[2], 0);
 			if (!tri_setup(r, d->tri_young_x[e], d->tri_young_y[e], d->tri_shear[e], d->tri_poisson_xy[e],
 			               d->tri_poisson_yx[e], &tri_x[6 * (size_t)e], &tri_invS[4 * (size_t)e], &tri_K[36 * (size_t)e]))
 			{
@@ -551,7 +551,7 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 		D.tet_q = C.take<float4>(b->nt);
 		D.tet_rec = C.take<float4>(4 * (size_t)b->nt);
 		D.tet_bc = C.take<float>(12 * (size_t)b->nt);
-		D.tri = C.take<uint4>(b->ntr);
+		D.tri = C.take<uint4>(b->ntr_fix);
 		D.tri_x = C.take<float>(6 * (size_t)b->ntr);
 		D.tri_invS = C.take<float>(4 * (size_t)b->ntr);
 		D.tri_K = C.take<float>(36 * (size_t)b->ntr);
@@ -649,7 +649,7 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	up(D.tet_invE, tet_invE.data(), tet_invE.size() * sizeof(float));
 	up(D.tet_mat, tet_mat.data(), b->nt * sizeof(float4));
 	up(D.tet_q, tet_q.data(), b->nt * sizeof(float4));
-	up(D.tri, tri.data(), b->ntr * sizeof(uint4));
+	up(D.tri, tri.data(), b->ntr_fix * sizeof(uint4));
 	up(D.tri_x, tri_x.data(), tri_x.size() * sizeof(float));
 	up(D.tri_invS, tri_invS.data(), tri_invS.size() * sizeof(float));
 	up(D.tri_K, tri_K.data(), tri_K.size() * sizeof(float));
@@ -697,6 +697,7 @@ int b3g_body_destroy(b3g_body* b)
 	for (int k = 0; k < 3; ++k)
 		if (b->prec[k].mem) cudaFree(b->prec[k].mem);
 	cudaFree(b->arena);
+	if (b->ray_buf) cudaFree(b->ray_buf);
 	delete b;
 	return B3G_OK;
 }
@@ -882,6 +883,43 @@ int b3g_body_set_rotations(b3g_body* b, const float* q)
 	cudaError_t e = cudaMemcpyAsync(b->d.tet_q, q, b->nt * sizeof(float4), cudaMemcpyHostToDevice, st);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
 	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "set_rotations");
+}
+
+int b3g_body_ray_cast(b3g_body* b, const float* segments, uint32_t count, b3g_ray_hit* hits)
+{
+	if (!b || (count && (!segments || !hits))) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	if (count == 0) return B3G_OK;
+	for (uint64_t k = 0; k < 6 * (uint64_t)count; ++k)
+		if (!std::isfinite(segments[k])) return fail(B3G_ERROR_INVALID_ARGUMENT, "segment %u is not finite", (uint32_t)(k / 6));
+	cudaSetDevice(b->ctx->device);
+	cudaStream_t st = b->ctx->stream;
+	auto layout = [](uint32_t cap, size_t* off_keys, size_t* off_hits) {
+		*off_keys = align_up(6 * sizeof(float) * (size_t)cap);
+		*off_hits = *off_keys + align_up(sizeof(unsigned long long) * (size_t)cap);
+		return *off_hits + align_up(sizeof(b3g_ray_hit) * (size_t)cap);
+	};
+	size_t off_keys, off_hits;
+	if (count > b->ray_cap)
+	{
+		uint32_t cap = std::max<uint32_t>(count, 64);
+		cudaError_t e = cudaStreamSynchronize(st);
+		if (e != cudaSuccess) return cuda_fail(e, "ray cast");
+		if (b->ray_buf) cudaFree(b->ray_buf);
+		b->ray_buf = nullptr;
+		b->ray_cap = 0;
+		e = cudaMalloc(&b->ray_buf, layout(cap, &off_keys, &off_hits));
+		if (e != cudaSuccess) return cuda_fail(e, "allocating ray cast scratch");
+		b->ray_cap = cap;
+	}
+	layout(b->ray_cap, &off_keys, &off_hits);
+	float* dseg = (float*)b->ray_buf;
+	unsigned long long* keys = (unsigned long long*)(b->ray_buf + off_keys);
+	b3g_ray_hit* dhits = (b3g_ray_hit*)(b->ray_buf + off_hits);
+	cudaError_t e = cudaMemcpyAsync(dseg, segments, 6 * sizeof(float) * (size_t)count, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = op_ray_cast(b->d, (int)b->ntr_fix, dseg, count, keys, dhits, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(hits, dhits, sizeof(b3g_ray_hit) * (size_t)count, cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "ray cast");
 }
 
 int b3g_body_get_masses(b3g_body* b, float* masses)

@@ -57,6 +57,9 @@ struct b3g_body
 	std::vector<float> h_tet_mass, h_tri_mass, h_given_mass;
 	std::vector<float> h_mass, h_invmass;
 	b3g_step_stats last{};
+	// ray cast scratch (segments, reduction keys, hits), grown on demand
+	char* ray_buf = nullptr;
+	uint32_t ray_cap = 0;
 };
 
 namespace b3g {

@@ -162,6 +162,101 @@ __global__ void __launch_bounds__(kThreads) k_cloth_forces(DevBody B, StepParams
 	}
 }
 
+// ------------------------------------------------------------------ ray casts
+// b3TriangleShape::RayCast (triangle_shape.cpp:314-387) for the segment p1 + t d, t in [0, 1].
+// Returns the fraction and the plane offset num = n . (A - p1), whose sign orients the normal.
+__device__ __forceinline__ bool ray_triangle(float3 p1, float3 d, float3 A, float3 B, float3 C, float& t, float& num,
+                                             float3& n)
+{
+	if (dot3(d, d) < kFltEps * kFltEps) return false;
+	const float3 AB = B - A, AC = C - A;
+	n = normalize3(cross3(AB, AC));
+	num = dot3(n, A - p1);
+	const float den = dot3(n, d);
+	if (den == 0.0f) return false;
+	t = num / den;
+	if (t < 0.0f || 1.0f < t) return false;
+	const float3 Q = p1 + t * d;
+	const float3 QA = A - Q, QB = B - Q, QC = C - Q;
+	const float3 N = cross3(AB, AC);
+	const float u = dot3(cross3(QB, QC), N);
+	const float v = dot3(cross3(QC, QA), N);
+	const float w = dot3(cross3(QA, QB), N);
+	return u >= 0.0f && v >= 0.0f && w >= 0.0f;
+}
+
+__device__ __forceinline__ unsigned long long ray_key(float t, unsigned tri)
+{
+	// t >= 0: its bit pattern orders like its value (-0 cannot pass the t < 0 test as a hit key
+	// below 0, and is mapped to +0)
+	return ((unsigned long long)__float_as_uint(fmaxf(t, 0.0f)) << 32) | tri;
+}
+
+// grid.x strides over triangles, grid.y over segments; one 64-bit atomicMin per warp and segment
+__global__ void __launch_bounds__(kThreads) k_ray_cast(DevBody B, int ntri, const float* __restrict__ seg,
+                                                        unsigned count, unsigned long long* keys)
+{
+	const int lane = threadIdx.x & 31;
+	for (unsigned r = blockIdx.y; r < count; r += gridDim.y)
+	{
+		const float3 p1 = f3(seg[6 * r], seg[6 * r + 1], seg[6 * r + 2]);
+		const float3 d = f3(seg[6 * r + 3], seg[6 * r + 4], seg[6 * r + 5]) - p1;
+		const int stride = gridDim.x * blockDim.x;
+		for (int base = blockIdx.x * blockDim.x; base < ntri; base += stride)
+		{
+			const int e = base + threadIdx.x;
+			unsigned long long key = ~0ull;
+			if (e < ntri)
+			{
+				const uint4 id = B.tri[e];
+				float t, num;
+				float3 n;
+				if (ray_triangle(p1, d, ld3(B.x, id.x), ld3(B.x, id.y), ld3(B.x, id.z), t, num, n))
+					key = ray_key(t, (unsigned)e);
+			}
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1)
+			{
+				const unsigned long long other = __shfl_xor_sync(0xffffffffu, key, o);
+				key = other < key ? other : key;
+			}
+			if (lane == 0 && key != ~0ull) atomicMin(keys + r, key);
+		}
+	}
+}
+
+// One thread per segment: the winner's normal, oriented as the reference orients it.
+__global__ void k_ray_finish(DevBody B, const float* __restrict__ seg, unsigned count,
+                             const unsigned long long* __restrict__ keys, b3g_ray_hit* hits)
+{
+	const unsigned r = blockIdx.x * blockDim.x + threadIdx.x;
+	if (r >= count) return;
+	b3g_ray_hit o;
+	o.hit = 0;
+	o.triangle = 0;
+	o.fraction = 0.0f;
+	o.normal[0] = o.normal[1] = o.normal[2] = 0.0f;
+	const unsigned long long key = keys[r];
+	if (key != ~0ull)
+	{
+		const unsigned e = (unsigned)(key & 0xffffffffu);
+		const uint4 id = B.tri[e];
+		const float3 p1 = f3(seg[6 * r], seg[6 * r + 1], seg[6 * r + 2]);
+		const float3 d = f3(seg[6 * r + 3], seg[6 * r + 4], seg[6 * r + 5]) - p1;
+		float t, num;
+		float3 n;
+		ray_triangle(p1, d, ld3(B.x, id.x), ld3(B.x, id.y), ld3(B.x, id.z), t, num, n);
+		if (num > 0.0f) n = -n;
+		o.hit = 1;
+		o.triangle = e;
+		o.fraction = __uint_as_float((unsigned)(key >> 32));
+		o.normal[0] = n.x;
+		o.normal[1] = n.y;
+		o.normal[2] = n.z;
+	}
+	hits[r] = o;
+}
+
 __device__ void pcg_start(Scalars* sc, double delta0)
 {
 	sc->delta = delta0;
@@ -505,6 +600,30 @@ cudaError_t launch_spmv(const DevBody& B, const TA* A, cudaStream_t st)
 cudaError_t op_begin(const DevBody& B, cudaStream_t st, int max_it, double tol2, int refresh, double newton_tol2)
 {
 	k_begin<<<1, 1, 0, st>>>(B.sc, max_it, tol2, refresh, newton_tol2);
+	return cudaGetLastError();
+}
+
+cudaError_t op_ray_cast(const DevBody& B, int ntri, const float* segments, uint32_t count, unsigned long long* keys,
+                        b3g_ray_hit* hits, cudaStream_t st)
+{
+	if (count == 0) return cudaSuccess;
+	cudaError_t e = cudaMemsetAsync(keys, 0xff, count * sizeof(unsigned long long), st);
+	if (e != cudaSuccess) return e;
+	if (ntri > 0)
+	{
+		// enough CTAs over the triangles to fill the GPU for one segment, fewer per segment when
+		// there are many segments
+		static const int sms = [] {
+			int dev = 0, n = 0;
+			cudaGetDevice(&dev);
+			cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+			return n > 0 ? n : 1;
+		}();
+		const int per_seg = std::max(1, std::min(grid_for(ntri, kThreads), 4 * sms / (int)std::min<uint32_t>(count, 64)));
+		dim3 grid((unsigned)per_seg, std::min<uint32_t>(count, 65535u));
+		k_ray_cast<<<grid, kThreads, 0, st>>>(B, ntri, segments, count, keys);
+	}
+	k_ray_finish<<<(count + 127) / 128, 128, 0, st>>>(B, segments, count, keys, hits);
 	return cudaGetLastError();
 }
 

@@ -37,6 +37,10 @@ cudaError_t op_post(const DevBody& B, float h, cudaStream_t st);
 cudaError_t op_nostep(const DevBody& B, cudaStream_t st);
 // clear a float array on the device
 cudaError_t op_fill_f32(float* p, size_t count, float value, cudaStream_t st);
+// Closest triangle-fixture hit of `count` segments (6 floats each, device): keys[r] (device,
+// count entries) is reduced to fraction bits << 32 | triangle, then decoded into hits (device).
+cudaError_t op_ray_cast(const DevBody& B, int ntri, const float* segments, uint32_t count, unsigned long long* keys,
+                        b3g_ray_hit* hits, cudaStream_t st);
 
 // Persistent batch kernel: every body listed in `big` (teams of `cluster` CTAs) and in `small`
 // (one CTA each) steps `steps` times in one launch.

@@ -295,6 +295,23 @@ B3G_API int b3g_body_get_masses(b3g_body* body, float* masses);
 /* Statistics of the body's last step (waits for it). */
 B3G_API int b3g_body_get_stats(b3g_body* body, b3g_step_stats* stats);
 
+/* One segment's closest hit on the body's triangle fixtures (b3BodyRayCastSingleOutput,
+ * include/bounce_softbody/dynamics/body.h:52-57): the triangle is its index in desc.tris. */
+typedef struct b3g_ray_hit
+{
+	int32_t hit;          /* 1 if the segment hits a triangle */
+	uint32_t triangle;    /* index into b3g_body_desc::tris */
+	float fraction;       /* p1 + fraction (p2 - p1) is the hit point, in [0, 1] */
+	float normal[3];      /* the triangle's unit normal, facing p1 */
+} b3g_ray_hit;
+
+/* b3Body::RayCastSingle (src/bounce_softbody/dynamics/body.cpp:468-521) for `count` segments
+ * (6 floats each: p1, p2) against every triangle fixture at the body's current positions, with
+ * b3TriangleShape::RayCast (src/bounce_softbody/collision/shapes/triangle_shape.cpp:314-387); the
+ * smallest fraction wins, ties go to the lowest triangle index. Synchronous: hits are in host
+ * memory on return. */
+B3G_API int b3g_body_ray_cast(b3g_body* body, const float* segments, uint32_t count, b3g_ray_hit* hits);
+
 /* ---------------------------------------------------------------- serving
  * A server steps many bodies on request, continuously batched: a worker thread repeatedly admits
  * waiting requests, steps every body with an active request once in one batched launch (the

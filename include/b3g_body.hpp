@@ -18,8 +18,8 @@
 //   b3_forceSolver*Iterations       b3Body::GetStepStats()
 // Extensions (no reference counterpart): SetSolverTolerance (the reference's Step always runs the
 // PCG at FLT_EPSILON), SetPrecision, SetPreconditioner.
-// Not provided (outside the implicit step): ray casts, debug draw, DestroyParticle and the other
-// Destroy* calls of fixtures.
+//   b3Body::RayCastSingle            b3g_body_ray_cast
+// Not provided: debug draw, DestroyParticle and the Destroy* calls of fixtures.
 #pragma once
 
 #include "b3g.h"
@@ -226,6 +226,21 @@ struct b3SphereFixtureDef : public b3FixtureDef
 {
 	b3Particle* p = nullptr;
 };
+// A triangle fixture (b3TriangleFixture): the handle CreateTriangle returns and ray casts report.
+struct b3TriangleFixture
+{
+	b3Particle *m_p1 = nullptr, *m_p2 = nullptr, *m_p3 = nullptr;
+	scalar m_density = 0;
+};
+
+// b3BodyRayCastSingleOutput (include/bounce_softbody/dynamics/body.h:52-57)
+struct b3BodyRayCastSingleOutput
+{
+	b3TriangleFixture* triangle = nullptr;
+	scalar fraction = 0;
+	b3Vec3 normal;
+};
+
 struct b3TriangleFixtureDef : public b3FixtureDef
 {
 	b3Particle *p1 = nullptr, *p2 = nullptr, *p3 = nullptr;
@@ -344,6 +359,7 @@ public:
 	{
 		for (b3Particle* p : m_particles) delete p;
 		for (b3Force* f : m_forceHandles) delete f;
+		for (b3TriangleFixture* t : m_triFixture) delete t;
 		if (m_body) b3g_body_destroy(m_body);
 		if (m_ctx) b3g_context_destroy(m_ctx);
 	}
@@ -408,7 +424,7 @@ public:
 				m_triKd.push_back(0);
 				m_triDensity.push_back(0);
 				m_triElem.push_back(0);
-				m_triFix.push_back(0);
+				m_triFixture.push_back(nullptr);
 			}
 			for (int k = 0; k < 3; ++k)
 				for (int c = 0; c < 3; ++c) m_triRest[9 * e + 3 * k + c] = (&vs[k].x)[c];
@@ -485,7 +501,7 @@ public:
 			drop(m_tetDensity, 1);
 			break;
 		case e_triangleElementForce:
-			if (m_triFix[e])
+			if (m_triFixture[e])
 			{
 				// the mass fixture stays
 				m_triElem[e] = 0;
@@ -495,7 +511,7 @@ public:
 			}
 			drop(m_tris, 3); drop(m_triRest, 9); drop(m_triEx, 1); drop(m_triEy, 1); drop(m_triEs, 1);
 			drop(m_triNxy, 1); drop(m_triNyx, 1); drop(m_triKd, 1); drop(m_triDensity, 1); drop(m_triElem, 1);
-			drop(m_triFix, 1);
+			drop(m_triFixture, 1);
 			break;
 		case e_springForce:
 			drop(m_springs, 2); drop(m_sprL0, 1); drop(m_sprKs, 1); drop(m_sprKd, 1);
@@ -535,7 +551,7 @@ public:
 	}
 	// A triangle fixture pairs with the element force of the same particles when there is one;
 	// otherwise it is a mass fixture of its own (cloth held by stretch and shear forces).
-	void CreateTriangle(const b3TriangleFixtureDef& def)
+	b3TriangleFixture* CreateTriangle(const b3TriangleFixtureDef& def)
 	{
 		const uint32 a[3] = {def.p1->m_index, def.p2->m_index, def.p3->m_index};
 		size_t e = find_tri(a, false);
@@ -547,11 +563,17 @@ public:
 				v->push_back(0);
 			m_triDensity.push_back(0);
 			m_triElem.push_back(0);
-			m_triFix.push_back(0);
+			m_triFixture.push_back(nullptr);
 		}
+		b3TriangleFixture* t = new b3TriangleFixture();
+		t->m_p1 = def.p1;
+		t->m_p2 = def.p2;
+		t->m_p3 = def.p3;
+		t->m_density = def.density;
+		m_triFixture[e] = t;
 		m_triDensity[e] = def.density;
-		m_triFix[e] = 1;
 		m_topologyDirty = true;
+		return t;
 	}
 	void CreateSphere(const b3SphereFixtureDef& def)
 	{
@@ -692,6 +714,24 @@ public:
 		m_hostFresh = false;
 	}
 
+	// b3Body::RayCastSingle (body.cpp:468-521): the closest triangle hit by the segment p1 -> p2,
+	// at the current positions (b3g_body_ray_cast). Triangles created only as element forces (no
+	// fixture) are hit too, and then reported with a null fixture.
+	bool RayCastSingle(b3BodyRayCastSingleOutput* output, const b3Vec3& p1, const b3Vec3& p2) const
+	{
+		b3Body* self = const_cast<b3Body*>(this);
+		self->build();
+		self->flush_state();  // pending forces and translations stay for the next Step
+		const float seg[6] = {p1.x, p1.y, p1.z, p2.x, p2.y, p2.z};
+		b3g_ray_hit h;
+		check(b3g_body_ray_cast(m_body, seg, 1, &h), "b3g_body_ray_cast");
+		if (!h.hit) return false;
+		output->triangle = m_triFixture[h.triangle];
+		output->fraction = h.fraction;
+		output->normal.Set(h.normal[0], h.normal[1], h.normal[2]);
+		return true;
+	}
+
 	scalar GetEnergy() const
 	{
 		const_cast<b3Body*>(this)->fetch();
@@ -742,7 +782,7 @@ private:
 	size_t find_tri(const uint32* a, bool want_fixture_only) const
 	{
 		for (size_t e = 0; e < m_triEx.size(); ++e)
-			if (same_set(&m_tris[3 * e], a, 3) && (want_fixture_only ? !m_triElem[e] : !m_triFix[e])) return e;
+			if (same_set(&m_tris[3 * e], a, 3) && (want_fixture_only ? !m_triElem[e] : !m_triFixture[e])) return e;
 		return m_triEx.size();
 	}
 
@@ -858,7 +898,8 @@ private:
 	}
 
 	// pending host-side changes -> device, before a step
-	void flush_inputs()
+	// host-side SetPosition / SetVelocity -> device
+	void flush_state()
 	{
 		if (m_stateDirty)
 		{
@@ -871,6 +912,11 @@ private:
 			check(b3g_body_set_state(m_body, x.data(), v.data()), "b3g_body_set_state");
 			m_stateDirty = false;
 		}
+	}
+
+	void flush_inputs()
+	{
+		flush_state();
 		bool f = false, t = false;
 		for (b3Particle* p : m_particles)
 		{
@@ -904,7 +950,8 @@ private:
 	std::vector<uint32> m_tets, m_tris, m_springs;
 	std::vector<float> m_tetRest, m_tetE, m_tetNu, m_tetKd, m_tetDensity;
 	std::vector<float> m_triRest, m_triEx, m_triEy, m_triEs, m_triNxy, m_triNyx, m_triKd, m_triDensity;
-	std::vector<uint8_t> m_triElem, m_triFix;  // per triangle entry: has an element / a fixture
+	std::vector<uint8_t> m_triElem;                // per triangle entry: has an element force
+	std::vector<b3TriangleFixture*> m_triFixture;  // per triangle entry: its fixture or null
 	std::vector<float> m_sprL0, m_sprKs, m_sprKd;
 	std::vector<uint32> m_stTris, m_shTris, m_msIds;
 	std::vector<float> m_stUv, m_stParams, m_shUv, m_shParams, m_msParams;

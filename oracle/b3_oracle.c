@@ -18,6 +18,8 @@
  *   - stretch (Baraff-Witkin), (u, v) Initialize src/bounce_softbody/dynamics/forces/stretch_force.cpp:36-388
  *   - shear (Baraff-Witkin)                      src/bounce_softbody/dynamics/forces/shear_force.cpp:25-244
  *   - mouse spring                               src/bounce_softbody/dynamics/forces/mouse_force.cpp:25-245
+ *   - body ray cast over triangle fixtures       src/bounce_softbody/dynamics/body.cpp:468-521,
+ *                                                src/bounce_softbody/collision/shapes/triangle_shape.cpp:314-387
  *   - sphere contact force and friction          src/bounce_softbody/dynamics/contacts/sphere_shape_contact.cpp:53-189
  *   - sphere shape collide                       src/bounce_softbody/collision/shapes/sphere_shape.cpp:50-77
  *   - contact creation / destruction             src/bounce_softbody/dynamics/contact_manager.cpp:65-146
@@ -1746,6 +1748,87 @@ int b3o_simulate(const b3o_desc* d, b3o_run* run)
 		run->x_out[3 * i + 0] = B->x[i].x; run->x_out[3 * i + 1] = B->x[i].y; run->x_out[3 * i + 2] = B->x[i].z;
 		run->v_out[3 * i + 0] = B->v[i].x; run->v_out[3 * i + 1] = B->v[i].y; run->v_out[3 * i + 2] = B->v[i].z;
 	}
+	body_free(B);
+	return 0;
+}
+
+/* ------------------------------------------------------------------ ray casts */
+typedef struct
+{
+	int32_t hit;
+	uint32_t triangle;
+	double fraction;
+	double normal[3];
+} b3o_hit;
+
+/* triangle_shape.cpp:314-387 b3TriangleShape::RayCast */
+static int ray_triangle(v3 p1, v3 p2, v3 A, v3 Bv, v3 C, real maxFraction, real* fraction, v3* normal)
+{
+	v3 d = sub(p2, p1);
+	if (dot(d, d) < B3O_EPS * B3O_EPS) return 0;
+	v3 n = normalize(cross(sub(Bv, A), sub(C, A)));
+	real num = dot(n, sub(A, p1));
+	real den = dot(n, d);
+	if (den == 0) return 0;
+	real t = num / den;
+	if (t < 0 || maxFraction < t) return 0;
+	v3 Q = add(p1, scl(t, d));
+	v3 AB = sub(Bv, A), AC = sub(C, A);
+	v3 QA = sub(A, Q), QB = sub(Bv, Q), QC = sub(C, Q);
+	v3 N = cross(AB, AC);
+	real u = dot(cross(QB, QC), N);
+	real v = dot(cross(QC, QA), N);
+	real w = dot(cross(QA, QB), N);
+	if (u >= 0 && v >= 0 && w >= 0)
+	{
+		*fraction = t;
+		*normal = num > 0 ? neg(n) : n;
+		return 1;
+	}
+	return 0;
+}
+
+/* body.cpp:468-521 b3Body::RayCastSingle after run->steps steps. The reference's tree only prunes
+ * (its callback keeps the full max fraction), so every triangle fixture whose ray cast succeeds
+ * is a candidate and the smallest fraction wins; ties go to the lowest triangle index. */
+int b3o_ray_cast(const b3o_desc* d, b3o_run* run, uint32_t count, const double* segs, b3o_hit* out)
+{
+	body_t* B = body_create(d);
+	if (!B) return 1;
+	for (uint32_t s = 0; s < run->steps; ++s)
+	{
+		uint32_t it = body_step(B, (real)run->dt, run->newton_iters, run->max_sub, (real)run->sub_tol);
+		if (run->sub_iters_out) run->sub_iters_out[s] = it;
+	}
+	for (uint32_t r = 0; r < count; ++r)
+	{
+		v3 p1 = D3(segs + 6 * r), p2 = D3(segs + 6 * r + 3);
+		b3o_hit h;
+		memset(&h, 0, sizeof(h));
+		real best = 0;
+		for (uint32_t e = 0; e < B->ntr; ++e)
+		{
+			real t;
+			v3 n;
+			const uint32_t* t3 = B->tri + 3 * e;
+			if (ray_triangle(p1, p2, B->x[t3[0]], B->x[t3[1]], B->x[t3[2]], 1, &t, &n) && (!h.hit || t < best))
+			{
+				best = t;
+				h.hit = 1;
+				h.triangle = e;
+				h.fraction = t;
+				h.normal[0] = n.x;
+				h.normal[1] = n.y;
+				h.normal[2] = n.z;
+			}
+		}
+		out[r] = h;
+	}
+	if (run->x_out)
+		for (uint32_t i = 0; i < B->n; ++i)
+		{
+			run->x_out[3 * i + 0] = B->x[i].x; run->x_out[3 * i + 1] = B->x[i].y; run->x_out[3 * i + 2] = B->x[i].z;
+		}
 	body_free(B);
 	return 0;
 }

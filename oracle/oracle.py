@@ -252,6 +252,36 @@ def simulate(body, steps: int, dt: float = 1.0 / 60.0, newton_iters: int = 1, ma
     return x, v, it[:steps].copy(), float(sec[0])
 
 
+class _Hit(C.Structure):
+    """Mirror of RefHit (oracle/ref_harness.cpp) and b3o_hit (oracle/b3_oracle.c)."""
+    _fields_ = [("hit", C.c_int32), ("triangle", C.c_uint32), ("fraction", C.c_double), ("normal", C.c_double * 3)]
+
+
+def ray_cast(body, steps: int, segments, dt: float = 1.0 / 60.0, newton_iters: int = 1, max_sub: int = 200,
+             sub_tol: float = 1e-5, kind: str = "port", bits: int = 64):
+    """b3Body::RayCastSingle for each segment (rows p1, p2) after ``steps`` steps.
+
+    Returns (hit bool array, triangle index array, fraction array, normal array, positions)."""
+    lib = _lib(kind, bits)
+    fn = lib.b3o_ray_cast if kind == "port" else lib.ref_ray_cast
+    fn.argtypes = [C.POINTER(_Desc), C.POINTER(_Run), C.c_uint32, _dp, C.POINTER(_Hit)]
+    fn.restype = C.c_int
+    desc, keep = _make_desc(body)
+    seg = np.ascontiguousarray(np.asarray(segments, np.float64).reshape(-1, 6))
+    out = (_Hit * max(len(seg), 1))()
+    x = np.zeros((body.n, 3))
+    run = _Run()
+    run.steps, run.dt, run.newton_iters, run.max_sub, run.sub_tol = steps, dt, newton_iters, max_sub, sub_tol
+    run.x_out = x.ctypes.data_as(_dp)
+    rc = fn(C.byref(desc), C.byref(run), len(seg), seg.ctypes.data_as(_dp), out)
+    if rc != 0:
+        raise RuntimeError(f"ray cast {kind}{bits} failed with {rc}")
+    del keep
+    hits = list(out)[: len(seg)]
+    return (np.array([h.hit != 0 for h in hits]), np.array([h.triangle for h in hits], np.int64),
+            np.array([h.fraction for h in hits]), np.array([list(h.normal) for h in hits]).reshape(-1, 3), x)
+
+
 def simulate_batch(bodies, steps: int, dt: float = 1.0 / 60.0, newton_iters: int = 1, max_sub: int = 200,
                    sub_tol: float = 1e-5, bits: int = 32, threads: int = 0):
     """Step independent bodies on `threads` host threads with the restatement.

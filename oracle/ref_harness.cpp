@@ -31,6 +31,7 @@
 #include <bounce_softbody/collision/geometry/mesh.h>
 #include <bounce_softbody/collision/geometry/sdf.h>
 
+#include <algorithm>
 #include <chrono>
 #include <new>
 #include <vector>
@@ -385,7 +386,8 @@ static b3Shape* MakeShape(const RefShape& w, ShapeStore& store)
 	return out;
 }
 
-b3Body* BuildBody(const RefDesc* d, std::vector<b3Particle*>& ps, ShapeStore& store)
+b3Body* BuildBody(const RefDesc* d, std::vector<b3Particle*>& ps, ShapeStore& store,
+                  std::vector<b3TriangleFixture*>* tris_out = nullptr)
 {
 	// b3Body embeds a 1 MiB stack allocator: keep it on the heap.
 	b3Body* body = new b3Body();
@@ -449,6 +451,7 @@ b3Body* BuildBody(const RefDesc* d, std::vector<b3Particle*>& ps, ShapeStore& st
 		if (body->m_triangleList) body->m_triangleList->m_prev = f;
 		body->m_triangleList = f;
 		++body->m_triangleCount;
+		if (tris_out) tris_out->push_back(f);
 
 		if (!d->tri_Ex) continue;  // a mass fixture without an element force
 		b3TriangleElementForceDef ed;
@@ -617,6 +620,52 @@ int ref_simulate(const RefDesc* d, RefRun* run)
 
 	delete body;
 
+	return 0;
+}
+
+struct RefHit
+{
+	int32_t hit;
+	uint32_t triangle;   // index of the triangle fixture in RefDesc::tris
+	double fraction;
+	double normal[3];
+};
+
+// b3Body::RayCastSingle (src/bounce_softbody/dynamics/body.cpp:468-521) on the body after
+// run->steps harness steps, for `count` segments (p1, p2: 6 doubles each).
+int ref_ray_cast(const RefDesc* d, RefRun* run, uint32_t count, const double* segs, RefHit* out)
+{
+	std::vector<b3Particle*> ps;
+	std::vector<b3TriangleFixture*> tris;
+	ShapeStore shapes;
+	b3Body* body = BuildBody(d, ps, shapes, &tris);
+	for (uint32_t s = 0; s < run->steps; ++s)
+	{
+		uint32 it = HarnessStep(body, scalar(run->dt), run->newton_iters, run->max_sub, scalar(run->sub_tol));
+		if (run->sub_iters_out) run->sub_iters_out[s] = it;
+	}
+	for (uint32_t r = 0; r < count; ++r)
+	{
+		b3BodyRayCastSingleOutput o;
+		RefHit h = {};
+		if (body->RayCastSingle(&o, V3(segs + 6 * r), V3(segs + 6 * r + 3)))
+		{
+			h.hit = 1;
+			h.triangle = (uint32_t)(std::find(tris.begin(), tris.end(), o.triangle) - tris.begin());
+			h.fraction = o.fraction;
+			h.normal[0] = o.normal.x;
+			h.normal[1] = o.normal.y;
+			h.normal[2] = o.normal.z;
+		}
+		out[r] = h;
+	}
+	if (run->x_out)
+		for (uint32_t i = 0; i < d->n; ++i)
+		{
+			b3Vec3 x = ps[i]->GetPosition();
+			run->x_out[3 * i + 0] = x.x; run->x_out[3 * i + 1] = x.y; run->x_out[3 * i + 2] = x.z;
+		}
+	delete body;
 	return 0;
 }
 

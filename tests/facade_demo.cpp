@@ -7,6 +7,7 @@
 // Baraff-Witkin cloth scene below instead (argv[1] is not read).
 #include "b3g_body.hpp"
 
+#include <algorithm>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -15,7 +16,9 @@
 // UniformBody's ClothDef, createElements = false): an m x m grid of triangle fixtures of density
 // 0.2 held by one b3StretchForce each (stiffness 1e5), border pinned, plus one b3ShearForce per
 // triangle. A BodyDragger-style b3MouseForce pulls the centre towards a static particle for
-// `drag` steps, is destroyed, and the cloth runs `steps - drag` steps more.
+// `drag` steps, is destroyed, and the cloth runs `steps - drag` steps more; then a vertical ray
+// picks the cloth (b3Body::RayCastSingle). Output: positions, velocities, then hit flag, triangle
+// index, fraction and normal.
 static int cloth(const char* out_path, uint32 m, uint32 steps, uint32 drag, float dt, float tol)
 {
 	b3Body body;
@@ -41,6 +44,7 @@ static int cloth(const char* out_path, uint32 m, uint32 steps, uint32 drag, floa
 				else tris.insert(tris.end(), {v00, v01, v10});
 			}
 	const uint32 T = (uint32)tris.size() / 3;
+	std::vector<b3TriangleFixture*> fixtures;
 	for (uint32 e = 0; e < T; ++e)
 	{
 		b3Particle *p1 = ps[tris[3 * e]], *p2 = ps[tris[3 * e + 1]], *p3 = ps[tris[3 * e + 2]];
@@ -48,7 +52,7 @@ static int cloth(const char* out_path, uint32 m, uint32 steps, uint32 drag, floa
 		td.p1 = p1; td.p2 = p2; td.p3 = p3;
 		td.v1 = p1->GetPosition(); td.v2 = p2->GetPosition(); td.v3 = p3->GetPosition();
 		td.density = 0.2f;
-		body.CreateTriangle(td);
+		fixtures.push_back(body.CreateTriangle(td));
 		b3StretchForceDef sd;
 		sd.Initialize(td.v1, td.v2, td.v3);
 		sd.p1 = p1; sd.p2 = p2; sd.p3 = p3;
@@ -83,6 +87,18 @@ static int cloth(const char* out_path, uint32 m, uint32 steps, uint32 drag, floa
 		if (s == drag) body.DestroyForce(mouse);  // BodyDragger::StopDragging
 		body.Step(dt, 1, 200);
 	}
+	// picking as BodyDragger::StartDragging does it: a ray from above through the cloth's centre
+	b3BodyRayCastSingleOutput hit;
+	float pick[6] = {0, 0, 0, 0, 0, 0};
+	if (body.RayCastSingle(&hit, b3Vec3(0.05f, 3.0f, 0.03f), b3Vec3(0.05f, -3.0f, 0.03f)))
+	{
+		pick[0] = 1.0f;
+		pick[1] = (float)(std::find(fixtures.begin(), fixtures.end(), hit.triangle) - fixtures.begin());
+		pick[2] = hit.fraction;
+		pick[3] = hit.normal.x;
+		pick[4] = hit.normal.y;
+		pick[5] = hit.normal.z;
+	}
 	FILE* o = std::fopen(out_path, "wb");
 	if (!o) return 6;
 	for (int pass = 0; pass < 2; ++pass)
@@ -92,6 +108,7 @@ static int cloth(const char* out_path, uint32 m, uint32 steps, uint32 drag, floa
 			float xyz[3] = {w.x, w.y, w.z};
 			std::fwrite(xyz, 4, 3, o);
 		}
+	std::fwrite(pick, 4, 6, o);
 	std::fclose(o);
 	std::printf("cloth steps=%u pcg=%u\n", steps, body.GetStepStats().pcg_iterations);
 	return 0;

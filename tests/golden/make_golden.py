@@ -78,6 +78,48 @@ FIELDS = ["x", "v", "type", "damping", "tets", "tet_E", "tet_nu", "tet_kdamp", "
           "shear_params", "mouse_ids", "mouse_params"]
 
 
+# b3Body::RayCastSingle on golden bodies after some steps: (golden case, steps). Segments pass
+# through interior points of random triangles (barycentric weights >= 0.15, away from edges) from
+# random directions (a few stop short of far layers); 8 segments far above the cloth and 8 that
+# end before reaching it miss.
+RAY_CASES = [("bw_pinned", 10), ("cloth12", 5)]
+
+
+def ray_segments(x, tris, rng, count=64):
+    t = rng.choice(len(tris), count, replace=False)
+    b = rng.uniform(0.15, 0.7, (count, 2))
+    b = np.where(b.sum(1, keepdims=True) > 0.85, b * 0.85 / b.sum(1, keepdims=True), b)
+    w = np.stack([1 - b[:, 0] - b[:, 1], b[:, 0], b[:, 1]], 1)
+    q = (w[:, :, None] * x[tris[t].astype(np.int64)]).sum(1)
+    dirn = rng.normal(size=(count, 3))
+    dirn /= np.linalg.norm(dirn, axis=1, keepdims=True)
+    length = rng.uniform(0.2, 1.0, (count, 1))
+    p1 = q + length * dirn
+    p2 = q - rng.uniform(0.3, 1.5, (count, 1)) * length * dirn
+    miss = np.concatenate([q[:8] + [0, 5, 0], q[:8] + [1, 6, 0]], 1)
+    short = np.concatenate([p1[8:16], p1[8:16] + 0.2 * (q[8:16] - p1[8:16])], 1)
+    return np.concatenate([np.concatenate([p1, p2], 1), miss, short])
+
+
+def make_rays():
+    out = {}
+    for case, steps in RAY_CASES:
+        z = np.load(os.path.join(HERE, f"{case}.npz"))
+        desc = next(make for name, make, _, _ in CASES if name == case)()
+        kw = next(k for name, _, _, k in CASES if name == case)
+        seg = ray_segments(z[f"ref64_x_{steps}"], desc.tris, np.random.default_rng(1))
+        out[f"{case}_steps"] = np.array(steps)
+        out[f"{case}_seg"] = seg
+        for bits in (32, 64):
+            hit, tri, frac, normal, _ = oracle.ray_cast(desc, steps, seg, kind="ref", bits=bits, **kw)
+            out[f"{case}_ref{bits}_hit"] = hit
+            out[f"{case}_ref{bits}_tri"] = tri
+            out[f"{case}_ref{bits}_frac"] = frac
+            out[f"{case}_ref{bits}_normal"] = normal
+    np.savez_compressed(os.path.join(HERE, "ray_casts.npz"), **out)
+    print("wrote ray_casts", {k: v.shape for k, v in out.items() if k.endswith("_seg")})
+
+
 def main():
     if not oracle.build_ref():
         raise SystemExit("the reference harness could not be built (reference sources absent)")
@@ -116,6 +158,8 @@ def main():
             out[f"ref64ulp_v_{s}"] = v
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
         print("wrote", name, {k: v.shape for k, v in out.items() if k.startswith("ref64_x")})
+    if not only or "ray_casts" in only:
+        make_rays()
 
 
 if __name__ == "__main__":

@@ -68,7 +68,8 @@ def test_facade_matches_c_abi(tmp_path, ctx, shapes):
 @pytest.mark.gpu
 def test_facade_cloth_forces_match_c_abi(tmp_path, ctx):
     """facade_demo.cpp "cloth": triangle mass fixtures + stretch + shear forces, a mouse spring
-    for 6 steps (then DestroyForce) and 6 steps more, against the same scene through the C ABI
+    for 6 steps (then DestroyForce), 6 steps more and a RayCastSingle pick, against the same
+    scene through the C ABI
     (meshes.bw_cloth; the mouse spring dropped by rebuilding the body from the state reached,
     with the initial rest frames and masses). The facade computes the (u, v) frames in float
     (b3StretchForceDef::Initialize), the C ABI in double, so the two agree to float rounding
@@ -79,7 +80,8 @@ def test_facade_cloth_forces_match_c_abi(tmp_path, ctx):
     assert r.returncode == 0, r.stdout + r.stderr
     desc = meshes.bw_cloth(10, pinned="edges", stretch_ks=1e5, shear_ks=1e3, shear_kd=10.0, mouse=True)
     x_init = desc.x.copy()
-    res = np.fromfile(out, np.float32).reshape(2, desc.n, 3)
+    raw = np.fromfile(out, np.float32)
+    res, pick = raw[: 6 * desc.n].reshape(2, desc.n, 3), raw[6 * desc.n:]
     dt, tol = 1.0 / 60.0, 1e-5
     cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=tol)
     g = b3g.Body(ctx, desc)
@@ -103,6 +105,12 @@ def test_facade_cloth_forces_match_c_abi(tmp_path, ctx):
     for _ in range(6):
         g.step(dt, cfg)
     x, v = g.state()
+    hit, tri, frac, normal = g.ray_cast(np.array([[0.05, 3.0, 0.03, 0.05, -3.0, 0.03]]))
     g.close()
     assert np.linalg.norm(res[0] - x) <= 1e-4 * np.linalg.norm(x - x_init) + 1e-6
     assert np.linalg.norm(res[1] - v) <= 1e-3 * np.linalg.norm(v) + 1e-5
+    # RayCastSingle through the facade: the same triangle as the C ABI's ray cast
+    assert pick[0] == 1.0 and hit[0]
+    assert int(pick[1]) == tri[0]
+    assert abs(pick[2] - frac[0]) < 1e-5
+    np.testing.assert_allclose(pick[3:], normal[0], atol=1e-4)

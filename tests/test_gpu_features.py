@@ -312,3 +312,64 @@ def test_invalid_cloth_forces_are_rejected(ctx):
         with pytest.raises(b3g.B3gError, match=msg):
             b3g.Body(ctx, desc)
     b3g.Body(ctx, meshes.bw_cloth(4, mouse=True, shear_ks=1.0)).close()
+
+
+@pytest.mark.parametrize("case", ["bw_pinned", "cloth12"])
+def test_ray_cast_matches_reference_golden(ctx, case):
+    """b3g_body_ray_cast after stepping a golden body against b3Body::RayCastSingle of the FP64
+    reference on its own trajectory: the same triangles hit; fractions and normals within the
+    reference's own FP32-vs-FP64 spread plus float rounding of the segment."""
+    import os
+    from conftest import GOLDEN, load_golden
+
+    z = np.load(os.path.join(GOLDEN, "ray_casts.npz"))
+    desc, _, st = load_golden(case)
+    steps = int(z[f"{case}_steps"])
+    cfg = b3g.solver_config(max_pcg_iterations=st["max_sub"], pcg_tolerance=st["sub_tol"])
+    g = b3g.Body(ctx, desc)
+    for _ in range(steps):
+        g.step(DT, cfg)
+    hit, tri, frac, normal = g.ray_cast(z[f"{case}_seg"])
+    g.close()
+    rh = z[f"{case}_ref64_hit"]
+    assert np.array_equal(hit, rh)
+    assert np.array_equal(tri[hit], z[f"{case}_ref64_tri"][hit])
+    spread = np.abs(z[f"{case}_ref32_frac"] - z[f"{case}_ref64_frac"]).max()
+    assert np.abs(frac[hit] - z[f"{case}_ref64_frac"][hit]).max() < max(20 * spread, 1e-4)
+    nspread = np.abs(z[f"{case}_ref32_normal"] - z[f"{case}_ref64_normal"]).max()
+    assert np.abs(normal[hit] - z[f"{case}_ref64_normal"][hit]).max() < max(20 * nspread, 1e-3)
+
+
+def test_ray_cast_edge_cases(ctx):
+    """No triangles, zero-length and non-finite segments, nearest of two stacked layers, normal
+    facing the segment's start from either side, ties to the lowest triangle index."""
+    # two parallel unit triangles at y = 0 and y = 1, and a duplicate of the lower one
+    x = np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1], [0, 1, 0], [1, 1, 0], [0, 1, 1]], np.float64)
+    tris = np.array([[0, 2, 1], [3, 5, 4], [0, 2, 1]], np.uint32)
+    desc = meshes.BodyDesc(x=x, v=np.zeros_like(x), type=np.zeros(6, np.int32), damping=np.zeros(6),
+                           tets=np.zeros((0, 4), np.uint32), tet_E=np.zeros(0), tet_nu=np.zeros(0),
+                           tet_kdamp=np.zeros(0), tet_density=np.zeros(0), tris=tris, tri_Ex=None, tri_Ey=None,
+                           tri_Es=None, tri_nuxy=None, tri_nuyx=None, tri_kdamp=None, tri_density=np.ones(3),
+                           springs=np.zeros((0, 2), np.uint32), spring_L0=np.zeros(0), spring_ks=np.zeros(0),
+                           spring_kd=np.zeros(0))
+    g = b3g.Body(ctx, desc)
+    seg = np.array([[0.2, 2.0, 0.2, 0.2, -1.0, 0.2],     # from above: the upper layer first
+                    [0.2, -1.0, 0.2, 0.2, 2.0, 0.2],     # from below: the lower layers, tie -> index 0
+                    [0.2, 0.5, 0.2, 0.2, 0.5, 0.2],      # zero length
+                    [0.9, 2.0, 0.9, 0.9, -1.0, 0.9],     # outside both triangles
+                    [0.2, 2.0, 0.2, 0.2, 1.5, 0.2]])     # ends before the upper layer
+    hit, tri, frac, normal = g.ray_cast(seg)
+    assert hit.tolist() == [True, True, False, False, False]
+    assert tri[:2].tolist() == [1, 0]
+    np.testing.assert_allclose(frac[:2], [1.0 / 3.0, 1.0 / 3.0], rtol=1e-6)
+    np.testing.assert_allclose(normal[0], [0, 1, 0], atol=1e-6)   # faces the start above
+    np.testing.assert_allclose(normal[1], [0, -1, 0], atol=1e-6)  # faces the start below
+    with pytest.raises(b3g.B3gError, match="not finite"):
+        g.ray_cast(np.array([[np.nan, 0, 0, 0, 1, 0]]))
+    assert g.ray_cast(np.zeros((0, 6)))[0].size == 0
+    g.close()
+    # a body without triangles never hits
+    t = meshes.tet_grid(3, 3, 3)
+    g = b3g.Body(ctx, t)
+    assert not g.ray_cast(np.array([[0.1, 5, 0.1, 0.1, -5, 0.1]]))[0].any()
+    g.close()

@@ -77,3 +77,22 @@ def test_port_matches_reference_live(seed):
     xp, vp, itp, _ = oracle.simulate(desc, 6, kind="port", bits=64)
     assert rel_disp(xp, xr, desc.x) < 1e-9
     assert np.array_equal(itp, itr)
+
+
+@pytest.mark.parametrize("case", ["bw_pinned", "cloth12"])
+def test_port_ray_cast_matches_reference_golden(case):
+    """b3Body::RayCastSingle: the restatement's brute-force closest hit against the reference's
+    tree query (tests/golden/ray_casts.npz): the same triangles hit, fractions and normals equal
+    up to the trajectory's own FP64 rounding spread."""
+    import os
+    from conftest import GOLDEN
+
+    z = np.load(os.path.join(GOLDEN, "ray_casts.npz"))
+    desc, _, st = load_golden(case)
+    steps = int(z[f"{case}_steps"])
+    hit, tri, frac, normal, _ = oracle.ray_cast(desc, steps, z[f"{case}_seg"], kind="port", bits=64, **st)
+    assert np.array_equal(hit, z[f"{case}_ref64_hit"])
+    assert np.array_equal(tri[hit], z[f"{case}_ref64_tri"][hit])
+    assert np.abs(frac - z[f"{case}_ref64_frac"]).max() < 1e-6
+    assert np.abs(normal - z[f"{case}_ref64_normal"]).max() < 1e-6
+    assert hit.sum() == 64  # every aimed segment hits, the 16 others miss
