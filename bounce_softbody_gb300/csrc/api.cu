@@ -378,6 +378,8 @@ int b3g_context_destroy(b3g_context* c)
 	cudaSetDevice(c->device);
 	cudaStreamSynchronize(c->stream);
 	destroy_batch_cache(c);
+	if (c->xfer) cudaFree(c->xfer);
+	if (c->xfer_table) cudaFree(c->xfer_table);
 	for (cudaEvent_t& e : c->tev)
 		if (e) cudaEventDestroy(e);
 	if (c->h_scalars) cudaFreeHost(c->h_scalars);
@@ -694,6 +696,8 @@ int b3g_body_destroy(b3g_body* b)
 	cudaSetDevice(b->ctx->device);
 	cudaStreamSynchronize(b->ctx->stream);
 	forget_body_in_batch_cache(b->ctx, b);
+	if (std::find(b->ctx->xfer_bodies.begin(), b->ctx->xfer_bodies.end(), b) != b->ctx->xfer_bodies.end())
+		b->ctx->xfer_bodies.clear();  // a later body at the same address must not reuse the table
 	for (int k = 0; k < 3; ++k)
 		if (b->prec[k].mem) cudaFree(b->prec[k].mem);
 	cudaFree(b->arena);

@@ -23,6 +23,16 @@ struct b3g_context
 	cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
 	double t_assembly_ms = 0.0, t_pcg_ms = 0.0;
 	unsigned long long t_steps = 0;
+	// batched host transfers (b3g_batch_apply_forces / b3g_batch_get_state): one contiguous
+	// device staging buffer, one copy each way and one scatter / gather launch per call; the
+	// body table is rebuilt when the body list changes
+	float* xfer = nullptr;
+	size_t xfer_cap = 0;                 // floats
+	b3g::XferBody* xfer_table = nullptr;
+	uint32_t xfer_table_cap = 0;
+	std::vector<b3g_body*> xfer_bodies;
+	uint32_t xfer_max_n3 = 0;
+	uint64_t xfer_total = 0;             // floats of the flat host array (3 per vertex)
 };
 
 namespace b3g {

@@ -429,21 +429,71 @@ extern "C" int b3g_batch_schedule(b3g_context* ctx, int32_t* out, uint32_t capac
 	return B3G_OK;
 }
 
+// The transfer table of a body list (rebuilt when the list differs from the last call's) and a
+// staging buffer of at least `floats` floats.
+static int prepare_xfer(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, size_t floats_per_total)
+{
+	bool same = ctx->xfer_bodies.size() == count;
+	for (uint32_t k = 0; same && k < count; ++k) same = ctx->xfer_bodies[k] == bodies[k];
+	cudaStream_t st = ctx->stream;
+	cudaError_t e = cudaSuccess;
+	if (!same)
+	{
+		std::vector<XferBody> t(count);
+		uint64_t off = 0;
+		uint32_t mx = 0;
+		for (uint32_t k = 0; k < count; ++k)
+		{
+			b3g_body* b = bodies[k];
+			if (!b || b->ctx != ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u is null or of another context", k);
+			t[k] = XferBody{b->d.x, b->d.v, b->d.fext, off, 3u * b->n, 0u};
+			off += 3ull * b->n;
+			mx = std::max(mx, 3u * b->n);
+		}
+		if (count > ctx->xfer_table_cap)
+		{
+			e = cudaStreamSynchronize(st);
+			if (ctx->xfer_table) cudaFree(ctx->xfer_table);
+			ctx->xfer_table = nullptr;
+			ctx->xfer_table_cap = 0;
+			if (e == cudaSuccess) e = cudaMalloc(&ctx->xfer_table, count * sizeof(XferBody));
+			if (e != cudaSuccess) return cuda_fail(e, "batch transfer table");
+			ctx->xfer_table_cap = count;
+		}
+		// earlier transfers on the stream may still read the old table; the copy from pageable
+		// memory completes before the call returns, so `t` may go
+		e = cudaStreamSynchronize(st);
+		if (e == cudaSuccess) e = cudaMemcpy(ctx->xfer_table, t.data(), count * sizeof(XferBody), cudaMemcpyHostToDevice);
+		if (e != cudaSuccess) return cuda_fail(e, "batch transfer table");
+		ctx->xfer_bodies.assign(bodies, bodies + count);
+		ctx->xfer_total = off;
+		ctx->xfer_max_n3 = mx;
+	}
+	const size_t need = floats_per_total * ctx->xfer_total;
+	if (need > ctx->xfer_cap)
+	{
+		e = cudaStreamSynchronize(st);
+		if (ctx->xfer) cudaFree(ctx->xfer);
+		ctx->xfer = nullptr;
+		ctx->xfer_cap = 0;
+		if (e == cudaSuccess) e = cudaMalloc(&ctx->xfer, need * sizeof(float));
+		if (e != cudaSuccess) return cuda_fail(e, "batch transfer staging");
+		ctx->xfer_cap = need;
+	}
+	return B3G_OK;
+}
+
 extern "C" int b3g_batch_apply_forces(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, const float* forces)
 {
 	if (!ctx || (!bodies && count) || (!forces && count)) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	if (count == 0) return B3G_OK;
+	cudaSetDevice(ctx->device);
+	int rc = prepare_xfer(ctx, bodies, count, 2);
+	if (rc != B3G_OK) return rc;
 	cudaStream_t st = ctx->stream;
-	size_t off = 0;
-	cudaError_t e = cudaSuccess;
-	for (uint32_t k = 0; k < count && e == cudaSuccess; ++k)
-	{
-		b3g_body* b = bodies[k];
-		if (!b || b->ctx != ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u is null or of another context", k);
-		size_t c = 3 * (size_t)b->n;
-		e = cudaMemcpyAsync(b->staging, forces + off, c * sizeof(float), cudaMemcpyHostToDevice, st);
-		if (e == cudaSuccess) e = op_accumulate(b->d.fext, b->staging, c, st);
-		off += c;
-	}
+	// one copy of the whole array, then one launch adds every body's slice to its fext
+	cudaError_t e = cudaMemcpyAsync(ctx->xfer, forces, ctx->xfer_total * sizeof(float), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = op_batch_scatter_add(ctx->xfer_table, count, ctx->xfer_max_n3, ctx->xfer, st);
 	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch_apply_forces");
 }
 
@@ -451,19 +501,19 @@ extern "C" int b3g_batch_get_state(b3g_context* ctx, b3g_body* const* bodies, ui
                                    float* velocities)
 {
 	if (!ctx || (!bodies && count)) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	if (count == 0 || (!positions && !velocities)) return B3G_OK;
+	cudaSetDevice(ctx->device);
+	int rc = prepare_xfer(ctx, bodies, count, 2);
+	if (rc != B3G_OK) return rc;
 	cudaStream_t st = ctx->stream;
-	size_t off = 0;
-	cudaError_t e = cudaSuccess;
-	for (uint32_t k = 0; k < count && e == cudaSuccess; ++k)
-	{
-		b3g_body* b = bodies[k];
-		if (!b || b->ctx != ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u is null or of another context", k);
-		size_t c = 3 * (size_t)b->n;
-		if (positions) e = cudaMemcpyAsync(positions + off, b->d.x, c * sizeof(float), cudaMemcpyDeviceToHost, st);
-		if (e == cudaSuccess && velocities)
-			e = cudaMemcpyAsync(velocities + off, b->d.v, c * sizeof(float), cudaMemcpyDeviceToHost, st);
-		off += c;
-	}
+	// one launch packs every body's x and v into the staging buffer, then one copy each
+	float* sx = ctx->xfer;
+	float* sv = ctx->xfer + ctx->xfer_total;
+	const size_t bytes = ctx->xfer_total * sizeof(float);
+	cudaError_t e = op_batch_gather(ctx->xfer_table, count, ctx->xfer_max_n3, positions ? sx : nullptr,
+	                                velocities ? sv : nullptr, st);
+	if (e == cudaSuccess && positions) e = cudaMemcpyAsync(positions, sx, bytes, cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess && velocities) e = cudaMemcpyAsync(velocities, sv, bytes, cudaMemcpyDeviceToHost, st);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
 	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch_get_state");
 }

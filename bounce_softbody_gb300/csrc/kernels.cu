@@ -717,6 +717,55 @@ cudaError_t op_nostep(const DevBody& B, cudaStream_t st)
 	return cudaGetLastError();
 }
 
+// grid.y walks the bodies, grid.x (with a stride) the floats of one body
+__global__ void __launch_bounds__(kThreads) k_batch_scatter_add(const XferBody* __restrict__ table, unsigned count,
+                                                                 const float* __restrict__ src)
+{
+	for (unsigned b = blockIdx.y; b < count; b += gridDim.y)
+	{
+		const XferBody t = table[b];
+		const float* s = src + t.off;
+		for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < t.n3; k += gridDim.x * blockDim.x)
+			t.fext[k] += s[k];
+	}
+}
+
+__global__ void __launch_bounds__(kThreads) k_batch_gather(const XferBody* __restrict__ table, unsigned count,
+                                                            float* __restrict__ dx, float* __restrict__ dv)
+{
+	for (unsigned b = blockIdx.y; b < count; b += gridDim.y)
+	{
+		const XferBody t = table[b];
+		for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < t.n3; k += gridDim.x * blockDim.x)
+		{
+			if (dx) dx[t.off + k] = t.x[k];
+			if (dv) dv[t.off + k] = t.v[k];
+		}
+	}
+}
+
+static dim3 xfer_grid(uint32_t count, uint32_t max_n3)
+{
+	return dim3((unsigned)std::max(1u, std::min<uint32_t>((max_n3 + kThreads - 1) / kThreads, 64u)),
+	            std::min<uint32_t>(std::max(count, 1u), 65535u));
+}
+
+cudaError_t op_batch_scatter_add(const XferBody* table, uint32_t count, uint32_t max_n3, const float* src,
+                                 cudaStream_t st)
+{
+	if (count == 0) return cudaSuccess;
+	k_batch_scatter_add<<<xfer_grid(count, max_n3), kThreads, 0, st>>>(table, count, src);
+	return cudaGetLastError();
+}
+
+cudaError_t op_batch_gather(const XferBody* table, uint32_t count, uint32_t max_n3, float* dst_x, float* dst_v,
+                            cudaStream_t st)
+{
+	if (count == 0) return cudaSuccess;
+	k_batch_gather<<<xfer_grid(count, max_n3), kThreads, 0, st>>>(table, count, dst_x, dst_v);
+	return cudaGetLastError();
+}
+
 cudaError_t op_accumulate(float* dst, const float* src, size_t count, cudaStream_t st)
 {
 	if (count == 0) return cudaSuccess;

@@ -37,6 +37,23 @@ cudaError_t op_post(const DevBody& B, float h, cudaStream_t st);
 cudaError_t op_nostep(const DevBody& B, cudaStream_t st);
 // clear a float array on the device
 cudaError_t op_fill_f32(float* p, size_t count, float value, cudaStream_t st);
+
+// One body of a batched host transfer: its state arrays and its place in the flat host array.
+struct XferBody
+{
+	float* x;
+	float* v;
+	float* fext;
+	unsigned long long off;  // first float of the body in the flat array
+	unsigned n3;             // 3 * vertices
+	unsigned pad;
+};
+// fext of every body += src[off .. off + n3) (one launch for the whole batch)
+cudaError_t op_batch_scatter_add(const XferBody* table, uint32_t count, uint32_t max_n3, const float* src,
+                                 cudaStream_t st);
+// dst_x / dst_v[off .. off + n3) = x / v of every body (either may be null)
+cudaError_t op_batch_gather(const XferBody* table, uint32_t count, uint32_t max_n3, float* dst_x, float* dst_v,
+                            cudaStream_t st);
 // Closest triangle-fixture hit of `count` segments (6 floats each, device): keys[r] (device,
 // count entries) is reduced to fraction bits << 32 | triangle, then decoded into hits (device).
 cudaError_t op_ray_cast(const DevBody& B, int ntri, const float* segments, uint32_t count, unsigned long long* keys,

@@ -118,3 +118,55 @@ def test_launch_timing_mode_same_results(ctx):
         assert np.array_equal(xa, xb) and np.array_equal(va, vb)
     for b in ref + tim:
         b.close()
+
+
+def test_batch_host_transfers_match_per_body_calls(ctx):
+    """b3g_batch_apply_forces / b3g_batch_get_state (one copy and one launch each way over a
+    cached body table) against the per-body calls: bitwise the same state, also after the body
+    list changes and after a listed body is destroyed."""
+    descs = meshes.batch_bodies(count=7, lo=3, hi=9, seed=13)
+    cfg = b3g.solver_config()
+
+    def run(batched, order, forces):
+        bodies = [b3g.Body(ctx, d) for d in descs]
+        sel = [bodies[k] for k in order]
+        n = [b.n for b in sel]
+        for f in forces:
+            if batched:
+                b3g.batch_apply_forces(ctx, sel, f.ctypes.data)
+            else:
+                off = 0
+                for b, m in zip(sel, n):
+                    b.apply_forces(f[off:off + 3 * m].reshape(m, 3))
+                    off += 3 * m
+            b3g.step_batch(ctx, bodies, DT, 1, cfg, stats=False)
+        x = np.zeros(3 * sum(n), np.float32)
+        v = np.zeros(3 * sum(n), np.float32)
+        if batched:
+            b3g.batch_get_state(ctx, sel, x.ctypes.data, v.ctypes.data)
+        else:
+            off = 0
+            for b, m in zip(sel, n):
+                xb, vb = b.state()
+                x[off:off + 3 * m], v[off:off + 3 * m] = xb.ravel(), vb.ravel()
+                off += 3 * m
+        return bodies, x, v
+
+    for order in ([0, 1, 2, 3, 4, 5, 6], [5, 2, 6]):
+        total = sum(descs[k].n for k in order)
+        forces = [np.random.default_rng(1 + s).standard_normal(3 * total).astype(np.float32) for s in range(3)]
+        b1, x1, v1 = run(True, order, forces)
+        b2, x2, v2 = run(False, order, forces)
+        assert np.array_equal(x1, x2) and np.array_equal(v1, v2), order
+        assert np.abs(v1).max() > 0
+        # a listed body goes away: the next batched call rebuilds its table
+        b1[order[0]].close()
+        rest = [b1[k] for k in order[1:]]
+        xs = np.zeros(3 * sum(b.n for b in rest), np.float32)
+        vs = np.zeros_like(xs)
+        b3g.batch_get_state(ctx, rest, xs.ctypes.data, vs.ctypes.data)
+        m = rest[0].n
+        xr, vr = rest[0].state()
+        assert np.array_equal(xs[:3 * m], xr.ravel()) and np.array_equal(vs[:3 * m], vr.ravel())
+        for b in b1 + b2:
+            b.close()
