@@ -372,12 +372,20 @@ int b3g_context_create(int device, b3g_context** out)
 	return B3G_OK;
 }
 
+static void release_body_memory(b3g_body* b);
+
 int b3g_context_destroy(b3g_context* c)
 {
 	if (!c) return B3G_OK;
 	cudaSetDevice(c->device);
 	cudaStreamSynchronize(c->stream);
 	destroy_batch_cache(c);
+	for (b3g_body* b : c->live_bodies)
+	{
+		release_body_memory(b);
+		b->ctx = nullptr;
+	}
+	c->live_bodies.clear();
 	if (c->xfer) cudaFree(c->xfer);
 	if (c->xfer_table) cudaFree(c->xfer_table);
 	for (cudaEvent_t& e : c->tev)
@@ -686,22 +694,41 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 		delete b;
 		return rc;
 	}
+	ctx->live_bodies.push_back(b);
 	*out = b;
 	return B3G_OK;
+}
+
+// Device memory of a body (its context is current and its stream idle).
+static void release_body_memory(b3g_body* b)
+{
+	for (int k = 0; k < 3; ++k)
+		if (b->prec[k].mem) cudaFree(b->prec[k].mem);
+	if (b->arena) cudaFree(b->arena);
+	if (b->ray_buf) cudaFree(b->ray_buf);
+	for (int k = 0; k < 3; ++k) b->prec[k] = PrecBuffers();
+	b->arena = nullptr;
+	b->ray_buf = nullptr;
+	b->ray_cap = 0;
 }
 
 int b3g_body_destroy(b3g_body* b)
 {
 	if (!b) return B3G_OK;
-	cudaSetDevice(b->ctx->device);
-	cudaStreamSynchronize(b->ctx->stream);
-	forget_body_in_batch_cache(b->ctx, b);
-	if (std::find(b->ctx->xfer_bodies.begin(), b->ctx->xfer_bodies.end(), b) != b->ctx->xfer_bodies.end())
-		b->ctx->xfer_bodies.clear();  // a later body at the same address must not reuse the table
-	for (int k = 0; k < 3; ++k)
-		if (b->prec[k].mem) cudaFree(b->prec[k].mem);
-	cudaFree(b->arena);
-	if (b->ray_buf) cudaFree(b->ray_buf);
+	b3g_context* c = b->ctx;
+	if (!c)
+	{
+		// its context was destroyed first and already released the device memory
+		delete b;
+		return B3G_OK;
+	}
+	cudaSetDevice(c->device);
+	cudaStreamSynchronize(c->stream);
+	forget_body_in_batch_cache(c, b);
+	if (std::find(c->xfer_bodies.begin(), c->xfer_bodies.end(), b) != c->xfer_bodies.end())
+		c->xfer_bodies.clear();  // a later body at the same address must not reuse the table
+	c->live_bodies.erase(std::remove(c->live_bodies.begin(), c->live_bodies.end(), b), c->live_bodies.end());
+	release_body_memory(b);
 	delete b;
 	return B3G_OK;
 }
@@ -730,6 +757,7 @@ int b3g_body_device_bytes(const b3g_body* b, uint64_t* bytes)
 int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_step_stats* stats)
 {
 	if (!b) return fail(B3G_ERROR_INVALID_ARGUMENT, "null body");
+	if (!b->ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "the body's context was destroyed");
 	b3g_solver_config cfg;
 	if (cfg_in) cfg = *cfg_in;
 	else b3g_solver_config_default(&cfg);
@@ -812,6 +840,7 @@ int b3g_body_get_stats(b3g_body* b, b3g_step_stats* stats)
 int b3g_body_get_state(b3g_body* b, float* positions, float* velocities)
 {
 	if (!b) return fail(B3G_ERROR_INVALID_ARGUMENT, "null body");
+	if (!b->ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "the body's context was destroyed");
 	cudaStream_t st = b->ctx->stream;
 	cudaError_t e = cudaSuccess;
 	size_t bytes = 3 * (size_t)b->n * sizeof(float);
@@ -824,6 +853,7 @@ int b3g_body_get_state(b3g_body* b, float* positions, float* velocities)
 int b3g_body_set_state(b3g_body* b, const float* positions, const float* velocities)
 {
 	if (!b) return fail(B3G_ERROR_INVALID_ARGUMENT, "null body");
+	if (!b->ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "the body's context was destroyed");
 	cudaStream_t st = b->ctx->stream;
 	cudaError_t e = cudaSuccess;
 	size_t bytes = 3 * (size_t)b->n * sizeof(float);
@@ -892,6 +922,7 @@ int b3g_body_set_rotations(b3g_body* b, const float* q)
 int b3g_body_ray_cast(b3g_body* b, const float* segments, uint32_t count, b3g_ray_hit* hits)
 {
 	if (!b || (count && (!segments || !hits))) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	if (!b->ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "the body's context was destroyed");
 	if (count == 0) return B3G_OK;
 	for (uint64_t k = 0; k < 6 * (uint64_t)count; ++k)
 		if (!std::isfinite(segments[k])) return fail(B3G_ERROR_INVALID_ARGUMENT, "segment %u is not finite", (uint32_t)(k / 6));

@@ -33,6 +33,9 @@ struct b3g_context
 	std::vector<b3g_body*> xfer_bodies;
 	uint32_t xfer_max_n3 = 0;
 	uint64_t xfer_total = 0;             // floats of the flat host array (3 per vertex)
+	// live bodies: destroying the context releases their device memory and detaches them, so a
+	// later b3g_body_destroy only frees the host object
+	std::vector<b3g_body*> live_bodies;
 };
 
 namespace b3g {

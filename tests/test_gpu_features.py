@@ -373,3 +373,16 @@ def test_ray_cast_edge_cases(ctx):
     g = b3g.Body(ctx, t)
     assert not g.ray_cast(np.array([[0.1, 5, 0.1, 0.1, -5, 0.1]]))[0].any()
     g.close()
+
+
+def test_body_outliving_its_context_is_detached(ctx):
+    """Destroying a context first releases its bodies' device memory and detaches them: a later
+    b3g_body_destroy only frees the host object, and other calls report an error."""
+    lib = b3g.load_library()
+    c2 = b3g.Context(0)
+    g = b3g.Body(c2, meshes.tet_grid(3, 3, 3))
+    assert lib.b3g_context_destroy(c2.handle) == 0
+    c2.handle = None
+    with pytest.raises(b3g.B3gError, match="context was destroyed"):
+        g.step(DT, b3g.solver_config())
+    g.close()
