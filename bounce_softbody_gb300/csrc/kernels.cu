@@ -561,7 +561,24 @@ StepParams dev_params(const StepParamsHost& P)
 
 int slice_grid(const DevBody& B) { return grid_for(B.nslices, kWarps); }
 
-int vertex_grid(const DevBody& B) { return grid_for(B.n, kThreads); }
+// Grid of the per-vertex kernels (vector update, final update): at most two CTAs per SM, each
+// thread striding over several vertices. One vertex per thread (1024 CTAs on the 64³ block) made
+// the vector update 1.6x slower: every CTA pays the reduction's fence and its atomic on one
+// counter. Measured per 64³ step: 17.9 ms (one vertex a thread), 17.3 (4 CTAs/SM), 16.7 (2),
+// 17.3 (1). B3G_VERTEX_CTAS overrides the cap (tuning knob, read once).
+int vertex_grid(const DevBody& B)
+{
+	static const int cap = [] {
+		const char* e = std::getenv("B3G_VERTEX_CTAS");
+		if (e) return std::atoi(e);
+		int dev = 0, sms = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		return 2 * sms;
+	}();
+	const int g = grid_for(B.n, kThreads);
+	return cap > 0 && cap < g ? cap : g;
+}
 
 // SpMV grid: every CTA resident at once and the same whole number of slices per warp, so that
 // no partial second wave trails the launch (64³ block: 8192 slices, 608 resident CTAs of 8 warps
