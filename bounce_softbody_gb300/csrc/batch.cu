@@ -46,6 +46,8 @@ struct BatchCache
 	double g_tol2 = 0.0, g_ntol2 = 0.0;
 	std::vector<std::pair<int, double>> tune_log;  // (cluster * 1e6 + threshold, ms)
 	unsigned long long* d_prof = nullptr;          // phase cycle counters when B3G_PHASE_PROFILE=1
+	unsigned* d_tet_off = nullptr;                  // first tetrahedron of each body, flat numbering
+	unsigned ntets = 0;
 };
 
 namespace {
@@ -58,6 +60,7 @@ void free_cache(BatchCache* c)
 	cudaFree(c->d_order);
 	cudaFree(c->d_queue);
 	cudaFree(c->d_prof);
+	cudaFree(c->d_tet_off);
 	delete c;
 }
 
@@ -88,6 +91,9 @@ BatchArgs make_args(BatchCache* c, float h, int steps, const b3g_solver_config& 
 	A.cluster = c->cluster;
 	A.ctas = c->ctas;
 	A.prof = c->d_prof;
+	A.tet_off = c->d_tet_off;
+	A.ntets = c->ntets;
+	A.nbodies = (int)c->bodies.size();
 	return A;
 }
 
@@ -214,6 +220,22 @@ int build_cache(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, int p
 	cudaError_t e = cudaMalloc(&c->d_bodies, std::max<size_t>(1, count) * sizeof(DevBody));
 	if (e == cudaSuccess) e = cudaMalloc(&c->d_order, std::max<size_t>(1, count) * sizeof(int));
 	if (e == cudaSuccess) e = cudaMalloc(&c->d_queue, 4 * sizeof(unsigned));
+	std::vector<unsigned> tet_off(count + 1, 0);
+	uint64_t ntets = 0;
+	for (uint32_t k = 0; k < count; ++k)
+	{
+		tet_off[k] = (unsigned)ntets;
+		ntets += bodies[k]->nt;
+	}
+	tet_off[count] = (unsigned)ntets;
+	if (e == cudaSuccess && ntets > 0 && ntets < (1ull << 32))
+	{
+		e = cudaMalloc(&c->d_tet_off, (count + 1) * sizeof(unsigned));
+		if (e == cudaSuccess)
+			e = cudaMemcpyAsync(c->d_tet_off, tet_off.data(), (count + 1) * sizeof(unsigned), cudaMemcpyHostToDevice,
+			                    ctx->stream);
+		c->ntets = (unsigned)ntets;
+	}
 	if (e == cudaSuccess && count)
 		e = cudaMemcpyAsync(c->d_bodies, h.data(), count * sizeof(DevBody), cudaMemcpyHostToDevice, ctx->stream);
 	if (e == cudaSuccess && count)

@@ -81,6 +81,12 @@ struct BatchArgs
 	int ctas;                // CTAs of the launch (multiple of cluster)
 	unsigned long long* prof; // optional phase cycle counters (8 per CTA), null = off
 	int part = 0;            // single-Newton steps: 0 both launches, 1 assembly only, 2 PCG only
+	// single-Newton steps: the tetrahedra of all bodies in one flat launch before the assembly
+	// (tet_off[k] = first tetrahedron of bodies[k] in the flat numbering, count + 1 entries);
+	// null = in the team phase, like several Newton iterations
+	const unsigned* tet_off = nullptr;
+	unsigned ntets = 0;
+	int nbodies = 0;
 };
 cudaError_t op_batch(const BatchArgs& A, cudaStream_t st);
 // Co-resident clusters of the batch kernel for this precision and cluster size (0 on error).

@@ -44,6 +44,7 @@ struct BatchParams
 	int refresh;
 	double newton_tol2;
 	unsigned long long* prof;  // optional: kPhases cycle counters per CTA
+	int tets_done;             // the tetrahedra of the first Newton iteration ran in k_batch_tets
 };
 
 namespace {
@@ -372,7 +373,8 @@ __device__ double team_assemble(Team<CL>& T, const DevBody& B, const BatchParams
 	StepParams sp;
 	sp.h = P.h;
 	sp.first_newton = k == 0 ? 1 : 0;
-	for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LD>(B, e, sp);
+	if (!(k == 0 && P.tets_done))
+		for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LD>(B, e, sp);
 	for (int e = T.tid(); e < B.ntr; e += T.nthreads()) tri_element<LD>(B, e, sp);
 	for (int e = T.tid(); e < B.ns; e += T.nthreads()) spring_element<LD>(B, e, sp);
 	for (int e = T.tid(); e < B.nbw; e += T.nthreads()) bw_element<LD>(B, e, sp);
