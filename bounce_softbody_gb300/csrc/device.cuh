@@ -90,56 +90,6 @@ __device__ __forceinline__ uint2 mat_ld8<MatCG>(const void* p, unsigned long lon
 	return r;
 }
 
-// single words of the matrix stream (the ragged last group of a slice)
-template <class M>
-__device__ __forceinline__ unsigned mat_ld4b(const void* p, unsigned long long pol);
-template <>
-__device__ __forceinline__ unsigned mat_ld4b<MatNC>(const void* p, unsigned long long pol)
-{
-	unsigned r;
-	asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
-	return r;
-}
-template <>
-__device__ __forceinline__ unsigned mat_ld4b<MatCG>(const void* p, unsigned long long pol)
-{
-	unsigned r;
-	asm volatile("ld.global.cg.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
-	return r;
-}
-template <class M>
-__device__ __forceinline__ unsigned long long mat_ld8b(const void* p, unsigned long long pol);
-template <>
-__device__ __forceinline__ unsigned long long mat_ld8b<MatNC>(const void* p, unsigned long long pol)
-{
-	unsigned long long r;
-	asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(pol));
-	return r;
-}
-template <>
-__device__ __forceinline__ unsigned long long mat_ld8b<MatCG>(const void* p, unsigned long long pol)
-{
-	unsigned long long r;
-	asm volatile("ld.global.cg.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(pol));
-	return r;
-}
-template <class M>
-__device__ __forceinline__ unsigned short mat_ld2b(const void* p, unsigned long long pol);
-template <>
-__device__ __forceinline__ unsigned short mat_ld2b<MatNC>(const void* p, unsigned long long pol)
-{
-	unsigned short r;
-	asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(r) : "l"(p), "l"(pol));
-	return r;
-}
-template <>
-__device__ __forceinline__ unsigned short mat_ld2b<MatCG>(const void* p, unsigned long long pol)
-{
-	unsigned short r;
-	asm volatile("ld.global.cg.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(r) : "l"(p), "l"(pol));
-	return r;
-}
-
 // ------------------------------------------------------------------ 4-wide solver vectors
 // Component c of vertex i at 4 i + c (the fourth component is padding, kept zero).
 template <class TV, class L>
@@ -1167,7 +1117,6 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	const float h = P.h;
 	const int w = B.rowlen[i];
 	const int base = B.slice_ptr[slice];
-	const int ws = (B.slice_ptr[slice + 1] - base) / kSlice;  // slice width (the slot layout's)
 	const bool Si = B.type[i] == B3G_DYNAMIC;
 	const float* X = P.first_newton ? B.x : B.xi;
 	const float* Vv = P.first_newton ? B.v : B.vi;
@@ -1281,7 +1230,7 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	for (int k = 0; k < w; ++k)
 	{
 		const int slot = base + k * kSlice + lane;           // contribution-list item
-		const size_t bs = block_slot((size_t)base, k, lane, ws); // block storage
+		const size_t bs = block_slot((size_t)base, k, lane); // block storage
 		const int j = B.col[bs];
 		const uint32_t st = st_n;
 		const int cnt = cnt_n;
@@ -1531,56 +1480,9 @@ __device__ __forceinline__ int4 mat_cols(const int* p, unsigned long long, MatVi
 __device__ __forceinline__ int4 mat_cols(const int* p, unsigned long long pol, MatNC*) { return hinted_cols<MatNC>(p, pol); }
 __device__ __forceinline__ int4 mat_cols(const int* p, unsigned long long pol, MatCG*) { return hinted_cols<MatCG>(p, pol); }
 
-// one block entry / column id of the ragged last group, by matrix stream
-template <class L>
-__device__ __forceinline__ float mat_load1(const float* p, unsigned long long, MatVia<L>*) { return L::ld(p); }
-template <class L>
-__device__ __forceinline__ double mat_load1(const double* p, unsigned long long, MatVia<L>*) { return L::ld(p); }
-template <class L>
-__device__ __forceinline__ float mat_load1(const __nv_bfloat16* p, unsigned long long, MatVia<L>*)
-{
-	return __bfloat162float(L::ld(p));
-}
-template <class M>
-__device__ __forceinline__ float mat_load1(const float* p, unsigned long long pol, M*)
-{
-	return __uint_as_float(mat_ld4b<M>(p, pol));
-}
-template <class M>
-__device__ __forceinline__ double mat_load1(const double* p, unsigned long long pol, M*)
-{
-	return __longlong_as_double((long long)mat_ld8b<M>(p, pol));
-}
-template <class M>
-__device__ __forceinline__ float mat_load1(const __nv_bfloat16* p, unsigned long long pol, M*)
-{
-	return __uint_as_float((unsigned)mat_ld2b<M>(p, pol) << 16);
-}
-template <class L>
-__device__ __forceinline__ int mat_col1(const int* p, unsigned long long, MatVia<L>*) { return __ldg(p); }
-template <class M>
-__device__ __forceinline__ int mat_col1(const int* p, unsigned long long pol, M*) { return (int)mat_ld4b<M>(p, pol); }
-
-// The ragged last group of a slice: gs (1..3) blocks per lane at off, gs * lane apart, read with
-// single loads; entries past gs are zero and their column is 0 (never gathered).
-template <class TA, class M>
-__device__ __forceinline__ void mat_tail(const TA* A, const int* __restrict__ col, size_t ns, size_t off, int gs,
-                                         unsigned long long pol, typename Acc<TA>::type a[9][4], int js[4])
-{
-#pragma unroll
-	for (int u = 0; u < 4; ++u)
-	{
-		js[u] = (u < gs) ? mat_col1(col + off + u, pol, (M*)nullptr) : 0;
-#pragma unroll
-		for (int p = 0; p < 9; ++p)
-			a[p][u] = (u < gs) ? mat_load1(A + p * ns + off + u, pol, (M*)nullptr) : (typename Acc<TA>::type)0;
-	}
-}
-
-// q_i = (A x)_i for row i = 32 s + lane of a slice of width w. Per full group of four blocks a
-// lane issues one 16-byte load of column ids, one vector load per value plane and four 16-byte
-// gathers of x, all before the first FMA; the ragged last group (w % 4 blocks) is read with
-// single loads. Padding blocks are zero.
+// q_i = (A x)_i for row i = 32 s + lane of a slice of width w (a multiple of 4). Per group of
+// four blocks a lane issues one 16-byte load of column ids, one vector load per value plane and
+// four 16-byte gathers of x, all before the first FMA. Padding blocks are zero.
 template <class TA, class TV, class L = LdPlain, class M = MatNC>
 __device__ __forceinline__ void spmv_row(const TA* A, const int* __restrict__ col, int nslots, int base, int w,
                                          int lane, const TV* x, TV out[3])
@@ -1589,10 +1491,9 @@ __device__ __forceinline__ void spmv_row(const TA* A, const int* __restrict__ co
 	AT o0 = 0, o1 = 0, o2 = 0;
 	const size_t ns = (size_t)nslots;
 	const unsigned long long pol = evict_first_policy();
-	const int wf = w & ~(kGroup - 1);
-	for (int k = 0; k < wf; k += kGroup)
+	for (int k = 0; k < w; k += kGroup)
 	{
-		const size_t off = block_slot((size_t)base, k, lane, w);
+		const size_t off = block_slot((size_t)base, k, lane);
 		const int4 jj = mat_cols(col + off, pol, (M*)nullptr);
 		AT a[9][4];
 #pragma unroll
@@ -1611,27 +1512,6 @@ __device__ __forceinline__ void spmv_row(const TA* A, const int* __restrict__ co
 			o2 += a[6][u] * x0 + a[7][u] * x1 + a[8][u] * x2;
 		}
 	}
-	if (wf < w)
-	{
-		// the ragged last group: all its loads in flight at once, like a full group
-		const int gs = w - wf;
-		AT a[9][4];
-		int js[4];
-		mat_tail<TA, M>(A, col, ns, block_slot((size_t)base, wf, lane, w), gs, pol, a, js);
-		TV xv[3][3];
-#pragma unroll
-		for (int u = 0; u < 3; ++u)
-			if (u < gs) vld<TV, L>(x, js[u], xv[u]);
-#pragma unroll
-		for (int u = 0; u < 3; ++u)
-			if (u < gs)
-			{
-				const AT x0 = (AT)xv[u][0], x1 = (AT)xv[u][1], x2 = (AT)xv[u][2];
-				o0 += a[0][u] * x0 + a[1][u] * x1 + a[2][u] * x2;
-				o1 += a[3][u] * x0 + a[4][u] * x1 + a[5][u] * x2;
-				o2 += a[6][u] * x0 + a[7][u] * x1 + a[8][u] * x2;
-			}
-	}
 	out[0] = (TV)o0;
 	out[1] = (TV)o1;
 	out[2] = (TV)o2;
@@ -1648,23 +1528,15 @@ __device__ __forceinline__ void spmv_row_ff(const float* A, const int* __restric
 	const unsigned long long pol = evict_first_policy();
 	for (int k = 0; k < w; k += kGroup)
 	{
-		const size_t off = block_slot((size_t)base, k, lane, w);
-		const int gs = w - k < kGroup ? w - k : kGroup;
+		const size_t off = block_slot((size_t)base, k, lane);
+		const int4 jj = mat_cols(col + off, pol, (MatNC*)nullptr);
 		float a[9][4];
-		int js[4];
-		if (gs == kGroup)
-		{
-			const int4 jj = mat_cols(col + off, pol, (MatNC*)nullptr);
 #pragma unroll
-			for (int p = 0; p < 9; ++p) mat_load4(A + p * ns + off, a[p], pol, (MatNC*)nullptr);
-			js[0] = jj.x; js[1] = jj.y; js[2] = jj.z; js[3] = jj.w;
-		}
-		else
-			mat_tail<float, MatNC>(A, col, ns, off, gs, pol, a, js);
+		for (int p = 0; p < 9; ++p) mat_load4(A + p * ns + off, a[p], pol, (MatNC*)nullptr);
+		const int js[4] = {jj.x, jj.y, jj.z, jj.w};
 #pragma unroll
 		for (int u = 0; u < 4; ++u)
 		{
-			if (u >= gs) break;
 			float xh[3], xl[3];
 			ff_ld(xff, js[u], xh, xl);
 #pragma unroll
@@ -1718,10 +1590,9 @@ __device__ __forceinline__ void spmv_row_dir(const TA* A, const int* __restrict_
 	AT o0 = 0, o1 = 0, o2 = 0;
 	const size_t ns = (size_t)nslots;
 	const unsigned long long pol = evict_first_policy();
-	const int wf = w & ~(kGroup - 1);
-	for (int k = 0; k < wf; k += kGroup)
+	for (int k = 0; k < w; k += kGroup)
 	{
-		const size_t off = block_slot((size_t)base, k, lane, w);
+		const size_t off = block_slot((size_t)base, k, lane);
 		const int4 jj = mat_cols(col + off, pol, (M*)nullptr);
 		AT a[9][4];
 #pragma unroll
@@ -1744,32 +1615,6 @@ __device__ __forceinline__ void spmv_row_dir(const TA* A, const int* __restrict_
 			o1 += a[3][u] * x0 + a[4][u] * x1 + a[5][u] * x2;
 			o2 += a[6][u] * x0 + a[7][u] * x1 + a[8][u] * x2;
 		}
-	}
-	if (wf < w)
-	{
-		// the ragged last group: all its loads in flight at once, like a full group
-		const int gs = w - wf;
-		AT a[9][4];
-		int js[4];
-		mat_tail<TA, M>(A, col, ns, block_slot((size_t)base, wf, lane, w), gs, pol, a, js);
-		TV xv[3][3];
-#pragma unroll
-		for (int u = 0; u < 3; ++u)
-			if (u < gs) gather_dir<TV, L>(s, d, beta, first, js[u], xv[u]);
-		if (wf == 0)
-		{
-#pragma unroll
-			for (int c = 0; c < 3; ++c) dn[c] = xv[0][c];
-		}
-#pragma unroll
-		for (int u = 0; u < 3; ++u)
-			if (u < gs)
-			{
-				const AT x0 = (AT)xv[u][0], x1 = (AT)xv[u][1], x2 = (AT)xv[u][2];
-				o0 += a[0][u] * x0 + a[1][u] * x1 + a[2][u] * x2;
-				o1 += a[3][u] * x0 + a[4][u] * x1 + a[5][u] * x2;
-				o2 += a[6][u] * x0 + a[7][u] * x1 + a[8][u] * x2;
-			}
 	}
 	out[0] = (TV)o0;
 	out[1] = (TV)o1;

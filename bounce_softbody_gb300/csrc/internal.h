@@ -3,17 +3,13 @@
 //
 // Matrix storage: sliced block-ELL with 32 rows per slice ("SELL-32", one warp per slice, one
 // lane per block row). Slice s owns slots [slice_ptr[s], slice_ptr[s+1]) = width_s * 32 slots,
-// width_s = the longest row of the slice. Its blocks form groups of kGroup = 4 (the last group
-// of a slice holds the width_s % 4 remaining ones when that is not zero); the k-th block of row
-// i = 32 s + lane sits in
-//   block_slot(s, k, lane, width_s) = slice_ptr[s] + 128 (k / 4) + g lane + k % 4,
-// g = the size of k's group, so one lane's blocks of a group are adjacent: a lane loads each of
-// the 9 value planes of a full group, and their column ids, as single 16-byte vectors, and a
-// warp's loads cover 512 consecutive bytes; the ragged last group is read with scalar loads
-// (no padding to a multiple of four: interior rows of a tetrahedral grid have 15 blocks).
-// Plane p (entry p = 3 * row + col of a 3x3 block) of every slot lives at p * nslots + slot.
-// Slots past the end of a row hold zero blocks whose column is the row itself. The diagonal
-// block is always k = 0.
+// width_s a multiple of kGroup = 4. The k-th block of row i = 32 s + lane sits in
+//   block_slot(s, k, lane) = slice_ptr[s] + 128 (k / 4) + 4 lane + k % 4,
+// so one lane's four consecutive blocks are adjacent: a lane loads each of the 9 value planes of
+// a group of four blocks, and their column ids, as single 16-byte vectors, and a warp's loads
+// cover 512 consecutive bytes. Plane p (entry p = 3 * row + col of a 3x3 block) of every slot
+// lives at p * nslots + slot. Slots past the end of a row hold zero blocks whose column is the
+// row itself. The diagonal block is always k = 0.
 // Per-slot contribution lists use the item index list_item(s, k, lane) = slice_ptr[s] + 32 k +
 // lane (same range, different order) so that a warp reading the lists of its 32 rows at one k
 // touches consecutive words.
@@ -43,12 +39,7 @@ namespace b3g {
 constexpr int kSlice = 32;
 constexpr int kGroup = 4;
 
-B3G_HD size_t block_slot(size_t base, int k, int lane, int width)
-{
-	const int g0 = k & ~3;
-	const int gs = width - g0 < 4 ? width - g0 : 4;
-	return base + 128 * (size_t)(k >> 2) + (size_t)gs * lane + (k & 3);
-}
+B3G_HD size_t block_slot(size_t base, int k, int lane) { return base + 128 * (size_t)(k >> 2) + 4 * lane + (k & 3); }
 constexpr int kMaxWorld = 16;   // world fixtures per body
 constexpr int kMaxTeamCtas = 16;
 

@@ -265,6 +265,7 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 	{
 		int w = 0;
 		for (int l = 0; l < kSlice; ++l) w = std::max(w, (int)rowlen[s * kSlice + l]);
+		w = (w + kGroup - 1) / kGroup * kGroup;  // whole groups of kGroup slots
 		P.maxw = std::max(P.maxw, w);
 		slice_ptr[s + 1] = slice_ptr[s] + w * kSlice;
 	}
@@ -273,7 +274,7 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 	auto slot_of = [&](uint32_t i, uint32_t k) -> uint32_t {
 		return (uint32_t)slice_ptr[i / kSlice] + k * kSlice + (i % kSlice);
 	};
-	// block slots: block_slot(s, k, lane, w) (groups of four, a ragged last group)
+	// block slots: block_slot(s, k, lane) = slice_ptr[s] + 128 (k / 4) + 4 lane + k % 4
 	std::vector<int> col(P.nslots, 0);
 	for (int s = 0; s < P.nslices; ++s)
 		for (int l = 0; l < kSlice; ++l)
@@ -281,7 +282,7 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 			uint32_t i = (uint32_t)(s * kSlice + l);
 			int w = (slice_ptr[s + 1] - slice_ptr[s]) / kSlice;
 			for (int k = 0; k < w; ++k)
-				col[block_slot(slice_ptr[s], k, l, w)] =
+				col[block_slot(slice_ptr[s], k, l)] =
 				    (i < n && (uint32_t)k < rowlen[i]) ? (int)cols[rowptr[i] + k] : (int)std::min<uint32_t>(i, n - 1);
 		}
 
