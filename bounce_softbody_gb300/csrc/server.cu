@@ -293,6 +293,8 @@ struct b3g_server
 	unsigned* d_queue = nullptr;
 	DevBody* h_table = nullptr;  // pinned
 	int* h_order = nullptr;      // pinned
+	unsigned* d_tet_off = nullptr;  // first tetrahedron of each table entry (flat numbering), + total
+	unsigned* h_tet_off = nullptr;  // pinned
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 	// statistics
 	std::vector<float> step_ms;
@@ -474,6 +476,14 @@ int prepare(b3g_server* s, const std::vector<uint32_t>& act, int* nbig)
 		s->h_table[k] = dev_for(B.body, prec, s->cfg.preconditioner);
 		s->h_order[k] = (int)k;
 	}
+	// the flat numbering of the active bodies' tetrahedra for the tetrahedron launch
+	uint64_t nt = 0;
+	for (size_t k = 0; k < act.size(); ++k)
+	{
+		s->h_tet_off[k] = (unsigned)nt;
+		nt += s->h_table[k].nt;
+	}
+	s->h_tet_off[act.size()] = nt < (1ull << 32) ? (unsigned)nt : 0u;
 	std::stable_sort(s->h_order, s->h_order + act.size(),
 	                 [&](int a, int b) { return s->bodies[act[a]].h.n > s->bodies[act[b]].h.n; });
 	// One schedule for every launch: bodies of kServerThreshold vertices or more are stepped by
@@ -492,6 +502,8 @@ int step_active(b3g_server* s, int count, int nbig)
 	cudaStream_t st = s->ctx->stream;
 	cudaError_t e = cudaMemcpyAsync(s->d_table, s->h_table, count * sizeof(DevBody), cudaMemcpyHostToDevice, st);
 	if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_order, s->h_order, count * sizeof(int), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(s->d_tet_off, s->h_tet_off, (count + 1) * sizeof(unsigned), cudaMemcpyHostToDevice, st);
 	if (e != cudaSuccess) return cuda_fail(e, "server upload");
 	int m = batch_max_clusters(prec, s->cluster);
 	if (m <= 0) m = std::max(1, s->ctx->sm_count / s->cluster);
@@ -513,6 +525,9 @@ int step_active(b3g_server* s, int count, int nbig)
 	A.cluster = s->cluster;
 	A.ctas = m * s->cluster;
 	A.prof = nullptr;
+	A.tet_off = s->d_tet_off;
+	A.ntets = s->h_tet_off[count];
+	A.nbodies = count;
 	cudaEventRecord(s->ev0, st);
 	e = op_batch(A, st);
 	cudaEventRecord(s->ev1, st);
@@ -623,6 +638,8 @@ int b3g_server_create(b3g_context* ctx, uint64_t memory_budget_bytes, uint32_t m
 	while (s->cluster > 1 && batch_max_clusters(prec_of(&s->cfg), s->cluster) <= 0) s->cluster /= 2;
 	cudaError_t e = cudaMalloc(&s->d_table, max_active * sizeof(DevBody));
 	if (e == cudaSuccess) e = cudaMalloc(&s->d_order, max_active * sizeof(int));
+	if (e == cudaSuccess) e = cudaMalloc(&s->d_tet_off, (max_active + 1) * sizeof(unsigned));
+	if (e == cudaSuccess) e = cudaMallocHost(&s->h_tet_off, (max_active + 1) * sizeof(unsigned));
 	if (e == cudaSuccess) e = cudaMalloc(&s->d_queue, 4 * sizeof(unsigned));
 	if (e == cudaSuccess) e = cudaMallocHost(&s->h_table, max_active * sizeof(DevBody));
 	if (e == cudaSuccess) e = cudaMallocHost(&s->h_order, max_active * sizeof(int));
@@ -632,9 +649,11 @@ int b3g_server_create(b3g_context* ctx, uint64_t memory_budget_bytes, uint32_t m
 	{
 		cudaFree(s->d_table);
 		cudaFree(s->d_order);
+		cudaFree(s->d_tet_off);
 		cudaFree(s->d_queue);
 		cudaFreeHost(s->h_table);
 		cudaFreeHost(s->h_order);
+		cudaFreeHost(s->h_tet_off);
 		delete s;
 		return cuda_fail(e, "server setup");
 	}
@@ -794,9 +813,11 @@ int b3g_server_destroy(b3g_server* s)
 	cudaEventDestroy(s->ev1);
 	cudaFree(s->d_table);
 	cudaFree(s->d_order);
+	cudaFree(s->d_tet_off);
 	cudaFree(s->d_queue);
 	cudaFreeHost(s->h_table);
 	cudaFreeHost(s->h_order);
+	cudaFreeHost(s->h_tet_off);
 	delete s;
 	return B3G_OK;
 }
