@@ -46,8 +46,8 @@ struct BatchCache
 	double g_tol2 = 0.0, g_ntol2 = 0.0;
 	std::vector<std::pair<int, double>> tune_log;  // (cluster * 1e6 + threshold, ms)
 	unsigned long long* d_prof = nullptr;          // phase cycle counters when B3G_PHASE_PROFILE=1
-	unsigned* d_tet_off = nullptr;                  // first tetrahedron of each body, flat numbering
-	unsigned ntets = 0;
+	unsigned* d_flat_off = nullptr;                 // flat numbering: element offsets, then slice offsets
+	unsigned nelem = 0, nslices = 0;
 };
 
 namespace {
@@ -60,7 +60,7 @@ void free_cache(BatchCache* c)
 	cudaFree(c->d_order);
 	cudaFree(c->d_queue);
 	cudaFree(c->d_prof);
-	cudaFree(c->d_tet_off);
+	cudaFree(c->d_flat_off);
 	delete c;
 }
 
@@ -91,8 +91,10 @@ BatchArgs make_args(BatchCache* c, float h, int steps, const b3g_solver_config& 
 	A.cluster = c->cluster;
 	A.ctas = c->ctas;
 	A.prof = c->d_prof;
-	A.tet_off = c->d_tet_off;
-	A.ntets = c->ntets;
+	A.elem_off = c->d_flat_off;
+	A.slice_off = c->d_flat_off ? c->d_flat_off + c->bodies.size() + 1 : nullptr;
+	A.nelem = c->nelem;
+	A.nslices = c->nslices;
 	A.nbodies = (int)c->bodies.size();
 	return A;
 }
@@ -220,21 +222,26 @@ int build_cache(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, int p
 	cudaError_t e = cudaMalloc(&c->d_bodies, std::max<size_t>(1, count) * sizeof(DevBody));
 	if (e == cudaSuccess) e = cudaMalloc(&c->d_order, std::max<size_t>(1, count) * sizeof(int));
 	if (e == cudaSuccess) e = cudaMalloc(&c->d_queue, 4 * sizeof(unsigned));
-	std::vector<unsigned> tet_off(count + 1, 0);
-	uint64_t ntets = 0;
+	// flat numbering of all bodies' elements and row slices (count + 1 offsets each)
+	std::vector<unsigned> off(2 * (size_t)(count + 1), 0);
+	uint64_t ne = 0, nsl = 0;
 	for (uint32_t k = 0; k < count; ++k)
 	{
-		tet_off[k] = (unsigned)ntets;
-		ntets += bodies[k]->nt;
+		off[k] = (unsigned)ne;
+		off[count + 1 + k] = (unsigned)nsl;
+		ne += (uint64_t)h[k].nt + h[k].ntr + h[k].ns + h[k].nbw + h[k].nms;
+		nsl += (uint64_t)h[k].nslices;
 	}
-	tet_off[count] = (unsigned)ntets;
-	if (e == cudaSuccess && ntets > 0 && ntets < (1ull << 32))
+	off[count] = (unsigned)ne;
+	off[2 * (size_t)count + 1] = (unsigned)nsl;
+	if (e == cudaSuccess && count && ne < (1ull << 32) && nsl < (1ull << 32))
 	{
-		e = cudaMalloc(&c->d_tet_off, (count + 1) * sizeof(unsigned));
+		e = cudaMalloc(&c->d_flat_off, off.size() * sizeof(unsigned));
 		if (e == cudaSuccess)
-			e = cudaMemcpyAsync(c->d_tet_off, tet_off.data(), (count + 1) * sizeof(unsigned), cudaMemcpyHostToDevice,
+			e = cudaMemcpyAsync(c->d_flat_off, off.data(), off.size() * sizeof(unsigned), cudaMemcpyHostToDevice,
 			                    ctx->stream);
-		c->ntets = (unsigned)ntets;
+		c->nelem = (unsigned)ne;
+		c->nslices = (unsigned)nsl;
 	}
 	if (e == cudaSuccess && count)
 		e = cudaMemcpyAsync(c->d_bodies, h.data(), count * sizeof(DevBody), cudaMemcpyHostToDevice, ctx->stream);

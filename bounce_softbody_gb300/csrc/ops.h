@@ -81,11 +81,15 @@ struct BatchArgs
 	int ctas;                // CTAs of the launch (multiple of cluster)
 	unsigned long long* prof; // optional phase cycle counters (8 per CTA), null = off
 	int part = 0;            // single-Newton steps: 0 both launches, 1 assembly only, 2 PCG only
-	// single-Newton steps: the tetrahedra of all bodies in one flat launch before the assembly
-	// (tet_off[k] = first tetrahedron of bodies[k] in the flat numbering, count + 1 entries);
-	// null = in the team phase, like several Newton iterations
-	const unsigned* tet_off = nullptr;
-	unsigned ntets = 0;
+	// single-Newton steps: the elements, then the rows, of all bodies in two flat launches before
+	// the PCG launch. elem_off[k] / slice_off[k]: first element / row slice of bodies[k] in the
+	// flat numbering (count + 1 entries each; elements of a body: tetrahedra, triangles, springs,
+	// stretch/shear triangles, mouse springs). Null = the team launches do both, as for several
+	// Newton iterations.
+	const unsigned* elem_off = nullptr;
+	const unsigned* slice_off = nullptr;
+	unsigned nelem = 0;
+	unsigned nslices = 0;
 	int nbodies = 0;
 };
 cudaError_t op_batch(const BatchArgs& A, cudaStream_t st);

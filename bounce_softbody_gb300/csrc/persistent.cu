@@ -5,35 +5,48 @@ namespace b3g {
 
 namespace {
 
-constexpr int kTetThreads = 256;
+constexpr int kElemThreads = 256;
 
-// The tetrahedra of every body of a batch, first Newton iteration of a step, one per thread over
-// a flat numbering (tet_off: first tetrahedron of each body). Separate from the team launch so
-// that it runs at its own register budget (80, 3 CTAs per SM) instead of the 128 the row
-// assembly needs: the rotation extraction's dependent chain wants the extra warps. The state it
-// reads was written by earlier launches, so plain (L1) loads.
-__global__ void __launch_bounds__(kTetThreads, 3)
-k_batch_tets(const DevBody* __restrict__ bodies, const unsigned* __restrict__ tet_off, int nbodies, unsigned ntets,
-             float h)
+// The elements of every body of a batch (tetrahedra, triangles, springs, stretch / shear
+// triangles, mouse springs; first Newton iteration of a step), one per thread over a flat
+// numbering (elem_off: first element of each body). Its own launch runs at its own register
+// budget (3 CTAs per SM) instead of the 128 registers the row assembly needs: the tetrahedra's
+// rotation extraction, a dependent chain, wants the extra warps. The state it reads was written
+// by earlier launches, so plain (L1) loads.
+__global__ void __launch_bounds__(kElemThreads, 3) k_batch_elements(BatchParams P)
 {
 	StepParams sp;
-	sp.h = h;
+	sp.h = P.h;
 	sp.first_newton = 1;
-	for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < ntets; g += gridDim.x * blockDim.x)
+	for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < P.nelem; g += gridDim.x * blockDim.x)
 	{
-		// the body whose range holds g: the last k with tet_off[k] <= g
-		int lo = 0, hi = nbodies - 1;
-		while (lo < hi)
+		const int b = flat_body(P.elem_off, P.nbodies, g);
+		const DevBody& B = P.bodies[b];
+		int e = (int)(g - __ldg(P.elem_off + b));
+		if (e < B.nt)
 		{
-			const int mid = (lo + hi + 1) >> 1;
-			if (__ldg(tet_off + mid) <= g) lo = mid;
-			else hi = mid - 1;
+			tet_element<LdPlain>(B, e, sp);
+			continue;
 		}
-		tet_element<LdPlain>(bodies[lo], (int)(g - __ldg(tet_off + lo)), sp);
+		e -= B.nt;
+		if (e < B.ntr)
+		{
+			tri_element<LdPlain>(B, e, sp);
+			continue;
+		}
+		e -= B.ntr;
+		if (e < B.ns)
+		{
+			spring_element<LdPlain>(B, e, sp);
+			continue;
+		}
+		e -= B.ns;
+		if (e < B.nbw) bw_element<LdPlain>(B, e, sp);
+		else mouse_element<LdPlain>(B, e - B.nbw, sp);
 	}
 }
 
-int tet_grid(unsigned ntets)
+int elem_grid(unsigned nelem)
 {
 	static const int cap = [] {
 		int dev = 0, sms = 0;
@@ -41,7 +54,7 @@ int tet_grid(unsigned ntets)
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 		return 3 * (sms > 0 ? sms : 1);
 	}();
-	const unsigned g = (ntets + kTetThreads - 1) / kTetThreads;
+	const unsigned g = (nelem + kElemThreads - 1) / kElemThreads;
 	return (int)(g < (unsigned)cap ? (g > 0 ? g : 1) : cap);
 }
 
@@ -71,18 +84,27 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 	P.refresh = A.refresh;
 	P.newton_tol2 = A.newton_tol2;
 	P.prof = A.prof;
-	P.tets_done = 0;
+	P.elem_off = A.elem_off;
+	P.slice_off = A.slice_off;
+	P.nelem = A.nelem;
+	P.nslices = A.nslices;
+	P.nbodies = A.nbodies;
+	// a single Newton iteration with the flat numbering: elements and rows in two flat launches,
+	// then the PCG launch (which knows from `flat` to sum delta0 itself)
+	P.flat = (P.newton == 1 && A.elem_off && A.slice_off && A.nslices > 0) ? 1 : 0;
 	if (A.part != 2)
 	{
 		// two counters per launch; the solve-only part reuses what the assembly part cleared
 		cudaError_t e = cudaMemsetAsync(A.queue, 0, 4 * sizeof(unsigned), st);
 		if (e != cudaSuccess) return e;
-		if (P.newton == 1 && A.tet_off && A.ntets > 0)
+		if (P.flat)
 		{
-			k_batch_tets<<<tet_grid(A.ntets), kTetThreads, 0, st>>>(A.bodies, A.tet_off, A.nbodies, A.ntets, A.h);
+			if (A.nelem > 0) k_batch_elements<<<elem_grid(A.nelem), kElemThreads, 0, st>>>(P);
 			e = cudaGetLastError();
-			if (e != cudaSuccess) return e;
-			P.tets_done = 1;
+			if (e == cudaSuccess)
+				e = A.prec == kP64 ? launch_rows_f64(P, st)
+				                   : (A.prec == kPBF ? launch_rows_bf16(P, st) : launch_rows_f32(P, st));
+			if (e != cudaSuccess || A.part == 1) return e;
 		}
 	}
 	if (A.prec == kP64) return launch_batch_f64(P, A.cluster, A.ctas, A.part, st);

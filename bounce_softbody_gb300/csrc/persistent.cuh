@@ -44,7 +44,14 @@ struct BatchParams
 	int refresh;
 	double newton_tol2;
 	unsigned long long* prof;  // optional: kPhases cycle counters per CTA
-	int tets_done;             // the tetrahedra of the first Newton iteration ran in k_batch_tets
+	// flat: the single Newton iteration's elements and rows ran in the flat launches (their
+	// numbering below); the PCG launch then starts by summing delta0 = r.s itself
+	int flat;
+	const unsigned* elem_off;
+	const unsigned* slice_off;
+	unsigned nelem;
+	unsigned nslices;
+	int nbodies;
 };
 
 namespace {
@@ -373,8 +380,7 @@ __device__ double team_assemble(Team<CL>& T, const DevBody& B, const BatchParams
 	StepParams sp;
 	sp.h = P.h;
 	sp.first_newton = k == 0 ? 1 : 0;
-	if (!(k == 0 && P.tets_done))
-		for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LD>(B, e, sp);
+	for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LD>(B, e, sp);
 	for (int e = T.tid(); e < B.ntr; e += T.nthreads()) tri_element<LD>(B, e, sp);
 	for (int e = T.tid(); e < B.ns; e += T.nthreads()) spring_element<LD>(B, e, sp);
 	for (int e = T.tid(); e < B.nbw; e += T.nthreads()) bw_element<LD>(B, e, sp);
@@ -503,7 +509,30 @@ __device__ void team_step_solve(Team<CL>& T, const DevBody& B, const BatchParams
 	const int lane = threadIdx.x & 31;
 	PhaseClock pc;
 	pc.start(P.prof);
-	const double delta0 = __ldcg(&B.sc->delta0);
+	double delta0;
+	if (P.flat)
+	{
+		// the flat row launch left r and s: delta0 = r.s, summed in the order the team assembly
+		// sums it (each warp its slices, then the team), so it is the same value bitwise
+		double part = 0.0;
+		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
+		{
+			const int i = sl * kSlice + lane;
+			if (i >= B.n) continue;
+			TV rr[3], ss[3];
+			vld<TV, LD>((const TV*)B.r, i, rr);
+			vld<TV, LD>((const TV*)B.s, i, ss);
+			part += dot3<TV>(rr, ss);
+		}
+		delta0 = T.reduce(part);
+		if (T.tid() == 0)
+		{
+			B.sc->fault = 0;
+			B.sc->delta0 = delta0;
+		}
+	}
+	else
+		delta0 = __ldcg(&B.sc->delta0);
 	const SolveOut so = team_pcg<CL, TA, TV, LD>(T, B, P, bf16, delta0, pc);
 	T.sync();
 	double part = 0.0;
@@ -657,13 +686,62 @@ template <int CL, class TA, class TV>
 cudaError_t launch_cl(const BatchParams& P, int ctas, int bf16, int part, cudaStream_t st)
 {
 	if (P.newton > 1) return launch_ph<CL, TA, TV, kPhaseWhole>(P, ctas, bf16, st);
-	if (part != 2)
+	if (part != 2 && !P.flat)
 	{
 		cudaError_t e = launch_ph<CL, TA, TV, kPhaseAssemble>(P, ctas, bf16, st);
 		if (e != cudaSuccess || part == 1) return e;
 	}
 	const int m = solve_clusters<CL, TA, TV>();
 	return launch_ph<CL, TA, TV, kPhaseSolve>(P, m > 0 ? m * CL : ctas, bf16, st);
+}
+
+// The body of flat item g: the last k with off[k] <= g.
+__device__ __forceinline__ int flat_body(const unsigned* __restrict__ off, int nbodies, unsigned g)
+{
+	int lo = 0, hi = nbodies - 1;
+	while (lo < hi)
+	{
+		const int mid = (lo + hi + 1) >> 1;
+		if (__ldg(off + mid) <= g) lo = mid;
+		else hi = mid - 1;
+	}
+	return lo;
+}
+
+// The row assembly of every body of a batch, one warp per slice over a flat numbering of all
+// bodies' slices: no team, no barrier, and the load spreads evenly over the GPU whatever the
+// bodies' sizes (the team launch's tail was set by its largest bodies). Element records come from
+// the flat element launch before it, state from earlier launches: plain loads. The PCG launch
+// sums delta0 = r.s per body itself.
+template <class TA, class TV>
+__global__ void __launch_bounds__(kPThreads, B3G_BATCH_MIN_BLOCKS) k_batch_rows(BatchParams P)
+{
+	const int lane = threadIdx.x & 31;
+	StepParams sp;
+	sp.h = P.h;
+	sp.first_newton = 1;
+	const unsigned nw = gridDim.x * kPWarps;
+	for (unsigned g = blockIdx.x * kPWarps + (threadIdx.x >> 5); g < P.nslices; g += nw)
+	{
+		const int b = flat_body(P.slice_off, P.nbodies, g);
+		assemble_row<TA, TV, LdPlain>(P.bodies[b], (int)(g - __ldg(P.slice_off + b)), lane, sp, true);
+	}
+}
+
+template <class TA, class TV>
+cudaError_t launch_rows(const BatchParams& P, cudaStream_t st)
+{
+	static const int resident = [] {
+		int dev = 0, sms = 0, per_sm = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_rows<TA, TV>, kPThreads, 0);
+		return std::max(1, sms * std::max(per_sm, 1));
+	}();
+	const unsigned need = (P.nslices + kPWarps - 1) / kPWarps;
+	const int grid = (int)std::max(1u, std::min(need, (unsigned)resident));
+	k_batch_rows<TA, TV><<<grid, kPThreads, 0, st>>>(P);
+	return cudaGetLastError();
 }
 
 template <class TA, class TV>
@@ -709,6 +787,9 @@ int max_clusters_prec(int cluster)
 cudaError_t launch_batch_f32(const BatchParams& P, int cluster, int ctas, int part, cudaStream_t st);
 cudaError_t launch_batch_f64(const BatchParams& P, int cluster, int ctas, int part, cudaStream_t st);
 cudaError_t launch_batch_bf16(const BatchParams& P, int cluster, int ctas, int part, cudaStream_t st);
+cudaError_t launch_rows_f32(const BatchParams& P, cudaStream_t st);
+cudaError_t launch_rows_f64(const BatchParams& P, cudaStream_t st);
+cudaError_t launch_rows_bf16(const BatchParams& P, cudaStream_t st);
 int max_clusters_f32(int cluster);
 int max_clusters_f64(int cluster);
 int max_clusters_bf16(int cluster);

@@ -8,6 +8,8 @@ cudaError_t launch_batch_f32(const BatchParams& P, int cluster, int ctas, int pa
 	return launch_prec<float, float>(P, cluster, ctas, 0, part, st);
 }
 
+cudaError_t launch_rows_f32(const BatchParams& P, cudaStream_t st) { return launch_rows<float, float>(P, st); }
+
 int max_clusters_f32(int cluster) { return max_clusters_prec<float, float>(cluster); }
 
 } // namespace b3g

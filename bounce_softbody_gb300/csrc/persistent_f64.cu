@@ -8,6 +8,8 @@ cudaError_t launch_batch_f64(const BatchParams& P, int cluster, int ctas, int pa
 	return launch_prec<double, double>(P, cluster, ctas, 0, part, st);
 }
 
+cudaError_t launch_rows_f64(const BatchParams& P, cudaStream_t st) { return launch_rows<double, double>(P, st); }
+
 int max_clusters_f64(int cluster) { return max_clusters_prec<double, double>(cluster); }
 
 } // namespace b3g

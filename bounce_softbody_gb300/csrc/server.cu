@@ -293,8 +293,8 @@ struct b3g_server
 	unsigned* d_queue = nullptr;
 	DevBody* h_table = nullptr;  // pinned
 	int* h_order = nullptr;      // pinned
-	unsigned* d_tet_off = nullptr;  // first tetrahedron of each table entry (flat numbering), + total
-	unsigned* h_tet_off = nullptr;  // pinned
+	unsigned* d_flat_off = nullptr;  // flat numbering: element offsets, then slice offsets
+	unsigned* h_flat_off = nullptr;  // pinned
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 	// statistics
 	std::vector<float> step_ms;
@@ -476,14 +476,19 @@ int prepare(b3g_server* s, const std::vector<uint32_t>& act, int* nbig)
 		s->h_table[k] = dev_for(B.body, prec, s->cfg.preconditioner);
 		s->h_order[k] = (int)k;
 	}
-	// the flat numbering of the active bodies' tetrahedra for the tetrahedron launch
-	uint64_t nt = 0;
-	for (size_t k = 0; k < act.size(); ++k)
+	// the flat numbering of the active bodies' elements and row slices for the flat launches
+	const size_t na = act.size();
+	uint64_t ne = 0, nsl = 0;
+	for (size_t k = 0; k < na; ++k)
 	{
-		s->h_tet_off[k] = (unsigned)nt;
-		nt += s->h_table[k].nt;
+		const DevBody& D = s->h_table[k];
+		s->h_flat_off[k] = (unsigned)ne;
+		s->h_flat_off[na + 1 + k] = (unsigned)nsl;
+		ne += (uint64_t)D.nt + D.ntr + D.ns + D.nbw + D.nms;
+		nsl += (uint64_t)D.nslices;
 	}
-	s->h_tet_off[act.size()] = nt < (1ull << 32) ? (unsigned)nt : 0u;
+	s->h_flat_off[na] = (unsigned)ne;
+	s->h_flat_off[2 * na + 1] = (unsigned)nsl;
 	std::stable_sort(s->h_order, s->h_order + act.size(),
 	                 [&](int a, int b) { return s->bodies[act[a]].h.n > s->bodies[act[b]].h.n; });
 	// One schedule for every launch: bodies of kServerThreshold vertices or more are stepped by
@@ -503,7 +508,8 @@ int step_active(b3g_server* s, int count, int nbig)
 	cudaError_t e = cudaMemcpyAsync(s->d_table, s->h_table, count * sizeof(DevBody), cudaMemcpyHostToDevice, st);
 	if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_order, s->h_order, count * sizeof(int), cudaMemcpyHostToDevice, st);
 	if (e == cudaSuccess)
-		e = cudaMemcpyAsync(s->d_tet_off, s->h_tet_off, (count + 1) * sizeof(unsigned), cudaMemcpyHostToDevice, st);
+		e = cudaMemcpyAsync(s->d_flat_off, s->h_flat_off, 2 * (count + 1) * sizeof(unsigned), cudaMemcpyHostToDevice,
+		                    st);
 	if (e != cudaSuccess) return cuda_fail(e, "server upload");
 	int m = batch_max_clusters(prec, s->cluster);
 	if (m <= 0) m = std::max(1, s->ctx->sm_count / s->cluster);
@@ -525,8 +531,10 @@ int step_active(b3g_server* s, int count, int nbig)
 	A.cluster = s->cluster;
 	A.ctas = m * s->cluster;
 	A.prof = nullptr;
-	A.tet_off = s->d_tet_off;
-	A.ntets = s->h_tet_off[count];
+	A.elem_off = s->d_flat_off;
+	A.slice_off = s->d_flat_off + count + 1;
+	A.nelem = s->h_flat_off[count];
+	A.nslices = s->h_flat_off[2 * count + 1];
 	A.nbodies = count;
 	cudaEventRecord(s->ev0, st);
 	e = op_batch(A, st);
@@ -638,8 +646,8 @@ int b3g_server_create(b3g_context* ctx, uint64_t memory_budget_bytes, uint32_t m
 	while (s->cluster > 1 && batch_max_clusters(prec_of(&s->cfg), s->cluster) <= 0) s->cluster /= 2;
 	cudaError_t e = cudaMalloc(&s->d_table, max_active * sizeof(DevBody));
 	if (e == cudaSuccess) e = cudaMalloc(&s->d_order, max_active * sizeof(int));
-	if (e == cudaSuccess) e = cudaMalloc(&s->d_tet_off, (max_active + 1) * sizeof(unsigned));
-	if (e == cudaSuccess) e = cudaMallocHost(&s->h_tet_off, (max_active + 1) * sizeof(unsigned));
+	if (e == cudaSuccess) e = cudaMalloc(&s->d_flat_off, 2 * (max_active + 1) * sizeof(unsigned));
+	if (e == cudaSuccess) e = cudaMallocHost(&s->h_flat_off, 2 * (max_active + 1) * sizeof(unsigned));
 	if (e == cudaSuccess) e = cudaMalloc(&s->d_queue, 4 * sizeof(unsigned));
 	if (e == cudaSuccess) e = cudaMallocHost(&s->h_table, max_active * sizeof(DevBody));
 	if (e == cudaSuccess) e = cudaMallocHost(&s->h_order, max_active * sizeof(int));
@@ -649,11 +657,11 @@ int b3g_server_create(b3g_context* ctx, uint64_t memory_budget_bytes, uint32_t m
 	{
 		cudaFree(s->d_table);
 		cudaFree(s->d_order);
-		cudaFree(s->d_tet_off);
+		cudaFree(s->d_flat_off);
 		cudaFree(s->d_queue);
 		cudaFreeHost(s->h_table);
 		cudaFreeHost(s->h_order);
-		cudaFreeHost(s->h_tet_off);
+		cudaFreeHost(s->h_flat_off);
 		delete s;
 		return cuda_fail(e, "server setup");
 	}
@@ -813,11 +821,11 @@ int b3g_server_destroy(b3g_server* s)
 	cudaEventDestroy(s->ev1);
 	cudaFree(s->d_table);
 	cudaFree(s->d_order);
-	cudaFree(s->d_tet_off);
+	cudaFree(s->d_flat_off);
 	cudaFree(s->d_queue);
 	cudaFreeHost(s->h_table);
 	cudaFreeHost(s->h_order);
-	cudaFreeHost(s->h_tet_off);
+	cudaFreeHost(s->h_flat_off);
 	delete s;
 	return B3G_OK;
 }
