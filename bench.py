@@ -424,12 +424,13 @@ def ours(args, world, rank, local, pg):
             launches += args.steps * (2 * launched + resid)
         roof["kernel"] = "per-op step: k_dir_spmv_dot (70 % of the kernel time) + k_update + refresh"
     else:
-        # single Newton iteration: the flat tetrahedron launch, the assembly launch and the PCG
+        # single Newton iteration: the flat element launch, the flat row launch and the PCG
         # launch; several: one whole-step launch
         if scfg.force_iterations > 1:
             launches = args.steps
         else:
-            launches = (3 if any(i["tets"] for i in infos) else 2) * args.steps
+            has_elements = any(i["tets"] or i["tris"] or i["springs"] for i in infos)
+            launches = (3 if has_elements else 2) * args.steps
     line = {"metric": METRIC, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "fp64": "f64", "bf16": "bf16+f32"}[args.precision],
