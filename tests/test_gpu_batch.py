@@ -170,3 +170,26 @@ def test_batch_host_transfers_match_per_body_calls(ctx):
         assert np.array_equal(xs[:3 * m], xr.ravel()) and np.array_equal(vs[:3 * m], vr.ravel())
         for b in b1 + b2:
             b.close()
+
+
+def test_mixed_batch_matches_oracle(ctx):
+    """One batch of every element kind (tetrahedra; membrane triangles and springs with sphere
+    contact; Baraff-Witkin stretch and shear with a mouse spring): the flat element launch
+    dispatches each body's elements by kind over one numbering, the flat row launch serves slices
+    of all of them; each body against the FP64 oracle within 20x the oracle's own FP32 spread."""
+    descs = [meshes.batch_bodies(count=1, lo=6, hi=9, seed=21)[0],
+             meshes.cloth_grid(12, side=1.2, height=0.56, sphere_radius=0.5, contact_radius=0.05),
+             meshes.bw_cloth(8, pinned="edges", stretch_ks=5e4, shear_ks=1e3, shear_kd=10.0, mouse=True),
+             meshes.batch_bodies(count=1, lo=10, hi=14, seed=22)[0]]
+    steps = 4
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    bodies = [b3g.Body(ctx, d) for d in descs]
+    b3g.step_batch(ctx, bodies, DT, steps, cfg, stats=False)
+    for g, d in zip(bodies, descs):
+        x, v = g.state()
+        x64, v64, _, _ = oracle.simulate(d, steps, kind="port", bits=64)
+        x32, v32, _, _ = oracle.simulate(d, steps, kind="port", bits=32)
+        assert disp_rel(x, x64, d.x) < max(1e-4, 20 * disp_rel(x32, x64, d.x)), d.name
+        fv = float(np.linalg.norm(v32 - v64) / max(np.linalg.norm(v64), 1e-30))
+        assert np.linalg.norm(v - v64) <= max(1e-3, 20 * fv) * np.linalg.norm(v64), d.name
+        g.close()
