@@ -706,6 +706,8 @@ static void release_body_memory(b3g_body* b)
 		if (b->prec[k].mem) cudaFree(b->prec[k].mem);
 	if (b->arena) cudaFree(b->arena);
 	if (b->ray_buf) cudaFree(b->ray_buf);
+	for (auto& g : b->chunk_graphs) cudaGraphExecDestroy(g.exec);
+	b->chunk_graphs.clear();
 	for (int k = 0; k < 3; ++k) b->prec[k] = PrecBuffers();
 	b->arena = nullptr;
 	b->ray_buf = nullptr;
@@ -754,6 +756,32 @@ int b3g_body_device_bytes(const b3g_body* b, uint64_t* bytes)
 	return B3G_OK;
 }
 
+// kPcgChunk iterations of the per-op PCG from iteration j0 (a multiple of kPcgChunk, so even):
+// one replay of the chunk's CUDA graph, captured on first use. The kernels decide on the device
+// whether the solve already finished; the host only checks between chunks. A chunk's launches
+// depend on j0 only through which iterations refresh, so a handful of graphs serve every chunk.
+static cudaError_t pcg_chunk(b3g_body* b, const DevBody& D, int prec, int precond, int j0, int refresh,
+                             cudaStream_t st)
+{
+	const unsigned mask = pcg_resid_mask(prec, j0, kPcgChunk, refresh);
+	for (const auto& g : b->chunk_graphs)
+		if (g.prec == prec && g.precond == precond && g.refresh == refresh && g.resid_mask == mask)
+			return cudaGraphLaunch(g.exec, st);
+	op_pcg_prime(D, prec);
+	cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+	if (e != cudaSuccess) return e;
+	for (int k = 0; k < kPcgChunk && e == cudaSuccess; ++k) e = op_pcg_iteration(D, prec, j0 + k, refresh, st);
+	cudaGraph_t graph = nullptr;
+	const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+	if (e == cudaSuccess) e = ec;
+	cudaGraphExec_t exec = nullptr;
+	if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+	if (graph) cudaGraphDestroy(graph);
+	if (e != cudaSuccess) return e;
+	b->chunk_graphs.push_back({prec, precond, refresh, mask, exec});
+	return cudaGraphLaunch(exec, st);
+}
+
 int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_step_stats* stats)
 {
 	if (!b) return fail(B3G_ERROR_INVALID_ARGUMENT, "null body");
@@ -785,7 +813,7 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 	const int newton = (int)std::max<uint32_t>(1u, cfg.force_iterations);
 	e = op_begin(D, st, (int)cfg.max_pcg_iterations, cfg.pcg_tolerance * cfg.pcg_tolerance, (int)cfg.refresh_period,
 	             cfg.newton_tolerance * cfg.newton_tolerance);
-	const int chunk = 8;
+	const int chunk = kPcgChunk;
 	Scalars* hs = b->ctx->h_scalars;
 	for (int k = 0; k < newton && e == cudaSuccess; ++k)
 	{
@@ -796,8 +824,11 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 		if (e == cudaSuccess && k > 0) e = op_pcg_init(D, prec, st);
 		for (int it = 0; it < (int)cfg.max_pcg_iterations && e == cudaSuccess; it += chunk)
 		{
-			for (int j = 0; j < chunk && it + j < (int)cfg.max_pcg_iterations && e == cudaSuccess; ++j)
-				e = op_pcg_iteration(D, prec, it + j, (int)cfg.refresh_period, st);
+			if (it + chunk <= (int)cfg.max_pcg_iterations)
+				e = pcg_chunk(b, D, prec, (int)cfg.preconditioner, it, (int)cfg.refresh_period, st);
+			else
+				for (int j = 0; it + j < (int)cfg.max_pcg_iterations && e == cudaSuccess; ++j)
+					e = op_pcg_iteration(D, prec, it + j, (int)cfg.refresh_period, st);
 			if (e != cudaSuccess) break;
 			e = cudaMemcpyAsync(&hs->done, &D.sc->done, sizeof(int), cudaMemcpyDeviceToHost, st);
 			if (e == cudaSuccess) e = cudaStreamSynchronize(st);

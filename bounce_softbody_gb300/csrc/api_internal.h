@@ -73,6 +73,15 @@ struct b3g_body
 	// ray cast scratch (segments, reduction keys, hits), grown on demand
 	char* ray_buf = nullptr;
 	uint32_t ray_cap = 0;
+	// the per-op PCG's chunks of kPcgChunk iterations, captured into CUDA graphs once per kind:
+	// precision, preconditioner, refresh period and which iterations of the chunk refresh
+	struct ChunkGraph
+	{
+		int prec, precond, refresh;
+		unsigned resid_mask;
+		cudaGraphExec_t exec;
+	};
+	std::vector<ChunkGraph> chunk_graphs;
 };
 
 namespace b3g {

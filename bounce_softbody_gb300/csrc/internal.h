@@ -37,6 +37,7 @@
 namespace b3g {
 
 constexpr int kSlice = 32;
+constexpr int kPcgChunk = 8;     // per-op PCG iterations between host checks of convergence
 constexpr int kGroup = 4;
 
 B3G_HD size_t block_slot(size_t base, int k, int lane) { return base + 128 * (size_t)(k >> 2) + 4 * lane + (k & 3); }

@@ -678,6 +678,23 @@ cudaError_t op_pcg_init(const DevBody& B, int prec, cudaStream_t st)
 	return cudaGetLastError();
 }
 
+unsigned pcg_resid_mask(int prec, int j0, int count, int refresh)
+{
+	unsigned m = 0;
+	for (int k = 0; k < count && k < 32; ++k)
+		if (prec == kPBF || (refresh > 0 && (j0 + k) % refresh == 0)) m |= 1u << k;
+	return m;
+}
+
+void op_pcg_prime(const DevBody& B, int prec)
+{
+	(void)slice_grid(B);
+	(void)vertex_grid(B);
+	if (prec == kP64) (void)spmv_grid<double, double>(B);
+	else if (prec == kPBF) (void)spmv_grid<__nv_bfloat16, float>(B);
+	else (void)spmv_grid<float, float>(B);
+}
+
 cudaError_t op_pcg_iteration(const DevBody& D, int prec, int j, int refresh, cudaStream_t st)
 {
 	// direction buffers alternate: iteration j reads the direction from one and writes the new

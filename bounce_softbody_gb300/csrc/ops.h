@@ -29,6 +29,11 @@ cudaError_t op_assemble(const DevBody& B, const StepParamsHost& P, int prec, boo
 cudaError_t op_pcg_init(const DevBody& B, int prec, cudaStream_t st);
 // iteration j (0-based) of the current solve; refresh = the true-residual refresh period
 cudaError_t op_pcg_iteration(const DevBody& B, int prec, int j, int refresh, cudaStream_t st);
+// Iterations of j that launch the true-residual refresh kernel (bit k: iteration j0 + k) for a
+// chunk of `count` iterations from j0; and the launch geometry of the iteration kernels computed
+// once outside any stream capture.
+unsigned pcg_resid_mask(int prec, int j0, int count, int refresh);
+void op_pcg_prime(const DevBody& B, int prec);
 // mode 0: write the Newton iterate (xi, vi); mode 1: write the state and finish the step
 cudaError_t op_final(const DevBody& B, const StepParamsHost& P, int prec, int mode, cudaStream_t st);
 // finish a multi-Newton step: iterate -> state, friction, clear, new contacts
