@@ -187,8 +187,8 @@ __device__ __forceinline__ bool ray_triangle(float3 p1, float3 d, float3 A, floa
 
 __device__ __forceinline__ unsigned long long ray_key(float t, unsigned tri)
 {
-	// t >= 0: its bit pattern orders like its value (-0 cannot pass the t < 0 test as a hit key
-	// below 0, and is mapped to +0)
+	// a hit has 0 <= t <= 1, and non-negative floats order like their bit patterns; fmaxf maps
+	// -0 (which passes the t < 0 test) to +0
 	return ((unsigned long long)__float_as_uint(fmaxf(t, 0.0f)) << 32) | tri;
 }
 
