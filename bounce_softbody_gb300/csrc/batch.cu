@@ -512,6 +512,24 @@ static int prepare_xfer(b3g_context* ctx, b3g_body* const* bodies, uint32_t coun
 	return B3G_OK;
 }
 
+// The device address of `floats` floats of page-locked host memory at p (cudaHostAlloc /
+// cudaHostRegister, which the GPU reads and writes directly over the CPU-GPU link), or null when
+// p is not such memory or the range is not one mapping.
+static float* mapped_host(const float* p, uint64_t floats)
+{
+	if (!p || floats == 0) return nullptr;
+	cudaPointerAttributes a0, a1;
+	if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, p + floats - 1) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return nullptr;
+	}
+	if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+		return nullptr;
+	float* d = (float*)a0.devicePointer;
+	return (float*)a1.devicePointer == d + (floats - 1) ? d : nullptr;
+}
+
 extern "C" int b3g_batch_apply_forces(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, const float* forces)
 {
 	if (!ctx || (!bodies && count) || (!forces && count)) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
@@ -520,9 +538,16 @@ extern "C" int b3g_batch_apply_forces(b3g_context* ctx, b3g_body* const* bodies,
 	int rc = prepare_xfer(ctx, bodies, count, 2);
 	if (rc != B3G_OK) return rc;
 	cudaStream_t st = ctx->stream;
-	// one copy of the whole array, then one launch adds every body's slice to its fext
-	cudaError_t e = cudaMemcpyAsync(ctx->xfer, forces, ctx->xfer_total * sizeof(float), cudaMemcpyHostToDevice, st);
-	if (e == cudaSuccess) e = op_batch_scatter_add(ctx->xfer_table, count, ctx->xfer_max_n3, ctx->xfer, st);
+	// page-locked host memory: one launch reads it directly and adds every body's slice to its
+	// fext; otherwise one copy of the whole array into the staging buffer first
+	cudaError_t e = cudaSuccess;
+	const float* src = mapped_host(forces, ctx->xfer_total);
+	if (!src)
+	{
+		e = cudaMemcpyAsync(ctx->xfer, forces, ctx->xfer_total * sizeof(float), cudaMemcpyHostToDevice, st);
+		src = ctx->xfer;
+	}
+	if (e == cudaSuccess) e = op_batch_scatter_add(ctx->xfer_table, count, ctx->xfer_max_n3, src, st);
 	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch_apply_forces");
 }
 
@@ -535,14 +560,17 @@ extern "C" int b3g_batch_get_state(b3g_context* ctx, b3g_body* const* bodies, ui
 	int rc = prepare_xfer(ctx, bodies, count, 2);
 	if (rc != B3G_OK) return rc;
 	cudaStream_t st = ctx->stream;
-	// one launch packs every body's x and v into the staging buffer, then one copy each
-	float* sx = ctx->xfer;
-	float* sv = ctx->xfer + ctx->xfer_total;
+	// one launch packs every body's x and v, straight into page-locked host arrays or into the
+	// staging buffer followed by one copy each
+	float* mx = mapped_host(positions, ctx->xfer_total);
+	float* mv = mapped_host(velocities, ctx->xfer_total);
+	float* sx = mx ? mx : ctx->xfer;
+	float* sv = mv ? mv : ctx->xfer + ctx->xfer_total;
 	const size_t bytes = ctx->xfer_total * sizeof(float);
 	cudaError_t e = op_batch_gather(ctx->xfer_table, count, ctx->xfer_max_n3, positions ? sx : nullptr,
 	                                velocities ? sv : nullptr, st);
-	if (e == cudaSuccess && positions) e = cudaMemcpyAsync(positions, sx, bytes, cudaMemcpyDeviceToHost, st);
-	if (e == cudaSuccess && velocities) e = cudaMemcpyAsync(velocities, sv, bytes, cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess && positions && !mx) e = cudaMemcpyAsync(positions, sx, bytes, cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess && velocities && !mv) e = cudaMemcpyAsync(velocities, sv, bytes, cudaMemcpyDeviceToHost, st);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
 	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch_get_state");
 }

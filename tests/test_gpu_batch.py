@@ -120,12 +120,24 @@ def test_launch_timing_mode_same_results(ctx):
         b.close()
 
 
-def test_batch_host_transfers_match_per_body_calls(ctx):
-    """b3g_batch_apply_forces / b3g_batch_get_state (one copy and one launch each way over a
-    cached body table) against the per-body calls: bitwise the same state, also after the body
-    list changes and after a listed body is destroyed."""
+@pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "page_locked"])
+def test_batch_host_transfers_match_per_body_calls(ctx, pinned):
+    """b3g_batch_apply_forces / b3g_batch_get_state (one launch each way over a cached body
+    table; page-locked host arrays are read and written by the launch directly, others go through
+    one staging copy) against the per-body calls: bitwise the same state, also after the body list
+    changes and after a listed body is destroyed."""
     descs = meshes.batch_bodies(count=7, lo=3, hi=9, seed=13)
     cfg = b3g.solver_config()
+    if pinned:
+        torch = pytest.importorskip("torch")
+
+        def host(a):
+            t = torch.from_numpy(np.ascontiguousarray(a, np.float32)).pin_memory()
+            return t, t.numpy()
+    else:
+        def host(a):
+            a = np.ascontiguousarray(a, np.float32)
+            return a, a
 
     def run(batched, order, forces):
         bodies = [b3g.Body(ctx, d) for d in descs]
@@ -133,15 +145,17 @@ def test_batch_host_transfers_match_per_body_calls(ctx):
         n = [b.n for b in sel]
         for f in forces:
             if batched:
-                b3g.batch_apply_forces(ctx, sel, f.ctypes.data)
+                keep, fa = host(f)
+                b3g.batch_apply_forces(ctx, sel, fa.ctypes.data)
+                ctx.synchronize()
             else:
                 off = 0
                 for b, m in zip(sel, n):
                     b.apply_forces(f[off:off + 3 * m].reshape(m, 3))
                     off += 3 * m
             b3g.step_batch(ctx, bodies, DT, 1, cfg, stats=False)
-        x = np.zeros(3 * sum(n), np.float32)
-        v = np.zeros(3 * sum(n), np.float32)
+        kx, x = host(np.zeros(3 * sum(n), np.float32))
+        kv, v = host(np.zeros(3 * sum(n), np.float32))
         if batched:
             b3g.batch_get_state(ctx, sel, x.ctypes.data, v.ctypes.data)
         else:
@@ -150,7 +164,7 @@ def test_batch_host_transfers_match_per_body_calls(ctx):
                 xb, vb = b.state()
                 x[off:off + 3 * m], v[off:off + 3 * m] = xb.ravel(), vb.ravel()
                 off += 3 * m
-        return bodies, x, v
+        return bodies, np.array(x), np.array(v)
 
     for order in ([0, 1, 2, 3, 4, 5, 6], [5, 2, 6]):
         total = sum(descs[k].n for k in order)
@@ -162,8 +176,8 @@ def test_batch_host_transfers_match_per_body_calls(ctx):
         # a listed body goes away: the next batched call rebuilds its table
         b1[order[0]].close()
         rest = [b1[k] for k in order[1:]]
-        xs = np.zeros(3 * sum(b.n for b in rest), np.float32)
-        vs = np.zeros_like(xs)
+        kxs, xs = host(np.zeros(3 * sum(b.n for b in rest), np.float32))
+        kvs, vs = host(np.zeros(3 * sum(b.n for b in rest), np.float32))
         b3g.batch_get_state(ctx, rest, xs.ctypes.data, vs.ctypes.data)
         m = rest[0].n
         xr, vr = rest[0].state()
