@@ -713,15 +713,23 @@ __device__ __forceinline__ int flat_body(const unsigned* __restrict__ off, int n
 // bodies' sizes (the team launch's tail was set by its largest bodies). Element records come from
 // the flat element launch before it, state from earlier launches: plain loads. The PCG launch
 // sums delta0 = r.s per body itself.
+#ifndef B3G_ROWS_THREADS
+#define B3G_ROWS_THREADS 256     // threads per CTA of the flat row launch
+#endif
+#ifndef B3G_ROWS_MIN_BLOCKS
+#define B3G_ROWS_MIN_BLOCKS 2    // resident CTAs per SM its register budget is sized for
+#endif
+constexpr int kRowsWarps = B3G_ROWS_THREADS / 32;
+
 template <class TA, class TV>
-__global__ void __launch_bounds__(kPThreads, B3G_BATCH_MIN_BLOCKS) k_batch_rows(BatchParams P)
+__global__ void __launch_bounds__(B3G_ROWS_THREADS, B3G_ROWS_MIN_BLOCKS) k_batch_rows(BatchParams P)
 {
 	const int lane = threadIdx.x & 31;
 	StepParams sp;
 	sp.h = P.h;
 	sp.first_newton = 1;
-	const unsigned nw = gridDim.x * kPWarps;
-	for (unsigned g = blockIdx.x * kPWarps + (threadIdx.x >> 5); g < P.nslices; g += nw)
+	const unsigned nw = gridDim.x * kRowsWarps;
+	for (unsigned g = blockIdx.x * kRowsWarps + (threadIdx.x >> 5); g < P.nslices; g += nw)
 	{
 		const int b = flat_body(P.slice_off, P.nbodies, g);
 		assemble_row<TA, TV, LdPlain>(P.bodies[b], (int)(g - __ldg(P.slice_off + b)), lane, sp, true);
@@ -735,12 +743,12 @@ cudaError_t launch_rows(const BatchParams& P, cudaStream_t st)
 		int dev = 0, sms = 0, per_sm = 0;
 		cudaGetDevice(&dev);
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_rows<TA, TV>, kPThreads, 0);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_rows<TA, TV>, B3G_ROWS_THREADS, 0);
 		return std::max(1, sms * std::max(per_sm, 1));
 	}();
-	const unsigned need = (P.nslices + kPWarps - 1) / kPWarps;
+	const unsigned need = (P.nslices + kRowsWarps - 1) / kRowsWarps;
 	const int grid = (int)std::max(1u, std::min(need, (unsigned)resident));
-	k_batch_rows<TA, TV><<<grid, kPThreads, 0, st>>>(P);
+	k_batch_rows<TA, TV><<<grid, B3G_ROWS_THREADS, 0, st>>>(P);
 	return cudaGetLastError();
 }
 
