@@ -768,8 +768,19 @@ static cudaError_t pcg_chunk(b3g_body* b, const DevBody& D, int prec, int precon
 		if (g.prec == prec && g.precond == precond && g.refresh == refresh && g.resid_mask == mask)
 			return cudaGraphLaunch(g.exec, st);
 	op_pcg_prime(D, prec);
-	cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-	if (e != cudaSuccess) return e;
+	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+	cudaError_t e = cudaStreamIsCapturing(st, &cs);
+	if (e == cudaSuccess && cs == cudaStreamCaptureStatusNone) e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+	else e = cudaErrorStreamCaptureUnsupported;
+	if (e != cudaSuccess)
+	{
+		// no graph (the stream is captured by someone else, or capture is unavailable): launch
+		// the chunk's kernels one by one
+		cudaGetLastError();
+		e = cudaSuccess;
+		for (int k = 0; k < kPcgChunk && e == cudaSuccess; ++k) e = op_pcg_iteration(D, prec, j0 + k, refresh, st);
+		return e;
+	}
 	for (int k = 0; k < kPcgChunk && e == cudaSuccess; ++k) e = op_pcg_iteration(D, prec, j0 + k, refresh, st);
 	cudaGraph_t graph = nullptr;
 	const cudaError_t ec = cudaStreamEndCapture(st, &graph);
