@@ -833,6 +833,11 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 		if (e == cudaSuccess) e = op_elements(D, P, st);
 		if (e == cudaSuccess) e = op_assemble(D, P, prec, k == 0, st);
 		if (e == cudaSuccess && k > 0) e = op_pcg_init(D, prec, st);
+		// the host first asks whether the solve ended one chunk before the previous step's solve
+		// did: the chunks before that queue back to back (a chunk launched after the end returns
+		// at once from every kernel)
+		const int quiet = std::max(0, b->pcg_chunks_hint - 1);
+		int chunks = 0;
 		for (int it = 0; it < (int)cfg.max_pcg_iterations && e == cudaSuccess; it += chunk)
 		{
 			if (it + chunk <= (int)cfg.max_pcg_iterations)
@@ -841,10 +846,12 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 				for (int j = 0; it + j < (int)cfg.max_pcg_iterations && e == cudaSuccess; ++j)
 					e = op_pcg_iteration(D, prec, it + j, (int)cfg.refresh_period, st);
 			if (e != cudaSuccess) break;
+			if (++chunks <= quiet) continue;
 			e = cudaMemcpyAsync(&hs->done, &D.sc->done, sizeof(int), cudaMemcpyDeviceToHost, st);
 			if (e == cudaSuccess) e = cudaStreamSynchronize(st);
 			if (e == cudaSuccess && hs->done) break;
 		}
+		if (k == 0) b->pcg_chunks_hint = chunks;
 		if (e != cudaSuccess) break;
 		const bool single = newton == 1;
 		e = op_final(D, P, prec, single ? 1 : 0, st);

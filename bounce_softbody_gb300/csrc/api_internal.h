@@ -82,6 +82,7 @@ struct b3g_body
 		cudaGraphExec_t exec;
 	};
 	std::vector<ChunkGraph> chunk_graphs;
+	int pcg_chunks_hint = 0;  // chunks the previous step's first solve launched
 };
 
 namespace b3g {
