@@ -60,7 +60,10 @@ namespace {
 #define B3G_BATCH_MIN_BLOCKS 2   // resident CTAs per SM the register budget is sized for
 #endif
 
-constexpr int kPThreads = 256;
+#ifndef B3G_PCG_THREADS
+#define B3G_PCG_THREADS 256      // threads per CTA of the team launches
+#endif
+constexpr int kPThreads = B3G_PCG_THREADS;
 constexpr int kPWarps = kPThreads / 32;
 
 struct TeamShared
