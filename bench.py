@@ -154,7 +154,8 @@ def spmv_bytes(info, vs=4, bs=36):
 
 
 def iteration_bytes(info, vs=4, bs=36):
-    """One PCG iteration: SpMV + (x, r, d, q, Minv read; x, r, s written) + (s, d read; d written)."""
+    """One PCG iteration: SpMV of s + (d, q read; d written: the direction d = s + beta d and
+    q = A s + beta q in the SpMV sweep) + update (x, r, d, q, Minv read; x, r, s written)."""
     n = info["vertices"]
     return spmv_bytes(info, vs, bs) + 8 * 3 * vs * n + 3 * 3 * vs * n
 

@@ -117,7 +117,8 @@ struct Team
 
 
 // Phases timed by the optional instrumentation (cycles of thread 0 of each CTA, barriers and
-// reductions included in the phase that ends with them).
+// reductions included in the phase that ends with them). The direction update runs inside the
+// SpMV sweep, so kPhDir stays zero; its slot keeps the numbering the host reads.
 enum { kPhElem = 0, kPhAsm = 1, kPhSpmv = 2, kPhUpdate = 3, kPhDir = 4, kPhFinal = 5, kPhIdle = 6, kPhases = 8 };
 
 struct PhaseClock
@@ -182,29 +183,6 @@ __device__ __forceinline__ double update_two(const DevBody& B, TV* __restrict__ 
 	return part;
 }
 
-// d = s + beta d for two rows, loads first
-template <class TV, class LD>
-__device__ __forceinline__ void direction_two(TV* __restrict__ d, const TV* __restrict__ s, int i0, int i1, bool ok1,
-                                              TV beta)
-{
-	TV s0[3], d0[3], s1[3], d1[3];
-	vld<TV, LD>(s, i0, s0);
-	vld<TV, LD>(d, i0, d0);
-	if (ok1)
-	{
-		vld<TV, LD>(s, i1, s1);
-		vld<TV, LD>(d, i1, d1);
-	}
-#pragma unroll
-	for (int c = 0; c < 3; ++c)
-	{
-		d0[c] = s0[c] + beta * d0[c];
-		d1[c] = s1[c] + beta * d1[c];
-	}
-	vst(d, i0, d0);
-	if (ok1) vst(d, i1, d1);
-}
-
 // r = pb - A x, s = M^-1 r for the rows of one warp's slices (init / refresh); optionally d = s
 template <class TA, class TV, class LD>
 __device__ __forceinline__ double residual_rows(const DevBody& B, const TA* A, const TV* x, int s0, int stride,
@@ -231,9 +209,13 @@ __device__ __forceinline__ double residual_rows(const DevBody& B, const TA* A, c
 	return part;
 }
 
-// q = A d and this warp's part of d.q
+// The direction and A times it by linearity, for the rows of one warp's slices: d = s + beta d
+// and q = A s + beta q (d = s, q = A s on a solve's first iteration), and this warp's part of
+// d.q. The SpMV gathers only s, which the update sweep finished before its reduction (a team
+// barrier), so no direction sweep and no barrier of its own precede it. d and q stay row-local.
 template <class TA, class TV, class LD>
-__device__ __forceinline__ double spmv_dot_rows(const DevBody& B, const TA* A, const TV* d, TV* q, int s0, int stride)
+__device__ __forceinline__ double spmv_lin_rows(const DevBody& B, const TA* A, const TV* s, TV* d, TV* q, TV beta,
+                                                bool first, int s0, int stride)
 {
 	const int lane = threadIdx.x & 31;
 	double part = 0.0;
@@ -243,9 +225,22 @@ __device__ __forceinline__ double spmv_dot_rows(const DevBody& B, const TA* A, c
 		if (i >= B.n) continue;
 		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 		TV o[3], dd[3];
-		spmv_row<TA, TV, LD, MatVia<LD>>(A, B.col, B.nslots, base, w, lane, d, o);
+		spmv_row<TA, TV, LD, MatVia<LD>>(A, B.col, B.nslots, base, w, lane, s, o);
+		vld<TV, LD>(s, i, dd);
+		if (!first)
+		{
+			TV dp[3], qp[3];
+			vld<TV, LD>(d, i, dp);
+			vld<TV, LD>(q, i, qp);
+#pragma unroll
+			for (int c = 0; c < 3; ++c)
+			{
+				dd[c] = dd[c] + beta * dp[c];
+				o[c] = o[c] + beta * qp[c];
+			}
+		}
 		vst(q, i, o);
-		vld<TV, LD>(d, i, dd);
+		vst(d, i, dd);
 		part += dot3<TV>(dd, o);
 	}
 	return part;
@@ -296,10 +291,11 @@ __device__ SolveOut team_pcg(Team<CL>& T, const DevBody& B, const BatchParams& P
 	else
 		done = false;
 	int iter = 0;
+	TV bt = (TV)0;
 	while (!done)
 	{
-		// q = A d, alpha = delta / d.q
-		double part = spmv_dot_rows<TA, TV, LD>(B, Asp, d, q, T.warp(), T.nwarps());
+		// d = s + beta d, q = A d (as A s + beta q), alpha = delta / d.q
+		double part = spmv_lin_rows<TA, TV, LD>(B, Asp, s, d, q, bt, iter == 0, T.warp(), T.nwarps());
 		const double dq = T.reduce(part);
 		pc.tick(kPhSpmv);
 		if (!isfinite(dq))
@@ -356,18 +352,7 @@ __device__ SolveOut team_pcg(Team<CL>& T, const DevBody& B, const BatchParams& P
 			out.status = B3G_SOLVE_MAX_ITERATIONS;
 			break;
 		}
-		// d = s + beta d as its own sweep: folding it into the SpMV (as the per-op path does)
-		// doubles the SpMV's vector gathers, which for the hundreds of bodies a launch runs at
-		// once come from DRAM rather than L2 (measured 4% slower on the 512-body batch)
-		const TV bt = (TV)beta;
-		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
-		{
-			const int i0 = sl * kSlice + lane;
-			if (i0 >= B.n) continue;
-			direction_two<TV, LD>(d, s, i0, i0, false, bt);
-		}
-		T.sync();
-		pc.tick(kPhDir);
+		bt = (TV)beta;
 	}
 	out.iter = iter;
 	out.delta = delta;
