@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libb3g.so")
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 PRECISION_FP32, PRECISION_FP64, PRECISION_BF16 = 0, 1, 2
 PRECOND_JACOBI, PRECOND_BLOCK_JACOBI = 0, 1
+CONTACT_PENALTY, CONTACT_FILTER = 0, 1
 SOLVE_STATUS = {0: "converged", 1: "max_iterations", 2: "nonfinite", 3: "breakdown", 4: "device_timeout"}
 
 _fp = C.POINTER(C.c_float)
@@ -66,7 +67,7 @@ class SolverConfig(C.Structure):
         ("force_iterations", C.c_uint32), ("max_pcg_iterations", C.c_uint32),
         ("pcg_tolerance", C.c_double), ("newton_tolerance", C.c_double),
         ("refresh_period", C.c_uint32), ("precision", C.c_int32), ("preconditioner", C.c_int32),
-        ("reserved", C.c_int32),
+        ("contact_mode", C.c_int32),
     ]
 
 
@@ -184,7 +185,9 @@ def _check(rc: int, what: str):
 
 def solver_config(force_iterations: int = 1, max_pcg_iterations: int = 200, pcg_tolerance: float = 1e-5,
                   refresh_period: int = 50, precision: int = PRECISION_FP32,
-                  preconditioner: int = PRECOND_JACOBI, newton_tolerance: Optional[float] = None) -> SolverConfig:
+                  preconditioner: int = PRECOND_JACOBI, newton_tolerance: Optional[float] = None,
+                  contact_mode: int = 0) -> SolverConfig:
+    """b3g_solver_config; contact_mode CONTACT_PENALTY (the reference's) or CONTACT_FILTER."""
     lib = load_library()
     c = SolverConfig()
     lib.b3g_solver_config_default(C.byref(c))
@@ -194,6 +197,7 @@ def solver_config(force_iterations: int = 1, max_pcg_iterations: int = 200, pcg_
     c.refresh_period = refresh_period
     c.precision = precision
     c.preconditioner = preconditioner
+    c.contact_mode = contact_mode
     if newton_tolerance is not None:
         c.newton_tolerance = newton_tolerance
     return c

@@ -291,8 +291,12 @@ int prec_of(const b3g_solver_config* c)
 	return kP32;
 }
 
-int check_config(const b3g_solver_config* c)
+int check_config(const b3g_solver_config* c, bool per_body)
 {
+	if (c->contact_mode != B3G_CONTACT_PENALTY && c->contact_mode != B3G_CONTACT_FILTER)
+		return fail(B3G_ERROR_INVALID_ARGUMENT, "unknown contact mode %d", c->contact_mode);
+	if (c->contact_mode == B3G_CONTACT_FILTER && !per_body)
+		return fail(B3G_ERROR_UNSUPPORTED, "filtered contacts are stepped by b3g_body_step only");
 	if (c->precision < 0 || c->precision > 2) return fail(B3G_ERROR_INVALID_ARGUMENT, "unknown precision %d", c->precision);
 	if (c->preconditioner < 0 || c->preconditioner > 1)
 		return fail(B3G_ERROR_INVALID_ARGUMENT, "unknown preconditioner %d", c->preconditioner);
@@ -338,7 +342,7 @@ void b3g_solver_config_default(b3g_solver_config* c)
 	c->refresh_period = 50;
 	c->precision = B3G_PRECISION_FP32;
 	c->preconditioner = B3G_PRECOND_JACOBI;
-	c->reserved = 0;
+	c->contact_mode = B3G_CONTACT_PENALTY;
 }
 
 const char* b3g_last_error(void) { return g_error.c_str(); }
@@ -706,12 +710,14 @@ static void release_body_memory(b3g_body* b)
 		if (b->prec[k].mem) cudaFree(b->prec[k].mem);
 	if (b->arena) cudaFree(b->arena);
 	if (b->ray_buf) cudaFree(b->ray_buf);
+	if (b->filt) cudaFree(b->filt);
 	for (auto& g : b->chunk_graphs) cudaGraphExecDestroy(g.exec);
 	b->chunk_graphs.clear();
 	for (int k = 0; k < 3; ++k) b->prec[k] = PrecBuffers();
 	b->arena = nullptr;
 	b->ray_buf = nullptr;
 	b->ray_cap = 0;
+	b->filt = nullptr;
 }
 
 int b3g_body_destroy(b3g_body* b)
@@ -800,7 +806,7 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 	b3g_solver_config cfg;
 	if (cfg_in) cfg = *cfg_in;
 	else b3g_solver_config_default(&cfg);
-	int rc = check_config(&cfg);
+	int rc = check_config(&cfg, true);
 	if (rc != B3G_OK) return rc;
 	cudaSetDevice(b->ctx->device);
 	cudaStream_t st = b->ctx->stream;
@@ -821,6 +827,19 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 	rc = ensure_precision(b, prec);
 	if (rc != B3G_OK) return rc;
 	DevBody D = dev_for(b, prec, cfg.preconditioner, true);
+	if (cfg.contact_mode == B3G_CONTACT_FILTER && b->d.contacts)
+	{
+		if (!b->filt)
+		{
+			e = cudaMalloc(&b->filt, std::max<size_t>(1, (size_t)b->d.n) * sizeof(float4));
+			if (e != cudaSuccess)
+			{
+				b->filt = nullptr;
+				return cuda_fail(e, "filtered contacts");
+			}
+		}
+		D.filt = b->filt;
+	}
 	const int newton = (int)std::max<uint32_t>(1u, cfg.force_iterations);
 	e = op_begin(D, st, (int)cfg.max_pcg_iterations, cfg.pcg_tolerance * cfg.pcg_tolerance, (int)cfg.refresh_period,
 	             cfg.newton_tolerance * cfg.newton_tolerance);
@@ -830,6 +849,7 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 	{
 		StepParamsHost P{dt, k == 0 ? 1 : 0};
 		if (k > 0) e = op_newton_begin(D, st);
+		else if (D.filt && e == cudaSuccess) e = op_contact_filter(D, dt, st);
 		if (e == cudaSuccess) e = op_elements(D, P, st);
 		if (e == cudaSuccess) e = op_assemble(D, P, prec, k == 0, st);
 		if (e == cudaSuccess && k > 0) e = op_pcg_init(D, prec, st);

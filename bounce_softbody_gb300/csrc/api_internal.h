@@ -73,6 +73,8 @@ struct b3g_body
 	// ray cast scratch (segments, reduction keys, hits), grown on demand
 	char* ray_buf = nullptr;
 	uint32_t ray_cap = 0;
+	// per-vertex constraints of filtered contacts, made on the first step in that mode
+	float4* filt = nullptr;
 	// the per-op PCG's chunks of kPcgChunk iterations, captured into CUDA graphs once per kind:
 	// precision, preconditioner, refresh period and which iterations of the chunk refresh
 	struct ChunkGraph
@@ -95,7 +97,8 @@ int ensure_precision(b3g_body* b, int prec);
 // refine: the per-op path's iterative refinement (float-float solution and refresh residual)
 DevBody dev_for(const b3g_body* b, int prec, int precond, bool refine = false);
 int prec_of(const b3g_solver_config* c);
-int check_config(const b3g_solver_config* c);
+// per_body: the caller is b3g_body_step (the only entry point with filtered contacts)
+int check_config(const b3g_solver_config* c, bool per_body = false);
 void stats_from(const Scalars& sc, b3g_step_stats* st);
 int read_scalars(b3g_body* b, Scalars* out);
 

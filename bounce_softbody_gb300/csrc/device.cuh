@@ -1103,12 +1103,55 @@ __device__ __forceinline__ void add_tet_block(float a[9], float4 ua, float4 ub)
 		for (int c = 0; c < 3; ++c) a[3 * r + c] += ratio * A3[r] * B3[c] + B3[r] * A3[c] + (r == c ? uab : 0.0f);
 }
 
+// Filtered contacts (B3G_CONTACT_FILTER) of vertex i at the start of a step: the contact update
+// of contact_manager.cpp:108-146, then the constraint of the first world shape (shape order) the
+// vertex overlaps: n the shape's normal towards the vertex, zn = vt - v.n with vt the Baumgarte
+// velocity min(0.2 C, 0.2) / h of the penalty force's depth C (sphere_shape_contact.cpp:98-126).
+// The assembly then uses S_i = I - n n^T and z_i = zn n in pA = S A S^T + I - S,
+// pb = S (b - A z), and the final update dv = y + z (sparse_force_solver.cpp:170-190, which the
+// reference only ever calls with S = I or 0 and z = 0).
+__device__ __forceinline__ void contact_filter_vertex(const DevBody& B, int i, float h)
+{
+	float4 f = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	const bool dyn = B.type[i] == B3G_DYNAMIC;
+	const float3 x = ld3(B.x, i);
+	const float r1 = B.srad[i];
+	bool found = false;
+	for (int k = 0; k < B.nw; ++k)
+	{
+		const int c = i * B.nw + k;
+		const DevShape& sh = B.shapes[k];
+		if (B.c_exists[c])
+		{
+			if (!dyn || !aabb_overlap(x, r1, sh)) B.c_exists[c] = 0;
+			else
+			{
+				B.c_nf[c] = 0.0f;
+				B.c_apply[c] = 0;
+			}
+		}
+		if (found || !B.c_exists[c]) continue;
+		float3 p2, n2;
+		if (!world_collide(sh, x, r1, p2, n2)) continue;
+		const float3 c1 = x - r1 * n2;
+		const float3 c2 = p2 + sh.radius * n2;
+		const float C = fminf(kBaumgarte * len3(c2 - c1), kMaxContactCorrection);
+		f = make_float4(n2.x, n2.y, n2.z, C / h - dot3(ld3(B.v, i), n2));
+		found = true;
+	}
+	B.filt[i] = f;
+}
+
+__device__ __forceinline__ bool filt_on(float4 f) { return f.x != 0.0f || f.y != 0.0f || f.z != 0.0f; }
+
 // Assembles row i of the pre-filtered system: pA = S A S^T + I - S and pb = S b with
 //   A = M - h dfdv - h^2 dfdx,  b = M (v0 - v) + h (fe + fi) + h dfdx (x0 - x + h v + y)
 // (sparse_force_solver.cpp:165-174), S = I for dynamic vertices and 0 otherwise
 // (force_solver.cpp:110-129). Also forms the Jacobi preconditioner and, when init_pcg is set
-// (initial guess zero), r = pb, s = M^-1 r, d = s; returns this row's r.s.
-template <class TA, class TV, class L = LdPlain>
+// (initial guess zero), r = pb, s = M^-1 r, d = s; returns this row's r.s. FILTER: filtered
+// contacts (B.filt) replace the penalty contacts: S_i = I - n n^T for a constrained vertex and
+// pb = S (b - A z), z nonzero in the first Newton iteration only.
+template <class TA, class TV, class L = LdPlain, bool FILTER = false>
 __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int lane, const StepParams& P,
                                                bool init_pcg)
 {
@@ -1137,7 +1180,7 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		diagExtra += h * damp * m;
 	}
 	float Kc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-	if (B.contacts)
+	if (!FILTER && B.contacts)
 	{
 		const float r1 = B.srad[i];
 		for (int k = 0; k < B.nw; ++k)
@@ -1218,6 +1261,11 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		}
 	}
 
+	float4 fi4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	if (FILTER) fi4 = B.filt[i];
+	const bool ci = FILTER && Si && filt_on(fi4);
+	float3 bz = f3(0.0f, 0.0f, 0.0f);  // (A z)_i
+
 	float diag[9];
 	// Slot pipeline: the next slot's list header and its first four tetrahedron codes load while
 	// this slot's records are gathered, so a slot waits on one gather instead of three dependent
@@ -1296,13 +1344,56 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 			for (int q = 0; q < 9; ++q) a[q] += sgn * L::ld(blk + q);
 		}
 		const bool Sj = B.type[j] == B3G_DYNAMIC;
+		if (FILTER)
+		{
+			if (k == 0)
+			{
+				a[0] += diagExtra;
+				a[4] += diagExtra;
+				a[8] += diagExtra;
+			}
+			const float4 fj = k == 0 ? fi4 : B.filt[j];
+			const bool cj = filt_on(fj);
+			// b - A z on the unfiltered block, then S_i A_ij S_j (+ n n^T = I - S_i on the diagonal)
+			if (cj && P.first_newton) bz = bz + mv9(a, f3(fj.w * fj.x, fj.w * fj.y, fj.w * fj.z));
+			if (Si && Sj)
+			{
+				const float nj[3] = {fj.x, fj.y, fj.z}, ni[3] = {fi4.x, fi4.y, fi4.z};
+				if (cj)
+#pragma unroll
+					for (int r = 0; r < 3; ++r)
+					{
+						const float an = a[3 * r] * nj[0] + a[3 * r + 1] * nj[1] + a[3 * r + 2] * nj[2];
+#pragma unroll
+						for (int c = 0; c < 3; ++c) a[3 * r + c] -= an * nj[c];
+					}
+				if (ci)
+				{
+#pragma unroll
+					for (int c = 0; c < 3; ++c)
+					{
+						const float na = ni[0] * a[c] + ni[1] * a[3 + c] + ni[2] * a[6 + c];
+#pragma unroll
+						for (int r = 0; r < 3; ++r) a[3 * r + c] -= ni[r] * na;
+					}
+					if (k == 0)
+#pragma unroll
+						for (int r = 0; r < 3; ++r)
+#pragma unroll
+							for (int c = 0; c < 3; ++c) a[3 * r + c] += ni[r] * ni[c];
+				}
+			}
+		}
 		if (k == 0)
 		{
+			if (!FILTER)
+			{
 #pragma unroll
-			for (int q = 0; q < 9; ++q) a[q] += h * h * Kc[q];
-			a[0] += diagExtra;
-			a[4] += diagExtra;
-			a[8] += diagExtra;
+				for (int q = 0; q < 9; ++q) a[q] += h * h * Kc[q];
+				a[0] += diagExtra;
+				a[4] += diagExtra;
+				a[8] += diagExtra;
+			}
 			if (!Si)
 			{
 #pragma unroll
@@ -1325,6 +1416,11 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		}
 	}
 	if (!Si) bi = f3(0, 0, 0);
+	else if (FILTER)
+	{
+		bi = bi - bz;
+		if (ci) bi = bi - dot3(f3(fi4.x, fi4.y, fi4.z), bi) * f3(fi4.x, fi4.y, fi4.z);
+	}
 	TV* pb = vp<TV>(B.pb);
 	const TV bv[3] = {(TV)bi.x, (TV)bi.y, (TV)bi.z};
 	vst(pb, i, bv);
@@ -1702,7 +1798,7 @@ __device__ __forceinline__ void find_new_contacts(const DevBody& B, int i, float
 // v = v + dv, x = x0 + h v + y (sparse_force_solver.cpp:194-200); returns |dv|^2 of the vertex.
 // finish != 0 also ends the step: friction, clearing of external forces and translations, new
 // contacts (body.cpp:572-603), and writes the state instead of the Newton iterate.
-template <class TV, class L = LdPlain>
+template <class TV, class L = LdPlain, bool FILTER = false>
 __device__ __forceinline__ double final_vertex(const DevBody& B, int i, float h, bool first_newton, bool finish)
 {
 	float3 dv;
@@ -1717,6 +1813,12 @@ __device__ __forceinline__ double final_vertex(const DevBody& B, int i, float h,
 		TV y3[3];
 		vld<TV, L>((const TV*)B.py, i, y3);
 		dv = f3((float)y3[0], (float)y3[1], (float)y3[2]);
+	}
+	if (FILTER && first_newton)
+	{
+		// dv = y + z (sparse_force_solver.cpp:187)
+		const float4 f = B.filt[i];
+		if (filt_on(f)) dv = dv + f.w * f3(f.x, f.y, f.z);
 	}
 	float3 v = ldl3<L>(first_newton ? B.v : B.vi, i) + dv;
 	float3 x = ldl3<L>(B.x, i) + h * v + ldl3<L>(B.trans, i);

@@ -189,6 +189,9 @@ struct DevBody
 	uint8_t* c_apply;
 	float* c_nf;                // accumulated normal force
 	float* c_normal;            // 3 per contact
+	// filtered contacts (B3G_CONTACT_FILTER, per-op step only; null otherwise): per vertex the
+	// constrained normal n (zero when free) and the normal velocity change zn of z = zn n
+	float4* filt;
 
 	// solver vectors (vector type), planar
 	void* pb;

@@ -282,13 +282,20 @@ __device__ void pcg_start(Scalars* sc, double delta0)
 		sc->done = 0;
 }
 
-template <class TA, class TV>
+// Filtered contacts: the contact update and each vertex's constraint at the start of a step
+__global__ void __launch_bounds__(kThreads) k_contact_filter(DevBody B, float h)
+{
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
+		contact_filter_vertex(B, i, h);
+}
+
+template <class TA, class TV, bool FILTER>
 __global__ void __launch_bounds__(kThreads) k_assemble(DevBody B, StepParams P, int init)
 {
 	const int lane = threadIdx.x & 31;
 	double part = 0.0;
 	for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < B.nslices; s += (gridDim.x * blockDim.x) >> 5)
-		part += assemble_row<TA, TV>(B, s, lane, P, init != 0);
+		part += assemble_row<TA, TV, LdPlain, FILTER>(B, s, lane, P, init != 0);
 	if (!init) return;
 	double total;
 	if (grid_reduce(part, B.partials, &B.sc->counter, &total)) pcg_start(B.sc, total);
@@ -473,12 +480,12 @@ __global__ void __launch_bounds__(kThreads) k_resid(DevBody B, const TA* A, int 
 // v = v + dv, x = x0 + h v + y, Newton error |dv|^2 (sparse_force_solver.cpp:194-223).
 // mode 1 also finishes the step: friction, clearing of external forces and translations,
 // new contacts (body.cpp:572-603).
-template <class TV>
+template <class TV, bool FILTER>
 __global__ void __launch_bounds__(kThreads) k_final(DevBody B, StepParams P, int mode)
 {
 	double part = 0.0;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
-		part += final_vertex<TV>(B, i, P.h, P.first_newton != 0, mode == 1);
+		part += final_vertex<TV, LdPlain, FILTER>(B, i, P.h, P.first_newton != 0, mode == 1);
 	double total;
 	if (grid_reduce(part, B.partials, &B.sc->counter, &total))
 	{
@@ -664,9 +671,22 @@ cudaError_t op_assemble(const DevBody& B, const StepParamsHost& Ph, int prec, bo
 {
 	StepParams P = dev_params(Ph);
 	int g = slice_grid(B);
-	if (prec == kP64) k_assemble<double, double><<<g, kThreads, 0, st>>>(B, P, init ? 1 : 0);
-	else if (prec == kPBF) k_assemble<__nv_bfloat16, float><<<g, kThreads, 0, st>>>(B, P, init ? 1 : 0);
-	else k_assemble<float, float><<<g, kThreads, 0, st>>>(B, P, init ? 1 : 0);
+	const int in = init ? 1 : 0;
+	if (B.filt)
+	{
+		if (prec == kP64) k_assemble<double, double, true><<<g, kThreads, 0, st>>>(B, P, in);
+		else if (prec == kPBF) k_assemble<__nv_bfloat16, float, true><<<g, kThreads, 0, st>>>(B, P, in);
+		else k_assemble<float, float, true><<<g, kThreads, 0, st>>>(B, P, in);
+	}
+	else if (prec == kP64) k_assemble<double, double, false><<<g, kThreads, 0, st>>>(B, P, in);
+	else if (prec == kPBF) k_assemble<__nv_bfloat16, float, false><<<g, kThreads, 0, st>>>(B, P, in);
+	else k_assemble<float, float, false><<<g, kThreads, 0, st>>>(B, P, in);
+	return cudaGetLastError();
+}
+
+cudaError_t op_contact_filter(const DevBody& B, float h, cudaStream_t st)
+{
+	k_contact_filter<<<vertex_grid(B), kThreads, 0, st>>>(B, h);
 	return cudaGetLastError();
 }
 
@@ -734,8 +754,13 @@ cudaError_t op_final(const DevBody& B, const StepParamsHost& Ph, int prec, int m
 {
 	StepParams P = dev_params(Ph);
 	int g = vertex_grid(B);
-	if (prec == kP64) k_final<double><<<g, kThreads, 0, st>>>(B, P, mode);
-	else k_final<float><<<g, kThreads, 0, st>>>(B, P, mode);
+	if (B.filt)
+	{
+		if (prec == kP64) k_final<double, true><<<g, kThreads, 0, st>>>(B, P, mode);
+		else k_final<float, true><<<g, kThreads, 0, st>>>(B, P, mode);
+	}
+	else if (prec == kP64) k_final<double, false><<<g, kThreads, 0, st>>>(B, P, mode);
+	else k_final<float, false><<<g, kThreads, 0, st>>>(B, P, mode);
 	return cudaGetLastError();
 }
 

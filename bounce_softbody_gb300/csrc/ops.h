@@ -26,6 +26,8 @@ cudaError_t op_begin(const DevBody& B, cudaStream_t st, int max_it, double tol2,
 cudaError_t op_newton_begin(const DevBody& B, cudaStream_t st);
 cudaError_t op_elements(const DevBody& B, const StepParamsHost& P, cudaStream_t st);
 cudaError_t op_assemble(const DevBody& B, const StepParamsHost& P, int prec, bool init, cudaStream_t st);
+// filtered contacts: contact update and per-vertex constraints (B.filt) at the start of a step
+cudaError_t op_contact_filter(const DevBody& B, float h, cudaStream_t st);
 cudaError_t op_pcg_init(const DevBody& B, int prec, cudaStream_t st);
 // iteration j (0-based) of the current solve; refresh = the true-residual refresh period
 cudaError_t op_pcg_iteration(const DevBody& B, int prec, int j, int refresh, cudaStream_t st);

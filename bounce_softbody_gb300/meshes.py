@@ -379,6 +379,21 @@ def _quat_axis_angle(axis, angle):
     return np.array([*(np.sin(0.5 * angle) * axis), np.cos(0.5 * angle)])
 
 
+def block_on_floor(a: int = 5, b: int = 4, c: int = 5, tilt: float = 0.05, seed: int = 4, E: float = 2e5,
+                   nu: float = 0.33, radius: float = 0.03, friction: float = 0.3) -> BodyDesc:
+    """A free Kuhn tet block (spacing 0.1, density 1000: about 50 kg for 5 x 4 x 5 vertices) with a
+    contact sphere of `radius` on every vertex, resting with its lowest layer on a static box floor
+    (1 x 0.05 x 1 half extents, tilted `tilt` rad about z) that its spheres already overlap. The
+    reference's penalty contact (stiffness 1000) cannot carry its weight: the block sinks through
+    the floor; filtered contacts hold it."""
+    d = tet_grid(a, b, c, seed=seed, E=E, nu=nu, pin="none", name=f"floor{a}{b}{c}")
+    d.sphere_radius = np.full(d.n, radius)
+    d.sphere_friction = np.full(d.n, friction)
+    d.world_shapes = [WorldShape(SHAPE_BOX, radius=0.0, friction=0.5, p=np.array([1.0, 0.05, 1.0, 0, 0, 0, 0, 0, 0]),
+                                 rotation=_quat_axis_angle([0, 0, 1], tilt), translation=np.array([0.2, -0.07, 0.2]))]
+    return d
+
+
 def shape_scene(kind: str, m: int = 12, height: float = 0.05) -> BodyDesc:
     """An m x m cloth (side 0.8, contact radius 0.01, friction 0.3, two corners pinned) hanging
     just above one static world shape of the given kind: "capsule" (horizontal, r = 0.2), "box"

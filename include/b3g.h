@@ -82,6 +82,20 @@ typedef enum b3g_preconditioner
 	B3G_PRECOND_BLOCK_JACOBI = 1   /* inverse of each 3x3 diagonal block */
 } b3g_preconditioner;
 
+/* How vertex spheres touching static world shapes are resolved. */
+typedef enum b3g_contact_mode
+{
+	/* the reference's penalty spring and friction impulse
+	 * (sphere_shape_contact.cpp:53-189) */
+	B3G_CONTACT_PENALTY = 0,
+	/* opt-in extension, b3g_body_step only: an overlapping dynamic vertex is constrained along the
+	 * contact normal n through the solver's pre-filter (S = I - n n^T, z = (vt - v.n) n in
+	 * pA = S A S^T + I - S, pb = S (b - A z), dv = y + z; sparse_force_solver.cpp:170-190), vt the
+	 * Baumgarte velocity min(0.2 C, 0.2) / h of the penalty force's depth C; inelastic and
+	 * frictionless */
+	B3G_CONTACT_FILTER = 1
+} b3g_contact_mode;
+
 /* Static world shapes the body's vertex spheres collide with (b3WorldFixture with a b3Shape,
  * include/bounce_softbody/collision/shapes/). All in world space unless noted. */
 typedef enum b3g_shape_type
@@ -194,7 +208,7 @@ typedef struct b3g_solver_config
 	uint32_t refresh_period;       /* recompute r = b - A x when iteration % period == 0 */
 	int32_t precision;             /* b3g_precision */
 	int32_t preconditioner;        /* b3g_preconditioner */
-	int32_t reserved;
+	int32_t contact_mode;          /* b3g_contact_mode (B3G_CONTACT_PENALTY, the reference's) */
 } b3g_solver_config;
 
 typedef struct b3g_step_stats

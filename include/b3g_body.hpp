@@ -17,7 +17,7 @@
 //                                   b3g_body_get_state / set_state / apply_* / set_types
 //   b3_forceSolver*Iterations       b3Body::GetStepStats()
 // Extensions (no reference counterpart): SetSolverTolerance (the reference's Step always runs the
-// PCG at FLT_EPSILON), SetPrecision, SetPreconditioner.
+// PCG at FLT_EPSILON), SetPrecision, SetPreconditioner, SetContactMode (filtered contacts).
 //   b3Body::RayCastSingle            b3g_body_ray_cast
 // Not provided: debug draw, DestroyParticle and the Destroy* calls of fixtures.
 #pragma once
@@ -747,6 +747,7 @@ public:
 	void SetSolverTolerance(double pcgTolerance) { m_cfg.pcg_tolerance = pcgTolerance; }
 	void SetPrecision(b3g_precision p) { m_cfg.precision = p; }
 	void SetPreconditioner(b3g_preconditioner p) { m_cfg.preconditioner = p; }
+	void SetContactMode(b3g_contact_mode m) { m_cfg.contact_mode = m; }
 	b3g_body* GetDeviceBody()
 	{
 		build();

@@ -268,6 +268,7 @@ typedef struct
 	double* v_out;
 	uint32_t* sub_iters_out;
 	double* seconds_out;
+	int32_t contact_mode; /* 0 penalty contacts (the reference), 1 filtered contacts */
 } b3o_run;
 
 enum { STATIC = 0, KINEMATIC = 1, DYNAMIC = 2 };
@@ -348,6 +349,12 @@ typedef struct
 	real* Mval;  /* mass-matrix scalar per row */
 	uint8_t* S;  /* 1 = free, 0 = constrained */
 	uint32_t contacts_found;
+	/* filtered contacts (contact_mode 1): per vertex a flag, the constrained normal n and the
+	   normal velocity change zn of z = zn n */
+	int contact_mode;
+	uint8_t* fcons;
+	v3* fn;
+	real* fzn;
 } body_t;
 
 static void* xcalloc(size_t n, size_t s) { return calloc(n ? n : 1, s ? s : 1); }
@@ -740,6 +747,9 @@ static body_t* body_create(const b3o_desc* d)
 	for (size_t k = 0; k < sizeof(vecs) / sizeof(vecs[0]); ++k) *vecs[k] = xcalloc(n, sizeof(v3));
 	B->Mval = xcalloc(n, sizeof(real));
 	B->S = xcalloc(n, 1);
+	B->fcons = xcalloc(n, 1);
+	B->fn = xcalloc(n, sizeof(v3));
+	B->fzn = xcalloc(n, sizeof(real));
 	return B;
 }
 
@@ -757,7 +767,8 @@ static void body_free(body_t* B)
 	                B->spr, B->L0, B->ks, B->kd, B->bw, B->ms, B->srad, B->sfric, B->c_exists,
 	                B->c_apply, B->c_normalForce, B->c_normal, B->rowptr, B->col, B->tet_slot, B->tri_slot,
 	                B->spr_slot, B->diag, B->dfdx, B->dfdv, B->A, B->x0, B->v0, B->fe, B->y, B->xx, B->vv,
-	                B->fi, B->b, B->pb, B->py, B->w, B->tmp, B->r, B->d, B->qv, B->s, B->Minv, B->Mval, B->S};
+	                B->fi, B->b, B->pb, B->py, B->w, B->tmp, B->r, B->d, B->qv, B->s, B->Minv, B->Mval, B->S,
+	                B->fcons, B->fn, B->fzn};
 	for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); ++k) free(ptrs[k]);
 	free(B);
 }
@@ -1491,10 +1502,61 @@ static void apply_forces(body_t* B)
 	if (B->tri_elements)
 		for (uint32_t e = B->ntr; e-- > 0;) tri_apply(B, e);
 	for (uint32_t e = B->nt; e-- > 0;) tet_apply(B, e);
-	if (B->srad)
+	if (B->srad && B->contact_mode == 0)
 		for (uint32_t i = 0; i < n; ++i)
 			for (uint32_t k = 0; k < B->nw; ++k)
 				if (B->c_exists[(size_t)i * B->nw + k]) contact_apply(B, i, k);
+}
+
+/* Filtered contacts (contact_mode 1), an opt-in extension that uses the general pre-filter of
+   sparse_force_solver.cpp:170-178 (any S and z; force_solver.cpp:110-129 itself only passes
+   S = I or 0 and z = 0) instead of penalty springs. At the start of a step a dynamic vertex that
+   overlaps a world fixture it has a contact with (the first in fixture order; n its normal, from
+   the fixture to the vertex) is constrained to the Baumgarte target vt = min(0.2 C, 0.2) / h
+   along n (C: distance of the two contact points, as the penalty force measures it):
+   S = I - n n^T and z = (vt - v.n) n, so that the step ends with v.n = vt, which falls to zero
+   as the overlap closes; a vertex that no longer overlaps is free. The contact is inelastic and
+   frictionless (the constraint reports no normal force for the friction impulse). */
+static void contact_filter(body_t* B, real h)
+{
+	for (uint32_t i = 0; i < B->n; ++i)
+	{
+		B->fcons[i] = 0;
+		B->fn[i] = V(0, 0, 0);
+		B->fzn[i] = 0;
+		if (B->type[i] != DYNAMIC) continue;
+		for (uint32_t k = 0; k < B->nw; ++k)
+		{
+			size_t c = (size_t)i * B->nw + k;
+			if (!B->c_exists[c]) continue;
+			v3 x1 = B->x[i];
+			real r1 = B->srad[i], r2 = B->ws[k].radius;
+			v3 x2, n2;
+			if (!world_collide(&B->ws[k], x1, r1, &x2, &n2)) continue;
+			v3 c1 = sub(x1, scl(r1, n2));
+			v3 c2 = add(x2, scl(r2, n2));
+			real C = len(sub(c2, c1));
+			C = B3O_BAUMGARTE * C < B3O_MAX_CONTACT_LINEAR_CORRECTION ? B3O_BAUMGARTE * C : B3O_MAX_CONTACT_LINEAR_CORRECTION;
+			real vt = C / h;
+			B->fcons[i] = 1;
+			B->fn[i] = n2;
+			B->fzn[i] = vt - dot(B->v[i], n2);
+			break;
+		}
+	}
+}
+
+/* S_i M for a vertex's filter: M - n (n^T M) when constrained */
+static m33 filt_left(v3 n, int cons, m33 M)
+{
+	if (!cons) return M;
+	return msub(M, outer(n, V(dot(n, M.c[0]), dot(n, M.c[1]), dot(n, M.c[2]))));
+}
+/* M S_j: M - (M n) n^T when constrained */
+static m33 filt_right(m33 M, v3 n, int cons)
+{
+	if (!cons) return M;
+	return msub(M, outer(mv(M, n), n));
 }
 
 /* ------------------------------------------------------------------ sparse helpers */
@@ -1589,25 +1651,38 @@ static uint32_t solve_be(body_t* B, real h, uint32_t maxIt, uint32_t maxSub, rea
 			v3 Mdv = scl(B->Mval[i], sub(B->v0[i], B->vv[i]));
 			B->b[i] = add(add(Mdv, scl(h, add(B->fe[i], B->fi[i]))), acc);
 		}
-		/* pA = S A S^T + I - S ; pb = S b */
+		/* pA = S A S^T + I - S ; pb = S (b - A z); z = 0 after the first Newton iteration */
+		const int filt = B->contact_mode == 1;
 		for (uint32_t i = 0; i < n; ++i)
 		{
+			v3 bz = V(0, 0, 0);
+			const int ci = filt && B->fcons[i];
 			for (uint32_t k = B->rowptr[i]; k < B->rowptr[i + 1]; ++k)
 			{
 				uint32_t j = B->col[k];
+				const int cj = filt && B->fcons[j];
+				if (cj && iteration == 0) bz = add(bz, mv(B->A[k], scl(B->fzn[j], B->fn[j])));
 				if (!(B->S[i] && B->S[j])) B->A[k] = mzero();
+				else if (filt) B->A[k] = filt_left(B->fn[i], ci, filt_right(B->A[k], B->fn[j], cj));
 			}
 			if (!B->S[i]) B->A[B->diag[i]] = mdiag(1);
-			B->pb[i] = B->S[i] ? B->b[i] : V(0, 0, 0);
+			else if (ci) B->A[B->diag[i]] = madd(B->A[B->diag[i]], outer(B->fn[i], B->fn[i]));
+			v3 rb = sub(B->b[i], bz);
+			if (ci) rb = sub(rb, scl(dot(B->fn[i], rb), B->fn[i]));
+			B->pb[i] = B->S[i] ? rb : V(0, 0, 0);
 		}
 		uint32_t sub_it = pcg(B, B->A, B->pb, B->py, maxSub, subEps);
 		if (sub_it > maxSubIt) maxSubIt = sub_it;
+		/* dv = py + z */
 		for (uint32_t i = 0; i < n; ++i)
 		{
-			B->vv[i] = add(B->vv[i], B->py[i]);
+			v3 dv = B->py[i];
+			if (filt && iteration == 0 && B->fcons[i]) dv = add(dv, scl(B->fzn[i], B->fn[i]));
+			B->tmp[i] = dv;
+			B->vv[i] = add(B->vv[i], dv);
 			B->xx[i] = add(add(B->x0[i], scl(h, B->vv[i])), B->y[i]);
 		}
-		error = vdot(B->py, B->py, n);
+		error = vdot(B->tmp, B->tmp, n);
 		if (iteration == 0)
 		{
 			error0 = error;
@@ -1668,6 +1743,7 @@ static uint32_t body_step(body_t* B, real dt, uint32_t newtonIt, uint32_t maxSub
 				B->S[i] = 0;
 			}
 		}
+		if (B->srad && B->contact_mode == 1) contact_filter(B, dt);
 		it = solve_be(B, dt, newtonIt, maxSub, subEps);
 		for (uint32_t i = 0; i < n; ++i)
 		{
@@ -1735,6 +1811,7 @@ int b3o_simulate(const b3o_desc* d, b3o_run* run)
 {
 	body_t* B = body_create(d);
 	if (!B) return 1;
+	B->contact_mode = run->contact_mode;
 	double t0 = now_sec();
 	for (uint32_t s = 0; s < run->steps; ++s)
 	{
@@ -1795,6 +1872,7 @@ int b3o_ray_cast(const b3o_desc* d, b3o_run* run, uint32_t count, const double* 
 {
 	body_t* B = body_create(d);
 	if (!B) return 1;
+	B->contact_mode = run->contact_mode;
 	for (uint32_t s = 0; s < run->steps; ++s)
 	{
 		uint32_t it = body_step(B, (real)run->dt, run->newton_iters, run->max_sub, (real)run->sub_tol);
@@ -1855,7 +1933,11 @@ static void* batch_worker(void* arg)
 		pthread_mutex_unlock(&J->lock);
 		if (k >= J->count) break;
 		b3o_run* run = J->runs + k;
-		if (J->phase == 0) J->bodies[k] = body_create(J->descs + k);
+		if (J->phase == 0)
+		{
+			J->bodies[k] = body_create(J->descs + k);
+			if (J->bodies[k]) J->bodies[k]->contact_mode = run->contact_mode;
+		}
 		else if (J->phase == 1)
 		{
 			body_t* B = J->bodies[k];

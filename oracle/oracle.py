@@ -66,6 +66,7 @@ class _Run(C.Structure):
         ("steps", C.c_uint32), ("dt", C.c_double), ("newton_iters", C.c_uint32), ("max_sub", C.c_uint32),
         ("sub_tol", C.c_double), ("use_body_step", C.c_int32),
         ("x_out", _dp), ("v_out", _dp), ("sub_iters_out", _up), ("seconds_out", _dp),
+        ("contact_mode", C.c_int32),
     ]
 
 
@@ -228,8 +229,13 @@ def _make_desc(body):
 
 def simulate(body, steps: int, dt: float = 1.0 / 60.0, newton_iters: int = 1, max_sub: int = 200,
              sub_tol: float = 1e-5, kind: str = "port", bits: int = 32, use_body_step: bool = False,
-             threads: int = 1):
-    """Run ``steps`` implicit steps on a CPU implementation. Returns (x, v, iters, seconds)."""
+             threads: int = 1, contact_mode: int = 0):
+    """Run ``steps`` implicit steps on a CPU implementation. Returns (x, v, iters, seconds).
+
+    contact_mode 1 (filtered contacts) exists in the restatement only: the reference has no such
+    mode."""
+    if contact_mode and kind != "port":
+        raise ValueError("filtered contacts are an extension of the restatement")
     lib = _lib(kind, bits)
     desc, keep = _make_desc(body)
     n = body.n
@@ -241,6 +247,7 @@ def simulate(body, steps: int, dt: float = 1.0 / 60.0, newton_iters: int = 1, ma
     run.steps, run.dt, run.newton_iters, run.max_sub = steps, dt, newton_iters, max_sub
     run.sub_tol = sub_tol
     run.use_body_step = 1 if use_body_step else 0
+    run.contact_mode = contact_mode
     run.x_out, run.v_out = x.ctypes.data_as(_dp), v.ctypes.data_as(_dp)
     run.sub_iters_out = it.ctypes.data_as(_up)
     run.seconds_out = sec.ctypes.data_as(_dp)

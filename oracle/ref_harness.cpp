@@ -132,6 +132,7 @@ struct RefRun
 	double* v_out;              // 3n
 	uint32_t* sub_iters_out;    // steps (max PCG iterations of each step), may be null
 	double* seconds_out;        // wall time of the stepping loop
+	int32_t contact_mode;       // unused: the reference has penalty contacts only
 };
 
 } // extern "C"
