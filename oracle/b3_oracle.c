@@ -27,6 +27,11 @@
  *   - Jacobi PCG, residual refresh every 50      src/bounce_softbody/sparse/sparse_solver.cpp:28-109
  *   - math (quaternion, basis, perp, adjugate)   include/bounce_softbody/common/math/{quat.h:63-146,mat33.h:276-327,vec3.h:255-270}
  *
+ * One extension has no reference counterpart and so no reference pin: filtered contacts
+ * (b3o_run.contact_mode 1, contact_filter below), which fills the pre-filter's general S and z
+ * (sparse_force_solver.cpp:170-190) from the contacts instead of adding penalty springs; its tests
+ * check its physics and hold the CUDA path to it.
+ *
  * The reference keeps sparse matrices as linked lists; here they are CSR rows of 3x3 blocks
  * with a fixed pattern. Element order follows the reference's head-inserted force and fixture
  * lists (newest first). Sums over a row run in column order, so float results differ from the
