@@ -1,4 +1,4 @@
-// Test infrastructure only: a driver around the reference library compiled from its own
+// Test infrastructure only: a harness around the reference library compiled from its own
 // sources (see oracle/Makefile). Nothing in the product links or loads this file.
 //
 // It builds a b3Body from flat arrays in O(n) and steps it exactly like b3Body::Step
