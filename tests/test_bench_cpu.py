@@ -55,3 +55,18 @@ dist.destroy_process_group()
     r = run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
              "--master-addr", "127.0.0.1", "--master-port", "29532", str(script)])
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_threaded_oracle_batch_equals_single_runs():
+    """The CPU baseline's threaded batch (oracle.simulate_batch: one body per task on host
+    threads) gives each body bitwise what a single run of the restatement gives."""
+    import numpy as np
+
+    import oracle
+    from bounce_softbody_gb300 import meshes
+
+    descs = meshes.batch_bodies(count=5, lo=3, hi=7, seed=2)
+    xs, vs, its, _ = oracle.simulate_batch(descs, 3, bits=32, threads=3)
+    for d, x, v, it in zip(descs, xs, vs, its):
+        xr, vr, itr, _ = oracle.simulate(d, 3, kind="port", bits=32)
+        assert np.array_equal(x, xr) and np.array_equal(v, vr) and np.array_equal(it, itr), d.name
