@@ -3,8 +3,9 @@
 // (binary: n, T, positions, types, tets, E, nu, density, damping, steps, dt, tol) from argv[1],
 // writes the final positions and velocities (binary floats) to argv[2]. With a third argument
 // "shapes" every particle also gets a contact sphere (radius 0.03, friction 0.3) and the body
-// collides with a static b3BoxShape floor and a b3CapsuleShape; with "cloth" it runs the
-// Baraff-Witkin cloth scene below instead (argv[1] is not read).
+// collides with a static b3BoxShape floor and a b3CapsuleShape ("shapes filter": the same with
+// filtered contacts, SetContactMode); with "cloth" it runs the Baraff-Witkin cloth scene below
+// instead (argv[1] is not read).
 #include "b3g_body.hpp"
 
 #include <algorithm>
@@ -183,6 +184,7 @@ int main(int argc, char** argv)
 		fd.shape = &pole;
 		fd.friction = 0.2f;
 		body.CreateFixture(fd);
+		if (argc > 4 && std::string(argv[4]) == "filter") body.SetContactMode(B3G_CONTACT_FILTER);
 	}
 	body.SetSolverTolerance(tol);
 	for (uint32 s = 0; s < steps; ++s) body.Step(dt, 1, 200);

@@ -26,8 +26,8 @@ def test_facade_compiles_and_links(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("shapes", [False, True])
-def test_facade_matches_c_abi(tmp_path, ctx, shapes):
+@pytest.mark.parametrize("shapes,mode", [(False, 0), (True, 0), (True, 1)], ids=["tets", "shapes", "shapes_filter"])
+def test_facade_matches_c_abi(tmp_path, ctx, shapes, mode):
     exe = build_demo(tmp_path)
     desc = meshes.tet_grid(6, 5, 7, seed=4, E=2e5, nu=0.33, pin="none" if shapes else "y0")
     if shapes:
@@ -51,12 +51,12 @@ def test_facade_matches_c_abi(tmp_path, ctx, shapes):
         np.array([steps], np.uint32).tofile(f)
         np.array([dt, tol], np.float32).tofile(f)
     out = tmp_path / "out.bin"
-    r = subprocess.run([exe, str(inp), str(out)] + (["shapes"] if shapes else []), capture_output=True, text=True,
-                       timeout=300)
+    extra = (["shapes"] if shapes else []) + (["filter"] if mode == 1 else [])
+    r = subprocess.run([exe, str(inp), str(out)] + extra, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     res = np.fromfile(out, np.float32).reshape(2, desc.n, 3)
     g = b3g.Body(ctx, desc)
-    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=tol)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=tol, contact_mode=mode)
     for _ in range(steps):
         g.step(dt, cfg)
     x, v = g.state()
