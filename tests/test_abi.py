@@ -99,3 +99,27 @@ def test_enum_values_match_the_header():
         assert getattr(meshes, py) == enum[c], py
     for code, name in b3g.SOLVE_STATUS.items():
         assert enum["B3G_SOLVE_" + name.upper()] == code, name
+
+
+def test_integration_c_example_compiles_and_links(tmp_path):
+    """The C usage example of INTEGRATION.md, wrapped in a function that declares its inputs,
+    compiles as C against include/b3g.h and links against libb3g.so (it is not run: no GPU)."""
+    import subprocess
+
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    block = re.search(r"```c\n(.*?)```", text, re.S).group(1)
+    src = tmp_path / "example.c"
+    src.write_text("#include <stdio.h>\n#include <stdint.h>\n" + block.replace('#include "b3g.h"', '#include "b3g.h"\n'
+                   "void example(uint32_t n, float* xyz, float* vel, const int32_t* types, const float* damp,\n"
+                   "             uint32_t T, const uint32_t* ids, const float* E, const float* nu, const float* rho) {", 1)
+                   + "}\n")
+    lib = os.path.dirname(b3g.LIB_PATH)
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-Wno-unused-variable", "-c", "-I",
+                        os.path.join(ROOT, "include"), str(src), "-o", str(tmp_path / "example.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    main = tmp_path / "main.c"
+    main.write_text("int main(void) { return 0; }\n")
+    r = subprocess.run(["gcc", str(tmp_path / "example.o"), str(main), "-L", lib, "-lb3g", "-o", str(tmp_path / "ex")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
