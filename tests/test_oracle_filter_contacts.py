@@ -68,3 +68,25 @@ def test_filtered_contacts_newton_iterations():
     x1, v1, _, _ = oracle.simulate(desc, 30, kind="port", bits=64, contact_mode=1)
     x3, v3, _, _ = oracle.simulate(desc, 30, kind="port", bits=64, contact_mode=1, newton_iters=3)
     assert np.linalg.norm(x3 - x1) / np.linalg.norm(x1 - desc.x) < 0.05
+
+
+def test_constrained_vertices_end_the_step_at_the_target_normal_velocity():
+    """The filtered system's solution has no component along a constrained vertex's normal
+    (n^T py = 0 when S = I - n n^T), so dv.n = z.n and a vertex that overlaps the floor at the
+    start of a step ends it with v.n = vt = min(0.2 (r - dist), 0.2) / h, recomputed here from the
+    floor's geometry, to the PCG's tolerance."""
+    tilt, h, s = 0.05, 1.0 / 60.0, 12
+    desc = meshes.block_on_floor(tilt=tilt)
+    r = desc.sphere_radius[0]
+    n = np.array([-np.sin(tilt), np.cos(tilt), 0.0])
+    xs, vs, _, _ = oracle.simulate(desc, s, kind="port", bits=64, contact_mode=1, sub_tol=1e-8)
+    x1, v1, _, _ = oracle.simulate(desc, s + 1, kind="port", bits=64, contact_mode=1, sub_tol=1e-8)
+    sh = desc.world_shapes[0]
+    top = np.asarray(sh.translation) + sh.p[1] * n          # a point of the top face
+    dist = (xs - top) @ n                                   # sphere centre above the face
+    inside = np.abs((xs - np.asarray(sh.translation)) @ np.array([np.cos(tilt), np.sin(tilt), 0.0])) < 0.9
+    cons = (dist < r) & inside
+    assert cons.sum() >= 20
+    vt = np.minimum(0.2 * (r - dist[cons]), 0.2) / h
+    # measured: 2e-11 m/s against targets of 0.002-0.024 m/s
+    np.testing.assert_allclose(v1[cons] @ n, vt, rtol=0, atol=1e-8)
