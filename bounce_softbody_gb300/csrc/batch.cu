@@ -685,7 +685,8 @@ extern "C" int b3g_step_batch_noalloc(b3g_context* ctx, b3g_body* const* bodies,
 		e = cudaMemcpyAsync(d_order, g_noalloc_host_order, count * sizeof(int), cudaMemcpyHostToDevice, st);
 	if (e != cudaSuccess) return cuda_fail(e, "b3g_step_batch_noalloc upload");
 
-	// the size heuristic of b3g_step_batch (no autotuning: it would need a state snapshot)
+	// fixed size rule, no autotuning (which would need a state snapshot): clusters of 4 CTAs for
+	// bodies of 4096 vertices or more, single CTAs below
 	const int cluster = maxn >= 4096 ? 4 : 1;
 	const int threshold = 4096;
 	int nbig = 0;
@@ -700,8 +701,8 @@ extern "C" int b3g_step_batch_noalloc(b3g_context* ctx, b3g_body* const* bodies,
 	A.nbig = nbig;
 	A.small = d_order + nbig;
 	A.nsmall = (int)count - nbig;
-	A.queue = d_queue;  // op_batch clears the two counters before the launch
-	A.steps = (int)steps;
+	A.queue = d_queue;  // op_batch clears the work counters before each step's launches
+	A.steps = 1;        // one step per op_batch: a single-Newton step is two launches (assembly, then PCG)
 	A.h = dt;
 	A.newton = (int)std::max<uint32_t>(1u, cfg.force_iterations);
 	A.max_iter = (int)cfg.max_pcg_iterations;
@@ -712,7 +713,7 @@ extern "C" int b3g_step_batch_noalloc(b3g_context* ctx, b3g_body* const* bodies,
 	A.cluster = cluster;
 	A.ctas = m * cluster;
 	A.prof = nullptr;
-	e = op_batch(A, st);
+	for (uint32_t s = 0; s < steps && e == cudaSuccess; ++s) e = op_batch(A, st);
 	if (e != cudaSuccess) return cuda_fail(e, "b3g_step_batch_noalloc launch");
 	if (stats)
 	{

@@ -252,17 +252,19 @@ B3G_API int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_t c
                    const b3g_solver_config* config, uint32_t steps, b3g_step_stats* stats);
 
 /* Like b3g_step_batch, without allocating anything. No counterpart in the reference.
- * For callers that cannot allocate device memory while they step: a frame captured into a CUDA
- * graph (cudaMalloc is not permitted during stream capture), engines that forbid allocation after
- * load or keep a fixed device-memory budget (cudaMalloc / cudaFree also synchronise the device).
- * b3g_step_batch allocates per-batch tables on first use; this entry point keeps them in a fixed
- * device array of the library instead (held by every GPU that loads the library until exit), for
- * at most 512 bodies per call (more fails with B3G_ERROR_UNSUPPORTED). The bodies bring their own
- * state and solver buffers: each must already have buffers for the requested precision (FP32
- * always does; FP64 / BF16 after a first step in that precision). The schedule is the size
- * heuristic (clusters of 4 CTAs for bodies of 4096 vertices or more), not autotuned; dt must be
- * > 0. The first call on a device looks the array up and clears it (set-up): make that first call
- * before any stream capture. Every call reuses the same array, so calls whose work overlaps on the
+ * For callers that cannot call cudaMalloc while they step: engines that forbid device allocation
+ * after load or run under a fixed device-memory budget, and real-time loops that cannot afford the
+ * device-wide synchronisation cudaMalloc / cudaFree bring. b3g_step_batch allocates per-batch
+ * tables on first use; this entry point keeps them in a fixed device array of the library instead
+ * (held by every GPU that loads the library until exit), for at most 512 bodies per call (more
+ * fails with B3G_ERROR_UNSUPPORTED). Differences from b3g_step_batch: each body must already have
+ * solver buffers for the requested precision (FP32 always does; FP64 / BF16 after a first step in
+ * that precision), where b3g_step_batch creates them; dt must be > 0 (b3g_step_batch steps each
+ * body alone for dt <= 0); the schedule is a fixed size rule (clusters of 4 CTAs for bodies of
+ * 4096 vertices or more, single CTAs below), not autotuned. The first call on a device looks the
+ * array up and clears it (set-up): make that first call before any stream capture. Each call
+ * copies the body descriptors to the device from static host arrays of the library, which the
+ * next call rewrites. Every call reuses the same device array, so calls whose work overlaps on the
  * GPU (other streams, other contexts on the same device) race; calls on one stream are ordered. */
 B3G_API int b3g_step_batch_noalloc(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float dt,
                                    const b3g_solver_config* config, uint32_t steps, b3g_step_stats* stats);
