@@ -39,6 +39,8 @@ PCG_MAX = 200
 # DRAM traffic / algorithmic bytes of the batch PCG launch, from the ncu capture of the
 # 128-body case (profiles/k_batch_batch512.md)
 PCG_TRAFFIC_RATIO = 1.056
+# steps of the CPU-baseline run and of the parity check, from the bodies' initial state
+PARITY_STEPS = 3
 
 
 def parse():
@@ -225,19 +227,29 @@ def measured_peak_hbm():
 
 
 # ------------------------------------------------------------------ CPU implementation (oracle port)
-def cpu_sample(descs):
-    """A bounded, size-stratified sample: every 8th body in size order (about 1/8 of the vertices)."""
-    order = sorted(range(len(descs)), key=lambda k: -descs[k].n)
-    return [descs[k] for k in order[::8]] if len(descs) > 8 else list(descs)
+def stratified(n_items, sizes, every):
+    """Indices of every `every`-th item in size order (largest first)."""
+    order = sorted(range(n_items), key=lambda k: -sizes[k])
+    return order[::every] if n_items > every else order
 
 
-def run_cpu(descs, steps, dt, max_sub, threads):
+def run_cpu(descs, steps, dt, max_sub, threads, bits=32):
+    """The oracle's C restatement of the reference step on `threads` host threads, from each body's
+    initial state. Returns (vertex-steps/s, seconds, iterations, positions, velocities)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
-    _, _, iters, sec = oracle.simulate_batch(descs, steps, dt=dt, max_sub=max_sub, sub_tol=PCG_TOL, bits=32,
-                                             threads=threads)
-    return sum(d.n for d in descs) * steps / sec, sec, iters
+    xs, vs, iters, sec = oracle.simulate_batch(descs, steps, dt=dt, max_sub=max_sub, sub_tol=PCG_TOL, bits=bits,
+                                               threads=threads)
+    return sum(d.n for d in descs) * steps / sec, sec, iters, xs, vs
+
+
+def rel_errors(x, v, xr, vr, x0):
+    """Position error relative to the oracle's displacement, velocity error relative to its norm."""
+    xr, vr = np.asarray(xr, np.float64), np.asarray(vr, np.float64)
+    ex = float(np.linalg.norm(np.asarray(x, np.float64) - xr) / max(np.linalg.norm(xr - x0), 1e-30))
+    ev = float(np.linalg.norm(np.asarray(v, np.float64) - vr) / max(np.linalg.norm(vr), 1e-30))
+    return ex, ev
 
 
 def reference_arm(args, world, rank, pg):
@@ -245,18 +257,18 @@ def reference_arm(args, world, rank, pg):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    sample = cpu_sample(descs)
+    sample = descs  # the whole workload: every body, one step from its initial state per timed step
     dt, mx = step_dt(args), pcg_max(args)
     for _ in range(args.warmup):
         run_cpu(sample, 1, dt, mx, threads)
     times = []
     for _ in range(args.steps):
-        _, sec, _ = run_cpu(sample, 1, dt, mx, threads)
+        _, sec, _, _, _ = run_cpu(sample, 1, dt, mx, threads)
         times.append(sec)
     total = sum(times)
     vs = sum(d.n for d in sample) * args.steps / total
-    desc = (f"oracle C restatement (FP32, Jacobi PCG, tol 1e-5) of {len(sample)} of {len(descs)} bodies "
-            f"({sum(d.n for d in sample)} vertices), 1 step per timed step, {threads} threads")
+    desc = (f"oracle C restatement (FP32, Jacobi PCG, tol 1e-5) of all {len(descs)} bodies "
+            f"({sum(d.n for d in sample)} vertices), 1 step from the initial state per timed step, {threads} threads")
     line = {"metric": METRIC, "value": vs, "unit": "vertex-steps/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes)",
@@ -417,13 +429,44 @@ def ours(args, world, rank, local, pg):
         plain_vs = sum(infos[k]["vertices"] for k in sample) / plain_s
         extras["plain"] = {"value": plain_vs, "unit": "vertex-steps/s", "bodies": len(sample),
                            "batched_over_plain": value / plain_vs}
-        # CPU baseline: the oracle restatement on this host's cores, bounded sample
+        # solver outcome of the last timed-region step of every body
+        last = [b.stats() for b in bodies]
+        # CPU baseline: the oracle restatement on this host's cores, every body of the workload,
+        # PARITY_STEPS steps from the initial state (FP32, as the reference's float build)
         threads = os.cpu_count() or 1
-        cs = cpu_sample(descs)
-        cvs, csec, _ = run_cpu(cs, 1, dt, mx, threads)
+        cvs, csec, c_its, c_xs, c_vs = run_cpu(descs, PARITY_STEPS, dt, mx, threads)
         extras["cpu_baseline"] = {"value": cvs, "unit": "vertex-steps/s", "cores": threads, "kind": "port",
-                                  "sample": f"{len(cs)} of {len(descs)} bodies ({sum(d.n for d in cs)} vertices), "
-                                            f"1 step, oracle C restatement FP32, {csec:.2f} s"}
+                                  "sample": f"all {len(descs)} bodies ({nverts} vertices), {PARITY_STEPS} steps from "
+                                            f"the initial state, oracle C restatement FP32, {csec:.2f} s"}
+        # parity: the GPU batch (the timed kernels, through the graph) from the same initial
+        # state against the FP32 restatement on every body and the FP64 restatement on a
+        # size-stratified sample
+        for b, d, i in zip(bodies, descs, infos):
+            b.set_state(d.x, d.v)
+            if i["tets"]:
+                q = np.zeros((i["tets"], 4), np.float32)
+                q[:, 3] = 1.0
+                b.set_rotations(q)
+        ctx.synchronize()
+        pst = b3g.step_batch(ctx, bodies, dt, PARITY_STEPS, scfg, stats=True)
+        g_state = [b.state() for b in bodies]
+        e32 = [rel_errors(x, v, c_xs[k], c_vs[k], descs[k].x) for k, (x, v) in enumerate(g_state)]
+        pick = stratified(len(descs), [d.n for d in descs], 8)
+        _, _, p_its, p_xs, p_vs = run_cpu([descs[k] for k in pick], PARITY_STEPS, dt, mx, threads, bits=64)
+        e64 = [rel_errors(*g_state[k], p_xs[j], p_vs[j], descs[k].x) for j, k in enumerate(pick)]
+        extras["parity"] = {
+            "oracle": f"FP64 restatement of the reference step, {len(pick)} of {len(descs)} bodies (every 8th by "
+                      f"size), {PARITY_STEPS} steps from the initial state through the timed batch kernels",
+            "rel_x_max": max(e[0] for e in e64), "rel_v_max": max(e[1] for e in e64),
+            "iters_diff_max": int(max(abs(int(pst[k]["pcg_iterations"]) - int(p_its[j][-1]))
+                                      for j, k in enumerate(pick))),
+            "vs_fp32_all_bodies": {"rel_x_max": max(e[0] for e in e32), "rel_v_max": max(e[1] for e in e32),
+                                   "iters_diff_max": int(max(abs(int(pst[k]["pcg_iterations"]) - int(c_its[k][-1]))
+                                                             for k in range(len(descs))))},
+            "x_error": "|x - x_oracle| / |x_oracle - x0| per body", "v_error": "|v - v_oracle| / |v_oracle| per body",
+            "bodies_max_iterations": sum(1 for s in last if s["solve_status"] != "converged"),
+            "residual_ratio_max": max(float(s["residual_ratio"]) for s in last),
+            "solver_outcome": "last timed step of every body: solves not converged, largest sqrt(delta/delta0)"}
 
     # persistent path: two launches per step (elements + assembly, then PCG + final update), plus
     # a 16-byte memset of the work counters that is not a kernel. Per-op path per step: begin,
