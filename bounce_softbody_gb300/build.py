@@ -21,7 +21,7 @@ LIB = os.path.join(OUT, "libb3g.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "kernels.cu", "batch.cu", "persistent.cu", "persistent_f32.cu", "persistent_f64.cu",
-           "persistent_bf16.cu", "server.cu", "pattern.cpp", "shapes.cpp", "forces.cpp"]
+           "persistent_bf16.cu", "server.cu", "sparse.cu", "pattern.cpp", "shapes.cpp", "forces.cpp"]
 
 
 def nvcc() -> str:
@@ -46,6 +46,7 @@ def _stale(obj: str, src: str) -> bool:
     t = os.path.getmtime(obj)
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     deps.append(os.path.join(HERE, "..", "include", "b3g.h"))
+    deps.append(os.path.join(HERE, "..", "include", "b3g_sparse.h"))
     return any(os.path.getmtime(d) > t for d in deps)
 
 

@@ -384,6 +384,7 @@ int b3g_context_destroy(b3g_context* c)
 	cudaSetDevice(c->device);
 	cudaStreamSynchronize(c->stream);
 	destroy_batch_cache(c);
+	release_sparse(c);
 	for (b3g_body* b : c->live_bodies)
 	{
 		release_body_memory(b);

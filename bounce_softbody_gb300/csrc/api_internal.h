@@ -9,6 +9,10 @@
 #include <vector>
 
 struct BatchCache;
+namespace b3g {
+struct SparseObject;
+struct SparseWork;
+}
 
 struct b3g_context
 {
@@ -36,6 +40,10 @@ struct b3g_context
 	// live bodies: destroying the context releases their device memory and detaches them, so a
 	// later b3g_body_destroy only frees the host object
 	std::vector<b3g_body*> live_bodies;
+	// containers of include/b3g_sparse.h made on this context (released with it), and the
+	// workspace of its solvers
+	std::vector<b3g::SparseObject*> live_sparse;
+	b3g::SparseWork* sparse_work = nullptr;
 };
 
 namespace b3g {
@@ -108,4 +116,6 @@ cudaError_t op_set_types(const DevBody& B, const int8_t* new_types, cudaStream_t
 } // namespace b3g
 
 void destroy_batch_cache(b3g_context* c);
+// frees the device memory of every sparse container of the context and detaches them
+void release_sparse(b3g_context* c);
 void forget_body_in_batch_cache(b3g_context* c, b3g_body* b);

@@ -78,11 +78,21 @@ def build_port() -> None:
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
 
 
+def reference_root() -> Optional[str]:
+    """The reference project's sources: $B3G_REFERENCE, else the read-only checkout this recipe
+    was written against; None where neither exists (the GPU host, for one)."""
+    for cand in (os.environ.get("B3G_REFERENCE"), "/root/reference"):
+        if cand and os.path.isdir(os.path.join(cand, "src")):
+            return cand
+    return None
+
+
 def build_ref() -> bool:
     """Build the reference harness if the reference sources are present; return availability."""
-    if not os.path.isdir("/root/reference/src"):
+    root = reference_root()
+    if root is None:
         return ref_available()
-    subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref"], check=True)
+    subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={root}"], check=True)
     return ref_available()
 
 
@@ -321,3 +331,126 @@ def simulate_batch(bodies, steps: int, dt: float = 1.0 / 60.0, newton_iters: int
         raise RuntimeError(f"oracle batch failed with {rc}")
     del keep
     return [o[0] for o in outs], [o[1] for o in outs], [o[2][:steps] for o in outs], float(sec.value)
+
+
+# ---------------------------------------------------------------- sparse containers and solvers
+class _Jac(C.Structure):
+    """Mirror of RefJacobians (oracle/ref_harness.cpp)."""
+    _fields_ = [("capacity", C.c_uint32), ("dfdx_count", C.c_uint32), ("dfdv_count", C.c_uint32),
+                ("dfdx_rows", _up), ("dfdx_cols", _up), ("dfdx_vals", _dp),
+                ("dfdv_rows", _up), ("dfdv_cols", _up), ("dfdv_vals", _dp),
+                ("x", _dp), ("v", _dp), ("f", _dp), ("fe", _dp), ("mass", _dp), ("dynamic", _ip)]
+
+
+class _SpIn(C.Structure):
+    """Mirror of RefSparseIn (oracle/ref_harness.cpp)."""
+    _fields_ = [("n", C.c_uint32), ("h", C.c_double),
+                ("dfdx_count", C.c_uint32), ("dfdx_rows", _up), ("dfdx_cols", _up), ("dfdx_vals", _dp),
+                ("dfdv_count", C.c_uint32), ("dfdv_rows", _up), ("dfdv_cols", _up), ("dfdv_vals", _dp),
+                ("f", _dp), ("x0", _dp), ("v0", _dp), ("fe", _dp), ("M", _dp), ("S", _dp), ("y", _dp), ("z", _dp),
+                ("u", _dp), ("D", _dp), ("s", C.c_double), ("cg_max_iterations", C.c_uint32),
+                ("cg_tolerance", C.c_double), ("capacity", C.c_uint32)]
+
+
+class _SpOut(C.Structure):
+    """Mirror of RefSparseOut (oracle/ref_harness.cpp)."""
+    _fields_ = [("spmv", _dp), ("b", _dp), ("pb", _dp), ("diag_u", _dp), ("dot_u_pb", C.c_double),
+                ("len2_pb", C.c_double), ("pA_row_ptr", _up), ("pA_cols", _up), ("pA_vals", _dp),
+                ("pA_count", C.c_uint32), ("cg_x", _dp), ("cg_iterations", C.c_uint32), ("cg_error", C.c_double),
+                ("be_x", _dp), ("be_v", _dp), ("be_iterations", C.c_uint32), ("be_error", C.c_double),
+                ("be_min_sub", C.c_uint32), ("be_max_sub", C.c_uint32)]
+
+
+# names of the SpMV products of RefSparseOut::spmv, in order
+SPARSE_PRODUCTS = ["A", "pA", "D_dfdx", "dfdx_D", "s_dfdx", "dfdx_plus_dfdv", "dfdx_minus_dfdv", "dfdx_plus_D",
+                   "D_minus_dfdx", "zero_dfdx"]
+
+
+def ref_jacobians(body, steps: int, dt: float = 1.0 / 60.0, max_sub: int = 200, sub_tol: float = 1e-5,
+                  bits: int = 32, capacity: Optional[int] = None) -> dict:
+    """The reference's force model evaluated once at the state after `steps` steps: f, dfdx and
+    dfdv (COO in the reference's row-list order, 9 values per block in b3Mat33 column order), the
+    state, external forces, masses and the dynamic flags, by input vertex index."""
+    lib = _lib("ref", bits)
+    fn = lib.ref_jacobians
+    fn.argtypes = [C.POINTER(_Desc), C.POINTER(_Run), C.POINTER(_Jac)]
+    fn.restype = C.c_int
+    desc, keep = _make_desc(body)
+    n = body.n
+    cap = capacity or 64 * n
+    arrs = {k: np.zeros(cap, np.uint32) for k in ("dfdx_rows", "dfdx_cols", "dfdv_rows", "dfdv_cols")}
+    arrs.update({k: np.zeros(9 * cap) for k in ("dfdx_vals", "dfdv_vals")})
+    arrs.update({k: np.zeros(3 * n) for k in ("x", "v", "f", "fe")})
+    arrs["mass"] = np.zeros(n)
+    arrs["dynamic"] = np.zeros(n, np.int32)
+    jac = _Jac()
+    jac.capacity = cap
+    for k, a in arrs.items():
+        setattr(jac, k, a.ctypes.data_as(_up if a.dtype == np.uint32 else (_ip if a.dtype == np.int32 else _dp)))
+    run = _Run()
+    run.steps, run.dt, run.newton_iters, run.max_sub, run.sub_tol = steps, dt, 1, max_sub, sub_tol
+    if fn(C.byref(desc), C.byref(run), C.byref(jac)) != 0:
+        raise RuntimeError("ref_jacobians: COO capacity too small")
+    del keep
+    out = {}
+    for m in ("dfdx", "dfdv"):
+        c = getattr(jac, f"{m}_count")
+        out[f"{m}_rows"] = arrs[f"{m}_rows"][:c].copy()
+        out[f"{m}_cols"] = arrs[f"{m}_cols"][:c].copy()
+        out[f"{m}_vals"] = arrs[f"{m}_vals"][:9 * c].reshape(c, 9).copy()
+    for k in ("x", "v", "f", "fe"):
+        out[k] = arrs[k].reshape(n, 3).copy()
+    out["mass"], out["dynamic"] = arrs["mass"], arrs["dynamic"]
+    return out
+
+
+def ref_sparse_ops(n: int, h: float, jac: dict, M, S, y, z, u, D, s: float, cg_max: int, cg_tol: float,
+                   bits: int = 32) -> dict:
+    """The reference's container operators, b3SparseSolveCG and a one-iteration b3SparseSolveBE on
+    the given matrices (see RefSparseIn / RefSparseOut in oracle/ref_harness.cpp)."""
+    lib = _lib("ref", bits)
+    fn = lib.ref_sparse_ops
+    fn.argtypes = [C.POINTER(_SpIn), C.POINTER(_SpOut)]
+    fn.restype = C.c_int
+    keep = []
+
+    def d(a):
+        a = np.ascontiguousarray(a, np.float64).ravel()
+        keep.append(a)
+        return a.ctypes.data_as(_dp)
+
+    def u32(a):
+        a = np.ascontiguousarray(a, np.uint32).ravel()
+        keep.append(a)
+        return a.ctypes.data_as(_up)
+
+    si = _SpIn()
+    si.n, si.h = n, h
+    for m in ("dfdx", "dfdv"):
+        setattr(si, f"{m}_count", len(jac[f"{m}_rows"]))
+        setattr(si, f"{m}_rows", u32(jac[f"{m}_rows"]))
+        setattr(si, f"{m}_cols", u32(jac[f"{m}_cols"]))
+        setattr(si, f"{m}_vals", d(jac[f"{m}_vals"]))
+    si.f, si.x0, si.v0, si.fe = d(jac["f"]), d(jac["x"]), d(jac["v"]), d(jac["fe"])
+    si.M, si.S, si.y, si.z, si.u, si.D = d(M), d(S), d(y), d(z), d(u), d(D)
+    si.s, si.cg_max_iterations, si.cg_tolerance = s, cg_max, cg_tol
+    cap = len(jac["dfdx_rows"]) + len(jac["dfdv_rows"]) + n
+    si.capacity = cap
+    o = {"spmv": np.zeros(10 * 3 * n), "b": np.zeros(3 * n), "pb": np.zeros(3 * n), "diag_u": np.zeros(3 * n),
+         "pA_row_ptr": np.zeros(n + 1, np.uint32), "pA_cols": np.zeros(cap, np.uint32), "pA_vals": np.zeros(9 * cap),
+         "cg_x": np.zeros(3 * n), "be_x": np.zeros(3 * n), "be_v": np.zeros(3 * n)}
+    so = _SpOut()
+    for k, a in o.items():
+        setattr(so, k, a.ctypes.data_as(_up if a.dtype == np.uint32 else _dp))
+    if fn(C.byref(si), C.byref(so)) != 0:
+        raise RuntimeError("ref_sparse_ops: CSR capacity too small")
+    del keep
+    c = so.pA_count
+    res = {"spmv": o["spmv"].reshape(10, n, 3), "b": o["b"].reshape(n, 3), "pb": o["pb"].reshape(n, 3),
+           "diag_u": o["diag_u"].reshape(n, 3), "dot_u_pb": so.dot_u_pb, "len2_pb": so.len2_pb,
+           "pA_row_ptr": o["pA_row_ptr"], "pA_cols": o["pA_cols"][:c].copy(),
+           "pA_vals": o["pA_vals"][:9 * c].reshape(c, 9).copy(),
+           "cg_x": o["cg_x"].reshape(n, 3), "cg_iterations": so.cg_iterations, "cg_error": so.cg_error,
+           "be_x": o["be_x"].reshape(n, 3), "be_v": o["be_v"].reshape(n, 3), "be_iterations": so.be_iterations,
+           "be_error": so.be_error, "be_min_sub": so.be_min_sub, "be_max_sub": so.be_max_sub}
+    return res

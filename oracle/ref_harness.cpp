@@ -19,6 +19,7 @@
 #include <bounce_softbody/dynamics/time_step.h>
 #include <bounce_softbody/dynamics/contacts/sphere_shape_contact.h>
 #include <bounce_softbody/sparse/sparse_force_solver.h>
+#include <bounce_softbody/sparse/sparse_solver.h>
 #include <bounce_softbody/sparse/dense_vec3.h>
 #include <bounce_softbody/sparse/diag_mat33.h>
 #include <bounce_softbody/sparse/sparse_mat33.h>
@@ -668,6 +669,355 @@ int ref_ray_cast(const RefDesc* d, RefRun* run, uint32_t count, const double* se
 		}
 	delete body;
 	return 0;
+}
+
+// ---------------------------------------------------------------- sparse containers and solvers
+// Golden vectors for the container / solver boundary (b3SparseMat33, b3DenseVec3, b3DiagMat33,
+// b3SparseSolveCG, b3SparseSolveBE). Block values cross this boundary as 9 doubles per block in
+// b3Mat33 order (column-major: column x, then y, then z).
+
+struct RefJacobians
+{
+	uint32_t capacity;       // entries the COO arrays hold
+	uint32_t dfdx_count;     // entries written (one per nonzero block, in the matrix's row-list order)
+	uint32_t dfdv_count;
+	uint32_t* dfdx_rows;     // capacity
+	uint32_t* dfdx_cols;
+	double* dfdx_vals;       // 9 * capacity
+	uint32_t* dfdv_rows;
+	uint32_t* dfdv_cols;
+	double* dfdv_vals;
+	double* x;               // 3n: state the forces are evaluated at (x0 = x, v0 = v)
+	double* v;
+	double* f;               // 3n: internal forces
+	double* fe;              // 3n: external forces incl. m g (force_solver.cpp:116)
+	double* mass;            // n: M[i] = mass I (dynamic) or I (force_solver.cpp:113, 125)
+	int32_t* dynamic;        // n: S[i] = I (1) or 0 (0) (force_solver.cpp:119, 128)
+};
+
+static void put_block(double* out, const b3Mat33& a)
+{
+	out[0] = a.x.x; out[1] = a.x.y; out[2] = a.x.z;
+	out[3] = a.y.x; out[4] = a.y.y; out[5] = a.y.z;
+	out[6] = a.z.x; out[7] = a.z.y; out[8] = a.z.z;
+}
+
+static b3Mat33 get_block(const double* in)
+{
+	b3Mat33 a;
+	a.x = b3Vec3(scalar(in[0]), scalar(in[1]), scalar(in[2]));
+	a.y = b3Vec3(scalar(in[3]), scalar(in[4]), scalar(in[5]));
+	a.z = b3Vec3(scalar(in[6]), scalar(in[7]), scalar(in[8]));
+	return a;
+}
+
+// Steps the body run->steps harness steps, then evaluates the force model once at the resulting
+// state exactly as the first Newton iteration of the next step does (after UpdateContacts and
+// ClearForces, sparse_force_solver.cpp:137-161). Vertex indices are the input's, not the
+// reference's solver ids. Returns 0, or 1 if the COO arrays are too small.
+int ref_jacobians(const RefDesc* d, RefRun* run, RefJacobians* out)
+{
+	std::vector<b3Particle*> ps;
+	ShapeStore shapes;
+	b3Body* body = BuildBody(d, ps, shapes);
+	for (uint32_t s = 0; s < run->steps; ++s)
+		HarnessStep(body, scalar(run->dt), run->newton_iters, run->max_sub, scalar(run->sub_tol));
+
+	body->m_contactManager.UpdateContacts();
+	for (b3Force* f = body->m_forceList; f; f = f->m_next) f->ClearForces();
+	std::vector<b3Particle*> particles;
+	std::vector<b3Force*> forces;
+	std::vector<b3SphereAndShapeContact*> contacts;
+	for (b3Particle* p = body->m_particleList; p; p = p->m_next)
+	{
+		p->m_solverId = (uint32)particles.size();
+		particles.push_back(p);
+	}
+	for (b3Force* f = body->m_forceList; f; f = f->m_next) forces.push_back(f);
+	for (b3SphereAndShapeContact* c = body->m_contactManager.m_contactList; c; c = c->m_next) contacts.push_back(c);
+	const uint32 n = (uint32)particles.size();
+	// solver id -> input index
+	std::vector<uint32_t> input_of(n);
+	for (uint32_t i = 0; i < d->n; ++i) input_of[ps[i]->m_solverId] = i;
+
+	b3DenseVec3 x(n), v(n), fi(n);
+	fi.SetZero();
+	b3SparseMat33 dfdx(n), dfdv(n);
+	const b3Vec3 g = body->m_gravity;
+	for (uint32 k = 0; k < n; ++k)
+	{
+		b3Particle* p = particles[k];
+		const uint32_t i = input_of[k];
+		x[k] = p->m_position;
+		v[k] = p->m_velocity;
+		b3Vec3 fe = p->m_force;
+		const bool dyn = p->m_type == e_dynamicParticle;
+		if (dyn) fe += p->m_mass * g;
+		out->fe[3 * i + 0] = fe.x; out->fe[3 * i + 1] = fe.y; out->fe[3 * i + 2] = fe.z;
+		out->mass[i] = dyn ? p->m_mass : 1.0;
+		out->dynamic[i] = dyn ? 1 : 0;
+		out->x[3 * i + 0] = x[k].x; out->x[3 * i + 1] = x[k].y; out->x[3 * i + 2] = x[k].z;
+		out->v[3 * i + 0] = v[k].x; out->v[3 * i + 1] = v[k].y; out->v[3 * i + 2] = v[k].z;
+	}
+	HarnessModel model;
+	model.particleCount = n;
+	model.particles = particles.data();
+	model.forceCount = (uint32)forces.size();
+	model.forces = forces.data();
+	model.contactCount = (uint32)contacts.size();
+	model.contacts = contacts.data();
+	b3SparseForceSolverData data;
+	data.h = scalar(run->dt);
+	data.inv_h = scalar(1) / scalar(run->dt);
+	data.x = &x;
+	data.v = &v;
+	data.f = &fi;
+	data.dfdx = &dfdx;
+	data.dfdv = &dfdv;
+	model.ApplyForces(&data);
+
+	for (uint32 k = 0; k < n; ++k)
+	{
+		const uint32_t i = input_of[k];
+		out->f[3 * i + 0] = fi[k].x; out->f[3 * i + 1] = fi[k].y; out->f[3 * i + 2] = fi[k].z;
+	}
+	int rc = 0;
+	auto dump = [&](const b3SparseMat33& m, uint32_t* rows, uint32_t* cols, double* vals, uint32_t* count) {
+		uint32_t c = 0;
+		for (uint32 r = 0; r < n; ++r)
+			for (b3RowEntry* e = m.rows[r].head; e; e = e->next)
+			{
+				if (c == out->capacity)
+				{
+					rc = 1;
+					continue;
+				}
+				rows[c] = input_of[r];
+				cols[c] = input_of[e->column];
+				put_block(vals + 9 * (size_t)c, e->value);
+				++c;
+			}
+		*count = c;
+	};
+	dump(dfdx, out->dfdx_rows, out->dfdx_cols, out->dfdx_vals, &out->dfdx_count);
+	dump(dfdv, out->dfdv_rows, out->dfdv_cols, out->dfdv_vals, &out->dfdv_count);
+	delete body;
+	return rc;
+}
+
+struct RefSparseIn
+{
+	uint32_t n;
+	double h;
+	uint32_t dfdx_count;
+	const uint32_t* dfdx_rows;
+	const uint32_t* dfdx_cols;
+	const double* dfdx_vals;
+	uint32_t dfdv_count;
+	const uint32_t* dfdv_rows;
+	const uint32_t* dfdv_cols;
+	const double* dfdv_vals;
+	const double* f;        // 3n
+	const double* x0;       // 3n; also the Newton iterate x of the first iteration
+	const double* v0;       // 3n; also v
+	const double* fe;       // 3n
+	const double* M;        // 9n
+	const double* S;        // 9n
+	const double* y;        // 3n
+	const double* z;        // 3n
+	const double* u;        // 3n test vector
+	const double* D;        // 9n test diagonal
+	double s;               // test scalar
+	uint32_t cg_max_iterations;
+	double cg_tolerance;
+	uint32_t capacity;      // entries the CSR output of pA holds
+};
+
+struct RefSparseOut
+{
+	// SpMV (b3Mul) of u with: A, pA, D dfdx, dfdx D, s dfdx, dfdx + dfdv, dfdx - dfdv, dfdx + D,
+	// D - dfdx (b3Sub(out, D, B) on a fresh out), 0 dfdx (b3Mul with s = 0 leaves out empty)
+	double* spmv;           // 10 * 3n
+	double* b;              // 3n right-hand side (sparse_force_solver.cpp:167)
+	double* pb;             // 3n
+	double* diag_u;         // 3n: D u (b3Mul(b3DenseVec3&, const b3DiagMat33&, const b3DenseVec3&))
+	double dot_u_pb;        // b3Dot(u, pb)
+	double len2_pb;         // b3LengthSquared(pb)
+	// pA as CSR, columns ascending within a row
+	uint32_t* pA_row_ptr;   // n + 1
+	uint32_t* pA_cols;      // capacity
+	double* pA_vals;        // 9 * capacity
+	uint32_t pA_count;
+	// b3SparseSolveCG(pA, pb) from x = 0
+	double* cg_x;           // 3n
+	uint32_t cg_iterations;
+	double cg_error;
+	// b3SparseSolveBE, one Newton iteration, with a force model that replays dfdx, dfdv and f
+	double* be_x;           // 3n
+	double* be_v;           // 3n
+	uint32_t be_iterations;
+	double be_error;
+	uint32_t be_min_sub, be_max_sub;
+};
+
+namespace {
+
+void load_coo(b3SparseMat33& m, uint32_t count, const uint32_t* rows, const uint32_t* cols, const double* vals)
+{
+	for (uint32_t k = 0; k < count; ++k) m(rows[k], cols[k]) += get_block(vals + 9 * (size_t)k);
+}
+
+void load_vec(b3DenseVec3& v, const double* p)
+{
+	for (uint32 i = 0; i < v.n; ++i) v[i] = V3(p + 3 * i);
+}
+
+void store_vec(double* p, const b3DenseVec3& v)
+{
+	for (uint32 i = 0; i < v.n; ++i)
+	{
+		p[3 * i + 0] = v[i].x; p[3 * i + 1] = v[i].y; p[3 * i + 2] = v[i].z;
+	}
+}
+
+struct ReplayModel : public b3SparseForceModel
+{
+	void ApplyForces(const b3SparseForceSolverData* data) override
+	{
+		load_coo(*data->dfdx, in->dfdx_count, in->dfdx_rows, in->dfdx_cols, in->dfdx_vals);
+		load_coo(*data->dfdv, in->dfdv_count, in->dfdv_rows, in->dfdv_cols, in->dfdv_vals);
+		for (uint32 i = 0; i < in->n; ++i) (*data->f)[i] += V3(in->f + 3 * i);
+	}
+	const RefSparseIn* in = nullptr;
+};
+
+} // namespace
+
+// The reference's own container operators, CG and backward-Euler solve on given matrices. Returns
+// 0, or 1 if the CSR output of pA is too small.
+int ref_sparse_ops(const RefSparseIn* in, RefSparseOut* out)
+{
+	const uint32 n = in->n;
+	const scalar h = scalar(in->h);
+	b3SparseMat33 dfdx(n), dfdv(n);
+	load_coo(dfdx, in->dfdx_count, in->dfdx_rows, in->dfdx_cols, in->dfdx_vals);
+	load_coo(dfdv, in->dfdv_count, in->dfdv_rows, in->dfdv_cols, in->dfdv_vals);
+	b3DenseVec3 fi(n), x0(n), v0(n), fe(n), y(n), z(n), u(n);
+	load_vec(fi, in->f);
+	load_vec(x0, in->x0);
+	load_vec(v0, in->v0);
+	load_vec(fe, in->fe);
+	load_vec(y, in->y);
+	load_vec(z, in->z);
+	load_vec(u, in->u);
+	b3DiagMat33 M(n), S(n), D(n);
+	for (uint32 i = 0; i < n; ++i)
+	{
+		M[i] = get_block(in->M + 9 * (size_t)i);
+		S[i] = get_block(in->S + 9 * (size_t)i);
+		D[i] = get_block(in->D + 9 * (size_t)i);
+	}
+	const b3DenseVec3& x = x0;
+	const b3DenseVec3& v = v0;
+
+	// sparse_force_solver.cpp:165-174
+	b3DiagMat33 ST(n);
+	b3Transpose(ST, S);
+	b3DiagMat33 I(n);
+	I.SetIdentity();
+	b3SparseMat33 A = M - h * dfdv - (h * h) * dfdx;
+	b3DenseVec3 b = M * (v0 - v) + h * (fe + fi) + h * dfdx * (x0 - x + h * v + y);
+	b3SparseMat33 pA = S * A * ST + I - S;
+	b3DenseVec3 pb = S * (b - A * z);
+
+	const size_t n3 = 3 * (size_t)n;
+	const scalar s = scalar(in->s);
+	store_vec(out->spmv + 0 * n3, A * u);
+	store_vec(out->spmv + 1 * n3, pA * u);
+	store_vec(out->spmv + 2 * n3, (D * dfdx) * u);
+	store_vec(out->spmv + 3 * n3, (dfdx * D) * u);
+	store_vec(out->spmv + 4 * n3, (s * dfdx) * u);
+	store_vec(out->spmv + 5 * n3, (dfdx + dfdv) * u);
+	store_vec(out->spmv + 6 * n3, (dfdx - dfdv) * u);
+	store_vec(out->spmv + 7 * n3, (dfdx + D) * u);
+	store_vec(out->spmv + 8 * n3, (D - dfdx) * u);
+	store_vec(out->spmv + 9 * n3, (scalar(0) * dfdx) * u);
+	store_vec(out->b, b);
+	store_vec(out->pb, pb);
+	store_vec(out->diag_u, D * u);
+	out->dot_u_pb = b3Dot(u, pb);
+	out->len2_pb = b3LengthSquared(pb);
+
+	int rc = 0;
+	uint32_t c = 0;
+	out->pA_row_ptr[0] = 0;
+	for (uint32 r = 0; r < n; ++r)
+	{
+		std::vector<std::pair<uint32, b3Mat33>> row;
+		for (b3RowEntry* e = pA.rows[r].head; e; e = e->next) row.push_back({e->column, e->value});
+		std::sort(row.begin(), row.end(), [](const std::pair<uint32, b3Mat33>& a, const std::pair<uint32, b3Mat33>& b) {
+			return a.first < b.first;
+		});
+		for (auto& e : row)
+		{
+			if (c == in->capacity)
+			{
+				rc = 1;
+				continue;
+			}
+			out->pA_cols[c] = e.first;
+			put_block(out->pA_vals + 9 * (size_t)c, e.second);
+			++c;
+		}
+		out->pA_row_ptr[r + 1] = c;
+	}
+	out->pA_count = c;
+
+	b3DenseVec3 xcg(n);
+	xcg.SetZero();
+	b3SolveCGInput ci;
+	ci.A = &pA;
+	ci.b = &pb;
+	ci.maxIterations = in->cg_max_iterations;
+	ci.tolerance = scalar(in->cg_tolerance);
+	b3SolveCGOutput co;
+	co.x = &xcg;
+	b3SparseSolveCG(&co, &ci);
+	store_vec(out->cg_x, xcg);
+	out->cg_iterations = co.iterations;
+	out->cg_error = co.error;
+
+	ReplayModel model;
+	model.in = in;
+	b3DenseVec3 xb(n), vb(n);
+	b3SolveBEInput bi;
+	bi.h = h;
+	bi.inv_h = scalar(1) / h;
+	bi.forceModel = &model;
+	bi.dofCount = n;
+	bi.x0 = &x0;
+	bi.v0 = &v0;
+	bi.fe = &fe;
+	bi.M = &M;
+	bi.y = &y;
+	bi.S = &S;
+	bi.z = &z;
+	bi.maxIterations = 1;
+	bi.maxSubIterations = in->cg_max_iterations;
+	bi.subTolerance = scalar(in->cg_tolerance);
+	b3SolveBEOutput bo;
+	bo.x = &xb;
+	bo.v = &vb;
+	bo.minSubIterations = B3_MAX_U32;
+	bo.maxSubIterations = 0;
+	b3SparseSolveBE(&bo, &bi);
+	store_vec(out->be_x, xb);
+	store_vec(out->be_v, vb);
+	out->be_iterations = bo.iterations;
+	out->be_error = bo.error;
+	out->be_min_sub = bo.minSubIterations;
+	out->be_max_sub = bo.maxSubIterations;
+	return rc;
 }
 
 int ref_scalar_size(void) { return (int)sizeof(scalar); }

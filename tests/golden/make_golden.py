@@ -6,6 +6,7 @@ tests need neither the reference nor the mesh generators to reproduce them) and 
 positions, velocities and PCG iteration counts after a number of steps.
 
 Run here, where the reference sources exist:  python tests/golden/make_golden.py [case ...]
+(cases: the names in CASES, "ray_casts", "sparse_tet10")
 """
 import copy
 import os
@@ -120,6 +121,70 @@ def make_rays():
     print("wrote ray_casts", {k: v.shape for k, v in out.items() if k.endswith("_seg")})
 
 
+def sparse_body():
+    """The 10^3 block of the single-body workload with stiffness damping 0.01 (so that dfdv carries
+    the full pattern, not only mass damping)."""
+    return meshes.tet_grid(10, 10, 10, spacing=0.1, jitter=0.01, seed=0, E=1e5, nu=0.3, density=1000.0,
+                           damping=0.01, pin="y0", kdamp=0.01, name="sparse_tet10")
+
+
+def make_sparse():
+    """sparse_tet10.npz: the reference's force model evaluated at the 10^3 block's state after 10
+    steps (f, dfdx, dfdv from its FP32 build), then the reference's own container operators
+    (b3Mul SpMV of ten matrix expressions, diag x dense, b3Dot, b3LengthSquared), the
+    backward-Euler system and its pre-filter (sparse_force_solver.cpp:165-174),
+    b3SparseSolveCG from x = 0 and one b3SparseSolveBE iteration driven by a force model that
+    replays f, dfdx and dfdv; by its FP32 build and by its FP64 build on the same (float-valued)
+    inputs."""
+    body = sparse_body()
+    steps, h = 10, 1.0 / 60.0
+    jac = oracle.ref_jacobians(body, steps, dt=h, bits=32)
+    n = body.n
+    f32 = lambda a: np.asarray(a, np.float32).astype(np.float64)  # noqa: E731
+    rng = np.random.default_rng(11)
+    eye = np.eye(3)
+    M = np.stack([m * eye for m in jac["mass"]]).transpose(0, 2, 1).reshape(n, 9)
+    S = np.stack([eye * dyn for dyn in jac["dynamic"]]).reshape(n, 9)
+    y = f32(rng.normal(scale=1e-4, size=(n, 3)))
+    z = f32(rng.normal(scale=1e-3, size=(n, 3)) * jac["dynamic"][:, None])
+    u = f32(rng.normal(size=(n, 3)))
+    D = f32(rng.normal(size=(n, 9)))
+    s = 0.75
+    out = {"n": np.array(n), "h": np.array(h), "steps": np.array(steps), "s": np.array(s),
+           "cg_max": np.array(200), "cg_tol": np.array(1e-5)}
+    for m in ("dfdx", "dfdv"):
+        out[f"{m}_rows"] = jac[f"{m}_rows"].astype(np.uint16)
+        out[f"{m}_cols"] = jac[f"{m}_cols"].astype(np.uint16)
+        out[f"{m}_vals"] = jac[f"{m}_vals"].astype(np.float32)
+    for k in ("x", "v", "f", "fe"):
+        out[k] = jac[k].astype(np.float32)
+    out["mass"] = jac["mass"].astype(np.float32)
+    out["dynamic"] = jac["dynamic"].astype(np.int8)
+    out.update(y=y.astype(np.float32), z=z.astype(np.float32), u=u.astype(np.float32), D=D.astype(np.float32))
+    for bits in (32, 64):
+        r = oracle.ref_sparse_ops(n, h, jac, M, S, y, z, u, D, s, 200, 1e-5, bits=bits)
+        t = np.float32 if bits == 32 else np.float64
+        out[f"ref{bits}_spmv"] = r["spmv"].astype(t)
+        for k in ("b", "pb", "diag_u", "cg_x", "be_x", "be_v"):
+            out[f"ref{bits}_{k}"] = r[k].astype(t)
+        for k in ("dot_u_pb", "len2_pb", "cg_iterations", "cg_error", "be_iterations", "be_error", "be_min_sub",
+                  "be_max_sub"):
+            out[f"ref{bits}_{k}"] = np.array(r[k])
+        if bits == 32:
+            # pA's pattern and its diagonal blocks (the full matrix is checked through its products)
+            rp, cols = r["pA_row_ptr"], r["pA_cols"]
+            out["ref32_pA_row_ptr"] = rp.astype(np.uint32)
+            out["ref32_pA_cols"] = cols.astype(np.uint16)
+            diag = np.zeros((n, 9))
+            for i in range(n):
+                k = rp[i] + int(np.nonzero(cols[rp[i]:rp[i + 1]] == i)[0][0])
+                diag[i] = r["pA_vals"][k]
+            out["ref32_pA_diag"] = diag.astype(np.float32)
+    np.savez_compressed(os.path.join(HERE, "sparse_tet10.npz"), **out)
+    print("wrote sparse_tet10", {k: v.shape for k, v in out.items() if k.endswith("_vals")},
+          "cg iterations", int(out["ref32_cg_iterations"]), int(out["ref64_cg_iterations"]))
+
+
 def main():
     if not oracle.build_ref():
         raise SystemExit("the reference harness could not be built (reference sources absent)")
@@ -160,6 +225,8 @@ def main():
         print("wrote", name, {k: v.shape for k, v in out.items() if k.startswith("ref64_x")})
     if not only or "ray_casts" in only:
         make_rays()
+    if not only or "sparse_tet10" in only:
+        make_sparse()
 
 
 if __name__ == "__main__":

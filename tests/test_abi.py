@@ -1,5 +1,5 @@
-"""The C-ABI library: every entry point declared in include/b3g.h is exported and bound, and the
-library fails loudly (an error code, no CPU fallback) when no GPU is usable."""
+"""The C-ABI library: every entry point declared in include/*.h (b3g.h, b3g_sparse.h) is exported
+and bound, and the library fails loudly (an error code, no CPU fallback) when no GPU is usable."""
 import ctypes as C
 import os
 import re
@@ -7,13 +7,15 @@ import re
 import pytest
 from conftest import ROOT, gpu_available
 
-from bounce_softbody_gb300 import b3g
+from bounce_softbody_gb300 import b3g, b3g_sparse
 
 HEADER = os.path.join(ROOT, "include", "b3g.h")
+HEADERS = [os.path.join(ROOT, "include", h) for h in sorted(os.listdir(os.path.join(ROOT, "include")))
+           if h.endswith(".h")]
 
 
 def declared():
-    text = open(HEADER).read()
+    text = "".join(open(h).read() for h in HEADERS)
     return sorted(set(re.findall(r"B3G_API\s+[\w\s\*]+?\b(b3g_\w+)\s*\(", text)))
 
 
@@ -26,7 +28,7 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_binding_covers_the_header():
-    assert sorted(b3g.SIGNATURES) == declared()
+    assert sorted(set(b3g.SIGNATURES) | set(b3g_sparse.SIGNATURES)) == declared()
 
 
 def test_solver_config_defaults_are_the_references():
@@ -54,7 +56,16 @@ def test_null_arguments_are_rejected():
 # ctypes mirror -> C struct of include/b3g.h
 MIRRORS = {"WorldShapeC": "b3g_world_shape", "RayHit": "b3g_ray_hit", "BodyDescC": "b3g_body_desc",
            "SolverConfig": "b3g_solver_config", "StepStats": "b3g_step_stats",
-           "RequestResult": "b3g_request_result", "ServerStats": "b3g_server_stats"}
+           "RequestResult": "b3g_request_result", "ServerStats": "b3g_server_stats",
+           "b3g_sparse.SolveCGInput": "b3g_solve_cg_input", "b3g_sparse.SolveCGOutput": "b3g_solve_cg_output",
+           "b3g_sparse.ForceSolverData": "b3g_sparse_force_solver_data",
+           "b3g_sparse.ForceModelC": "b3g_sparse_force_model", "b3g_sparse.SolveBEInput": "b3g_solve_be_input",
+           "b3g_sparse.SolveBEOutput": "b3g_solve_be_output"}
+
+
+def mirror(name):
+    mod, _, cls = name.rpartition(".")
+    return getattr(b3g_sparse if mod == "b3g_sparse" else b3g, cls)
 
 
 def test_struct_layouts_match_the_header(tmp_path):
@@ -62,10 +73,10 @@ def test_struct_layouts_match_the_header(tmp_path):
     header's struct (a host binding with a stale layout would pass garbage through the ABI)."""
     import subprocess
 
-    lines = ["#include <cstdio>", "#include <cstddef>", '#include "b3g.h"', "int main() {"]
+    lines = ["#include <cstdio>", "#include <cstddef>", '#include "b3g.h"', '#include "b3g_sparse.h"', "int main() {"]
     for py, c in MIRRORS.items():
         lines.append(f'std::printf("{py} size %zu\\n", sizeof({c}));')
-        for f, _ in getattr(b3g, py)._fields_:
+        for f, _ in mirror(py)._fields_:
             lines.append(f'std::printf("{py} {f} %zu\\n", offsetof({c}, {f}));')
     lines += ["return 0; }"]
     src = tmp_path / "layout.cpp"
@@ -77,7 +88,7 @@ def test_struct_layouts_match_the_header(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
     for line in filter(None, out):
         py, what, val = line.split()
-        cls = getattr(b3g, py)
+        cls = mirror(py)
         got = C.sizeof(cls) if what == "size" else getattr(cls, what).offset
         assert got == int(val), (py, what, got, int(val))
 
@@ -102,20 +113,14 @@ def test_enum_values_match_the_header():
 
 
 def test_integration_c_example_compiles_and_links(tmp_path):
-    """The C usage example of INTEGRATION.md, wrapped in a function that declares its inputs,
-    compiles as C against include/b3g.h and links against libb3g.so (it is not run: no GPU)."""
+    """The C usage example of the integration guide (tests/integration_example.c) compiles as C
+    against include/b3g.h and links against libb3g.so (it is not run: no GPU)."""
     import subprocess
 
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    block = re.search(r"```c\n(.*?)```", text, re.S).group(1)
-    src = tmp_path / "example.c"
-    src.write_text("#include <stdio.h>\n#include <stdint.h>\n" + block.replace('#include "b3g.h"', '#include "b3g.h"\n'
-                   "void example(uint32_t n, float* xyz, float* vel, const int32_t* types, const float* damp,\n"
-                   "             uint32_t T, const uint32_t* ids, const float* E, const float* nu, const float* rho) {", 1)
-                   + "}\n")
+    src = os.path.join(ROOT, "tests", "integration_example.c")
     lib = os.path.dirname(b3g.LIB_PATH)
     r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-Wno-unused-variable", "-c", "-I",
-                        os.path.join(ROOT, "include"), str(src), "-o", str(tmp_path / "example.o")],
+                        os.path.join(ROOT, "include"), src, "-o", str(tmp_path / "example.o")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     main = tmp_path / "main.c"
