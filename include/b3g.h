@@ -27,6 +27,9 @@
  *                              (include/bounce_softbody/dynamics/forces/tetrahedron_element_force.h:154)
  *   b3g_body_get_stats         b3_forceSolverIterations / Min / MaxSubIterations
  *                              (src/bounce_softbody/dynamics/force_solver.cpp:29-34)
+ * The sparse containers and the CG / backward-Euler solvers as calls of their own
+ * (b3SparseMat33, b3DenseVec3, b3DiagMat33, b3SparseSolveCG, b3SparseSolveBE with a force-model
+ * callback) are in b3g_sparse.h.
  */
 #ifndef B3G_H
 #define B3G_H

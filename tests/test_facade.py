@@ -114,3 +114,64 @@ def test_facade_cloth_forces_match_c_abi(tmp_path, ctx):
     assert int(pick[1]) == tri[0]
     assert abs(pick[2] - frac[0]) < 1e-5
     np.testing.assert_allclose(pick[3:], normal[0], atol=1e-4)
+
+
+# ---------------------------------------------------------------- the sparse layer (b3g_sparse.hpp)
+def build_sparse_demo(tmp_path):
+    exe = str(tmp_path / "sparse_demo")
+    r = subprocess.run(["g++", "-O2", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "sparse_demo.cpp"), "-L", LIBDIR, "-lb3g",
+                        f"-Wl,-rpath,{LIBDIR}", "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_sparse_facade_compiles_and_links(tmp_path):
+    build_sparse_demo(tmp_path)
+
+
+@pytest.mark.gpu
+def test_sparse_facade_matches_reference(tmp_path):
+    """The reference's own expressions (A = M - h dfdv - h^2 dfdx, pA = S A S^T + I - S, ...),
+    b3SparseSolveCG and b3SparseSolveBE with a C++ b3SparseForceModel, written against the façade,
+    against the reference's outputs in tests/golden/sparse_tet10.npz (tolerances of
+    tests/test_gpu_sparse.py)."""
+    z = np.load(os.path.join(ROOT, "tests", "golden", "sparse_tet10.npz"))
+    n = int(z["n"])
+    inp = tmp_path / "in.bin"
+    with open(inp, "wb") as f:
+        np.array([n], np.uint32).tofile(f)
+        np.array([float(z["h"])], np.float32).tofile(f)
+        for m in ("dfdx", "dfdv"):
+            np.array([len(z[f"{m}_rows"])], np.uint32).tofile(f)
+            z[f"{m}_rows"].astype(np.uint32).tofile(f)
+            z[f"{m}_cols"].astype(np.uint32).tofile(f)
+            z[f"{m}_vals"].astype(np.float32).tofile(f)
+        for k in ("f", "x", "v", "fe", "y", "z", "u"):
+            z[k].astype(np.float32).tofile(f)
+        z["mass"].astype(np.float32).tofile(f)
+        z["dynamic"].astype(np.int32).tofile(f)
+        np.array([int(z["cg_max"])], np.uint32).tofile(f)
+        np.array([float(z["cg_tol"])], np.float32).tofile(f)
+    out = tmp_path / "out.bin"
+    exe = build_sparse_demo(tmp_path)
+    r = subprocess.run([exe, str(inp), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    res = np.fromfile(out, np.float32)
+    vecs = res[:6 * 3 * n].reshape(6, n, 3)
+    its = res[6 * 3 * n:]
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(np.asarray(b, np.float64)))
+
+    assert rel(vecs[0], z["ref32_spmv"][0]) < 2e-5  # A u
+    assert rel(vecs[1], z["ref32_spmv"][1]) < 2e-5  # pA u
+    assert rel(vecs[2], z["ref32_pb"]) < 2e-5
+    floor = rel(z["ref32_cg_x"], z["ref64_cg_x"])
+    assert rel(vecs[3], z["ref64_cg_x"]) < max(1e-4, 20 * floor)
+    assert abs(its[0] - int(z["ref32_cg_iterations"])) <= 3
+    x64 = z["ref64_be_x"]
+    fx = np.linalg.norm(z["ref32_be_x"].astype(np.float64) - x64) / np.linalg.norm(x64 - z["x"])
+    assert np.linalg.norm(vecs[4] - x64) / np.linalg.norm(x64 - z["x"]) < max(1e-4, 20 * fx)
+    assert rel(vecs[5], z["ref64_be_v"]) < max(1e-3, 20 * rel(z["ref32_be_v"], z["ref64_be_v"]))
+    assert its[1] == 1 and abs(its[2] - int(z["ref32_be_max_sub"])) <= 3
