@@ -51,6 +51,9 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="batch", choices=["batch", "tet64", "cloth128", "tet10", "serve"])
     p.add_argument("--bodies", type=int, default=512)
+    p.add_argument("--split", action="store_true",
+                   help="several GPUs: one body list split over the ranks by device footprint (strong scaling) "
+                        "instead of a batch per rank (weak scaling)")
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "bf16"])
     p.add_argument("--no-extras", action="store_true", help="skip e2e, plain path and CPU baseline")
     p.add_argument("--path", default="plain", choices=["plain", "batch"],
@@ -117,10 +120,41 @@ def sum_over_ranks(pg, value: float, device=None) -> float:
 
 
 # ------------------------------------------------------------------ workload
-def workload(args, rank):
+def split_workload(descs, world, rank):
+    """This rank's share of one body list split over `world` GPUs by estimated device bytes
+    (b3g_body_desc_estimate_bytes, b3g_partition_bodies: host only, the same split on every rank).
+    Returns the indices of this rank's bodies and the estimated bytes of every rank."""
+    from bounce_softbody_gb300 import b3g
+
+    sizes = [b3g.estimate_bytes(d) for d in descs]
+    owner = b3g.partition(sizes, world)
+    mine = [k for k in range(len(descs)) if int(owner[k]) == rank]
+    per_rank = [int(sum(s for s, o in zip(sizes, owner) if int(o) == r)) for r in range(world)]
+    return mine, per_rank
+
+
+def gather_rank_stats(pg, stats: dict, world: int):
+    """Every rank's stats dict on every rank (host objects: gloo or NCCL)."""
+    if pg is None:
+        return [stats]
+    out = [None] * world
+    pg.all_gather_object(out, stats)
+    return out
+
+
+def workload(args, rank, world=1):
     from bounce_softbody_gb300 import meshes
 
-    if args.workload == "batch":
+    if args.workload == "batch" and args.split:
+        # one list for the whole job, the same on every rank; each rank keeps its share
+        descs = meshes.batch_bodies(args.bodies, seed=3)
+        mine, per_rank = split_workload(descs, world, rank)
+        descs = [descs[k] for k in mine]
+        cfg = {"workload": f"batch of {args.bodies} Kuhn tet blocks a,b,c~U{{4..40}} split over {world} GPUs by "
+                           f"device footprint", "bodies": args.bodies, "bodies_this_rank": len(descs),
+               "estimated_bytes_per_rank": per_rank, "E": "log-uniform 1e4..1e6", "poisson": "U[0.2,0.45]",
+               "h": "1/60", "pcg_tol": PCG_TOL, "pcg_max_iter": PCG_MAX}
+    elif args.workload == "batch":
         descs = meshes.batch_bodies(args.bodies, seed=3 + 1000 * rank)
         cfg = {"workload": f"batch of {args.bodies} Kuhn tet blocks a,b,c~U{{4..40}}", "bodies": args.bodies,
                "E": "log-uniform 1e4..1e6", "poisson": "U[0.2,0.45]", "h": "1/60", "pcg_tol": PCG_TOL,
@@ -286,7 +320,7 @@ def ours(args, world, rank, local, pg):
 
     from bounce_softbody_gb300 import b3g
 
-    descs, cfg = workload(args, rank)
+    descs, cfg = workload(args, rank, world)
     dt, mx = step_dt(args), pcg_max(args)
     prec = {"fp32": b3g.PRECISION_FP32, "fp64": b3g.PRECISION_FP64, "bf16": b3g.PRECISION_BF16}[args.precision]
     scfg = b3g.solver_config(max_pcg_iterations=mx, pcg_tolerance=PCG_TOL, precision=prec)
@@ -345,6 +379,8 @@ def ours(args, world, rank, local, pg):
     iters = [a - b for a, b in zip(after, before)]
     t_max = max_over_ranks(pg, total_ms / 1e3, local)
     value = sum_over_ranks(pg, nverts * args.steps, local) / t_max
+    rank_stats = gather_rank_stats(pg, {"rank": rank, "bodies": len(bodies), "vertices": nverts,
+                                        "ms_per_step": total_ms / args.steps}, world)
 
     # rooflines. Whole step: every kernel of the timed region. Persistent path: the PCG launch
     # (the dominant kernel, 78 % of a step) and the assembly launch, each timed live with CUDA
@@ -496,12 +532,15 @@ def ours(args, world, rank, local, pg):
             launches = (3 if has_elements else 2) * args.steps
     line = {"metric": METRIC, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "fp64": "f64", "bf16": "bf16+f32"}[args.precision],
+            "scaling": "strong" if args.split else "weak", "vs_baseline": None,
+            "dtype": {"fp32": "f32", "fp64": "f64", "bf16": "bf16+f32"}[args.precision],
             "data": "synthetic (seeded meshes)",
             "config": dict(cfg, vertices=nverts, l2="inputs larger than L2 (no flush needed)",
                            precision=args.precision, setup_s=round(setup_s, 2)),
             "p50_step_ms": statistics.median(step_ms), "p99_step_ms": float(np.percentile(step_ms, 99)),
             "roofline": roof, "clocks": clk, "gpu_launches": launches}
+    if world > 1:
+        line["ranks"] = rank_stats
     if sched:
         line["schedule"] = {k: sched[k] for k in ("cluster", "threshold", "cluster_bodies", "ctas", "autotuned")}
     line.update(extras)

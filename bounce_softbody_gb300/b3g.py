@@ -152,6 +152,8 @@ SIGNATURES = {
     "b3g_server_reset_stats": (C.c_int, [C.c_void_p]),
     "b3g_server_get_state": (C.c_int, [C.c_void_p, C.c_uint32, _fp, _fp]),
     "b3g_server_destroy": (C.c_int, [C.c_void_p]),
+    "b3g_body_desc_estimate_bytes": (C.c_int, [C.POINTER(BodyDescC), C.POINTER(C.c_uint64)]),
+    "b3g_partition_bodies": (C.c_int, [C.POINTER(C.c_uint64), C.c_uint32, C.c_uint32, _up]),
 }
 
 _lib = None
@@ -346,6 +348,24 @@ def _desc_struct(desc, masses=None):
         d.mouse_ids = u(ms)
         d.mouse_params = f(desc.mouse_params)
     return d, keep
+
+
+def estimate_bytes(desc) -> int:
+    """b3g_body_desc_estimate_bytes: device bytes of a body made from desc (host only)."""
+    d, keep = _desc_struct(desc)
+    out = C.c_uint64()
+    _check(load_library().b3g_body_desc_estimate_bytes(C.byref(d), C.byref(out)), "b3g_body_desc_estimate_bytes")
+    del keep
+    return int(out.value)
+
+
+def partition(sizes, ranks: int) -> np.ndarray:
+    """b3g_partition_bodies: the GPU of each body for a split of `sizes` (bytes) over `ranks`."""
+    b = np.ascontiguousarray(np.asarray(sizes, np.uint64).reshape(-1))
+    out = np.zeros(max(b.size, 1), np.uint32)
+    _check(load_library().b3g_partition_bodies(b.ctypes.data_as(C.POINTER(C.c_uint64)), b.size, ranks,
+                                               out.ctypes.data_as(_up)), "b3g_partition_bodies")
+    return out[:b.size]
 
 
 class Body:

@@ -21,7 +21,7 @@ LIB = os.path.join(OUT, "libb3g.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "kernels.cu", "batch.cu", "persistent.cu", "persistent_f32.cu", "persistent_f64.cu",
-           "persistent_bf16.cu", "server.cu", "sparse.cu", "pattern.cpp", "shapes.cpp", "forces.cpp"]
+           "persistent_bf16.cu", "server.cu", "sparse.cu", "pattern.cpp", "partition.cpp", "shapes.cpp", "forces.cpp"]
 
 
 def nvcc() -> str:

@@ -110,6 +110,9 @@ int check_config(const b3g_solver_config* c, bool per_body = false);
 void stats_from(const Scalars& sc, b3g_step_stats* st);
 int read_scalars(b3g_body* b, Scalars* out);
 
+// device bytes of a body made from d, estimated on the host (partition.cpp)
+uint64_t estimate_desc_bytes(const b3g_body_desc& d);
+
 cudaError_t op_accumulate(float* dst, const float* src, size_t count, cudaStream_t st);
 cudaError_t op_set_types(const DevBody& B, const int8_t* new_types, cudaStream_t st);
 

@@ -215,31 +215,9 @@ b3g_body_desc make_desc(const HostDesc& h)
 	return d;
 }
 
-// Device bytes of a body that has not been created yet, from its counts and the layout of the
-// body's arena and FP32 solver vectors (api.cu): about 15 matrix blocks per vertex for
-// tetrahedral meshes and 11 for cloth with bending springs, a quarter more for the padding of the
-// sliced layout and the interleaved contribution lists. Meant to be slightly high; once a body has
-// been created its exact size is used instead.
-uint64_t estimate_bytes(const HostDesc& h)
-{
-	const double n = h.n, nt = h.nt, ntr = h.ntr, ns = h.ns, nw = h.nw;
-	const double nbw = (double)h.nst + h.nsh, nms = h.nms;
-	const double npad = 32.0 * std::ceil(n / 32.0);
-	const double nnzb = (h.nt ? 15.0 * n : (h.ntr || h.ns || nbw ? 11.0 * n : n)) + 16 * nms;
-	const double slots = 1.25 * nnzb + 128.0;
-	double b = slots * (4 + 36 + 4 + 2 + 4 + 2);                                       // col, blocks, list heads
-	b += 1.4 * 4.0 * (16 * nt + 9 * ntr + 4 * ns + 4 * nt + 3 * ntr + 2 * ns);          // contribution lists
-	b += npad * (1 + 6 + 6) + n * (6 * 12 + 13 + 12);                                   // row lists, vertex state
-	b += nt * (16 + 36 + 16 + 16 + 64 + 48) + ntr * (16 + 24 + 16 + 144 + 4) + ns * 20;  // elements
-	b += 36 * (9 * ntr + ns) + 12 * (3 * ntr + ns);                                     // explicit blocks
-	b += nbw * (16 + 4 * kBwFloats + 36 * 9 + 12 * 3 + 1.4 * 4 * 12) +                  // cloth forces
-	     nms * (16 + 4 * kMouseFloats + 36 * 16 + 12 * 4 + 1.4 * 4 * 20);
-	b += nw * n * 18 + (nw ? 8 * n : 0);                                                // contacts
-	b += 160 * npad;                                                                    // FP32 solver vectors
-	for (const b3g_world_shape& w : h.shapes)                                           // mesh triangles, voxels
-		b += 4.0 * kMeshTriFloats * w.triangle_count + 4.0 * w.grid[0] * w.grid[1] * w.grid[2];
-	return (uint64_t)(1.15 * b) + (64u << 10);
-}
+// Device bytes of a body that has not been created yet (partition.cpp); once a body has been
+// created its exact size is used instead.
+uint64_t estimate_bytes(const HostDesc& h) { return estimate_desc_bytes(make_desc(h)); }
 
 constexpr int kServerCluster = 8;  // default team size of large bodies (B3G_SERVER_CLUSTER overrides)
 constexpr uint32_t kServerThreshold = 4096;

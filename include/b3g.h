@@ -297,6 +297,19 @@ B3G_API int b3g_batch_apply_forces(b3g_context* ctx, b3g_body* const* bodies, ui
 B3G_API int b3g_batch_get_state(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float* positions,
                                 float* velocities);
 
+/* ---------------------------------------------------------------- several GPUs
+ * Bodies never interact (b3Body::Step, src/bounce_softbody/dynamics/body.cpp:552-604, touches one
+ * body), so a body list spreads over GPUs with no exchange between them: one context per GPU,
+ * each stepping its share. No reference counterpart (the reference is single-threaded). Neither
+ * call needs a GPU. */
+/* Device bytes a body made from desc would take, estimated from its counts (slightly high by
+ * design; b3g_body_device_bytes gives the exact figure once the body exists). */
+B3G_API int b3g_body_desc_estimate_bytes(const b3g_body_desc* desc, uint64_t* bytes);
+/* Split `count` bodies of the given device bytes over `ranks` GPUs: largest first, each to the
+ * GPU with the fewest bytes so far (ties: lowest rank). rank_of[k] receives body k's GPU. The
+ * split is deterministic, so every rank computes the same one. */
+B3G_API int b3g_partition_bodies(const uint64_t* bytes, uint32_t count, uint32_t ranks, uint32_t* rank_of);
+
 /* Host <-> device state transfer (3 floats per vertex each; either pointer may be NULL). */
 B3G_API int b3g_body_get_state(b3g_body* body, float* positions, float* velocities);
 B3G_API int b3g_body_set_state(b3g_body* body, const float* positions, const float* velocities);

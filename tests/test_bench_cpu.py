@@ -1,9 +1,12 @@
 """bench.py's host side: the CPU reference arm prints one valid JSON line, alone and as rank 0 of
-a two-rank gloo job (the other rank exits without work)."""
+a two-rank gloo job (the other rank exits without work); the rank reductions; the split of one
+body list over ranks by device footprint and the per-rank stats gather on two gloo ranks."""
 import json
 import os
 import subprocess
 import sys
+
+import pytest
 
 from conftest import ROOT
 
@@ -70,3 +73,53 @@ def test_threaded_oracle_batch_equals_single_runs():
     for d, x, v, it in zip(descs, xs, vs, its):
         xr, vr, itr, _ = oracle.simulate(d, 3, kind="port", bits=32)
         assert np.array_equal(x, xr) and np.array_equal(v, vr) and np.array_equal(it, itr), d.name
+
+
+def test_split_over_two_ranks_gloo(tmp_path):
+    """bench.py --split on two gloo ranks: every rank computes the same footprint split of one body
+    list (host only), the shares are disjoint and cover the list, the estimated bytes per rank are
+    balanced to within the largest body, and the per-rank stats gather reaches every rank."""
+    code = r'''
+import os, sys
+sys.path.insert(0, %r)
+import torch.distributed as dist
+import bench
+from bounce_softbody_gb300 import b3g, meshes
+dist.init_process_group("gloo")
+r, w = dist.get_rank(), dist.get_world_size()
+descs = meshes.batch_bodies(24, lo=4, hi=14, seed=3)
+mine, per_rank = bench.split_workload(descs, w, r)
+shares = bench.gather_rank_stats(dist, {"rank": r, "bodies": mine, "per_rank": per_rank}, w)
+assert [s["rank"] for s in shares] == list(range(w))
+assert all(s["per_rank"] == per_rank for s in shares)          # the same split everywhere
+allb = sorted(k for s in shares for k in s["bodies"])
+assert allb == list(range(len(descs))), allb                     # disjoint and complete
+sizes = [b3g.estimate_bytes(d) for d in descs]
+assert sum(per_rank) == sum(sizes)
+assert max(per_rank) - min(per_rank) <= max(sizes)               # greedy bound
+for s in shares:
+    assert sum(sizes[k] for k in s["bodies"]) == per_rank[s["rank"]]
+class A: pass
+a = A(); a.workload, a.split, a.bodies = "batch", True, 24
+d2, cfg = bench.workload(a, r, w)
+assert cfg["bodies_this_rank"] == len(mine) and len(d2) == len(mine)
+dist.destroy_process_group()
+''' % ROOT
+    script = tmp_path / "split.py"
+    script.write_text(code)
+    r = run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+             "--master-addr", "127.0.0.1", "--master-port", "29533", str(script)])
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_partition_rule():
+    """b3g_partition_bodies: largest first to the least-loaded rank, ties to the lowest rank."""
+    from bounce_softbody_gb300 import b3g
+
+    owner = b3g.partition([5, 9, 3, 9, 1], 2)
+    # order 9(1), 9(3), 5(0), 3(2), 1(4): 1->0, 3->1, 0->0 (9 vs 9: rank 0), 2->1, 4->1
+    assert list(owner) == [0, 0, 1, 1, 1]
+    assert list(b3g.partition([7, 7, 7], 1)) == [0, 0, 0]
+    assert len(b3g.partition([], 4)) == 0
+    with pytest.raises(b3g.B3gError):
+        b3g.partition([1, 2], 0)
