@@ -60,7 +60,8 @@ def parse():
                    help="single-body workloads: the per-op kernels (plain) or the persistent kernel with one body")
     # serving (--workload serve): Poisson arrivals over a pool of bodies
     p.add_argument("--serve-rate", type=float, default=2000.0, help="requests per second")
-    p.add_argument("--serve-seconds", type=float, default=10.0, help="length of the arrival stream")
+    p.add_argument("--serve-seconds", type=float, default=60.0, help="length of the arrival stream")
+    p.add_argument("--no-serve", action="store_true", help="batch workload: skip the serving sub-run")
     p.add_argument("--serve-grace", type=float, default=5.0, help="seconds to keep serving after the stream")
     p.add_argument("--serve-pool", type=int, default=256, help="distinct bodies of the stream")
     p.add_argument("--serve-max-active", type=int, default=256, help="bodies per launch at most")
@@ -172,6 +173,11 @@ def workload(args, rank, world=1):
         cfg = {"workload": "10^3 Kuhn tet block", "bodies": 1, "h": "1/60", "pcg_tol": PCG_TOL,
                "pcg_max_iter": PCG_MAX}
     return descs, cfg
+
+
+def bf16_inner():
+    """Inner BF16 iterations per outer iteration of the per-op BF16 mode (the library's default)."""
+    return int(os.environ.get("B3G_BF16_INNER", "20"))
 
 
 def step_dt(args):
@@ -388,7 +394,14 @@ def ours(args, world, rank, local, pg):
     # extra steps run after the timed region.
     bs, vsz = {"fp32": (36, 4), "fp64": (72, 8), "bf16": (18, 4)}[args.precision]
     alg_asm = sum(args.steps * assembly_bytes(i) for i in infos)
-    alg_pcg = sum(it * iteration_bytes(i, vsz, bs) + args.steps * final_bytes(i) for i, it in zip(infos, iters))
+    if per_op and args.precision == "bf16":
+        # the per-op BF16 mode counts outer iterations of its flexible CG: each is BF16_INNER inner
+        # iterations with the bf16 blocks, one FP32 product with its update, and z.q_prev
+        m = bf16_inner()
+        alg_pcg = sum(it * (m * iteration_bytes(i, 4, 18) + iteration_bytes(i, 4, 36) + 32 * i["vertices"])
+                      + args.steps * final_bytes(i) for i, it in zip(infos, iters))
+    else:
+        alg_pcg = sum(it * iteration_bytes(i, vsz, bs) + args.steps * final_bytes(i) for i, it in zip(infos, iters))
     alg = alg_asm + alg_pcg
     achieved = alg / (total_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
@@ -508,8 +521,8 @@ def ours(args, world, rank, local, pg):
     # a 16-byte memset of the work counters that is not a kernel. Per-op path per step: begin,
     # one element kernel per element kind, assembly, then per PCG iteration the fused
     # direction/SpMV/dot kernel and the update kernel (launched in chunks of 8 iterations between
-    # convergence checks), the true-residual refresh when due (every iteration in bf16 mode), and
-    # the final update.
+    # convergence checks), the true-residual refresh when due, and the final update; in bf16 mode
+    # the outer iterations of the flexible CG instead (counted below).
     if per_op:
         i0 = infos[0]
         per_step = 1 + (1 if i0["tets"] else 0) + (1 if i0["tris"] else 0) + (1 if i0["springs"] else 0) + 1 + 1
@@ -517,9 +530,14 @@ def ours(args, world, rank, local, pg):
         refresh = scfg.refresh_period
         for it in iters:  # total over the timed steps; every step of a run takes about the same
             per = int(it) / max(args.steps, 1)
+            if args.precision == "bf16":
+                # per outer iteration: inner begin (2), 2 per inner iteration, z.q_prev (not on the
+                # first), direction / product, update, refresh check
+                outer = int(round(per))
+                launches += args.steps * (outer * (2 + 2 * bf16_inner() + 4) - 1)
+                continue
             launched = min(-(-int(round(per)) // 8) * 8, mx)
-            resid = launched if args.precision == "bf16" else (
-                sum(1 for j in range(launched) if refresh > 0 and j % refresh == 0))
+            resid = sum(1 for j in range(launched) if refresh > 0 and j % refresh == 0)
             launches += args.steps * (2 * launched + resid)
         roof["kernel"] = "per-op step: k_dir_spmv_dot (70 % of the kernel time) + k_update + refresh"
     else:
@@ -542,20 +560,32 @@ def ours(args, world, rank, local, pg):
     if world > 1:
         line["ranks"] = rank_stats
     if sched:
-        line["schedule"] = {k: sched[k] for k in ("cluster", "threshold", "cluster_bodies", "ctas", "autotuned")}
+        line["schedule"] = {k: sched[k] for k in ("cluster", "threshold", "cluster_bodies", "ctas", "autotuned", "order")}
+        line["schedule"]["candidates_timed"] = len(sched["candidates_ms"])
+        # the chosen schedule per size bucket: which team steps the bucket's bodies
+        edges = [0, 1024, 2048, 4096, 8192, 16384, 32768, 1 << 31]
+        iters_all = [b.stats()["pcg_iterations"] for b in bodies] if not per_op else []
+        buckets = []
+        for lo, hi in zip(edges[:-1], edges[1:]):
+            ks = [k for k, i in enumerate(infos) if lo <= i["vertices"] < hi]
+            if not ks:
+                continue
+            clustered = sched["threshold"] >= 0 and sched["cluster"] > 1 and lo >= sched["threshold"]
+            buckets.append({"vertices": f"[{lo},{hi})" if hi < (1 << 31) else f"[{lo},)", "bodies": len(ks),
+                            "team": f"cluster of {sched['cluster']} CTAs" if clustered else "one CTA",
+                            "mean_pcg_iterations": float(np.mean([iters_all[k] for k in ks])) if iters_all else None})
+        line["schedule"]["buckets"] = buckets
     line.update(extras)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     for b in bodies:
         b.close()
     ctx.close()
-    return 0
+    return line if rank == 0 else None
 
 
 # ------------------------------------------------------------------ serving
 def serve_arm(args, rank, local):
     """Continuous-batching server under a Poisson request stream; the same stream through the
-    plain one-body-at-a-time path on a bounded sample."""
+    plain one-body-at-a-time path on a bounded sample. Returns the line (rank 0)."""
     from bounce_softbody_gb300 import b3g, meshes
 
     pool = meshes.serving_bodies(args.serve_pool, seed=5 + 1000 * rank)
@@ -654,20 +684,33 @@ def serve_arm(args, rank, local):
             "p50_step_ms": st["step_ms_p50"], "p99_step_ms": st["step_ms_p99"],
             "launches": int(st["iterations"]), "gpu_busy_frac": st["gpu_seconds"] / st["wall_seconds"] if st["wall_seconds"] else None,
             "clocks": clk, "gpu_launches": int(st["iterations"]), "plain": plain}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    return 0
+    return line if rank == 0 else None
+
+
+SERVING_KEYS = ["config", "demand_vertex_steps_per_s", "requests", "request_latency_ms", "request_latency_per_step_ms",
+                "p50_step_ms", "p99_step_ms", "launches", "gpu_busy_frac", "clocks", "plain"]
 
 
 def main():
     args = parse()
     world, rank, local, pg = dist_setup(args)
+    rc = 0
     if args.impl == "ours" and args.workload == "serve":
-        rc = serve_arm(args, rank, local)
+        line = serve_arm(args, rank, local)
+        if line is not None:
+            print(json.dumps(line), flush=True)
     elif args.impl == "reference":
         rc = reference_arm(args, world, rank, pg)
     else:
-        rc = ours(args, world, rank, local, pg)
+        line = ours(args, world, rank, local, pg)
+        if line is not None and args.workload == "batch" and world == 1 and not args.no_serve and not args.no_extras:
+            # the serving workload (continuous batching under Poisson arrivals) on the same GPU,
+            # after the batch's bodies are released
+            srv = serve_arm(args, rank, local)
+            line["serving"] = {"metric": srv["metric"], "value": srv["value"], "unit": srv["unit"],
+                               **{k: srv[k] for k in SERVING_KEYS}}
+        if line is not None:
+            print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
     return rc

@@ -152,6 +152,9 @@ SIGNATURES = {
     "b3g_server_reset_stats": (C.c_int, [C.c_void_p]),
     "b3g_server_get_state": (C.c_int, [C.c_void_p, C.c_uint32, _fp, _fp]),
     "b3g_server_destroy": (C.c_int, [C.c_void_p]),
+    "b3g_body_contact_fixtures": (C.c_int, [C.c_void_p, _up]),
+    "b3g_body_get_contacts": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8), _fp, _fp]),
+    "b3g_body_set_contacts": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8), _fp, _fp]),
     "b3g_body_desc_estimate_bytes": (C.c_int, [C.POINTER(BodyDescC), C.POINTER(C.c_uint64)]),
     "b3g_partition_bodies": (C.c_int, [C.POINTER(C.c_uint64), C.c_uint32, C.c_uint32, _up]),
 }
@@ -457,6 +460,31 @@ class Body:
         _check(load_library().b3g_body_get_stats(self.handle, C.byref(st)), "b3g_body_get_stats")
         return st.as_dict()
 
+    def contacts(self) -> dict:
+        """b3g_body_get_contacts: per (vertex, fixture) exists, apply_friction, normal_force, normal."""
+        lib = load_library()
+        k = C.c_uint32()
+        _check(lib.b3g_body_contact_fixtures(self.handle, C.byref(k)), "b3g_body_contact_fixtures")
+        c = self.n * k.value
+        out = {"fixtures": k.value, "exists": np.zeros(c, np.uint8), "apply_friction": np.zeros(c, np.uint8),
+               "normal_force": np.zeros(c, np.float32), "normal": np.zeros((c, 3), np.float32)}
+        u8 = C.POINTER(C.c_uint8)
+        _check(lib.b3g_body_get_contacts(self.handle, out["exists"].ctypes.data_as(u8),
+                                         out["apply_friction"].ctypes.data_as(u8),
+                                         out["normal_force"].ctypes.data_as(_fp), out["normal"].ctypes.data_as(_fp)),
+               "b3g_body_get_contacts")
+        return out
+
+    def set_contacts(self, c: dict):
+        u8 = C.POINTER(C.c_uint8)
+        ex = np.ascontiguousarray(c["exists"], np.uint8)
+        ap = np.ascontiguousarray(c["apply_friction"], np.uint8)
+        nf = np.ascontiguousarray(c["normal_force"], np.float32)
+        nn = np.ascontiguousarray(c["normal"], np.float32)
+        _check(load_library().b3g_body_set_contacts(self.handle, ex.ctypes.data_as(u8), ap.ctypes.data_as(u8),
+                                                    nf.ctypes.data_as(_fp), nn.ctypes.data_as(_fp)),
+               "b3g_body_set_contacts")
+
     def close(self):
         if self.handle:
             load_library().b3g_body_destroy(self.handle)
@@ -493,13 +521,16 @@ def step_batch_noalloc(ctx: Context, bodies: Sequence[Body], dt: float, steps: i
 
 
 def batch_schedule(ctx: Context) -> dict:
-    buf = np.zeros(256, np.int32)
+    """b3g_batch_schedule: the schedule of the context's current batch and the autotuner's timings."""
+    buf = np.zeros(512, np.int32)
     _check(load_library().b3g_batch_schedule(ctx.handle, buf.ctypes.data_as(_ip), buf.size), "b3g_batch_schedule")
     n = int(buf[5])
-    cands = [(int(buf[6 + 2 * k]) // 1000000, int(buf[6 + 2 * k]) % 1000000, buf[7 + 2 * k] / 1000.0)
-             for k in range(min(n, (buf.size - 6) // 2))]
+    cands = [((int(buf[7 + 2 * k]) // 1000000) % 100, int(buf[7 + 2 * k]) % 1000000,
+              "lpt" if int(buf[7 + 2 * k]) >= 100000000 else "size", buf[8 + 2 * k] / 1000.0)
+             for k in range(min(n, (buf.size - 7) // 2))]
     return {"cluster": int(buf[0]), "threshold": int(buf[1]), "cluster_bodies": int(buf[2]),
-            "ctas": int(buf[3]), "autotuned": bool(buf[4]), "candidates_ms": cands}
+            "ctas": int(buf[3]), "autotuned": bool(buf[4]), "order": "lpt" if int(buf[6]) else "size",
+            "candidates_ms": cands}
 
 
 def batch_apply_forces(ctx: Context, bodies: Sequence[Body], forces_ptr: int):

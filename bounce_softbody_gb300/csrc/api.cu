@@ -240,6 +240,11 @@ int ensure_precision(b3g_body* b, int prec)
 	bytes += align_up(alo);
 	const size_t xff = prec == kP64 ? 0 : 8 * np * sizeof(float);  // float-float solution for refinement
 	bytes += align_up(xff);
+	// BF16: the flexible outer CG's workspace (7 vectors, inner scalars, outer scalars, partials)
+	const size_t fcg = prec == kPBF ? align_up(7 * 4 * np * vs) + align_up(sizeof(Scalars)) +
+	                                      align_up(sizeof(FcgScalars)) + align_up(2 * kMaxPartials * sizeof(double))
+	                                : 0;
+	bytes += fcg;
 	char* mem = nullptr;
 	cudaError_t e = cudaMalloc(&mem, bytes);
 	if (e != cudaSuccess) return cuda_fail(e, "allocating solver vectors");
@@ -263,6 +268,17 @@ int ensure_precision(b3g_body* b, int prec)
 	pb.alo = alo ? p : nullptr;
 	p += align_up(alo);
 	pb.xff = xff ? (float*)p : nullptr;
+	p += align_up(xff);
+	if (fcg)
+	{
+		for (int k = 0; k < 7; ++k) pb.fcg_vec[k] = p + k * 4 * np * vs;
+		p += align_up(7 * 4 * np * vs);
+		pb.fcg_inner = (Scalars*)p;
+		p += align_up(sizeof(Scalars));
+		pb.fcg = (FcgScalars*)p;
+		p += align_up(sizeof(FcgScalars));
+		pb.fcg_part = (double*)p;
+	}
 	return B3G_OK;
 }
 
@@ -714,6 +730,8 @@ static void release_body_memory(b3g_body* b)
 	if (b->filt) cudaFree(b->filt);
 	for (auto& g : b->chunk_graphs) cudaGraphExecDestroy(g.exec);
 	b->chunk_graphs.clear();
+	for (auto& g : b->fcg_graphs) cudaGraphExecDestroy(g.exec);
+	b->fcg_graphs.clear();
 	for (int k = 0; k < 3; ++k) b->prec[k] = PrecBuffers();
 	b->arena = nullptr;
 	b->ray_buf = nullptr;
@@ -800,6 +818,90 @@ static cudaError_t pcg_chunk(b3g_body* b, const DevBody& D, int prec, int precon
 	return cudaGraphLaunch(exec, st);
 }
 
+// Inner BF16 PCG iterations per outer iteration of the BF16 mode (B3G_BF16_INNER overrides).
+static int bf16_inner_iterations()
+{
+	static const int m = [] {
+		const char* e = std::getenv("B3G_BF16_INNER");
+		const int v = e ? std::atoi(e) : 0;
+		return v > 0 ? v : 20;
+	}();
+	return m;
+}
+
+// The BF16 mode's solve: a flexible CG on the FP32 blocks (float-float solution, the true residual
+// refreshed every refresh_period outer iterations) preconditioned by a fixed number of Jacobi-PCG
+// iterations with the BF16 blocks (from z = 0). The matrix is read mostly as BF16: per outer
+// iteration one FP32 product and bf16_inner_iterations() BF16 products. Unlike refining a BF16
+// PCG, this converges when the BF16 rounding of the matrix times its condition number exceeds
+// one: the outer iteration only needs the inner solve to be a fair approximation of A^-1.
+// max_pcg_iterations bounds the outer iterations; the step's PCG statistics count them.
+static cudaError_t run_bf16_fcg(b3g_body* b, const DevBody& D, const b3g_solver_config& cfg, cudaStream_t st)
+{
+	const PrecBuffers& pb = b->prec[kPBF];
+	DevBody Bin = D;
+	Bin.pb = D.r;  // the inner solve's right-hand side is the outer residual
+	Bin.py = pb.fcg_vec[0];
+	Bin.r = pb.fcg_vec[1];
+	Bin.s = pb.fcg_vec[2];
+	Bin.d = pb.fcg_vec[3];
+	Bin.d2 = pb.fcg_vec[4];
+	Bin.q = pb.fcg_vec[5];
+	Bin.xff = nullptr;
+	Bin.sc = pb.fcg_inner;
+	const int m = bf16_inner_iterations();
+	Scalars* hs = b->ctx->h_scalars;
+	// one outer iteration's launches: the inner solve, then the outer direction, product and update
+	auto launch = [&](int k) -> cudaError_t {
+		cudaError_t e = op_fcg_inner_begin(Bin, D.sc, m, 0.0, st);
+		for (int j = 0; j < m && e == cudaSuccess; ++j) e = op_fcg_inner_iteration(Bin, j, st);
+		// p and p_prev alternate between d and d2, q and q_prev between q and the workspace's
+		DevBody Bo = D;
+		if (k & 1) std::swap(Bo.d, Bo.d2);
+		float* qa = (float*)D.q;
+		float* qb = (float*)pb.fcg_vec[6];
+		Bo.q = (k & 1) ? qb : qa;
+		if (e == cudaSuccess) e = op_fcg_outer(Bo, (const float*)Bin.py, (k & 1) ? qa : qb, pb.fcg, pb.fcg_part, k, st);
+		return e;
+	};
+	// ... replayed as a CUDA graph per variant (first, odd, even), captured on first use; launched
+	// directly when the stream is being captured by the caller
+	auto run = [&](int k) -> cudaError_t {
+		const int variant = k == 0 ? 0 : ((k & 1) ? 1 : 2);
+		for (const auto& g : b->fcg_graphs)
+			if (g.variant == variant && g.inner == m && g.precond == D.precond) return cudaGraphLaunch(g.exec, st);
+		op_pcg_prime(Bin, kPBF);
+		op_pcg_prime(D, kP32);
+		cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+		cudaError_t e = cudaStreamIsCapturing(st, &cs);
+		if (e != cudaSuccess || cs != cudaStreamCaptureStatusNone ||
+		    cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+		{
+			cudaGetLastError();
+			return launch(k);
+		}
+		e = launch(k);
+		cudaGraph_t graph = nullptr;
+		const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+		if (e == cudaSuccess) e = ec;
+		cudaGraphExec_t exec = nullptr;
+		if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+		if (graph) cudaGraphDestroy(graph);
+		if (e != cudaSuccess) return e;
+		b->fcg_graphs.push_back({variant, m, D.precond, exec});
+		return cudaGraphLaunch(exec, st);
+	};
+	cudaError_t e = cudaSuccess;
+	for (int k = 0; k < (int)cfg.max_pcg_iterations && e == cudaSuccess; ++k)
+	{
+		e = run(k);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(&hs->done, &D.sc->done, sizeof(int), cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+		if (e == cudaSuccess && hs->done) break;
+	}
+	return e;
+}
+
 int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_step_stats* stats)
 {
 	if (!b) return fail(B3G_ERROR_INVALID_ARGUMENT, "null body");
@@ -859,7 +961,8 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 		// at once from every kernel)
 		const int quiet = std::max(0, b->pcg_chunks_hint - 1);
 		int chunks = 0;
-		for (int it = 0; it < (int)cfg.max_pcg_iterations && e == cudaSuccess; it += chunk)
+		if (prec == kPBF && e == cudaSuccess) e = run_bf16_fcg(b, D, cfg, st);
+		for (int it = 0; prec != kPBF && it < (int)cfg.max_pcg_iterations && e == cudaSuccess; it += chunk)
 		{
 			if (it + chunk <= (int)cfg.max_pcg_iterations)
 				e = pcg_chunk(b, D, prec, (int)cfg.preconditioner, it, (int)cfg.refresh_period, st);
@@ -987,6 +1090,56 @@ int b3g_body_set_rotations(b3g_body* b, const float* q)
 	cudaError_t e = cudaMemcpyAsync(b->d.tet_q, q, b->nt * sizeof(float4), cudaMemcpyHostToDevice, st);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
 	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "set_rotations");
+}
+
+int b3g_body_contact_fixtures(const b3g_body* b, uint32_t* fixtures)
+{
+	if (!b || !fixtures) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	*fixtures = b->d.contacts ? b->nw : 0u;
+	return B3G_OK;
+}
+
+// vertex-major per (vertex, fixture): exists, apply friction, accumulated normal force, normal
+int b3g_body_get_contacts(b3g_body* b, uint8_t* exists, uint8_t* apply_friction, float* normal_force, float* normals)
+{
+	if (!b) return fail(B3G_ERROR_INVALID_ARGUMENT, "null body");
+	if (!b->ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "the body's context was destroyed");
+	const size_t c = b->d.contacts ? (size_t)b->n * b->nw : 0;
+	if (!c) return B3G_OK;
+	cudaStream_t st = b->ctx->stream;
+	cudaError_t e = cudaSuccess;
+	if (exists) e = cudaMemcpyAsync(exists, b->d.c_exists, c, cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess && apply_friction) e = cudaMemcpyAsync(apply_friction, b->d.c_apply, c, cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess && normal_force)
+		e = cudaMemcpyAsync(normal_force, b->d.c_nf, c * sizeof(float), cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess && normals) e = cudaMemcpyAsync(normals, b->d.c_normal, 3 * c * sizeof(float), cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "get_contacts");
+}
+
+int b3g_body_set_contacts(b3g_body* b, const uint8_t* exists, const uint8_t* apply_friction, const float* normal_force,
+                          const float* normals)
+{
+	if (!b) return fail(B3G_ERROR_INVALID_ARGUMENT, "null body");
+	if (!b->ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "the body's context was destroyed");
+	const size_t c = b->d.contacts ? (size_t)b->n * b->nw : 0;
+	if (!c) return B3G_OK;
+	if (exists)
+		for (size_t k = 0; k < c; ++k)
+			if (exists[k] > 1) return fail(B3G_ERROR_INVALID_ARGUMENT, "exists[%zu] is %u (0 or 1)", k, exists[k]);
+	if (apply_friction)
+		for (size_t k = 0; k < c; ++k)
+			if (apply_friction[k] > 1)
+				return fail(B3G_ERROR_INVALID_ARGUMENT, "apply_friction[%zu] is %u (0 or 1)", k, apply_friction[k]);
+	cudaStream_t st = b->ctx->stream;
+	cudaError_t e = cudaSuccess;
+	if (exists) e = cudaMemcpyAsync(b->d.c_exists, exists, c, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess && apply_friction) e = cudaMemcpyAsync(b->d.c_apply, apply_friction, c, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess && normal_force)
+		e = cudaMemcpyAsync(b->d.c_nf, normal_force, c * sizeof(float), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess && normals) e = cudaMemcpyAsync(b->d.c_normal, normals, 3 * c * sizeof(float), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "set_contacts");
 }
 
 int b3g_body_ray_cast(b3g_body* b, const float* segments, uint32_t count, b3g_ray_hit* hits)

@@ -57,6 +57,13 @@ struct PrecBuffers
 	void* minv = nullptr;
 	void* alo = nullptr;
 	float* xff = nullptr;  // float-float solution (FP32 and BF16 modes), 8 floats per vertex
+	// BF16 mode of the per-op step (flexible outer CG around inner BF16 PCG solves): the inner
+	// solution z, the inner r s d d2 q, the outer q of the previous iteration (7 vectors, 4-wide),
+	// the inner solve's scalars, the outer's extra scalars and their reduction partials
+	void* fcg_vec[7] = {};
+	Scalars* fcg_inner = nullptr;
+	FcgScalars* fcg = nullptr;
+	double* fcg_part = nullptr;
 };
 
 } // namespace b3g
@@ -92,6 +99,14 @@ struct b3g_body
 		cudaGraphExec_t exec;
 	};
 	std::vector<ChunkGraph> chunk_graphs;
+	// the BF16 mode's outer iterations captured into CUDA graphs: variant 0 = the first outer
+	// iteration, 1 / 2 = later odd / even ones (buffers alternate), for `inner` inner iterations
+	struct FcgGraph
+	{
+		int variant, inner, precond;
+		cudaGraphExec_t exec;
+	};
+	std::vector<FcgGraph> fcg_graphs;
 	int pcg_chunks_hint = 0;  // chunks the previous step's first solve launched
 };
 

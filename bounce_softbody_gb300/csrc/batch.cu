@@ -10,6 +10,7 @@
 #include "api_internal.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <mutex>
 #include <cstdlib>
@@ -31,9 +32,11 @@ struct BatchCache
 	std::vector<b3g_body*> bodies;
 	int prec = 0, precond = 0;
 	DevBody* d_bodies = nullptr;
-	int* d_order = nullptr;      // all bodies sorted by size, descending
+	int* d_order = nullptr;      // cluster-stepped bodies, then the others, each longest first
 	unsigned* d_queue = nullptr;
 	std::vector<int> order;
+	std::vector<int> iters;      // PCG iterations of each body's last step (0 = not known yet)
+	int lpt = 0;                 // queues ordered by estimated solve time (1) or by size (0)
 	int cluster = 1;
 	int threshold = 1 << 30;
 	int nbig = 0;
@@ -48,6 +51,7 @@ struct BatchCache
 	unsigned long long* d_prof = nullptr;          // phase cycle counters when B3G_PHASE_PROFILE=1
 	unsigned* d_flat_off = nullptr;                 // flat numbering: element offsets, then slice offsets
 	unsigned nelem = 0, nslices = 0;
+	int tets_only = 0;   // every body: tetrahedra only, no contact spheres
 };
 
 namespace {
@@ -96,24 +100,73 @@ BatchArgs make_args(BatchCache* c, float h, int steps, const b3g_solver_config& 
 	A.nelem = c->nelem;
 	A.nslices = c->nslices;
 	A.nbodies = (int)c->bodies.size();
+	A.tets_only = c->tets_only;
 	return A;
 }
 
-void set_schedule(BatchCache* c, int cluster, int threshold, int sms)
+// Estimated solve time of body k on a team of `warps` warps, in units of one warp's pass over one
+// slice: every PCG iteration is a sweep of ceil(slices / warps) passes plus about two passes'
+// worth of team barriers and reductions. Iteration counts come from a step already taken; before
+// one is known every body counts one iteration, so the order is by size.
+double est_time(const BatchCache* c, int k, int warps)
+{
+	const double slices = std::ceil((double)c->bodies[k]->n / kSlice);
+	const double it = c->iters.empty() || c->iters[k] <= 0 ? 1.0 : (double)c->iters[k];
+	return it * (2.0 + std::ceil(slices / warps));
+}
+
+// Bodies of at least `threshold` vertices are stepped by clusters of `cluster` CTAs, the others by
+// single CTAs. Each queue runs largest first, or with lpt longest estimated solve first
+// (longest-processing-time order), so that a small body with many PCG iterations does not start
+// last and trail the launch; the autotuner tries both.
+void set_schedule(BatchCache* c, int cluster, int threshold, int sms, cudaStream_t st, int lpt = 0)
 {
 	c->cluster = cluster;
 	c->threshold = threshold;
-	int nbig = 0;
-	if (cluster > 1)
-		for (int k : c->order)
-			if ((int)c->bodies[k]->n >= threshold) ++nbig;
-	c->nbig = nbig;
+	c->lpt = lpt;
+	constexpr int kCtaWarps = 8;  // warps of one CTA of the PCG launch
+	std::vector<int> big, small;
+	for (int k = 0; k < (int)c->bodies.size(); ++k)
+		((cluster > 1 && (int)c->bodies[k]->n >= threshold) ? big : small).push_back(k);
+	auto by_time = [&](std::vector<int>& v, int warps) {
+		std::vector<double> t(c->bodies.size());
+		for (int k : v) t[k] = lpt ? est_time(c, k, warps) : (double)c->bodies[k]->n;
+		std::stable_sort(v.begin(), v.end(), [&](int a, int b) {
+			if (t[a] != t[b]) return t[a] > t[b];
+			return c->bodies[a]->n > c->bodies[b]->n;
+		});
+	};
+	by_time(big, kCtaWarps * cluster);
+	by_time(small, kCtaWarps);
+	c->order = big;
+	c->order.insert(c->order.end(), small.begin(), small.end());
+	c->nbig = (int)big.size();
 	c->ctas = schedule_ctas(c->prec, cluster, sms);
+	if (!c->order.empty())
+		cudaMemcpyAsync(c->d_order, c->order.data(), c->order.size() * sizeof(int), cudaMemcpyHostToDevice, st);
 	if (c->graph)
 	{
 		cudaGraphExecDestroy(c->graph);
 		c->graph = nullptr;
 	}
+}
+
+// PCG iterations of every body's last step (the solver scalars on the device)
+int read_iters(b3g_context* ctx, BatchCache* c)
+{
+	cudaStream_t st = ctx->stream;
+	const uint32_t count = (uint32_t)c->bodies.size();
+	c->iters.assign(count, 0);
+	cudaError_t e = cudaSuccess;
+	for (uint32_t k0 = 0; k0 < count && e == cudaSuccess; k0 += 1024)
+	{
+		const uint32_t m = std::min<uint32_t>(1024, count - k0);
+		for (uint32_t k = 0; k < m && e == cudaSuccess; ++k)
+			e = cudaMemcpyAsync(ctx->h_scalars + k, c->bodies[k0 + k]->d.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+		for (uint32_t k = 0; k < m && e == cudaSuccess; ++k) c->iters[k0 + k] = ctx->h_scalars[k].iter;
+	}
+	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch iteration counts");
 }
 
 // the mutable per-body state a step changes
@@ -164,24 +217,44 @@ int autotune(b3g_context* ctx, BatchCache* c, float h, const b3g_solver_config& 
 
 	int maxn = 0;
 	for (b3g_body* b : c->bodies) maxn = std::max(maxn, (int)b->n);
-	std::vector<std::pair<int, int>> cands;
-	cands.push_back({1, 1 << 30});
-	const int thresholds[] = {4096, 8192, 16384, 32768};
+	// candidates: (cluster size, size threshold of cluster-stepped bodies, queue order)
+	struct Cand
+	{
+		int cl, thr, lpt;
+	};
+	std::vector<Cand> cands;
+	cands.push_back({1, 1 << 30, 0});
+	cands.push_back({1, 1 << 30, 1});
+	const int thresholds[] = {2048, 4096, 8192, 16384, 32768};
 	const int clusters[] = {2, 4, 8, 16};
 	for (int cl : clusters)
 		if (batch_max_clusters(c->prec, cl) > 0)  // 16-CTA clusters need hardware support
 			for (int t : thresholds)
-				if (t <= maxn) cands.push_back({cl, t});
+				if (t <= maxn)
+					for (int o = 0; o < 2; ++o) cands.push_back({cl, t, o});
 	cudaEvent_t e0, e1;
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
 	float best = 1e30f;
-	std::pair<int, int> best_c = {c->cluster, c->threshold};
+	Cand best_c = {c->cluster, c->threshold, c->lpt};
 	for (auto& cd : cands)
 	{
-		set_schedule(c, cd.first, cd.second, ctx->sm_count);
+		set_schedule(c, cd.cl, cd.thr, ctx->sm_count, st, cd.lpt);
 		BatchArgs A = make_args(c, h, 1, cfg);
 		e = run_once(c, A, st);  // warm-up
+		if (e == cudaSuccess && c->iters.empty())
+		{
+			// the first warm-up step gives every body's iteration count, which the estimated
+			// solve times of the lpt order use
+			int rc = read_iters(ctx, c);
+			if (rc != B3G_OK)
+			{
+				e = cudaErrorUnknown;
+				break;
+			}
+			set_schedule(c, cd.cl, cd.thr, ctx->sm_count, st, cd.lpt);
+			A = make_args(c, h, 1, cfg);
+		}
 		for (const Snapshot& s : L) cudaMemcpyAsync((void*)s.src, s.dst, s.bytes, cudaMemcpyDeviceToDevice, st);
 		cudaEventRecord(e0, st);
 		if (e == cudaSuccess) e = run_once(c, A, st);
@@ -191,7 +264,7 @@ int autotune(b3g_context* ctx, BatchCache* c, float h, const b3g_solver_config& 
 		if (e != cudaSuccess) break;
 		float ms = 0.0f;
 		cudaEventElapsedTime(&ms, e0, e1);
-		c->tune_log.push_back({cd.first * 1000000 + std::min(cd.second, 999999), (double)ms});
+		c->tune_log.push_back({cd.lpt * 100000000 + cd.cl * 1000000 + std::min(cd.thr, 999999), (double)ms});
 		if (ms < best)
 		{
 			best = ms;
@@ -203,7 +276,7 @@ int autotune(b3g_context* ctx, BatchCache* c, float h, const b3g_solver_config& 
 	cudaEventDestroy(e1);
 	cudaFree(store);
 	if (e != cudaSuccess) return cuda_fail(e, "batch autotune");
-	set_schedule(c, best_c.first, best_c.second, ctx->sm_count);
+	set_schedule(c, best_c.cl, best_c.thr, ctx->sm_count, st, best_c.lpt);
 	c->tuned = true;
 	return B3G_OK;
 }
@@ -234,6 +307,9 @@ int build_cache(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, int p
 	}
 	off[count] = (unsigned)ne;
 	off[2 * (size_t)count + 1] = (unsigned)nsl;
+	c->tets_only = 1;
+	for (uint32_t k = 0; k < count; ++k)
+		if (h[k].ntr || h[k].ns || h[k].nbw || h[k].nms || h[k].contacts) c->tets_only = 0;
 	if (e == cudaSuccess && count && ne < (1ull << 32) && nsl < (1ull << 32))
 	{
 		e = cudaMalloc(&c->d_flat_off, off.size() * sizeof(unsigned));
@@ -263,8 +339,8 @@ int build_cache(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, int p
 	// size heuristic: clusters of 4 for bodies of 16k vertices or more
 	int maxn = 0;
 	for (uint32_t k = 0; k < count; ++k) maxn = std::max(maxn, (int)bodies[k]->n);
-	if (maxn >= 16384) set_schedule(c, 4, 16384, ctx->sm_count);
-	else set_schedule(c, 1, 1 << 30, ctx->sm_count);
+	if (maxn >= 16384) set_schedule(c, 4, 16384, ctx->sm_count, ctx->stream);
+	else set_schedule(c, 1, 1 << 30, ctx->sm_count, ctx->stream);
 	*out = c;
 	return B3G_OK;
 }
@@ -350,10 +426,11 @@ extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_
 		if (rc != B3G_OK) return rc;
 		ctx->batch = c;
 		const char* env = std::getenv("B3G_AUTOTUNE");
-		const char* forced = std::getenv("B3G_BATCH_SCHEDULE");  // "cluster,threshold"
-		int fc = 0, ft = 0;
-		if (forced && std::sscanf(forced, "%d,%d", &fc, &ft) == 2 && (fc == 1 || fc == 2 || fc == 4 || fc == 8 || fc == 16))
-			set_schedule(c, fc, ft > 0 ? ft : (1 << 30), ctx->sm_count);
+		const char* forced = std::getenv("B3G_BATCH_SCHEDULE");  // "cluster,threshold[,lpt]"
+		int fc = 0, ft = 0, fo = 0;
+		if (forced && std::sscanf(forced, "%d,%d,%d", &fc, &ft, &fo) >= 2 &&
+		    (fc == 1 || fc == 2 || fc == 4 || fc == 8 || fc == 16))
+			set_schedule(c, fc, ft > 0 ? ft : (1 << 30), ctx->sm_count, ctx->stream, fo ? 1 : 0);
 		else if (!(env && env[0] == '0'))
 		{
 			rc = autotune(ctx, c, dt, cfg);
@@ -448,7 +525,7 @@ extern "C" int b3g_batch_schedule(b3g_context* ctx, int32_t* out, uint32_t capac
 	if (!ctx->batch) return fail(B3G_ERROR_INVALID_ARGUMENT, "no batch has been stepped on this context");
 	BatchCache* c = ctx->batch;
 	std::vector<int32_t> v = {c->cluster, c->threshold == (1 << 30) ? -1 : c->threshold, c->nbig, c->ctas,
-	                          c->tuned ? 1 : 0, (int32_t)c->tune_log.size()};
+	                          c->tuned ? 1 : 0, (int32_t)c->tune_log.size(), c->lpt};
 	for (auto& t : c->tune_log)
 	{
 		v.push_back(t.first);

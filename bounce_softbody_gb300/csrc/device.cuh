@@ -1151,7 +1151,9 @@ __device__ __forceinline__ bool filt_on(float4 f) { return f.x != 0.0f || f.y !=
 // (initial guess zero), r = pb, s = M^-1 r, d = s; returns this row's r.s. FILTER: filtered
 // contacts (B.filt) replace the penalty contacts: S_i = I - n n^T for a constrained vertex and
 // pb = S (b - A z), z nonzero in the first Newton iteration only.
-template <class TA, class TV, class L = LdPlain, bool FILTER = false>
+// TETS: the body has tetrahedra only and no contact spheres (no explicit blocks or vectors, no
+// contact terms), so those parts are compiled out: fewer registers, the same arithmetic.
+template <class TA, class TV, class L = LdPlain, bool FILTER = false, bool TETS = false>
 __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int lane, const StepParams& P,
                                                bool init_pcg)
 {
@@ -1180,7 +1182,7 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		diagExtra += h * damp * m;
 	}
 	float Kc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-	if (!FILTER && B.contacts)
+	if (!FILTER && !TETS && B.contacts)
 	{
 		const float r1 = B.srad[i];
 		for (int k = 0; k < B.nw; ++k)
@@ -1231,7 +1233,7 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	}
 	float3 bi = Mi * (v0 - vi) + h * (fe + fi);
 	// contact dfdx w term: h dfdx w = -h Kc w
-	bi = bi - h * mv9(Kc, wi);
+	if (!TETS) bi = bi - h * mv9(Kc, wi);
 	{
 		// tetrahedra's right-hand-side parts of this vertex, four in flight at a time
 		const uint32_t st = __ldg(B.vt_start + i);
@@ -1250,6 +1252,7 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		}
 		for (; t < cnt; ++t) bi = bi + ldl3<L>(B.tet_bc, __ldg(B.vt_list + st + kSlice * t));
 	}
+	if (!TETS)
 	{
 		const uint32_t st = __ldg(B.vb_start + i);
 		const int cnt = __ldg(B.vb_cnt + i);
@@ -1333,8 +1336,8 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 				add_tet_block(a, L::ld(B.tet_rec + r0 + ((code >> 2) & 3u)), L::ld(B.tet_rec + r0 + (code & 3u)));
 			}
 		}
-		const uint32_t bst = __ldg(B.blk_cstart + slot);
-		const int bcnt = __ldg(B.blk_ccnt + slot);
+		const uint32_t bst = TETS ? 0u : __ldg(B.blk_cstart + slot);
+		const int bcnt = TETS ? 0 : __ldg(B.blk_ccnt + slot);
 		for (int t = 0; t < bcnt; ++t)
 		{
 			uint32_t code = __ldg(B.blk_clist + bst + kSlice * t);
@@ -1388,8 +1391,9 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		{
 			if (!FILTER)
 			{
+				if (!TETS)
 #pragma unroll
-				for (int q = 0; q < 9; ++q) a[q] += h * h * Kc[q];
+					for (int q = 0; q < 9; ++q) a[q] += h * h * Kc[q];
 				a[0] += diagExtra;
 				a[4] += diagExtra;
 				a[8] += diagExtra;

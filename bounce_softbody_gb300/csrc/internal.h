@@ -69,6 +69,18 @@ struct Scalars
 	unsigned long long total_steps;
 };
 
+// Scalars of the flexible outer CG of the BF16 mode (per-op path): z.q_prev, p.r, p.q of this
+// iteration and of the previous one, and the arrival counter of its two-value reductions.
+struct FcgScalars
+{
+	double gamma;      // z . q_prev
+	double rho;        // p . r
+	double pq;         // p . q
+	double pq_prev;    // p_prev . q_prev
+	unsigned counter;
+	int pad;
+};
+
 // One static world shape (b3WorldFixture + b3Shape) on the device. Geometry is in world space
 // except where the shape keeps a frame (box, sdf: rotation q, translation t; mesh triangles are
 // stored transformed). lo / hi: the fixture's AABB as the reference computes it, for contact

@@ -558,6 +558,159 @@ __global__ void k_fill(float* p, size_t n, float v)
 	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
 }
 
+// ------------------------------------------------------------------ BF16 mode: flexible outer CG
+// Sum two values over the whole grid (like grid_reduce); true in thread 0 of the last CTA to
+// arrive, with the totals in *ta, *tb, summed in CTA order.
+__device__ bool grid_reduce2(double a, double b, double* partials, unsigned* counter, double* ta, double* tb)
+{
+	__shared__ double sa[32], sb[32];
+	__shared__ int last;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	a = warp_sum(a);
+	b = warp_sum(b);
+	if (lane == 0)
+	{
+		sa[warp] = a;
+		sb[warp] = b;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		double x = 0.0, y = 0.0;
+		for (int k = 0; k < nw; ++k)
+		{
+			x += sa[k];
+			y += sb[k];
+		}
+		partials[2 * blockIdx.x] = x;
+		partials[2 * blockIdx.x + 1] = y;
+		__threadfence();
+		unsigned prev = atomicAdd(counter, 1u);
+		last = (prev == gridDim.x - 1) ? 1 : 0;
+	}
+	__syncthreads();
+	if (!last) return false;
+	__threadfence();
+	double x = 0.0, y = 0.0;
+	for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x)
+	{
+		x += ((volatile double*)partials)[2 * k];
+		y += ((volatile double*)partials)[2 * k + 1];
+	}
+	x = warp_sum(x);
+	y = warp_sum(y);
+	__syncthreads();
+	if (lane == 0)
+	{
+		sa[warp] = x;
+		sb[warp] = y;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		double u = 0.0, v = 0.0;
+		for (int k = 0; k < nw; ++k)
+		{
+			u += sa[k];
+			v += sb[k];
+		}
+		*ta = u;
+		*tb = v;
+		*counter = 0u;
+	}
+	return threadIdx.x == 0;
+}
+
+// Start of an inner BF16 solve M_bf16 z = r from z = 0: r_in = r, s = M^-1 r, d = s, delta0. If
+// the outer solve is already done the inner one is marked done at once (every later launch of the
+// outer iteration returns immediately).
+__global__ void __launch_bounds__(kThreads) k_fcg_inner_init(DevBody B, const Scalars* outer)
+{
+	if (outer->done)
+	{
+		if (blockIdx.x == 0 && threadIdx.x == 0) B.sc->done = 1;
+		return;
+	}
+	double part = 0.0;
+	const float zero[3] = {0.0f, 0.0f, 0.0f};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
+	{
+		float r[3], sv[3];
+		vld<float, LdPlain>((const float*)B.pb, i, r);
+		precond_row<float>(B, i, r, sv);
+		vst((float*)B.r, i, r);
+		vst((float*)B.s, i, sv);
+		vst((float*)B.d, i, sv);
+		vst((float*)B.py, i, zero);
+		part += dot3<float>(r, sv);
+	}
+	double total;
+	if (grid_reduce(part, B.partials, &B.sc->counter, &total)) pcg_start(B.sc, total);
+}
+
+// gamma = z . q_prev (the flexible CG's orthogonalisation against the previous direction)
+__global__ void __launch_bounds__(kThreads) k_fcg_gamma(DevBody B, const float* z, const float* q_prev,
+                                                        FcgScalars* f, double* part)
+{
+	if (B.sc->done) return;
+	double a = 0.0;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n; i += gridDim.x * blockDim.x)
+	{
+		float zz[3], qq[3];
+		vld<float, LdPlain>(z, i, zz);
+		vld<float, LdPlain>(q_prev, i, qq);
+		a += dot3<float>(zz, qq);
+	}
+	double ta, tb;
+	if (grid_reduce2(a, 0.0, part, &f->counter, &ta, &tb)) f->gamma = ta;
+}
+
+// p = z + beta p_prev with beta = -gamma / (p_prev . q_prev) (p = z on the first iteration), formed
+// on the fly for every gathered column; q = A p with the FP32 blocks; p.q and p.r; alpha = p.r / p.q.
+// p_prev is B.d, p is written to B.d2, q to B.q.
+__global__ void __launch_bounds__(kThreads, B3G_SPMV_MIN_BLOCKS) k_fcg_dir_spmv(DevBody B, const float* z,
+                                                                              FcgScalars* f, double* part, int first)
+{
+	Scalars* sc = B.sc;
+	if (sc->done) return;
+	const int lane = threadIdx.x & 31;
+	const float beta = first ? 0.0f : (float)(-f->gamma / f->pq_prev);
+	double pq = 0.0, pr = 0.0;
+	for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < B.nslices; sl += (gridDim.x * blockDim.x) >> 5)
+	{
+		const int i = sl * kSlice + lane;
+		if (i >= B.n) continue;
+		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
+		float o[3], dn[3], r[3];
+		spmv_row_dir<float, float>(B.A32, B.col, B.nslots, base, w, lane, z, (const float*)B.d, beta, first != 0, o, dn);
+		vld<float, LdPlain>((const float*)B.r, i, r);
+		vst((float*)B.q, i, o);
+		vst((float*)B.d2, i, dn);
+		pq += dot3<float>(dn, o);
+		pr += dot3<float>(dn, r);
+	}
+	double tq, tr;
+	if (grid_reduce2(pq, pr, part, &f->counter, &tq, &tr))
+	{
+		f->pq_prev = tq;
+		f->pq = tq;
+		f->rho = tr;
+		sc->dq = tq;
+		if (!finite_d(tq) || !finite_d(tr))
+		{
+			sc->status = B3G_SOLVE_NONFINITE;
+			sc->done = 1;
+		}
+		else if (!(tq > 0.0))
+		{
+			sc->status = B3G_SOLVE_BREAKDOWN;
+			sc->done = 1;
+		}
+		else
+			sc->alpha = tr / tq;
+	}
+}
+
 StepParams dev_params(const StepParamsHost& P)
 {
 	StepParams p;
@@ -747,6 +900,37 @@ cudaError_t op_pcg_iteration(const DevBody& D, int prec, int j, int refresh, cud
 		k_update<float><<<gv, kThreads, 0, st>>>(B, 0);
 		if (resid) k_resid<float, float><<<gs, kThreads, 0, st>>>(B, B.A32, 0);
 	}
+	return cudaGetLastError();
+}
+
+cudaError_t op_fcg_inner_begin(const DevBody& Bin, const Scalars* outer_sc, int max_it, double tol2, cudaStream_t st)
+{
+	k_begin<<<1, 1, 0, st>>>(Bin.sc, max_it, tol2, 0, 0.0);
+	k_fcg_inner_init<<<vertex_grid(Bin), kThreads, 0, st>>>(Bin, outer_sc);
+	return cudaGetLastError();
+}
+
+cudaError_t op_fcg_inner_iteration(const DevBody& Din, int j, cudaStream_t st)
+{
+	// the inner iteration of the body step's PCG with the BF16 blocks: fused direction / SpMV /
+	// d.q, then x (= z) += alpha d, r -= alpha q, s = M^-1 r, r.s and the exit test; no refresh
+	DevBody B = Din;
+	if (j & 1) std::swap(B.d, B.d2);
+	cudaError_t e = launch_spmv<__nv_bfloat16, float>(B, (const __nv_bfloat16*)B.Alo, st);
+	if (e != cudaSuccess) return e;
+	k_update<float><<<vertex_grid(B), kThreads, 0, st>>>(B, 0);
+	return cudaGetLastError();
+}
+
+cudaError_t op_fcg_outer(const DevBody& Bo, const float* z, const float* q_prev, FcgScalars* f, double* part, int k,
+                         cudaStream_t st)
+{
+	if (k > 0) k_fcg_gamma<<<vertex_grid(Bo), kThreads, 0, st>>>(Bo, z, q_prev, f, part);
+	k_fcg_dir_spmv<<<spmv_grid<float, float>(Bo), kThreads, 0, st>>>(Bo, z, f, part, k == 0 ? 1 : 0);
+	// x += alpha p (float-float), r -= alpha q, s = M^-1 r, r.s and the exit test; the true residual
+	// r = b - A x (float-float) replaces the recursive one when the iteration is a refresh
+	k_update<float><<<vertex_grid(Bo), kThreads, 0, st>>>(Bo, 0);
+	k_resid<float, float><<<slice_grid(Bo), kThreads, 0, st>>>(Bo, Bo.A32, 0);
 	return cudaGetLastError();
 }
 

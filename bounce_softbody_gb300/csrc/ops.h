@@ -36,6 +36,18 @@ cudaError_t op_pcg_iteration(const DevBody& B, int prec, int j, int refresh, cud
 // once outside any stream capture.
 unsigned pcg_resid_mask(int prec, int j0, int count, int refresh);
 void op_pcg_prime(const DevBody& B, int prec);
+// BF16 mode of the per-op step: a flexible CG (Notay's FCG with one stored direction) on the FP32
+// blocks whose preconditioner is an inner Jacobi-PCG solve with the BF16 blocks.
+//   Bin: the inner solve's view (pb = the outer residual, py = z, its own r s d d2 q and scalars,
+//        no float-float solution); inner_begin starts it (max_it iterations, tolerance tol2) unless
+//        the outer solve is done (outer_sc), inner_iteration runs iteration j.
+//   Bo:  the outer view of outer iteration k (d = p_prev, d2 = p, q = q of this iteration), z the
+//        inner solution, q_prev the previous iteration's q: p = z - (z.q_prev / p_prev.q_prev)
+//        p_prev, q = A p, alpha = p.r / p.q, then the body step's update and true-residual refresh.
+cudaError_t op_fcg_inner_begin(const DevBody& Bin, const Scalars* outer_sc, int max_it, double tol2, cudaStream_t st);
+cudaError_t op_fcg_inner_iteration(const DevBody& Bin, int j, cudaStream_t st);
+cudaError_t op_fcg_outer(const DevBody& Bo, const float* z, const float* q_prev, FcgScalars* f, double* part, int k,
+                         cudaStream_t st);
 // mode 0: write the Newton iterate (xi, vi); mode 1: write the state and finish the step
 cudaError_t op_final(const DevBody& B, const StepParamsHost& P, int prec, int mode, cudaStream_t st);
 // finish a multi-Newton step: iterate -> state, friction, clear, new contacts
@@ -98,6 +110,7 @@ struct BatchArgs
 	unsigned nelem = 0;
 	unsigned nslices = 0;
 	int nbodies = 0;
+	int tets_only = 0;       // every body has tetrahedra only and no contact spheres
 };
 cudaError_t op_batch(const BatchArgs& A, cudaStream_t st);
 // Co-resident clusters of the batch kernel for this precision and cluster size (0 on error).

@@ -89,6 +89,7 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 	P.nelem = A.nelem;
 	P.nslices = A.nslices;
 	P.nbodies = A.nbodies;
+	P.tets_only = A.tets_only;
 	// a single Newton iteration with the flat numbering: elements and rows in two flat launches,
 	// then the PCG launch (which knows from `flat` to sum delta0 itself)
 	P.flat = (P.newton == 1 && A.elem_off && A.slice_off && A.nslices > 0) ? 1 : 0;

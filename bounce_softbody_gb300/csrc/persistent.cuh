@@ -52,6 +52,7 @@ struct BatchParams
 	unsigned nelem;
 	unsigned nslices;
 	int nbodies;
+	int tets_only;   // every body: tetrahedra only, no contact spheres (the row assembly's short form)
 };
 
 namespace {
@@ -709,8 +710,13 @@ __device__ __forceinline__ int flat_body(const unsigned* __restrict__ off, int n
 #endif
 constexpr int kRowsWarps = B3G_ROWS_THREADS / 32;
 
-template <class TA, class TV>
-__global__ void __launch_bounds__(B3G_ROWS_THREADS, B3G_ROWS_MIN_BLOCKS) k_batch_rows(BatchParams P)
+#ifndef B3G_ROWS_TETS_MIN_BLOCKS
+#define B3G_ROWS_TETS_MIN_BLOCKS 3  // the tetrahedra-only row assembly fits more CTAs per SM
+#endif
+
+template <class TA, class TV, bool TETS>
+__global__ void __launch_bounds__(B3G_ROWS_THREADS, TETS ? B3G_ROWS_TETS_MIN_BLOCKS : B3G_ROWS_MIN_BLOCKS)
+k_batch_rows(BatchParams P)
 {
 	const int lane = threadIdx.x & 31;
 	StepParams sp;
@@ -720,24 +726,31 @@ __global__ void __launch_bounds__(B3G_ROWS_THREADS, B3G_ROWS_MIN_BLOCKS) k_batch
 	for (unsigned g = blockIdx.x * kRowsWarps + (threadIdx.x >> 5); g < P.nslices; g += nw)
 	{
 		const int b = flat_body(P.slice_off, P.nbodies, g);
-		assemble_row<TA, TV, LdPlain>(P.bodies[b], (int)(g - __ldg(P.slice_off + b)), lane, sp, true);
+		assemble_row<TA, TV, LdPlain, false, TETS>(P.bodies[b], (int)(g - __ldg(P.slice_off + b)), lane, sp, true);
 	}
 }
 
-template <class TA, class TV>
-cudaError_t launch_rows(const BatchParams& P, cudaStream_t st)
+template <class TA, class TV, bool TETS>
+cudaError_t launch_rows_t(const BatchParams& P, cudaStream_t st)
 {
 	static const int resident = [] {
 		int dev = 0, sms = 0, per_sm = 0;
 		cudaGetDevice(&dev);
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_rows<TA, TV>, B3G_ROWS_THREADS, 0);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_rows<TA, TV, TETS>, B3G_ROWS_THREADS, 0);
 		return std::max(1, sms * std::max(per_sm, 1));
 	}();
 	const unsigned need = (P.nslices + kRowsWarps - 1) / kRowsWarps;
 	const int grid = (int)std::max(1u, std::min(need, (unsigned)resident));
-	k_batch_rows<TA, TV><<<grid, B3G_ROWS_THREADS, 0, st>>>(P);
+	k_batch_rows<TA, TV, TETS><<<grid, B3G_ROWS_THREADS, 0, st>>>(P);
 	return cudaGetLastError();
+}
+
+// the tetrahedra-only kernel when every body of the batch qualifies (P.tets_only)
+template <class TA, class TV>
+cudaError_t launch_rows(const BatchParams& P, cudaStream_t st)
+{
+	return P.tets_only ? launch_rows_t<TA, TV, true>(P, st) : launch_rows_t<TA, TV, false>(P, st);
 }
 
 template <class TA, class TV>

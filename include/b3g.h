@@ -274,7 +274,8 @@ B3G_API int b3g_step_batch_noalloc(b3g_context* ctx, b3g_body* const* bodies, ui
 
 /* Schedule of the context's current batch: cluster size, size threshold of cluster-stepped bodies
  * (-1 = none), bodies stepped by clusters, CTAs per launch, autotuned (0/1), number of timed
- * candidates, then (candidate code = cluster * 1e6 + threshold, microseconds) per candidate. */
+ * candidates, queue order (0: largest first, 1: longest estimated solve first), then per
+ * candidate (code = order * 1e8 + cluster * 1e6 + threshold, microseconds). */
 B3G_API int b3g_batch_schedule(b3g_context* ctx, int32_t* out, uint32_t capacity);
 
 /* Cycles spent per phase of the batch kernel, summed over CTAs (elements, assembly, SpMV, update,
@@ -322,6 +323,18 @@ B3G_API int b3g_body_set_types(b3g_body* body, const int32_t* types);
 /* Element rotations as quaternions (x, y, z, w), 4 floats per tetrahedron. */
 B3G_API int b3g_body_get_rotations(b3g_body* body, float* quaternions);
 B3G_API int b3g_body_set_rotations(b3g_body* body, const float* quaternions);
+/* Contact state between steps, for checkpoint / resume: the b3SphereAndShapeContact of each vertex
+ * sphere and world fixture (m_manifold's normal, m_normalForce, m_applyFriction and whether the
+ * contact exists; include/bounce_softbody/dynamics/contacts/sphere_shape_contact.h:50-52, created by
+ * b3ContactManager::FindNewContacts, src/bounce_softbody/dynamics/contacts/contact_manager.cpp:65-82).
+ * Arrays are vertex-major: entry v * fixtures + k for vertex v and fixture k (world spheres first,
+ * then world shapes); normals hold 3 floats per entry. fixtures is 0 for a body without vertex
+ * spheres. Any array may be NULL (not transferred). set_contacts takes flags of 0 or 1. */
+B3G_API int b3g_body_contact_fixtures(const b3g_body* body, uint32_t* fixtures);
+B3G_API int b3g_body_get_contacts(b3g_body* body, uint8_t* exists, uint8_t* apply_friction, float* normal_force,
+                                  float* normals);
+B3G_API int b3g_body_set_contacts(b3g_body* body, const uint8_t* exists, const uint8_t* apply_friction,
+                                  const float* normal_force, const float* normals);
 /* Lumped vertex masses as b3Body::ResetMass computed them (1 float per vertex). */
 B3G_API int b3g_body_get_masses(b3g_body* body, float* masses);
 /* Statistics of the body's last step (waits for it). */

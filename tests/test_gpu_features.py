@@ -386,3 +386,44 @@ def test_body_outliving_its_context_is_detached(ctx):
     with pytest.raises(b3g.B3gError, match="context was destroyed"):
         g.step(DT, b3g.solver_config())
     g.close()
+
+
+@pytest.mark.parametrize("scene", ["sphere", "capsule"])
+def test_contact_checkpoint_resumes_bitwise(ctx, scene):
+    """Checkpoint / resume of a cloth in contact through the C ABI: positions, velocities and the
+    contact state (b3g_body_get/set_contacts: exists, friction flag, normal force, normal per
+    vertex and fixture) restored into a fresh body continue bit for bit; without the contact state
+    the continuation differs (contacts created at the end of a step act in the next)."""
+    if scene == "sphere":
+        desc = meshes.cloth_grid(24, side=1.2, height=0.52, sphere_radius=0.5, contact_radius=0.05)
+    else:
+        desc = meshes.shape_scene("capsule", m=12, height=0.002)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    a = b3g.Body(ctx, desc)
+    for _ in range(4):
+        a.step(DT, cfg)
+    x, v = a.state()
+    c = a.contacts()
+    assert c["fixtures"] >= 1 and c["exists"].sum() > 0 and c["apply_friction"].sum() > 0
+    for _ in range(4):
+        a.step(DT, cfg)
+    xa, va = a.state()
+    b = b3g.Body(ctx, desc)
+    b.set_state(x, v)
+    b.set_contacts(c)
+    assert all(np.array_equal(b.contacts()[k], c[k]) for k in ("exists", "apply_friction", "normal_force", "normal"))
+    for _ in range(4):
+        b.step(DT, cfg)
+    xb, vb = b.state()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    d = b3g.Body(ctx, desc)  # state without the contacts
+    d.set_state(x, v)
+    for _ in range(4):
+        d.step(DT, cfg)
+    xd, _ = d.state()
+    assert not np.array_equal(xa, xd)
+    bad = dict(c, exists=np.full_like(c["exists"], 2))
+    with pytest.raises(b3g.B3gError):
+        d.set_contacts(bad)
+    for g in (a, b, d):
+        g.close()

@@ -8,8 +8,11 @@ and compared with the oracle's FP64 restatement of the reference step on the sam
   refinement the FP32 solve stalls near a relative residual of 5e-4, as the reference's own FP32
   build does (it runs to any iteration cap on this block).
 * BF16-stored blocks: the bf16 rounding of the matrix (2^-8 relative) times the condition
-  number of this system (about 3e3) exceeds one, so the FP32-refined BF16 solve cannot reach
-  1e-5; it reports max_iterations honestly and stays within 5e-3 of the oracle."""
+  number of this system (about 3e3) exceeds one, so refining a BF16 PCG cannot be relied on to
+  reach 1e-5. The BF16 mode therefore runs a flexible CG on the FP32 blocks (float-float
+  solution) whose preconditioner is a fixed number of Jacobi-PCG iterations with the BF16 blocks;
+  it converges to 1e-5 and agrees with the FP64 oracle to 1e-4, reading the matrix mostly as
+  BF16."""
 import numpy as np
 import pytest
 
@@ -44,8 +47,11 @@ def test_precision_variant_vs_fp64_oracle(ctx, block_and_oracle, name, precision
           f"position error {ex:.2e} of the displacement, velocity error {ev:.2e}")
     assert np.isfinite(x).all() and np.isfinite(v).all()
     if name == "bf16":
-        assert st["solve_status"] == "max_iterations"
-        assert ex <= 5e-3 and ev <= 5e-3
+        # outer iterations of the flexible CG (each with 20 inner BF16 iterations)
+        assert st["solve_status"] == "converged", st
+        assert st["residual_ratio"] <= 1e-5
+        assert st["pcg_iterations"] <= 60
+        assert ex <= 1e-4 and ev <= 1e-4
     else:
         assert st["solve_status"] == "converged"
         assert abs(st["pcg_iterations"] - oracle_iters) <= 0.1 * oracle_iters
