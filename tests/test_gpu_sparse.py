@@ -248,3 +248,72 @@ def test_queued_writes_apply_in_call_order(ctx):
         sp_op("mul_vec", u, a, u)  # out must not be the input
     with pytest.raises(b3g.B3gError):
         a.add_blocks([n], [0], np.zeros((1, 9)))  # row outside the matrix
+
+
+def test_edge_cases_and_errors(ctx):
+    """Empty containers, mismatched sizes, aliasing, the reference's b3Sub(out, D, B) and s = 0
+    quirks, a CG already converged, and a backward-Euler solve with a force model that writes
+    nothing (free particles under gravity in closed form)."""
+    # zero-sized containers work and do nothing
+    e0 = DenseVec3(ctx, 0)
+    m0 = SparseMat33(ctx, 0)
+    out0 = DenseVec3(ctx, 0)
+    sp_op("mul_vec", out0, m0, e0)
+    assert e0.dot(e0) == 0.0 and m0.size() == (0, 0)
+    # mismatched sizes are rejected
+    a, b = DenseVec3(ctx, 4), DenseVec3(ctx, 5)
+    with pytest.raises(b3g.B3gError):
+        vec_op("add", a, a, b)
+    with pytest.raises(b3g.B3gError):
+        a.dot(b)
+    # aliasing: out = a + out gives the sum
+    rng = np.random.default_rng(1)
+    va, vb = rng.normal(size=(4, 3)), rng.normal(size=(4, 3))
+    a.set(va)
+    c = DenseVec3(ctx, 4, vb)
+    vec_op("add", c, a, c)
+    np.testing.assert_allclose(c.get(), (va + vb).astype(np.float32), rtol=1e-6)
+    # b3Sub(out, D, B) keeps out's other blocks and sets its diagonal to D
+    n = 3
+    eye9 = np.eye(3, dtype=np.float32).reshape(9)
+    out = SparseMat33(ctx, n)
+    blk = rng.normal(size=9).astype(np.float32)
+    out.add_blocks([0], [2], blk[None])
+    B = SparseMat33(ctx, n)
+    bb = rng.normal(size=9).astype(np.float32)
+    B.add_blocks([1], [1], bb[None])
+    D = DiagMat33(ctx, n, np.tile(2.0 * eye9, (n, 1)))
+    sp_op("diag_sub", out, D, B)
+    np.testing.assert_array_equal(out.get_block(0, 2), blk)
+    np.testing.assert_allclose(out.get_block(1, 1), 2.0 * eye9 - bb, rtol=1e-6)
+    np.testing.assert_allclose(out.get_block(0, 0), 2.0 * eye9, rtol=1e-6)
+    # b3Mul(out, 0, B) leaves out as it was
+    before = out.export()
+    sp_op("scale", out, 0.0, B)
+    after = out.export()
+    assert all(np.array_equal(x, y) for x, y in zip(before, after))
+    # a CG whose right-hand side is zero stops at once
+    I = SparseMat33(ctx, n)
+    I.add_blocks(np.arange(n), np.arange(n), np.tile(eye9, (n, 1)))
+    zb, x = DenseVec3(ctx, n), DenseVec3(ctx, n)
+    res = solve_cg(I, zb, x, 10, 1e-5)
+    assert res["iterations"] == 0 and not np.any(x.get())
+    with pytest.raises(b3g.B3gError):
+        solve_cg(I, zb, zb, 10, 1e-5)     # x must not be b
+    with pytest.raises(b3g.B3gError):
+        solve_cg(I, zb, x, 10, 1.5)       # tolerance outside (0, 1)
+    # backward Euler with no internal forces: v = v0 + h g, x = x0 + h v (one PCG iteration)
+    m, h, grav = 2.0, 1.0 / 60.0, np.array([0.0, -9.8, 0.0])
+    x0 = DenseVec3(ctx, n, rng.normal(size=(n, 3)))
+    v0 = DenseVec3(ctx, n, rng.normal(size=(n, 3)))
+    fe = DenseVec3(ctx, n, np.tile(m * grav, (n, 1)))
+    M = DiagMat33(ctx, n, np.tile(m * eye9, (n, 1)))
+    S = DiagMat33(ctx, n, np.tile(eye9, (n, 1)))
+    y, z = DenseVec3(ctx, n), DenseVec3(ctx, n)
+    xo, vo = DenseVec3(ctx, n), DenseVec3(ctx, n)
+    out = solve_be(ctx, lambda data: None, h, x0, v0, fe, M, y, S, z, xo, vo, max_iterations=1,
+                   max_sub_iterations=20, sub_tolerance=1e-6)
+    v_exp = v0.get().astype(np.float64) + h * grav
+    np.testing.assert_allclose(vo.get(), v_exp, rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(xo.get(), x0.get().astype(np.float64) + h * v_exp, rtol=1e-6, atol=1e-7)
+    assert out["max_sub"] == 1 and out["status"] == "converged"
