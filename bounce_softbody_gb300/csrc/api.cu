@@ -307,12 +307,25 @@ int prec_of(const b3g_solver_config* c)
 	return kP32;
 }
 
-int check_config(const b3g_solver_config* c, bool per_body)
+// The per-vertex constraint buffer of filtered contacts, made on the first step in that mode.
+int ensure_filter(b3g_body* b)
+{
+	if (b->filt) return B3G_OK;
+	cudaError_t e = cudaMalloc(&b->filt, std::max<size_t>(1, (size_t)b->d.n) * sizeof(float4));
+	if (e != cudaSuccess)
+	{
+		b->filt = nullptr;
+		return cuda_fail(e, "filtered contacts");
+	}
+	return B3G_OK;
+}
+
+int check_config(const b3g_solver_config* c, bool filter_ok)
 {
 	if (c->contact_mode != B3G_CONTACT_PENALTY && c->contact_mode != B3G_CONTACT_FILTER)
 		return fail(B3G_ERROR_INVALID_ARGUMENT, "unknown contact mode %d", c->contact_mode);
-	if (c->contact_mode == B3G_CONTACT_FILTER && !per_body)
-		return fail(B3G_ERROR_UNSUPPORTED, "filtered contacts are stepped by b3g_body_step only");
+	if (c->contact_mode == B3G_CONTACT_FILTER && !filter_ok)
+		return fail(B3G_ERROR_UNSUPPORTED, "filtered contacts are stepped by b3g_body_step and b3g_step_batch only");
 	if (c->precision < 0 || c->precision > 2) return fail(B3G_ERROR_INVALID_ARGUMENT, "unknown precision %d", c->precision);
 	if (c->preconditioner < 0 || c->preconditioner > 1)
 		return fail(B3G_ERROR_INVALID_ARGUMENT, "unknown preconditioner %d", c->preconditioner);
@@ -932,15 +945,8 @@ int b3g_body_step(b3g_body* b, float dt, const b3g_solver_config* cfg_in, b3g_st
 	DevBody D = dev_for(b, prec, cfg.preconditioner, true);
 	if (cfg.contact_mode == B3G_CONTACT_FILTER && b->d.contacts)
 	{
-		if (!b->filt)
-		{
-			e = cudaMalloc(&b->filt, std::max<size_t>(1, (size_t)b->d.n) * sizeof(float4));
-			if (e != cudaSuccess)
-			{
-				b->filt = nullptr;
-				return cuda_fail(e, "filtered contacts");
-			}
-		}
+		rc = ensure_filter(b);
+		if (rc != B3G_OK) return rc;
 		D.filt = b->filt;
 	}
 	const int newton = (int)std::max<uint32_t>(1u, cfg.force_iterations);

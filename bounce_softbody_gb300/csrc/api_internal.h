@@ -120,8 +120,10 @@ int ensure_precision(b3g_body* b, int prec);
 // refine: the per-op path's iterative refinement (float-float solution and refresh residual)
 DevBody dev_for(const b3g_body* b, int prec, int precond, bool refine = false);
 int prec_of(const b3g_solver_config* c);
-// per_body: the caller is b3g_body_step (the only entry point with filtered contacts)
-int check_config(const b3g_solver_config* c, bool per_body = false);
+// filter_ok: the caller steps filtered contacts (b3g_body_step, b3g_step_batch)
+int check_config(const b3g_solver_config* c, bool filter_ok = false);
+// the per-vertex constraint buffer of filtered contacts (made on first use)
+int ensure_filter(b3g_body* b);
 void stats_from(const Scalars& sc, b3g_step_stats* st);
 int read_scalars(b3g_body* b, Scalars* out);
 

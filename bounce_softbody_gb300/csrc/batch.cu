@@ -52,6 +52,7 @@ struct BatchCache
 	unsigned* d_flat_off = nullptr;                 // flat numbering: element offsets, then slice offsets
 	unsigned nelem = 0, nslices = 0;
 	int tets_only = 0;   // every body: tetrahedra only, no contact spheres
+	int filter = 0;      // filtered contacts: bodies with contact spheres carry a constraint buffer
 };
 
 namespace {
@@ -101,6 +102,7 @@ BatchArgs make_args(BatchCache* c, float h, int steps, const b3g_solver_config& 
 	A.nslices = c->nslices;
 	A.nbodies = (int)c->bodies.size();
 	A.tets_only = c->tets_only;
+	A.filter = c->filter;
 	return A;
 }
 
@@ -281,14 +283,21 @@ int autotune(b3g_context* ctx, BatchCache* c, float h, const b3g_solver_config& 
 	return B3G_OK;
 }
 
-int build_cache(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, int prec, int precond, BatchCache** out)
+int build_cache(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, int prec, int precond, int filter,
+                BatchCache** out)
 {
 	BatchCache* c = new BatchCache();
 	c->bodies.assign(bodies, bodies + count);
 	c->prec = prec;
 	c->precond = precond;
 	std::vector<DevBody> h(count);
-	for (uint32_t k = 0; k < count; ++k) h[k] = dev_for(bodies[k], prec, precond);
+	for (uint32_t k = 0; k < count; ++k)
+	{
+		h[k] = dev_for(bodies[k], prec, precond);
+		// filtered contacts for the bodies with contact spheres (their buffers exist: b3g_step_batch)
+		h[k].filt = filter && bodies[k]->d.contacts ? bodies[k]->filt : nullptr;
+		if (h[k].filt) c->filter = 1;
+	}
 	c->order.resize(count);
 	std::iota(c->order.begin(), c->order.end(), 0);
 	std::stable_sort(c->order.begin(), c->order.end(), [&](int a, int b) { return bodies[a]->n > bodies[b]->n; });
@@ -302,14 +311,14 @@ int build_cache(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, int p
 	{
 		off[k] = (unsigned)ne;
 		off[count + 1 + k] = (unsigned)nsl;
-		ne += (uint64_t)h[k].nt + h[k].ntr + h[k].ns + h[k].nbw + h[k].nms;
+		ne += (uint64_t)h[k].nt + h[k].ntr + h[k].ns + h[k].nbw + h[k].nms + (h[k].filt ? (uint64_t)h[k].n : 0u);
 		nsl += (uint64_t)h[k].nslices;
 	}
 	off[count] = (unsigned)ne;
 	off[2 * (size_t)count + 1] = (unsigned)nsl;
 	c->tets_only = 1;
 	for (uint32_t k = 0; k < count; ++k)
-		if (h[k].ntr || h[k].ns || h[k].nbw || h[k].nms || h[k].contacts) c->tets_only = 0;
+		if (h[k].ntr || h[k].ns || h[k].nbw || h[k].nms || h[k].contacts || h[k].filt) c->tets_only = 0;
 	if (e == cudaSuccess && count && ne < (1ull << 32) && nsl < (1ull << 32))
 	{
 		e = cudaMalloc(&c->d_flat_off, off.size() * sizeof(unsigned));
@@ -388,8 +397,9 @@ extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_
 	b3g_solver_config cfg;
 	if (cfg_in) cfg = *cfg_in;
 	else b3g_solver_config_default(&cfg);
-	int rc = check_config(&cfg);
+	int rc = check_config(&cfg, true);
 	if (rc != B3G_OK) return rc;
+	const int filter = cfg.contact_mode == B3G_CONTACT_FILTER ? 1 : 0;
 	for (uint32_t k = 0; k < count; ++k)
 	{
 		if (!bodies[k]) return fail(B3G_ERROR_INVALID_ARGUMENT, "body %u is null", k);
@@ -411,18 +421,24 @@ extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_
 		return b3g_context_synchronize(ctx);
 	}
 	const int prec = prec_of(&cfg);
+	int want_filter = 0;
 	for (uint32_t k = 0; k < count; ++k)
 	{
 		rc = ensure_precision(bodies[k], prec);
+		if (rc == B3G_OK && filter && bodies[k]->d.contacts)
+		{
+			rc = ensure_filter(bodies[k]);
+			want_filter = 1;
+		}
 		if (rc != B3G_OK) return rc;
 	}
 	BatchCache* c = ctx->batch;
-	bool same = c && c->prec == prec && c->precond == cfg.preconditioner && c->bodies.size() == count &&
-	            std::equal(c->bodies.begin(), c->bodies.end(), bodies);
+	bool same = c && c->prec == prec && c->precond == cfg.preconditioner && c->filter == want_filter &&
+	            c->bodies.size() == count && std::equal(c->bodies.begin(), c->bodies.end(), bodies);
 	if (!same)
 	{
 		destroy_batch_cache(ctx);
-		rc = build_cache(ctx, bodies, count, prec, cfg.preconditioner, &c);
+		rc = build_cache(ctx, bodies, count, prec, cfg.preconditioner, filter, &c);
 		if (rc != B3G_OK) return rc;
 		ctx->batch = c;
 		const char* env = std::getenv("B3G_AUTOTUNE");

@@ -111,6 +111,8 @@ struct BatchArgs
 	unsigned nslices = 0;
 	int nbodies = 0;
 	int tets_only = 0;       // every body has tetrahedra only and no contact spheres
+	int filter = 0;          // filtered contacts: bodies with a filt buffer; their vertices follow
+	                         // their elements in the flat element numbering
 };
 cudaError_t op_batch(const BatchArgs& A, cudaStream_t st);
 // Co-resident clusters of the batch kernel for this precision and cluster size (0 on error).

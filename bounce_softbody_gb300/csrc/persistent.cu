@@ -8,7 +8,8 @@ namespace {
 constexpr int kElemThreads = 256;
 
 // The elements of every body of a batch (tetrahedra, triangles, springs, stretch / shear
-// triangles, mouse springs; first Newton iteration of a step), one per thread over a flat
+// triangles, mouse springs, then the vertices of bodies with filtered contacts; first Newton
+// iteration of a step), one per thread over a flat
 // numbering (elem_off: first element of each body). Its own launch runs at its own register
 // budget (3 CTAs per SM) instead of the 128 registers the row assembly needs: the tetrahedra's
 // rotation extraction, a dependent chain, wants the extra warps. The state it reads was written
@@ -41,8 +42,20 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_batch_elements(BatchParams 
 			continue;
 		}
 		e -= B.ns;
-		if (e < B.nbw) bw_element<LdPlain>(B, e, sp);
-		else mouse_element<LdPlain>(B, e - B.nbw, sp);
+		if (e < B.nbw)
+		{
+			bw_element<LdPlain>(B, e, sp);
+			continue;
+		}
+		e -= B.nbw;
+		if (e < B.nms)
+		{
+			mouse_element<LdPlain>(B, e, sp);
+			continue;
+		}
+		// filtered contacts: the body's vertices follow its elements in the numbering; the
+		// contact update and each vertex's constraint at the step's start (no element reads them)
+		contact_filter_vertex(B, e - B.nms, P.h);
 	}
 }
 
@@ -90,6 +103,7 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 	P.nslices = A.nslices;
 	P.nbodies = A.nbodies;
 	P.tets_only = A.tets_only;
+	P.filter = A.filter;
 	// a single Newton iteration with the flat numbering: elements and rows in two flat launches,
 	// then the PCG launch (which knows from `flat` to sum delta0 itself)
 	P.flat = (P.newton == 1 && A.elem_off && A.slice_off && A.nslices > 0) ? 1 : 0;

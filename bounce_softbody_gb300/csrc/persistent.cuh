@@ -53,6 +53,7 @@ struct BatchParams
 	unsigned nslices;
 	int nbodies;
 	int tets_only;   // every body: tetrahedra only, no contact spheres (the row assembly's short form)
+	int filter;      // filtered contacts: bodies with a constraint buffer (filt) are stepped in that mode
 };
 
 namespace {
@@ -247,6 +248,26 @@ __device__ __forceinline__ double spmv_lin_rows(const DevBody& B, const TA* A, c
 	return part;
 }
 
+// Filtered-contact forms of the row assembly and of the final update, out of line so that the
+// default forms inlined in the team kernels keep their register allocation.
+template <class TA, class TV, class LD>
+__device__ __noinline__ double assemble_row_filtered(const DevBody& B, int sl, int lane, const StepParams& sp,
+                                                     bool init)
+{
+	return assemble_row<TA, TV, LD, true>(B, sl, lane, sp, init);
+}
+
+__device__ __noinline__ void contact_filter_vertex_ool(const DevBody& B, int i, float h)
+{
+	contact_filter_vertex(B, i, h);
+}
+
+template <class TV, class LD>
+__device__ __noinline__ double final_vertex_filtered(const DevBody& B, int i, float h, bool first, bool finish)
+{
+	return final_vertex<TV, LD, true>(B, i, h, first, finish);
+}
+
 // Result of one PCG solve of a team.
 struct SolveOut
 {
@@ -369,6 +390,12 @@ __device__ double team_assemble(Team<CL>& T, const DevBody& B, const BatchParams
 	StepParams sp;
 	sp.h = P.h;
 	sp.first_newton = k == 0 ? 1 : 0;
+	if (k == 0 && B.filt)
+	{
+		// filtered contacts: the contact update and each vertex's constraint at the step's start
+		for (int i = T.tid(); i < B.n; i += T.nthreads()) contact_filter_vertex_ool(B, i, P.h);
+		T.sync();
+	}
 	for (int e = T.tid(); e < B.nt; e += T.nthreads()) tet_element<LD>(B, e, sp);
 	for (int e = T.tid(); e < B.ntr; e += T.nthreads()) tri_element<LD>(B, e, sp);
 	for (int e = T.tid(); e < B.ns; e += T.nthreads()) spring_element<LD>(B, e, sp);
@@ -378,7 +405,8 @@ __device__ double team_assemble(Team<CL>& T, const DevBody& B, const BatchParams
 	pc.tick(kPhElem);
 	double part = 0.0;
 	for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
-		part += assemble_row<TA, TV, LD>(B, sl, lane, sp, k == 0);
+		part += B.filt ? assemble_row_filtered<TA, TV, LD>(B, sl, lane, sp, k == 0)
+		               : assemble_row<TA, TV, LD>(B, sl, lane, sp, k == 0);
 	if (k > 0)
 	{
 		const TA* Asp = (sizeof(TA) == sizeof(float) && !bf16) ? (const TA*)B.A32 : (const TA*)B.Alo;
@@ -453,7 +481,9 @@ __device__ void team_step(Team<CL>& T, const DevBody& B, const BatchParams& P, b
 		for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
 		{
 			const int i = sl * kSlice + lane;
-			if (i < B.n) part += final_vertex<TV, LD>(B, i, h, k == 0, finish);
+			if (i < B.n)
+				part += B.filt ? final_vertex_filtered<TV, LD>(B, i, h, k == 0, finish)
+				               : final_vertex<TV, LD>(B, i, h, k == 0, finish);
 		}
 		err = T.reduce(part);
 		pc.tick(kPhFinal);
@@ -528,7 +558,8 @@ __device__ void team_step_solve(Team<CL>& T, const DevBody& B, const BatchParams
 	for (int sl = T.warp(); sl < B.nslices; sl += T.nwarps())
 	{
 		const int i = sl * kSlice + lane;
-		if (i < B.n) part += final_vertex<TV, LD>(B, i, P.h, true, true);
+		if (i < B.n)
+			part += B.filt ? final_vertex_filtered<TV, LD>(B, i, P.h, true, true) : final_vertex<TV, LD>(B, i, P.h, true, true);
 	}
 	const double err = T.reduce(part);
 	pc.tick(kPhFinal);
@@ -714,7 +745,8 @@ constexpr int kRowsWarps = B3G_ROWS_THREADS / 32;
 #define B3G_ROWS_TETS_MIN_BLOCKS 3  // the tetrahedra-only row assembly fits more CTAs per SM
 #endif
 
-template <class TA, class TV, bool TETS>
+// FILT: some bodies have filtered contacts (their filt buffer set); each body takes its own form
+template <class TA, class TV, bool TETS, bool FILT = false>
 __global__ void __launch_bounds__(B3G_ROWS_THREADS, TETS ? B3G_ROWS_TETS_MIN_BLOCKS : B3G_ROWS_MIN_BLOCKS)
 k_batch_rows(BatchParams P)
 {
@@ -726,31 +758,36 @@ k_batch_rows(BatchParams P)
 	for (unsigned g = blockIdx.x * kRowsWarps + (threadIdx.x >> 5); g < P.nslices; g += nw)
 	{
 		const int b = flat_body(P.slice_off, P.nbodies, g);
-		assemble_row<TA, TV, LdPlain, false, TETS>(P.bodies[b], (int)(g - __ldg(P.slice_off + b)), lane, sp, true);
+		const DevBody& B = P.bodies[b];
+		const int sl = (int)(g - __ldg(P.slice_off + b));
+		if (FILT && B.filt) assemble_row_filtered<TA, TV, LdPlain>(B, sl, lane, sp, true);
+		else assemble_row<TA, TV, LdPlain, false, TETS>(B, sl, lane, sp, true);
 	}
 }
 
-template <class TA, class TV, bool TETS>
+template <class TA, class TV, bool TETS, bool FILT>
 cudaError_t launch_rows_t(const BatchParams& P, cudaStream_t st)
 {
 	static const int resident = [] {
 		int dev = 0, sms = 0, per_sm = 0;
 		cudaGetDevice(&dev);
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_rows<TA, TV, TETS>, B3G_ROWS_THREADS, 0);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_rows<TA, TV, TETS, FILT>, B3G_ROWS_THREADS, 0);
 		return std::max(1, sms * std::max(per_sm, 1));
 	}();
 	const unsigned need = (P.nslices + kRowsWarps - 1) / kRowsWarps;
 	const int grid = (int)std::max(1u, std::min(need, (unsigned)resident));
-	k_batch_rows<TA, TV, TETS><<<grid, B3G_ROWS_THREADS, 0, st>>>(P);
+	k_batch_rows<TA, TV, TETS, FILT><<<grid, B3G_ROWS_THREADS, 0, st>>>(P);
 	return cudaGetLastError();
 }
 
-// the tetrahedra-only kernel when every body of the batch qualifies (P.tets_only)
+// the tetrahedra-only kernel when every body of the batch qualifies (P.tets_only), the kernel
+// with both row forms when some body has filtered contacts (P.filter)
 template <class TA, class TV>
 cudaError_t launch_rows(const BatchParams& P, cudaStream_t st)
 {
-	return P.tets_only ? launch_rows_t<TA, TV, true>(P, st) : launch_rows_t<TA, TV, false>(P, st);
+	if (P.filter) return launch_rows_t<TA, TV, false, true>(P, st);
+	return P.tets_only ? launch_rows_t<TA, TV, true, false>(P, st) : launch_rows_t<TA, TV, false, false>(P, st);
 }
 
 template <class TA, class TV>

@@ -91,7 +91,8 @@ typedef enum b3g_contact_mode
 	/* the reference's penalty spring and friction impulse
 	 * (sphere_shape_contact.cpp:53-189) */
 	B3G_CONTACT_PENALTY = 0,
-	/* opt-in extension, b3g_body_step only: an overlapping dynamic vertex is constrained along the
+	/* opt-in extension of b3g_body_step and b3g_step_batch (the server and the allocation-free
+	 * step refuse it): an overlapping dynamic vertex is constrained along the
 	 * contact normal n through the solver's pre-filter (S = I - n n^T, z = (vt - v.n) n in
 	 * pA = S A S^T + I - S, pb = S (b - A z), dv = y + z; sparse_force_solver.cpp:170-190), vt the
 	 * Baumgarte velocity min(0.2 C, 0.2) / h of the penalty force's depth C; inelastic and

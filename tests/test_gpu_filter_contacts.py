@@ -1,6 +1,6 @@
-"""Filtered contacts (B3G_CONTACT_FILTER, an opt-in extension of b3g_body_step) against the
-oracle's restatement of the same mode: overlapping dynamic vertices constrained along the
-contact normal through the solver's pre-filter instead of penalty springs."""
+"""Filtered contacts (B3G_CONTACT_FILTER, an opt-in extension of b3g_body_step and
+b3g_step_batch) against the oracle's restatement of the same mode: overlapping dynamic vertices
+constrained along the contact normal through the solver's pre-filter instead of penalty springs."""
 import numpy as np
 import pytest
 
@@ -73,15 +73,45 @@ def test_filter_mode_without_contact_spheres_is_the_default_path(ctx):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
-def test_filter_mode_is_refused_by_batched_entry_points(ctx):
+def test_filter_mode_is_refused_by_the_server_and_the_allocation_free_step(ctx):
     desc = meshes.block_on_floor(a=3, b=3, c=3)
     g = b3g.Body(ctx, desc)
-    with pytest.raises(b3g.B3gError, match="b3g_body_step only"):
-        b3g.step_batch(ctx, [g], DT, 1, filt_config())
-    with pytest.raises(b3g.B3gError, match="b3g_body_step only"):
+    with pytest.raises(b3g.B3gError, match="b3g_body_step and b3g_step_batch only"):
         b3g.Server(ctx, 1 << 28, 8, DT, config=filt_config())
+    with pytest.raises(b3g.B3gError, match="b3g_body_step and b3g_step_batch only"):
+        b3g.step_batch_noalloc(ctx, [g], DT, 1, filt_config())
     bad = b3g.solver_config()
     bad.contact_mode = 7
     with pytest.raises(b3g.B3gError, match="unknown contact mode"):
         g.step(DT, bad)
     g.close()
+
+
+@pytest.mark.parametrize("newton,precision", [(1, b3g.PRECISION_FP32), (3, b3g.PRECISION_FP64)])
+def test_batched_filtered_contacts_match_oracle(ctx, newton, precision):
+    """b3g_step_batch in the filtered mode: blocks on a flat and a tilted floor, batched with a body
+    without contact spheres (stepped in the default form), against the oracle's filtered mode.
+    One Newton iteration runs the flat element / row launches (the vertex constraints in the
+    element launch), several the whole-step team launch."""
+    descs = [meshes.block_on_floor(tilt=0.05), meshes.block_on_floor(a=4, b=3, c=4, tilt=0.0, seed=6),
+             meshes.tet_grid(5, 5, 5, seed=3, E=1e5, nu=0.3, pin="y0", name="free")]
+    steps = 20
+    cfg = filt_config(force_iterations=newton, precision=precision)
+    bodies = [b3g.Body(ctx, d) for d in descs]
+    st = b3g.step_batch(ctx, bodies, DT, steps, cfg)
+    for k, d in enumerate(descs):
+        x, v = bodies[k].state()
+        check_against_oracle(x, v, d, steps, newton_iters=newton)
+        assert st[k]["total_steps"] == steps
+    # the blocks rest on / slide along the floor instead of sinking through it
+    for k in (0, 1):
+        assert bodies[k].state()[0][:, 1].min() > -0.05
+    # the body without contact spheres steps exactly as in the default mode
+    plain = b3g.Body(ctx, descs[2])
+    b3g.step_batch(ctx, [plain], DT, steps, b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5,
+                                                               force_iterations=newton, precision=precision))
+    alone = b3g.Body(ctx, descs[2])
+    b3g.step_batch(ctx, [alone], DT, steps, cfg)
+    assert np.array_equal(plain.state()[0], alone.state()[0])
+    for b in bodies + [plain, alone]:
+        b.close()
