@@ -131,6 +131,8 @@ SIGNATURES = {
     "b3g_batch_launch_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int]),
     "b3g_batch_apply_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp]),
     "b3g_batch_get_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp, _fp]),
+    "b3g_batch_get_state_async": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp, _fp]),
+    "b3g_batch_wait_state": (C.c_int, [C.c_void_p]),
     "b3g_body_get_state": (C.c_int, [C.c_void_p, _fp, _fp]),
     "b3g_body_set_state": (C.c_int, [C.c_void_p, _fp, _fp]),
     "b3g_body_apply_forces": (C.c_int, [C.c_void_p, _fp]),
@@ -545,6 +547,18 @@ def batch_get_state(ctx: Context, bodies: Sequence[Body], x_ptr: int, v_ptr: int
     arr = (C.c_void_p * len(bodies))(*[b.handle for b in bodies])
     _check(load_library().b3g_batch_get_state(ctx.handle, arr, len(bodies), C.cast(x_ptr, _fp), C.cast(v_ptr, _fp)),
            "b3g_batch_get_state")
+
+
+def batch_get_state_async(ctx: Context, bodies: Sequence[Body], x_ptr: int, v_ptr: int):
+    """b3g_batch_get_state_async: the same copy on the context's second stream; the host arrays
+    are filled once batch_wait_state returns."""
+    arr = (C.c_void_p * len(bodies))(*[b.handle for b in bodies])
+    _check(load_library().b3g_batch_get_state_async(ctx.handle, arr, len(bodies), C.cast(x_ptr, _fp),
+                                                    C.cast(v_ptr, _fp)), "b3g_batch_get_state_async")
+
+
+def batch_wait_state(ctx: Context):
+    _check(load_library().b3g_batch_wait_state(ctx.handle), "b3g_batch_wait_state")
 
 
 def batch_set_launch_timing(ctx: Context, on: bool):

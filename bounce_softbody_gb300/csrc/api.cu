@@ -420,6 +420,11 @@ int b3g_context_destroy(b3g_context* c)
 		b->ctx = nullptr;
 	}
 	c->live_bodies.clear();
+	if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+	if (c->snap) cudaFree(c->snap);
+	if (c->ev_snap) cudaEventDestroy(c->ev_snap);
+	if (c->ev_copied) cudaEventDestroy(c->ev_copied);
+	if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
 	if (c->xfer) cudaFree(c->xfer);
 	if (c->xfer_table) cudaFree(c->xfer_table);
 	for (cudaEvent_t& e : c->tev)
@@ -441,6 +446,11 @@ int b3g_context_synchronize(b3g_context* c)
 {
 	if (!c) return fail(B3G_ERROR_INVALID_ARGUMENT, "null context");
 	cudaError_t e = cudaStreamSynchronize(c->stream);
+	if (e == cudaSuccess && c->copy_stream)
+	{
+		e = cudaStreamSynchronize(c->copy_stream);
+		c->copy_pending = false;
+	}
 	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "synchronize");
 }
 

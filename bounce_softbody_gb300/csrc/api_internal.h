@@ -40,6 +40,13 @@ struct b3g_context
 	// live bodies: destroying the context releases their device memory and detaches them, so a
 	// later b3g_body_destroy only frees the host object
 	std::vector<b3g_body*> live_bodies;
+	// asynchronous state reads (b3g_batch_get_state_async): a device snapshot of the bodies' x and
+	// v copied to the host on a second stream, so that the copy overlaps the next step
+	cudaStream_t copy_stream = nullptr;
+	cudaEvent_t ev_snap = nullptr, ev_copied = nullptr;
+	float* snap = nullptr;
+	size_t snap_cap = 0;                 // floats
+	bool copy_pending = false;
 	// containers of include/b3g_sparse.h made on this context (released with it), and the
 	// workspace of its solvers
 	std::vector<b3g::SparseObject*> live_sparse;

@@ -668,6 +668,63 @@ extern "C" int b3g_batch_get_state(b3g_context* ctx, b3g_body* const* bodies, ui
 	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch_get_state");
 }
 
+extern "C" int b3g_batch_get_state_async(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float* positions,
+                                         float* velocities)
+{
+	if (!ctx || (!bodies && count)) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	if (count == 0 || (!positions && !velocities)) return B3G_OK;
+	cudaSetDevice(ctx->device);
+	int rc = prepare_xfer(ctx, bodies, count, 2);
+	if (rc != B3G_OK) return rc;
+	cudaError_t e = cudaSuccess;
+	if (!ctx->copy_stream)
+	{
+		e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+		if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_snap, cudaEventDisableTiming);
+		if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_copied, cudaEventDisableTiming);
+		if (e != cudaSuccess) return cuda_fail(e, "batch_get_state_async streams");
+	}
+	const size_t need = 2 * ctx->xfer_total;
+	if (need > ctx->snap_cap)
+	{
+		e = cudaStreamSynchronize(ctx->copy_stream);  // the old snapshot may still be in flight
+		if (ctx->snap) cudaFree(ctx->snap);
+		ctx->snap = nullptr;
+		ctx->snap_cap = 0;
+		ctx->copy_pending = false;
+		if (e == cudaSuccess) e = cudaMalloc(&ctx->snap, need * sizeof(float));
+		if (e != cudaSuccess) return cuda_fail(e, "batch_get_state_async snapshot");
+		ctx->snap_cap = need;
+	}
+	cudaStream_t st = ctx->stream;
+	// the previous copy must have left the snapshot before the gather overwrites it
+	if (ctx->copy_pending) e = cudaStreamWaitEvent(st, ctx->ev_copied, 0);
+	float* sx = ctx->snap;
+	float* sv = ctx->snap + ctx->xfer_total;
+	const size_t bytes = ctx->xfer_total * sizeof(float);
+	if (e == cudaSuccess)
+		e = op_batch_gather(ctx->xfer_table, count, ctx->xfer_max_n3, positions ? sx : nullptr, velocities ? sv : nullptr, st);
+	if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_snap, st);
+	if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_snap, 0);
+	if (e == cudaSuccess && positions) e = cudaMemcpyAsync(positions, sx, bytes, cudaMemcpyDeviceToHost, ctx->copy_stream);
+	if (e == cudaSuccess && velocities) e = cudaMemcpyAsync(velocities, sv, bytes, cudaMemcpyDeviceToHost, ctx->copy_stream);
+	if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_copied, ctx->copy_stream);
+	if (e != cudaSuccess) return cuda_fail(e, "batch_get_state_async");
+	ctx->copy_pending = true;
+	return B3G_OK;
+}
+
+extern "C" int b3g_batch_wait_state(b3g_context* ctx)
+{
+	if (!ctx) return fail(B3G_ERROR_INVALID_ARGUMENT, "null context");
+	if (!ctx->copy_pending) return B3G_OK;
+	// later work on the context stream is ordered after the copy, and the host waits for it
+	cudaError_t e = cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0);
+	if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev_copied);
+	ctx->copy_pending = false;
+	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch_wait_state");
+}
+
 extern "C" int b3g_batch_phase_cycles(b3g_context* ctx, uint64_t out[8], int reset)
 {
 	if (!ctx || !out) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");

@@ -312,6 +312,17 @@ B3G_API int b3g_body_desc_estimate_bytes(const b3g_body_desc* desc, uint64_t* by
  * split is deterministic, so every rank computes the same one. */
 B3G_API int b3g_partition_bodies(const uint64_t* bytes, uint32_t count, uint32_t ranks, uint32_t* rank_of);
 
+/* b3g_batch_get_state without waiting (no reference counterpart): one launch snapshots every
+ * body's x and v on the device, and a second stream of the context copies the snapshot to the
+ * host arrays, so that the copy overlaps the work queued next (the next step). The arrays are
+ * filled once b3g_batch_wait_state (or b3g_context_synchronize) returns; they must stay valid
+ * and untouched until then. Page-locked arrays (cudaHostAlloc / cudaHostRegister) make the copy
+ * asynchronous; with pageable ones the call waits for it. A later call on the context reuses
+ * the snapshot only after the previous copy has left it. */
+B3G_API int b3g_batch_get_state_async(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float* positions,
+                                      float* velocities);
+B3G_API int b3g_batch_wait_state(b3g_context* ctx);
+
 /* Host <-> device state transfer (3 floats per vertex each; either pointer may be NULL). */
 B3G_API int b3g_body_get_state(b3g_body* body, float* positions, float* velocities);
 B3G_API int b3g_body_set_state(b3g_body* body, const float* positions, const float* velocities);

@@ -207,3 +207,37 @@ def test_mixed_batch_matches_oracle(ctx):
         fv = float(np.linalg.norm(v32 - v64) / max(np.linalg.norm(v64), 1e-30))
         assert np.linalg.norm(v - v64) <= max(1e-3, 20 * fv) * np.linalg.norm(v64), d.name
         g.close()
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_async_state_read_is_a_snapshot(ctx, pinned):
+    """b3g_batch_get_state_async: the host arrays receive the state at the call, even though the
+    next step is queued before the copy is waited for; they match b3g_batch_get_state."""
+    descs = small_batch(count=7, seed=21)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    bodies = [b3g.Body(ctx, d) for d in descs]
+    n3 = 3 * sum(d.n for d in descs)
+    if pinned:
+        torch = pytest.importorskip("torch")
+        xa = torch.zeros(n3, dtype=torch.float32).pin_memory()
+        va = torch.zeros(n3, dtype=torch.float32).pin_memory()
+        xp, vp = xa.data_ptr(), va.data_ptr()
+        get = lambda t: t.numpy().copy()  # noqa: E731
+    else:
+        xa, va = np.zeros(n3, np.float32), np.zeros(n3, np.float32)
+        xp, vp = xa.ctypes.data, va.ctypes.data
+        get = lambda a: a.copy()  # noqa: E731
+    b3g.step_batch(ctx, bodies, DT, 2, cfg, stats=False)
+    xs, vs = np.zeros(n3, np.float32), np.zeros(n3, np.float32)
+    b3g.batch_get_state(ctx, bodies, xs.ctypes.data, vs.ctypes.data)
+    b3g.batch_get_state_async(ctx, bodies, xp, vp)
+    b3g.step_batch(ctx, bodies, DT, 1, cfg, stats=False)  # queued behind the snapshot
+    b3g.batch_wait_state(ctx)
+    assert np.array_equal(get(xa), xs) and np.array_equal(get(va), vs)
+    # a second read after the step: the new state
+    b3g.batch_get_state_async(ctx, bodies, xp, vp)
+    b3g.batch_wait_state(ctx)
+    b3g.batch_get_state(ctx, bodies, xs.ctypes.data, vs.ctypes.data)
+    assert np.array_equal(get(xa), xs) and not np.array_equal(xs, np.zeros_like(xs))
+    for b in bodies:
+        b.close()
