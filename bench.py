@@ -432,7 +432,9 @@ def ours(args, world, rank, local, pg):
         if args.precision == "fp32":
             roof["traffic"] = PCG_TRAFFIC_RATIO * pcg_b
         roof["assembly_launch"] = {"achieved": asm_b / (asm_ms / 1e3) / 1e9, "frac": asm_b / (asm_ms / 1e3) / 1e9 / peak,
-                                   "algorithmic_bytes_per_launch": asm_b, "launch_ms": asm_ms}
+                                   "algorithmic_bytes_per_launch": asm_b, "launch_ms": asm_ms,
+                                   "element_launch_ms": lt["elements_ms"] / lt["steps"],
+                                   "row_launch_ms": (lt["assembly_ms"] - lt["elements_ms"]) / lt["steps"]}
     roof["whole_step"] = step_roof
     sched = b3g.batch_schedule(ctx) if not per_op else None
 

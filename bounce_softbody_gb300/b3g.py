@@ -129,6 +129,7 @@ SIGNATURES = {
     "b3g_batch_phase_cycles": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int]),
     "b3g_batch_set_launch_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "b3g_batch_launch_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int]),
+    "b3g_batch_element_launch_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "b3g_batch_apply_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp]),
     "b3g_batch_get_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp, _fp]),
     "b3g_batch_get_state_async": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp, _fp]),
@@ -566,10 +567,14 @@ def batch_set_launch_timing(ctx: Context, on: bool):
 
 
 def batch_launch_times(ctx: Context, reset: bool = True) -> dict:
-    """Accumulated device ms of the assembly and PCG launches of timed batched steps."""
+    """Accumulated device ms of the assembly and PCG launches of timed batched steps, and the
+    element launch's part of the assembly ms."""
+    lib = load_library()
+    el = C.c_double(0.0)
+    _check(lib.b3g_batch_element_launch_ms(ctx.handle, C.byref(el)), "b3g_batch_element_launch_ms")
     a = (C.c_double * 3)()
-    _check(load_library().b3g_batch_launch_times(ctx.handle, a, 1 if reset else 0), "b3g_batch_launch_times")
-    return {"assembly_ms": a[0], "pcg_ms": a[1], "steps": int(a[2])}
+    _check(lib.b3g_batch_launch_times(ctx.handle, a, 1 if reset else 0), "b3g_batch_launch_times")
+    return {"assembly_ms": a[0], "pcg_ms": a[1], "steps": int(a[2]), "elements_ms": el.value}
 
 
 PHASES = ["elements", "assembly", "spmv", "update", "direction", "final", "-", "-"]

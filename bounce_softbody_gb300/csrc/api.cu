@@ -499,9 +499,13 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	b->nw = d->sphere_radius ? (uint32_t)shapes.size() : 0;
 
 	char err[256];
+	// device storage order of the tetrahedra (b->tet_order[k] = element at position k)
+	b->tet_order = tet_storage_order(b->nt, d->tets);
+	std::vector<uint32_t> tet_rank(b->nt);
+	for (uint32_t k = 0; k < b->nt; ++k) tet_rank[b->tet_order[k]] = k;
 	Pattern P;
 	if (!build_pattern(n, b->nt, d->tets, b->ntr, d->tris, b->ns, d->springs, nbw, cf.bw_ids.data(), nms,
-	                   cf.ms_ids.data(), &P, err, sizeof(err)))
+	                   cf.ms_ids.data(), tet_rank.data(), &P, err, sizeof(err)))
 	{
 		delete b;
 		return fail(B3G_ERROR_INVALID_ARGUMENT, "%s", err);
@@ -520,21 +524,23 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	for (uint32_t e = 0; e < b->nt; ++e)
 	{
 		const uint32_t* t = d->tets + 4 * e;
-		tet[e] = make_uint4(t[0], t[1], t[2], t[3]);
+		const uint32_t k_e = tet_rank[e];
+		tet[k_e] = make_uint4(t[0], t[1], t[2], t[3]);
 		float r[12];
 		for (int k = 0; k < 4; ++k)
 			for (int c = 0; c < 3; ++c) r[3 * k + c] = d->tet_rest ? d->tet_rest[12 * e + 3 * k + c] : d->positions[3 * t[k] + c];
-		float vol, lam, mu;
-		tet_setup(r, d->tet_young[e], d->tet_poisson[e], &tet_invE[9 * (size_t)e], &vol, &lam, &mu);
-		if (!(vol > 0.0f) || !std::isfinite(tet_invE[9 * (size_t)e]))
+		float vol, lam, mu, ie[9];
+		tet_setup(r, d->tet_young[e], d->tet_poisson[e], ie, &vol, &lam, &mu);
+		if (!(vol > 0.0f) || !std::isfinite(ie[0]))
 		{
 			free_pattern(&P);
 			delete b;
 			return fail(B3G_ERROR_INVALID_ARGUMENT, "tetrahedron %u is degenerate", e);
 		}
+		for (int q = 0; q < 9; ++q) tet_invE[(size_t)q * b->nt + k_e] = ie[q];
 		float kd = d->tet_stiffness_damping ? d->tet_stiffness_damping[e] : 0.0f;
-		tet_mat[e] = make_float4(vol, lam, mu, kd);
-		tet_q[e] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+		tet_mat[k_e] = make_float4(vol, lam, mu, kd);
+		tet_q[k_e] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
 		// tetrahedron_fixture.cpp:34-45 (same volume as the element's)
 		float dens = d->tet_density ? d->tet_density[e] : 0.0f;
 		b->h_tet_mass[e] = dens * vol;
@@ -1090,20 +1096,26 @@ int b3g_body_set_types(b3g_body* b, const int32_t* types)
 	return upload_masses(b);
 }
 
+// rotations in the caller's element order; the device keeps them in storage order
 int b3g_body_get_rotations(b3g_body* b, float* q)
 {
 	if (!b || !q) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
 	cudaStream_t st = b->ctx->stream;
-	cudaError_t e = cudaMemcpyAsync(q, b->d.tet_q, b->nt * sizeof(float4), cudaMemcpyDeviceToHost, st);
+	std::vector<float4> stored(b->nt);
+	cudaError_t e = cudaMemcpyAsync(stored.data(), b->d.tet_q, b->nt * sizeof(float4), cudaMemcpyDeviceToHost, st);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "get_rotations");
+	if (e != cudaSuccess) return cuda_fail(e, "get_rotations");
+	for (uint32_t k = 0; k < b->nt; ++k) std::memcpy(q + 4 * (size_t)b->tet_order[k], &stored[k], sizeof(float4));
+	return B3G_OK;
 }
 
 int b3g_body_set_rotations(b3g_body* b, const float* q)
 {
 	if (!b || !q) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
 	cudaStream_t st = b->ctx->stream;
-	cudaError_t e = cudaMemcpyAsync(b->d.tet_q, q, b->nt * sizeof(float4), cudaMemcpyHostToDevice, st);
+	std::vector<float4> stored(b->nt);
+	for (uint32_t k = 0; k < b->nt; ++k) std::memcpy(&stored[k], q + 4 * (size_t)b->tet_order[k], sizeof(float4));
+	cudaError_t e = cudaMemcpyAsync(b->d.tet_q, stored.data(), b->nt * sizeof(float4), cudaMemcpyHostToDevice, st);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
 	return e == cudaSuccess ? B3G_OK : cuda_fail(e, "set_rotations");
 }

@@ -24,8 +24,8 @@ struct b3g_context
 	// b3g_batch_set_launch_timing: batched steps launch directly (no graph) with events around
 	// the assembly and PCG launches; device milliseconds accumulate here
 	bool launch_timing = false;
-	cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
-	double t_assembly_ms = 0.0, t_pcg_ms = 0.0;
+	cudaEvent_t tev[4] = {nullptr, nullptr, nullptr, nullptr};
+	double t_assembly_ms = 0.0, t_pcg_ms = 0.0, t_elements_ms = 0.0;
 	unsigned long long t_steps = 0;
 	// batched host transfers (b3g_batch_apply_forces / b3g_batch_get_state): one contiguous
 	// device staging buffer, one copy each way and one scatter / gather launch per call; the
@@ -89,6 +89,7 @@ struct b3g_body
 	// host copies needed by ResetMass / SetType
 	std::vector<int32_t> h_type;
 	std::vector<uint32_t> h_tets, h_tris;
+	std::vector<uint32_t> tet_order;     // device storage order: element at each position
 	std::vector<float> h_tet_mass, h_tri_mass, h_given_mass;
 	std::vector<float> h_mass, h_invmass;
 	b3g_step_stats last{};

@@ -463,17 +463,21 @@ extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_
 		{
 			cudaError_t e = cudaEventRecord(ctx->tev[0], st);
 			A.part = 1;
+			A.ev_rows = ctx->tev[3];
 			if (e == cudaSuccess) e = op_batch(A, st);
+			A.ev_rows = nullptr;
 			if (e == cudaSuccess) e = cudaEventRecord(ctx->tev[1], st);
 			A.part = 2;
 			if (e == cudaSuccess) e = op_batch(A, st);
 			if (e == cudaSuccess) e = cudaEventRecord(ctx->tev[2], st);
 			if (e == cudaSuccess) e = cudaEventSynchronize(ctx->tev[2]);
 			if (e != cudaSuccess) return cuda_fail(e, "timed batch step");
-			float m1 = 0.0f, m2 = 0.0f;
+			float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f;
 			cudaEventElapsedTime(&m1, ctx->tev[0], ctx->tev[1]);
 			cudaEventElapsedTime(&m2, ctx->tev[1], ctx->tev[2]);
+			cudaEventElapsedTime(&m3, ctx->tev[0], ctx->tev[3]);
 			ctx->t_assembly_ms += m1;
+			ctx->t_elements_ms += m3;
 			ctx->t_pcg_ms += m2;
 			ctx->t_steps += 1;
 		}
@@ -529,9 +533,16 @@ extern "C" int b3g_batch_launch_times(b3g_context* ctx, double out[3], int reset
 	out[2] = (double)ctx->t_steps;
 	if (reset)
 	{
-		ctx->t_assembly_ms = ctx->t_pcg_ms = 0.0;
+		ctx->t_assembly_ms = ctx->t_pcg_ms = ctx->t_elements_ms = 0.0;
 		ctx->t_steps = 0;
 	}
+	return B3G_OK;
+}
+
+extern "C" int b3g_batch_element_launch_ms(b3g_context* ctx, double* out)
+{
+	if (!ctx || !out) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	*out = ctx->t_elements_ms;
 	return B3G_OK;
 }
 

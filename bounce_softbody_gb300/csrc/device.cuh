@@ -262,39 +262,60 @@ __device__ __forceinline__ void quat_to_mat(float4 q, float R[9])
 // Mueller et al., "A Robust Method to Extract the Rotational Part of Deformations", warm
 // started from q0, with the stopping rules of tetrahedron_element_force.cpp:273-311
 // (den == 0, |omega| < 1e-9, inverse denominator + 1e-9, at most 32 iterations).
+// In float the |omega| < 1e-9 rule sits at the rounding floor of the torque, so most
+// tetrahedra run all 32 iterations (as the reference's float build does); each iteration is
+// therefore written without divisions or sincosf for the usual small angles:
+//  * the update quaternion (sin(w/2) omega / w, cos(w/2)) from Taylor series in w^2 of
+//    sin(x) / x and cos(x), x = w / 2, for w < 1 (truncation below 3e-10; sincosf otherwise);
+//  * the test |omega| < 1e-9 as |omega|^2 < 1e-18;
+//  * the normalisation 1 / |q| of a product of unit quaternions, |q|^2 = 1 + d with
+//    |d| < 1e-4, as 1 - d / 2 (error 3 d^2 / 8 < 4e-9), else a square root and one reciprocal.
 __device__ __forceinline__ float4 extract_rotation(const float F[9], float4 q)
 {
 	const float kTol = 1.0e-9f;
+	const float3 a0 = f3(F[0], F[3], F[6]), a1 = f3(F[1], F[4], F[7]), a2 = f3(F[2], F[5], F[8]);
 #pragma unroll 1
 	for (int it = 0; it < 32; ++it)
 	{
 		float R[9];
 		quat_to_mat(q, R);
 		// columns: R(:, c) . F(:, c) and R(:, c) x F(:, c)
-		float3 r0 = f3(R[0], R[3], R[6]), r1 = f3(R[1], R[4], R[7]), r2 = f3(R[2], R[5], R[8]);
-		float3 a0 = f3(F[0], F[3], F[6]), a1 = f3(F[1], F[4], F[7]), a2 = f3(F[2], F[5], F[8]);
-		float den = fabsf(dot3(r0, a0) + dot3(r1, a1) + dot3(r2, a2));
+		const float3 r0 = f3(R[0], R[3], R[6]), r1 = f3(R[1], R[4], R[7]), r2 = f3(R[2], R[5], R[8]);
+		const float den = fabsf(dot3(r0, a0) + dot3(r1, a1) + dot3(r2, a2));
 		if (den == 0.0f) break;
-		float3 torque = cross3(r0, a0) + cross3(r1, a1) + cross3(r2, a2);
-		float inv_den = 1.0f / den + kTol;
-		float3 omega = inv_den * torque;
-		float w = len3(omega);
-		if (w < kTol) break;
-		float3 axis = f3(omega.x / w, omega.y / w, omega.z / w);
-		float sn, cs;
-		sincosf(0.5f * w, &sn, &cs);
-		float4 qw = make_float4(sn * axis.x, sn * axis.y, sn * axis.z, cs);
-		// quat.h:204 b3Mul(qw, q)
-		float3 av = f3(qw.x, qw.y, qw.z), bv = f3(q.x, q.y, q.z);
-		float3 rv = cross3(av, bv) + qw.w * bv + q.w * av;
-		float rs = qw.w * q.w - dot3(av, bv);
-		float l = sqrtf(dot3(rv, rv) + rs * rs);
-		if (l > kFltEps)
+		const float3 torque = cross3(r0, a0) + cross3(r1, a1) + cross3(r2, a2);
+		const float inv_den = 1.0f / den + kTol;
+		const float3 omega = inv_den * torque;
+		const float w2 = dot3(omega, omega);
+		if (w2 < kTol * kTol) break;
+		float half_sinc, cw;  // sin(w / 2) / w and cos(w / 2)
+		if (w2 < 1.0f)
 		{
-			rv = f3(rv.x / l, rv.y / l, rv.z / l);
-			rs = rs / l;
+			const float y = 0.25f * w2;  // x^2
+			half_sinc = 0.5f * (1.0f - y * (1.0f / 6.0f) * (1.0f - y * (1.0f / 20.0f) * (1.0f - y * (1.0f / 42.0f) * (1.0f - y * (1.0f / 72.0f)))));
+			cw = 1.0f - y * 0.5f * (1.0f - y * (1.0f / 12.0f) * (1.0f - y * (1.0f / 30.0f) * (1.0f - y * (1.0f / 56.0f))));
 		}
-		q = make_float4(rv.x, rv.y, rv.z, rs);
+		else
+		{
+			const float w = sqrtf(w2);
+			float sn;
+			sincosf(0.5f * w, &sn, &cw);
+			half_sinc = sn / w;
+		}
+		const float3 av = half_sinc * omega, bv = f3(q.x, q.y, q.z);
+		// quat.h:204 b3Mul(qw, q)
+		float3 rv = cross3(av, bv) + cw * bv + q.w * av;
+		float rs = cw * q.w - dot3(av, bv);
+		const float l2 = dot3(rv, rv) + rs * rs;
+		const float d = l2 - 1.0f;
+		float inv_l;
+		if (fabsf(d) < 1.0e-4f) inv_l = 1.0f - 0.5f * d;
+		else
+		{
+			const float l = sqrtf(l2);
+			inv_l = l > kFltEps ? 1.0f / l : 1.0f;
+		}
+		q = make_float4(inv_l * rv.x, inv_l * rv.y, inv_l * rv.z, inv_l * rs);
 	}
 	return q;
 }
@@ -333,9 +354,10 @@ __device__ __forceinline__ void tet_element(const DevBody& B, int e, const StepP
 	uint4 id = B.tet[e];
 	const float* X = P.first_newton ? B.x : B.xi;
 	const float* Vv = P.first_newton ? B.v : B.vi;
+	const size_t nt = (size_t)B.nt;
 	float ie[9];
 #pragma unroll
-	for (int k = 0; k < 9; ++k) ie[k] = B.tet_invE[9 * (size_t)e + k];
+	for (int k = 0; k < 9; ++k) ie[k] = B.tet_invE[k * nt + e];
 	float4 mat = B.tet_mat[e];  // volume, lambda, mu, kd
 	float3 p1 = ldl3<L>(X, id.x), p2 = ldl3<L>(X, id.y), p3 = ldl3<L>(X, id.z), p4 = ldl3<L>(X, id.w);
 	float F[9];
@@ -389,19 +411,19 @@ __device__ __forceinline__ void tet_element(const DevBody& B, int e, const StepP
 	const float c = (h * h + h * kd) * vol;
 	const float su = sqrtf(c * mu);
 	const float ratio = mu > 0.0f ? lam / mu : 0.0f;
-	float* bc = B.tet_bc + 12 * (size_t)e;
-	float4* rec = B.tet_rec + 4 * (size_t)e;
+	float* bc = B.tet_bc + e;
+	float4* rec = B.tet_rec + e;
 #pragma unroll
 	for (int a = 0; a < 4; ++a)
 	{
 		float3 t = mv9(S, g[a]);
 		float3 f = mv9(R, t);
 		float s = -h * vol;
-		bc[3 * a + 0] = s * f.x;
-		bc[3 * a + 1] = s * f.y;
-		bc[3 * a + 2] = s * f.z;
+		bc[(3 * a + 0) * nt] = s * f.x;
+		bc[(3 * a + 1) * nt] = s * f.y;
+		bc[(3 * a + 2) * nt] = s * f.z;
 		float3 rg = mv9(R, g[a]);
-		rec[a] = make_float4(su * rg.x, su * rg.y, su * rg.z, ratio);
+		rec[a * nt] = make_float4(su * rg.x, su * rg.y, su * rg.z, ratio);
 	}
 }
 
@@ -1090,6 +1112,14 @@ __device__ __forceinline__ bool aabb_overlap(float3 p, float r, const DevShape& 
 template <class TV>
 __device__ __forceinline__ TV* vp(void* p) { return (TV*)p; }
 
+// Right-hand-side part of local vertex (code & 3) of the tetrahedron at position code >> 2.
+template <class L>
+__device__ __forceinline__ float3 tet_bc_part(const float* bc, size_t nt, uint32_t code)
+{
+	const float* p = bc + (code >> 2) + 3 * (code & 3u) * nt;
+	return f3(L::ld(p), L::ld(p + nt), L::ld(p + 2 * nt));
+}
+
 // a += (h^2 + h kd) R K0_ab R^T of one tetrahedron from its factored record:
 // ratio u_a u_b^T + u_b u_a^T + (u_a . u_b) I with u = sqrt(c mu) R g and ratio = lambda / mu
 __device__ __forceinline__ void add_tet_block(float a[9], float4 ua, float4 ub)
@@ -1234,8 +1264,10 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	float3 bi = Mi * (v0 - vi) + h * (fe + fi);
 	// contact dfdx w term: h dfdx w = -h Kc w
 	if (!TETS) bi = bi - h * mv9(Kc, wi);
+	const size_t nt = (size_t)B.nt;
 	{
-		// tetrahedra's right-hand-side parts of this vertex, four in flight at a time
+		// tetrahedra's right-hand-side parts of this vertex (code: position << 2 | local vertex),
+		// four in flight at a time
 		const uint32_t st = __ldg(B.vt_start + i);
 		const int cnt = __ldg(B.vt_cnt + i);
 		int t = 0;
@@ -1246,11 +1278,11 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 #pragma unroll
 			for (int u = 0; u < 4; ++u) e[u] = __ldg(B.vt_list + st + kSlice * (t + u));
 #pragma unroll
-			for (int u = 0; u < 4; ++u) c[u] = ldl3<L>(B.tet_bc, e[u]);
+			for (int u = 0; u < 4; ++u) c[u] = tet_bc_part<L>(B.tet_bc, nt, e[u]);
 #pragma unroll
 			for (int u = 0; u < 4; ++u) bi = bi + c[u];
 		}
-		for (; t < cnt; ++t) bi = bi + ldl3<L>(B.tet_bc, __ldg(B.vt_list + st + kSlice * t));
+		for (; t < cnt; ++t) bi = bi + tet_bc_part<L>(B.tet_bc, nt, __ldg(B.vt_list + st + kSlice * t));
 	}
 	if (!TETS)
 	{
@@ -1300,9 +1332,9 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 			for (int u = 0; u < 4; ++u)
 				if (u < cnt)
 				{
-					const size_t r0 = 4 * (size_t)(cd[u] >> 4);
-					ua[u] = L::ld(B.tet_rec + r0 + ((cd[u] >> 2) & 3u));
-					ub[u] = L::ld(B.tet_rec + r0 + (cd[u] & 3u));
+					const float4* r0 = B.tet_rec + (cd[u] >> 4);
+					ua[u] = L::ld(r0 + ((cd[u] >> 2) & 3u) * nt);
+					ub[u] = L::ld(r0 + (cd[u] & 3u) * nt);
 				}
 			if (k + 1 < w)
 			{
@@ -1322,9 +1354,9 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 #pragma unroll
 				for (int u = 0; u < 4; ++u)
 				{
-					const size_t r0 = 4 * (size_t)(code[u] >> 4);
-					ua[u] = L::ld(B.tet_rec + r0 + ((code[u] >> 2) & 3u));
-					ub[u] = L::ld(B.tet_rec + r0 + (code[u] & 3u));
+					const float4* r0 = B.tet_rec + (code[u] >> 4);
+					ua[u] = L::ld(r0 + ((code[u] >> 2) & 3u) * nt);
+					ub[u] = L::ld(r0 + (code[u] & 3u) * nt);
 				}
 #pragma unroll
 				for (int u = 0; u < 4; ++u) add_tet_block(a, ua[u], ub[u]);
@@ -1332,8 +1364,8 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 			for (; t < cnt; ++t)
 			{
 				const uint32_t code = __ldg(B.tet_clist + st + kSlice * t);
-				const size_t r0 = 4 * (size_t)(code >> 4);
-				add_tet_block(a, L::ld(B.tet_rec + r0 + ((code >> 2) & 3u)), L::ld(B.tet_rec + r0 + (code & 3u)));
+				const float4* r0 = B.tet_rec + (code >> 4);
+				add_tet_block(a, L::ld(r0 + ((code >> 2) & 3u) * nt), L::ld(r0 + (code & 3u) * nt));
 			}
 		}
 		const uint32_t bst = TETS ? 0u : __ldg(B.blk_cstart + slot);

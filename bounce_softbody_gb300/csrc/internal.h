@@ -22,6 +22,8 @@
 #include <stdint.h>
 #include <stddef.h>
 
+#include <vector>
+
 #include "../../include/b3g.h"
 
 #include <vector_types.h>
@@ -160,12 +162,14 @@ struct DevBody
 	const int8_t* type;
 
 	// tetrahedra
+	// tetrahedra in device storage order (tet_storage_order); the per-tet arrays are planes of
+	// nt entries, so that consecutive tetrahedra's values are consecutive words
 	const uint4* tet;
-	const float* tet_invE;      // 9 per tet, column-major like b3Mat33
+	const float* tet_invE;      // 9 planes: plane 3 j + r = invE(r, j) (column-major like b3Mat33)
 	const float4* tet_mat;      // volume, lambda, mu, stiffness damping
 	float4* tet_q;              // rotation quaternion (x, y, z, w)
-	float4* tet_rec;            // 4 float4 per tet: (sqrt(c mu) R g_a, lambda / mu), c = (h^2 + h kd) V
-	float* tet_bc;              // 12 per tet: h * (f + dfdx w) per local vertex
+	float4* tet_rec;            // 4 planes, plane a: (sqrt(c mu) R g_a, lambda / mu), c = (h^2 + h kd) V
+	float* tet_bc;              // 12 planes, plane 3 a + c: h * (f + dfdx w) of local vertex a
 
 	// triangles
 	const uint4* tri;           // 3 ids + pad
@@ -249,10 +253,19 @@ struct Pattern
 };
 
 // Builds the SELL-32 pattern and every contribution list. Returns false with a message on a
-// malformed mesh (vertex index out of range, degenerate element).
+// malformed mesh (vertex index out of range, degenerate element). tet_rank (may be null: the
+// identity) maps each tetrahedron to its position in device storage; the lists name that
+// position, while each slot still lists its contributions in the caller's element order.
 bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, const uint32_t* tris,
                    uint32_t ns, const uint32_t* springs, uint32_t nbw, const uint32_t* bw, uint32_t nms,
-                   const uint32_t* ms, Pattern* out, char* err, size_t errlen);
+                   const uint32_t* ms, const uint32_t* tet_rank, Pattern* out, char* err, size_t errlen);
+
+// Device storage order of a body's tetrahedra (order[k] = the element stored at position k).
+// When the mesh has few distinct vertex-offset signatures (t1 - t0, t2 - t0, t3 - t0), as a
+// structured grid has, the tetrahedra are grouped by signature and ordered by first vertex
+// within a group: rows that are neighbours in the vertex numbering then read neighbouring
+// records. Any other mesh keeps its own order.
+std::vector<uint32_t> tet_storage_order(uint32_t nt, const uint32_t* tets);
 void free_pattern(Pattern* p);
 
 } // namespace b3g

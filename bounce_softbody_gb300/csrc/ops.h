@@ -100,6 +100,7 @@ struct BatchArgs
 	int ctas;                // CTAs of the launch (multiple of cluster)
 	unsigned long long* prof; // optional phase cycle counters (8 per CTA), null = off
 	int part = 0;            // single-Newton steps: 0 both launches, 1 assembly only, 2 PCG only
+	cudaEvent_t ev_rows = nullptr;  // if set, recorded between the element and the row launches
 	// single-Newton steps: the elements, then the rows, of all bodies in two flat launches before
 	// the PCG launch. elem_off[k] / slice_off[k]: first element / row slice of bodies[k] in the
 	// flat numbering (count + 1 entries each; elements of a body: tetrahedra, triangles, springs,

@@ -91,6 +91,45 @@ static void free_lists(Pattern::Lists* l)
 	*l = Pattern::Lists();
 }
 
+std::vector<uint32_t> tet_storage_order(uint32_t nt, const uint32_t* tets)
+{
+	std::vector<uint32_t> order(nt);
+	for (uint32_t e = 0; e < nt; ++e) order[e] = e;
+	// signatures as offsets from the first vertex; a mesh with more than kMaxSignatures of them
+	// has no repeating cell to exploit
+	constexpr size_t kMaxSignatures = 64;
+	struct Sig
+	{
+		int64_t d[3];
+		bool operator<(const Sig& o) const
+		{
+			return d[0] != o.d[0] ? d[0] < o.d[0] : (d[1] != o.d[1] ? d[1] < o.d[1] : d[2] < o.d[2]);
+		}
+		bool operator==(const Sig& o) const { return d[0] == o.d[0] && d[1] == o.d[1] && d[2] == o.d[2]; }
+	};
+	auto sig_of = [&](uint32_t e) {
+		const uint32_t* t = tets + 4 * (size_t)e;
+		return Sig{{(int64_t)t[1] - t[0], (int64_t)t[2] - t[0], (int64_t)t[3] - t[0]}};
+	};
+	std::vector<Sig> seen;
+	for (uint32_t e = 0; e < nt; ++e)
+	{
+		const Sig s = sig_of(e);
+		if (std::find(seen.begin(), seen.end(), s) != seen.end()) continue;
+		if (seen.size() == kMaxSignatures) return order;
+		seen.push_back(s);
+	}
+	std::sort(seen.begin(), seen.end());
+	std::vector<uint32_t> group(nt);
+	for (uint32_t e = 0; e < nt; ++e)
+		group[e] = (uint32_t)(std::lower_bound(seen.begin(), seen.end(), sig_of(e)) - seen.begin());
+	std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+		if (group[a] != group[b]) return group[a] < group[b];
+		return tets[4 * (size_t)a] < tets[4 * (size_t)b];
+	});
+	return order;
+}
+
 void free_pattern(Pattern* p)
 {
 	std::free(p->slice_ptr);
@@ -105,7 +144,7 @@ void free_pattern(Pattern* p)
 
 bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, const uint32_t* tris,
                    uint32_t ns, const uint32_t* springs, uint32_t nbw, const uint32_t* bw, uint32_t nms,
-                   const uint32_t* ms, Pattern* out, char* err, size_t errlen)
+                   const uint32_t* ms, const uint32_t* tet_rank, Pattern* out, char* err, size_t errlen)
 {
 	*out = Pattern();
 	if (n == 0)
@@ -315,7 +354,7 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 				for (uint32_t b = 0; b < elem_size(c.kind); ++b)
 				{
 					uint32_t slot = slot_of(i, find_k(i, elem_vertex(c, b)));
-					if (c.kind == 0) tlist[tf[slot]++] = (c.e << 4) | (c.a << 2) | b;
+					if (c.kind == 0) tlist[tf[slot]++] = ((tet_rank ? tet_rank[c.e] : c.e) << 4) | (c.a << 2) | b;
 					else if (c.kind == 1) blist[bf[slot]++] = ((9u * c.e + 3u * c.a + b) << 1);
 					else if (c.kind == 2) blist[bf[slot]++] = ((9u * ntr + c.e) << 1) | (c.a != b ? 1u : 0u);
 					else if (c.kind == 3) blist[bf[slot]++] = (uint32_t)(blk_bw + 9u * c.e + 3u * c.a + b) << 1;
@@ -333,7 +372,7 @@ bool build_pattern(uint32_t n, uint32_t nt, const uint32_t* tets, uint32_t ntr, 
 		for (uint32_t k = inc_cnt[i]; k < inc_cnt[i + 1]; ++k)
 		{
 			const Inc& c = inc[k];
-			if (c.kind == 0) vtl.push_back(4u * c.e + c.a);
+			if (c.kind == 0) vtl.push_back(((tet_rank ? tet_rank[c.e] : c.e) << 2) | c.a);
 			else if (c.kind == 1) vbl.push_back((3u * c.e + c.a) << 1);
 			else if (c.kind == 2) vbl.push_back(((3u * ntr + c.e) << 1) | (c.a == 1 ? 1u : 0u));
 			else if (c.kind == 3) vbl.push_back((uint32_t)(vec_bw + 3u * c.e + c.a) << 1);

@@ -116,6 +116,7 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 		{
 			if (A.nelem > 0) k_batch_elements<<<elem_grid(A.nelem), kElemThreads, 0, st>>>(P);
 			e = cudaGetLastError();
+			if (e == cudaSuccess && A.ev_rows) e = cudaEventRecord(A.ev_rows, st);
 			if (e == cudaSuccess)
 				e = A.prec == kP64 ? launch_rows_f64(P, st)
 				                   : (A.prec == kPBF ? launch_rows_bf16(P, st) : launch_rows_f32(P, st));

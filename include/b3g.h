@@ -291,6 +291,9 @@ B3G_API int b3g_batch_phase_cycles(b3g_context* ctx, uint64_t out[8], int reset)
  * launches and of the PCG launches and the number of timed steps (out[0..2]). */
 B3G_API int b3g_batch_set_launch_timing(b3g_context* ctx, int on);
 B3G_API int b3g_batch_launch_times(b3g_context* ctx, double out[3], int reset);
+/* The element launch's share of the assembly milliseconds above (the rest is the row assembly),
+ * accumulated and reset with them. */
+B3G_API int b3g_batch_element_launch_ms(b3g_context* ctx, double* out);
 
 /* Host-buffer transfers for a list of bodies of one context; the host arrays are the bodies'
  * arrays concatenated in list order (3 floats per vertex). Pinned host memory makes them
