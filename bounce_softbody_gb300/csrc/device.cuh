@@ -266,7 +266,8 @@ __device__ __forceinline__ void quat_to_mat(float4 q, float R[9])
 // tetrahedra run all 32 iterations (as the reference's float build does); each iteration is
 // therefore written without divisions or sincosf for the usual small angles:
 //  * the update quaternion (sin(w/2) omega / w, cos(w/2)) from Taylor series in w^2 of
-//    sin(x) / x and cos(x), x = w / 2, for w < 1 (truncation below 3e-10; sincosf otherwise);
+//    sin(x) / x and cos(x), x = w / 2: two terms for w < 1e-3 (the next ones below 1e-14),
+//    five for w < 1 (truncation below 3e-10), sincosf otherwise;
 //  * the test |omega| < 1e-9 as |omega|^2 < 1e-18;
 //  * the normalisation 1 / |q| of a product of unit quaternions, |q|^2 = 1 + d with
 //    |d| < 1e-4, as 1 - d / 2 (error 3 d^2 / 8 < 4e-9), else a square root and one reciprocal.
@@ -289,7 +290,13 @@ __device__ __forceinline__ float4 extract_rotation(const float F[9], float4 q)
 		const float w2 = dot3(omega, omega);
 		if (w2 < kTol * kTol) break;
 		float half_sinc, cw;  // sin(w / 2) / w and cos(w / 2)
-		if (w2 < 1.0f)
+		if (w2 < 1.0e-6f)
+		{
+			const float y = 0.25f * w2;  // x^2
+			half_sinc = 0.5f - y * (1.0f / 12.0f);
+			cw = 1.0f - 0.5f * y;
+		}
+		else if (w2 < 1.0f)
 		{
 			const float y = 0.25f * w2;  // x^2
 			half_sinc = 0.5f * (1.0f - y * (1.0f / 6.0f) * (1.0f - y * (1.0f / 20.0f) * (1.0f - y * (1.0f / 42.0f) * (1.0f - y * (1.0f / 72.0f)))));

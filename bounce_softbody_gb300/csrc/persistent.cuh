@@ -750,7 +750,12 @@ template <class TA, class TV, bool TETS, bool FILT = false>
 __global__ void __launch_bounds__(B3G_ROWS_THREADS, TETS ? B3G_ROWS_TETS_MIN_BLOCKS : B3G_ROWS_MIN_BLOCKS)
 k_batch_rows(BatchParams P)
 {
+	// each warp's body descriptor, copied to shared memory: the row code's stores to global
+	// memory cannot alias it there, so its fields need not be re-read after each store
+	static_assert(sizeof(DevBody) % 8 == 0, "DevBody is copied in 8-byte words");
+	__shared__ DevBody s_body[kRowsWarps];
 	const int lane = threadIdx.x & 31;
+	DevBody& B = s_body[threadIdx.x >> 5];
 	StepParams sp;
 	sp.h = P.h;
 	sp.first_newton = 1;
@@ -758,7 +763,13 @@ k_batch_rows(BatchParams P)
 	for (unsigned g = blockIdx.x * kRowsWarps + (threadIdx.x >> 5); g < P.nslices; g += nw)
 	{
 		const int b = flat_body(P.slice_off, P.nbodies, g);
-		const DevBody& B = P.bodies[b];
+		__syncwarp();
+		{
+			const unsigned long long* src = reinterpret_cast<const unsigned long long*>(P.bodies + b);
+			unsigned long long* dst = reinterpret_cast<unsigned long long*>(&B);
+			for (int w = lane; w < (int)(sizeof(DevBody) / 8); w += 32) dst[w] = __ldg(src + w);
+		}
+		__syncwarp();
 		const int sl = (int)(g - __ldg(P.slice_off + b));
 		if (FILT && B.filt) assemble_row_filtered<TA, TV, LdPlain>(B, sl, lane, sp, true);
 		else assemble_row<TA, TV, LdPlain, false, TETS>(B, sl, lane, sp, true);
