@@ -672,6 +672,19 @@ int b3g_body_create(b3g_context* ctx, const b3g_body_desc* d, b3g_body** out)
 	D.gravity[1] = d->gravity[1];
 	D.gravity[2] = d->gravity[2];
 	D.precond = B3G_PRECOND_JACOBI;
+	// the ratio the element kernel stores in each record (mu > 0 ? lambda / mu : 0), when it is
+	// the same for every tetrahedron
+	D.tet_ratio = -1.0f;
+	for (uint32_t k = 0; k < b->nt; ++k)
+	{
+		const float r = tet_mat[k].z > 0.0f ? tet_mat[k].y / tet_mat[k].z : 0.0f;
+		if (k == 0) D.tet_ratio = r;
+		else if (r != D.tet_ratio)
+		{
+			D.tet_ratio = -1.0f;
+			break;
+		}
+	}
 	b->d = D;
 
 	cudaStream_t st = ctx->stream;

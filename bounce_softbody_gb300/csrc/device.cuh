@@ -1119,6 +1119,28 @@ __device__ __forceinline__ bool aabb_overlap(float3 p, float r, const DevShape& 
 template <class TV>
 __device__ __forceinline__ TV* vp(void* p) { return (TV*)p; }
 
+// p += u_a u_b^T: the outer-product sum of a slot whose tetrahedra share one ratio lambda / mu,
+// which add_tet_blocks_uniform turns into that slot's block
+__device__ __forceinline__ void add_outer(float p[9], float4 ua, float4 ub)
+{
+	const float A3[3] = {ua.x, ua.y, ua.z}, B3[3] = {ub.x, ub.y, ub.z};
+#pragma unroll
+	for (int r = 0; r < 3; ++r)
+#pragma unroll
+		for (int c = 0; c < 3; ++c) p[3 * r + c] += A3[r] * B3[c];
+}
+
+// The sum over a slot's tetrahedra of add_tet_block's blocks with one ratio for all, from their
+// outer-product sum P = sum u_a u_b^T: ratio P + P^T + tr(P) I (the same sum, reassociated).
+__device__ __forceinline__ void add_tet_blocks_uniform(float a[9], const float p[9], float ratio)
+{
+	const float tr = p[0] + p[4] + p[8];
+#pragma unroll
+	for (int r = 0; r < 3; ++r)
+#pragma unroll
+		for (int c = 0; c < 3; ++c) a[3 * r + c] += ratio * p[3 * r + c] + p[3 * c + r] + (r == c ? tr : 0.0f);
+}
+
 // Right-hand-side part of local vertex (code & 3) of the tetrahedron at position code >> 2.
 template <class L>
 __device__ __forceinline__ float3 tet_bc_part(const float* bc, size_t nt, uint32_t code)
@@ -1180,6 +1202,72 @@ __device__ __forceinline__ void contact_filter_vertex(const DevBody& B, int i, f
 }
 
 __device__ __forceinline__ bool filt_on(float4 f) { return f.x != 0.0f || f.y != 0.0f || f.z != 0.0f; }
+
+// The end of row i's assembly once its right-hand side bi and diagonal block are final: pb,
+// the Jacobi preconditioner and, when init_pcg is set, r = pb, s = d = M^-1 r and the zero
+// initial guess; returns r.s (0 without init_pcg).
+template <class TV>
+__device__ __forceinline__ double row_finish(const DevBody& B, int i, float3 bi, const float diag[9], bool init_pcg)
+{
+	TV* pb = vp<TV>(B.pb);
+	const TV bv[3] = {(TV)bi.x, (TV)bi.y, (TV)bi.z};
+	vst(pb, i, bv);
+
+	// preconditioner: scalar Jacobi (sparse_solver.cpp:38-55) as one 4-wide value, or the rows of
+	// the inverted 3x3 diagonal block as three
+	TV* Mv = vp<TV>(B.Minv);
+	TV m3[9];
+	if (B.precond == B3G_PRECOND_BLOCK_JACOBI)
+	{
+		double d0 = diag[0], d1 = diag[1], d2 = diag[2], d3 = diag[3], d4 = diag[4], d5 = diag[5], d6 = diag[6],
+		       d7 = diag[7], d8 = diag[8];
+		double c00 = d4 * d8 - d5 * d7, c01 = d2 * d7 - d1 * d8, c02 = d1 * d5 - d2 * d4;
+		double c10 = d5 * d6 - d3 * d8, c11 = d0 * d8 - d2 * d6, c12 = d2 * d3 - d0 * d5;
+		double c20 = d3 * d7 - d4 * d6, c21 = d1 * d6 - d0 * d7, c22 = d0 * d4 - d1 * d3;
+		double det = d0 * c00 + d1 * c10 + d2 * c20;
+		double id = 1.0 / det;
+		double inv[9] = {c00 * id, c01 * id, c02 * id, c10 * id, c11 * id, c12 * id, c20 * id, c21 * id, c22 * id};
+#pragma unroll
+		for (int q = 0; q < 9; ++q) m3[q] = (TV)inv[q];
+		vst(Mv, 3 * i, m3);
+		vst(Mv, 3 * i + 1, m3 + 3);
+		vst(Mv, 3 * i + 2, m3 + 6);
+	}
+	else
+	{
+		m3[0] = (TV)(1.0f / diag[0]);
+		m3[4] = (TV)(1.0f / diag[4]);
+		m3[8] = (TV)(1.0f / diag[8]);
+		const TV md[3] = {m3[0], m3[4], m3[8]};
+		vst(Mv, i, md);
+	}
+	if (!init_pcg) return 0.0;
+	const TV r0 = bv[0], r1 = bv[1], r2 = bv[2];
+	TV sv[3];
+	if (B.precond == B3G_PRECOND_BLOCK_JACOBI)
+	{
+		sv[0] = m3[0] * r0 + m3[1] * r1 + m3[2] * r2;
+		sv[1] = m3[3] * r0 + m3[4] * r1 + m3[5] * r2;
+		sv[2] = m3[6] * r0 + m3[7] * r1 + m3[8] * r2;
+	}
+	else
+	{
+		sv[0] = m3[0] * r0;
+		sv[1] = m3[4] * r1;
+		sv[2] = m3[8] * r2;
+	}
+	const TV zero[3] = {0, 0, 0};
+	vst(vp<TV>(B.r), i, bv);
+	vst(vp<TV>(B.s), i, sv);
+	vst(vp<TV>(B.d), i, sv);
+	vst(vp<TV>(B.py), i, zero);
+	if (B.xff)
+	{
+		const float z[3] = {0.0f, 0.0f, 0.0f};
+		ff_st(B.xff, i, z, z);
+	}
+	return dot3<TV>(bv, sv);
+}
 
 // Assembles row i of the pre-filtered system: pA = S A S^T + I - S and pb = S b with
 //   A = M - h dfdv - h^2 dfdx,  b = M (v0 - v) + h (fe + fi) + h dfdx (x0 - x + h v + y)
@@ -1309,9 +1397,10 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	float3 bz = f3(0.0f, 0.0f, 0.0f);  // (A z)_i
 
 	float diag[9];
-	// Slot pipeline: the next slot's list header and its first four tetrahedron codes load while
-	// this slot's records are gathered, so a slot waits on one gather instead of three dependent
-	// loads. Contributions are added in list order, as before.
+	double rsd = 0.0;  // r.s of the row (unfiltered form: from the k = 0 slot)
+	// Slot pipeline: the list header of the slot after next and the next slot's first four
+	// tetrahedron codes load while this slot's records are gathered, so a slot waits on one
+	// gather instead of three dependent loads. Contributions are added in list order.
 	uint32_t st_n = __ldg(B.tet_cstart + base + lane);
 	int cnt_n = __ldg(B.tet_ccnt + base + lane);
 	uint32_t cd_n[4];
@@ -1334,6 +1423,9 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		}
 		float a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 		{
+			// uniform: every tetrahedron of the body has the same ratio, so the slot sums the
+			// outer products u_a u_b^T (in a) and forms its block once at the end
+			const bool uniform = B.tet_ratio >= 0.0f;
 			float4 ua[4], ub[4];
 #pragma unroll
 			for (int u = 0; u < 4; ++u)
@@ -1348,9 +1440,18 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 #pragma unroll
 				for (int u = 0; u < 4; ++u) cd_n[u] = u < cnt_n ? __ldg(B.tet_clist + st_n + kSlice * u) : 0u;
 			}
+			if (uniform)
+			{
 #pragma unroll
-			for (int u = 0; u < 4; ++u)
-				if (u < cnt) add_tet_block(a, ua[u], ub[u]);
+				for (int u = 0; u < 4; ++u)
+					if (u < cnt) add_outer(a, ua[u], ub[u]);
+			}
+			else
+			{
+#pragma unroll
+				for (int u = 0; u < 4; ++u)
+					if (u < cnt) add_tet_block(a, ua[u], ub[u]);
+			}
 			// the rest of the slot's contributions, four in flight at a time
 			int t = 4;
 			for (; t + 4 <= cnt; t += 4)
@@ -1365,14 +1466,35 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 					ua[u] = L::ld(r0 + ((code[u] >> 2) & 3u) * nt);
 					ub[u] = L::ld(r0 + (code[u] & 3u) * nt);
 				}
+				if (uniform)
+				{
 #pragma unroll
-				for (int u = 0; u < 4; ++u) add_tet_block(a, ua[u], ub[u]);
+					for (int u = 0; u < 4; ++u) add_outer(a, ua[u], ub[u]);
+				}
+				else
+				{
+#pragma unroll
+					for (int u = 0; u < 4; ++u) add_tet_block(a, ua[u], ub[u]);
+				}
 			}
 			for (; t < cnt; ++t)
 			{
 				const uint32_t code = __ldg(B.tet_clist + st + kSlice * t);
 				const float4* r0 = B.tet_rec + (code >> 4);
-				add_tet_block(a, L::ld(r0 + ((code >> 2) & 3u) * nt), L::ld(r0 + (code & 3u) * nt));
+				const float4 u0 = L::ld(r0 + ((code >> 2) & 3u) * nt), u1 = L::ld(r0 + (code & 3u) * nt);
+				if (uniform) add_outer(a, u0, u1);
+				else add_tet_block(a, u0, u1);
+			}
+			if (uniform)
+			{
+				float p[9];
+#pragma unroll
+				for (int q = 0; q < 9; ++q)
+				{
+					p[q] = a[q];
+					a[q] = 0.0f;
+				}
+				add_tet_blocks_uniform(a, p, B.tet_ratio);
 			}
 		}
 		const uint32_t bst = TETS ? 0u : __ldg(B.blk_cstart + slot);
@@ -1464,64 +1586,7 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 		bi = bi - bz;
 		if (ci) bi = bi - dot3(f3(fi4.x, fi4.y, fi4.z), bi) * f3(fi4.x, fi4.y, fi4.z);
 	}
-	TV* pb = vp<TV>(B.pb);
-	const TV bv[3] = {(TV)bi.x, (TV)bi.y, (TV)bi.z};
-	vst(pb, i, bv);
-
-	// preconditioner: scalar Jacobi (sparse_solver.cpp:38-55) as one 4-wide value, or the rows of
-	// the inverted 3x3 diagonal block as three
-	TV* Mv = vp<TV>(B.Minv);
-	TV m3[9];
-	if (B.precond == B3G_PRECOND_BLOCK_JACOBI)
-	{
-		double d0 = diag[0], d1 = diag[1], d2 = diag[2], d3 = diag[3], d4 = diag[4], d5 = diag[5], d6 = diag[6],
-		       d7 = diag[7], d8 = diag[8];
-		double c00 = d4 * d8 - d5 * d7, c01 = d2 * d7 - d1 * d8, c02 = d1 * d5 - d2 * d4;
-		double c10 = d5 * d6 - d3 * d8, c11 = d0 * d8 - d2 * d6, c12 = d2 * d3 - d0 * d5;
-		double c20 = d3 * d7 - d4 * d6, c21 = d1 * d6 - d0 * d7, c22 = d0 * d4 - d1 * d3;
-		double det = d0 * c00 + d1 * c10 + d2 * c20;
-		double id = 1.0 / det;
-		double inv[9] = {c00 * id, c01 * id, c02 * id, c10 * id, c11 * id, c12 * id, c20 * id, c21 * id, c22 * id};
-#pragma unroll
-		for (int q = 0; q < 9; ++q) m3[q] = (TV)inv[q];
-		vst(Mv, 3 * i, m3);
-		vst(Mv, 3 * i + 1, m3 + 3);
-		vst(Mv, 3 * i + 2, m3 + 6);
-	}
-	else
-	{
-		m3[0] = (TV)(1.0f / diag[0]);
-		m3[4] = (TV)(1.0f / diag[4]);
-		m3[8] = (TV)(1.0f / diag[8]);
-		const TV md[3] = {m3[0], m3[4], m3[8]};
-		vst(Mv, i, md);
-	}
-	if (!init_pcg) return 0.0;
-	const TV r0 = bv[0], r1 = bv[1], r2 = bv[2];
-	TV sv[3];
-	if (B.precond == B3G_PRECOND_BLOCK_JACOBI)
-	{
-		sv[0] = m3[0] * r0 + m3[1] * r1 + m3[2] * r2;
-		sv[1] = m3[3] * r0 + m3[4] * r1 + m3[5] * r2;
-		sv[2] = m3[6] * r0 + m3[7] * r1 + m3[8] * r2;
-	}
-	else
-	{
-		sv[0] = m3[0] * r0;
-		sv[1] = m3[4] * r1;
-		sv[2] = m3[8] * r2;
-	}
-	const TV zero[3] = {0, 0, 0};
-	vst(vp<TV>(B.r), i, bv);
-	vst(vp<TV>(B.s), i, sv);
-	vst(vp<TV>(B.d), i, sv);
-	vst(vp<TV>(B.py), i, zero);
-	if (B.xff)
-	{
-		const float z[3] = {0.0f, 0.0f, 0.0f};
-		ff_st(B.xff, i, z, z);
-	}
-	return dot3<TV>(bv, sv);
+	return row_finish<TV>(B, i, bi, diag, init_pcg);
 }
 
 // Four consecutive blocks of one lane in one plane, widened to the arithmetic type.

@@ -227,7 +227,7 @@ struct DevBody
 	double* partials;           // reduction scratch of the per-op kernels (kMaxPartials)
 	double* team_partials;      // reduction scratch of the grid team (persistent kernel)
 	int precond;                // b3g_preconditioner
-	int pad_;
+	float tet_ratio;            // lambda / mu when every tetrahedron has the same ratio, else -1
 };
 
 constexpr int kMaxPartials = 4096;
