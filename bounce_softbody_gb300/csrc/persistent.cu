@@ -13,8 +13,13 @@ constexpr int kElemThreads = 256;
 // numbering (elem_off: first element of each body). Its own launch runs at its own register
 // budget (3 CTAs per SM) instead of the 128 registers the row assembly needs: the tetrahedra's
 // rotation extraction, a dependent chain, wants the extra warps. The state it reads was written
-// by earlier launches, so plain (L1) loads.
-__global__ void __launch_bounds__(kElemThreads, 3) k_batch_elements(BatchParams P)
+// by earlier launches, so plain (L1) loads. TETS: every body has tetrahedra only (and no filtered
+// contacts), so only the tetrahedron code is compiled, which fits four CTAs per SM.
+#ifndef B3G_ELEM_TETS_MIN_BLOCKS
+#define B3G_ELEM_TETS_MIN_BLOCKS 4
+#endif
+template <bool TETS>
+__global__ void __launch_bounds__(kElemThreads, TETS ? B3G_ELEM_TETS_MIN_BLOCKS : 3) k_batch_elements(BatchParams P)
 {
 	StepParams sp;
 	sp.h = P.h;
@@ -24,7 +29,7 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_batch_elements(BatchParams 
 		const int b = flat_body(P.elem_off, P.nbodies, g);
 		const DevBody& B = P.bodies[b];
 		int e = (int)(g - __ldg(P.elem_off + b));
-		if (e < B.nt)
+		if (TETS || e < B.nt)
 		{
 			tet_element<LdPlain>(B, e, sp);
 			continue;
@@ -59,16 +64,17 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_batch_elements(BatchParams 
 	}
 }
 
-int elem_grid(unsigned nelem)
+int elem_grid(unsigned nelem, int per_sm)
 {
-	static const int cap = [] {
-		int dev = 0, sms = 0;
+	static const int sms = [] {
+		int dev = 0, n = 0;
 		cudaGetDevice(&dev);
-		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-		return 3 * (sms > 0 ? sms : 1);
+		cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+		return n > 0 ? n : 1;
 	}();
+	const unsigned cap = (unsigned)(per_sm * sms);
 	const unsigned g = (nelem + kElemThreads - 1) / kElemThreads;
-	return (int)(g < (unsigned)cap ? (g > 0 ? g : 1) : cap);
+	return (int)(g < cap ? (g > 0 ? g : 1) : cap);
 }
 
 } // namespace
@@ -114,7 +120,15 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 		if (e != cudaSuccess) return e;
 		if (P.flat)
 		{
-			if (A.nelem > 0) k_batch_elements<<<elem_grid(A.nelem), kElemThreads, 0, st>>>(P);
+			if (A.nelem > 0)
+			{
+				// the batch's elements are all tetrahedra when every body qualifies for the
+				// tetrahedra-only row form
+				if (P.tets_only)
+					k_batch_elements<true><<<elem_grid(A.nelem, B3G_ELEM_TETS_MIN_BLOCKS), kElemThreads, 0, st>>>(P);
+				else
+					k_batch_elements<false><<<elem_grid(A.nelem, 3), kElemThreads, 0, st>>>(P);
+			}
 			e = cudaGetLastError();
 			if (e == cudaSuccess && A.ev_rows) e = cudaEventRecord(A.ev_rows, st);
 			if (e == cudaSuccess)
