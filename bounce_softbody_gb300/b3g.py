@@ -130,6 +130,7 @@ SIGNATURES = {
     "b3g_batch_set_launch_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "b3g_batch_launch_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int]),
     "b3g_batch_element_launch_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "b3g_batch_assembly_split": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
     "b3g_batch_apply_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp]),
     "b3g_batch_get_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp, _fp]),
     "b3g_batch_get_state_async": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, _fp, _fp]),
@@ -534,6 +535,14 @@ def batch_schedule(ctx: Context) -> dict:
     return {"cluster": int(buf[0]), "threshold": int(buf[1]), "cluster_bodies": int(buf[2]),
             "ctas": int(buf[3]), "autotuned": bool(buf[4]), "order": "lpt" if int(buf[6]) else "size",
             "candidates_ms": cands}
+
+
+def batch_assembly_split(ctx: Context) -> dict:
+    """b3g_batch_assembly_split: where the second body group of the split assembly starts."""
+    a = (C.c_uint32 * 4)()
+    _check(load_library().b3g_batch_assembly_split(ctx.handle, a), "b3g_batch_assembly_split")
+    return {"elem_mid": int(a[0]), "slice_mid": int(a[1]), "element_ctas_per_sm": int(a[2]),
+            "row_ctas_per_sm": int(a[3])}
 
 
 def batch_apply_forces(ctx: Context, bodies: Sequence[Body], forces_ptr: int):

@@ -425,6 +425,10 @@ int b3g_context_destroy(b3g_context* c)
 	if (c->ev_snap) cudaEventDestroy(c->ev_snap);
 	if (c->ev_copied) cudaEventDestroy(c->ev_copied);
 	if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+	if (c->side_stream) cudaStreamSynchronize(c->side_stream);
+	if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+	if (c->ev_join) cudaEventDestroy(c->ev_join);
+	if (c->side_stream) cudaStreamDestroy(c->side_stream);
 	if (c->xfer) cudaFree(c->xfer);
 	if (c->xfer_table) cudaFree(c->xfer_table);
 	for (cudaEvent_t& e : c->tev)

@@ -43,6 +43,9 @@ struct b3g_context
 	// asynchronous state reads (b3g_batch_get_state_async): a device snapshot of the bodies' x and
 	// v copied to the host on a second stream, so that the copy overlaps the next step
 	cudaStream_t copy_stream = nullptr;
+	// the batched step's split assembly: a second stream and its fork / join events
+	cudaStream_t side_stream = nullptr;
+	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 	cudaEvent_t ev_snap = nullptr, ev_copied = nullptr;
 	float* snap = nullptr;
 	size_t snap_cap = 0;                 // floats

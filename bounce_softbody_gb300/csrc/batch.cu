@@ -51,6 +51,10 @@ struct BatchCache
 	unsigned long long* d_prof = nullptr;          // phase cycle counters when B3G_PHASE_PROFILE=1
 	unsigned* d_flat_off = nullptr;                 // flat numbering: element offsets, then slice offsets
 	unsigned nelem = 0, nslices = 0;
+	// split assembly: flat element / slice offsets of the first body of group 2 (0: no split),
+	// CTAs per SM of group 2's element launch and of group 1's row launch
+	unsigned elem_mid = 0, slice_mid = 0;
+	int split_elem_per_sm = 0, split_rows_per_sm = 0;
 	int tets_only = 0;   // every body: tetrahedra only, no contact spheres
 	int filter = 0;      // filtered contacts: bodies with contact spheres carry a constraint buffer
 };
@@ -103,6 +107,10 @@ BatchArgs make_args(BatchCache* c, float h, int steps, const b3g_solver_config& 
 	A.nbodies = (int)c->bodies.size();
 	A.tets_only = c->tets_only;
 	A.filter = c->filter;
+	A.elem_mid = c->elem_mid;
+	A.slice_mid = c->slice_mid;
+	A.split_elem_per_sm = c->split_elem_per_sm;
+	A.split_rows_per_sm = c->split_rows_per_sm;
 	return A;
 }
 
@@ -327,6 +335,27 @@ int build_cache(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, int p
 			                    ctx->stream);
 		c->nelem = (unsigned)ne;
 		c->nslices = (unsigned)nsl;
+		// split assembly: group 2 starts at the first body whose elements begin past half of all
+		// elements; its element launch takes one CTA per SM beside two of group 1's row launch
+		// (64 + 2 x 80 registers a thread of 256-thread CTAs fit one SM's register file). Only
+		// for tetrahedra-only batches, whose kernels are that small; B3G_ASM_SPLIT =
+		// "fraction,element CTAs per SM,row CTAs per SM" overrides it, "0" turns it off.
+		const char* se = std::getenv("B3G_ASM_SPLIT");
+		double frac = c->tets_only ? 0.5 : 0.0;
+		int ecta = 1, rcta = 2;
+		if (se) std::sscanf(se, "%lf,%d,%d", &frac, &ecta, &rcta);
+		if (frac > 0.0 && frac < 1.0)
+		{
+			for (uint32_t k = 1; k < count; ++k)
+				if ((double)off[k] >= frac * (double)ne)
+				{
+					c->elem_mid = off[k];
+					c->slice_mid = off[count + 1 + k];
+					break;
+				}
+			c->split_elem_per_sm = std::max(0, ecta);
+			c->split_rows_per_sm = std::max(0, rcta);
+		}
 	}
 	if (e == cudaSuccess && count)
 		e = cudaMemcpyAsync(c->d_bodies, h.data(), count * sizeof(DevBody), cudaMemcpyHostToDevice, ctx->stream);
@@ -454,6 +483,18 @@ extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_
 		}
 	}
 	BatchArgs A = make_args(c, dt, 1, cfg);
+	if (c->elem_mid > 0 && A.newton == 1)
+	{
+		// the split assembly's second stream and fork / join events, made once per context
+		cudaError_t e = cudaSuccess;
+		if (!ctx->side_stream) e = cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking);
+		if (e == cudaSuccess && !ctx->ev_fork) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+		if (e == cudaSuccess && !ctx->ev_join) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
+		if (e != cudaSuccess) return cuda_fail(e, "split assembly stream");
+		A.side = ctx->side_stream;
+		A.ev_fork = ctx->ev_fork;
+		A.ev_join = ctx->ev_join;
+	}
 	if (ctx->launch_timing && A.newton == 1)
 	{
 		// timed steps: the two launches of each step bracketed by events, no graph
@@ -463,7 +504,7 @@ extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_
 		{
 			cudaError_t e = cudaEventRecord(ctx->tev[0], st);
 			A.part = 1;
-			A.ev_rows = ctx->tev[3];
+			A.ev_rows = A.side ? nullptr : ctx->tev[3];  // no single element/row boundary when split
 			if (e == cudaSuccess) e = op_batch(A, st);
 			A.ev_rows = nullptr;
 			if (e == cudaSuccess) e = cudaEventRecord(ctx->tev[1], st);
@@ -475,7 +516,7 @@ extern "C" int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_
 			float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f;
 			cudaEventElapsedTime(&m1, ctx->tev[0], ctx->tev[1]);
 			cudaEventElapsedTime(&m2, ctx->tev[1], ctx->tev[2]);
-			cudaEventElapsedTime(&m3, ctx->tev[0], ctx->tev[3]);
+			if (!A.side) cudaEventElapsedTime(&m3, ctx->tev[0], ctx->tev[3]);
 			ctx->t_assembly_ms += m1;
 			ctx->t_elements_ms += m3;
 			ctx->t_pcg_ms += m2;
@@ -543,6 +584,18 @@ extern "C" int b3g_batch_element_launch_ms(b3g_context* ctx, double* out)
 {
 	if (!ctx || !out) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
 	*out = ctx->t_elements_ms;
+	return B3G_OK;
+}
+
+extern "C" int b3g_batch_assembly_split(b3g_context* ctx, uint32_t out[4])
+{
+	if (!ctx || !out) return fail(B3G_ERROR_INVALID_ARGUMENT, "null argument");
+	if (!ctx->batch) return fail(B3G_ERROR_INVALID_ARGUMENT, "no batch has been stepped on this context");
+	const BatchCache* c = ctx->batch;
+	out[0] = c->elem_mid;
+	out[1] = c->slice_mid;
+	out[2] = (uint32_t)c->split_elem_per_sm;
+	out[3] = (uint32_t)c->split_rows_per_sm;
 	return B3G_OK;
 }
 

@@ -114,6 +114,14 @@ struct BatchArgs
 	int tets_only = 0;       // every body has tetrahedra only and no contact spheres
 	int filter = 0;          // filtered contacts: bodies with a filt buffer; their vertices follow
 	                         // their elements in the flat element numbering
+	// Split assembly (side stream set): bodies below the flat element offset elem_mid (slice
+	// offset slice_mid) form group 1, the rest group 2; group 2's elements run on `side`,
+	// forked and joined through ev_fork / ev_join, concurrently with group 1's rows. CTAs per SM
+	// of the element and row launches (0: their defaults).
+	cudaStream_t side = nullptr;
+	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+	unsigned elem_mid = 0, slice_mid = 0;
+	int split_elem_per_sm = 0, split_rows_per_sm = 0;
 };
 cudaError_t op_batch(const BatchArgs& A, cudaStream_t st);
 // Co-resident clusters of the batch kernel for this precision and cluster size (0 on error).

@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(kElemThreads, TETS ? B3G_ELEM_TETS_MIN_BLOCKS 
 	StepParams sp;
 	sp.h = P.h;
 	sp.first_newton = 1;
-	for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < P.nelem; g += gridDim.x * blockDim.x)
+	for (unsigned g = P.g_begin + blockIdx.x * blockDim.x + threadIdx.x; g < P.nelem; g += gridDim.x * blockDim.x)
 	{
 		const int b = flat_body(P.elem_off, P.nbodies, g);
 		const DevBody& B = P.bodies[b];
@@ -110,6 +110,9 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 	P.nbodies = A.nbodies;
 	P.tets_only = A.tets_only;
 	P.filter = A.filter;
+	P.g_begin = 0;
+	P.s_begin = 0;
+	P.rows_per_sm = 0;
 	// a single Newton iteration with the flat numbering: elements and rows in two flat launches,
 	// then the PCG launch (which knows from `flat` to sum delta0 itself)
 	P.flat = (P.newton == 1 && A.elem_off && A.slice_off && A.nslices > 0) ? 1 : 0;
@@ -120,20 +123,46 @@ cudaError_t op_batch(const BatchArgs& A, cudaStream_t st)
 		if (e != cudaSuccess) return e;
 		if (P.flat)
 		{
-			if (A.nelem > 0)
-			{
-				// the batch's elements are all tetrahedra when every body qualifies for the
-				// tetrahedra-only row form
-				if (P.tets_only)
-					k_batch_elements<true><<<elem_grid(A.nelem, B3G_ELEM_TETS_MIN_BLOCKS), kElemThreads, 0, st>>>(P);
+			// the batch's elements are all tetrahedra when every body qualifies for the
+			// tetrahedra-only row form
+			auto elements = [&](const BatchParams& Q, int per_sm, cudaStream_t s) -> cudaError_t {
+				const unsigned count = Q.nelem - Q.g_begin;
+				if (count == 0) return cudaSuccess;
+				if (Q.tets_only)
+					k_batch_elements<true><<<elem_grid(count, per_sm > 0 ? per_sm : B3G_ELEM_TETS_MIN_BLOCKS), kElemThreads, 0, s>>>(Q);
 				else
-					k_batch_elements<false><<<elem_grid(A.nelem, 3), kElemThreads, 0, st>>>(P);
+					k_batch_elements<false><<<elem_grid(count, per_sm > 0 ? per_sm : 3), kElemThreads, 0, s>>>(Q);
+				return cudaGetLastError();
+			};
+			auto rows = [&](const BatchParams& Q, cudaStream_t s) -> cudaError_t {
+				return A.prec == kP64 ? launch_rows_f64(Q, s) : (A.prec == kPBF ? launch_rows_bf16(Q, s) : launch_rows_f32(Q, s));
+			};
+			if (A.side && A.elem_mid > 0 && A.elem_mid < A.nelem && A.slice_mid > 0 && A.slice_mid < A.nslices)
+			{
+				// two body groups: group 1's elements alone, then group 2's elements on the side
+				// stream while group 1's rows run here (an ALU-bound and a latency-bound launch
+				// sharing the SMs), then group 2's rows
+				BatchParams E1 = P, E2 = P, R1 = P, R2 = P;
+				E1.nelem = A.elem_mid;
+				E2.g_begin = A.elem_mid;
+				R1.nslices = A.slice_mid;
+				R2.s_begin = A.slice_mid;
+				R1.rows_per_sm = A.split_rows_per_sm;
+				e = elements(E1, 0, st);
+				if (e == cudaSuccess) e = cudaEventRecord(A.ev_fork, st);
+				if (e == cudaSuccess) e = cudaStreamWaitEvent(A.side, A.ev_fork, 0);
+				if (e == cudaSuccess) e = elements(E2, A.split_elem_per_sm, A.side);
+				if (e == cudaSuccess) e = cudaEventRecord(A.ev_join, A.side);
+				if (e == cudaSuccess) e = rows(R1, st);
+				if (e == cudaSuccess) e = cudaStreamWaitEvent(st, A.ev_join, 0);
+				if (e == cudaSuccess) e = rows(R2, st);
 			}
-			e = cudaGetLastError();
-			if (e == cudaSuccess && A.ev_rows) e = cudaEventRecord(A.ev_rows, st);
-			if (e == cudaSuccess)
-				e = A.prec == kP64 ? launch_rows_f64(P, st)
-				                   : (A.prec == kPBF ? launch_rows_bf16(P, st) : launch_rows_f32(P, st));
+			else
+			{
+				e = elements(P, 0, st);
+				if (e == cudaSuccess && A.ev_rows) e = cudaEventRecord(A.ev_rows, st);
+				if (e == cudaSuccess) e = rows(P, st);
+			}
 			if (e != cudaSuccess || A.part == 1) return e;
 		}
 	}

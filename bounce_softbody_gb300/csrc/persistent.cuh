@@ -23,6 +23,7 @@
 #include <atomic>
 #include <cooperative_groups.h>
 #include <type_traits>
+#include <utility>
 
 namespace cg = cooperative_groups;
 
@@ -54,6 +55,11 @@ struct BatchParams
 	int nbodies;
 	int tets_only;   // every body: tetrahedra only, no contact spheres (the row assembly's short form)
 	int filter;      // filtered contacts: bodies with a constraint buffer (filt) are stepped in that mode
+	// flat launches over part of the numbering: elements [g_begin, nelem), slices [s_begin,
+	// nslices); rows_per_sm > 0 caps the row launch at that many CTAs per SM (0: all resident)
+	unsigned g_begin;
+	unsigned s_begin;
+	int rows_per_sm;
 };
 
 namespace {
@@ -760,7 +766,7 @@ k_batch_rows(BatchParams P)
 	sp.h = P.h;
 	sp.first_newton = 1;
 	const unsigned nw = gridDim.x * kRowsWarps;
-	for (unsigned g = blockIdx.x * kRowsWarps + (threadIdx.x >> 5); g < P.nslices; g += nw)
+	for (unsigned g = P.s_begin + blockIdx.x * kRowsWarps + (threadIdx.x >> 5); g < P.nslices; g += nw)
 	{
 		const int b = flat_body(P.slice_off, P.nbodies, g);
 		__syncwarp();
@@ -779,15 +785,16 @@ k_batch_rows(BatchParams P)
 template <class TA, class TV, bool TETS, bool FILT>
 cudaError_t launch_rows_t(const BatchParams& P, cudaStream_t st)
 {
-	static const int resident = [] {
+	static const std::pair<int, int> resident = [] {  // SMs, resident CTAs per SM
 		int dev = 0, sms = 0, per_sm = 0;
 		cudaGetDevice(&dev);
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_rows<TA, TV, TETS, FILT>, B3G_ROWS_THREADS, 0);
-		return std::max(1, sms * std::max(per_sm, 1));
+		return std::make_pair(std::max(1, sms), std::max(per_sm, 1));
 	}();
-	const unsigned need = (P.nslices + kRowsWarps - 1) / kRowsWarps;
-	const int grid = (int)std::max(1u, std::min(need, (unsigned)resident));
+	const int cap = resident.first * (P.rows_per_sm > 0 ? std::min(P.rows_per_sm, resident.second) : resident.second);
+	const unsigned need = (P.nslices - P.s_begin + kRowsWarps - 1) / kRowsWarps;
+	const int grid = (int)std::max(1u, std::min(need, (unsigned)cap));
 	k_batch_rows<TA, TV, TETS, FILT><<<grid, B3G_ROWS_THREADS, 0, st>>>(P);
 	return cudaGetLastError();
 }

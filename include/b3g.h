@@ -279,6 +279,12 @@ B3G_API int b3g_step_batch_noalloc(b3g_context* ctx, b3g_body* const* bodies, ui
  * candidate (code = order * 1e8 + cluster * 1e6 + threshold, microseconds). */
 B3G_API int b3g_batch_schedule(b3g_context* ctx, int32_t* out, uint32_t capacity);
 
+/* Split assembly of the context's current batch (single Newton iteration, tetrahedra-only
+ * bodies): the flat element and row-slice offsets where the second body group starts (0 = no
+ * split), the CTAs per SM of that group's element launch, which runs on a second stream beside
+ * the first group's row launch, and of that row launch. */
+B3G_API int b3g_batch_assembly_split(b3g_context* ctx, uint32_t out[4]);
+
 /* Cycles spent per phase of the batch kernel, summed over CTAs (elements, assembly, SpMV, update,
  * direction, final update, -, -). Only counted when the environment variable B3G_PHASE_PROFILE=1
  * is set when the batch is first stepped; zeros otherwise. reset != 0 clears the counters. */

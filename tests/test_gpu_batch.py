@@ -98,6 +98,31 @@ def test_batch_is_deterministic(ctx, cluster_env, monkeypatch):
         assert np.array_equal(x1, x2) and np.array_equal(v1, v2)
 
 
+@pytest.mark.parametrize("split", ["0.5,1,2", "0.3,2,1"])
+def test_split_assembly_is_bitwise_equal(ctx, split, monkeypatch):
+    """The split assembly (the second body group's element launch on a second stream beside the
+    first group's row launch) computes every element and row exactly as the two whole-batch
+    launches do: bitwise equal states after several steps, graph-replayed and timed."""
+    monkeypatch.setenv("B3G_AUTOTUNE", "0")
+    descs = small_batch(count=12, seed=29)
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    out = []
+    for env, timed in (("0", False), (split, False), (split, True)):
+        monkeypatch.setenv("B3G_ASM_SPLIT", env)
+        bodies = [b3g.Body(ctx, d) for d in descs]
+        b3g.batch_set_launch_timing(ctx, timed)
+        b3g.step_batch(ctx, bodies, DT, 4, cfg, stats=False)
+        b3g.batch_set_launch_timing(ctx, False)
+        sp = b3g.batch_assembly_split(ctx)
+        assert (sp["elem_mid"] > 0) == (env != "0") and (sp["slice_mid"] > 0) == (env != "0")
+        out.append([b.state() for b in bodies])
+        for b in bodies:
+            b.close()
+    for run in out[1:]:
+        for (x1, v1), (x2, v2) in zip(out[0], run):
+            assert np.array_equal(x1, x2) and np.array_equal(v1, v2)
+
+
 def test_launch_timing_mode_same_results(ctx):
     """Timed batched steps (direct launches with events around the assembly and PCG launches)
     compute exactly what the graph-replayed steps compute, and report positive launch times."""
