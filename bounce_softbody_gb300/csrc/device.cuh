@@ -1435,6 +1435,10 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 					ua[u] = L::ld(r0 + ((cd[u] >> 2) & 3u) * nt);
 					ub[u] = L::ld(r0 + (cd[u] & 3u) * nt);
 				}
+			// the codes of the slot's next four contributions, while these records load
+			uint32_t nx[4];
+#pragma unroll
+			for (int u = 0; u < 4; ++u) nx[u] = 4 + u < cnt ? __ldg(B.tet_clist + st + kSlice * (4 + u)) : 0u;
 			if (k + 1 < w)
 			{
 #pragma unroll
@@ -1452,38 +1456,32 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 				for (int u = 0; u < 4; ++u)
 					if (u < cnt) add_tet_block(a, ua[u], ub[u]);
 			}
-			// the rest of the slot's contributions, four in flight at a time
-			int t = 4;
-			for (; t + 4 <= cnt; t += 4)
+			// the rest of the slot's contributions, four in flight at a time (the last group
+			// partial), each group's codes loaded with the group before
+			for (int t = 4; t < cnt; t += 4)
 			{
-				uint32_t code[4];
-#pragma unroll
-				for (int u = 0; u < 4; ++u) code[u] = __ldg(B.tet_clist + st + kSlice * (t + u));
 #pragma unroll
 				for (int u = 0; u < 4; ++u)
-				{
-					const float4* r0 = B.tet_rec + (code[u] >> 4);
-					ua[u] = L::ld(r0 + ((code[u] >> 2) & 3u) * nt);
-					ub[u] = L::ld(r0 + (code[u] & 3u) * nt);
-				}
+					if (t + u < cnt)
+					{
+						const float4* r0 = B.tet_rec + (nx[u] >> 4);
+						ua[u] = L::ld(r0 + ((nx[u] >> 2) & 3u) * nt);
+						ub[u] = L::ld(r0 + (nx[u] & 3u) * nt);
+					}
+#pragma unroll
+				for (int u = 0; u < 4; ++u) nx[u] = t + 4 + u < cnt ? __ldg(B.tet_clist + st + kSlice * (t + 4 + u)) : 0u;
 				if (uniform)
 				{
 #pragma unroll
-					for (int u = 0; u < 4; ++u) add_outer(a, ua[u], ub[u]);
+					for (int u = 0; u < 4; ++u)
+						if (t + u < cnt) add_outer(a, ua[u], ub[u]);
 				}
 				else
 				{
 #pragma unroll
-					for (int u = 0; u < 4; ++u) add_tet_block(a, ua[u], ub[u]);
+					for (int u = 0; u < 4; ++u)
+						if (t + u < cnt) add_tet_block(a, ua[u], ub[u]);
 				}
-			}
-			for (; t < cnt; ++t)
-			{
-				const uint32_t code = __ldg(B.tet_clist + st + kSlice * t);
-				const float4* r0 = B.tet_rec + (code >> 4);
-				const float4 u0 = L::ld(r0 + ((code >> 2) & 3u) * nt), u1 = L::ld(r0 + (code & 3u) * nt);
-				if (uniform) add_outer(a, u0, u1);
-				else add_tet_block(a, u0, u1);
 			}
 			if (uniform)
 			{
