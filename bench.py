@@ -209,11 +209,14 @@ def final_bytes(info):
 
 
 def assembly_bytes(info):
-    """Element phase and row assembly of one step (first touch of every array, FP32)."""
+    """Element phase and row assembly of one step (first touch of every array, FP32; the
+    precomputed contribution lists are not counted)."""
     n, nt, nnzb = info["vertices"], info["tets"], info["nnzb"]
     tets = nt * (16 + 36 + 16 + 16 + 16 + 64 + 48)     # ids, invE, material, q r/w, records, rhs parts
     gathers = n * (12 * 4)                             # x, v, translation, fext
-    rows = 40 * nnzb + 16 * nt * 4 + nt * 4 * 4 + n * (4 + 4 + 1 + 12) + n * 12 * 7
+    # blocks written and column ids; each tetrahedron's four records (16 B) and four
+    # right-hand-side parts (12 B) read by its vertices' rows; vertex terms and the six vectors
+    rows = 40 * nnzb + nt * 4 * 16 + nt * 4 * 12 + n * (4 + 4 + 1 + 12) + n * 12 * 7
     return tets + gathers + rows
 
 
