@@ -340,8 +340,9 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(DevBody B, const TA* A)
 }
 
 // d' = s + beta d (d' = s on a solve's first iteration), q = A d' and alpha = delta / d'.q.
-// Reads the direction from B.d and writes the new one to B.d2; the host swaps the two buffers
-// every iteration.
+// q is formed by linearity, q = A s + beta q (the previous q, which is A d): the SpMV gathers only
+// s, and each row updates its own d and q. Reads the direction from B.d and writes the new one to
+// B.d2; the host swaps the two buffers every iteration.
 #ifndef B3G_SPMV_MIN_BLOCKS
 #define B3G_SPMV_MIN_BLOCKS 4   // 64 registers: 4 CTAs (32 warps) per SM hide more gather latency
 #endif
@@ -359,7 +360,20 @@ __global__ void __launch_bounds__(kThreads, B3G_SPMV_MIN_BLOCKS) k_dir_spmv_dot(
 		if (i >= B.n) continue;
 		const int base = B.slice_ptr[sl], w = (B.slice_ptr[sl + 1] - base) / kSlice;
 		TV o[3], dn[3];
-		spmv_row_dir<TA, TV>(A, B.col, B.nslots, base, w, lane, (const TV*)B.s, (const TV*)B.d, beta, first, o, dn);
+		spmv_row<TA, TV>(A, B.col, B.nslots, base, w, lane, (const TV*)B.s, o);
+		vld<TV, LdPlain>((const TV*)B.s, i, dn);
+		if (!first)
+		{
+			TV dp[3], qp[3];
+			vld<TV, LdPlain>((const TV*)B.d, i, dp);
+			vld<TV, LdPlain>((const TV*)B.q, i, qp);
+#pragma unroll
+			for (int c = 0; c < 3; ++c)
+			{
+				dn[c] = dn[c] + beta * dp[c];
+				o[c] = o[c] + beta * qp[c];
+			}
+		}
 		vst((TV*)B.q, i, o);
 		vst((TV*)B.d2, i, dn);
 		part += dot3<TV>(dn, o);
