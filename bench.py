@@ -459,9 +459,10 @@ def ours(args, world, rank, local, pg):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
         def e2e_step():
-            # inputs up, the step, then the results read back on the context's second stream: the
-            # copy of step k overlaps step k + 1 (the host arrays of step k are complete when the
-            # next read is queued; every copy is complete when the timed region ends)
+            # inputs up on the context's upload stream (the copy for step k overlaps step k - 1),
+            # the step, then the results read back on its second stream: the copy of step k
+            # overlaps step k + 1 (the host arrays of step k are complete when the next read is
+            # queued; every copy is complete when the timed region ends)
             b3g.batch_apply_forces(ctx, bodies, f_h.data_ptr())
             step_once()
             b3g.batch_get_state_async(ctx, bodies, x_h.data_ptr(), v_h.data_ptr())
@@ -487,6 +488,7 @@ def ours(args, world, rank, local, pg):
         e2e_ok = bool(np.array_equal(x_h[:3 * infos[0]["vertices"]].numpy().reshape(-1, 3), x_chk))
         extras["e2e"] = {"value": nverts * args.steps / (e2e_ms / 1e3), "unit": "vertex-steps/s",
                          "h2d_bytes_per_step": 12 * nverts, "d2h_bytes_per_step": 24 * nverts,
+                         "upload": "upload stream, overlapping the step before",
                          "read_back": "second stream, overlapping the next step", "host_arrays_match": e2e_ok}
         # plain one-body-at-a-time GPU path (per-op kernels) on a size-stratified sample
         sample = sorted(range(len(bodies)), key=lambda k: -infos[k]["vertices"])[::16] if len(bodies) > 16 else list(

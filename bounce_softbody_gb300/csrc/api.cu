@@ -425,6 +425,14 @@ int b3g_context_destroy(b3g_context* c)
 	if (c->ev_snap) cudaEventDestroy(c->ev_snap);
 	if (c->ev_copied) cudaEventDestroy(c->ev_copied);
 	if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+	if (c->up_stream) cudaStreamSynchronize(c->up_stream);
+	for (int k = 0; k < 2; ++k)
+	{
+		if (c->ev_up_copied[k]) cudaEventDestroy(c->ev_up_copied[k]);
+		if (c->ev_up_used[k]) cudaEventDestroy(c->ev_up_used[k]);
+	}
+	if (c->up_buf) cudaFree(c->up_buf);
+	if (c->up_stream) cudaStreamDestroy(c->up_stream);
 	if (c->side_stream) cudaStreamSynchronize(c->side_stream);
 	if (c->ev_fork) cudaEventDestroy(c->ev_fork);
 	if (c->ev_join) cudaEventDestroy(c->ev_join);
@@ -450,6 +458,7 @@ int b3g_context_synchronize(b3g_context* c)
 {
 	if (!c) return fail(B3G_ERROR_INVALID_ARGUMENT, "null context");
 	cudaError_t e = cudaStreamSynchronize(c->stream);
+	if (e == cudaSuccess && c->up_stream) e = cudaStreamSynchronize(c->up_stream);
 	if (e == cudaSuccess && c->copy_stream)
 	{
 		e = cudaStreamSynchronize(c->copy_stream);

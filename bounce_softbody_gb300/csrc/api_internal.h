@@ -43,6 +43,15 @@ struct b3g_context
 	// asynchronous state reads (b3g_batch_get_state_async): a device snapshot of the bodies' x and
 	// v copied to the host on a second stream, so that the copy overlaps the next step
 	cudaStream_t copy_stream = nullptr;
+	// overlapped force uploads from page-locked host arrays: an upload stream, two device staging
+	// buffers taken in turn (up_cap floats each), and per buffer the events "copied" (upload
+	// stream) and "consumed" (context stream, after the scatter that reads it)
+	cudaStream_t up_stream = nullptr;
+	float* up_buf = nullptr;
+	size_t up_cap = 0;
+	cudaEvent_t ev_up_copied[2] = {nullptr, nullptr}, ev_up_used[2] = {nullptr, nullptr};
+	bool up_used_pending[2] = {false, false};
+	int up_next = 0;
 	// the batched step's split assembly: a second stream and its fork / join events
 	cudaStream_t side_stream = nullptr;
 	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;

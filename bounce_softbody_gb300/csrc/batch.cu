@@ -695,10 +695,53 @@ extern "C" int b3g_batch_apply_forces(b3g_context* ctx, b3g_body* const* bodies,
 	int rc = prepare_xfer(ctx, bodies, count, 2);
 	if (rc != B3G_OK) return rc;
 	cudaStream_t st = ctx->stream;
-	// page-locked host memory: one launch reads it directly and adds every body's slice to its
-	// fext; otherwise one copy of the whole array into the staging buffer first
 	cudaError_t e = cudaSuccess;
 	const float* src = mapped_host(forces, ctx->xfer_total);
+	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+	if (src) e = cudaStreamIsCapturing(st, &cap);
+	if (e != cudaSuccess) return cuda_fail(e, "batch_apply_forces");
+	if (src && cap == cudaStreamCaptureStatusNone)
+	{
+		// page-locked host memory: the array is copied on the upload stream into one of two
+		// staging buffers as soon as that buffer's previous scatter has run, so the copy overlaps
+		// whatever the context stream is doing (the step before); the context stream waits for
+		// the copy and adds every body's slice to its fext
+		const size_t total = ctx->xfer_total;
+		if (total > ctx->up_cap)
+		{
+			if (ctx->up_stream) e = cudaStreamSynchronize(ctx->up_stream);
+			if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+			if (ctx->up_buf) cudaFree(ctx->up_buf);
+			ctx->up_buf = nullptr;
+			ctx->up_cap = 0;
+			ctx->up_used_pending[0] = ctx->up_used_pending[1] = false;
+			if (e == cudaSuccess) e = cudaMalloc(&ctx->up_buf, 2 * total * sizeof(float));
+			if (e != cudaSuccess) return cuda_fail(e, "force upload buffers");
+			ctx->up_cap = total;
+		}
+		if (!ctx->up_stream) e = cudaStreamCreateWithFlags(&ctx->up_stream, cudaStreamNonBlocking);
+		for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+		{
+			if (!ctx->ev_up_copied[k]) e = cudaEventCreateWithFlags(&ctx->ev_up_copied[k], cudaEventDisableTiming);
+			if (e == cudaSuccess && !ctx->ev_up_used[k])
+				e = cudaEventCreateWithFlags(&ctx->ev_up_used[k], cudaEventDisableTiming);
+		}
+		if (e != cudaSuccess) return cuda_fail(e, "force upload stream");
+		const int k = ctx->up_next;
+		ctx->up_next ^= 1;
+		float* buf = ctx->up_buf + (size_t)k * ctx->up_cap;
+		if (ctx->up_used_pending[k]) e = cudaStreamWaitEvent(ctx->up_stream, ctx->ev_up_used[k], 0);
+		if (e == cudaSuccess)
+			e = cudaMemcpyAsync(buf, forces, total * sizeof(float), cudaMemcpyHostToDevice, ctx->up_stream);
+		if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_up_copied[k], ctx->up_stream);
+		if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->ev_up_copied[k], 0);
+		if (e == cudaSuccess) e = op_batch_scatter_add(ctx->xfer_table, count, ctx->xfer_max_n3, buf, st);
+		if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_up_used[k], st);
+		ctx->up_used_pending[k] = e == cudaSuccess;
+		return e == cudaSuccess ? B3G_OK : cuda_fail(e, "batch_apply_forces");
+	}
+	// pageable memory: one copy of the whole array into the staging buffer first; a stream being
+	// captured: one launch reads the page-locked array directly
 	if (!src)
 	{
 		e = cudaMemcpyAsync(ctx->xfer, forces, ctx->xfer_total * sizeof(float), cudaMemcpyHostToDevice, st);

@@ -303,7 +303,10 @@ B3G_API int b3g_batch_element_launch_ms(b3g_context* ctx, double* out);
 
 /* Host-buffer transfers for a list of bodies of one context; the host arrays are the bodies'
  * arrays concatenated in list order (3 floats per vertex). Pinned host memory makes them
- * asynchronous copies; get waits for the copies. */
+ * asynchronous copies; get waits for the copies. apply_forces from pinned memory copies on an
+ * upload stream of the context into one of two device buffers taken in turn, so the copy
+ * overlaps the step queued before it; the host array must stay unchanged until the step queued
+ * after the call has completed (or b3g_context_synchronize). */
 B3G_API int b3g_batch_apply_forces(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, const float* forces);
 B3G_API int b3g_batch_get_state(b3g_context* ctx, b3g_body* const* bodies, uint32_t count, float* positions,
                                 float* velocities);

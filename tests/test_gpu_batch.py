@@ -145,6 +145,39 @@ def test_launch_timing_mode_same_results(ctx):
         b.close()
 
 
+def test_queued_force_uploads_overlap_and_match(ctx):
+    """Page-locked force arrays are copied on the context's upload stream into two staging
+    buffers taken in turn, overlapping the step queued before. Five steps queued without any
+    synchronisation, each with its own forces, end bitwise where the per-body calls take the
+    same bodies."""
+    torch = pytest.importorskip("torch")
+    descs = meshes.batch_bodies(count=6, lo=3, hi=9, seed=31)
+    cfg = b3g.solver_config()
+    rng = np.random.default_rng(5)
+    nsteps = 5
+    a = [b3g.Body(ctx, d) for d in descs]
+    b = [b3g.Body(ctx, d) for d in descs]
+    total = sum(x.n for x in a)
+    forces = [rng.uniform(-2.0, 2.0, 3 * total).astype(np.float32) for _ in range(nsteps)]
+    pinned = [torch.from_numpy(f.copy()).pin_memory() for f in forces]
+    for p in pinned:
+        b3g.batch_apply_forces(ctx, a, p.data_ptr())
+        b3g.step_batch(ctx, a, DT, 1, cfg, stats=False)
+    for f in forces:
+        off = 0
+        for body in b:
+            body.apply_forces(f[off:off + 3 * body.n].reshape(body.n, 3))
+            off += 3 * body.n
+        b3g.step_batch(ctx, b, DT, 1, cfg, stats=False)
+    ctx.synchronize()
+    for x, y in zip(a, b):
+        xa, va = x.state()
+        xb, vb = y.state()
+        assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    for body in a + b:
+        body.close()
+
+
 @pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "page_locked"])
 def test_batch_host_transfers_match_per_body_calls(ctx, pinned):
     """b3g_batch_apply_forces / b3g_batch_get_state (one launch each way over a cached body
