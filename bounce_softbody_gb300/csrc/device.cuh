@@ -1397,10 +1397,9 @@ __device__ __forceinline__ double assemble_row(const DevBody& B, int slice, int 
 	float3 bz = f3(0.0f, 0.0f, 0.0f);  // (A z)_i
 
 	float diag[9];
-	double rsd = 0.0;  // r.s of the row (unfiltered form: from the k = 0 slot)
-	// Slot pipeline: the list header of the slot after next and the next slot's first four
-	// tetrahedron codes load while this slot's records are gathered, so a slot waits on one
-	// gather instead of three dependent loads. Contributions are added in list order.
+	// Slot pipeline: the next slot's list header and its first four tetrahedron codes load while
+	// this slot's records are gathered, so a slot waits on one gather instead of three dependent
+	// loads. Contributions are added in list order.
 	uint32_t st_n = __ldg(B.tet_cstart + base + lane);
 	int cnt_n = __ldg(B.tet_ccnt + base + lane);
 	uint32_t cd_n[4];

@@ -157,6 +157,45 @@ def test_rotations_roundtrip_and_determinism(ctx):
     g.close()
 
 
+def _quat_mat(q):
+    x, y, z, w = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
+def test_rotations_come_back_in_element_order(ctx):
+    """Tetrahedra are stored grouped by vertex-offset signature, not in the caller's order; the
+    rotations read back are in the caller's order. The tetrahedra of a block are shuffled, the
+    body steps (the last step extracts each rotation from the deformation gradient of the state
+    it starts from), and every returned rotation is the polar rotation of its own tetrahedron's
+    gradient (numpy SVD), to the float tolerance of the iteration."""
+    desc = meshes.tet_grid(6, 5, 7, seed=4, pin="y0")
+    rng = np.random.default_rng(2)
+    perm = rng.permutation(desc.tets.shape[0])
+    for k in ("tets", "tet_E", "tet_nu", "tet_kdamp", "tet_density"):
+        setattr(desc, k, np.asarray(getattr(desc, k))[perm].copy())
+    cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
+    g = b3g.Body(ctx, desc)
+    for _ in range(3):
+        g.step(DT, cfg)
+    x, _ = g.state()
+    g.step(DT, cfg)
+    q = g.rotations()
+    rest = np.asarray(desc.x, np.float64)
+    cur = np.asarray(x, np.float64)
+    worst = 0.0
+    for e, t in enumerate(np.asarray(desc.tets)):
+        Dm = np.stack([rest[t[k]] - rest[t[0]] for k in (1, 2, 3)], axis=1)
+        Ds = np.stack([cur[t[k]] - cur[t[0]] for k in (1, 2, 3)], axis=1)
+        F = Ds @ np.linalg.inv(Dm)
+        U, _, Vt = np.linalg.svd(F)
+        R = U @ Vt
+        worst = max(worst, float(np.abs(_quat_mat(q[e]) - R).max()))
+    assert worst < 1e-4, worst
+    g.close()
+
+
 def test_nonfinite_input_reports_status(ctx):
     """A NaN external force makes the solve report NONFINITE instead of failing silently."""
     desc = meshes.tet_grid(4, 4, 4, seed=1, pin="y0")
