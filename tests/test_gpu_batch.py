@@ -98,13 +98,25 @@ def test_batch_is_deterministic(ctx, cluster_env, monkeypatch):
         assert np.array_equal(x1, x2) and np.array_equal(v1, v2)
 
 
-@pytest.mark.parametrize("split", ["0.5,1,2", "0.3,2,1"])
-def test_split_assembly_is_bitwise_equal(ctx, split, monkeypatch):
+def mixed_bodies():
+    """Every element kind: tetrahedra; membrane triangles and springs with sphere contact;
+    Baraff-Witkin stretch and shear with a mouse spring."""
+    return [meshes.batch_bodies(count=1, lo=6, hi=9, seed=21)[0],
+            meshes.cloth_grid(12, side=1.2, height=0.56, sphere_radius=0.5, contact_radius=0.05),
+            meshes.bw_cloth(8, pinned="edges", stretch_ks=5e4, shear_ks=1e3, shear_kd=10.0, mouse=True),
+            meshes.batch_bodies(count=1, lo=10, hi=14, seed=22)[0]]
+
+
+@pytest.mark.parametrize("split,mixed", [("0.5,1,2", False), ("0.3,2,1", False), ("0.1,1,2", True)],
+                         ids=["tets-half", "tets-third", "mixed-kinds"])
+def test_split_assembly_is_bitwise_equal(ctx, split, mixed, monkeypatch):
     """The split assembly (the second body group's element launch on a second stream beside the
     first group's row launch) computes every element and row exactly as the two whole-batch
-    launches do: bitwise equal states after several steps, graph-replayed and timed."""
+    launches do: bitwise equal states after several steps, graph-replayed and timed. Batches of
+    tetrahedra only split by default; a batch of mixed element kinds only when asked to, which
+    it then also handles."""
     monkeypatch.setenv("B3G_AUTOTUNE", "0")
-    descs = small_batch(count=12, seed=29)
+    descs = mixed_bodies() if mixed else small_batch(count=12, seed=29)
     cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
     out = []
     for env, timed in (("0", False), (split, False), (split, True)):
@@ -249,10 +261,7 @@ def test_mixed_batch_matches_oracle(ctx):
     contact; Baraff-Witkin stretch and shear with a mouse spring): the flat element launch
     dispatches each body's elements by kind over one numbering, the flat row launch serves slices
     of all of them; each body against the FP64 oracle within 20x the oracle's own FP32 spread."""
-    descs = [meshes.batch_bodies(count=1, lo=6, hi=9, seed=21)[0],
-             meshes.cloth_grid(12, side=1.2, height=0.56, sphere_radius=0.5, contact_radius=0.05),
-             meshes.bw_cloth(8, pinned="edges", stretch_ks=5e4, shear_ks=1e3, shear_kd=10.0, mouse=True),
-             meshes.batch_bodies(count=1, lo=10, hi=14, seed=22)[0]]
+    descs = mixed_bodies()
     steps = 4
     cfg = b3g.solver_config(max_pcg_iterations=200, pcg_tolerance=1e-5)
     bodies = [b3g.Body(ctx, d) for d in descs]
