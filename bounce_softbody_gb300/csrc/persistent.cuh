@@ -64,14 +64,12 @@ struct BatchParams
 
 namespace {
 
+// resident CTAs per SM the team assembly's register budget is sized for (128 registers a thread)
 #ifndef B3G_BATCH_MIN_BLOCKS
-#define B3G_BATCH_MIN_BLOCKS 2   // resident CTAs per SM the register budget is sized for
+#define B3G_BATCH_MIN_BLOCKS (B3G_PCG_THREADS >= 512 ? 1 : 2)
 #endif
 
-#ifndef B3G_PCG_THREADS
-#define B3G_PCG_THREADS 256      // threads per CTA of the team launches
-#endif
-constexpr int kPThreads = B3G_PCG_THREADS;
+constexpr int kPThreads = B3G_PCG_THREADS;  // ops.h
 constexpr int kPWarps = kPThreads / 32;
 
 struct TeamShared
@@ -580,8 +578,8 @@ __device__ void load_body(DevBody* dst, const DevBody* src)
 	for (int k = threadIdx.x; k < words; k += blockDim.x) d[k] = __ldcg(s + k);
 }
 
-#ifndef B3G_SOLVE_MIN_BLOCKS
-#define B3G_SOLVE_MIN_BLOCKS 4   // resident CTAs per SM of the PCG launch (64 registers a thread)
+#ifndef B3G_SOLVE_MIN_BLOCKS  // resident CTAs per SM of the PCG launch (64 registers a thread)
+#define B3G_SOLVE_MIN_BLOCKS (B3G_PCG_THREADS >= 512 ? 2 : 4)
 #endif
 
 // Launch phases: the whole step (any number of Newton iterations), or the two parts of a

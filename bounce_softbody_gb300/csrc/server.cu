@@ -219,7 +219,8 @@ b3g_body_desc make_desc(const HostDesc& h)
 // created its exact size is used instead.
 uint64_t estimate_bytes(const HostDesc& h) { return estimate_desc_bytes(make_desc(h)); }
 
-constexpr int kServerCluster = 8;  // default team size of large bodies (B3G_SERVER_CLUSTER overrides)
+// default team size of large bodies, 64 warps (B3G_SERVER_CLUSTER overrides)
+constexpr int kServerCluster = 2048 / B3G_PCG_THREADS;
 constexpr uint32_t kServerThreshold = 4096;
 
 struct Request
