@@ -1,6 +1,7 @@
 """bench.py's host side: the CPU reference arm prints one valid JSON line, alone and as rank 0 of
 a two-rank gloo job (the other rank exits without work); the rank reductions; the split of one
-body list over ranks by device footprint and the per-rank stats gather on two gloo ranks."""
+body list over ranks by device footprint and the per-rank stats gather on two gloo ranks; the
+algorithmic byte counts of the rooflines."""
 import json
 import os
 import subprocess
@@ -123,3 +124,24 @@ def test_partition_rule():
     assert len(b3g.partition([], 4)) == 0
     with pytest.raises(b3g.B3gError):
         b3g.partition([1, 2], 0)
+
+
+def test_algorithmic_byte_counts_follow_their_units():
+    """The roofline's algorithmic bytes, per unit, as the design notes state them: SpMV
+    40·nnzb + n + 24·n; a PCG iteration that plus 36·n (direction and product in the SpMV sweep)
+    and 96·n (update); the final update 112·n; the assembly 212·T + 48·n (elements and state
+    gathers) + 40·nnzb + 112·T + 105·n (rows). The counts come from a Kuhn block's mesh."""
+    import numpy as np
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from bounce_softbody_gb300 import meshes
+    d = meshes.tet_grid(5, 4, 6, pin="y0")
+    n, nt = d.x.shape[0], d.tets.shape[0]
+    pairs = {(int(t[a]), int(t[b])) for t in d.tets for a in range(4) for b in range(4) if a != b}
+    nnzb = n + len(pairs)
+    info = {"vertices": n, "tets": nt, "nnzb": nnzb}
+    assert bench.spmv_bytes(info) == 40 * nnzb + n + 24 * n
+    assert bench.iteration_bytes(info) == 40 * nnzb + n + 24 * n + 36 * n + 96 * n
+    assert bench.final_bytes(info) == 112 * n
+    assert bench.assembly_bytes(info) == 212 * nt + 48 * n + 40 * nnzb + 112 * nt + 105 * n
+    assert np.isclose(nt, 6 * 4 * 3 * 5)
