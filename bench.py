@@ -38,7 +38,7 @@ PCG_TOL = 1e-5
 PCG_MAX = 200
 # DRAM traffic / algorithmic bytes of the batch PCG launch, from the ncu capture of the
 # 128-body case (profiles/k_batch_batch512.md)
-PCG_TRAFFIC_RATIO = 1.093
+PCG_TRAFFIC_RATIO = 1.072
 # steps of the CPU-baseline run and of the parity check, from the bodies' initial state
 PARITY_STEPS = 3
 
@@ -429,9 +429,9 @@ def ours(args, world, rank, local, pg):
         ach = pcg_b / (pcg_ms / 1e3) / 1e9
         roof.update({"achieved": ach, "frac": ach / peak, "kernel": "k_batch PCG launch (PCG + final update)",
                      "algorithmic_bytes_per_launch": pcg_b, "launch_ms": pcg_ms, "launches_timed": lt["steps"]})
-        # DRAM traffic of the PCG launch: ncu on the 128-body case measured 40.32 GB for
-        # 36.89 GB of algorithmic bytes (PCG_TRAFFIC_RATIO); traffic grows with the work, so the ratio
-        # scales it to this launch
+        # DRAM traffic of the PCG launch: ncu on the 128-body case measured 39.55 GB for
+        # 36.90 GB of algorithmic bytes with 256-thread CTAs (PCG_TRAFFIC_RATIO; 1.093 with
+        # 512-thread CTAs); traffic grows with the work, so the ratio scales it to this launch
         if args.precision == "fp32":
             roof["traffic"] = PCG_TRAFFIC_RATIO * pcg_b
         roof["assembly_launch"] = {"achieved": asm_b / (asm_ms / 1e3) / 1e9, "frac": asm_b / (asm_ms / 1e3) / 1e9 / peak,

@@ -7,11 +7,11 @@
 #include <cuda_runtime.h>
 
 // Threads per CTA of the batch kernel's team launches (the PCG launch and the team assembly).
-// 512-thread CTAs at 2 per SM (64 registers a thread) measured 1 % faster on the 512-body batch
-// than 256-thread CTAs at 4 per SM: the same 32 warps per SM, half the CTAs (and clusters) for
-// a team of the same size.
+// On the 512-body batch with every body on a cluster, 256-thread CTAs at 4 per SM (clusters of
+// 8) measured 1 % faster than 512-thread CTAs at 2 per SM (clusters of 4); with small bodies on
+// single CTAs it was the other way round.
 #ifndef B3G_PCG_THREADS
-#define B3G_PCG_THREADS 512
+#define B3G_PCG_THREADS 256
 #endif
 
 namespace b3g {

@@ -264,7 +264,7 @@ B3G_API int b3g_step_batch(b3g_context* ctx, b3g_body* const* bodies, uint32_t c
  * fails with B3G_ERROR_UNSUPPORTED). Differences from b3g_step_batch: each body must already have
  * solver buffers for the requested precision (FP32 always does; FP64 / BF16 after a first step in
  * that precision), where b3g_step_batch creates them; dt must be > 0 (b3g_step_batch steps each
- * body alone for dt <= 0); the schedule is a fixed size rule (clusters of 4 CTAs of 512 threads
+ * body alone for dt <= 0); the schedule is a fixed size rule (clusters of 4 CTAs of 256 threads
  * for bodies of 4096 vertices or more, single CTAs below), not autotuned. The first call on a device looks the
  * array up and clears it (set-up): make that first call before any stream capture. Each call
  * copies the body descriptors to the device from static host arrays of the library, which the
